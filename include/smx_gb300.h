@@ -1,0 +1,95 @@
+/* smx_gb300.h — C ABI of the GB300-native MACE energy/force engine.
+ *
+ * Drop-in for libsymmetrix's evaluator path.  Each entry point names the
+ * reference interface it replaces (paths are within the symmetrix repository):
+ *
+ *   smx_create / smx_destroy        MACE::MACE(std::string filename)
+ *                                   (libsymmetrix/source/mace.hpp:16, mace.cpp:12-15)
+ *   smx_compute_node_energies_forces
+ *                                   MACE::compute_node_energies_forces
+ *                                   (libsymmetrix/source/mace.hpp:29-35, mace.cpp:17-64);
+ *                                   the results the reference leaves in the members
+ *                                   node_energies / node_forces are written to caller
+ *                                   buffers instead
+ *   smx_compute_node_energies_forces_device
+ *                                   the same call on device-resident arrays, as the Kokkos
+ *                                   pair style passes them (pair_symmetrix/
+ *                                   pair_symmetrix_mace_kokkos.cpp:390-394)
+ *   smx_num_elements, smx_num_channels, smx_r_cut, smx_l_max, smx_L_max, smx_num_LM,
+ *   smx_atomic_numbers              public fields of class MACE (mace.hpp:18-25)
+ *   smx_get_stage                   the read-only stage buffers the Python binding exposes
+ *                                   (symmetrix/source/cpp/mace.cpp:14-34)
+ *
+ * Conventions (identical to the reference):
+ *   - edges are a full directed list grouped by centre node: node i owns edges
+ *     [sum(num_neigh[:i]), sum(num_neigh[:i+1])); neigh_indices[e] = j;
+ *   - xyz[3e..3e+2] = x_j - x_i (periodic image included), r[e] = |xyz[e]|, 0 < r < r_cut;
+ *   - node_types / neigh_types index the model's atomic_numbers list;
+ *   - node_forces[3e..3e+2] = -dE/dxyz[e] (a per-edge "partial force"); atomic forces
+ *     are F_j += f_e, F_i -= f_e and the virial is sum_e xyz[e] (x) f_e.
+ *
+ * Errors are status codes (the reference throws C++ exceptions); smx_last_error()
+ * returns the message of the last failing call on the calling thread.
+ * An engine is not thread-safe (like the reference's MACE object): one caller at a time.
+ */
+#ifndef SMX_GB300_H
+#define SMX_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SMX_OK 0
+#define SMX_ERR_INVALID 1   /* bad argument or input outside the model's domain */
+#define SMX_ERR_MODEL 2     /* model file missing, malformed or unsupported */
+#define SMX_ERR_CUDA 3      /* CUDA runtime error (message has the CUDA error string) */
+#define SMX_ERR_CAPACITY 4  /* a fixed-capacity buffer is too small for the request */
+#define SMX_ERR_TIMEOUT 5   /* a bounded device-side wait gave up */
+
+#define SMX_PRECISION_FP32 0 /* plain form: float32 throughout, float64 outputs */
+
+typedef struct smx_engine smx_engine;
+
+/* Load a libsymmetrix JSON model onto CUDA device `device`.  NULL on failure. */
+smx_engine* smx_create(const char* model_path, int precision, int device);
+void smx_destroy(smx_engine* eng);
+const char* smx_last_error(void);
+
+int smx_num_elements(const smx_engine* eng);
+int smx_num_channels(const smx_engine* eng);
+double smx_r_cut(const smx_engine* eng);
+int smx_l_max(const smx_engine* eng);
+int smx_L_max(const smx_engine* eng);
+int smx_num_LM(const smx_engine* eng);
+/* Copies up to cap atomic numbers; returns the number of species. */
+int smx_atomic_numbers(const smx_engine* eng, int* out, int cap);
+
+/* Host arrays in, host arrays out (node_energies[num_nodes], node_forces[3*num_edges]).
+ * Inputs are validated (index ranges, 0 < r < r_cut, sum(num_neigh) == num_edges). */
+int smx_compute_node_energies_forces(smx_engine* eng, int num_nodes, const int* node_types, const int* num_neigh,
+                                     const int* neigh_indices, const int* neigh_types, long num_edges,
+                                     const double* xyz, const double* r, double* node_energies,
+                                     double* node_forces);
+
+/* Same, with every pointer in device memory of the engine's device; runs on
+ * `stream` (a cudaStream_t, or NULL for the engine's own stream) and returns
+ * without synchronising.  Inputs are not validated; edges with r >= r_cut
+ * contribute nothing. */
+int smx_compute_node_energies_forces_device(smx_engine* eng, int num_nodes, const int* node_types,
+                                            const int* num_neigh, const int* neigh_indices, const int* neigh_types,
+                                            long num_edges, const double* xyz, const double* r,
+                                            double* node_energies, double* node_forces, void* stream);
+
+/* Copies the last call's stage buffer `name` (A0, M0, H1, Phi1, A1, M1, H2, A0_adj,
+ * M0_adj, H1_adj, Phi1_adj, A1_adj, M1_adj, H2_adj; reference layouts, see
+ * libsymmetrix/source/mace.hpp) as float64.  Returns its length, -1 for an unknown
+ * name.  A0_adj is kept only after smx_set_option(eng, "keep_stages", 1). */
+long smx_get_stage(smx_engine* eng, const char* name, double* out, long cap);
+
+int smx_set_option(smx_engine* eng, const char* key, long value);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SMX_GB300_H */

@@ -1,0 +1,182 @@
+// Device-side model view and helpers shared by the GB300 kernels.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include <type_traits>
+#include <utility>
+
+namespace smx {
+
+constexpr int kEdgeChunk = 32;  // edges staged in shared memory per block iteration
+
+// Device view of a packed model (see model.hpp for layouts).  Passed by value.
+struct DevModel {
+  int S, C, L_max, nLM, n_lme, n_instr, n_p, nint, T0, T1, n_hidden;
+  float h, inv_h, r_cut, ro2_scale;
+  const float4* spl0;  // [S*S][nint][4][C]
+  const float4* spl1;  // [npairs][nint][n_instr][C]
+  const int* mono0;
+  int mono0_off[10];
+  const float* coef0;  // [S][nLM][T0][C]
+  const int* mono1;
+  const float* coef1;  // [S][T1][C]
+  const float* H1W;
+  const float* H1W_T;
+  const int* cg_fwd_off;
+  const int* cg_fwd_p;
+  const float* cg_fwd_v;
+  const int* cg_rev_off;
+  const int* cg_rev_lme;
+  const float* cg_rev_v;
+  int lme_off[4], num_e[4];
+  const float* A1W[4];
+  const float* A1W_T[4];
+  const float* H2W_H1;
+  const float* H2W_H1_T;
+  const float* H2W_M1;
+  const float* H2W_M1_T;
+  const float* ro1;
+  const float* ro2_w1;
+  const float* ro2_w2;
+  const float* e0;
+};
+
+// Edge list in the evaluator's layout (libsymmetrix/source/mace.hpp:29-35): CSR by
+// centre node, xyz = x_j - x_i, r = |xyz|.  Edges with r >= r_cut are skipped
+// (they contribute nothing), which lets an MD driver keep a skin list.
+struct EdgeIn {
+  const int* first;      // [N+1]
+  const int* node_type;  // [N]
+  const int* nidx;       // [E]
+  const int* ntype_e;    // [E]
+  const double* xyz;     // [E][3]
+  const double* r;       // [E]
+  int N;
+};
+
+// Canonical layer-1 tensor-product instructions (l1 from Y_lm, l2 from H1),
+// ordered by output l; the loader reorders model data to this order.
+__host__ __device__ constexpr int ins_count(int LMAX) { return LMAX == 1 ? 10 : 17; }
+__host__ __device__ constexpr int ins_l1(int LMAX, int q) {
+  constexpr int a1[10] = {0, 1, 1, 0, 2, 2, 1, 3, 3, 2};
+  constexpr int a2[17] = {0, 1, 2, 1, 0, 2, 1, 3, 2, 1, 3, 0, 2, 3, 2, 1, 3};
+  return LMAX == 1 ? a1[q] : a2[q];
+}
+__host__ __device__ constexpr int ins_l2(int LMAX, int q) {
+  constexpr int b1[10] = {0, 1, 0, 1, 1, 0, 1, 1, 0, 1};
+  constexpr int b2[17] = {0, 1, 2, 0, 1, 1, 2, 2, 0, 1, 1, 2, 2, 0, 1, 2, 2};
+  return LMAX == 1 ? b1[q] : b2[q];
+}
+// offset of instruction q's (m1, m2) block in the Phi1r row p = (q, m1, m2)
+__host__ __device__ constexpr int ins_poff(int LMAX, int q) {
+  int p = 0;
+  for (int w = 0; w < q; ++w) p += (2 * ins_l1(LMAX, w) + 1) * (2 * ins_l2(LMAX, w) + 1);
+  return p;
+}
+__host__ __device__ constexpr int ins_np(int LMAX) { return ins_poff(LMAX, ins_count(LMAX)); }
+
+// Calls f(std::integral_constant<int, q>) for every instruction q, so that the
+// loop body sees l1, l2 and the Phi1r offset as compile-time constants.
+template <typename F, int... Q>
+__device__ __forceinline__ void for_each_ins_impl(F&& f, std::integer_sequence<int, Q...>) {
+  (f(std::integral_constant<int, Q>{}), ...);
+}
+template <int LMAX, typename F>
+__device__ __forceinline__ void for_each_ins(F&& f) {
+  for_each_ins_impl(f, std::make_integer_sequence<int, ins_count(LMAX)>{});
+}
+
+__device__ __forceinline__ float spline_val(const float4 c, float x) {
+  return fmaf(x, fmaf(x, fmaf(x, c.w, c.z), c.y), c.x);
+}
+__device__ __forceinline__ float spline_der(const float4 c, float x) {
+  return fmaf(x, fmaf(3.0f * x, c.w, 2.0f * c.z), c.y);
+}
+
+// Real spherical harmonics l <= 3 of the edge vector v in the evaluator's
+// convention: shuffle (x,y,z) -> (z,x,y), orthonormal real Y_lm without the
+// Condon-Shortley phase, times 2 sqrt(pi) (libsymmetrix/source/mace.cpp:118-148).
+// Each Y_lm = s P_lm(u) with P_lm homogeneous of degree l and u the unit vector;
+// the gradient with respect to v is s (grad P_lm(u) - l P_lm(u) u) / |v|.
+template <bool GRAD>
+__device__ __forceinline__ void sph_harm16(float vx, float vy, float vz, float* Y, float* G /*[3][16]*/) {
+  const float r2 = vx * vx + vy * vy + vz * vz;
+  const float inv_r = rsqrtf(r2);
+  const float X = vz * inv_r, Yv = vx * inv_r, Z = vy * inv_r;  // shuffled unit vector
+  // 2 sqrt(pi) times the orthonormal normalisation constants
+  const float s0 = 1.0f;
+  const float s1 = 1.7320508075688772f;                      // sqrt(3)
+  const float s2a = 3.872983346207417f;                      // sqrt(15)
+  const float s2b = 1.118033988749895f;                      // sqrt(5)/2
+  const float s2c = 1.9364916731037085f;                     // sqrt(15)/2
+  const float s3a = 2.091650066335189f;                      // sqrt(35/8)
+  const float s3b = 10.246950765959598f;                     // sqrt(105)
+  const float s3c = 1.620185174601965f;                      // sqrt(21/8)
+  const float s3d = 1.3228756555322954f;                     // sqrt(7)/2
+  const float s3e = 5.123475382979799f;                      // sqrt(105)/2
+  const float XX = X * X, YY = Yv * Yv, ZZ = Z * Z;
+  Y[0] = s0;
+  Y[1] = s1 * Yv;
+  Y[2] = s1 * Z;
+  Y[3] = s1 * X;
+  Y[4] = s2a * X * Yv;
+  Y[5] = s2a * Yv * Z;
+  Y[6] = s2b * (2.0f * ZZ - XX - YY);
+  Y[7] = s2a * X * Z;
+  Y[8] = s2c * (XX - YY);
+  Y[9] = s3a * Yv * (3.0f * XX - YY);
+  Y[10] = s3b * X * Yv * Z;
+  Y[11] = s3c * Yv * (4.0f * ZZ - XX - YY);
+  Y[12] = s3d * Z * (2.0f * ZZ - 3.0f * XX - 3.0f * YY);
+  Y[13] = s3c * X * (4.0f * ZZ - XX - YY);
+  Y[14] = s3e * Z * (XX - YY);
+  Y[15] = s3a * X * (XX - 3.0f * YY);
+  if constexpr (GRAD) {
+    // dP/d(X, Y, Z) in shuffled axes
+    float D[3][16];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int q = 0; q < 16; ++q) D[a][q] = 0.0f;
+    D[1][1] = s1;
+    D[2][2] = s1;
+    D[0][3] = s1;
+    D[0][4] = s2a * Yv; D[1][4] = s2a * X;
+    D[1][5] = s2a * Z;  D[2][5] = s2a * Yv;
+    D[0][6] = -2.0f * s2b * X; D[1][6] = -2.0f * s2b * Yv; D[2][6] = 4.0f * s2b * Z;
+    D[0][7] = s2a * Z; D[2][7] = s2a * X;
+    D[0][8] = 2.0f * s2c * X; D[1][8] = -2.0f * s2c * Yv;
+    D[0][9] = 6.0f * s3a * X * Yv; D[1][9] = 3.0f * s3a * (XX - YY);
+    D[0][10] = s3b * Yv * Z; D[1][10] = s3b * X * Z; D[2][10] = s3b * X * Yv;
+    D[0][11] = -2.0f * s3c * X * Yv; D[1][11] = s3c * (4.0f * ZZ - XX - 3.0f * YY); D[2][11] = 8.0f * s3c * Yv * Z;
+    D[0][12] = -6.0f * s3d * X * Z; D[1][12] = -6.0f * s3d * Yv * Z; D[2][12] = s3d * (6.0f * ZZ - 3.0f * XX - 3.0f * YY);
+    D[0][13] = s3c * (4.0f * ZZ - 3.0f * XX - YY); D[1][13] = -2.0f * s3c * X * Yv; D[2][13] = 8.0f * s3c * X * Z;
+    D[0][14] = 2.0f * s3e * X * Z; D[1][14] = -2.0f * s3e * Yv * Z; D[2][14] = s3e * (XX - YY);
+    D[0][15] = 3.0f * s3a * (XX - YY); D[1][15] = -6.0f * s3a * X * Yv;
+    const float u[3] = {X, Yv, Z};
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      const float l = q == 0 ? 0.0f : (q < 4 ? 1.0f : (q < 9 ? 2.0f : 3.0f));
+      const float lp = l * Y[q];
+      const float gX = (D[0][q] - lp * u[0]) * inv_r;
+      const float gY = (D[1][q] - lp * u[1]) * inv_r;
+      const float gZ = (D[2][q] - lp * u[2]) * inv_r;
+      // back to (x, y, z): d/dx = d/dY', d/dy = d/dZ', d/dz = d/dX'
+      G[0 * 16 + q] = gY;
+      G[1 * 16 + q] = gZ;
+      G[2 * 16 + q] = gX;
+    }
+  }
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+inline int ceil_div(long a, long b) { return static_cast<int>((a + b - 1) / b); }
+
+}  // namespace smx

@@ -1,0 +1,429 @@
+// Edge kernels: the neighbour sums of both interaction layers and their adjoints.
+//
+// One thread block per centre node i, one thread per channel k (blockDim = C).
+// Edges of node i are staged kernel-wide in chunks of kEdgeChunk: geometry,
+// spline interval, Y_lm (and dY/dx in the adjoints) are computed once per edge by
+// one thread and shared; every thread then runs the per-channel arithmetic for
+// its k with channel-fastest, coalesced loads of spline coefficients (float4:
+// one cubic per (spline, channel)) and neighbour features.  Sums over neighbours
+// accumulate in registers of the destination node's block, so the forward
+// A-basis and Phi1 sums use no atomics.
+//
+// Reference stages restated here (libsymmetrix/source/mace.cpp):
+//   k_layer0_fwd : compute_Y + compute_R0 + compute_A0 (:66-201) + compute_M0 (:348-370)
+//   k_layer1_fwd : compute_R1 + compute_Phi1 (:92-116, :453-502)
+//   k_layer1_rev : reverse_Phi1 (:504-605)
+//   k_layer0_rev : reverse_M0 + reverse_A0 (:372-395, :203-271)
+#include <cuda_runtime.h>
+
+#include "device.cuh"
+#include "kernels.h"
+
+namespace smx {
+
+namespace {
+
+// Stage the geometry of edges [eb, eb+ne) of centre node i into shared memory.
+// base[t] = spline row (pair * nint + interval) * stride, or -1 if r >= r_cut.
+template <bool GRAD>
+__device__ __forceinline__ void stage_edges(const DevModel& m, const EdgeIn& in, int ti, int eb, int ne,
+                                            bool ordered_pair, int stride, float (*sY)[kEdgeChunk],
+                                            float (*sG)[kEdgeChunk], float (*su)[kEdgeChunk], float* sx,
+                                            int* sbase, int* sj) {
+  for (int t = threadIdx.x; t < ne; t += blockDim.x) {
+    const long e = static_cast<long>(eb) + t;
+    const float vx = static_cast<float>(in.xyz[3 * e]);
+    const float vy = static_cast<float>(in.xyz[3 * e + 1]);
+    const float vz = static_cast<float>(in.xyz[3 * e + 2]);
+    const float rr = static_cast<float>(in.r[e]);
+    float Y[16], G[48];
+    sph_harm16<GRAD>(vx, vy, vz, Y, G);
+#pragma unroll
+    for (int q = 0; q < 16; ++q) sY[q][t] = Y[q];
+    if constexpr (GRAD) {
+#pragma unroll
+      for (int q = 0; q < 48; ++q) sG[q][t] = G[q];
+      const float inv = 1.0f / rr;
+      su[0][t] = vx * inv;
+      su[1][t] = vy * inv;
+      su[2][t] = vz * inv;
+    }
+    int iv = static_cast<int>(rr * m.inv_h);
+    iv = iv < 0 ? 0 : (iv >= m.nint ? m.nint - 1 : iv);
+    sx[t] = rr - static_cast<float>(iv) * m.h;
+    const int tj = in.ntype_e[e];
+    int pr;
+    if (ordered_pair) {
+      pr = ti * m.S + tj;
+    } else {
+      const int a = ti < tj ? ti : tj, b = ti < tj ? tj : ti;
+      pr = a * (2 * m.S - a - 1) / 2 + b;
+    }
+    sbase[t] = (rr < m.r_cut) ? (pr * m.nint + iv) * stride : -1;
+    if (sj) sj[t] = in.nidx[e];
+  }
+}
+
+// Sum a per-thread 3-vector over the block's channels for edge t: warp shuffles,
+// then one partial per warp into sF (reduced after the chunk).
+__device__ __forceinline__ void block_reduce3(float fx, float fy, float fz, float (*sF)[8][3], int t) {
+  fx = warp_sum(fx);
+  fy = warp_sum(fy);
+  fz = warp_sum(fz);
+  if ((threadIdx.x & 31) == 0) {
+    const int w = threadIdx.x >> 5;
+    sF[t][w][0] = fx;
+    sF[t][w][1] = fy;
+    sF[t][w][2] = fz;
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Layer 0 forward: A0[i,lm,k] = sum_j Y_lm(x_ij) R0'_{ti,tj,l}(r_ij)[k] with the
+// folded ordered-pair splines, then M0[i,LM,k] = P_{ti,LM,k}(A0[i,:,k]).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_layer0_fwd(DevModel m, EdgeIn in, float* __restrict__ A0,
+                                                    float* __restrict__ M0) {
+  extern __shared__ float dyn[];
+  __shared__ float sY[16][kEdgeChunk];
+  __shared__ float sx[kEdgeChunk];
+  __shared__ int sbase[kEdgeChunk];
+  const int C = m.C, k = threadIdx.x, i = blockIdx.x;
+  const int ti = in.node_type[i];
+  const int e0 = in.first[i], e1 = in.first[i + 1];
+  float acc[16];
+#pragma unroll
+  for (int q = 0; q < 16; ++q) acc[q] = 0.0f;
+  for (int eb = e0; eb < e1; eb += kEdgeChunk) {
+    const int ne = min(kEdgeChunk, e1 - eb);
+    __syncthreads();
+    stage_edges<false>(m, in, ti, eb, ne, true, 4, sY, nullptr, nullptr, sx, sbase, nullptr);
+    __syncthreads();
+    for (int t = 0; t < ne; ++t) {
+      const int base = sbase[t];
+      if (base < 0) continue;
+      const float4* c = m.spl0 + static_cast<size_t>(base) * C + k;
+      const float x = sx[t];
+#pragma unroll
+      for (int l = 0; l < 4; ++l) {
+        const float R = spline_val(__ldg(c + l * C), x);
+#pragma unroll
+        for (int q = l * l; q < (l + 1) * (l + 1); ++q) acc[q] = fmaf(R, sY[q][t], acc[q]);
+      }
+    }
+  }
+  float* sA = dyn;  // [17][C]: this thread's A0 column (+ constant one) for the contraction
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    A0[(static_cast<size_t>(i) * 16 + q) * C + k] = acc[q];
+    sA[q * C + k] = acc[q];
+  }
+  sA[16 * C + k] = 1.0f;
+  for (int LM = 0; LM < m.nLM; ++LM) {
+    const int t0 = m.mono0_off[LM], t1 = m.mono0_off[LM + 1];
+    const float* cf = m.coef0 + (static_cast<size_t>(ti * m.nLM + LM) * m.T0) * C + k;
+    float f = 0.0f;
+    for (int t = t0; t < t1; ++t) {
+      const int pk = __ldg(m.mono0 + t);
+      const float xa = sA[(pk & 255) * C + k], xb = sA[((pk >> 8) & 255) * C + k], xc = sA[(pk >> 16) * C + k];
+      f = fmaf(__ldg(cf + static_cast<size_t>(t - t0) * C), xa * xb * xc, f);
+    }
+    M0[(static_cast<size_t>(i) * m.nLM + LM) * C + k] = f;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Layer 1 forward: Phi1r[i,p,k] = sum_j R1_q(r_ij)[k] Y_{l1 m1}(x_ij) H1[j, l2 m2, k]
+// accumulated in registers (p = (instruction, m1, m2), canonical order), then
+// Phi1[i,lme,k] = sum_p CG[lme,p] Phi1r[i,p,k].
+// ---------------------------------------------------------------------------
+template <int LMAX>
+__global__ void __launch_bounds__(256) k_layer1_fwd(DevModel m, EdgeIn in, const float* __restrict__ H1,
+                                                    float* __restrict__ Phi1) {
+  constexpr int NL2 = (LMAX + 1) * (LMAX + 1);
+  constexpr int NI = ins_count(LMAX);
+  constexpr int NP = ins_np(LMAX);
+  extern __shared__ float dyn[];
+  __shared__ float sY[16][kEdgeChunk];
+  __shared__ float sx[kEdgeChunk];
+  __shared__ int sbase[kEdgeChunk];
+  __shared__ int sj[kEdgeChunk];
+  const int C = m.C, k = threadIdx.x, i = blockIdx.x;
+  const int ti = in.node_type[i];
+  const int e0 = in.first[i], e1 = in.first[i + 1];
+  float acc[NP];
+#pragma unroll
+  for (int p = 0; p < NP; ++p) acc[p] = 0.0f;
+  for (int eb = e0; eb < e1; eb += kEdgeChunk) {
+    const int ne = min(kEdgeChunk, e1 - eb);
+    __syncthreads();
+    stage_edges<false>(m, in, ti, eb, ne, false, NI, sY, nullptr, nullptr, sx, sbase, sj);
+    __syncthreads();
+    for (int t = 0; t < ne; ++t) {
+      const int base = sbase[t];
+      if (base < 0) continue;
+      const float* hj = H1 + static_cast<size_t>(sj[t]) * NL2 * C + k;
+      float hv[NL2];
+#pragma unroll
+      for (int q = 0; q < NL2; ++q) hv[q] = __ldg(hj + q * C);
+      const float4* cp = m.spl1 + static_cast<size_t>(base) * C + k;
+      const float x = sx[t];
+      for_each_ins<LMAX>([&](auto qc) {
+        constexpr int q = decltype(qc)::value;
+        constexpr int l1 = ins_l1(LMAX, q), l2 = ins_l2(LMAX, q), p0 = ins_poff(LMAX, q);
+        const float R = spline_val(__ldg(cp + q * C), x);
+#pragma unroll
+        for (int a = 0; a < 2 * l1 + 1; ++a) {
+          const float ry = R * sY[l1 * l1 + a][t];
+#pragma unroll
+          for (int b = 0; b < 2 * l2 + 1; ++b)
+            acc[p0 + a * (2 * l2 + 1) + b] = fmaf(ry, hv[l2 * l2 + b], acc[p0 + a * (2 * l2 + 1) + b]);
+        }
+      });
+    }
+  }
+  float* sP = dyn;  // [NP][C]: this thread's Phi1r column
+#pragma unroll
+  for (int p = 0; p < NP; ++p) sP[p * C + k] = acc[p];
+  for (int lme = 0; lme < m.n_lme; ++lme) {
+    float s = 0.0f;
+    const int g1 = __ldg(m.cg_fwd_off + lme + 1);
+    for (int g = __ldg(m.cg_fwd_off + lme); g < g1; ++g) s = fmaf(__ldg(m.cg_fwd_v + g), sP[__ldg(m.cg_fwd_p + g) * C + k], s);
+    Phi1[(static_cast<size_t>(i) * m.n_lme + lme) * C + k] = s;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Layer 1 adjoint.  g[p] = sum_lme CG[lme,p] dPhi1[i,lme,k]; per edge:
+//   dE/dx_ij += sum_k sum_p g_p h_{m2} (R1'_q(r) u Y_{m1} + R1_q(r) dY_{m1}/dx)
+//   H1_adj[j, l2 m2, k] += sum_p R1_q(r) Y_{m1} g_p        (atomic scatter)
+// f1[e] receives dE/dx_ij from this layer.
+// ---------------------------------------------------------------------------
+template <int LMAX>
+__global__ void __launch_bounds__(256) k_layer1_rev(DevModel m, EdgeIn in, const float* __restrict__ H1,
+                                                    const float* __restrict__ dPhi1, float* __restrict__ H1_adj,
+                                                    float* __restrict__ f1) {
+  constexpr int NL2 = (LMAX + 1) * (LMAX + 1);
+  constexpr int NI = ins_count(LMAX);
+  constexpr int NP = ins_np(LMAX);
+  extern __shared__ float dyn[];
+  __shared__ float sY[16][kEdgeChunk];
+  __shared__ float sG[48][kEdgeChunk];
+  __shared__ float su[3][kEdgeChunk];
+  __shared__ float sx[kEdgeChunk];
+  __shared__ int sbase[kEdgeChunk];
+  __shared__ int sj[kEdgeChunk];
+  __shared__ float sF[kEdgeChunk][8][3];
+  const int C = m.C, k = threadIdx.x, i = blockIdx.x;
+  const int nwarp = C >> 5;
+  const int ti = in.node_type[i];
+  const int e0 = in.first[i], e1 = in.first[i + 1];
+  // g[p] = sum_lme CG[lme,p] dPhi1[i,lme,k], formed in this thread's shared-memory
+  // column (data-driven indices) and then moved to registers with constant indices
+  float* sD = dyn;                 // [n_lme][C]
+  float* sP = dyn + m.n_lme * C;   // [NP][C]
+  for (int lme = 0; lme < m.n_lme; ++lme) sD[lme * C + k] = dPhi1[(static_cast<size_t>(i) * m.n_lme + lme) * C + k];
+  for (int p = 0; p < NP; ++p) {
+    float s = 0.0f;
+    const int q1 = __ldg(m.cg_rev_off + p + 1);
+    for (int q = __ldg(m.cg_rev_off + p); q < q1; ++q) s = fmaf(__ldg(m.cg_rev_v + q), sD[__ldg(m.cg_rev_lme + q) * C + k], s);
+    sP[p * C + k] = s;
+  }
+  float g[NP];
+#pragma unroll
+  for (int p = 0; p < NP; ++p) g[p] = sP[p * C + k];
+  for (int eb = e0; eb < e1; eb += kEdgeChunk) {
+    const int ne = min(kEdgeChunk, e1 - eb);
+    __syncthreads();
+    stage_edges<true>(m, in, ti, eb, ne, false, NI, sY, sG, su, sx, sbase, sj);
+    __syncthreads();
+    for (int t = 0; t < ne; ++t) {
+      const int base = sbase[t];
+      if (base < 0) {
+        if ((threadIdx.x & 31) == 0) sF[t][threadIdx.x >> 5][0] = sF[t][threadIdx.x >> 5][1] = sF[t][threadIdx.x >> 5][2] = 0.0f;
+        continue;
+      }
+      const int j = sj[t];
+      const float* hj = H1 + static_cast<size_t>(j) * NL2 * C + k;
+      float hv[NL2], hadj[NL2];
+#pragma unroll
+      for (int q = 0; q < NL2; ++q) {
+        hv[q] = __ldg(hj + q * C);
+        hadj[q] = 0.0f;
+      }
+      float dY[16];
+#pragma unroll
+      for (int q = 0; q < 16; ++q) dY[q] = 0.0f;
+      const float4* cp = m.spl1 + static_cast<size_t>(base) * C + k;
+      const float x = sx[t];
+      float dr = 0.0f;
+      for_each_ins<LMAX>([&](auto qc) {
+        constexpr int q = decltype(qc)::value;
+        constexpr int l1 = ins_l1(LMAX, q), l2 = ins_l2(LMAX, q), p0 = ins_poff(LMAX, q);
+        const float4 cc = __ldg(cp + q * C);
+        const float R = spline_val(cc, x), Rd = spline_der(cc, x);
+        float dRq = 0.0f;
+#pragma unroll
+        for (int a = 0; a < 2 * l1 + 1; ++a) {
+          const float y = sY[l1 * l1 + a][t];
+          float gs = 0.0f;
+#pragma unroll
+          for (int b = 0; b < 2 * l2 + 1; ++b) gs = fmaf(g[p0 + a * (2 * l2 + 1) + b], hv[l2 * l2 + b], gs);
+          dRq = fmaf(gs, y, dRq);
+          dY[l1 * l1 + a] = fmaf(R, gs, dY[l1 * l1 + a]);
+          const float ry = R * y;
+#pragma unroll
+          for (int b = 0; b < 2 * l2 + 1; ++b)
+            hadj[l2 * l2 + b] = fmaf(ry, g[p0 + a * (2 * l2 + 1) + b], hadj[l2 * l2 + b]);
+        }
+        dr = fmaf(dRq, Rd, dr);
+      });
+      float fx = dr * su[0][t], fy = dr * su[1][t], fz = dr * su[2][t];
+#pragma unroll
+      for (int q = 0; q < 16; ++q) {
+        fx = fmaf(dY[q], sG[q][t], fx);
+        fy = fmaf(dY[q], sG[16 + q][t], fy);
+        fz = fmaf(dY[q], sG[32 + q][t], fz);
+      }
+      block_reduce3(fx, fy, fz, sF, t);
+      float* aj = H1_adj + static_cast<size_t>(j) * NL2 * C + k;
+#pragma unroll
+      for (int q = 0; q < NL2; ++q) atomicAdd(aj + q * C, hadj[q]);
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < ne; t += blockDim.x) {
+      float s[3] = {0.0f, 0.0f, 0.0f};
+      for (int w = 0; w < nwarp; ++w)
+        for (int a = 0; a < 3; ++a) s[a] += sF[t][w][a];
+      for (int a = 0; a < 3; ++a) f1[3 * (static_cast<long>(eb) + t) + a] = s[a];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Layer 0 adjoint: dA0[i,:,k] = sum_LM dM0[i,LM,k] grad P_{ti,LM,k}(A0[i,:,k]), then
+//   dE/dx_ij = sum_k sum_lm dA0[lm] (R0'_l'(r) u Y_lm + R0'_l(r) dY_lm/dx)
+// and node_forces[e] = -(layer-0 + layer-1 contributions), in float64.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_layer0_rev(DevModel m, EdgeIn in, const float* __restrict__ A0,
+                                                    const float* __restrict__ M0_adj, const float* __restrict__ f1,
+                                                    float* __restrict__ A0_adj, double* __restrict__ forces) {
+  extern __shared__ float dyn[];
+  __shared__ float sY[16][kEdgeChunk];
+  __shared__ float sG[48][kEdgeChunk];
+  __shared__ float su[3][kEdgeChunk];
+  __shared__ float sx[kEdgeChunk];
+  __shared__ int sbase[kEdgeChunk];
+  __shared__ float sF[kEdgeChunk][8][3];
+  const int C = m.C, k = threadIdx.x, i = blockIdx.x;
+  const int nwarp = C >> 5;
+  const int ti = in.node_type[i];
+  const int e0 = in.first[i], e1 = in.first[i + 1];
+  float* sA = dyn;            // [17][C] A0 column
+  float* sGd = dyn + 17 * C;  // [17][C] gradient column (row 16 absorbs the constant slot)
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    sA[q * C + k] = A0[(static_cast<size_t>(i) * 16 + q) * C + k];
+    sGd[q * C + k] = 0.0f;
+  }
+  sA[16 * C + k] = 1.0f;
+  sGd[16 * C + k] = 0.0f;
+  for (int LM = 0; LM < m.nLM; ++LM) {
+    const float w = M0_adj[(static_cast<size_t>(i) * m.nLM + LM) * C + k];
+    const int t0 = m.mono0_off[LM], t1 = m.mono0_off[LM + 1];
+    const float* cf = m.coef0 + (static_cast<size_t>(ti * m.nLM + LM) * m.T0) * C + k;
+    for (int t = t0; t < t1; ++t) {
+      const int pk = __ldg(m.mono0 + t);
+      const int a = pk & 255, b = (pk >> 8) & 255, c = pk >> 16;
+      const float cw = __ldg(cf + static_cast<size_t>(t - t0) * C) * w;
+      const float xa = sA[a * C + k], xb = sA[b * C + k], xc = sA[c * C + k];
+      sGd[a * C + k] += cw * xb * xc;
+      sGd[b * C + k] += cw * xa * xc;
+      sGd[c * C + k] += cw * xa * xb;
+    }
+  }
+  float dA[16];
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    dA[q] = sGd[q * C + k];
+    if (A0_adj) A0_adj[(static_cast<size_t>(i) * 16 + q) * C + k] = dA[q];
+  }
+  for (int eb = e0; eb < e1; eb += kEdgeChunk) {
+    const int ne = min(kEdgeChunk, e1 - eb);
+    __syncthreads();
+    stage_edges<true>(m, in, ti, eb, ne, true, 4, sY, sG, su, sx, sbase, nullptr);
+    __syncthreads();
+    for (int t = 0; t < ne; ++t) {
+      const int base = sbase[t];
+      if (base < 0) {
+        if ((threadIdx.x & 31) == 0) sF[t][threadIdx.x >> 5][0] = sF[t][threadIdx.x >> 5][1] = sF[t][threadIdx.x >> 5][2] = 0.0f;
+        continue;
+      }
+      const float4* c = m.spl0 + static_cast<size_t>(base) * C + k;
+      const float x = sx[t];
+      float dr = 0.0f, fx = 0.0f, fy = 0.0f, fz = 0.0f;
+#pragma unroll
+      for (int l = 0; l < 4; ++l) {
+        const float4 cc = __ldg(c + l * C);
+        const float R = spline_val(cc, x), Rd = spline_der(cc, x);
+        float dRl = 0.0f;
+#pragma unroll
+        for (int q = l * l; q < (l + 1) * (l + 1); ++q) {
+          dRl = fmaf(dA[q], sY[q][t], dRl);
+          const float w = dA[q] * R;
+          fx = fmaf(w, sG[q][t], fx);
+          fy = fmaf(w, sG[16 + q][t], fy);
+          fz = fmaf(w, sG[32 + q][t], fz);
+        }
+        dr = fmaf(dRl, Rd, dr);
+      }
+      fx = fmaf(dr, su[0][t], fx);
+      fy = fmaf(dr, su[1][t], fy);
+      fz = fmaf(dr, su[2][t], fz);
+      block_reduce3(fx, fy, fz, sF, t);
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < ne; t += blockDim.x) {
+      const long e = static_cast<long>(eb) + t;
+      float s[3] = {0.0f, 0.0f, 0.0f};
+      for (int w = 0; w < nwarp; ++w)
+        for (int a = 0; a < 3; ++a) s[a] += sF[t][w][a];
+      for (int a = 0; a < 3; ++a) forces[3 * e + a] = -(static_cast<double>(s[a]) + static_cast<double>(f1[3 * e + a]));
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+void launch_layer0_fwd(const DevModel& m, const EdgeIn& in, float* A0, float* M0, cudaStream_t s) {
+  if (in.N <= 0) return;
+  const size_t smem = 17 * sizeof(float) * m.C;
+  k_layer0_fwd<<<in.N, m.C, smem, s>>>(m, in, A0, M0);
+}
+
+void launch_layer1_fwd(const DevModel& m, const EdgeIn& in, const float* H1, float* Phi1, cudaStream_t s) {
+  if (in.N <= 0) return;
+  const size_t smem = sizeof(float) * ins_np(1) * m.C;
+  cudaFuncSetAttribute(k_layer1_fwd<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  k_layer1_fwd<1><<<in.N, m.C, smem, s>>>(m, in, H1, Phi1);
+}
+
+void launch_layer1_rev(const DevModel& m, const EdgeIn& in, const float* H1, const float* dPhi1, float* H1_adj,
+                       float* f1, cudaStream_t s) {
+  if (in.N <= 0) return;
+  const size_t smem = sizeof(float) * (m.n_lme + ins_np(1)) * m.C;
+  cudaFuncSetAttribute(k_layer1_rev<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  k_layer1_rev<1><<<in.N, m.C, smem, s>>>(m, in, H1, dPhi1, H1_adj, f1);
+}
+
+void launch_layer0_rev(const DevModel& m, const EdgeIn& in, const float* A0, const float* M0_adj, const float* f1,
+                       float* A0_adj, double* forces, cudaStream_t s) {
+  if (in.N <= 0) return;
+  const size_t smem = 34 * sizeof(float) * m.C;
+  k_layer0_rev<<<in.N, m.C, smem, s>>>(m, in, A0, M0_adj, f1, A0_adj, forces);
+}
+
+}  // namespace smx

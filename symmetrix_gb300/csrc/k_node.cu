@@ -1,0 +1,244 @@
+// Node-level kernels: channel-mixing GEMMs, the layer-1 node tail (symmetric
+// contraction M1, H2, readouts, energy and the adjoint seeds), and small utilities.
+//
+// Reference stages restated here (libsymmetrix/source/mace.cpp):
+//   k_gemm       : compute_H1 / reverse_H1 (:397-451), compute_A1 / reverse_A1 (:607-679)
+//   k_node_tail  : compute_M1 (:759-777), compute_H2 (:796-832), compute_readouts (:876-903)
+//                  with MultilayerPerceptron::evaluate_gradient (multilayer_perceptron.cpp:76-150),
+//                  reverse_H2 (:834-874), reverse_M1 (:779-794)
+#include <cuda_runtime.h>
+
+#include "device.cuh"
+#include "kernels.h"
+
+namespace smx {
+
+// ---------------------------------------------------------------------------
+// FP32 SIMT GEMM, 64x64 tile, 16-deep k slices, 256 threads with a 4x4 register
+// tile each.  blockIdx.z selects the segment.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_gemm(GemmBatch gb) {
+  const GemmSeg g = gb.s[blockIdx.z];
+  const int row0 = blockIdx.x * 64, col0 = blockIdx.y * 64;
+  if (row0 >= g.rows || col0 >= g.ncols) return;
+  __shared__ __align__(16) float As[16][64 + 4];
+  __shared__ __align__(16) float Bs[16][64];
+  const int tid = threadIdx.x;
+  const int tr = tid >> 4, tc = tid & 15;
+  // A loader: row tid/4, k offset (tid%4)*4
+  const int a_row = row0 + (tid >> 2);
+  const int a_k = (tid & 3) * 4;
+  const float* a_ptr = nullptr;
+  if (a_row < g.rows) {
+    const int node = a_row / g.rpn, sub = a_row - node * g.rpn;
+    a_ptr = g.X + node * g.x_ns + g.x_off + static_cast<long>(sub) * g.x_rs;
+  }
+  // B loader: k row tid/16, cols (tid%16)*4
+  const int b_k = tid >> 4;
+  const int b_col = col0 + (tid & 15) * 4;
+  float acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) acc[a][b] = 0.0f;
+  for (int k0 = 0; k0 < g.K; k0 += 16) {
+    float4 av = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (a_ptr) av = __ldg(reinterpret_cast<const float4*>(a_ptr + k0 + a_k));
+    float4 bv = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (b_col < g.ncols) bv = __ldg(reinterpret_cast<const float4*>(g.B + static_cast<long>(k0 + b_k) * g.ncols + b_col));
+    __syncthreads();
+    As[a_k + 0][tid >> 2] = av.x;
+    As[a_k + 1][tid >> 2] = av.y;
+    As[a_k + 2][tid >> 2] = av.z;
+    As[a_k + 3][tid >> 2] = av.w;
+    *reinterpret_cast<float4*>(&Bs[b_k][(tid & 15) * 4]) = bv;
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < 16; ++kk) {
+      const float4 a4 = *reinterpret_cast<const float4*>(&As[kk][tr * 4]);
+      const float4 b4 = *reinterpret_cast<const float4*>(&Bs[kk][tc * 4]);
+      const float ar[4] = {a4.x, a4.y, a4.z, a4.w};
+      const float br[4] = {b4.x, b4.y, b4.z, b4.w};
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = fmaf(ar[a], br[b], acc[a][b]);
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    const int r = row0 + tr * 4 + a;
+    if (r >= g.rows) continue;
+    const int node = r / g.rpn, sub = r - node * g.rpn;
+    float* y = g.Y + node * g.y_ns + g.y_off + static_cast<long>(sub) * g.y_rs + col0 + tc * 4;
+    if (col0 + tc * 4 < g.ncols) *reinterpret_cast<float4*>(y) = make_float4(acc[a][0], acc[a][1], acc[a][2], acc[a][3]);
+  }
+}
+
+void launch_gemm(const GemmBatch& b, cudaStream_t s) {
+  int maxr = 0, maxc = 0;
+  for (int q = 0; q < b.n; ++q) {
+    maxr = b.s[q].rows > maxr ? b.s[q].rows : maxr;
+    maxc = b.s[q].ncols > maxc ? b.s[q].ncols : maxc;
+  }
+  if (maxr == 0 || b.n == 0) return;
+  dim3 grid(ceil_div(maxr, 64), ceil_div(maxc, 64), b.n);
+  k_gemm<<<grid, 256, 0, s>>>(b);
+}
+
+// ---------------------------------------------------------------------------
+// Layer-1 node tail, one block per node, one thread per channel.
+//   M1[k] = P1_{ti,k}(A1[i,:,k]) and its gradient,
+//   H2 = W_H1[ti]^T H1[i,0,:] + W_M1^T M1,
+//   E_i = e0[ti] + w1 . H1[i,0,:] + w2 . s*silu(W1 H2)           (float64 output),
+//   dE/dH2 (MLP gradient), H1_adj[i,0,:] = w1 + W_H1[ti] dE/dH2 (other rows 0),
+//   M1_adj = W_M1 dE/dH2, A1_adj[i,lm,k] = dM1/dA1[lm] * M1_adj[k].
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_node_tail(DevModel m, const int* __restrict__ ntype, const float* __restrict__ A1,
+                                                   const float* __restrict__ H1, float* __restrict__ M1o,
+                                                   float* __restrict__ H2o, float* __restrict__ A1_adj,
+                                                   float* __restrict__ H1_adj, float* __restrict__ M1_adj_o,
+                                                   float* __restrict__ H2_adj_o, double* __restrict__ energies) {
+  extern __shared__ float dyn[];
+  const int C = m.C, k = threadIdx.x, i = blockIdx.x;
+  const int nwarp = C >> 5, lane = k & 31, warp = k >> 5;
+  const int ti = ntype[i];
+  const int nh = m.n_hidden;
+  float* sX = dyn;              // [17][C]
+  float* sG = sX + 17 * C;      // [17][C]
+  float* sM1 = sG + 17 * C;     // [C]
+  float* sH10 = sM1 + C;        // [C]
+  float* sH2 = sH10 + C;        // [C]
+  float* sdH2 = sH2 + C;        // [C]
+  float* sRed = sdH2 + C;       // [33][8]
+  float* sS = sRed + 33 * 8;    // [33]
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    sX[q * C + k] = A1[(static_cast<size_t>(i) * 16 + q) * C + k];
+    sG[q * C + k] = 0.0f;
+  }
+  sX[16 * C + k] = 1.0f;
+  sG[16 * C + k] = 0.0f;
+  float f = 0.0f;
+  const float* cf = m.coef1 + static_cast<size_t>(ti) * m.T1 * C + k;
+  for (int t = 0; t < m.T1; ++t) {
+    const int pk = __ldg(m.mono1 + t);
+    const int a = pk & 255, b = (pk >> 8) & 255, c = pk >> 16;
+    const float w = __ldg(cf + static_cast<size_t>(t) * C);
+    const float xa = sX[a * C + k], xb = sX[b * C + k], xc = sX[c * C + k];
+    f = fmaf(w, xa * xb * xc, f);
+    sG[a * C + k] += w * xb * xc;
+    sG[b * C + k] += w * xa * xc;
+    sG[c * C + k] += w * xa * xb;
+  }
+  sM1[k] = f;
+  const float h10 = H1[static_cast<size_t>(i) * m.nLM * C + k];
+  sH10[k] = h10;
+  __syncthreads();
+  float h2 = 0.0f;
+  const float* W = m.H2W_H1 + static_cast<size_t>(ti) * C * C + k;
+  for (int r = 0; r < C; ++r) {
+    h2 = fmaf(sH10[r], __ldg(W + static_cast<size_t>(r) * C), h2);
+    h2 = fmaf(sM1[r], __ldg(m.H2W_M1 + static_cast<size_t>(r) * C + k), h2);
+  }
+  sH2[k] = h2;
+  // hidden pre-activations s_u = W1[u,:] . H2 and the linear readout w1 . H1[i,0,:] (slot nh)
+  for (int u = 0; u <= nh; ++u) {
+    float v = (u < nh) ? __ldg(m.ro2_w1 + static_cast<size_t>(u) * C + k) * h2 : __ldg(m.ro1 + k) * h10;
+    v = warp_sum(v);
+    if (lane == 0) sRed[u * 8 + warp] = v;
+  }
+  __syncthreads();
+  for (int u = k; u <= nh; u += C) {
+    float s = 0.0f;
+    for (int w = 0; w < nwarp; ++w) s += sRed[u * 8 + w];
+    sS[u] = s;
+  }
+  __syncthreads();
+  float dh2 = 0.0f;
+  for (int u = 0; u < nh; ++u) {
+    const float s = sS[u];
+    const float sg = 1.0f / (1.0f + expf(-s));
+    const float dact = m.ro2_scale * sg + m.ro2_scale * s * sg * (1.0f - sg);
+    dh2 = fmaf(__ldg(m.ro2_w2 + u) * dact, __ldg(m.ro2_w1 + static_cast<size_t>(u) * C + k), dh2);
+  }
+  sdH2[k] = dh2;
+  if (k == 0) {
+    double e = static_cast<double>(__ldg(m.e0 + ti)) + static_cast<double>(sS[nh]);
+    for (int u = 0; u < nh; ++u) {
+      const float s = sS[u];
+      const float sg = 1.0f / (1.0f + expf(-s));
+      e += static_cast<double>(__ldg(m.ro2_w2 + u) * (m.ro2_scale * s * sg));
+    }
+    energies[i] = e;
+  }
+  __syncthreads();
+  float ha = __ldg(m.ro1 + k), m1a = 0.0f;
+  const float* WT = m.H2W_H1_T + static_cast<size_t>(ti) * C * C + k;
+  for (int c = 0; c < C; ++c) {
+    const float d = sdH2[c];
+    ha = fmaf(__ldg(WT + static_cast<size_t>(c) * C), d, ha);
+    m1a = fmaf(__ldg(m.H2W_M1_T + static_cast<size_t>(c) * C + k), d, m1a);
+  }
+#pragma unroll
+  for (int q = 0; q < 16; ++q) A1_adj[(static_cast<size_t>(i) * 16 + q) * C + k] = sG[q * C + k] * m1a;
+  H1_adj[static_cast<size_t>(i) * m.nLM * C + k] = ha;
+  for (int LM = 1; LM < m.nLM; ++LM) H1_adj[(static_cast<size_t>(i) * m.nLM + LM) * C + k] = 0.0f;
+  M1o[static_cast<size_t>(i) * C + k] = f;
+  H2o[static_cast<size_t>(i) * C + k] = h2;
+  M1_adj_o[static_cast<size_t>(i) * C + k] = m1a;
+  H2_adj_o[static_cast<size_t>(i) * C + k] = dh2;
+}
+
+void launch_node_tail(const DevModel& m, const int* node_type, int N, const float* A1, const float* H1, float* M1,
+                      float* H2, float* A1_adj, float* H1_adj, float* M1_adj, float* H2_adj, double* energies,
+                      cudaStream_t s) {
+  if (N <= 0) return;
+  const size_t smem = sizeof(float) * (34 * m.C + 4 * m.C + 33 * 8 + 33);
+  k_node_tail<<<N, m.C, smem, s>>>(m, node_type, A1, H1, M1, H2, A1_adj, H1_adj, M1_adj, H2_adj, energies);
+}
+
+// first[0] = 0, first[i+1] = first[i] + num_neigh[i]; one block, sequential tiles.
+__global__ void __launch_bounds__(1024) k_scan_first(const int* __restrict__ num_neigh, int N, int* __restrict__ first) {
+  __shared__ int sw[32];
+  __shared__ int carry;
+  if (threadIdx.x == 0) {
+    carry = 0;
+    first[0] = 0;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int base = 0; base < N; base += 1024) {
+    const int idx = base + threadIdx.x;
+    int v = idx < N ? num_neigh[idx] : 0;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) sw[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      int w = sw[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += y;
+      }
+      sw[lane] = w;
+    }
+    __syncthreads();
+    const int incl = x + (warp > 0 ? sw[warp - 1] : 0) + carry;
+    if (idx < N) first[idx + 1] = incl;
+    __syncthreads();
+    if (threadIdx.x == 1023) carry = incl;
+    __syncthreads();
+  }
+}
+
+void launch_scan_first(const int* num_neigh, int N, int* first, cudaStream_t s) {
+  k_scan_first<<<1, 1024, 0, s>>>(num_neigh, N, first);
+}
+
+}  // namespace smx

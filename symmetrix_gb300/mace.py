@@ -1,0 +1,94 @@
+"""`MACE`: the Python face of the GB300 engine, shaped like the reference binding.
+
+Mirrors `symmetrix.MACE` (symmetrix/source/cpp/mace.cpp:12-243): construct from a
+JSON model path, call `compute_node_energies_forces(num_nodes, node_types,
+num_neigh, neigh_indices, neigh_types, xyz, r)`, then read `node_energies` and
+`node_forces` (= -dE/dxyz per directed edge).  Stage buffers (`A0`, `M0`, `H1`,
+`Phi1`, `A1`, `M1`, `H2` and the `*_adj` adjoints) are exposed read-only for
+stage-level checks like the reference's test_mace.py.  Errors raise ValueError /
+RuntimeError like the reference binding.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+
+STAGES = ("A0", "M0", "H1", "Phi1", "A1", "M1", "H2", "A0_adj", "M0_adj", "H1_adj", "Phi1_adj", "A1_adj",
+          "M1_adj", "H2_adj")
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None and a.size else None
+
+
+class MACE:
+    def __init__(self, filename, device=0, precision="float32", keep_stages=False):
+        self._lib = _lib.load()
+        if precision not in ("float32",):
+            raise ValueError(f"unsupported precision '{precision}'")
+        h = self._lib.smx_create(str(filename).encode(), 0, int(device))
+        if not h:
+            msg = self._lib.smx_last_error().decode(errors="replace")
+            raise RuntimeError(msg)
+        self._h = ctypes.c_void_p(h)
+        if keep_stages:
+            _lib.raise_for(self._lib.smx_set_option(self._h, b"keep_stages", 1))
+        n = self._lib.smx_num_elements(self._h)
+        buf = (ctypes.c_int * n)()
+        self._lib.smx_atomic_numbers(self._h, ctypes.cast(buf, ctypes.c_void_p), n)
+        self.atomic_numbers = list(buf)
+        self.num_elements = n
+        self.num_channels = self._lib.smx_num_channels(self._h)
+        self.r_cut = self._lib.smx_r_cut(self._h)
+        self.l_max = self._lib.smx_l_max(self._h)
+        self.L_max = self._lib.smx_L_max(self._h)
+        self.num_LM = self._lib.smx_num_LM(self._h)
+        self.node_energies = np.zeros(0)
+        self.node_forces = np.zeros(0)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            self._lib.smx_destroy(h)
+            self._h = None
+
+    def compute_node_energies_forces(self, num_nodes, node_types, num_neigh, neigh_indices, neigh_types, xyz, r):
+        node_types = np.ascontiguousarray(node_types, dtype=np.int32)[:num_nodes]
+        num_neigh = np.ascontiguousarray(num_neigh, dtype=np.int32)[:num_nodes]
+        neigh_indices = np.ascontiguousarray(neigh_indices, dtype=np.int32)
+        neigh_types = np.ascontiguousarray(neigh_types, dtype=np.int32)
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1)
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        E = len(r)
+        if len(neigh_indices) != E or len(neigh_types) != E or len(xyz) != 3 * E:
+            raise ValueError("edge arrays have inconsistent lengths")
+        energies = np.zeros(num_nodes)
+        forces = np.zeros(3 * E)
+        code = self._lib.smx_compute_node_energies_forces(
+            self._h, int(num_nodes), _ptr(node_types), _ptr(num_neigh), _ptr(neigh_indices), _ptr(neigh_types), E,
+            _ptr(xyz), _ptr(r), _ptr(energies), _ptr(forces))
+        _lib.raise_for(code, self._lib)
+        self.node_energies = energies
+        self.node_forces = forces
+
+    def compute_device(self, num_nodes, node_types, num_neigh, neigh_indices, neigh_types, num_edges, xyz, r,
+                       node_energies, node_forces, stream=None):
+        """Device-pointer variant: every argument is an integer device address."""
+        code = self._lib.smx_compute_node_energies_forces_device(
+            self._h, int(num_nodes), node_types, num_neigh, neigh_indices, neigh_types, int(num_edges), xyz, r,
+            node_energies, node_forces, stream)
+        _lib.raise_for(code, self._lib)
+
+    def stage(self, name):
+        n = self._lib.smx_get_stage(self._h, name.encode(), None, 0)
+        if n < 0:
+            raise KeyError(name)
+        out = np.zeros(n)
+        self._lib.smx_get_stage(self._h, name.encode(), _ptr(out), n)
+        return out
+
+    def __getattr__(self, name):
+        if name in STAGES:
+            return self.stage(name)
+        raise AttributeError(name)

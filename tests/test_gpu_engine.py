@@ -1,0 +1,139 @@
+"""GPU engine parity: the FP32 CUDA path through the C ABI against the float64 oracle.
+
+Tolerances (FP32 plain form vs the FP64 oracle): per-atom energies 2e-5 eV,
+per-edge and per-atom forces 1e-5 eV/A on the seeded workloads below; stage
+buffers to 1e-4 relative of their scale.
+"""
+import numpy as np
+import pytest
+
+from helpers import atomic_forces, edge_args
+from oracle.pyoracle import Evaluator
+from symmetrix_gb300.synth.model import CONFIGS, make_model, write_model
+from symmetrix_gb300.synth.structures import neighbor_list, random_box
+
+pytestmark = pytest.mark.gpu
+
+E_TOL = 2e-5
+F_TOL = 1e-5
+
+
+def _report(tag, a, b):
+    d = np.abs(np.asarray(a) - np.asarray(b))
+    print(f"{tag}: max|d|={d.max() if d.size else 0:.3e} rms={np.sqrt((d ** 2).mean()) if d.size else 0:.3e}")
+    return d.max() if d.size else 0.0
+
+
+def _engine(path, **kw):
+    from symmetrix_gb300 import MACE
+    return MACE(path, **kw)
+
+
+def test_small_workload_matches_reference_golden(engine_lib, small_model_path, small_golden):
+    g = small_golden
+    species = g["species"].astype(np.int32)
+    nl = {k: g[k] for k in ("num_neigh", "neigh_indices", "xyz", "r")}
+    m = _engine(small_model_path)
+    m.compute_node_energies_forces(*edge_args(species, nl))
+    assert _report("E_i", m.node_energies, g["node_energies"]) < E_TOL
+    assert _report("f_edge", m.node_forces, g["node_forces"]) < F_TOL
+    Fg = atomic_forces(64, g["edge_i"], g["neigh_indices"], g["node_forces"])
+    F = atomic_forces(64, g["edge_i"], g["neigh_indices"], m.node_forces)
+    assert _report("F_atom", F, Fg) < F_TOL
+
+
+def test_stages_match_oracle(engine_lib, small_model_path, small_golden):
+    g = small_golden
+    species = g["species"].astype(np.int32)
+    nl = {k: g[k] for k in ("num_neigh", "neigh_indices", "xyz", "r")}
+    m = _engine(small_model_path, keep_stages=True)
+    m.compute_node_energies_forces(*edge_args(species, nl))
+    ref = Evaluator(small_model_path, "port")
+    ref.compute_node_energies_forces(*edge_args(species, nl))
+    for s in ("A0", "M0", "H1", "Phi1", "A1", "M1", "H2", "H2_adj", "M1_adj", "A1_adj", "Phi1_adj", "H1_adj",
+              "M0_adj", "A0_adj"):
+        a, b = m.stage(s), ref.get(s)
+        assert a.shape == b.shape, s
+        scale = max(np.abs(b).max(), 1e-30)
+        assert _report(s, a, b) <= 1e-4 * scale, s
+
+
+def test_isolated_and_ragged_nodes(engine_lib, small_model_path):
+    pos = np.array([[0, 0, 0], [1.2, 0.1, 0], [0.3, 1.4, 0.2], [20.0, 20, 20], [-1.0, -0.8, 0.9]], dtype=float)
+    species = np.array([0, 1, 2, 1, 0], dtype=np.int32)
+    nl = neighbor_list(pos, 5.0)
+    m = _engine(small_model_path)
+    m.compute_node_energies_forces(*edge_args(species, nl))
+    ref = Evaluator(small_model_path, "port")
+    ref.compute_node_energies_forces(*edge_args(species, nl))
+    assert _report("E_i", m.node_energies, ref.node_energies) < E_TOL
+    assert _report("f_edge", m.node_forces, ref.node_forces) < F_TOL
+
+
+def test_empty_and_single_atom(engine_lib, small_model_path):
+    m = _engine(small_model_path)
+    m.compute_node_energies_forces(0, [], [], [], [], np.zeros((0, 3)), np.zeros(0))
+    assert m.node_energies.shape == (0,) and m.node_forces.shape == (0,)
+    m.compute_node_energies_forces(1, [2], [0], [], [], np.zeros((0, 3)), np.zeros(0))
+    ref = Evaluator(small_model_path, "port")
+    ref.compute_node_energies_forces(1, [2], [0], [], [], np.zeros((0, 3)), np.zeros(0))
+    assert abs(m.node_energies[0] - ref.node_energies[0]) < E_TOL
+
+
+def test_invalid_inputs_are_rejected(engine_lib, small_model_path):
+    m = _engine(small_model_path)
+    xyz = np.array([[1.0, 0.5, 0.2], [-1.0, -0.5, -0.2]])
+    r = np.linalg.norm(xyz, axis=1)
+    with pytest.raises(ValueError):  # neighbour index out of range
+        m.compute_node_energies_forces(2, [0, 1], [1, 1], [1, 2], [1, 0], xyz, r)
+    with pytest.raises(ValueError):  # species out of range
+        m.compute_node_energies_forces(2, [0, 7], [1, 1], [1, 0], [7, 0], xyz, r)
+    with pytest.raises(ValueError):  # r >= r_cut
+        m.compute_node_energies_forces(2, [0, 1], [1, 1], [1, 0], [1, 0], xyz * 10, r * 10)
+    with pytest.raises(ValueError):  # sum(num_neigh) != edges
+        m.compute_node_energies_forces(2, [0, 1], [2, 1], [1, 0], [1, 0], xyz, r)
+    with pytest.raises(RuntimeError):
+        _engine("/nonexistent/model.json")
+
+
+@pytest.fixture(scope="module")
+def wide_model(tmp_path_factory):
+    """128x0e+128x1o, H/C/N/O (the 4096-atom workload's shape), 50 knots to keep the file small."""
+    cfg = dict(CONFIGS["fp32_4096"], num_knots=50)
+    return write_model(make_model(**cfg, seed=7), str(tmp_path_factory.mktemp("wide") / "wide.json"))
+
+
+def test_wide_model_periodic_box(engine_lib, wide_model):
+    pos, L, species = random_box(160, 0.10, 0.9, 4, seed=9)
+    nl = neighbor_list(pos, 5.0, L)
+    m = _engine(wide_model)
+    m.compute_node_energies_forces(*edge_args(species, nl))
+    ref = Evaluator(wide_model, "port")
+    ref.compute_node_energies_forces(*edge_args(species, nl))
+    assert _report("E_i", m.node_energies, ref.node_energies) < E_TOL
+    assert _report("f_edge", m.node_forces, ref.node_forces) < F_TOL
+    F = atomic_forces(160, nl["i"], nl["neigh_indices"], m.node_forces)
+    Fr = atomic_forces(160, nl["i"], nl["neigh_indices"], ref.node_forces)
+    assert _report("F_atom", F, Fr) < F_TOL
+
+
+def test_device_api_matches_host_api(engine_lib, small_model_path, small_golden):
+    torch = pytest.importorskip("torch")
+    g = small_golden
+    species = g["species"].astype(np.int32)
+    m = _engine(small_model_path)
+    m.compute_node_energies_forces(64, species, g["num_neigh"], g["neigh_indices"],
+                                   species[g["neigh_indices"]], g["xyz"], g["r"])
+    dev = lambda a, dt: torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device="cuda")
+    t = [dev(species, torch.int32), dev(g["num_neigh"], torch.int32), dev(g["neigh_indices"], torch.int32),
+         dev(species[g["neigh_indices"]], torch.int32), dev(g["xyz"].reshape(-1), torch.float64),
+         dev(g["r"], torch.float64)]
+    E = len(g["r"])
+    e_out = torch.zeros(64, dtype=torch.float64, device="cuda")
+    f_out = torch.zeros(3 * E, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    m.compute_device(64, *[x.data_ptr() for x in t[:4]], E, t[4].data_ptr(), t[5].data_ptr(), e_out.data_ptr(),
+                     f_out.data_ptr(), stream)
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(e_out.cpu().numpy(), m.node_energies, rtol=0, atol=1e-6)
+    np.testing.assert_allclose(f_out.cpu().numpy(), m.node_forces, rtol=0, atol=1e-6)

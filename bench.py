@@ -1,0 +1,434 @@
+#!/usr/bin/env python3
+"""Throughput of the GB300 MACE engine on the 4096-atom FP32 workload.
+
+Workload (the single-GPU configuration the headline metric is quoted on): a
+periodic cubic box of 4096 atoms at 0.10 atoms/A^3 (H/C/N/O uniform, minimum pair
+distance 0.9 A, seeded random insertion) with a seeded random 2-layer MACE of
+128x0e+128x1o channels, l_max 3, correlation 3, r_cut 5 A, 8 Bessel radials with
+p=5 envelope tabulated on 200 spline knots.  Synthetic data: no public dataset or
+checkpoint is involved.
+
+A step is one energy + force evaluation of the whole box (forward and adjoint
+pass, per-edge forces, per-atom energies) on device-resident inputs.  `value`
+is atoms x steps / device time, with L2 (129 MB) flushed by a 256 MB write
+between timed steps; `e2e` is the same metric through the host-pointer C ABI
+call a LAMMPS/ASE caller makes (host->device copies of the neighbour list and
+device->host copies of energies and forces inside the timed region).
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+Multi-GPU (torchrun): every rank evaluates its own replica of the box (the
+engine does not shard one box over GPUs); value is the job's total.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "atom-steps/s (E+F) on 1 GB300: BF16-mixed vs FP32 at <=10 meV/A force error"
+UNIT = "atom-steps/s"
+WORKLOAD = dict(name="fp32_4096", n_atoms=4096, density=0.10, min_dist=0.9, model_seed=1, struct_seed=2,
+                cpu_sample_atoms=256)
+CACHE = os.path.join(tempfile.gettempdir(), "smx_bench")
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ---------------------------------------------------------------------------
+# workload
+# ---------------------------------------------------------------------------
+def model_path():
+    from symmetrix_gb300.synth.model import CONFIGS, make_model, write_model
+    os.makedirs(CACHE, exist_ok=True)
+    path = os.path.join(CACHE, f"model_{WORKLOAD['name']}_s{WORKLOAD['model_seed']}.json")
+    if not os.path.exists(path):
+        t = time.time()
+        write_model(make_model(**CONFIGS["fp32_4096"], seed=WORKLOAD["model_seed"]), path + ".tmp")
+        os.replace(path + ".tmp", path)
+        log(f"model written in {time.time() - t:.1f} s")
+    return path
+
+
+def structure(n_atoms, seed):
+    from symmetrix_gb300.synth.structures import neighbor_list, random_box
+    pos, L, species = random_box(n_atoms, WORKLOAD["density"], WORKLOAD["min_dist"], 4, seed=seed)
+    nl = neighbor_list(pos, 5.0, L)
+    return pos, L, species, nl
+
+
+def model_dims(eng, path):
+    with open(path) as f:
+        m = json.load(f)
+    C = m["num_channels"]
+    L_max = m["L_max"]
+    n_e = [sum(1 for l in m["Phi1_l"] if l == ll) for ll in range(4)]
+    return dict(C=C, S=m["num_elements"], nLM=(L_max + 1) ** 2, n_lme=sum((2 * l + 1) for l in m["Phi1_l"]),
+                NI=len(m["Phi1_l"]), NP=sum((2 * a + 1) * (2 * b + 1) for a, b in zip(m["Phi1_l1"], m["Phi1_l2"])),
+                G=len(m["Phi1_clebsch_gordan"]), T0=[len(m["M0_monomials"][str(q)]) for q in range((L_max + 1) ** 2)],
+                T1=len(m["M1_monomials"]), nint=len(m["radial_spline_values_0"][0][0]) - 1,
+                npairs=len(m["radial_spline_values_0"]), n_e=n_e, nh=len(m["readout_2_weights_2"]),
+                l1=m["Phi1_l1"], l2=m["Phi1_l2"])
+
+
+def stage_costs(d, N, E):
+    """Algorithmic FLOPs and compulsory DRAM bytes of each kernel launch (FP32 storage)."""
+    C, S, nLM, n_lme, NI, NP, G = d["C"], d["S"], d["nLM"], d["n_lme"], d["NI"], d["NP"], d["G"]
+    f4 = 4
+    spl0 = S * S * d["nint"] * 4 * C * 16
+    spl1 = d["npairs"] * d["nint"] * NI * C * 16
+    coef0 = S * sum(d["T0"]) * C * f4
+    sum_2l1 = sum(2 * a + 1 for a in d["l1"])
+    out = {}
+    out["layer0_fwd"] = (E * C * 56 + N * C * 4 * sum(d["T0"]),
+                         E * 36 + 8 * N + spl0 + coef0 + N * (16 + nLM) * C * f4)
+    out["gemm_H1"] = (2 * N * nLM * C * C, 2 * N * nLM * C * f4 + nLM * C * C * f4)
+    out["layer1_fwd"] = (E * C * (6 * NI + sum_2l1 + 2 * NP) + 2 * N * C * G,
+                         E * 40 + 8 * N + N * nLM * C * f4 + spl1 + N * n_lme * C * f4)
+    out["gemm_A1"] = (2 * N * C * C * n_lme, N * (n_lme + 16) * C * f4 + n_lme * C * C * f4)
+    out["node_tail"] = (N * C * (10 * d["T1"] + 8 * C + 4 * d["nh"]),
+                        N * (16 + 1) * C * f4 + N * (4 + 16 + nLM) * C * f4 + 8 * N + (2 * S + 2) * C * C * f4)
+    out["gemm_Phi1_adj"] = (2 * N * C * C * n_lme, N * (n_lme + 16) * C * f4 + n_lme * C * C * f4)
+    out["layer1_rev"] = (E * C * (10 * NI + 4 * NP + 5 * sum_2l1 + 2 * NI + 102) + 2 * N * C * G,
+                         E * 52 + 8 * N + N * (n_lme + nLM) * C * f4 + spl1 + 2 * N * nLM * C * f4)
+    out["gemm_M0_adj"] = (2 * N * nLM * C * C, 2 * N * nLM * C * f4 + nLM * C * C * f4)
+    out["layer0_rev"] = (E * C * (40 + 16 * 9 + 14) + N * C * 10 * sum(d["T0"]),
+                         E * (36 + 12 + 24) + 8 * N + spl0 + coef0 + N * (16 + nLM) * C * f4)
+    return out
+
+
+# ---------------------------------------------------------------------------
+# clocks
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(tempfile.gettempdir(), f"smx_clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline (the oracle: reference build where present, else the port)
+# ---------------------------------------------------------------------------
+def cpu_evaluators(path, threads):
+    """The reference's own evaluator (oracle/_ref) where it was built here, else the port."""
+    from oracle import build as ob
+    from oracle.pyoracle import Evaluator
+    if os.path.exists(ob.REF_SO) and os.path.isdir(ob.REF_SRC):
+        evs = [None] * threads
+
+        def load(q):
+            evs[q] = Evaluator(path, "reference")
+
+        ths = [threading.Thread(target=load, args=(q,)) for q in range(threads)]
+        for th in ths:
+            th.start()
+        for th in ths:
+            th.join()
+        return "reference", evs
+    ev = Evaluator(path, "port")
+    return "port", [ev] + [ev.clone() for _ in range(threads - 1)]
+
+
+def cpu_rate(path, threads, repeats, n_atoms):
+    """atom-steps/s of `threads` independent evaluations of an n_atoms sub-box."""
+    kind, evs = cpu_evaluators(path, threads)
+    pos, L, species, nl = structure(n_atoms, WORKLOAD["struct_seed"] + 100)
+    args = (n_atoms, species, nl["num_neigh"], nl["neigh_indices"], species[nl["neigh_indices"]], nl["xyz"], nl["r"])
+
+    def run(ev):
+        ev.compute_node_energies_forces(*args)
+
+    times = []
+    for rep in range(repeats + 1):
+        t = time.perf_counter()
+        ths = [threading.Thread(target=run, args=(ev,)) for ev in evs]
+        for th in ths:
+            th.start()
+        for th in ths:
+            th.join()
+        if rep > 0:
+            times.append(time.perf_counter() - t)
+    dt = statistics.median(times)
+    return kind, threads * n_atoms / dt, dt, len(nl["r"])
+
+
+def reference_arm(args, rank, world):
+    if rank != 0:
+        return
+    path = model_path()
+    threads = os.cpu_count() or 1
+    n = WORKLOAD["cpu_sample_atoms"]
+    kind, evs = cpu_evaluators(path, threads)
+    pos, L, species, nl = structure(n, WORKLOAD["struct_seed"] + 100)
+    a = (n, species, nl["num_neigh"], nl["neigh_indices"], species[nl["neigh_indices"]], nl["xyz"], nl["r"])
+
+    def step():
+        ths = [threading.Thread(target=ev.compute_node_energies_forces, args=a) for ev in evs]
+        for th in ths:
+            th.start()
+        for th in ths:
+            th.join()
+
+    for _ in range(args.warmup):
+        step()
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = (time.perf_counter() - t) / args.steps
+    value = threads * n / dt
+    sample = (f"{threads} threads, each one E+F evaluation per step of a {n}-atom box of the same model, density "
+              f"and species mix ({len(nl['r'])} edges); " + ("the reference's libsymmetrix/source/mace.cpp built "
+              "from its sources" if kind == "reference" else "float64 oracle restatement of libsymmetrix/source/"
+              "mace.cpp"))
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD["name"], "atoms_per_step": n * threads, "threads": threads},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def gpu_arm(args, rank, world, local_rank):
+    import ctypes
+
+    import torch
+
+    from symmetrix_gb300 import MACE, _lib
+    from symmetrix_gb300.build import build
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    build()
+    path = model_path()
+    N = WORKLOAD["n_atoms"]
+    pos, L, species, nl = structure(N, WORKLOAD["struct_seed"] + rank)
+    E = len(nl["r"])
+    eng = MACE(path, device=local_rank)
+    eng.set_option("profile", 1)
+    dims = model_dims(eng, path)
+
+    dev = torch.device("cuda", local_rank)
+    t_types = torch.as_tensor(species, dtype=torch.int32, device=dev)
+    t_nn = torch.as_tensor(nl["num_neigh"], dtype=torch.int32, device=dev)
+    t_idx = torch.as_tensor(nl["neigh_indices"], dtype=torch.int32, device=dev)
+    t_nt = torch.as_tensor(species[nl["neigh_indices"]], dtype=torch.int32, device=dev)
+    t_xyz = torch.as_tensor(nl["xyz"].reshape(-1), dtype=torch.float64, device=dev)
+    t_r = torch.as_tensor(nl["r"], dtype=torch.float64, device=dev)
+    t_e = torch.zeros(N, dtype=torch.float64, device=dev)
+    t_f = torch.zeros(3 * E, dtype=torch.float64, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    sptr = stream.cuda_stream
+
+    def step():
+        eng.compute_device(N, t_types.data_ptr(), t_nn.data_ptr(), t_idx.data_ptr(), t_nt.data_ptr(), E,
+                           t_xyz.data_ptr(), t_r.data_ptr(), t_e.data_ptr(), t_f.data_ptr(), sptr)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            flush.fill_(1)
+            step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    time.sleep(0.3)
+    stage_tot = {}
+    step_ms = []
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.fill_(k & 255)
+            ev[k][0].record(stream)
+            step()
+            ev[k][1].record(stream)
+            st = eng.stage_times()  # waits for this step; keeps per-kernel times
+            for n_, v in st.items():
+                stage_tot[n_] = stage_tot.get(n_, 0.0) + v
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    T = sum(step_ms) / 1e3
+    if dist:
+        tt = torch.tensor([T], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        T = tt.item()
+    value = world * N * args.steps / T
+
+    # energy / force sanity of the last step
+    e_tot = t_e.sum().item()
+
+    # ---- e2e: the host-pointer C ABI with pinned host buffers ----
+    lib = _lib.load()
+    pin = lambda a, dt: torch.as_tensor(np.ascontiguousarray(a), dtype=dt).pin_memory()
+    h = [pin(species, torch.int32), pin(nl["num_neigh"], torch.int32), pin(nl["neigh_indices"], torch.int32),
+         pin(species[nl["neigh_indices"]], torch.int32), pin(nl["xyz"].reshape(-1), torch.float64),
+         pin(nl["r"], torch.float64)]
+    h_e = torch.zeros(N, dtype=torch.float64).pin_memory()
+    h_f = torch.zeros(3 * E, dtype=torch.float64).pin_memory()
+    P = lambda t: ctypes.c_void_p(t.data_ptr())
+
+    def e2e_step():
+        code = lib.smx_compute_node_energies_forces(eng._h, N, P(h[0]), P(h[1]), P(h[2]), P(h[3]), E, P(h[4]),
+                                                    P(h[5]), P(h_e), P(h_f))
+        _lib.raise_for(code, lib)
+
+    eng.set_option("profile", 0)
+    for _ in range(args.warmup):
+        e2e_step()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    t_e2e = time.perf_counter() - t0
+    if dist:
+        tt = torch.tensor([t_e2e], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_e2e = tt.item()
+    e2e = {"value": world * N * args.steps / t_e2e, "unit": UNIT,
+           "h2d_bytes_per_step": 4 * N + 4 * (N + 1) + E * (4 + 4 + 24 + 8), "d2h_bytes_per_step": 8 * N + 24 * E}
+    e2e_energy = h_e.sum().item()
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    # ---- roofline of the dominant kernel (live CUDA-event times) ----
+    costs = stage_costs(dims, N, E)
+    avg = {n_: v / args.steps for n_, v in stage_tot.items()}
+    dom = max(avg, key=avg.get)
+    flops, bytes_ = costs[dom]
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        peaks = json.load(open(peaks_path))
+        hbm, peak_src = peaks["hbm_gbs"], "measured"
+    else:
+        hbm, peak_src = 6800.0, "fallback"
+    t_dom = avg[dom] / 1e3
+    achieved = bytes_ / t_dom / 1e9
+    sm_mhz = clk.get("sm_mhz") or 2070.0
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "peak_source": peak_src, "traffic": None,
+                "algorithmic_bytes_per_launch": bytes_,
+                "fp32_simt": {"achieved_tflops": flops / t_dom / 1e12, "peak_tflops": fp32_peak,
+                              "frac": flops / t_dom / 1e12 / fp32_peak,
+                              "peak_source": "152 SMs x 128 FP32 lanes x 2 x median SM clock under load"}}
+    per_stage = {n_: {"ms": avg[n_], "gflop": costs[n_][0] / 1e9, "tflops": costs[n_][0] / (avg[n_] / 1e3) / 1e12,
+                      "gbs": costs[n_][1] / (avg[n_] / 1e3) / 1e9} for n_ in avg}
+
+    # ---- CPU baseline: the oracle, one thread, bounded sample ----
+    kind, cpu_val, cpu_dt, cpu_edges = cpu_rate(path, 1, 2, WORKLOAD["cpu_sample_atoms"])
+    cpu = {"value": cpu_val, "unit": UNIT, "cores": 1, "kind": kind,
+           "sample": f"median of 2 E+F evaluations of a {WORKLOAD['cpu_sample_atoms']}-atom box of the same model, "
+                     f"density and species mix ({cpu_edges} edges), float64, 1 thread"}
+
+    launches_per_step = 10  # scan + 9 stage kernels
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": T / args.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "fp32_4096: periodic box, 4096 atoms, 0.10 atoms/A^3, H/C/N/O, "
+                               "128x0e+128x1o, l_max 3, correlation 3, r_cut 5 A, 200 spline knots",
+                   "atoms": N, "edges": E, "step": "one E+F evaluation (forward + adjoint), device-resident inputs",
+                   "l2": "flushed between timed steps (256 MB write, untimed)", "replicas_per_gpu": 1},
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": launches_per_step * args.steps,
+        "clocks": clk,
+        "stages_ms": per_stage,
+        "wall_s_timed_region": t_wall,
+        "check": {"energy_device": e_tot, "energy_e2e": e2e_energy},
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local_rank = int(os.environ.get("LOCAL_RANK", 0))
+    if args.impl == "reference":
+        reference_arm(args, rank, world)
+    else:
+        gpu_arm(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

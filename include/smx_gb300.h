@@ -19,6 +19,14 @@
  *   smx_atomic_numbers              public fields of class MACE (mace.hpp:18-25)
  *   smx_get_stage                   the read-only stage buffers the Python binding exposes
  *                                   (symmetrix/source/cpp/mace.cpp:14-34)
+ *   smx_compute_atoms               what the callers do around the evaluator: neighbour list,
+ *                                   evaluation, F_j += f_e / F_i -= f_e and the virial
+ *                                   (Symmetrix.calculate, symmetrix_calc.py:72-102;
+ *                                   PairSymmetrixMACE::compute_no_domain_decomposition,
+ *                                   pair_symmetrix/pair_symmetrix_mace.cpp:242-372)
+ *   smx_md_*                        a GPU-resident velocity-Verlet loop with a skin neighbour
+ *                                   list, the role LAMMPS `fix nve` plays around the pair
+ *                                   style (pair_symmetrix/test/test_pair_symmetrix_mace.py:253)
  *
  * Conventions (identical to the reference):
  *   - edges are a full directed list grouped by centre node: node i owns edges
@@ -86,7 +94,42 @@ int smx_compute_node_energies_forces_device(smx_engine* eng, int num_nodes, cons
  * name.  A0_adj is kept only after smx_set_option(eng, "keep_stages", 1). */
 long smx_get_stage(smx_engine* eng, const char* name, double* out, long cap);
 
+/* Options: "keep_stages" (keep A0_adj for smx_get_stage), "profile" (record CUDA
+ * events between the kernels of every evaluation). */
 int smx_set_option(smx_engine* eng, const char* key, long value);
+
+/* With "profile" on: device time (ms) of each stage of the last evaluation, in launch
+ * order: layer0_fwd, gemm_H1, layer1_fwd, gemm_A1, node_tail, gemm_Phi1_adj,
+ * layer1_rev, gemm_M0_adj, layer0_rev.  Returns the number of stages (0 if profiling
+ * is off).  Blocks until the last evaluation has finished. */
+int smx_stage_times(smx_engine* eng, double* out_ms, int cap);
+
+/* Atom-level evaluation: positions[3n] (A), species[n] (indices into atomic_numbers),
+ * box_lengths[3] of an orthorhombic periodic cell (NULL = non-periodic).  Builds the
+ * full neighbour list (r < r_cut) on the GPU, evaluates, and returns the total energy,
+ * optionally node_energies[n], atomic forces[3n] and the virial[9] W_ab = sum_e xyz_a f_b
+ * (row-major, float64).  Host pointers; synchronous. */
+int smx_compute_atoms(smx_engine* eng, int n_atoms, const double* positions, const int* species,
+                      const double* box_lengths, double* energy, double* node_energies, double* forces,
+                      double* virial);
+
+/* Velocity-Verlet MD on the GPU.  Units: A, fs, amu, eV.  velocities may be NULL (zero).
+ * The neighbour list (r_cut + skin) is rebuilt every rebuild_every steps; the steps in
+ * between run as one captured CUDA graph.  NULL on failure (see smx_last_error). */
+typedef struct smx_md smx_md;
+smx_md* smx_md_create(smx_engine* eng, int n_atoms, const double* positions, const double* velocities,
+                      const int* species, const double* masses, const double* box_lengths, double dt_fs, double skin,
+                      int rebuild_every);
+/* Enqueue `steps` steps on the engine's stream; returns without waiting for them
+ * except at neighbour-list rebuilds. */
+int smx_md_run(smx_md* md, int steps);
+int smx_md_sync(smx_md* md);
+/* Current state (any pointer may be NULL): positions[3n], velocities[3n] (A/fs),
+ * forces[3n], potential energy, virial[9], step count.  Synchronous. */
+int smx_md_state(smx_md* md, double* positions, double* velocities, double* forces, double* potential_energy,
+                 double* virial, long* step);
+long smx_md_num_edges(smx_md* md);
+void smx_md_destroy(smx_md* md);
 
 #ifdef __cplusplus
 }

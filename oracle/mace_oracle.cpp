@@ -784,6 +784,10 @@ void* orc_load(const char* path) {
 
 void orc_free(void* h) { delete static_cast<Oracle*>(h); }
 
+// An independent evaluator sharing nothing with h (copies the loaded model), so
+// several threads can evaluate in parallel without re-reading the model file.
+void* orc_clone(void* h) { return new Oracle(*static_cast<Oracle*>(h)); }
+
 int orc_info(void* h, int* out) {
   auto* o = static_cast<Oracle*>(h);
   out[0] = o->S;

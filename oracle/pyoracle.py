@@ -34,6 +34,9 @@ def library(which="port"):
     f("load").restype = P
     f("load").argtypes = [ctypes.c_char_p]
     f("free").argtypes = [P]
+    if pre == "orc_":
+        f("clone").restype = P
+        f("clone").argtypes = [P]
     f("info").argtypes = [P, ip]
     f("compute").restype = I
     f("compute").argtypes = [P, I, ip, ip, ip, ip, L, dp, dp]
@@ -63,14 +66,23 @@ def _dp(a):
 
 
 class Evaluator:
-    def __init__(self, model_path, which="port"):
+    def __init__(self, model_path, which="port", _clone_of=None):
         self.lib, self.pre = library(which)
-        self.h = getattr(self.lib, self.pre + "load")(str(model_path).encode())
+        if _clone_of is not None:
+            self.h = getattr(self.lib, "orc_clone")(_clone_of.h)
+        else:
+            self.h = getattr(self.lib, self.pre + "load")(str(model_path).encode())
         if not self.h:
             raise RuntimeError(getattr(self.lib, self.pre + "last_error")().decode())
         info = (ctypes.c_int * 6)()
         getattr(self.lib, self.pre + "info")(self.h, info)
         self.num_elements, self.num_channels, self.l_max, self.L_max, self.num_lme, self.num_lelm1lm2 = list(info)
+
+    def clone(self):
+        """An independent evaluator with the same model (port only), for parallel threads."""
+        if self.pre != "orc_":
+            raise ValueError("clone() is available for the port only")
+        return Evaluator(None, "port", _clone_of=self)
 
     def __del__(self):
         if getattr(self, "h", None):

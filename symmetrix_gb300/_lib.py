@@ -33,7 +33,18 @@ SIGNATURES = [
     ("smx_compute_node_energies_forces_device", _I, [_P, _I, _P, _P, _P, _P, _L, _P, _P, _P, _P, _P]),
     ("smx_get_stage", _L, [_P, _S, _P, _L]),
     ("smx_set_option", _I, [_P, _S, _L]),
+    ("smx_stage_times", _I, [_P, _P, _I]),
+    ("smx_compute_atoms", _I, [_P, _I, _P, _P, _P, _P, _P, _P, _P]),
+    ("smx_md_create", _P, [_P, _I, _P, _P, _P, _P, _P, _D, _D, _I]),
+    ("smx_md_run", _I, [_P, _I]),
+    ("smx_md_sync", _I, [_P]),
+    ("smx_md_state", _I, [_P, _P, _P, _P, _P, _P, _P]),
+    ("smx_md_num_edges", _L, [_P]),
+    ("smx_md_destroy", None, [_P]),
 ]
+
+STAGE_NAMES = ("layer0_fwd", "gemm_H1", "layer1_fwd", "gemm_A1", "node_tail", "gemm_Phi1_adj", "layer1_rev",
+               "gemm_M0_adj", "layer0_rev")
 
 _lib = None
 

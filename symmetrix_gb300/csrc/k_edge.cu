@@ -64,17 +64,22 @@ __device__ __forceinline__ void stage_edges(const DevModel& m, const EdgeIn& in,
   }
 }
 
-// Sum a per-thread 3-vector over the block's channels for edge t: warp shuffles,
-// then one partial per warp into sF (reduced after the chunk).
-__device__ __forceinline__ void block_reduce3(float fx, float fy, float fz, float (*sF)[8][3], int t) {
-  fx = warp_sum(fx);
-  fy = warp_sum(fy);
-  fz = warp_sum(fz);
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Sum a per-thread 3-vector over the block's channels for edge t in float64 (the
+// channel sum of per-edge force terms cancels strongly): warp shuffles, then one
+// partial per warp into sF (reduced after the chunk).
+__device__ __forceinline__ void block_reduce3(float fx, float fy, float fz, double (*sF)[8][3], int t) {
+  const double x = warp_sum_d(fx), y = warp_sum_d(fy), z = warp_sum_d(fz);
   if ((threadIdx.x & 31) == 0) {
     const int w = threadIdx.x >> 5;
-    sF[t][w][0] = fx;
-    sF[t][w][1] = fy;
-    sF[t][w][2] = fz;
+    sF[t][w][0] = x;
+    sF[t][w][1] = y;
+    sF[t][w][2] = z;
   }
 }
 
@@ -204,7 +209,7 @@ __global__ void __launch_bounds__(256) k_layer1_fwd(DevModel m, EdgeIn in, const
 template <int LMAX>
 __global__ void __launch_bounds__(256) k_layer1_rev(DevModel m, EdgeIn in, const float* __restrict__ H1,
                                                     const float* __restrict__ dPhi1, float* __restrict__ H1_adj,
-                                                    float* __restrict__ f1) {
+                                                    double* __restrict__ f1) {
   constexpr int NL2 = (LMAX + 1) * (LMAX + 1);
   constexpr int NI = ins_count(LMAX);
   constexpr int NP = ins_np(LMAX);
@@ -215,7 +220,7 @@ __global__ void __launch_bounds__(256) k_layer1_rev(DevModel m, EdgeIn in, const
   __shared__ float sx[kEdgeChunk];
   __shared__ int sbase[kEdgeChunk];
   __shared__ int sj[kEdgeChunk];
-  __shared__ float sF[kEdgeChunk][8][3];
+  __shared__ double sF[kEdgeChunk][8][3];
   const int C = m.C, k = threadIdx.x, i = blockIdx.x;
   const int nwarp = C >> 5;
   const int ti = in.node_type[i];
@@ -294,7 +299,7 @@ __global__ void __launch_bounds__(256) k_layer1_rev(DevModel m, EdgeIn in, const
     }
     __syncthreads();
     for (int t = threadIdx.x; t < ne; t += blockDim.x) {
-      float s[3] = {0.0f, 0.0f, 0.0f};
+      double s[3] = {0.0, 0.0, 0.0};
       for (int w = 0; w < nwarp; ++w)
         for (int a = 0; a < 3; ++a) s[a] += sF[t][w][a];
       for (int a = 0; a < 3; ++a) f1[3 * (static_cast<long>(eb) + t) + a] = s[a];
@@ -308,7 +313,7 @@ __global__ void __launch_bounds__(256) k_layer1_rev(DevModel m, EdgeIn in, const
 // and node_forces[e] = -(layer-0 + layer-1 contributions), in float64.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_layer0_rev(DevModel m, EdgeIn in, const float* __restrict__ A0,
-                                                    const float* __restrict__ M0_adj, const float* __restrict__ f1,
+                                                    const float* __restrict__ M0_adj, const double* __restrict__ f1,
                                                     float* __restrict__ A0_adj, double* __restrict__ forces) {
   extern __shared__ float dyn[];
   __shared__ float sY[16][kEdgeChunk];
@@ -316,7 +321,7 @@ __global__ void __launch_bounds__(256) k_layer0_rev(DevModel m, EdgeIn in, const
   __shared__ float su[3][kEdgeChunk];
   __shared__ float sx[kEdgeChunk];
   __shared__ int sbase[kEdgeChunk];
-  __shared__ float sF[kEdgeChunk][8][3];
+  __shared__ double sF[kEdgeChunk][8][3];
   const int C = m.C, k = threadIdx.x, i = blockIdx.x;
   const int nwarp = C >> 5;
   const int ti = in.node_type[i];
@@ -387,10 +392,10 @@ __global__ void __launch_bounds__(256) k_layer0_rev(DevModel m, EdgeIn in, const
     __syncthreads();
     for (int t = threadIdx.x; t < ne; t += blockDim.x) {
       const long e = static_cast<long>(eb) + t;
-      float s[3] = {0.0f, 0.0f, 0.0f};
+      double s[3] = {0.0, 0.0, 0.0};
       for (int w = 0; w < nwarp; ++w)
         for (int a = 0; a < 3; ++a) s[a] += sF[t][w][a];
-      for (int a = 0; a < 3; ++a) forces[3 * e + a] = -(static_cast<double>(s[a]) + static_cast<double>(f1[3 * e + a]));
+      for (int a = 0; a < 3; ++a) forces[3 * e + a] = -(s[a] + f1[3 * e + a]);
     }
   }
 }
@@ -398,6 +403,16 @@ __global__ void __launch_bounds__(256) k_layer0_rev(DevModel m, EdgeIn in, const
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
+// Dynamic shared memory above 48 KB must be opted into once per kernel (outside
+// any stream capture).
+cudaError_t init_edge_kernels(const DevModel& m) {
+  cudaError_t e = cudaFuncSetAttribute(k_layer1_fwd<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(sizeof(float) * ins_np(1) * m.C));
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_layer1_rev<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              static_cast<int>(sizeof(float) * (m.n_lme + ins_np(1)) * m.C));
+}
+
 void launch_layer0_fwd(const DevModel& m, const EdgeIn& in, float* A0, float* M0, cudaStream_t s) {
   if (in.N <= 0) return;
   const size_t smem = 17 * sizeof(float) * m.C;
@@ -407,19 +422,17 @@ void launch_layer0_fwd(const DevModel& m, const EdgeIn& in, float* A0, float* M0
 void launch_layer1_fwd(const DevModel& m, const EdgeIn& in, const float* H1, float* Phi1, cudaStream_t s) {
   if (in.N <= 0) return;
   const size_t smem = sizeof(float) * ins_np(1) * m.C;
-  cudaFuncSetAttribute(k_layer1_fwd<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
   k_layer1_fwd<1><<<in.N, m.C, smem, s>>>(m, in, H1, Phi1);
 }
 
 void launch_layer1_rev(const DevModel& m, const EdgeIn& in, const float* H1, const float* dPhi1, float* H1_adj,
-                       float* f1, cudaStream_t s) {
+                       double* f1, cudaStream_t s) {
   if (in.N <= 0) return;
   const size_t smem = sizeof(float) * (m.n_lme + ins_np(1)) * m.C;
-  cudaFuncSetAttribute(k_layer1_rev<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
   k_layer1_rev<1><<<in.N, m.C, smem, s>>>(m, in, H1, dPhi1, H1_adj, f1);
 }
 
-void launch_layer0_rev(const DevModel& m, const EdgeIn& in, const float* A0, const float* M0_adj, const float* f1,
+void launch_layer0_rev(const DevModel& m, const EdgeIn& in, const float* A0, const float* M0_adj, const double* f1,
                        float* A0_adj, double* forces, cudaStream_t s) {
   if (in.N <= 0) return;
   const size_t smem = 34 * sizeof(float) * m.C;

@@ -1,0 +1,342 @@
+// Neighbour lists, per-step edge geometry, atomic forces / virial and velocity
+// Verlet for the MD driver and the atom-level API.
+//
+// The reference delegates neighbour lists to its callers: the LAMMPS pair style
+// filters LAMMPS's full list to r < r_cut (pair_symmetrix_mace.cpp:242-315) and
+// the ASE calculator calls neighbor_list('ijdD') (symmetrix_calc.py:77).  Here a
+// cell list builds the same full, directed, CSR-ordered list on the GPU with a
+// skin, deterministically: atoms are binned, each cell's atom list is sorted by
+// index, and every centre scans its 27 neighbour cells in a fixed order.
+// Atomic forces and the virial follow pair_symmetrix_mace.cpp:324-368
+// (F_j += f_e, F_i -= f_e; W = sum_e xyz_e (x) f_e), reduced without atomics via
+// the reverse-edge map, in float64.
+#include <cuda_runtime.h>
+
+#include "device.cuh"
+#include "kernels.h"
+
+namespace smx {
+
+namespace {
+
+__device__ __forceinline__ int wrapi(int c, int n) { return c < 0 ? c + n : (c >= n ? c - n : c); }
+
+}  // namespace
+
+// ---- cell list ----
+__global__ void k_cell_assign(const double* __restrict__ pos, int N, double3 box, int3 nc, int* __restrict__ cell,
+                              int* __restrict__ cell_count) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= N) return;
+  double p[3] = {pos[3 * a], pos[3 * a + 1], pos[3 * a + 2]};
+  const double L[3] = {box.x, box.y, box.z};
+  const int n[3] = {nc.x, nc.y, nc.z};
+  int c[3];
+  for (int d = 0; d < 3; ++d) {
+    double f = p[d] / L[d];
+    f -= floor(f);
+    int q = static_cast<int>(f * n[d]);
+    c[d] = q < 0 ? 0 : (q >= n[d] ? n[d] - 1 : q);
+  }
+  const int id = (c[0] * n[1] + c[1]) * n[2] + c[2];
+  cell[a] = id;
+  atomicAdd(cell_count + id, 1);
+}
+
+__global__ void k_cell_fill(const int* __restrict__ cell, int N, const int* __restrict__ cell_start,
+                            int* __restrict__ cell_fill, int* __restrict__ cell_atoms) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= N) return;
+  const int c = cell[a];
+  cell_atoms[cell_start[c] + atomicAdd(cell_fill + c, 1)] = a;
+}
+
+// one thread per cell: insertion sort of the cell's atoms by index (cells hold tens of atoms)
+__global__ void k_cell_sort(int ncell, const int* __restrict__ cell_start, int* __restrict__ cell_atoms) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncell) return;
+  const int b = cell_start[c], e = cell_start[c + 1];
+  for (int q = b + 1; q < e; ++q) {
+    const int v = cell_atoms[q];
+    int w = q - 1;
+    while (w >= b && cell_atoms[w] > v) {
+      cell_atoms[w + 1] = cell_atoms[w];
+      --w;
+    }
+    cell_atoms[w + 1] = v;
+  }
+}
+
+// Pass 0 counts, pass 1 fills.  Periodic images enter through the integer shift
+// (sx, sy, sz) in box lengths; the list holds pairs with r < rl, excluding i itself.
+template <bool FILL>
+__global__ void k_neigh_cells(const double* __restrict__ pos, const int* __restrict__ species, int N, double3 box,
+                              int3 nc, int3 periodic, double rl2, const int* __restrict__ cell,
+                              const int* __restrict__ cell_start, const int* __restrict__ cell_atoms,
+                              int* __restrict__ num_neigh, const int* __restrict__ first, int* __restrict__ nidx,
+                              int* __restrict__ ntype_e, int* __restrict__ edge_i, char4* __restrict__ shift,
+                              long cap) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const double xi = pos[3 * i], yi = pos[3 * i + 1], zi = pos[3 * i + 2];
+  const int ci = cell[i];
+  const int cz = ci % nc.z, cy = (ci / nc.z) % nc.y, cx = ci / (nc.z * nc.y);
+  int count = 0;
+  long slot = FILL ? first[i] : 0;
+  for (int dx = -1; dx <= 1; ++dx) {
+    int qx = cx + dx, sx = 0;
+    if (qx < 0) { if (!periodic.x) continue; qx += nc.x; sx = -1; }
+    if (qx >= nc.x) { if (!periodic.x) continue; qx -= nc.x; sx = 1; }
+    for (int dy = -1; dy <= 1; ++dy) {
+      int qy = cy + dy, sy = 0;
+      if (qy < 0) { if (!periodic.y) continue; qy += nc.y; sy = -1; }
+      if (qy >= nc.y) { if (!periodic.y) continue; qy -= nc.y; sy = 1; }
+      for (int dz = -1; dz <= 1; ++dz) {
+        int qz = cz + dz, sz = 0;
+        if (qz < 0) { if (!periodic.z) continue; qz += nc.z; sz = -1; }
+        if (qz >= nc.z) { if (!periodic.z) continue; qz -= nc.z; sz = 1; }
+        const int q = (qx * nc.y + qy) * nc.z + qz;
+        const double ox = sx * box.x, oy = sy * box.y, oz = sz * box.z;
+        for (int w = cell_start[q]; w < cell_start[q + 1]; ++w) {
+          const int j = cell_atoms[w];
+          if (j == i && sx == 0 && sy == 0 && sz == 0) continue;
+          const double ddx = pos[3 * j] + ox - xi, ddy = pos[3 * j + 1] + oy - yi, ddz = pos[3 * j + 2] + oz - zi;
+          if (ddx * ddx + ddy * ddy + ddz * ddz < rl2) {
+            if (FILL) {
+              if (slot < cap) {
+                nidx[slot] = j;
+                ntype_e[slot] = species[j];
+                edge_i[slot] = i;
+                shift[slot] = make_char4(sx, sy, sz, 0);
+              }
+              ++slot;
+            } else {
+              ++count;
+            }
+          }
+        }
+      }
+    }
+  }
+  if (!FILL) num_neigh[i] = count;
+}
+
+// Small or non-periodic systems: all pairs over the periodic images in range.
+template <bool FILL>
+__global__ void k_neigh_brute(const double* __restrict__ pos, const int* __restrict__ species, int N, double3 box,
+                              int3 nimg, double rl2, int* __restrict__ num_neigh, const int* __restrict__ first,
+                              int* __restrict__ nidx, int* __restrict__ ntype_e, int* __restrict__ edge_i,
+                              char4* __restrict__ shift, long cap) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const double xi = pos[3 * i], yi = pos[3 * i + 1], zi = pos[3 * i + 2];
+  int count = 0;
+  long slot = FILL ? first[i] : 0;
+  for (int j = 0; j < N; ++j)
+    for (int sx = -nimg.x; sx <= nimg.x; ++sx)
+      for (int sy = -nimg.y; sy <= nimg.y; ++sy)
+        for (int sz = -nimg.z; sz <= nimg.z; ++sz) {
+          if (j == i && sx == 0 && sy == 0 && sz == 0) continue;
+          const double ddx = pos[3 * j] + sx * box.x - xi, ddy = pos[3 * j + 1] + sy * box.y - yi,
+                       ddz = pos[3 * j + 2] + sz * box.z - zi;
+          if (ddx * ddx + ddy * ddy + ddz * ddz < rl2) {
+            if (FILL) {
+              if (slot < cap) {
+                nidx[slot] = j;
+                ntype_e[slot] = species[j];
+                edge_i[slot] = i;
+                shift[slot] = make_char4(sx, sy, sz, 0);
+              }
+              ++slot;
+            } else {
+              ++count;
+            }
+          }
+        }
+  if (!FILL) num_neigh[i] = count;
+}
+
+// Wrap positions into the periodic box (done before each neighbour build; positions
+// then move continuously until the next build, so stored image shifts stay valid).
+__global__ void k_wrap(int N, double3 box, int3 periodic, double* __restrict__ pos) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= N) return;
+  const double L[3] = {box.x, box.y, box.z};
+  const int per[3] = {periodic.x, periodic.y, periodic.z};
+  for (int d = 0; d < 3; ++d)
+    if (per[d]) pos[3 * a + d] -= L[d] * floor(pos[3 * a + d] / L[d]);
+}
+
+// rev[e] = index of the reverse edge (j -> i, -shift) of e = (i -> j, shift); -1 if absent.
+// The edge count is read from first[N] on the device, so launches do not depend on it.
+__global__ void k_reverse_edges(long cap, int N, const int* __restrict__ first, const int* __restrict__ nidx,
+                                const int* __restrict__ edge_i, const char4* __restrict__ shift, int* __restrict__ rev) {
+  const long e = static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  const long E = first[N] < cap ? first[N] : cap;
+  if (e >= E) return;
+  const int i = edge_i[e], j = nidx[e];
+  const char4 s = shift[e];
+  int found = -1;
+  for (int w = first[j]; w < first[j + 1]; ++w) {
+    const char4 t = shift[w];
+    if (nidx[w] == i && t.x == -s.x && t.y == -s.y && t.z == -s.z) {
+      found = w;
+      break;
+    }
+  }
+  rev[e] = found;
+}
+
+// xyz_e = x_j + shift_e * box - x_i, r_e = |xyz_e|
+__global__ void k_edge_geometry(long cap, int N, const int* __restrict__ first, const double* __restrict__ pos,
+                                double3 box, const int* __restrict__ nidx, const int* __restrict__ edge_i,
+                                const char4* __restrict__ shift, double* __restrict__ xyz, double* __restrict__ r) {
+  const long e = static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  const long E = first[N] < cap ? first[N] : cap;
+  if (e >= E) return;
+  const int i = edge_i[e], j = nidx[e];
+  const char4 s = shift[e];
+  const double dx = pos[3 * j] + s.x * box.x - pos[3 * i];
+  const double dy = pos[3 * j + 1] + s.y * box.y - pos[3 * i + 1];
+  const double dz = pos[3 * j + 2] + s.z * box.z - pos[3 * i + 2];
+  xyz[3 * e] = dx;
+  xyz[3 * e + 1] = dy;
+  xyz[3 * e + 2] = dz;
+  r[e] = sqrt(dx * dx + dy * dy + dz * dz);
+}
+
+// F_a = sum_{e in out(a)} (f[rev e] - f[e]); one thread per atom, no atomics
+__global__ void k_atom_forces(int N, const int* __restrict__ first, const int* __restrict__ rev,
+                              const double* __restrict__ f, double* __restrict__ F) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= N) return;
+  double s[3] = {0.0, 0.0, 0.0};
+  for (int e = first[a]; e < first[a + 1]; ++e) {
+    const int q = rev[e];
+    for (int c = 0; c < 3; ++c) s[c] += (q >= 0 ? f[3 * static_cast<long>(q) + c] : 0.0) - f[3 * static_cast<long>(e) + c];
+  }
+  for (int c = 0; c < 3; ++c) F[3 * a + c] = s[c];
+}
+
+// Deterministic float64 reduction of the energy (slot 0) and the 9 virial
+// components W_ab = sum_e xyz_e,a f_e,b (slots 1..9): per-block partials, then one
+// block sums the partials in a fixed order.
+__global__ void k_reduce_partials(int N, const int* __restrict__ first, const double* __restrict__ energies,
+                                  const double* __restrict__ xyz, const double* __restrict__ f,
+                                  double* __restrict__ partial) {
+  __shared__ double sh[10][256];
+  const long E = first[N];
+  double acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  const long stride = static_cast<long>(gridDim.x) * blockDim.x;
+  for (long e = static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x; e < E; e += stride)
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) acc[1 + 3 * a + b] += xyz[3 * e + a] * f[3 * e + b];
+  for (long i = static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x; i < N; i += stride) acc[0] += energies[i];
+  for (int q = 0; q < 10; ++q) sh[q][threadIdx.x] = acc[q];
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w)
+      for (int q = 0; q < 10; ++q) sh[q][threadIdx.x] += sh[q][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x < 10) partial[blockIdx.x * 10 + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+__global__ void k_reduce_final(int nblocks, const double* __restrict__ partial, double* __restrict__ out) {
+  if (threadIdx.x < 10) {
+    double s = 0.0;
+    for (int b = 0; b < nblocks; ++b) s += partial[b * 10 + threadIdx.x];
+    out[threadIdx.x] = s;
+  }
+}
+
+// velocity Verlet halves (positions A, velocities A/fs, forces eV/A, masses amu, dt fs)
+constexpr double kAccel = 9.648533212331e-3;  // (eV/A)/amu in A/fs^2
+
+__global__ void k_vv_first(int N, double dt, const double* __restrict__ F, const double* __restrict__ inv_m,
+                           double* __restrict__ v, double* __restrict__ x) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= N) return;
+  const double h = 0.5 * dt * kAccel * inv_m[a];
+  for (int c = 0; c < 3; ++c) {
+    v[3 * a + c] += h * F[3 * a + c];
+    x[3 * a + c] += dt * v[3 * a + c];
+  }
+}
+
+__global__ void k_vv_second(int N, double dt, const double* __restrict__ F, const double* __restrict__ inv_m,
+                            double* __restrict__ v) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= N) return;
+  const double h = 0.5 * dt * kAccel * inv_m[a];
+  for (int c = 0; c < 3; ++c) v[3 * a + c] += h * F[3 * a + c];
+}
+
+// ---- launchers ----
+void launch_cell_list(const double* pos, int N, double3 box, int3 nc, int* cell, int* cell_count, int* cell_start,
+                      int* cell_fill, int* cell_atoms, cudaStream_t s) {
+  const int ncell = nc.x * nc.y * nc.z;
+  cudaMemsetAsync(cell_count, 0, sizeof(int) * ncell, s);
+  cudaMemsetAsync(cell_fill, 0, sizeof(int) * ncell, s);
+  k_cell_assign<<<ceil_div(N, 256), 256, 0, s>>>(pos, N, box, nc, cell, cell_count);
+  launch_scan_first(cell_count, ncell, cell_start, s);
+  k_cell_fill<<<ceil_div(N, 256), 256, 0, s>>>(cell, N, cell_start, cell_fill, cell_atoms);
+  k_cell_sort<<<ceil_div(ncell, 128), 128, 0, s>>>(ncell, cell_start, cell_atoms);
+}
+
+void launch_neigh_pass(bool fill, bool brute, const double* pos, const int* species, int N, double3 box, int3 nc,
+                       int3 periodic, int3 nimg, double rl, const int* cell, const int* cell_start,
+                       const int* cell_atoms, int* num_neigh, const int* first, int* nidx, int* ntype_e, int* edge_i,
+                       char4* shift, long cap, cudaStream_t s) {
+  const double rl2 = rl * rl;
+  const int g = ceil_div(N, 128);
+  if (brute) {
+    if (fill)
+      k_neigh_brute<true><<<g, 128, 0, s>>>(pos, species, N, box, nimg, rl2, num_neigh, first, nidx, ntype_e, edge_i,
+                                            shift, cap);
+    else
+      k_neigh_brute<false><<<g, 128, 0, s>>>(pos, species, N, box, nimg, rl2, num_neigh, first, nidx, ntype_e,
+                                             edge_i, shift, cap);
+  } else {
+    if (fill)
+      k_neigh_cells<true><<<g, 128, 0, s>>>(pos, species, N, box, nc, periodic, rl2, cell, cell_start, cell_atoms,
+                                            num_neigh, first, nidx, ntype_e, edge_i, shift, cap);
+    else
+      k_neigh_cells<false><<<g, 128, 0, s>>>(pos, species, N, box, nc, periodic, rl2, cell, cell_start, cell_atoms,
+                                             num_neigh, first, nidx, ntype_e, edge_i, shift, cap);
+  }
+}
+
+void launch_wrap(int N, double3 box, int3 periodic, double* pos, cudaStream_t s) {
+  if (N > 0) k_wrap<<<ceil_div(N, 128), 128, 0, s>>>(N, box, periodic, pos);
+}
+
+void launch_reverse_edges(long cap, int N, const int* first, const int* nidx, const int* edge_i, const char4* shift,
+                          int* rev, cudaStream_t s) {
+  if (cap > 0) k_reverse_edges<<<ceil_div(cap, 256), 256, 0, s>>>(cap, N, first, nidx, edge_i, shift, rev);
+}
+
+void launch_edge_geometry(long cap, int N, const int* first, const double* pos, double3 box, const int* nidx,
+                          const int* edge_i, const char4* shift, double* xyz, double* r, cudaStream_t s) {
+  if (cap > 0) k_edge_geometry<<<ceil_div(cap, 256), 256, 0, s>>>(cap, N, first, pos, box, nidx, edge_i, shift, xyz, r);
+}
+
+void launch_atom_forces(int N, const int* first, const int* rev, const double* f, double* F, cudaStream_t s) {
+  if (N > 0) k_atom_forces<<<ceil_div(N, 128), 128, 0, s>>>(N, first, rev, f, F);
+}
+
+void launch_reduce(int N, const int* first, const double* energies, const double* xyz, const double* f,
+                   double* partial, int nblocks, double* out, cudaStream_t s) {
+  k_reduce_partials<<<nblocks, 256, 0, s>>>(N, first, energies, xyz, f, partial);
+  k_reduce_final<<<1, 32, 0, s>>>(nblocks, partial, out);
+}
+
+void launch_vv_first(int N, double dt, const double* F, const double* inv_m, double* v, double* x, cudaStream_t s) {
+  if (N > 0) k_vv_first<<<ceil_div(N, 128), 128, 0, s>>>(N, dt, F, inv_m, v, x);
+}
+
+void launch_vv_second(int N, double dt, const double* F, const double* inv_m, double* v, cudaStream_t s) {
+  if (N > 0) k_vv_second<<<ceil_div(N, 128), 128, 0, s>>>(N, dt, F, inv_m, v);
+}
+
+}  // namespace smx

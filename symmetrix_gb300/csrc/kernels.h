@@ -8,11 +8,12 @@
 namespace smx {
 
 // k_edge.cu
+cudaError_t init_edge_kernels(const DevModel& m);
 void launch_layer0_fwd(const DevModel& m, const EdgeIn& in, float* A0, float* M0, cudaStream_t s);
 void launch_layer1_fwd(const DevModel& m, const EdgeIn& in, const float* H1, float* Phi1, cudaStream_t s);
 void launch_layer1_rev(const DevModel& m, const EdgeIn& in, const float* H1, const float* dPhi1, float* H1_adj,
-                       float* f1, cudaStream_t s);
-void launch_layer0_rev(const DevModel& m, const EdgeIn& in, const float* A0, const float* M0_adj, const float* f1,
+                       double* f1, cudaStream_t s);
+void launch_layer0_rev(const DevModel& m, const EdgeIn& in, const float* A0, const float* M0_adj, const double* f1,
                        float* A0_adj, double* forces, cudaStream_t s);
 
 // k_node.cu
@@ -40,5 +41,23 @@ void launch_node_tail(const DevModel& m, const int* node_type, int N, const floa
                       float* H2, float* A1_adj, float* H1_adj, float* M1_adj, float* H2_adj, double* energies,
                       cudaStream_t s);
 void launch_scan_first(const int* num_neigh, int N, int* first, cudaStream_t s);
+
+// k_md.cu
+void launch_wrap(int N, double3 box, int3 periodic, double* pos, cudaStream_t s);
+void launch_cell_list(const double* pos, int N, double3 box, int3 nc, int* cell, int* cell_count, int* cell_start,
+                      int* cell_fill, int* cell_atoms, cudaStream_t s);
+void launch_neigh_pass(bool fill, bool brute, const double* pos, const int* species, int N, double3 box, int3 nc,
+                       int3 periodic, int3 nimg, double rl, const int* cell, const int* cell_start,
+                       const int* cell_atoms, int* num_neigh, const int* first, int* nidx, int* ntype_e, int* edge_i,
+                       char4* shift, long cap, cudaStream_t s);
+void launch_reverse_edges(long cap, int N, const int* first, const int* nidx, const int* edge_i, const char4* shift,
+                          int* rev, cudaStream_t s);
+void launch_edge_geometry(long cap, int N, const int* first, const double* pos, double3 box, const int* nidx,
+                          const int* edge_i, const char4* shift, double* xyz, double* r, cudaStream_t s);
+void launch_atom_forces(int N, const int* first, const int* rev, const double* f, double* F, cudaStream_t s);
+void launch_reduce(int N, const int* first, const double* energies, const double* xyz, const double* f,
+                   double* partial, int nblocks, double* out, cudaStream_t s);
+void launch_vv_first(int N, double dt, const double* F, const double* inv_m, double* v, double* x, cudaStream_t s);
+void launch_vv_second(int N, double dt, const double* F, const double* inv_m, double* v, cudaStream_t s);
 
 }  // namespace smx

@@ -1,0 +1,378 @@
+// Atom-level evaluation and the velocity-Verlet MD driver (C ABI in include/smx_gb300.h).
+//
+// These are the GPU-resident counterparts of what the reference's callers do
+// around MACE::compute_node_energies_forces: build the neighbour list, call the
+// evaluator, scatter per-edge forces to atoms and reduce the virial
+// (pair_symmetrix/pair_symmetrix_mace.cpp:242-372; symmetrix_calc.py:72-102), and,
+// for MD, LAMMPS's `fix nve` (the reference's tests run it in
+// pair_symmetrix/test/test_pair_symmetrix_mace.py:253).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "engine.hpp"
+
+using smx::fail;
+
+namespace {
+
+// Full directed neighbour list on the device with a skin, CSR by centre atom.
+struct NeighList {
+  int capN = 0, ncell_cap = 0;
+  long capE = 0;
+  int *cell = nullptr, *cell_count = nullptr, *cell_start = nullptr, *cell_fill = nullptr, *cell_atoms = nullptr;
+  int *num_neigh = nullptr, *first = nullptr, *nidx = nullptr, *ntype_e = nullptr, *edge_i = nullptr, *rev = nullptr;
+  char4* shift = nullptr;
+  double *xyz = nullptr, *r = nullptr, *forces = nullptr;
+  long E = 0;
+  bool realloc_happened = false;
+
+  ~NeighList() { release(); }
+  void release() {
+    void* ps[] = {cell, cell_count, cell_start, cell_fill, cell_atoms, num_neigh, first, nidx, ntype_e, edge_i, rev,
+                  shift, xyz, r, forces};
+    for (void* p : ps)
+      if (p) cudaFree(p);
+    cell = cell_count = cell_start = cell_fill = cell_atoms = num_neigh = first = nidx = ntype_e = edge_i = rev = nullptr;
+    shift = nullptr;
+    xyz = r = forces = nullptr;
+    capN = ncell_cap = 0;
+    capE = 0;
+  }
+  void reserve_nodes(int N, int ncell) {
+    if (N > capN) {
+      for (int** p : {&cell, &num_neigh, &first})
+        if (*p) cudaFree(*p);
+      cell = dalloc<int>(N);
+      num_neigh = dalloc<int>(N);
+      first = dalloc<int>(N + 1);
+      capN = N;
+      realloc_happened = true;
+    }
+    if (ncell + 1 > ncell_cap) {
+      for (int** p : {&cell_count, &cell_start, &cell_fill})
+        if (*p) cudaFree(*p);
+      cell_count = dalloc<int>(ncell + 1);
+      cell_start = dalloc<int>(ncell + 2);
+      cell_fill = dalloc<int>(ncell + 1);
+      ncell_cap = ncell + 1;
+    }
+    if (!cell_atoms) cell_atoms = dalloc<int>(N);
+  }
+  void reserve_edges(long E_) {
+    if (E_ <= capE) return;
+    const long nE = static_cast<long>(E_ * 1.25) + 1024;
+    void* ps[] = {nidx, ntype_e, edge_i, rev, shift, xyz, r, forces};
+    for (void* p : ps)
+      if (p) cudaFree(p);
+    nidx = dalloc<int>(nE);
+    ntype_e = dalloc<int>(nE);
+    edge_i = dalloc<int>(nE);
+    rev = dalloc<int>(nE);
+    shift = dalloc<char4>(nE);
+    xyz = dalloc<double>(3 * nE);
+    r = dalloc<double>(nE);
+    forces = dalloc<double>(3 * nE);
+    capE = nE;
+    realloc_happened = true;
+  }
+
+  // Build the list for positions pos (wrapped in place for periodic axes).
+  void build(double* pos, const int* species, int N, double3 box, int3 periodic, double rl, cudaStream_t s) {
+    const double L[3] = {box.x, box.y, box.z};
+    const int per[3] = {periodic.x, periodic.y, periodic.z};
+    int n[3];
+    bool brute = false;
+    int3 nimg = make_int3(0, 0, 0);
+    int* img[3] = {&nimg.x, &nimg.y, &nimg.z};
+    for (int d = 0; d < 3; ++d) {
+      if (!per[d]) {
+        brute = true;
+        n[d] = 1;
+        continue;
+      }
+      n[d] = static_cast<int>(std::floor(L[d] / rl));
+      *img[d] = static_cast<int>(std::ceil(rl / L[d]));
+      if (n[d] < 3) brute = true;
+    }
+    if (brute && N > 200000)
+      throw std::invalid_argument("non-periodic or small-box neighbour search is limited to 200000 atoms");
+    const int3 nc = make_int3(n[0], n[1], n[2]);
+    reserve_nodes(N, nc.x * nc.y * nc.z);
+    smx::launch_wrap(N, box, periodic, pos, s);
+    if (!brute)
+      smx::launch_cell_list(pos, N, box, nc, cell, cell_count, cell_start, cell_fill, cell_atoms, s);
+    smx::launch_neigh_pass(false, brute, pos, species, N, box, nc, periodic, nimg, rl, cell, cell_start, cell_atoms,
+                           num_neigh, first, nidx, ntype_e, edge_i, shift, capE, s);
+    smx::launch_scan_first(num_neigh, N, first, s);
+    int total = 0;
+    check(cudaMemcpyAsync(&total, first + N, sizeof(int), cudaMemcpyDeviceToHost, s), "D2H");
+    check(cudaStreamSynchronize(s), "neighbour count");
+    E = total;
+    reserve_edges(E);
+    smx::launch_neigh_pass(true, brute, pos, species, N, box, nc, periodic, nimg, rl, cell, cell_start, cell_atoms,
+                           num_neigh, first, nidx, ntype_e, edge_i, shift, capE, s);
+    smx::launch_reverse_edges(capE, N, first, nidx, edge_i, shift, rev, s);
+  }
+};
+
+void box_args(const double* box_lengths, double3& box, int3& periodic) {
+  if (box_lengths) {
+    box = make_double3(box_lengths[0], box_lengths[1], box_lengths[2]);
+    periodic = make_int3(1, 1, 1);
+    if (!(box.x > 0 && box.y > 0 && box.z > 0)) throw std::invalid_argument("box lengths must be positive");
+  } else {
+    box = make_double3(1.0, 1.0, 1.0);
+    periodic = make_int3(0, 0, 0);
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// MD driver
+// ---------------------------------------------------------------------------
+struct smx_md {
+  smx_engine* eng = nullptr;
+  int N = 0;
+  double3 box{};
+  int3 periodic{};
+  double dt = 0.5, skin = 1.0;
+  int rebuild_every = 10;
+  long step = 0;
+  double *pos = nullptr, *vel = nullptr, *F = nullptr, *inv_m = nullptr, *energies = nullptr, *partial = nullptr,
+         *reduced = nullptr;
+  int* species = nullptr;
+  NeighList nl;
+  cudaGraphExec_t graph = nullptr;
+  int graph_steps = 0;
+  static constexpr int kReduceBlocks = 64;
+
+  ~smx_md() {
+    if (graph) cudaGraphExecDestroy(graph);
+    void* ps[] = {pos, vel, F, inv_m, energies, partial, reduced, species};
+    for (void* p : ps)
+      if (p) cudaFree(p);
+  }
+
+  smx::EdgeIn edges() const {
+    return smx::EdgeIn{nl.first, species, nl.nidx, nl.ntype_e, nl.xyz, nl.r, N};
+  }
+
+  // forces at the current positions (geometry + evaluator + scatter); graph-capturable
+  void forces(cudaStream_t s) {
+    smx::launch_edge_geometry(nl.capE, N, nl.first, pos, box, nl.nidx, nl.edge_i, nl.shift, nl.xyz, nl.r, s);
+    eng->run(edges(), energies, nl.forces, s);
+    smx::launch_atom_forces(N, nl.first, nl.rev, nl.forces, F, s);
+  }
+
+  void one_step(cudaStream_t s) {
+    smx::launch_vv_first(N, dt, F, inv_m, vel, pos, s);
+    forces(s);
+    smx::launch_vv_second(N, dt, F, inv_m, vel, s);
+  }
+
+  void rebuild(cudaStream_t s) {
+    nl.realloc_happened = false;
+    nl.build(pos, species, N, box, periodic, eng->hm.r_cut + skin, s);
+    eng->reserve(N, nl.capE);
+    if (nl.realloc_happened && graph) {
+      cudaGraphExecDestroy(graph);
+      graph = nullptr;
+    }
+  }
+
+  void run(int steps) {
+    cudaStream_t s = eng->stream;
+    const bool prof = eng->profile;
+    eng->profile = false;
+    while (steps > 0) {
+      if (step % rebuild_every == 0) rebuild(s);
+      const int seg = std::min<long>(steps, rebuild_every - step % rebuild_every);
+      if (seg == rebuild_every) {
+        if (!graph || graph_steps != seg) {
+          if (graph) cudaGraphExecDestroy(graph);
+          graph = nullptr;
+          cudaGraph_t g;
+          check(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+          for (int q = 0; q < seg; ++q) one_step(s);
+          check(cudaStreamEndCapture(s, &g), "cudaStreamEndCapture");
+          check(cudaGraphInstantiate(&graph, g, 0), "cudaGraphInstantiate");
+          cudaGraphDestroy(g);
+          graph_steps = seg;
+        }
+        check(cudaGraphLaunch(graph, s), "cudaGraphLaunch");
+      } else {
+        for (int q = 0; q < seg; ++q) one_step(s);
+      }
+      step += seg;
+      steps -= seg;
+    }
+    check(cudaGetLastError(), "MD launch");
+    eng->profile = prof;
+  }
+};
+
+extern "C" {
+
+int smx_compute_atoms(smx_engine* eng, int n_atoms, const double* positions, const int* species,
+                      const double* box_lengths, double* energy, double* node_energies, double* forces,
+                      double* virial) {
+  if (!eng) return fail(SMX_ERR_INVALID, "engine is NULL");
+  if (n_atoms < 0 || (n_atoms > 0 && (!positions || !species || !forces)))
+    return fail(SMX_ERR_INVALID, "bad atom arrays");
+  for (int a = 0; a < n_atoms; ++a)
+    if (species[a] < 0 || species[a] >= eng->hm.S) return fail(SMX_ERR_INVALID, "species out of range");
+  try {
+    check(cudaSetDevice(eng->device), "cudaSetDevice");
+    double3 box;
+    int3 periodic;
+    box_args(box_lengths, box, periodic);
+    smx_md md;  // borrowed as a workspace: no dynamics
+    md.eng = eng;
+    md.N = n_atoms;
+    md.box = box;
+    md.periodic = periodic;
+    md.skin = 0.0;
+    cudaStream_t s = eng->stream;
+    if (n_atoms == 0) {
+      if (energy) *energy = 0.0;
+      if (virial) std::memset(virial, 0, 9 * sizeof(double));
+      return SMX_OK;
+    }
+    md.pos = dalloc<double>(3 * n_atoms);
+    md.F = dalloc<double>(3 * n_atoms);
+    md.energies = dalloc<double>(n_atoms);
+    md.species = dalloc<int>(n_atoms);
+    md.partial = dalloc<double>(10 * smx_md::kReduceBlocks);
+    md.reduced = dalloc<double>(10);
+    check(cudaMemcpyAsync(md.pos, positions, sizeof(double) * 3 * n_atoms, cudaMemcpyHostToDevice, s), "H2D");
+    check(cudaMemcpyAsync(md.species, species, sizeof(int) * n_atoms, cudaMemcpyHostToDevice, s), "H2D");
+    md.rebuild(s);
+    md.forces(s);
+    smx::launch_reduce(n_atoms, md.nl.first, md.energies, md.nl.xyz, md.nl.forces, md.partial, smx_md::kReduceBlocks,
+                       md.reduced, s);
+    double red[10];
+    check(cudaMemcpyAsync(red, md.reduced, sizeof(red), cudaMemcpyDeviceToHost, s), "D2H");
+    check(cudaMemcpyAsync(forces, md.F, sizeof(double) * 3 * n_atoms, cudaMemcpyDeviceToHost, s), "D2H");
+    if (node_energies)
+      check(cudaMemcpyAsync(node_energies, md.energies, sizeof(double) * n_atoms, cudaMemcpyDeviceToHost, s), "D2H");
+    check(cudaStreamSynchronize(s), "evaluation");
+    if (energy) *energy = red[0];
+    if (virial)
+      for (int q = 0; q < 9; ++q) virial[q] = red[1 + q];
+  } catch (const CudaError& e) {
+    return fail(SMX_ERR_CUDA, e.what());
+  } catch (const std::exception& e) {
+    return fail(SMX_ERR_INVALID, e.what());
+  }
+  return SMX_OK;
+}
+
+smx_md* smx_md_create(smx_engine* eng, int n_atoms, const double* positions, const double* velocities,
+                      const int* species, const double* masses, const double* box_lengths, double dt_fs, double skin,
+                      int rebuild_every) {
+  if (!eng || n_atoms <= 0 || !positions || !species || !masses || rebuild_every < 1 || !(dt_fs > 0) ||
+      !(skin >= 0)) {
+    fail(SMX_ERR_INVALID, "bad MD arguments");
+    return nullptr;
+  }
+  for (int a = 0; a < n_atoms; ++a)
+    if (species[a] < 0 || species[a] >= eng->hm.S || !(masses[a] > 0)) {
+      fail(SMX_ERR_INVALID, "species out of range or non-positive mass");
+      return nullptr;
+    }
+  auto md = std::make_unique<smx_md>();
+  try {
+    check(cudaSetDevice(eng->device), "cudaSetDevice");
+    box_args(box_lengths, md->box, md->periodic);
+    md->eng = eng;
+    md->N = n_atoms;
+    md->dt = dt_fs;
+    md->skin = skin;
+    md->rebuild_every = rebuild_every;
+    cudaStream_t s = eng->stream;
+    md->pos = dalloc<double>(3 * n_atoms);
+    md->vel = dalloc<double>(3 * n_atoms);
+    md->F = dalloc<double>(3 * n_atoms);
+    md->inv_m = dalloc<double>(n_atoms);
+    md->energies = dalloc<double>(n_atoms);
+    md->species = dalloc<int>(n_atoms);
+    md->partial = dalloc<double>(10 * smx_md::kReduceBlocks);
+    md->reduced = dalloc<double>(10);
+    std::vector<double> inv(n_atoms), v(3 * static_cast<size_t>(n_atoms), 0.0);
+    for (int a = 0; a < n_atoms; ++a) inv[a] = 1.0 / masses[a];
+    if (velocities) std::memcpy(v.data(), velocities, sizeof(double) * 3 * n_atoms);
+    check(cudaMemcpyAsync(md->pos, positions, sizeof(double) * 3 * n_atoms, cudaMemcpyHostToDevice, s), "H2D");
+    check(cudaMemcpyAsync(md->vel, v.data(), sizeof(double) * 3 * n_atoms, cudaMemcpyHostToDevice, s), "H2D");
+    check(cudaMemcpyAsync(md->inv_m, inv.data(), sizeof(double) * n_atoms, cudaMemcpyHostToDevice, s), "H2D");
+    check(cudaMemcpyAsync(md->species, species, sizeof(int) * n_atoms, cudaMemcpyHostToDevice, s), "H2D");
+    md->rebuild(s);
+    md->forces(s);
+    check(cudaStreamSynchronize(s), "initial forces");
+  } catch (const CudaError& e) {
+    fail(SMX_ERR_CUDA, e.what());
+    return nullptr;
+  } catch (const std::exception& e) {
+    fail(SMX_ERR_INVALID, e.what());
+    return nullptr;
+  }
+  return md.release();
+}
+
+int smx_md_run(smx_md* md, int steps) {
+  if (!md || steps < 0) return fail(SMX_ERR_INVALID, "bad MD arguments");
+  try {
+    check(cudaSetDevice(md->eng->device), "cudaSetDevice");
+    md->run(steps);
+  } catch (const CudaError& e) {
+    return fail(SMX_ERR_CUDA, e.what());
+  } catch (const std::exception& e) {
+    return fail(SMX_ERR_INVALID, e.what());
+  }
+  return SMX_OK;
+}
+
+int smx_md_sync(smx_md* md) {
+  if (!md) return fail(SMX_ERR_INVALID, "md is NULL");
+  const cudaError_t e = cudaStreamSynchronize(md->eng->stream);
+  return e == cudaSuccess ? SMX_OK : fail(SMX_ERR_CUDA, cudaGetErrorString(e));
+}
+
+int smx_md_state(smx_md* md, double* positions, double* velocities, double* forces, double* potential_energy,
+                 double* virial, long* step) {
+  if (!md) return fail(SMX_ERR_INVALID, "md is NULL");
+  try {
+    cudaStream_t s = md->eng->stream;
+    const int N = md->N;
+    smx::launch_reduce(N, md->nl.first, md->energies, md->nl.xyz, md->nl.forces, md->partial, smx_md::kReduceBlocks,
+                       md->reduced, s);
+    double red[10];
+    check(cudaMemcpyAsync(red, md->reduced, sizeof(red), cudaMemcpyDeviceToHost, s), "D2H");
+    if (positions) check(cudaMemcpyAsync(positions, md->pos, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, s), "D2H");
+    if (velocities) check(cudaMemcpyAsync(velocities, md->vel, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, s), "D2H");
+    if (forces) check(cudaMemcpyAsync(forces, md->F, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, s), "D2H");
+    check(cudaStreamSynchronize(s), "MD state");
+    if (potential_energy) *potential_energy = red[0];
+    if (virial)
+      for (int q = 0; q < 9; ++q) virial[q] = red[1 + q];
+    if (step) *step = md->step;
+  } catch (const std::exception& e) {
+    return fail(SMX_ERR_CUDA, e.what());
+  }
+  return SMX_OK;
+}
+
+long smx_md_num_edges(smx_md* md) { return md ? md->nl.E : -1; }
+
+void smx_md_destroy(smx_md* md) {
+  if (!md) return;
+  cudaSetDevice(md->eng->device);
+  cudaStreamSynchronize(md->eng->stream);
+  delete md;
+}
+
+}  // extern "C"

@@ -80,6 +80,39 @@ class MACE:
             node_energies, node_forces, stream)
         _lib.raise_for(code, self._lib)
 
+    def compute_atoms(self, positions, species, box=None):
+        """Energy, node energies, atomic forces (n, 3) and virial (3, 3) of a structure.
+
+        Builds the neighbour list on the GPU (box = three orthorhombic lengths, or None
+        for a non-periodic system), like the reference's callers do around
+        compute_node_energies_forces (symmetrix_calc.py:72-102).
+        """
+        pos = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
+        n = len(pos)
+        sp = np.ascontiguousarray(species, dtype=np.int32)
+        if len(sp) != n:
+            raise ValueError("species and positions differ in length")
+        bx = None if box is None else np.ascontiguousarray(np.broadcast_to(box, 3), dtype=np.float64)
+        e = ctypes.c_double(0.0)
+        node_e = np.zeros(n)
+        forces = np.zeros((n, 3))
+        virial = np.zeros(9)
+        code = self._lib.smx_compute_atoms(self._h, n, _ptr(pos), _ptr(sp), _ptr(bx), ctypes.byref(e), _ptr(node_e),
+                                           _ptr(forces), _ptr(virial))
+        _lib.raise_for(code, self._lib)
+        return e.value, node_e, forces, virial.reshape(3, 3)
+
+    def set_option(self, key, value):
+        _lib.raise_for(self._lib.smx_set_option(self._h, key.encode(), int(value)), self._lib)
+
+    def stage_times(self):
+        """Per-stage device times (ms) of the last evaluation; needs set_option('profile', 1)."""
+        out = np.zeros(16)
+        n = self._lib.smx_stage_times(self._h, _ptr(out), 16)
+        if n < 0:
+            _lib.raise_for(-n, self._lib)
+        return dict(zip(_lib.STAGE_NAMES, out[:n]))
+
     def stage(self, name):
         n = self._lib.smx_get_stage(self._h, name.encode(), None, 0)
         if n < 0:

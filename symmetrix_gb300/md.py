@@ -1,0 +1,57 @@
+"""GPU-resident velocity-Verlet molecular dynamics over the engine (smx_md_* in the C ABI).
+
+Units: A, fs, amu, eV.  The neighbour list uses r_cut + skin and is rebuilt every
+`rebuild_every` steps; the steps in between run as one captured CUDA graph.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .mace import _ptr
+
+
+class MD:
+    def __init__(self, engine, positions, species, masses, box=None, velocities=None, dt=0.5, skin=1.0,
+                 rebuild_every=10):
+        self._lib = _lib.load()
+        self.engine = engine  # keeps the engine alive
+        pos = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
+        self.n = len(pos)
+        sp = np.ascontiguousarray(species, dtype=np.int32)
+        m = np.ascontiguousarray(masses, dtype=np.float64)
+        v = None if velocities is None else np.ascontiguousarray(velocities, dtype=np.float64).reshape(-1, 3)
+        bx = None if box is None else np.ascontiguousarray(np.broadcast_to(box, 3), dtype=np.float64)
+        h = self._lib.smx_md_create(engine._h, self.n, _ptr(pos), _ptr(v), _ptr(sp), _ptr(m), _ptr(bx), float(dt),
+                                    float(skin), int(rebuild_every))
+        if not h:
+            raise RuntimeError(self._lib.smx_last_error().decode(errors="replace"))
+        self._h = ctypes.c_void_p(h)
+
+    def run(self, steps):
+        _lib.raise_for(self._lib.smx_md_run(self._h, int(steps)), self._lib)
+
+    def sync(self):
+        _lib.raise_for(self._lib.smx_md_sync(self._h), self._lib)
+
+    def state(self):
+        pos = np.zeros((self.n, 3))
+        vel = np.zeros((self.n, 3))
+        f = np.zeros((self.n, 3))
+        e = ctypes.c_double(0.0)
+        w = np.zeros(9)
+        step = ctypes.c_long(0)
+        _lib.raise_for(self._lib.smx_md_state(self._h, _ptr(pos), _ptr(vel), _ptr(f), ctypes.byref(e), _ptr(w),
+                                              ctypes.byref(step)), self._lib)
+        return dict(positions=pos, velocities=vel, forces=f, potential_energy=e.value, virial=w.reshape(3, 3),
+                    step=step.value)
+
+    @property
+    def num_edges(self):
+        return self._lib.smx_md_num_edges(self._h)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            self._lib.smx_md_destroy(h)
+            self._h = None

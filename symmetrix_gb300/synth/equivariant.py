@@ -13,7 +13,7 @@ Neither e3nn nor mace-torch is available here, so both are derived from the
 mathematics in the evaluator's own Y_lm basis: a real CG tensor C^L_{l1 l2} is
 the one-dimensional invariant subspace of D_L (x) D_l1 (x) D_l2 (null space over
 random rotations), and the degree-nu equivariant polynomial maps R^16 -> V_L are
-spanned by the coupling trees ((x_l1 x_l2)_l12 x_l3)_L, orthonormalised by SVD.
+spanned by the coupling trees ((x_l1 x_l2)_l12 x_l3)_L, orthonormalised in order.
 Because everything is derived in the evaluator's basis, energies from a
 synthetic model are invariant under O(3) to round-off.
 """
@@ -125,9 +125,21 @@ def equivariant_polynomial_basis(L, degree, l_in_max=3):
     for c, p in enumerate(cands):
         for (M, key), val in p.items():
             A[c, M * len(keys) + idx[key]] = val
-    _, s, vt = np.linalg.svd(A, full_matrices=False)
-    rank = int(np.sum(s > 1e-9 * s[0]))
-    U = vt[:rank].reshape(rank, 2 * L + 1, len(keys))
+    # Ordered modified Gram-Schmidt (twice): unlike an SVD, the basis it returns
+    # depends only on the candidate order, so every platform builds the same model.
+    basis = []
+    # candidates that vanish identically (antisymmetric couplings of equal irreps) have
+    # round-off norms; the threshold is absolute on the scale of the largest candidate
+    tol = 1e-7 * np.linalg.norm(A, axis=1).max()
+    for v in A:
+        w = v.copy()
+        for _ in range(2):
+            for b in basis:
+                w -= (b @ w) * b
+        nw = np.linalg.norm(w)
+        if nw > tol:
+            basis.append(w / nw)
+    U = np.array(basis).reshape(len(basis), 2 * L + 1, len(keys))
     U[np.abs(U) < 1e-12] = 0.0
     used = np.nonzero(np.any(np.abs(U) > 0, axis=(0, 1)))[0]
     keys = [keys[i] for i in used]

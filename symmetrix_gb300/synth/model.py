@@ -70,7 +70,7 @@ def _spline_tables(r_knots, values):
 
 def make_model(num_channels=32, species=("H", "C", "O"), r_cut=5.0, L_max=1, correlation=3,
                num_bessel=8, envelope_p=5, num_knots=200, avg_num_neighbors=None, seed=0,
-               radial_hidden=(64, 64), l_max=3, a0_gain=7.0, a1_gain=12.0):
+               radial_hidden=(64, 64), l_max=3, a0_gain=7.0, a1_gain=12.0, energy_scale=0.35):
     """Return a dict in libsymmetrix's MACE JSON layout for a random two-layer MACE."""
     if l_max != 3:
         raise ValueError("the evaluator supports l_max = 3 only")
@@ -175,9 +175,11 @@ def make_model(num_channels=32, species=("H", "C", "O"), r_cut=5.0, L_max=1, cor
     # ----- H2 and readouts (extract_mace_data.py:476-519) -----
     out["H2_weights_for_H1"] = [(rng.normal(size=(C, C)) / np.sqrt(C)).flatten().tolist() for _ in range(S)]
     out["H2_weights_for_M1"] = (rng.normal(size=(C, C)) / np.sqrt(C)).flatten().tolist()
-    out["readout_1_weights"] = (rng.normal(size=C) / np.sqrt(C)).tolist()
+    # energy_scale plays the role of MACE's scale_shift.scale, which the extractor
+    # multiplies into both readouts (extract_mace_data.py:514, :520)
+    out["readout_1_weights"] = (energy_scale * rng.normal(size=C) / np.sqrt(C)).tolist()
     out["readout_2_weights_1"] = (rng.normal(size=(16, C)) / np.sqrt(C)).flatten().tolist()
-    out["readout_2_weights_2"] = (rng.normal(size=16) / 4.0).tolist()
+    out["readout_2_weights_2"] = (energy_scale * rng.normal(size=16) / 4.0).tolist()
     out["readout_2_scale_factor"] = 1.679
     return out
 

@@ -38,6 +38,17 @@ def small_model(path):
     return write_model(make_model(**CONFIGS["small"], seed=SMALL_SEED, avg_num_neighbors=SMALL_AVG_NEIGH), path)
 
 
+def model_fingerprint(path):
+    """A few sums over the model file: regenerating the model must reproduce them."""
+    with open(path) as f:
+        m = json.load(f)
+    return np.array([np.abs(np.asarray(m["radial_spline_values_1"])).sum(),
+                     sum(np.abs(np.asarray(v)).sum() for s in m["M0_weights"].values() for l in s.values()
+                         for v in l.values()),
+                     sum(np.abs(np.asarray(v)).sum() for s in m["M1_weights"].values() for v in s.values()),
+                     np.abs(np.asarray(m["A1_weights"][1])).sum(), np.abs(np.asarray(m["Phi1_clebsch_gordan"])).sum()])
+
+
 def tiny_cluster():
     pos = np.array([[0.0, -2.0, 0.0], [1.0, 0.0, 0.0], [0.0, 1.0, 0.0], [2.1, 1.3, -0.4],
                     [-1.2, 0.4, 1.1], [0.7, -0.6, 1.9], [3.2, -0.9, 0.8]])
@@ -77,7 +88,7 @@ def main():
     out = run_reference(small_path, 64, species, nl)
     np.savez_compressed(os.path.join(HERE, "small_golden.npz"), positions=pos, box=L, species=species,
                         num_neigh=nl["num_neigh"], neigh_indices=nl["neigh_indices"], xyz=nl["xyz"], r=nl["r"],
-                        edge_i=nl["i"], **out)
+                        edge_i=nl["i"], model_fingerprint=model_fingerprint(small_path), **out)
     print("wrote", tiny_path, "and goldens; small E =", out["node_energies"].sum())
 
 

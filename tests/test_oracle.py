@@ -44,6 +44,12 @@ def test_tiny_golden_matches_reference_outputs():
         assert ev.get(s).sum() == pytest.approx(g["sum_" + s], rel=1e-10, abs=1e-12), s
 
 
+def test_regenerated_model_matches_golden_fingerprint(small_model_path, small_golden):
+    """The seeded generator must rebuild the exact model the goldens were made with."""
+    from make_golden import model_fingerprint
+    np.testing.assert_allclose(model_fingerprint(small_model_path), small_golden["model_fingerprint"], rtol=1e-10)
+
+
 def test_small_golden_matches_reference_outputs(small_model_path, small_golden):
     g = small_golden
     species = g["species"].astype(np.int32)

@@ -64,17 +64,11 @@ __device__ __forceinline__ void stage_edges(const DevModel& m, const EdgeIn& in,
   }
 }
 
-__device__ __forceinline__ double warp_sum_d(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
-// Sum a per-thread 3-vector over the block's channels for edge t in float64 (the
-// channel sum of per-edge force terms cancels strongly): warp shuffles, then one
-// partial per warp into sF (reduced after the chunk).
-__device__ __forceinline__ void block_reduce3(float fx, float fy, float fz, double (*sF)[8][3], int t) {
-  const double x = warp_sum_d(fx), y = warp_sum_d(fy), z = warp_sum_d(fz);
+// Sum a per-thread 3-vector over the block's channels for edge t: float32 warp
+// shuffles (float64 arithmetic is slow on this part), then one partial per warp into
+// sF, summed across warps in float64 after the chunk.
+__device__ __forceinline__ void block_reduce3(float fx, float fy, float fz, float (*sF)[8][3], int t) {
+  const float x = warp_sum(fx), y = warp_sum(fy), z = warp_sum(fz);
   if ((threadIdx.x & 31) == 0) {
     const int w = threadIdx.x >> 5;
     sF[t][w][0] = x;
@@ -220,7 +214,7 @@ __global__ void __launch_bounds__(256) k_layer1_rev(DevModel m, EdgeIn in, const
   __shared__ float sx[kEdgeChunk];
   __shared__ int sbase[kEdgeChunk];
   __shared__ int sj[kEdgeChunk];
-  __shared__ double sF[kEdgeChunk][8][3];
+  __shared__ float sF[kEdgeChunk][8][3];
   const int C = m.C, k = threadIdx.x, i = blockIdx.x;
   const int nwarp = C >> 5;
   const int ti = in.node_type[i];
@@ -301,7 +295,7 @@ __global__ void __launch_bounds__(256) k_layer1_rev(DevModel m, EdgeIn in, const
     for (int t = threadIdx.x; t < ne; t += blockDim.x) {
       double s[3] = {0.0, 0.0, 0.0};
       for (int w = 0; w < nwarp; ++w)
-        for (int a = 0; a < 3; ++a) s[a] += sF[t][w][a];
+        for (int a = 0; a < 3; ++a) s[a] += static_cast<double>(sF[t][w][a]);
       for (int a = 0; a < 3; ++a) f1[3 * (static_cast<long>(eb) + t) + a] = s[a];
     }
   }
@@ -321,7 +315,7 @@ __global__ void __launch_bounds__(256) k_layer0_rev(DevModel m, EdgeIn in, const
   __shared__ float su[3][kEdgeChunk];
   __shared__ float sx[kEdgeChunk];
   __shared__ int sbase[kEdgeChunk];
-  __shared__ double sF[kEdgeChunk][8][3];
+  __shared__ float sF[kEdgeChunk][8][3];
   const int C = m.C, k = threadIdx.x, i = blockIdx.x;
   const int nwarp = C >> 5;
   const int ti = in.node_type[i];
@@ -394,7 +388,7 @@ __global__ void __launch_bounds__(256) k_layer0_rev(DevModel m, EdgeIn in, const
       const long e = static_cast<long>(eb) + t;
       double s[3] = {0.0, 0.0, 0.0};
       for (int w = 0; w < nwarp; ++w)
-        for (int a = 0; a < 3; ++a) s[a] += sF[t][w][a];
+        for (int a = 0; a < 3; ++a) s[a] += static_cast<double>(sF[t][w][a]);
       for (int a = 0; a < 3; ++a) forces[3 * e + a] = -(s[a] + f1[3 * e + a]);
     }
   }

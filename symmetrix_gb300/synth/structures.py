@@ -142,9 +142,9 @@ def neighbor_list(pos, cutoff, box=None):
 
 
 def maxwell_boltzmann(masses, T, rng):
-    """Velocities (A / internal time) at temperature T with zero net momentum."""
+    """Velocities in A/fs at temperature T (K) with zero net momentum (masses in amu)."""
     m = np.asarray(masses, dtype=np.float64)[:, None]
-    v = rng.normal(size=(len(m), 3)) * np.sqrt(KB_EV * T / m)
+    v = rng.normal(size=(len(m), 3)) * np.sqrt(KB_EV * T / m) / TIME_UNIT_FS
     v -= (m * v).sum(0) / m.sum()
     return v
 

@@ -32,7 +32,8 @@ def test_compute_atoms_matches_edge_api(engine_lib, small_model_path, n, density
     Fh = atomic_forces(n, nl["i"], nl["neigh_indices"], m.node_forces)
     Wh = virial(nl["xyz"], m.node_forces)
     assert abs(E - m.node_energies.sum()) < 1e-6 * n
-    np.testing.assert_allclose(node_e, m.node_energies, atol=1e-6)
+    # the GPU list orders a node's edges differently, so float32 sums differ by round-off
+    np.testing.assert_allclose(node_e, m.node_energies, atol=1e-5)
     np.testing.assert_allclose(F, Fh, atol=1e-5)
     np.testing.assert_allclose(W, Wh, atol=1e-4 * max(1.0, np.abs(Wh).max()))
     np.testing.assert_allclose(F.sum(0), 0.0, atol=1e-6)

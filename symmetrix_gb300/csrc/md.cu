@@ -137,6 +137,7 @@ void box_args(const double* box_lengths, double3& box, int3& periodic) {
 // ---------------------------------------------------------------------------
 struct smx_md {
   smx_engine* eng = nullptr;
+  int device = 0;  // kept here: destruction must not touch the engine, which may be gone
   int N = 0;
   double3 box{};
   int3 periodic{};
@@ -290,6 +291,7 @@ smx_md* smx_md_create(smx_engine* eng, int n_atoms, const double* positions, con
     check(cudaSetDevice(eng->device), "cudaSetDevice");
     box_args(box_lengths, md->box, md->periodic);
     md->eng = eng;
+    md->device = eng->device;
     md->N = n_atoms;
     md->dt = dt_fs;
     md->skin = skin;
@@ -370,8 +372,9 @@ long smx_md_num_edges(smx_md* md) { return md ? md->nl.E : -1; }
 
 void smx_md_destroy(smx_md* md) {
   if (!md) return;
-  cudaSetDevice(md->eng->device);
-  cudaStreamSynchronize(md->eng->stream);
+  // the engine (and its stream) may already be destroyed: wait on the device instead
+  cudaSetDevice(md->device);
+  cudaDeviceSynchronize();
   delete md;
 }
 

@@ -131,6 +131,25 @@ int smx_md_state(smx_md* md, double* positions, double* velocities, double* forc
 long smx_md_num_edges(smx_md* md);
 void smx_md_destroy(smx_md* md);
 
+/* Energy and virial of one evaluation, summed on the GPU without allocating anything.
+ * No counterpart in the reference: it serves callers that may not call cudaMalloc
+ * where they need the sum (device memory owned by another framework's pools, such as
+ * a Kokkos pair style, or a fixed memory budget).  All pointers are device memory of
+ * the current device: node_energies[num_nodes], xyz[3*num_edges],
+ * node_forces[3*num_edges] (as returned by smx_compute_node_energies_forces_device),
+ * out[10] = {sum of node energies, W_xx, W_xy, ..., W_zz} with W_ab = sum_e xyz_e,a f_e,b.
+ * Scratch is a fixed 1.25 MiB device array inside the library (one float64 partial per
+ * 4096 nodes/edges), so at most 67,108,864 nodes and edges are accepted; larger inputs
+ * return SMX_ERR_CAPACITY without launching.  The first call on each device looks up
+ * that array's device address; make it before any stream capture.  Every call on a
+ * device shares that array (it keeps the last call's partial sums; nothing in it needs
+ * to start at zero), so calls that overlap on the same GPU, e.g. on two streams, race:
+ * serialise them.  Enqueued on `stream`
+ * (a cudaStream_t, NULL = legacy default stream); returns without synchronising.
+ * Results are bitwise reproducible. */
+int smx_energy_virial_device_noalloc(int num_nodes, long num_edges, const double* node_energies, const double* xyz,
+                                     const double* node_forces, double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -41,6 +41,7 @@ SIGNATURES = [
     ("smx_md_state", _I, [_P, _P, _P, _P, _P, _P, _P]),
     ("smx_md_num_edges", _L, [_P]),
     ("smx_md_destroy", None, [_P]),
+    ("smx_energy_virial_device_noalloc", _I, [_I, _L, _P, _P, _P, _P, _P]),
 ]
 
 STAGE_NAMES = ("layer0_fwd", "gemm_H1", "layer1_fwd", "gemm_A1", "node_tail", "gemm_Phi1_adj", "layer1_rev",

@@ -98,6 +98,10 @@ long smx_get_stage(smx_engine* eng, const char* name, double* out, long cap);
  * events between the kernels of every evaluation). */
 int smx_set_option(smx_engine* eng, const char* key, long value);
 
+/* The engine's own CUDA stream (a cudaStream_t): host-pointer calls and the MD driver
+ * run on it, so callers can order their work or record CUDA events against it. */
+void* smx_engine_stream(smx_engine* eng);
+
 /* With "profile" on: device time (ms) of each stage of the last evaluation, in launch
  * order: layer0_fwd, gemm_H1, layer1_fwd, gemm_A1, node_tail, gemm_Phi1_adj,
  * layer1_rev, gemm_M0_adj, layer0_rev.  Returns the number of stages (0 if profiling

@@ -41,7 +41,42 @@ struct DevModel {
   const float* ro2_w1;
   const float* ro2_w2;
   const float* e0;
+  // ZBL pair repulsion (optional)
+  int has_zbl, zbl_p;
+  float zbl_c[4];
+  const float4* zbl_pair;  // [S*S]: (1/a, 0.5*14.3996*Zu*Zv, r_max, 0)
 };
+
+// ZBL energy of one directed edge and its r-derivative, as zbl.cpp:22-94
+// (energy 0.5 * v(r) * envelope(r); each pair appears as two directed edges).
+__device__ __forceinline__ void zbl_edge(const DevModel& m, float4 pq, float r, float& V, float& dV) {
+  V = 0.0f;
+  dV = 0.0f;
+  const float rmax = pq.z;
+  if (!(r < rmax)) return;
+  const float ce[4] = {-3.2f, -0.9423f, -0.4028f, -0.2016f};
+  float phi = 0.0f, dphi = 0.0f;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const float e = m.zbl_c[q] * expf(ce[q] * r * pq.x);
+    phi += e;
+    dphi += ce[q] * pq.x * e;
+  }
+  const float v = pq.y * 2.0f * phi / r;                      // 14.3996 Zu Zv phi / r
+  const float dv = pq.y * 2.0f * (r * dphi - phi) / (r * r);
+  const float t = r / rmax;
+  const int p = m.zbl_p;
+  float tp1 = 1.0f;  // t^(p-1)
+  for (int q = 0; q < p - 1; ++q) tp1 *= t;
+  const float tp = tp1 * t, tp2 = tp * t, tp3 = tp2 * t;
+  const float fp = static_cast<float>(p);
+  const float env = 1.0f - (fp + 1.0f) * (fp + 2.0f) * 0.5f * tp + fp * (fp + 2.0f) * tp2 -
+                    fp * (fp + 1.0f) * 0.5f * tp3;
+  const float denv = (-(fp + 1.0f) * (fp + 2.0f) * 0.5f * fp * tp1 + fp * (fp + 2.0f) * (fp + 1.0f) * tp -
+                      fp * (fp + 1.0f) * 0.5f * (fp + 2.0f) * tp2) / rmax;
+  V = 0.5f * v * env;
+  dV = 0.5f * (v * denv + dv * env);
+}
 
 // Edge list in the evaluator's layout (libsymmetrix/source/mace.hpp:29-35): CSR by
 // centre node, xyz = x_j - x_i, r = |xyz|.  Edges with r >= r_cut are skipped

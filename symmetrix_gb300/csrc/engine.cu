@@ -93,6 +93,8 @@ int smx_atomic_numbers(const smx_engine* eng, int* out, int cap) {
   return eng->hm.S;
 }
 
+void* smx_engine_stream(smx_engine* eng) { return eng ? static_cast<void*>(eng->stream) : nullptr; }
+
 int smx_set_option(smx_engine* eng, const char* key, long value) {
   if (!eng || !key) return fail(SMX_ERR_INVALID, "NULL argument");
   if (std::strcmp(key, "keep_stages") == 0) {

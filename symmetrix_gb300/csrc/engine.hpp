@@ -55,6 +55,7 @@ struct smx_engine {
   float *A0_adj = nullptr, *M0_adj = nullptr, *H1_adj = nullptr, *Phi1_adj = nullptr, *A1_adj = nullptr;
   float *M1_adj = nullptr, *H2_adj = nullptr;
   double* f1 = nullptr;  // layer-1 edge forces (float64 accumulation)
+  float* zbl_e = nullptr;  // per-node ZBL energy
   int *first = nullptr, *ntype = nullptr, *nidx = nullptr, *ntype_e = nullptr;
   double *xyz = nullptr, *r = nullptr, *energies = nullptr, *forces = nullptr;
   int lastN = 0;
@@ -115,7 +116,6 @@ struct smx_engine {
     m.ro2_w1 = upload(pm.ro2_w1);
     m.ro2_w2 = upload(pm.ro2_w2);
     m.e0 = upload(pm.e0);
-    if (hm.has_zbl) throw std::invalid_argument("model file: ZBL pair repulsion is not supported by this build");
     check(smx::init_edge_kernels(dm), "cudaFuncSetAttribute");
     if (hm.L_max != 1) throw std::invalid_argument("model file: this build supports L_max = 1 (hidden irreps 0e + 1o)");
     if (hm.A0_scaled || hm.A1_scaled)
@@ -129,6 +129,8 @@ struct smx_engine {
       if (p) cudaFree(p);
     A0 = M0 = H1 = Phi1 = A1 = M1 = H2 = A0_adj = M0_adj = H1_adj = Phi1_adj = A1_adj = M1_adj = H2_adj = nullptr;
     f1 = nullptr;
+    if (zbl_e) cudaFree(zbl_e);
+    zbl_e = nullptr;
     first = ntype = nidx = ntype_e = nullptr;
     xyz = r = energies = forces = nullptr;
     capN = capE = 0;
@@ -154,6 +156,7 @@ struct smx_engine {
     M1_adj = dalloc<float>(nN * C);
     H2_adj = dalloc<float>(nN * C);
     f1 = dalloc<double>(3 * nE);
+    zbl_e = dalloc<float>(nN);
     first = dalloc<int>(nN + 1);
     ntype = dalloc<int>(nN);
     nidx = dalloc<int>(nE);
@@ -200,7 +203,7 @@ struct smx_engine {
       for (auto& e : ev) check(cudaEventCreate(&e), "cudaEventCreate");
     prof_stream = s;
     mark(0, s);
-    smx::launch_layer0_fwd(dm, in, A0, M0, s);
+    smx::launch_layer0_fwd(dm, in, A0, M0, dm.has_zbl ? zbl_e : nullptr, s);
     mark(1, s);
     {  // H1 = M0 @ H1W[L]  (mace.cpp:397-423)
       smx::GemmBatch b{};
@@ -222,7 +225,8 @@ struct smx_engine {
       smx::launch_gemm(b, s);
     }
     mark(4, s);
-    smx::launch_node_tail(dm, in.node_type, N, A1, H1, M1, H2, A1_adj, H1_adj, M1_adj, H2_adj, out_e, s);
+    smx::launch_node_tail(dm, in.node_type, N, A1, H1, M1, H2, A1_adj, H1_adj, M1_adj, H2_adj,
+                          dm.has_zbl ? zbl_e : nullptr, out_e, s);
     mark(5, s);
     {  // Phi1_adj = A1_adj @ A1W[l]^T  (mace.cpp:644-679)
       smx::GemmBatch b{};

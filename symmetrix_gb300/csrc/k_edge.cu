@@ -84,7 +84,7 @@ __device__ __forceinline__ void block_reduce3(float fx, float fy, float fz, floa
 // folded ordered-pair splines, then M0[i,LM,k] = P_{ti,LM,k}(A0[i,:,k]).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_layer0_fwd(DevModel m, EdgeIn in, float* __restrict__ A0,
-                                                    float* __restrict__ M0) {
+                                                    float* __restrict__ M0, float* __restrict__ zbl_e) {
   extern __shared__ float dyn[];
   __shared__ float sY[16][kEdgeChunk];
   __shared__ float sx[kEdgeChunk];
@@ -111,6 +111,23 @@ __global__ void __launch_bounds__(256) k_layer0_fwd(DevModel m, EdgeIn in, float
 #pragma unroll
         for (int q = l * l; q < (l + 1) * (l + 1); ++q) acc[q] = fmaf(R, sY[q][t], acc[q]);
       }
+    }
+  }
+  if (m.has_zbl) {  // ZBL energy of node i: sum over its directed edges (zbl.cpp:96-125)
+    __shared__ float sz[8];
+    float z = 0.0f;
+    for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+      float V, dV;
+      zbl_edge(m, m.zbl_pair[ti * m.S + in.ntype_e[e]], static_cast<float>(in.r[e]), V, dV);
+      z += V;
+    }
+    z = warp_sum(z);
+    if ((threadIdx.x & 31) == 0) sz[threadIdx.x >> 5] = z;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float t = 0.0f;
+      for (int w = 0; w < (C >> 5); ++w) t += sz[w];
+      zbl_e[i] = t;
     }
   }
   float* sA = dyn;  // [17][C]: this thread's A0 column (+ constant one) for the contraction
@@ -389,6 +406,12 @@ __global__ void __launch_bounds__(256) k_layer0_rev(DevModel m, EdgeIn in, const
       double s[3] = {0.0, 0.0, 0.0};
       for (int w = 0; w < nwarp; ++w)
         for (int a = 0; a < 3; ++a) s[a] += static_cast<double>(sF[t][w][a]);
+      if (m.has_zbl) {  // node_forces -= xyz / r * dV_ZBL/dr (zbl.cpp:118-121)
+        float V, dV;
+        const double r = in.r[e];
+        zbl_edge(m, m.zbl_pair[ti * m.S + in.ntype_e[e]], static_cast<float>(r), V, dV);
+        for (int a = 0; a < 3; ++a) s[a] += in.xyz[3 * e + a] / r * static_cast<double>(dV);
+      }
       for (int a = 0; a < 3; ++a) forces[3 * e + a] = -(s[a] + f1[3 * e + a]);
     }
   }
@@ -407,10 +430,10 @@ cudaError_t init_edge_kernels(const DevModel& m) {
                               static_cast<int>(sizeof(float) * (m.n_lme + ins_np(1)) * m.C));
 }
 
-void launch_layer0_fwd(const DevModel& m, const EdgeIn& in, float* A0, float* M0, cudaStream_t s) {
+void launch_layer0_fwd(const DevModel& m, const EdgeIn& in, float* A0, float* M0, float* zbl_e, cudaStream_t s) {
   if (in.N <= 0) return;
   const size_t smem = 17 * sizeof(float) * m.C;
-  k_layer0_fwd<<<in.N, m.C, smem, s>>>(m, in, A0, M0);
+  k_layer0_fwd<<<in.N, m.C, smem, s>>>(m, in, A0, M0, zbl_e);
 }
 
 void launch_layer1_fwd(const DevModel& m, const EdgeIn& in, const float* H1, float* Phi1, cudaStream_t s) {

@@ -98,7 +98,8 @@ __global__ void __launch_bounds__(256) k_node_tail(DevModel m, const int* __rest
                                                    const float* __restrict__ H1, float* __restrict__ M1o,
                                                    float* __restrict__ H2o, float* __restrict__ A1_adj,
                                                    float* __restrict__ H1_adj, float* __restrict__ M1_adj_o,
-                                                   float* __restrict__ H2_adj_o, double* __restrict__ energies) {
+                                                   float* __restrict__ H2_adj_o, const float* __restrict__ zbl_e,
+                                                   double* __restrict__ energies) {
   extern __shared__ float dyn[];
   const int C = m.C, k = threadIdx.x, i = blockIdx.x;
   const int nwarp = C >> 5, lane = k & 31, warp = k >> 5;
@@ -170,6 +171,7 @@ __global__ void __launch_bounds__(256) k_node_tail(DevModel m, const int* __rest
       const float sg = 1.0f / (1.0f + expf(-s));
       e += static_cast<double>(__ldg(m.ro2_w2 + u) * (m.ro2_scale * s * sg));
     }
+    if (zbl_e) e += static_cast<double>(zbl_e[i]);
     energies[i] = e;
   }
   __syncthreads();
@@ -191,11 +193,11 @@ __global__ void __launch_bounds__(256) k_node_tail(DevModel m, const int* __rest
 }
 
 void launch_node_tail(const DevModel& m, const int* node_type, int N, const float* A1, const float* H1, float* M1,
-                      float* H2, float* A1_adj, float* H1_adj, float* M1_adj, float* H2_adj, double* energies,
-                      cudaStream_t s) {
+                      float* H2, float* A1_adj, float* H1_adj, float* M1_adj, float* H2_adj, const float* zbl_e,
+                      double* energies, cudaStream_t s) {
   if (N <= 0) return;
   const size_t smem = sizeof(float) * (34 * m.C + 4 * m.C + 33 * 8 + 33);
-  k_node_tail<<<N, m.C, smem, s>>>(m, node_type, A1, H1, M1, H2, A1_adj, H1_adj, M1_adj, H2_adj, energies);
+  k_node_tail<<<N, m.C, smem, s>>>(m, node_type, A1, H1, M1, H2, A1_adj, H1_adj, M1_adj, H2_adj, zbl_e, energies);
 }
 
 // first[0] = 0, first[i+1] = first[i] + num_neigh[i]; one block, sequential tiles.

@@ -9,7 +9,7 @@ namespace smx {
 
 // k_edge.cu
 cudaError_t init_edge_kernels(const DevModel& m);
-void launch_layer0_fwd(const DevModel& m, const EdgeIn& in, float* A0, float* M0, cudaStream_t s);
+void launch_layer0_fwd(const DevModel& m, const EdgeIn& in, float* A0, float* M0, float* zbl_e, cudaStream_t s);
 void launch_layer1_fwd(const DevModel& m, const EdgeIn& in, const float* H1, float* Phi1, cudaStream_t s);
 void launch_layer1_rev(const DevModel& m, const EdgeIn& in, const float* H1, const float* dPhi1, float* H1_adj,
                        double* f1, cudaStream_t s);
@@ -38,8 +38,8 @@ struct GemmBatch {
 void launch_gemm(const GemmBatch& b, cudaStream_t s);
 
 void launch_node_tail(const DevModel& m, const int* node_type, int N, const float* A1, const float* H1, float* M1,
-                      float* H2, float* A1_adj, float* H1_adj, float* M1_adj, float* H2_adj, double* energies,
-                      cudaStream_t s);
+                      float* H2, float* A1_adj, float* H1_adj, float* M1_adj, float* H2_adj, const float* zbl_e,
+                      double* energies, cudaStream_t s);
 void launch_scan_first(const int* num_neigh, int N, int* first, cudaStream_t s);
 
 // k_md.cu

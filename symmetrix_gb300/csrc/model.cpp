@@ -414,6 +414,26 @@ PackedModel pack_model(const HostModel& hm) {
   pm.n_hidden = hm.n_hidden;
   pm.e0 = f32(hm.e0);
   pm.Z = hm.Z;
+  if (hm.has_zbl) {
+    pm.has_zbl = 1;
+    pm.zbl_p = hm.zbl_p;
+    for (int q = 0; q < 4; ++q) pm.zbl_c[q] = static_cast<float>(hm.zbl_c[q]);
+    pm.zbl_pair.assign(static_cast<size_t>(S) * S * 4, 0.0f);
+    for (int a = 0; a < S; ++a)
+      for (int b = 0; b < S; ++b) {
+        const int Zu = hm.Z[a], Zv = hm.Z[b];
+        if (Zu < 0 || Zv < 0 || Zu >= static_cast<int>(hm.zbl_radii.size()) ||
+            Zv >= static_cast<int>(hm.zbl_radii.size()))
+          throw std::invalid_argument("model file: zbl_covalent_radii does not cover the model's atomic numbers");
+        // zbl.cpp:22-40: a = a_prefactor * 0.529 / (Zu^a_exp + Zv^a_exp), r_max = rcov_u + rcov_v
+        const double a_len = hm.zbl_a_pref * 0.529 / (std::pow(double(Zu), hm.zbl_a_exp) + std::pow(double(Zv), hm.zbl_a_exp));
+        float* q = &pm.zbl_pair[(static_cast<size_t>(a) * S + b) * 4];
+        q[0] = static_cast<float>(1.0 / a_len);
+        q[1] = static_cast<float>(0.5 * 14.3996 * Zu * Zv);
+        q[2] = static_cast<float>(hm.zbl_radii[Zu] + hm.zbl_radii[Zv]);
+        q[3] = 0.0f;
+      }
+  }
   return pm;
 }
 

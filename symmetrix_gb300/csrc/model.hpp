@@ -104,6 +104,10 @@ struct PackedModel {
   int n_hidden;
   std::vector<float> e0;
   std::vector<int> Z;
+  // ZBL pair repulsion (zbl.cpp): per ordered species pair (1/a, 0.5 * 14.3996 Zu Zv, r_max, 0)
+  int has_zbl = 0, zbl_p = 0;
+  float zbl_c[4] = {0, 0, 0, 0};
+  std::vector<float> zbl_pair;  // [S*S][4]
 };
 
 PackedModel pack_model(const HostModel& hm);

@@ -102,6 +102,11 @@ class MACE:
         _lib.raise_for(code, self._lib)
         return e.value, node_e, forces, virial.reshape(3, 3)
 
+    @property
+    def stream(self):
+        """Address of the engine's CUDA stream (host-pointer calls and MD run on it)."""
+        return self._lib.smx_engine_stream(self._h)
+
     def set_option(self, key, value):
         _lib.raise_for(self._lib.smx_set_option(self._h, key.encode(), int(value)), self._lib)
 

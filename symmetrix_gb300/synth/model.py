@@ -34,6 +34,13 @@ def atomic_number(sym):
     return CHEMICAL_SYMBOLS.index(sym)
 
 
+# Covalent radii (A) by atomic number, Z = 0..30 (Cordero et al., Dalton Trans. 2008, as
+# tabulated by ASE; index 0 is ASE's placeholder 0.2).  The ZBL block indexes them by Z
+# (zbl.cpp:25-26), as the extractor writes them (extract_mace_data.py:135-136).
+COVALENT_RADII = [0.2, 0.31, 0.28, 1.28, 0.96, 0.84, 0.76, 0.71, 0.66, 0.57, 0.58, 1.66, 1.41, 1.21, 1.11,
+                  1.07, 1.05, 1.02, 1.06, 2.03, 1.76, 1.70, 1.60, 1.53, 1.39, 1.39, 1.32, 1.26, 1.24, 1.32, 1.22]
+
+
 def bessel_envelope(r, r_cut, num_bessel=8, p=5):
     """MACE radial embedding: sqrt(2/rc) sin(n pi r/rc)/r times the polynomial envelope."""
     n = np.arange(1, num_bessel + 1)
@@ -70,7 +77,7 @@ def _spline_tables(r_knots, values):
 
 def make_model(num_channels=32, species=("H", "C", "O"), r_cut=5.0, L_max=1, correlation=3,
                num_bessel=8, envelope_p=5, num_knots=200, avg_num_neighbors=None, seed=0,
-               radial_hidden=(64, 64), l_max=3, a0_gain=7.0, a1_gain=12.0, energy_scale=0.35):
+               radial_hidden=(64, 64), l_max=3, a0_gain=7.0, a1_gain=12.0, energy_scale=0.35, zbl=False):
     """Return a dict in libsymmetrix's MACE JSON layout for a random two-layer MACE."""
     if l_max != 3:
         raise ValueError("the evaluator supports l_max = 3 only")
@@ -88,9 +95,14 @@ def make_model(num_channels=32, species=("H", "C", "O"), r_cut=5.0, L_max=1, cor
         "num_elements": S, "num_channels": C, "r_cut": float(r_cut), "l_max": l_max, "L_max": L_max,
         "atomic_numbers": Z,
         "atomic_energies": rng.normal(size=S).tolist(),
-        "has_zbl": False,
+        "has_zbl": bool(zbl),
         "A0_scaled": False, "A1_scaled": False,
     }
+    if zbl:
+        # MACE's ZBLBasis defaults (p = 6, Ziegler-Biersack-Littmark universal screening)
+        out.update({"zbl_a_exp": 0.300, "zbl_a_prefactor": 0.4543,
+                    "zbl_c": [0.1818, 0.5099, 0.2802, 0.02817], "zbl_covalent_radii": COVALENT_RADII,
+                    "zbl_p": 6})
     phi, num_e = phi1_tables(l_max, L_max)
     n_instr = len(phi["Phi1_l"])
 

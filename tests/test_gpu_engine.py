@@ -138,3 +138,21 @@ def test_device_api_matches_host_api(engine_lib, small_model_path, small_golden)
     # H1_adj is accumulated with float atomics, so two runs agree to float32 rounding only
     np.testing.assert_allclose(e_out.cpu().numpy(), m.node_energies, rtol=0, atol=1e-6)
     np.testing.assert_allclose(f_out.cpu().numpy(), m.node_forces, rtol=0, atol=2e-6)
+
+
+def test_zbl_model_matches_oracle(engine_lib, tmp_path):
+    """ZBL pair repulsion (zbl.cpp:22-125) on close pairs, against the oracle."""
+    path = write_model(make_model(num_channels=32, species=("H", "C", "O"), num_knots=60, seed=4, zbl=True),
+                       str(tmp_path / "zbl.json"))
+    rng = np.random.default_rng(2)
+    pos = rng.normal(size=(40, 3)) * 1.8
+    species = rng.integers(0, 3, size=40).astype(np.int32)
+    nl = neighbor_list(pos, 5.0)
+    assert nl["r"].min() < 1.0
+    m = _engine(path)
+    m.compute_node_energies_forces(*edge_args(species, nl))
+    ref = Evaluator(path, "port")
+    ref.compute_node_energies_forces(*edge_args(species, nl))
+    scale = max(1.0, np.abs(ref.node_forces).max())
+    assert _report("E_i", m.node_energies, ref.node_energies) < E_TOL * max(1.0, np.abs(ref.node_energies).max())
+    assert _report("f_edge", m.node_forces, ref.node_forces) < F_TOL * scale

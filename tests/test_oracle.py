@@ -245,3 +245,21 @@ def test_mlp_matches_numpy(which):
            - getattr(lib, pre + "mlp_eval")(3, 6, _dp(w0.flatten()), _dp(w1), s, _dp(x - h * e), _dp(np.zeros(3))))
           / (2 * h) for e in np.eye(3)]
     np.testing.assert_allclose(g, gn, rtol=1e-6)
+
+
+@needs_ref
+def test_port_matches_reference_with_zbl(tmp_path):
+    """Models with ZBL pair repulsion (zbl.cpp:96-125), close pairs inside r_max."""
+    from symmetrix_gb300.synth.model import make_model, write_model
+    path = write_model(make_model(num_channels=8, species=("H", "C", "O"), num_knots=40, seed=4, zbl=True,
+                                  radial_hidden=(16,)), str(tmp_path / "zbl.json"))
+    rng = np.random.default_rng(2)
+    pos = rng.normal(size=(10, 3)) * 1.1
+    species = rng.integers(0, 3, size=10).astype(np.int32)
+    nl = neighbor_list(pos, 5.0)
+    assert nl["r"].min() < 1.0
+    port, ref = Evaluator(path, "port"), Evaluator(path, "reference")
+    for ev in (port, ref):
+        ev.compute_node_energies_forces(*edge_args(species, nl))
+    np.testing.assert_allclose(port.node_energies, ref.node_energies, rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(port.node_forces, ref.node_forces, rtol=1e-10, atol=1e-12)

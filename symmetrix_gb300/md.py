@@ -55,3 +55,36 @@ class MD:
         if h is not None and h.value:
             self._lib.smx_md_destroy(h)
             self._h = None
+
+
+def relax_fire(engine, positions, species, box=None, steps=300, fmax=0.05, dt=0.5, dt_max=2.0, maxmove=0.1):
+    """FIRE minimisation (Bitzek et al., PRL 97, 170201 (2006)) with atom-level GPU
+    evaluations; unit masses, time in fs.  Returns (positions, energy, max |F|)."""
+    x = np.array(positions, dtype=np.float64).reshape(-1, 3)
+    v = np.zeros_like(x)
+    alpha, n_pos = 0.1, 0
+    E, _, F, _ = engine.compute_atoms(x, species, box=box)
+    for _ in range(steps):
+        fm = np.abs(F).max()
+        if fm < fmax:
+            break
+        P = float((F * v).sum())
+        if P > 0:
+            vn, fn = np.linalg.norm(v), np.linalg.norm(F)
+            v = (1 - alpha) * v + alpha * F * (vn / max(fn, 1e-300))
+            n_pos += 1
+            if n_pos > 5:
+                dt = min(dt * 1.1, dt_max)
+                alpha *= 0.99
+        else:
+            v[:] = 0.0
+            dt *= 0.5
+            alpha, n_pos = 0.1, 0
+        v += dt * F
+        dx = dt * v
+        big = np.linalg.norm(dx, axis=1).max()
+        if big > maxmove:
+            dx *= maxmove / big
+        x += dx
+        E, _, F, _ = engine.compute_atoms(x, species, box=box)
+    return x, E, float(np.abs(F).max())

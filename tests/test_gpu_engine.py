@@ -145,7 +145,9 @@ def test_zbl_model_matches_oracle(engine_lib, tmp_path):
     path = write_model(make_model(num_channels=32, species=("H", "C", "O"), num_knots=60, seed=4, zbl=True),
                        str(tmp_path / "zbl.json"))
     rng = np.random.default_rng(2)
-    pos = rng.normal(size=(40, 3)) * 1.8
+    base = rng.normal(size=(32, 3)) * 1.8
+    close = base[:8] + rng.normal(size=(8, 3)) * 0.35  # partners inside the ZBL range
+    pos = np.concatenate([base, close])
     species = rng.integers(0, 3, size=40).astype(np.int32)
     nl = neighbor_list(pos, 5.0)
     assert nl["r"].min() < 1.0

@@ -259,8 +259,8 @@ def gpu_arm(args, rank, world, local_rank):
 
     from symmetrix_gb300 import MACE, _lib
     from symmetrix_gb300.build import build
-    from symmetrix_gb300.md import MD, relax_fire
-    from symmetrix_gb300.synth.structures import maxwell_boltzmann, neighbor_list, species_masses
+    from symmetrix_gb300.md import MD
+    from symmetrix_gb300.synth.structures import maxwell_boltzmann, species_masses
 
     torch.cuda.set_device(local_rank)
     dist = None
@@ -276,13 +276,6 @@ def gpu_arm(args, rank, world, local_rank):
     dims = model_dims(eng, path)
     dev = torch.device("cuda", local_rank)
     estream = torch.cuda.ExternalStream(eng.stream, device=dev)
-
-    # ---- setup (untimed): relax the random insertion so 300 K dynamics are stable ----
-    t_relax = time.time()
-    pos, e_relaxed, fmax_relaxed = relax_fire(eng, pos, species, box=L, steps=400)
-    t_relax = time.time() - t_relax
-    nl = neighbor_list(pos, 5.0, L)
-    E = len(nl["r"])
 
     # ---- MD: the timed region ----
     masses = species_masses(eng.atomic_numbers, species)
@@ -317,8 +310,7 @@ def gpu_arm(args, rank, world, local_rank):
     st1 = md.state()
     acc = 9.648533212331e-3
     ke = lambda v: 0.5 * float((masses[:, None] * v ** 2).sum()) / acc
-    md_check = {"relax": {"steps_max": 400, "seconds": t_relax, "fmax_eV_A": fmax_relaxed},
-                "E_total_start": st0["potential_energy"] + ke(st0["velocities"]),
+    md_check = {"E_total_start": st0["potential_energy"] + ke(st0["velocities"]),
                 "E_total_end": st1["potential_energy"] + ke(st1["velocities"]),
                 "T_end_K": 2 * ke(st1["velocities"]) / (3 * N * 8.617333262e-5), "edges_skin_list": md.num_edges}
     del md

@@ -77,7 +77,8 @@ def _spline_tables(r_knots, values):
 
 def make_model(num_channels=32, species=("H", "C", "O"), r_cut=5.0, L_max=1, correlation=3,
                num_bessel=8, envelope_p=5, num_knots=200, avg_num_neighbors=None, seed=0,
-               radial_hidden=(64, 64), l_max=3, a0_gain=7.0, a1_gain=12.0, energy_scale=0.35, zbl=False):
+               radial_hidden=(64, 64), l_max=3, a0_gain=7.0, a1_gain=12.0, energy_scale=0.35, zbl=False,
+               core=(0.8, 1.3)):
     """Return a dict in libsymmetrix's MACE JSON layout for a random two-layer MACE."""
     if l_max != 3:
         raise ValueError("the evaluator supports l_max = 3 only")
@@ -111,8 +112,16 @@ def make_model(num_channels=32, species=("H", "C", "O"), r_cut=5.0, L_max=1, cor
     emb = bessel_envelope(r_knots, r_cut, num_bessel, envelope_p)
     mlp0 = _radial_mlp(rng, num_bessel, radial_hidden, (l_max + 1) * C)
     mlp1 = _radial_mlp(rng, num_bessel, radial_hidden, n_instr * C)
-    base0 = _apply_mlp(mlp0, emb)
-    base1 = _apply_mlp(mlp1, emb)
+    # A random potential has no repulsive core and grows without bound as pairs close in;
+    # the radials are switched off smoothly (C2) inside `core` so that short range is left
+    # to the ZBL term and the energy stays bounded below.
+    if core:
+        xs = np.clip((r_knots - core[0]) / (core[1] - core[0]), 0.0, 1.0)
+        damp = (xs ** 3 * (10.0 - 15.0 * xs + 6.0 * xs ** 2))[:, None]
+    else:
+        damp = 1.0
+    base0 = _apply_mlp(mlp0, emb) * damp
+    base1 = _apply_mlp(mlp1, emb) * damp
     v0, d0, v1, d1 = [], [], [], []
     for a in range(S):
         for b in range(a, S):

@@ -14,6 +14,7 @@ constexpr int kEdgeChunk = 32;  // edges staged in shared memory per block itera
 // Device view of a packed model (see model.hpp for layouts).  Passed by value.
 struct DevModel {
   int S, C, L_max, nLM, n_lme, n_instr, n_p, nint, T0, T1, n_hidden;
+  int poly_canon;  // coefficients in canonical order: use the generated polynomials
   float h, inv_h, r_cut, ro2_scale;
   const float4* spl0;  // [S*S][nint][4][C]
   const float4* spl1;  // [npairs][nint][n_instr][C]

@@ -209,7 +209,7 @@ long smx_get_stage(smx_engine* eng, const char* name, double* out, long cap) {
   else if (s == "A1") { src = eng->A1; n = N * 16 * C; }
   else if (s == "M1") { src = eng->M1; n = N * C; }
   else if (s == "H2") { src = eng->H2; n = N * C; }
-  else if (s == "A0_adj") { src = eng->keep_stages ? eng->A0_adj : nullptr; n = N * 16 * C; }
+  else if (s == "A0_adj") { src = eng->A0_adj; n = N * 16 * C; }
   else if (s == "M0_adj") { src = eng->M0_adj; n = N * eng->dm.nLM * C; }
   else if (s == "H1_adj") { src = eng->H1_adj; n = N * eng->dm.nLM * C; }
   else if (s == "Phi1_adj") { src = eng->Phi1_adj; n = N * eng->dm.n_lme * C; }

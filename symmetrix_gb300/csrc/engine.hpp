@@ -82,6 +82,7 @@ struct smx_engine {
     m.nint = pm.nint;
     m.T0 = pm.T0;
     m.T1 = pm.T1;
+    m.poly_canon = pm.poly_canon;
     m.n_hidden = pm.n_hidden;
     m.h = pm.h;
     m.inv_h = static_cast<float>(1.0 / hm.spl_h);
@@ -247,7 +248,7 @@ struct smx_engine {
       smx::launch_gemm(b, s);
     }
     mark(8, s);
-    smx::launch_layer0_rev(dm, in, A0, M0_adj, f1, keep_stages ? A0_adj : nullptr, out_f, s);
+    smx::launch_layer0_rev(dm, in, A0, M0_adj, f1, A0_adj, out_f, s);
     mark(9, s);
     check(cudaGetLastError(), "kernel launch");
   }

@@ -18,6 +18,7 @@
 
 #include "device.cuh"
 #include "kernels.h"
+#include "poly_canon.h"
 
 namespace smx {
 
@@ -130,12 +131,21 @@ __global__ void __launch_bounds__(256) k_layer0_fwd(DevModel m, EdgeIn in, float
       zbl_e[i] = t;
     }
   }
+#pragma unroll
+  for (int q = 0; q < 16; ++q) A0[(static_cast<size_t>(i) * 16 + q) * C + k] = acc[q];
+  if (m.poly_canon) {  // generated straight-line polynomials, A0 column in registers
+    const float* cf = m.coef0 + static_cast<size_t>(ti * m.nLM) * m.T0 * C + k;
+    const size_t st = static_cast<size_t>(m.T0) * C;
+    float* out = M0 + static_cast<size_t>(i) * m.nLM * C + k;
+    out[0] = poly::value_LM0(acc, cf, C);
+    out[C] = poly::value_LM1(acc, cf + st, C);
+    out[2 * C] = poly::value_LM2(acc, cf + 2 * st, C);
+    out[3 * C] = poly::value_LM3(acc, cf + 3 * st, C);
+    return;
+  }
   float* sA = dyn;  // [17][C]: this thread's A0 column (+ constant one) for the contraction
 #pragma unroll
-  for (int q = 0; q < 16; ++q) {
-    A0[(static_cast<size_t>(i) * 16 + q) * C + k] = acc[q];
-    sA[q * C + k] = acc[q];
-  }
+  for (int q = 0; q < 16; ++q) sA[q * C + k] = acc[q];
   sA[16 * C + k] = 1.0f;
   for (int LM = 0; LM < m.nLM; ++LM) {
     const int t0 = m.mono0_off[LM], t1 = m.mono0_off[LM + 1];
@@ -319,14 +329,70 @@ __global__ void __launch_bounds__(256) k_layer1_rev(DevModel m, EdgeIn in, const
 }
 
 // ---------------------------------------------------------------------------
-// Layer 0 adjoint: dA0[i,:,k] = sum_LM dM0[i,LM,k] grad P_{ti,LM,k}(A0[i,:,k]), then
+// Layer-0 contraction adjoint (mace.cpp:372-395):
+//   A0_adj[i,:,k] = sum_LM M0_adj[i,LM,k] grad P_{ti,LM,k}(A0[i,:,k]).
+// Its own kernel, so its register-heavy generated code does not limit the occupancy
+// of the layer-0 edge adjoint.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_contract0_rev(DevModel m, const int* __restrict__ node_type,
+                                                       const float* __restrict__ A0, const float* __restrict__ M0_adj,
+                                                       float* __restrict__ A0_adj) {
+  extern __shared__ float dyn[];
+  const int C = m.C, k = threadIdx.x, i = blockIdx.x;
+  const int ti = node_type[i];
+  float dA[16];
+  if (m.poly_canon) {  // dA0 = sum_LM dM0[LM] grad P_LM, generated code, registers only
+    float x[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      x[q] = A0[(static_cast<size_t>(i) * 16 + q) * C + k];
+      dA[q] = 0.0f;
+    }
+    const float* cf = m.coef0 + static_cast<size_t>(ti * m.nLM) * m.T0 * C + k;
+    const size_t st = static_cast<size_t>(m.T0) * C;
+    const float* w = M0_adj + static_cast<size_t>(i) * m.nLM * C + k;
+    poly::grad_LM0(x, w[0], cf, C, dA);
+    poly::grad_LM1(x, w[C], cf + st, C, dA);
+    poly::grad_LM2(x, w[2 * C], cf + 2 * st, C, dA);
+    poly::grad_LM3(x, w[3 * C], cf + 3 * st, C, dA);
+  } else {  // data-driven monomial lists, this thread's columns in shared memory
+    float* sA = dyn;            // [17][C] A0 column
+    float* sGd = dyn + 17 * C;  // [17][C] gradient column (row 16 absorbs the constant slot)
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      sA[q * C + k] = A0[(static_cast<size_t>(i) * 16 + q) * C + k];
+      sGd[q * C + k] = 0.0f;
+    }
+    sA[16 * C + k] = 1.0f;
+    sGd[16 * C + k] = 0.0f;
+    for (int LM = 0; LM < m.nLM; ++LM) {
+      const float w = M0_adj[(static_cast<size_t>(i) * m.nLM + LM) * C + k];
+      const int t0 = m.mono0_off[LM], t1 = m.mono0_off[LM + 1];
+      const float* cf = m.coef0 + (static_cast<size_t>(ti * m.nLM + LM) * m.T0) * C + k;
+      for (int t = t0; t < t1; ++t) {
+        const int pk = __ldg(m.mono0 + t);
+        const int a = pk & 255, b = (pk >> 8) & 255, c = pk >> 16;
+        const float cw = __ldg(cf + static_cast<size_t>(t - t0) * C) * w;
+        const float xa = sA[a * C + k], xb = sA[b * C + k], xc = sA[c * C + k];
+        sGd[a * C + k] += cw * xb * xc;
+        sGd[b * C + k] += cw * xa * xc;
+        sGd[c * C + k] += cw * xa * xb;
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 16; ++q) dA[q] = sGd[q * C + k];
+  }
+#pragma unroll
+  for (int q = 0; q < 16; ++q) A0_adj[(static_cast<size_t>(i) * 16 + q) * C + k] = dA[q];
+}
+
+// ---------------------------------------------------------------------------
+// Layer 0 edge adjoint, from dA0 (k_contract0_rev):
 //   dE/dx_ij = sum_k sum_lm dA0[lm] (R0'_l'(r) u Y_lm + R0'_l(r) dY_lm/dx)
 // and node_forces[e] = -(layer-0 + layer-1 contributions), in float64.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_layer0_rev(DevModel m, EdgeIn in, const float* __restrict__ A0,
-                                                    const float* __restrict__ M0_adj, const double* __restrict__ f1,
-                                                    float* __restrict__ A0_adj, double* __restrict__ forces) {
-  extern __shared__ float dyn[];
+__global__ void __launch_bounds__(256) k_layer0_rev(DevModel m, EdgeIn in, const float* __restrict__ A0_adj,
+                                                    const double* __restrict__ f1, double* __restrict__ forces) {
   __shared__ float sY[16][kEdgeChunk];
   __shared__ float sG[48][kEdgeChunk];
   __shared__ float su[3][kEdgeChunk];
@@ -337,35 +403,9 @@ __global__ void __launch_bounds__(256) k_layer0_rev(DevModel m, EdgeIn in, const
   const int nwarp = C >> 5;
   const int ti = in.node_type[i];
   const int e0 = in.first[i], e1 = in.first[i + 1];
-  float* sA = dyn;            // [17][C] A0 column
-  float* sGd = dyn + 17 * C;  // [17][C] gradient column (row 16 absorbs the constant slot)
-#pragma unroll
-  for (int q = 0; q < 16; ++q) {
-    sA[q * C + k] = A0[(static_cast<size_t>(i) * 16 + q) * C + k];
-    sGd[q * C + k] = 0.0f;
-  }
-  sA[16 * C + k] = 1.0f;
-  sGd[16 * C + k] = 0.0f;
-  for (int LM = 0; LM < m.nLM; ++LM) {
-    const float w = M0_adj[(static_cast<size_t>(i) * m.nLM + LM) * C + k];
-    const int t0 = m.mono0_off[LM], t1 = m.mono0_off[LM + 1];
-    const float* cf = m.coef0 + (static_cast<size_t>(ti * m.nLM + LM) * m.T0) * C + k;
-    for (int t = t0; t < t1; ++t) {
-      const int pk = __ldg(m.mono0 + t);
-      const int a = pk & 255, b = (pk >> 8) & 255, c = pk >> 16;
-      const float cw = __ldg(cf + static_cast<size_t>(t - t0) * C) * w;
-      const float xa = sA[a * C + k], xb = sA[b * C + k], xc = sA[c * C + k];
-      sGd[a * C + k] += cw * xb * xc;
-      sGd[b * C + k] += cw * xa * xc;
-      sGd[c * C + k] += cw * xa * xb;
-    }
-  }
   float dA[16];
 #pragma unroll
-  for (int q = 0; q < 16; ++q) {
-    dA[q] = sGd[q * C + k];
-    if (A0_adj) A0_adj[(static_cast<size_t>(i) * 16 + q) * C + k] = dA[q];
-  }
+  for (int q = 0; q < 16; ++q) dA[q] = A0_adj[(static_cast<size_t>(i) * 16 + q) * C + k];
   for (int eb = e0; eb < e1; eb += kEdgeChunk) {
     const int ne = min(kEdgeChunk, e1 - eb);
     __syncthreads();
@@ -452,8 +492,8 @@ void launch_layer1_rev(const DevModel& m, const EdgeIn& in, const float* H1, con
 void launch_layer0_rev(const DevModel& m, const EdgeIn& in, const float* A0, const float* M0_adj, const double* f1,
                        float* A0_adj, double* forces, cudaStream_t s) {
   if (in.N <= 0) return;
-  const size_t smem = 34 * sizeof(float) * m.C;
-  k_layer0_rev<<<in.N, m.C, smem, s>>>(m, in, A0, M0_adj, f1, A0_adj, forces);
+  k_contract0_rev<<<in.N, m.C, m.poly_canon ? 0 : 34 * sizeof(float) * m.C, s>>>(m, in.node_type, A0, M0_adj, A0_adj);
+  k_layer0_rev<<<in.N, m.C, 0, s>>>(m, in, A0_adj, f1, forces);
 }
 
 }  // namespace smx

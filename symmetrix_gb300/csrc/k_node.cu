@@ -10,6 +10,7 @@
 
 #include "device.cuh"
 #include "kernels.h"
+#include "poly_canon.h"
 
 namespace smx {
 
@@ -113,6 +114,19 @@ __global__ void __launch_bounds__(256) k_node_tail(DevModel m, const int* __rest
   float* sdH2 = sH2 + C;        // [C]
   float* sRed = sdH2 + C;       // [33][8]
   float* sS = sRed + 33 * 8;    // [33]
+  float f = 0.0f;
+  const float* cf = m.coef1 + static_cast<size_t>(ti) * m.T1 * C + k;
+  if (m.poly_canon) {  // generated straight-line M1 polynomial and gradient
+    float x[16], g[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      x[q] = A1[(static_cast<size_t>(i) * 16 + q) * C + k];
+      g[q] = 0.0f;
+    }
+    f = poly::value_grad_M1(x, cf, C, g);
+#pragma unroll
+    for (int q = 0; q < 16; ++q) sG[q * C + k] = g[q];
+  } else {
 #pragma unroll
   for (int q = 0; q < 16; ++q) {
     sX[q * C + k] = A1[(static_cast<size_t>(i) * 16 + q) * C + k];
@@ -120,8 +134,6 @@ __global__ void __launch_bounds__(256) k_node_tail(DevModel m, const int* __rest
   }
   sX[16 * C + k] = 1.0f;
   sG[16 * C + k] = 0.0f;
-  float f = 0.0f;
-  const float* cf = m.coef1 + static_cast<size_t>(ti) * m.T1 * C + k;
   for (int t = 0; t < m.T1; ++t) {
     const int pk = __ldg(m.mono1 + t);
     const int a = pk & 255, b = (pk >> 8) & 255, c = pk >> 16;
@@ -131,6 +143,7 @@ __global__ void __launch_bounds__(256) k_node_tail(DevModel m, const int* __rest
     sG[a * C + k] += w * xb * xc;
     sG[b * C + k] += w * xa * xc;
     sG[c * C + k] += w * xa * xb;
+  }
   }
   sM1[k] = f;
   const float h10 = H1[static_cast<size_t>(i) * m.nLM * C + k];

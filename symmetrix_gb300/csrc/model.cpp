@@ -10,6 +10,7 @@
 #include <stdexcept>
 
 #include "json_reader.hpp"
+#include "poly_canon_tables.h"
 
 namespace smx {
 
@@ -356,6 +357,39 @@ PackedModel pack_model(const HostModel& hm) {
   }
 
   // ---- polynomials ----
+  // Canonical layout when the model's monomials are a subset of the generated sets.
+  // Monomial factors commute, so each is matched by its sorted index tuple; an exact
+  // repeat of an earlier monomial is dropped, as MultivariatePolynomial's ordered map
+  // does (multivariate_polynomial.cpp:34-44).
+  auto sorted_pack = [](std::vector<int> m) {
+    std::sort(m.begin(), m.end());
+    return pack_mono(m);
+  };
+  auto canon_index = [&](int LM, int packed) {
+    for (int t = poly::kOffset[LM]; t < poly::kOffset[LM + 1]; ++t)
+      if (poly::kMono[t] == packed) return t - poly::kOffset[LM];
+    return -1;
+  };
+  auto map_list = [&](int LM, const std::vector<std::vector<int>>& monos, std::vector<int>& dst) {
+    dst.assign(monos.size(), -1);
+    for (size_t t = 0; t < monos.size(); ++t) {
+      bool repeat = false;
+      for (size_t u = 0; u < t; ++u) repeat = repeat || monos[u] == monos[t];
+      if (repeat) continue;
+      const int c = canon_index(LM, sorted_pack(monos[t]));
+      if (c < 0) return false;
+      dst[t] = c;
+    }
+    return true;
+  };
+  pm.poly_canon = (hm.L_max == 1 && hm.nLM == poly::kNumLM) ? 1 : 0;
+  std::vector<std::vector<int>> cmap0(hm.nLM);
+  std::vector<int> cmap1;
+  if (pm.poly_canon) {
+    for (int LM = 0; LM < hm.nLM && pm.poly_canon; ++LM)
+      if (!map_list(LM, hm.M0_mono[LM], cmap0[LM])) pm.poly_canon = 0;
+    if (pm.poly_canon && !map_list(0, hm.M1_mono, cmap1)) pm.poly_canon = 0;
+  }
   pm.mono0_off.assign(hm.nLM + 1, 0);
   pm.T0 = 0;
   for (int LM = 0; LM < hm.nLM; ++LM) {
@@ -363,22 +397,31 @@ PackedModel pack_model(const HostModel& hm) {
     pm.mono0_off[LM + 1] = static_cast<int>(pm.mono0.size());
     pm.T0 = std::max<int>(pm.T0, hm.M0_mono[LM].size());
   }
+  if (pm.poly_canon) pm.T0 = poly::kMaxCount;
   pm.coef0.assign(static_cast<size_t>(S) * hm.nLM * std::max(pm.T0, 1) * C, 0.0f);
   for (int s = 0; s < S; ++s)
     for (int LM = 0; LM < hm.nLM; ++LM)
       for (int k = 0; k < C; ++k) {
         const auto& v = hm.M0_coef[(static_cast<size_t>(s) * hm.nLM + LM) * C + k];
-        for (size_t t = 0; t < v.size(); ++t)
-          pm.coef0[((static_cast<size_t>(s) * hm.nLM + LM) * pm.T0 + t) * C + k] = static_cast<float>(v[t]);
+        for (size_t t = 0; t < v.size(); ++t) {
+          const int slot = pm.poly_canon ? cmap0[LM][t] : static_cast<int>(t);
+          if (slot < 0) continue;
+          float& dst = pm.coef0[((static_cast<size_t>(s) * hm.nLM + LM) * pm.T0 + slot) * C + k];
+          dst = pm.poly_canon ? dst + static_cast<float>(v[t]) : static_cast<float>(v[t]);
+        }
       }
   for (const auto& m : hm.M1_mono) pm.mono1.push_back(pack_mono(m));
-  pm.T1 = static_cast<int>(hm.M1_mono.size());
+  pm.T1 = pm.poly_canon ? poly::kOffset[1] : static_cast<int>(hm.M1_mono.size());
   pm.coef1.assign(static_cast<size_t>(S) * std::max(pm.T1, 1) * C, 0.0f);
   for (int s = 0; s < S; ++s)
     for (int k = 0; k < C; ++k) {
       const auto& v = hm.M1_coef[static_cast<size_t>(s) * C + k];
-      for (size_t t = 0; t < v.size(); ++t)
-        pm.coef1[(static_cast<size_t>(s) * pm.T1 + t) * C + k] = static_cast<float>(v[t]);
+      for (size_t t = 0; t < v.size(); ++t) {
+        const int slot = pm.poly_canon ? cmap1[t] : static_cast<int>(t);
+        if (slot < 0) continue;
+        float& dst = pm.coef1[(static_cast<size_t>(s) * pm.T1 + slot) * C + k];
+        dst = pm.poly_canon ? dst + static_cast<float>(v[t]) : static_cast<float>(v[t]);
+      }
     }
 
   // ---- channel mixing ----

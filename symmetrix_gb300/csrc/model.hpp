@@ -87,6 +87,10 @@ struct PackedModel {
   std::vector<int> mono1;
   int T1 = 0;
   std::vector<float> coef1;  // [S][T1][C]
+  // 1 when every monomial of the model is in the canonical sets of poly_canon.h; the
+  // coefficients are then stored in canonical order (zero for absent monomials) and
+  // the kernels use the generated straight-line polynomials
+  int poly_canon = 0;
   std::vector<float> H1W, H1W_T;  // [L][C][C]
   // CG table: sorted by lme (forward) and by canonical p (adjoint)
   std::vector<int> cg_fwd_off;  // [n_lme + 1]

@@ -117,6 +117,10 @@ struct smx_engine {
     m.ro2_w1 = upload(pm.ro2_w1);
     m.ro2_w2 = upload(pm.ro2_w2);
     m.e0 = upload(pm.e0);
+    m.has_zbl = pm.has_zbl;
+    m.zbl_p = pm.zbl_p;
+    for (int q = 0; q < 4; ++q) m.zbl_c[q] = pm.zbl_c[q];
+    m.zbl_pair = pm.has_zbl ? reinterpret_cast<const float4*>(upload(pm.zbl_pair)) : nullptr;
     check(smx::init_edge_kernels(dm), "cudaFuncSetAttribute");
     if (hm.L_max != 1) throw std::invalid_argument("model file: this build supports L_max = 1 (hidden irreps 0e + 1o)");
     if (hm.A0_scaled || hm.A1_scaled)

@@ -226,7 +226,125 @@ __global__ void __launch_bounds__(256) k_layer1_fwd(DevModel m, EdgeIn in, const
 //   dE/dx_ij += sum_k sum_p g_p h_{m2} (R1'_q(r) u Y_{m1} + R1_q(r) dY_{m1}/dx)
 //   H1_adj[j, l2 m2, k] += sum_p R1_q(r) Y_{m1} g_p        (atomic scatter)
 // f1[e] receives dE/dx_ij from this layer.
+//
+// Edges of a chunk are compacted to the active ones (r < r_cut) and processed two at
+// a time: the two edges' dependent FMA chains interleave, which is what keeps the FMA
+// pipe busy at the two resident warps per scheduler the register budget allows.
 // ---------------------------------------------------------------------------
+namespace {
+
+struct EdgeStage {
+  float4 Y[kEdgeChunk][4];    // Y_lm, 16 per edge
+  float4 G[kEdgeChunk][12];   // dY_lm/dx, dY_lm/dy, dY_lm/dz
+  float4 u[kEdgeChunk];       // unit vector (w unused)
+  float x[kEdgeChunk];        // offset inside the spline interval
+  int base[kEdgeChunk];       // spline row * stride, or -1 (r >= r_cut)
+  int j[kEdgeChunk];
+  int act[kEdgeChunk];        // compacted list of active edges
+  int nact;
+};
+
+// Stage edges [eb, eb+ne) (ne <= 32, all handled by warp 0) with Y and dY/dx packed
+// as float4 rows, and compact the active ones.
+__device__ __forceinline__ void stage_edges_packed(const DevModel& m, const EdgeIn& in, int ti, int eb, int ne,
+                                                   int stride, EdgeStage& st) {
+  if (threadIdx.x >= 32) return;
+  const int t = threadIdx.x;
+  bool active = false;
+  if (t < ne) {
+    const long e = static_cast<long>(eb) + t;
+    const float vx = static_cast<float>(in.xyz[3 * e]);
+    const float vy = static_cast<float>(in.xyz[3 * e + 1]);
+    const float vz = static_cast<float>(in.xyz[3 * e + 2]);
+    const float rr = static_cast<float>(in.r[e]);
+    float Y[16], G[48];
+    sph_harm16<true>(vx, vy, vz, Y, G);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) st.Y[t][q] = make_float4(Y[4 * q], Y[4 * q + 1], Y[4 * q + 2], Y[4 * q + 3]);
+#pragma unroll
+    for (int q = 0; q < 12; ++q) st.G[t][q] = make_float4(G[4 * q], G[4 * q + 1], G[4 * q + 2], G[4 * q + 3]);
+    const float inv = 1.0f / rr;
+    st.u[t] = make_float4(vx * inv, vy * inv, vz * inv, 0.0f);
+    int iv = static_cast<int>(rr * m.inv_h);
+    iv = iv < 0 ? 0 : (iv >= m.nint ? m.nint - 1 : iv);
+    st.x[t] = rr - static_cast<float>(iv) * m.h;
+    const int tj = in.ntype_e[e];
+    const int a = ti < tj ? ti : tj, b = ti < tj ? tj : ti;
+    const int pr = a * (2 * m.S - a - 1) / 2 + b;
+    active = rr < m.r_cut;
+    st.base[t] = active ? (pr * m.nint + iv) * stride : -1;
+    st.j[t] = in.nidx[e];
+  }
+  const unsigned ball = __ballot_sync(0xffffffffu, active);
+  if (active) st.act[__popc(ball & ((1u << t) - 1u))] = t;
+  if (t == 0) st.nact = __popc(ball);
+}
+
+// One edge of the layer-1 adjoint for this thread's channel.
+template <int LMAX>
+__device__ __forceinline__ void l1_rev_edge(const float* g, const float4* __restrict__ cp, int C, float x,
+                                            const float4* Yrow, const float4* Grow, float4 u, const float* hv,
+                                            float* hadj, float& fx, float& fy, float& fz) {
+  constexpr int NL2 = (LMAX + 1) * (LMAX + 1);
+  float Y[16];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const float4 v = Yrow[q];
+    Y[4 * q] = v.x; Y[4 * q + 1] = v.y; Y[4 * q + 2] = v.z; Y[4 * q + 3] = v.w;
+  }
+  float dY[16];
+#pragma unroll
+  for (int q = 0; q < 16; ++q) dY[q] = 0.0f;
+  float hA[NL2], hB[NL2];  // two partial sums per H1_adj component (shorter chains)
+#pragma unroll
+  for (int q = 0; q < NL2; ++q) hA[q] = hB[q] = 0.0f;
+  float drA = 0.0f, drB = 0.0f;
+  for_each_ins<LMAX>([&](auto qc) {
+    constexpr int q = decltype(qc)::value;
+    constexpr int l1 = ins_l1(LMAX, q), l2 = ins_l2(LMAX, q), p0 = ins_poff(LMAX, q);
+    const float4 cc = __ldg(cp + q * C);
+    const float R = spline_val(cc, x), Rd = spline_der(cc, x);
+    float dRq = 0.0f;
+#pragma unroll
+    for (int a = 0; a < 2 * l1 + 1; ++a) {
+      const float y = Y[l1 * l1 + a];
+      float gs = 0.0f;
+#pragma unroll
+      for (int b = 0; b < 2 * l2 + 1; ++b) gs = fmaf(g[p0 + a * (2 * l2 + 1) + b], hv[l2 * l2 + b], gs);
+      dRq = fmaf(gs, y, dRq);
+      dY[l1 * l1 + a] = fmaf(R, gs, dY[l1 * l1 + a]);
+      const float ry = R * y;
+#pragma unroll
+      for (int b = 0; b < 2 * l2 + 1; ++b) {
+        if ((q + a) & 1)
+          hB[l2 * l2 + b] = fmaf(ry, g[p0 + a * (2 * l2 + 1) + b], hB[l2 * l2 + b]);
+        else
+          hA[l2 * l2 + b] = fmaf(ry, g[p0 + a * (2 * l2 + 1) + b], hA[l2 * l2 + b]);
+      }
+    }
+    if (q & 1) drB = fmaf(dRq, Rd, drB);
+    else drA = fmaf(dRq, Rd, drA);
+  });
+#pragma unroll
+  for (int q = 0; q < NL2; ++q) hadj[q] = hA[q] + hB[q];
+  const float dr = drA + drB;
+  float ax = dr * u.x, ay = dr * u.y, az = dr * u.z;
+  float bx = 0.0f, by = 0.0f, bz = 0.0f;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const float4 gx = Grow[q], gy = Grow[4 + q], gz = Grow[8 + q];
+    ax = fmaf(dY[4 * q], gx.x, ax); ay = fmaf(dY[4 * q], gy.x, ay); az = fmaf(dY[4 * q], gz.x, az);
+    bx = fmaf(dY[4 * q + 1], gx.y, bx); by = fmaf(dY[4 * q + 1], gy.y, by); bz = fmaf(dY[4 * q + 1], gz.y, bz);
+    ax = fmaf(dY[4 * q + 2], gx.z, ax); ay = fmaf(dY[4 * q + 2], gy.z, ay); az = fmaf(dY[4 * q + 2], gz.z, az);
+    bx = fmaf(dY[4 * q + 3], gx.w, bx); by = fmaf(dY[4 * q + 3], gy.w, by); bz = fmaf(dY[4 * q + 3], gz.w, bz);
+  }
+  fx = ax + bx;
+  fy = ay + by;
+  fz = az + bz;
+}
+
+}  // namespace
+
 template <int LMAX>
 __global__ void __launch_bounds__(256) k_layer1_rev(DevModel m, EdgeIn in, const float* __restrict__ H1,
                                                     const float* __restrict__ dPhi1, float* __restrict__ H1_adj,
@@ -235,12 +353,7 @@ __global__ void __launch_bounds__(256) k_layer1_rev(DevModel m, EdgeIn in, const
   constexpr int NI = ins_count(LMAX);
   constexpr int NP = ins_np(LMAX);
   extern __shared__ float dyn[];
-  __shared__ float sY[16][kEdgeChunk];
-  __shared__ float sG[48][kEdgeChunk];
-  __shared__ float su[3][kEdgeChunk];
-  __shared__ float sx[kEdgeChunk];
-  __shared__ int sbase[kEdgeChunk];
-  __shared__ int sj[kEdgeChunk];
+  __shared__ EdgeStage st;
   __shared__ float sF[kEdgeChunk][8][3];
   const int C = m.C, k = threadIdx.x, i = blockIdx.x;
   const int nwarp = C >> 5;
@@ -263,67 +376,51 @@ __global__ void __launch_bounds__(256) k_layer1_rev(DevModel m, EdgeIn in, const
   for (int eb = e0; eb < e1; eb += kEdgeChunk) {
     const int ne = min(kEdgeChunk, e1 - eb);
     __syncthreads();
-    stage_edges<true>(m, in, ti, eb, ne, false, NI, sY, sG, su, sx, sbase, sj);
+    stage_edges_packed(m, in, ti, eb, ne, NI, st);
     __syncthreads();
-    for (int t = 0; t < ne; ++t) {
-      const int base = sbase[t];
-      if (base < 0) {
-        if ((threadIdx.x & 31) == 0) sF[t][threadIdx.x >> 5][0] = sF[t][threadIdx.x >> 5][1] = sF[t][threadIdx.x >> 5][2] = 0.0f;
-        continue;
-      }
-      const int j = sj[t];
-      const float* hj = H1 + static_cast<size_t>(j) * NL2 * C + k;
-      float hv[NL2], hadj[NL2];
+    const int na = st.nact;
+    int a = 0;
+    for (; a + 1 < na; a += 2) {
+      const int t0 = st.act[a], t1 = st.act[a + 1];
+      const int j0 = st.j[t0], j1 = st.j[t1];
+      float h0[NL2], h1[NL2], hadj0[NL2], hadj1[NL2];
 #pragma unroll
       for (int q = 0; q < NL2; ++q) {
-        hv[q] = __ldg(hj + q * C);
-        hadj[q] = 0.0f;
+        h0[q] = __ldg(H1 + (static_cast<size_t>(j0) * NL2 + q) * C + k);
+        h1[q] = __ldg(H1 + (static_cast<size_t>(j1) * NL2 + q) * C + k);
       }
-      float dY[16];
+      float fx0, fy0, fz0, fx1, fy1, fz1;
+      l1_rev_edge<LMAX>(g, m.spl1 + static_cast<size_t>(st.base[t0]) * C + k, C, st.x[t0], st.Y[t0], st.G[t0],
+                        st.u[t0], h0, hadj0, fx0, fy0, fz0);
+      l1_rev_edge<LMAX>(g, m.spl1 + static_cast<size_t>(st.base[t1]) * C + k, C, st.x[t1], st.Y[t1], st.G[t1],
+                        st.u[t1], h1, hadj1, fx1, fy1, fz1);
+      block_reduce3(fx0, fy0, fz0, sF, t0);
+      block_reduce3(fx1, fy1, fz1, sF, t1);
 #pragma unroll
-      for (int q = 0; q < 16; ++q) dY[q] = 0.0f;
-      const float4* cp = m.spl1 + static_cast<size_t>(base) * C + k;
-      const float x = sx[t];
-      float dr = 0.0f;
-      for_each_ins<LMAX>([&](auto qc) {
-        constexpr int q = decltype(qc)::value;
-        constexpr int l1 = ins_l1(LMAX, q), l2 = ins_l2(LMAX, q), p0 = ins_poff(LMAX, q);
-        const float4 cc = __ldg(cp + q * C);
-        const float R = spline_val(cc, x), Rd = spline_der(cc, x);
-        float dRq = 0.0f;
-#pragma unroll
-        for (int a = 0; a < 2 * l1 + 1; ++a) {
-          const float y = sY[l1 * l1 + a][t];
-          float gs = 0.0f;
-#pragma unroll
-          for (int b = 0; b < 2 * l2 + 1; ++b) gs = fmaf(g[p0 + a * (2 * l2 + 1) + b], hv[l2 * l2 + b], gs);
-          dRq = fmaf(gs, y, dRq);
-          dY[l1 * l1 + a] = fmaf(R, gs, dY[l1 * l1 + a]);
-          const float ry = R * y;
-#pragma unroll
-          for (int b = 0; b < 2 * l2 + 1; ++b)
-            hadj[l2 * l2 + b] = fmaf(ry, g[p0 + a * (2 * l2 + 1) + b], hadj[l2 * l2 + b]);
-        }
-        dr = fmaf(dRq, Rd, dr);
-      });
-      float fx = dr * su[0][t], fy = dr * su[1][t], fz = dr * su[2][t];
-#pragma unroll
-      for (int q = 0; q < 16; ++q) {
-        fx = fmaf(dY[q], sG[q][t], fx);
-        fy = fmaf(dY[q], sG[16 + q][t], fy);
-        fz = fmaf(dY[q], sG[32 + q][t], fz);
+      for (int q = 0; q < NL2; ++q) {
+        atomicAdd(H1_adj + (static_cast<size_t>(j0) * NL2 + q) * C + k, hadj0[q]);
+        atomicAdd(H1_adj + (static_cast<size_t>(j1) * NL2 + q) * C + k, hadj1[q]);
       }
-      block_reduce3(fx, fy, fz, sF, t);
-      float* aj = H1_adj + static_cast<size_t>(j) * NL2 * C + k;
+    }
+    if (a < na) {
+      const int t0 = st.act[a], j0 = st.j[t0];
+      float h0[NL2], hadj0[NL2];
 #pragma unroll
-      for (int q = 0; q < NL2; ++q) atomicAdd(aj + q * C, hadj[q]);
+      for (int q = 0; q < NL2; ++q) h0[q] = __ldg(H1 + (static_cast<size_t>(j0) * NL2 + q) * C + k);
+      float fx0, fy0, fz0;
+      l1_rev_edge<LMAX>(g, m.spl1 + static_cast<size_t>(st.base[t0]) * C + k, C, st.x[t0], st.Y[t0], st.G[t0],
+                        st.u[t0], h0, hadj0, fx0, fy0, fz0);
+      block_reduce3(fx0, fy0, fz0, sF, t0);
+#pragma unroll
+      for (int q = 0; q < NL2; ++q) atomicAdd(H1_adj + (static_cast<size_t>(j0) * NL2 + q) * C + k, hadj0[q]);
     }
     __syncthreads();
     for (int t = threadIdx.x; t < ne; t += blockDim.x) {
       double s[3] = {0.0, 0.0, 0.0};
-      for (int w = 0; w < nwarp; ++w)
-        for (int a = 0; a < 3; ++a) s[a] += static_cast<double>(sF[t][w][a]);
-      for (int a = 0; a < 3; ++a) f1[3 * (static_cast<long>(eb) + t) + a] = s[a];
+      if (st.base[t] >= 0)
+        for (int w = 0; w < nwarp; ++w)
+          for (int c = 0; c < 3; ++c) s[c] += static_cast<double>(sF[t][w][c]);
+      for (int c = 0; c < 3; ++c) f1[3 * (static_cast<long>(eb) + t) + c] = s[c];
     }
   }
 }

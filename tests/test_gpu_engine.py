@@ -153,3 +153,49 @@ def test_zbl_model_matches_oracle(engine_lib, tmp_path):
     ref.compute_node_energies_forces(*edge_args(species, nl))
     assert _report("E_i", m.node_energies, ref.node_energies) < E_TOL
     assert _report("f_edge", m.node_forces, ref.node_forces) < F_TOL
+
+
+def _edited_model(src, dst, edit):
+    import json
+    with open(src) as f:
+        m = json.load(f)
+    edit(m)
+    with open(dst, "w") as f:
+        json.dump(m, f)
+    return dst
+
+
+@pytest.mark.parametrize("variant", ["shuffled", "extra_monomial"])
+def test_polynomial_paths(engine_lib, small_model_path, small_golden, tmp_path, variant):
+    """Monomial lists in another order (generated canonical kernels through the loader's
+    mapping) and with a monomial outside the canonical sets (data-driven kernels)."""
+    rng = np.random.default_rng(3)
+
+    def shuffle(m):
+        for LM, monos in m["M0_monomials"].items():
+            perm = rng.permutation(len(monos))
+            m["M0_monomials"][LM] = [monos[p] for p in perm]
+            for s in m["M0_weights"]:
+                for k, c in m["M0_weights"][s][LM].items():
+                    m["M0_weights"][s][LM][k] = [c[p] for p in perm]
+
+    def extra(m):
+        m["M0_monomials"]["0"].append([0, 1, 4])  # parity-odd: not an equivariant term
+        for s in m["M0_weights"]:
+            for k in m["M0_weights"][s]["0"]:
+                m["M0_weights"][s]["0"][k].append(float(rng.normal() * 0.1))
+        m["M1_monomials"].append([2, 3])
+        for s in m["M1_weights"]:
+            for k in m["M1_weights"][s]:
+                m["M1_weights"][s][k].append(float(rng.normal() * 0.1))
+
+    path = _edited_model(small_model_path, str(tmp_path / f"{variant}.json"), shuffle if variant == "shuffled" else extra)
+    g = small_golden
+    species = g["species"].astype(np.int32)
+    nl = {k: g[k] for k in ("num_neigh", "neigh_indices", "xyz", "r")}
+    m = _engine(path)
+    m.compute_node_energies_forces(*edge_args(species, nl))
+    ref = Evaluator(path, "port")
+    ref.compute_node_energies_forces(*edge_args(species, nl))
+    assert _report("E_i", m.node_energies, ref.node_energies) < E_TOL
+    assert _report("f_edge", m.node_forces, ref.node_forces) < F_TOL

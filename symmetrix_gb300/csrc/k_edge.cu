@@ -160,6 +160,78 @@ __global__ void __launch_bounds__(256) k_layer0_fwd(DevModel m, EdgeIn in, float
   }
 }
 
+namespace {
+
+// Edge chunk staged for the layer-1 kernels: Y (and, for the adjoint, dY/dx and the
+// unit vector) packed as float4 rows, the spline row, and the compacted list of
+// active edges (r < r_cut).
+template <bool GRAD>
+struct EdgeStage {
+  float4 Y[kEdgeChunk][4];              // Y_lm, 16 per edge
+  float4 G[GRAD ? kEdgeChunk : 1][12];  // dY_lm/dx, dY_lm/dy, dY_lm/dz
+  float4 u[GRAD ? kEdgeChunk : 1];      // unit vector (w unused)
+  float x[kEdgeChunk];                  // offset inside the spline interval
+  int base[kEdgeChunk];                 // spline row * stride, or -1 (r >= r_cut)
+  int j[kEdgeChunk];
+  int act[kEdgeChunk];                  // compacted list of active edges
+  int nact;
+};
+
+// Stage edges [eb, eb+ne) (ne <= 32, all handled by warp 0) with the unordered
+// species-pair spline rows of layer 1.
+template <bool GRAD>
+__device__ __forceinline__ void stage_edges_packed(const DevModel& m, const EdgeIn& in, int ti, int eb, int ne,
+                                                   int stride, EdgeStage<GRAD>& st) {
+  if (threadIdx.x >= 32) return;
+  const int t = threadIdx.x;
+  bool active = false;
+  if (t < ne) {
+    const long e = static_cast<long>(eb) + t;
+    const float vx = static_cast<float>(in.xyz[3 * e]);
+    const float vy = static_cast<float>(in.xyz[3 * e + 1]);
+    const float vz = static_cast<float>(in.xyz[3 * e + 2]);
+    const float rr = static_cast<float>(in.r[e]);
+    float Y[16], G[GRAD ? 48 : 1];
+    sph_harm16<GRAD>(vx, vy, vz, Y, G);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) st.Y[t][q] = make_float4(Y[4 * q], Y[4 * q + 1], Y[4 * q + 2], Y[4 * q + 3]);
+    if constexpr (GRAD) {
+#pragma unroll
+      for (int q = 0; q < 12; ++q) st.G[t][q] = make_float4(G[4 * q], G[4 * q + 1], G[4 * q + 2], G[4 * q + 3]);
+      const float inv = 1.0f / rr;
+      st.u[t] = make_float4(vx * inv, vy * inv, vz * inv, 0.0f);
+    }
+    int iv = static_cast<int>(rr * m.inv_h);
+    iv = iv < 0 ? 0 : (iv >= m.nint ? m.nint - 1 : iv);
+    st.x[t] = rr - static_cast<float>(iv) * m.h;
+    const int tj = in.ntype_e[e];
+    const int a = ti < tj ? ti : tj, b = ti < tj ? tj : ti;
+    const int pr = a * (2 * m.S - a - 1) / 2 + b;
+    active = rr < m.r_cut;
+    st.base[t] = active ? (pr * m.nint + iv) * stride : -1;
+    st.j[t] = in.nidx[e];
+  }
+  const unsigned ball = __ballot_sync(0xffffffffu, active);
+  if (active) st.act[__popc(ball & ((1u << t) - 1u))] = t;
+  if (t == 0) st.nact = __popc(ball);
+}
+
+// Gather the spline row (NI float4 cubics) and neighbour features (NL2 floats) of
+// active edge a of the staged chunk for channel k.
+template <int NI, int NL2, bool GRAD>
+__device__ __forceinline__ void fetch_edge(const DevModel& m, const float* __restrict__ H1, const EdgeStage<GRAD>& st,
+                                           int a, int C, int k, float4* c, float* h) {
+  const int t = st.act[a];
+  const float4* cp = m.spl1 + static_cast<size_t>(st.base[t]) * C + k;
+#pragma unroll
+  for (int q = 0; q < NI; ++q) c[q] = __ldg(cp + q * C);
+  const float* hj = H1 + static_cast<size_t>(st.j[t]) * NL2 * C + k;
+#pragma unroll
+  for (int q = 0; q < NL2; ++q) h[q] = __ldg(hj + q * C);
+}
+
+}  // namespace
+
 // ---------------------------------------------------------------------------
 // Layer 1 forward: Phi1r[i,p,k] = sum_j R1_q(r_ij)[k] Y_{l1 m1}(x_ij) H1[j, l2 m2, k]
 // accumulated in registers (p = (instruction, m1, m2), canonical order), then
@@ -172,10 +244,7 @@ __global__ void __launch_bounds__(256) k_layer1_fwd(DevModel m, EdgeIn in, const
   constexpr int NI = ins_count(LMAX);
   constexpr int NP = ins_np(LMAX);
   extern __shared__ float dyn[];
-  __shared__ float sY[16][kEdgeChunk];
-  __shared__ float sx[kEdgeChunk];
-  __shared__ int sbase[kEdgeChunk];
-  __shared__ int sj[kEdgeChunk];
+  __shared__ EdgeStage<false> st;
   const int C = m.C, k = threadIdx.x, i = blockIdx.x;
   const int ti = in.node_type[i];
   const int e0 = in.first[i], e1 = in.first[i + 1];
@@ -185,27 +254,30 @@ __global__ void __launch_bounds__(256) k_layer1_fwd(DevModel m, EdgeIn in, const
   for (int eb = e0; eb < e1; eb += kEdgeChunk) {
     const int ne = min(kEdgeChunk, e1 - eb);
     __syncthreads();
-    stage_edges<false>(m, in, ti, eb, ne, false, NI, sY, nullptr, nullptr, sx, sbase, sj);
+    stage_edges_packed<false>(m, in, ti, eb, ne, NI, st);
     __syncthreads();
-    for (int t = 0; t < ne; ++t) {
-      const int base = sbase[t];
-      if (base < 0) continue;
-      const float* hj = H1 + static_cast<size_t>(sj[t]) * NL2 * C + k;
+    // (the accumulators leave no registers for a prefetch of the next edge: residency
+    // of four blocks per SM hides the gather latency instead)
+    const int na = st.nact;
+    for (int a = 0; a < na; ++a) {
+      const int t = st.act[a];
+      const float x = st.x[t];
       float hv[NL2];
+      const float* hj = H1 + static_cast<size_t>(st.j[t]) * NL2 * C + k;
 #pragma unroll
       for (int q = 0; q < NL2; ++q) hv[q] = __ldg(hj + q * C);
-      const float4* cp = m.spl1 + static_cast<size_t>(base) * C + k;
-      const float x = sx[t];
+      const float4* cp = m.spl1 + static_cast<size_t>(st.base[t]) * C + k;
+      const float* Y = reinterpret_cast<const float*>(st.Y[t]);
       for_each_ins<LMAX>([&](auto qc) {
         constexpr int q = decltype(qc)::value;
         constexpr int l1 = ins_l1(LMAX, q), l2 = ins_l2(LMAX, q), p0 = ins_poff(LMAX, q);
         const float R = spline_val(__ldg(cp + q * C), x);
 #pragma unroll
-        for (int a = 0; a < 2 * l1 + 1; ++a) {
-          const float ry = R * sY[l1 * l1 + a][t];
+        for (int a1 = 0; a1 < 2 * l1 + 1; ++a1) {
+          const float ry = R * Y[l1 * l1 + a1];
 #pragma unroll
           for (int b = 0; b < 2 * l2 + 1; ++b)
-            acc[p0 + a * (2 * l2 + 1) + b] = fmaf(ry, hv[l2 * l2 + b], acc[p0 + a * (2 * l2 + 1) + b]);
+            acc[p0 + a1 * (2 * l2 + 1) + b] = fmaf(ry, hv[l2 * l2 + b], acc[p0 + a1 * (2 * l2 + 1) + b]);
         }
       });
     }
@@ -233,58 +305,11 @@ __global__ void __launch_bounds__(256) k_layer1_fwd(DevModel m, EdgeIn in, const
 // ---------------------------------------------------------------------------
 namespace {
 
-struct EdgeStage {
-  float4 Y[kEdgeChunk][4];    // Y_lm, 16 per edge
-  float4 G[kEdgeChunk][12];   // dY_lm/dx, dY_lm/dy, dY_lm/dz
-  float4 u[kEdgeChunk];       // unit vector (w unused)
-  float x[kEdgeChunk];        // offset inside the spline interval
-  int base[kEdgeChunk];       // spline row * stride, or -1 (r >= r_cut)
-  int j[kEdgeChunk];
-  int act[kEdgeChunk];        // compacted list of active edges
-  int nact;
-};
-
-// Stage edges [eb, eb+ne) (ne <= 32, all handled by warp 0) with Y and dY/dx packed
-// as float4 rows, and compact the active ones.
-__device__ __forceinline__ void stage_edges_packed(const DevModel& m, const EdgeIn& in, int ti, int eb, int ne,
-                                                   int stride, EdgeStage& st) {
-  if (threadIdx.x >= 32) return;
-  const int t = threadIdx.x;
-  bool active = false;
-  if (t < ne) {
-    const long e = static_cast<long>(eb) + t;
-    const float vx = static_cast<float>(in.xyz[3 * e]);
-    const float vy = static_cast<float>(in.xyz[3 * e + 1]);
-    const float vz = static_cast<float>(in.xyz[3 * e + 2]);
-    const float rr = static_cast<float>(in.r[e]);
-    float Y[16], G[48];
-    sph_harm16<true>(vx, vy, vz, Y, G);
-#pragma unroll
-    for (int q = 0; q < 4; ++q) st.Y[t][q] = make_float4(Y[4 * q], Y[4 * q + 1], Y[4 * q + 2], Y[4 * q + 3]);
-#pragma unroll
-    for (int q = 0; q < 12; ++q) st.G[t][q] = make_float4(G[4 * q], G[4 * q + 1], G[4 * q + 2], G[4 * q + 3]);
-    const float inv = 1.0f / rr;
-    st.u[t] = make_float4(vx * inv, vy * inv, vz * inv, 0.0f);
-    int iv = static_cast<int>(rr * m.inv_h);
-    iv = iv < 0 ? 0 : (iv >= m.nint ? m.nint - 1 : iv);
-    st.x[t] = rr - static_cast<float>(iv) * m.h;
-    const int tj = in.ntype_e[e];
-    const int a = ti < tj ? ti : tj, b = ti < tj ? tj : ti;
-    const int pr = a * (2 * m.S - a - 1) / 2 + b;
-    active = rr < m.r_cut;
-    st.base[t] = active ? (pr * m.nint + iv) * stride : -1;
-    st.j[t] = in.nidx[e];
-  }
-  const unsigned ball = __ballot_sync(0xffffffffu, active);
-  if (active) st.act[__popc(ball & ((1u << t) - 1u))] = t;
-  if (t == 0) st.nact = __popc(ball);
-}
-
 // One edge of the layer-1 adjoint for this thread's channel.
 template <int LMAX>
-__device__ __forceinline__ void l1_rev_edge(const float* g, const float4* __restrict__ cp, int C, float x,
-                                            const float4* Yrow, const float4* Grow, float4 u, const float* hv,
-                                            float* hadj, float& fx, float& fy, float& fz) {
+__device__ __forceinline__ void l1_rev_edge(const float* g, const float* Rv, const float* Rdv, const float4* Yrow,
+                                            const float4* Grow, float4 u, const float* hv, float* hadj, float& fx,
+                                            float& fy, float& fz) {
   constexpr int NL2 = (LMAX + 1) * (LMAX + 1);
   float Y[16];
 #pragma unroll
@@ -302,8 +327,7 @@ __device__ __forceinline__ void l1_rev_edge(const float* g, const float4* __rest
   for_each_ins<LMAX>([&](auto qc) {
     constexpr int q = decltype(qc)::value;
     constexpr int l1 = ins_l1(LMAX, q), l2 = ins_l2(LMAX, q), p0 = ins_poff(LMAX, q);
-    const float4 cc = __ldg(cp + q * C);
-    const float R = spline_val(cc, x), Rd = spline_der(cc, x);
+    const float R = Rv[q], Rd = Rdv[q];
     float dRq = 0.0f;
 #pragma unroll
     for (int a = 0; a < 2 * l1 + 1; ++a) {
@@ -353,7 +377,7 @@ __global__ void __launch_bounds__(256) k_layer1_rev(DevModel m, EdgeIn in, const
   constexpr int NI = ins_count(LMAX);
   constexpr int NP = ins_np(LMAX);
   extern __shared__ float dyn[];
-  __shared__ EdgeStage st;
+  __shared__ EdgeStage<true> st;
   __shared__ float sF[kEdgeChunk][8][3];
   const int C = m.C, k = threadIdx.x, i = blockIdx.x;
   const int nwarp = C >> 5;
@@ -376,43 +400,35 @@ __global__ void __launch_bounds__(256) k_layer1_rev(DevModel m, EdgeIn in, const
   for (int eb = e0; eb < e1; eb += kEdgeChunk) {
     const int ne = min(kEdgeChunk, e1 - eb);
     __syncthreads();
-    stage_edges_packed(m, in, ti, eb, ne, NI, st);
+    stage_edges_packed<true>(m, in, ti, eb, ne, NI, st);
     __syncthreads();
+    // Active edges one at a time.  The spline row of an edge is reduced to R and R'
+    // first; the gathers of the next edge's spline row and neighbour features are then
+    // issued into the freed registers, so their L2 latency overlaps the rest of this
+    // edge's arithmetic.
     const int na = st.nact;
-    int a = 0;
-    for (; a + 1 < na; a += 2) {
-      const int t0 = st.act[a], t1 = st.act[a + 1];
-      const int j0 = st.j[t0], j1 = st.j[t1];
-      float h0[NL2], h1[NL2], hadj0[NL2], hadj1[NL2];
+    float4 c[NI];
+    float h[NL2];
+    if (na > 0) fetch_edge<NI, NL2>(m, H1, st, 0, C, k, c, h);
+    for (int a = 0; a < na; ++a) {
+      const int t = st.act[a];
+      const float x = st.x[t];
+      float R[NI], Rd[NI], hv[NL2];
 #pragma unroll
-      for (int q = 0; q < NL2; ++q) {
-        h0[q] = __ldg(H1 + (static_cast<size_t>(j0) * NL2 + q) * C + k);
-        h1[q] = __ldg(H1 + (static_cast<size_t>(j1) * NL2 + q) * C + k);
+      for (int q = 0; q < NI; ++q) {
+        R[q] = spline_val(c[q], x);
+        Rd[q] = spline_der(c[q], x);
       }
-      float fx0, fy0, fz0, fx1, fy1, fz1;
-      l1_rev_edge<LMAX>(g, m.spl1 + static_cast<size_t>(st.base[t0]) * C + k, C, st.x[t0], st.Y[t0], st.G[t0],
-                        st.u[t0], h0, hadj0, fx0, fy0, fz0);
-      l1_rev_edge<LMAX>(g, m.spl1 + static_cast<size_t>(st.base[t1]) * C + k, C, st.x[t1], st.Y[t1], st.G[t1],
-                        st.u[t1], h1, hadj1, fx1, fy1, fz1);
-      block_reduce3(fx0, fy0, fz0, sF, t0);
-      block_reduce3(fx1, fy1, fz1, sF, t1);
 #pragma unroll
-      for (int q = 0; q < NL2; ++q) {
-        atomicAdd(H1_adj + (static_cast<size_t>(j0) * NL2 + q) * C + k, hadj0[q]);
-        atomicAdd(H1_adj + (static_cast<size_t>(j1) * NL2 + q) * C + k, hadj1[q]);
-      }
-    }
-    if (a < na) {
-      const int t0 = st.act[a], j0 = st.j[t0];
-      float h0[NL2], hadj0[NL2];
+      for (int q = 0; q < NL2; ++q) hv[q] = h[q];
+      const int j = st.j[t];
+      if (a + 1 < na) fetch_edge<NI, NL2>(m, H1, st, a + 1, C, k, c, h);
+      float hadj[NL2], fx, fy, fz;
+      l1_rev_edge<LMAX>(g, R, Rd, st.Y[t], st.G[t], st.u[t], hv, hadj, fx, fy, fz);
+      block_reduce3(fx, fy, fz, sF, t);
+      float* dst = H1_adj + static_cast<size_t>(j) * NL2 * C + k;
 #pragma unroll
-      for (int q = 0; q < NL2; ++q) h0[q] = __ldg(H1 + (static_cast<size_t>(j0) * NL2 + q) * C + k);
-      float fx0, fy0, fz0;
-      l1_rev_edge<LMAX>(g, m.spl1 + static_cast<size_t>(st.base[t0]) * C + k, C, st.x[t0], st.Y[t0], st.G[t0],
-                        st.u[t0], h0, hadj0, fx0, fy0, fz0);
-      block_reduce3(fx0, fy0, fz0, sF, t0);
-#pragma unroll
-      for (int q = 0; q < NL2; ++q) atomicAdd(H1_adj + (static_cast<size_t>(j0) * NL2 + q) * C + k, hadj0[q]);
+      for (int q = 0; q < NL2; ++q) atomicAdd(dst + q * C, hadj[q]);
     }
     __syncthreads();
     for (int t = threadIdx.x; t < ne; t += blockDim.x) {

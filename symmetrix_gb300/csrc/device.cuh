@@ -17,7 +17,8 @@ struct DevModel {
   int poly_canon;  // coefficients in canonical order: use the generated polynomials
   float h, inv_h, r_cut, ro2_scale;
   const float4* spl0;  // [S*S][nint][4][C]
-  const float4* spl1;  // [npairs][nint][n_instr][C]
+  const float4* spl1;      // [npairs][nint][n_instr][2][C/2]: channel-pair planes (adjoint)
+  const float4* spl1_fwd;  // [npairs][nint][n_instr][C]: per-channel cubics (forward)
   const int* mono0;
   int mono0_off[10];
   const float* coef0;  // [S][nLM][T0][C]

@@ -90,6 +90,7 @@ struct smx_engine {
     m.ro2_scale = pm.ro2_scale;
     m.spl0 = reinterpret_cast<const float4*>(upload(pm.spl0));
     m.spl1 = reinterpret_cast<const float4*>(upload(pm.spl1));
+    m.spl1_fwd = reinterpret_cast<const float4*>(upload(pm.spl1_fwd));
     m.mono0 = upload(pm.mono0);
     for (int q = 0; q < 10; ++q) m.mono0_off[q] = q < static_cast<int>(pm.mono0_off.size()) ? pm.mono0_off[q] : pm.mono0_off.back();
     m.coef0 = upload(pm.coef0);

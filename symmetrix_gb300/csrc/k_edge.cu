@@ -11,8 +11,6 @@
 //
 // Reference stages restated here (libsymmetrix/source/mace.cpp):
 //   k_layer0_fwd : compute_Y + compute_R0 + compute_A0 (:66-201) + compute_M0 (:348-370)
-//   k_layer1_fwd : compute_R1 + compute_Phi1 (:92-116, :453-502)
-//   k_layer1_rev : reverse_Phi1 (:504-605)
 //   k_layer0_rev : reverse_M0 + reverse_A0 (:372-395, :203-271)
 #include <cuda_runtime.h>
 
@@ -160,287 +158,6 @@ __global__ void __launch_bounds__(256) k_layer0_fwd(DevModel m, EdgeIn in, float
   }
 }
 
-namespace {
-
-// Edge chunk staged for the layer-1 kernels: Y (and, for the adjoint, dY/dx and the
-// unit vector) packed as float4 rows, the spline row, and the compacted list of
-// active edges (r < r_cut).
-template <bool GRAD>
-struct EdgeStage {
-  float4 Y[kEdgeChunk][4];              // Y_lm, 16 per edge
-  float4 G[GRAD ? kEdgeChunk : 1][12];  // dY_lm/dx, dY_lm/dy, dY_lm/dz
-  float4 u[GRAD ? kEdgeChunk : 1];      // unit vector (w unused)
-  float x[kEdgeChunk];                  // offset inside the spline interval
-  int base[kEdgeChunk];                 // spline row * stride, or -1 (r >= r_cut)
-  int j[kEdgeChunk];
-  int act[kEdgeChunk];                  // compacted list of active edges
-  int nact;
-};
-
-// Stage edges [eb, eb+ne) (ne <= 32, all handled by warp 0) with the unordered
-// species-pair spline rows of layer 1.
-template <bool GRAD>
-__device__ __forceinline__ void stage_edges_packed(const DevModel& m, const EdgeIn& in, int ti, int eb, int ne,
-                                                   int stride, EdgeStage<GRAD>& st) {
-  if (threadIdx.x >= 32) return;
-  const int t = threadIdx.x;
-  bool active = false;
-  if (t < ne) {
-    const long e = static_cast<long>(eb) + t;
-    const float vx = static_cast<float>(in.xyz[3 * e]);
-    const float vy = static_cast<float>(in.xyz[3 * e + 1]);
-    const float vz = static_cast<float>(in.xyz[3 * e + 2]);
-    const float rr = static_cast<float>(in.r[e]);
-    float Y[16], G[GRAD ? 48 : 1];
-    sph_harm16<GRAD>(vx, vy, vz, Y, G);
-#pragma unroll
-    for (int q = 0; q < 4; ++q) st.Y[t][q] = make_float4(Y[4 * q], Y[4 * q + 1], Y[4 * q + 2], Y[4 * q + 3]);
-    if constexpr (GRAD) {
-#pragma unroll
-      for (int q = 0; q < 12; ++q) st.G[t][q] = make_float4(G[4 * q], G[4 * q + 1], G[4 * q + 2], G[4 * q + 3]);
-      const float inv = 1.0f / rr;
-      st.u[t] = make_float4(vx * inv, vy * inv, vz * inv, 0.0f);
-    }
-    int iv = static_cast<int>(rr * m.inv_h);
-    iv = iv < 0 ? 0 : (iv >= m.nint ? m.nint - 1 : iv);
-    st.x[t] = rr - static_cast<float>(iv) * m.h;
-    const int tj = in.ntype_e[e];
-    const int a = ti < tj ? ti : tj, b = ti < tj ? tj : ti;
-    const int pr = a * (2 * m.S - a - 1) / 2 + b;
-    active = rr < m.r_cut;
-    st.base[t] = active ? (pr * m.nint + iv) * stride : -1;
-    st.j[t] = in.nidx[e];
-  }
-  const unsigned ball = __ballot_sync(0xffffffffu, active);
-  if (active) st.act[__popc(ball & ((1u << t) - 1u))] = t;
-  if (t == 0) st.nact = __popc(ball);
-}
-
-// Gather the spline row (NI float4 cubics) and neighbour features (NL2 floats) of
-// active edge a of the staged chunk for channel k.
-template <int NI, int NL2, bool GRAD>
-__device__ __forceinline__ void fetch_edge(const DevModel& m, const float* __restrict__ H1, const EdgeStage<GRAD>& st,
-                                           int a, int C, int k, float4* c, float* h) {
-  const int t = st.act[a];
-  const float4* cp = m.spl1 + static_cast<size_t>(st.base[t]) * C + k;
-#pragma unroll
-  for (int q = 0; q < NI; ++q) c[q] = __ldg(cp + q * C);
-  const float* hj = H1 + static_cast<size_t>(st.j[t]) * NL2 * C + k;
-#pragma unroll
-  for (int q = 0; q < NL2; ++q) h[q] = __ldg(hj + q * C);
-}
-
-}  // namespace
-
-// ---------------------------------------------------------------------------
-// Layer 1 forward: Phi1r[i,p,k] = sum_j R1_q(r_ij)[k] Y_{l1 m1}(x_ij) H1[j, l2 m2, k]
-// accumulated in registers (p = (instruction, m1, m2), canonical order), then
-// Phi1[i,lme,k] = sum_p CG[lme,p] Phi1r[i,p,k].
-// ---------------------------------------------------------------------------
-template <int LMAX>
-__global__ void __launch_bounds__(256) k_layer1_fwd(DevModel m, EdgeIn in, const float* __restrict__ H1,
-                                                    float* __restrict__ Phi1) {
-  constexpr int NL2 = (LMAX + 1) * (LMAX + 1);
-  constexpr int NI = ins_count(LMAX);
-  constexpr int NP = ins_np(LMAX);
-  extern __shared__ float dyn[];
-  __shared__ EdgeStage<false> st;
-  const int C = m.C, k = threadIdx.x, i = blockIdx.x;
-  const int ti = in.node_type[i];
-  const int e0 = in.first[i], e1 = in.first[i + 1];
-  float acc[NP];
-#pragma unroll
-  for (int p = 0; p < NP; ++p) acc[p] = 0.0f;
-  for (int eb = e0; eb < e1; eb += kEdgeChunk) {
-    const int ne = min(kEdgeChunk, e1 - eb);
-    __syncthreads();
-    stage_edges_packed<false>(m, in, ti, eb, ne, NI, st);
-    __syncthreads();
-    // (the accumulators leave no registers for a prefetch of the next edge: residency
-    // of four blocks per SM hides the gather latency instead)
-    const int na = st.nact;
-    for (int a = 0; a < na; ++a) {
-      const int t = st.act[a];
-      const float x = st.x[t];
-      float hv[NL2];
-      const float* hj = H1 + static_cast<size_t>(st.j[t]) * NL2 * C + k;
-#pragma unroll
-      for (int q = 0; q < NL2; ++q) hv[q] = __ldg(hj + q * C);
-      const float4* cp = m.spl1 + static_cast<size_t>(st.base[t]) * C + k;
-      const float* Y = reinterpret_cast<const float*>(st.Y[t]);
-      for_each_ins<LMAX>([&](auto qc) {
-        constexpr int q = decltype(qc)::value;
-        constexpr int l1 = ins_l1(LMAX, q), l2 = ins_l2(LMAX, q), p0 = ins_poff(LMAX, q);
-        const float R = spline_val(__ldg(cp + q * C), x);
-#pragma unroll
-        for (int a1 = 0; a1 < 2 * l1 + 1; ++a1) {
-          const float ry = R * Y[l1 * l1 + a1];
-#pragma unroll
-          for (int b = 0; b < 2 * l2 + 1; ++b)
-            acc[p0 + a1 * (2 * l2 + 1) + b] = fmaf(ry, hv[l2 * l2 + b], acc[p0 + a1 * (2 * l2 + 1) + b]);
-        }
-      });
-    }
-  }
-  float* sP = dyn;  // [NP][C]: this thread's Phi1r column
-#pragma unroll
-  for (int p = 0; p < NP; ++p) sP[p * C + k] = acc[p];
-  for (int lme = 0; lme < m.n_lme; ++lme) {
-    float s = 0.0f;
-    const int g1 = __ldg(m.cg_fwd_off + lme + 1);
-    for (int g = __ldg(m.cg_fwd_off + lme); g < g1; ++g) s = fmaf(__ldg(m.cg_fwd_v + g), sP[__ldg(m.cg_fwd_p + g) * C + k], s);
-    Phi1[(static_cast<size_t>(i) * m.n_lme + lme) * C + k] = s;
-  }
-}
-
-// ---------------------------------------------------------------------------
-// Layer 1 adjoint.  g[p] = sum_lme CG[lme,p] dPhi1[i,lme,k]; per edge:
-//   dE/dx_ij += sum_k sum_p g_p h_{m2} (R1'_q(r) u Y_{m1} + R1_q(r) dY_{m1}/dx)
-//   H1_adj[j, l2 m2, k] += sum_p R1_q(r) Y_{m1} g_p        (atomic scatter)
-// f1[e] receives dE/dx_ij from this layer.
-//
-// Edges of a chunk are compacted to the active ones (r < r_cut) and processed two at
-// a time: the two edges' dependent FMA chains interleave, which is what keeps the FMA
-// pipe busy at the two resident warps per scheduler the register budget allows.
-// ---------------------------------------------------------------------------
-namespace {
-
-// One edge of the layer-1 adjoint for this thread's channel.
-template <int LMAX>
-__device__ __forceinline__ void l1_rev_edge(const float* g, const float* Rv, const float* Rdv, const float4* Yrow,
-                                            const float4* Grow, float4 u, const float* hv, float* hadj, float& fx,
-                                            float& fy, float& fz) {
-  constexpr int NL2 = (LMAX + 1) * (LMAX + 1);
-  float Y[16];
-#pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const float4 v = Yrow[q];
-    Y[4 * q] = v.x; Y[4 * q + 1] = v.y; Y[4 * q + 2] = v.z; Y[4 * q + 3] = v.w;
-  }
-  float dY[16];
-#pragma unroll
-  for (int q = 0; q < 16; ++q) dY[q] = 0.0f;
-  float hA[NL2], hB[NL2];  // two partial sums per H1_adj component (shorter chains)
-#pragma unroll
-  for (int q = 0; q < NL2; ++q) hA[q] = hB[q] = 0.0f;
-  float drA = 0.0f, drB = 0.0f;
-  for_each_ins<LMAX>([&](auto qc) {
-    constexpr int q = decltype(qc)::value;
-    constexpr int l1 = ins_l1(LMAX, q), l2 = ins_l2(LMAX, q), p0 = ins_poff(LMAX, q);
-    const float R = Rv[q], Rd = Rdv[q];
-    float dRq = 0.0f;
-#pragma unroll
-    for (int a = 0; a < 2 * l1 + 1; ++a) {
-      const float y = Y[l1 * l1 + a];
-      float gs = 0.0f;
-#pragma unroll
-      for (int b = 0; b < 2 * l2 + 1; ++b) gs = fmaf(g[p0 + a * (2 * l2 + 1) + b], hv[l2 * l2 + b], gs);
-      dRq = fmaf(gs, y, dRq);
-      dY[l1 * l1 + a] = fmaf(R, gs, dY[l1 * l1 + a]);
-      const float ry = R * y;
-#pragma unroll
-      for (int b = 0; b < 2 * l2 + 1; ++b) {
-        if ((q + a) & 1)
-          hB[l2 * l2 + b] = fmaf(ry, g[p0 + a * (2 * l2 + 1) + b], hB[l2 * l2 + b]);
-        else
-          hA[l2 * l2 + b] = fmaf(ry, g[p0 + a * (2 * l2 + 1) + b], hA[l2 * l2 + b]);
-      }
-    }
-    if (q & 1) drB = fmaf(dRq, Rd, drB);
-    else drA = fmaf(dRq, Rd, drA);
-  });
-#pragma unroll
-  for (int q = 0; q < NL2; ++q) hadj[q] = hA[q] + hB[q];
-  const float dr = drA + drB;
-  float ax = dr * u.x, ay = dr * u.y, az = dr * u.z;
-  float bx = 0.0f, by = 0.0f, bz = 0.0f;
-#pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const float4 gx = Grow[q], gy = Grow[4 + q], gz = Grow[8 + q];
-    ax = fmaf(dY[4 * q], gx.x, ax); ay = fmaf(dY[4 * q], gy.x, ay); az = fmaf(dY[4 * q], gz.x, az);
-    bx = fmaf(dY[4 * q + 1], gx.y, bx); by = fmaf(dY[4 * q + 1], gy.y, by); bz = fmaf(dY[4 * q + 1], gz.y, bz);
-    ax = fmaf(dY[4 * q + 2], gx.z, ax); ay = fmaf(dY[4 * q + 2], gy.z, ay); az = fmaf(dY[4 * q + 2], gz.z, az);
-    bx = fmaf(dY[4 * q + 3], gx.w, bx); by = fmaf(dY[4 * q + 3], gy.w, by); bz = fmaf(dY[4 * q + 3], gz.w, bz);
-  }
-  fx = ax + bx;
-  fy = ay + by;
-  fz = az + bz;
-}
-
-}  // namespace
-
-template <int LMAX>
-__global__ void __launch_bounds__(256) k_layer1_rev(DevModel m, EdgeIn in, const float* __restrict__ H1,
-                                                    const float* __restrict__ dPhi1, float* __restrict__ H1_adj,
-                                                    double* __restrict__ f1) {
-  constexpr int NL2 = (LMAX + 1) * (LMAX + 1);
-  constexpr int NI = ins_count(LMAX);
-  constexpr int NP = ins_np(LMAX);
-  extern __shared__ float dyn[];
-  __shared__ EdgeStage<true> st;
-  __shared__ float sF[kEdgeChunk][8][3];
-  const int C = m.C, k = threadIdx.x, i = blockIdx.x;
-  const int nwarp = C >> 5;
-  const int ti = in.node_type[i];
-  const int e0 = in.first[i], e1 = in.first[i + 1];
-  // g[p] = sum_lme CG[lme,p] dPhi1[i,lme,k], formed in this thread's shared-memory
-  // column (data-driven indices) and then moved to registers with constant indices
-  float* sD = dyn;                 // [n_lme][C]
-  float* sP = dyn + m.n_lme * C;   // [NP][C]
-  for (int lme = 0; lme < m.n_lme; ++lme) sD[lme * C + k] = dPhi1[(static_cast<size_t>(i) * m.n_lme + lme) * C + k];
-  for (int p = 0; p < NP; ++p) {
-    float s = 0.0f;
-    const int q1 = __ldg(m.cg_rev_off + p + 1);
-    for (int q = __ldg(m.cg_rev_off + p); q < q1; ++q) s = fmaf(__ldg(m.cg_rev_v + q), sD[__ldg(m.cg_rev_lme + q) * C + k], s);
-    sP[p * C + k] = s;
-  }
-  float g[NP];
-#pragma unroll
-  for (int p = 0; p < NP; ++p) g[p] = sP[p * C + k];
-  for (int eb = e0; eb < e1; eb += kEdgeChunk) {
-    const int ne = min(kEdgeChunk, e1 - eb);
-    __syncthreads();
-    stage_edges_packed<true>(m, in, ti, eb, ne, NI, st);
-    __syncthreads();
-    // Active edges one at a time.  The spline row of an edge is reduced to R and R'
-    // first; the gathers of the next edge's spline row and neighbour features are then
-    // issued into the freed registers, so their L2 latency overlaps the rest of this
-    // edge's arithmetic.
-    const int na = st.nact;
-    float4 c[NI];
-    float h[NL2];
-    if (na > 0) fetch_edge<NI, NL2>(m, H1, st, 0, C, k, c, h);
-    for (int a = 0; a < na; ++a) {
-      const int t = st.act[a];
-      const float x = st.x[t];
-      float R[NI], Rd[NI], hv[NL2];
-#pragma unroll
-      for (int q = 0; q < NI; ++q) {
-        R[q] = spline_val(c[q], x);
-        Rd[q] = spline_der(c[q], x);
-      }
-#pragma unroll
-      for (int q = 0; q < NL2; ++q) hv[q] = h[q];
-      const int j = st.j[t];
-      if (a + 1 < na) fetch_edge<NI, NL2>(m, H1, st, a + 1, C, k, c, h);
-      float hadj[NL2], fx, fy, fz;
-      l1_rev_edge<LMAX>(g, R, Rd, st.Y[t], st.G[t], st.u[t], hv, hadj, fx, fy, fz);
-      block_reduce3(fx, fy, fz, sF, t);
-      float* dst = H1_adj + static_cast<size_t>(j) * NL2 * C + k;
-#pragma unroll
-      for (int q = 0; q < NL2; ++q) atomicAdd(dst + q * C, hadj[q]);
-    }
-    __syncthreads();
-    for (int t = threadIdx.x; t < ne; t += blockDim.x) {
-      double s[3] = {0.0, 0.0, 0.0};
-      if (st.base[t] >= 0)
-        for (int w = 0; w < nwarp; ++w)
-          for (int c = 0; c < 3; ++c) s[c] += static_cast<double>(sF[t][w][c]);
-      for (int c = 0; c < 3; ++c) f1[3 * (static_cast<long>(eb) + t) + c] = s[c];
-    }
-  }
-}
-
 // ---------------------------------------------------------------------------
 // Layer-0 contraction adjoint (mace.cpp:372-395):
 //   A0_adj[i,:,k] = sum_LM M0_adj[i,LM,k] grad P_{ti,LM,k}(A0[i,:,k]).
@@ -575,31 +292,12 @@ __global__ void __launch_bounds__(256) k_layer0_rev(DevModel m, EdgeIn in, const
 // ---------------------------------------------------------------------------
 // Dynamic shared memory above 48 KB must be opted into once per kernel (outside
 // any stream capture).
-cudaError_t init_edge_kernels(const DevModel& m) {
-  cudaError_t e = cudaFuncSetAttribute(k_layer1_fwd<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       static_cast<int>(sizeof(float) * ins_np(1) * m.C));
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_layer1_rev<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              static_cast<int>(sizeof(float) * (m.n_lme + ins_np(1)) * m.C));
-}
+cudaError_t init_edge_kernels(const DevModel& m) { return init_layer1_kernels(m); }
 
 void launch_layer0_fwd(const DevModel& m, const EdgeIn& in, float* A0, float* M0, float* zbl_e, cudaStream_t s) {
   if (in.N <= 0) return;
   const size_t smem = 17 * sizeof(float) * m.C;
   k_layer0_fwd<<<in.N, m.C, smem, s>>>(m, in, A0, M0, zbl_e);
-}
-
-void launch_layer1_fwd(const DevModel& m, const EdgeIn& in, const float* H1, float* Phi1, cudaStream_t s) {
-  if (in.N <= 0) return;
-  const size_t smem = sizeof(float) * ins_np(1) * m.C;
-  k_layer1_fwd<1><<<in.N, m.C, smem, s>>>(m, in, H1, Phi1);
-}
-
-void launch_layer1_rev(const DevModel& m, const EdgeIn& in, const float* H1, const float* dPhi1, float* H1_adj,
-                       double* f1, cudaStream_t s) {
-  if (in.N <= 0) return;
-  const size_t smem = sizeof(float) * (m.n_lme + ins_np(1)) * m.C;
-  k_layer1_rev<1><<<in.N, m.C, smem, s>>>(m, in, H1, dPhi1, H1_adj, f1);
 }
 
 void launch_layer0_rev(const DevModel& m, const EdgeIn& in, const float* A0, const float* M0_adj, const double* f1,

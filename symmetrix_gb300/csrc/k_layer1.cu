@@ -1,0 +1,485 @@
+// Layer-1 edge kernels: the tensor-product neighbour sum and its adjoint.
+//
+// Reference stages restated here (libsymmetrix/source/mace.cpp):
+//   k_layer1_fwd : compute_R1 + compute_Phi1 (:92-116, :453-502)
+//   k_layer1_rev : reverse_Phi1 (:504-605)
+//
+// The adjoint (the costlier kernel): one thread block per centre node i.  A thread owns a channel pair (2c, 2c+1) and
+// one half of the layer-1 instructions: the block is two groups of HW threads
+// (HW = C/2 rounded up to a warp), group 0 runs the instructions of half 0 and
+// group 1 those of half 1, so the split is warp-uniform.  All per-channel
+// arithmetic is on float2 pairs with the packed FP32 FMA of sm_100 and later
+// (__ffma2_rn: two IEEE single-precision FMAs per issued instruction).  These kernels
+// are issue-bound, so the packed form halves their instruction stream, and the
+// instruction split halves the per-thread footprint of the CG-contracted adjoint g.
+//
+// Spline rows of layer 1 are packed for channel pairs (model.cpp): for each
+// instruction, two planes of C/2 float4: plane 0 = (c0, c0', c1, c1') and plane 1 =
+// (c2, c2', c3, c3'), ' marking the odd channel of the pair, so that every cubic
+// coefficient pair is one aligned float2 operand.
+#include <cuda_runtime.h>
+
+#include "device.cuh"
+#include "kernels.h"
+
+namespace smx {
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Instruction halves for L_max = 1 (canonical instruction order, see ins_l1/ins_l2):
+// {1, 6, 7, 8} and {0, 2, 3, 4, 5, 9}.  Chosen by exhaustive search over the 2^10
+// splits for equal packed-FMA work per edge (spline + per-row terms: 212 vs 210) and
+// near-equal CG path counts (46 vs 42 register pairs).
+// ---------------------------------------------------------------------------
+__host__ __device__ constexpr int half_count(int H) { return H == 0 ? 4 : 6; }
+__host__ __device__ constexpr int half_ins(int H, int i) {
+  constexpr int h0[4] = {1, 6, 7, 8};
+  constexpr int h1[6] = {0, 2, 3, 4, 5, 9};
+  return H == 0 ? h0[i] : h1[i];
+}
+// number of CG paths (l1 m1, l2 m2) of instruction q
+__host__ __device__ constexpr int ins_paths(int LMAX, int q) {
+  return (2 * ins_l1(LMAX, q) + 1) * (2 * ins_l2(LMAX, q) + 1);
+}
+// offset of the i-th instruction of half H inside the half's path list
+template <int LMAX, int H>
+__host__ __device__ constexpr int half_goff(int i) {
+  int s = 0;
+  for (int w = 0; w < i; ++w) s += ins_paths(LMAX, half_ins(H, w));
+  return s;
+}
+template <int LMAX, int H>
+__host__ __device__ constexpr int half_np() {
+  return half_goff<LMAX, H>(half_count(H));
+}
+// does half H use Y component c (lm index)?
+template <int LMAX, int H>
+__host__ __device__ constexpr bool half_uses_y(int c) {
+  for (int w = 0; w < half_count(H); ++w) {
+    const int l1 = ins_l1(LMAX, half_ins(H, w));
+    if (c >= l1 * l1 && c < (l1 + 1) * (l1 + 1)) return true;
+  }
+  return false;
+}
+
+template <typename F, int... I>
+__device__ __forceinline__ void static_for_impl(F&& f, std::integer_sequence<int, I...>) {
+  (f(std::integral_constant<int, I>{}), ...);
+}
+// f(std::integral_constant<int, i>) for i in [0, N)
+template <int N, typename F>
+__device__ __forceinline__ void static_for(F&& f) {
+  static_for_impl(f, std::make_integer_sequence<int, N>{});
+}
+
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+
+// Cubic of a channel pair at offset x2 = (x, x) inside its interval, value only.
+__device__ __forceinline__ float2 spline2_val(float4 lo, float4 hi, float2 x2) {
+  const float2 c0 = make_float2(lo.x, lo.y), c1 = make_float2(lo.z, lo.w);
+  const float2 c2 = make_float2(hi.x, hi.y), c3 = make_float2(hi.z, hi.w);
+  return fma2(fma2(fma2(c3, x2, c2), x2, c1), x2, c0);
+}
+// Value and derivative by the two-row Horner scheme (5 packed FMAs).
+__device__ __forceinline__ void spline2(float4 lo, float4 hi, float2 x2, float2& R, float2& Rd) {
+  const float2 c0 = make_float2(lo.x, lo.y), c1 = make_float2(lo.z, lo.w);
+  const float2 c2 = make_float2(hi.x, hi.y), c3 = make_float2(hi.z, hi.w);
+  float2 p = fma2(c3, x2, c2);
+  float2 d = fma2(c3, x2, p);
+  p = fma2(p, x2, c1);
+  d = fma2(d, x2, p);
+  R = fma2(p, x2, c0);
+  Rd = d;
+}
+
+// Sum a per-thread 3-vector over the block for edge t (float32 shuffles; one
+// partial per warp into sF, summed across warps in float64 after the chunk).
+__device__ __forceinline__ void block_reduce3(float fx, float fy, float fz, float (*sF)[8][3], int t) {
+  const float x = warp_sum(fx), y = warp_sum(fy), z = warp_sum(fz);
+  if ((threadIdx.x & 31) == 0) {
+    const int w = threadIdx.x >> 5;
+    sF[t][w][0] = x;
+    sF[t][w][1] = y;
+    sF[t][w][2] = z;
+  }
+}
+
+// Edge chunk staged for the layer-1 kernels.
+template <bool GRAD>
+struct L1Stage {
+  float2 Y2[kEdgeChunk][16];            // (Y_lm, Y_lm): operand of the packed FMAs
+  float4 G[GRAD ? kEdgeChunk : 1][16];  // (dY_lm/dx, dY_lm/dy, dY_lm/dz, 0)
+  float4 u[GRAD ? kEdgeChunk : 1];      // unit vector (w unused)
+  float x[kEdgeChunk];                  // offset inside the spline interval
+  int row[kEdgeChunk];                  // spline row (pair * nint + interval), or -1
+  int j[kEdgeChunk];
+  int act[kEdgeChunk];                  // compacted list of active edges (r < r_cut)
+  int nact;
+};
+
+// Stage edges [eb, eb+ne) (ne <= 32; warp 0) with the unordered species-pair rows.
+template <bool GRAD>
+__device__ __forceinline__ void stage_l1(const DevModel& m, const EdgeIn& in, int ti, int eb, int ne,
+                                         L1Stage<GRAD>& st) {
+  if (threadIdx.x >= 32) return;
+  const int t = threadIdx.x;
+  bool active = false;
+  if (t < ne) {
+    const long e = static_cast<long>(eb) + t;
+    const float vx = static_cast<float>(in.xyz[3 * e]);
+    const float vy = static_cast<float>(in.xyz[3 * e + 1]);
+    const float vz = static_cast<float>(in.xyz[3 * e + 2]);
+    const float rr = static_cast<float>(in.r[e]);
+    float Y[16], G[GRAD ? 48 : 1];
+    sph_harm16<GRAD>(vx, vy, vz, Y, G);
+#pragma unroll
+    for (int c = 0; c < 16; ++c) st.Y2[t][c] = make_float2(Y[c], Y[c]);
+    if constexpr (GRAD) {
+#pragma unroll
+      for (int c = 0; c < 16; ++c) st.G[t][c] = make_float4(G[c], G[16 + c], G[32 + c], 0.0f);
+      const float inv = 1.0f / rr;
+      st.u[t] = make_float4(vx * inv, vy * inv, vz * inv, 0.0f);
+    }
+    int iv = static_cast<int>(rr * m.inv_h);
+    iv = iv < 0 ? 0 : (iv >= m.nint ? m.nint - 1 : iv);
+    st.x[t] = rr - static_cast<float>(iv) * m.h;
+    const int tj = in.ntype_e[e];
+    const int a = ti < tj ? ti : tj, b = ti < tj ? tj : ti;
+    const int pr = a * (2 * m.S - a - 1) / 2 + b;
+    active = rr < m.r_cut;
+    st.row[t] = active ? pr * m.nint + iv : -1;
+    st.j[t] = in.nidx[e];
+  }
+  const unsigned ball = __ballot_sync(0xffffffffu, active);
+  if (active) st.act[__popc(ball & ((1u << t) - 1u))] = t;
+  if (t == 0) st.nact = __popc(ball);
+}
+
+// Per-thread view of the block layout.
+struct Lane2 {
+  int C, C2;   // channels, channel pairs
+  int cp;      // this thread's channel pair (clamped to a valid one on idle lanes)
+  int kc;      // first channel of the pair
+  bool live;   // owns a real channel pair
+};
+
+// Gather the spline coefficients of half H's instructions for spline row `row` and
+// the neighbour features H1[j] of this channel pair.
+template <int LMAX, int H, int NL2>
+__device__ __forceinline__ void fetch_l1(const DevModel& m, const float* __restrict__ H1, int row, int j,
+                                         const Lane2& L, float4* c, float2* h) {
+  const float4* rp = m.spl1 + static_cast<size_t>(row) * ins_count(LMAX) * L.C + L.cp;
+  static_for<half_count(H)>([&](auto ic) {
+    constexpr int i = decltype(ic)::value;
+    constexpr int q = half_ins(H, i);
+    c[2 * i] = __ldg(rp + (2 * q) * L.C2);
+    c[2 * i + 1] = __ldg(rp + (2 * q + 1) * L.C2);
+  });
+  const float2* hp = reinterpret_cast<const float2*>(H1 + static_cast<size_t>(j) * NL2 * L.C + L.kc);
+#pragma unroll
+  for (int b = 0; b < NL2; ++b) h[b] = __ldg(hp + b * L.C2);
+}
+
+// Read half H's CG-contracted adjoint pairs from the block's [NP][C] column array.
+template <int LMAX, int H>
+__device__ __forceinline__ void l1_load_g(const float* sP, const Lane2& L, float2* g) {
+  static_for<half_count(H)>([&](auto ic) {
+    constexpr int i = decltype(ic)::value;
+    constexpr int q = half_ins(H, i);
+    constexpr int np = ins_paths(LMAX, q), p0 = ins_poff(LMAX, q), g0 = half_goff<LMAX, H>(i);
+#pragma unroll
+    for (int p = 0; p < np; ++p) g[g0 + p] = *reinterpret_cast<const float2*>(sP + (p0 + p) * L.C + L.kc);
+  });
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint, one edge, half H.  With g_p = sum_lme CG[lme,p] dPhi1[i,lme,k]:
+//   dE/dx_ij += sum_k sum_p g_p h_{m2} (R1'_q u Y_{m1} + R1_q dY_{m1}/dx)
+//   H1_adj[j, l2 m2, k] += sum_p R1_q Y_{m1} g_p
+// ---------------------------------------------------------------------------
+template <int LMAX, int H>
+__device__ __forceinline__ void l1_rev_edge(const float2* g, const float2* R, const float2* Rd, const float2* Y2,
+                                            const float4* G, float4 u, const float2* hv, float2* hadj, float& fx,
+                                            float& fy, float& fz) {
+  constexpr int NL2 = (LMAX + 1) * (LMAX + 1);
+  float2 dY[16];
+#pragma unroll
+  for (int c = 0; c < 16; ++c) dY[c] = make_float2(0.0f, 0.0f);
+  // two partial sums per H1_adj component (even / odd rows) halve the dependent chains
+  float2 hA[NL2], hB[NL2];
+#pragma unroll
+  for (int b = 0; b < NL2; ++b) hA[b] = hB[b] = make_float2(0.0f, 0.0f);
+  float2 dr = make_float2(0.0f, 0.0f);
+  static_for<half_count(H)>([&](auto ic) {
+    constexpr int i = decltype(ic)::value;
+    constexpr int q = half_ins(H, i);
+    constexpr int l1 = ins_l1(LMAX, q), l2 = ins_l2(LMAX, q), g0 = half_goff<LMAX, H>(i);
+    constexpr int nb = 2 * l2 + 1;
+    float2 dRq = make_float2(0.0f, 0.0f);
+#pragma unroll
+    for (int a = 0; a < 2 * l1 + 1; ++a) {
+      const float2 y = Y2[l1 * l1 + a];
+      float2 gs = mul2(g[g0 + a * nb], hv[l2 * l2]);
+#pragma unroll
+      for (int b = 1; b < nb; ++b) gs = fma2(g[g0 + a * nb + b], hv[l2 * l2 + b], gs);
+      dRq = fma2(gs, y, dRq);
+      dY[l1 * l1 + a] = fma2(R[i], gs, dY[l1 * l1 + a]);
+      const float2 ry = mul2(R[i], y);
+      float2* hs = ((i + a) & 1) ? hB : hA;
+#pragma unroll
+      for (int b = 0; b < nb; ++b) hs[l2 * l2 + b] = fma2(ry, g[g0 + a * nb + b], hs[l2 * l2 + b]);
+    }
+    dr = fma2(dRq, Rd[i], dr);
+  });
+#pragma unroll
+  for (int b = 0; b < NL2; ++b) hadj[b] = __fadd2_rn(hA[b], hB[b]);
+  const float d = dr.x + dr.y;
+  float ax = d * u.x, ay = d * u.y, az = d * u.z;
+  static_for<16>([&](auto cc) {
+    constexpr int c = decltype(cc)::value;
+    if constexpr (half_uses_y<LMAX, H>(c)) {
+      const float s = dY[c].x + dY[c].y;
+      const float4 gc = G[c];
+      ax = fmaf(s, gc.x, ax);
+      ay = fmaf(s, gc.y, ay);
+      az = fmaf(s, gc.z, az);
+    }
+  });
+  fx = ax;
+  fy = ay;
+  fz = az;
+}
+
+// Adjoint, one staged chunk, half H.  The spline row of an edge is reduced to R and
+// R' first; the gathers of the next edge are then issued into the freed registers so
+// that their L2 latency overlaps this edge's arithmetic.
+template <int LMAX, int H>
+__device__ __forceinline__ void l1_rev_chunk(const DevModel& m, const float* __restrict__ H1,
+                                             float* __restrict__ H1_adj, const L1Stage<true>& st, const Lane2& L,
+                                             const float2* g, float (*sF)[8][3]) {
+  constexpr int NL2 = (LMAX + 1) * (LMAX + 1);
+  constexpr int NQ = half_count(H);
+  const int na = st.nact;
+  float4 c[2 * NQ];
+  float2 h[NL2];
+  if (na > 0) fetch_l1<LMAX, H, NL2>(m, H1, st.row[st.act[0]], st.j[st.act[0]], L, c, h);
+  for (int a = 0; a < na; ++a) {
+    const int t = st.act[a];
+    const float2 x2 = make_float2(st.x[t], st.x[t]);
+    float2 R[NQ], Rd[NQ], hv[NL2];
+#pragma unroll
+    for (int i = 0; i < NQ; ++i) spline2(c[2 * i], c[2 * i + 1], x2, R[i], Rd[i]);
+#pragma unroll
+    for (int b = 0; b < NL2; ++b) hv[b] = h[b];
+    const int j = st.j[t];
+    if (a + 1 < na) {
+      const int tn = st.act[a + 1];
+      fetch_l1<LMAX, H, NL2>(m, H1, st.row[tn], st.j[tn], L, c, h);
+    }
+    float2 hadj[NL2];
+    float fx, fy, fz;
+    l1_rev_edge<LMAX, H>(g, R, Rd, st.Y2[t], st.G[t], st.u[t], hv, hadj, fx, fy, fz);
+    if (!L.live) fx = fy = fz = 0.0f;
+    block_reduce3(fx, fy, fz, sF, t);
+    if (L.live) {
+      float2* dst = reinterpret_cast<float2*>(H1_adj + static_cast<size_t>(j) * NL2 * L.C + L.kc);
+#pragma unroll
+      for (int b = 0; b < NL2; ++b) atomicAdd(dst + b * L.C2, hadj[b]);
+    }
+  }
+}
+
+__device__ __forceinline__ Lane2 lane2(const int C, int& half) {
+  Lane2 L;
+  L.C = C;
+  L.C2 = C >> 1;
+  const int HW = (L.C2 + 31) & ~31;
+  half = threadIdx.x >= HW ? 1 : 0;
+  const int cp = threadIdx.x - half * HW;
+  L.live = cp < L.C2;
+  L.cp = L.live ? cp : 0;
+  L.kc = 2 * L.cp;
+  return L;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Layer 1 forward: Phi1r[i,p,k] = sum_j R1_q(r_ij)[k] Y_{l1 m1}(x_ij) H1[j, l2 m2, k]
+// accumulated in registers, then Phi1[i,lme,k] = sum_p CG[lme,p] Phi1r[i,p,k].
+//
+// One thread per channel with scalar FMAs over all instructions, on the per-channel
+// spline table spl1_fwd ([npairs][nint][n_instr][C] float4).  The forward pass moves
+// the same 20 KB spline row per edge as the adjoint but does a third of its
+// arithmetic, so it is bound by the L2 gathers: it is laid out for residency (128
+// registers, four blocks of 128 threads per SM) rather than for the packed FMAs.
+// ---------------------------------------------------------------------------
+template <int LMAX, int CT>
+__global__ void __launch_bounds__(256) k_layer1_fwd(DevModel m, EdgeIn in, const float* __restrict__ H1,
+                                                    float* __restrict__ Phi1) {
+  constexpr int NL2 = (LMAX + 1) * (LMAX + 1);
+  constexpr int NI = ins_count(LMAX);
+  constexpr int NP = ins_np(LMAX);
+  extern __shared__ float dyn[];
+  __shared__ L1Stage<false> st;
+  const int C = CT > 0 ? CT : m.C;
+  const int k = threadIdx.x, i = blockIdx.x;
+  const int ti = in.node_type[i];
+  const int e0 = in.first[i], e1 = in.first[i + 1];
+  float acc[NP];
+#pragma unroll
+  for (int p = 0; p < NP; ++p) acc[p] = 0.0f;
+  for (int eb = e0; eb < e1; eb += kEdgeChunk) {
+    const int ne = min(kEdgeChunk, e1 - eb);
+    __syncthreads();
+    stage_l1<false>(m, in, ti, eb, ne, st);
+    __syncthreads();
+    const int na = st.nact;
+    for (int a = 0; a < na; ++a) {
+      const int t = st.act[a];
+      const float x = st.x[t];
+      float hv[NL2];
+      const float* hj = H1 + static_cast<size_t>(st.j[t]) * NL2 * C + k;
+#pragma unroll
+      for (int b = 0; b < NL2; ++b) hv[b] = __ldg(hj + b * C);
+      const float4* cp = m.spl1_fwd + static_cast<size_t>(st.row[t]) * NI * C + k;
+      const float2* Y2 = st.Y2[t];
+      for_each_ins<LMAX>([&](auto qc) {
+        constexpr int q = decltype(qc)::value;
+        constexpr int l1 = ins_l1(LMAX, q), l2 = ins_l2(LMAX, q), p0 = ins_poff(LMAX, q);
+        const float R = spline_val(__ldg(cp + q * C), x);
+#pragma unroll
+        for (int a1 = 0; a1 < 2 * l1 + 1; ++a1) {
+          const float ry = R * Y2[l1 * l1 + a1].x;
+#pragma unroll
+          for (int b = 0; b < 2 * l2 + 1; ++b)
+            acc[p0 + a1 * (2 * l2 + 1) + b] = fmaf(ry, hv[l2 * l2 + b], acc[p0 + a1 * (2 * l2 + 1) + b]);
+        }
+      });
+    }
+  }
+  float* sP = dyn;  // [NP][C]: this thread's Phi1r column
+#pragma unroll
+  for (int p = 0; p < NP; ++p) sP[p * C + k] = acc[p];
+  for (int lme = 0; lme < m.n_lme; ++lme) {
+    float s = 0.0f;
+    const int p1 = __ldg(m.cg_fwd_off + lme + 1);
+    for (int p = __ldg(m.cg_fwd_off + lme); p < p1; ++p)
+      s = fmaf(__ldg(m.cg_fwd_v + p), sP[__ldg(m.cg_fwd_p + p) * C + k], s);
+    Phi1[(static_cast<size_t>(i) * m.n_lme + lme) * C + k] = s;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Layer 1 adjoint.  g (this thread's half of the CG-contracted dPhi1 paths, channel
+// pair) stays in registers across the node's edges; f1[e] receives dE/dx_ij.
+// ---------------------------------------------------------------------------
+template <int LMAX, int CT>
+__global__ void __launch_bounds__(256) k_layer1_rev(DevModel m, EdgeIn in, const float* __restrict__ H1,
+                                                    const float* __restrict__ dPhi1, float* __restrict__ H1_adj,
+                                                    double* __restrict__ f1) {
+  static_assert(LMAX == 1, "instruction halves are tabulated for L_max = 1");
+  constexpr int NP = ins_np(LMAX);
+  constexpr int NG = half_np<LMAX, 0>() > half_np<LMAX, 1>() ? half_np<LMAX, 0>() : half_np<LMAX, 1>();
+  extern __shared__ float dyn[];
+  __shared__ L1Stage<true> st;
+  __shared__ float sF[kEdgeChunk][8][3];
+  const int C = CT > 0 ? CT : m.C, i = blockIdx.x;
+  int half;
+  const Lane2 L = lane2(C, half);
+  const int nwarp = blockDim.x >> 5;
+  const int ti = in.node_type[i];
+  const int e0 = in.first[i], e1 = in.first[i + 1];
+  // sP[p][k] = sum_lme CG[lme,p] dPhi1[i,lme,k], one channel per thread
+  float* sD = dyn;                 // [n_lme][C]
+  float* sP = dyn + m.n_lme * C;   // [NP][C]
+  for (int k = threadIdx.x; k < C; k += blockDim.x) {
+    for (int lme = 0; lme < m.n_lme; ++lme) sD[lme * C + k] = dPhi1[(static_cast<size_t>(i) * m.n_lme + lme) * C + k];
+    for (int p = 0; p < NP; ++p) {
+      float s = 0.0f;
+      const int q1 = __ldg(m.cg_rev_off + p + 1);
+      for (int q = __ldg(m.cg_rev_off + p); q < q1; ++q)
+        s = fmaf(__ldg(m.cg_rev_v + q), sD[__ldg(m.cg_rev_lme + q) * C + k], s);
+      sP[p * C + k] = s;
+    }
+  }
+  __syncthreads();
+  float2 g[NG];
+  if (half == 0)
+    l1_load_g<LMAX, 0>(sP, L, g);
+  else
+    l1_load_g<LMAX, 1>(sP, L, g);
+  for (int eb = e0; eb < e1; eb += kEdgeChunk) {
+    const int ne = min(kEdgeChunk, e1 - eb);
+    __syncthreads();
+    stage_l1<true>(m, in, ti, eb, ne, st);
+    __syncthreads();
+    if (half == 0)
+      l1_rev_chunk<LMAX, 0>(m, H1, H1_adj, st, L, g, sF);
+    else
+      l1_rev_chunk<LMAX, 1>(m, H1, H1_adj, st, L, g, sF);
+    __syncthreads();
+    for (int t = threadIdx.x; t < ne; t += blockDim.x) {
+      double s[3] = {0.0, 0.0, 0.0};
+      if (st.row[t] >= 0)
+        for (int w = 0; w < nwarp; ++w)
+          for (int c = 0; c < 3; ++c) s[c] += static_cast<double>(sF[t][w][c]);
+      for (int c = 0; c < 3; ++c) f1[3 * (static_cast<long>(eb) + t) + c] = s[c];
+    }
+  }
+}
+
+// threads per block of the layer-1 kernels: two warp-aligned groups of C/2
+int layer1_block(int C) { return 2 * (((C >> 1) + 31) & ~31); }
+
+namespace {
+
+template <int CT>
+cudaError_t set_smem(const DevModel& m) {
+  cudaError_t e = cudaFuncSetAttribute(k_layer1_fwd<1, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(sizeof(float) * ins_np(1) * m.C));
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_layer1_rev<1, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              static_cast<int>(sizeof(float) * (m.n_lme + ins_np(1)) * m.C));
+}
+
+// Channel counts with a compile-time specialisation (addresses fold to immediates).
+template <typename F>
+void dispatch_c(int C, F&& f) {
+  switch (C) {
+    case 32: f(std::integral_constant<int, 32>{}); break;
+    case 64: f(std::integral_constant<int, 64>{}); break;
+    case 128: f(std::integral_constant<int, 128>{}); break;
+    case 256: f(std::integral_constant<int, 256>{}); break;
+    default: f(std::integral_constant<int, 0>{}); break;
+  }
+}
+
+}  // namespace
+
+cudaError_t init_layer1_kernels(const DevModel& m) {
+  cudaError_t e = cudaSuccess;
+  dispatch_c(m.C, [&](auto ct) { e = set_smem<decltype(ct)::value>(m); });
+  return e;
+}
+
+void launch_layer1_fwd(const DevModel& m, const EdgeIn& in, const float* H1, float* Phi1, cudaStream_t s) {
+  if (in.N <= 0) return;
+  const size_t smem = sizeof(float) * ins_np(1) * m.C;
+  dispatch_c(m.C, [&](auto ct) {
+    k_layer1_fwd<1, decltype(ct)::value><<<in.N, m.C, smem, s>>>(m, in, H1, Phi1);
+  });
+}
+
+void launch_layer1_rev(const DevModel& m, const EdgeIn& in, const float* H1, const float* dPhi1, float* H1_adj,
+                       double* f1, cudaStream_t s) {
+  if (in.N <= 0) return;
+  const size_t smem = sizeof(float) * (m.n_lme + ins_np(1)) * m.C;
+  dispatch_c(m.C, [&](auto ct) {
+    k_layer1_rev<1, decltype(ct)::value><<<in.N, layer1_block(m.C), smem, s>>>(m, in, H1, dPhi1, H1_adj, f1);
+  });
+}
+
+}  // namespace smx

@@ -10,11 +10,15 @@ namespace smx {
 // k_edge.cu
 cudaError_t init_edge_kernels(const DevModel& m);
 void launch_layer0_fwd(const DevModel& m, const EdgeIn& in, float* A0, float* M0, float* zbl_e, cudaStream_t s);
+void launch_layer0_rev(const DevModel& m, const EdgeIn& in, const float* A0, const float* M0_adj, const double* f1,
+                       float* A0_adj, double* forces, cudaStream_t s);
+
+// k_layer1.cu
+cudaError_t init_layer1_kernels(const DevModel& m);
+int layer1_block(int C);
 void launch_layer1_fwd(const DevModel& m, const EdgeIn& in, const float* H1, float* Phi1, cudaStream_t s);
 void launch_layer1_rev(const DevModel& m, const EdgeIn& in, const float* H1, const float* dPhi1, float* H1_adj,
                        double* f1, cudaStream_t s);
-void launch_layer0_rev(const DevModel& m, const EdgeIn& in, const float* A0, const float* M0_adj, const double* f1,
-                       float* A0_adj, double* forces, cudaStream_t s);
 
 // k_node.cu
 // One segment of a row-gathered GEMM  Y[rows, ncols] = X[rows, K] @ B[K, ncols].

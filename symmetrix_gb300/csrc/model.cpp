@@ -297,6 +297,7 @@ PackedModel pack_model(const HostModel& hm) {
   for (int q = 1; q < hm.n_instr; ++q)
     if (hm.phi_l[q] < hm.phi_l[q - 1]) throw std::invalid_argument("model file: Phi1_l must be sorted");
   pm.spl1.assign(static_cast<size_t>(hm.npairs) * nint * hm.n_instr * C * 4, 0.0f);
+  pm.spl1_fwd.assign(pm.spl1.size(), 0.0f);
   for (int pr = 0; pr < hm.npairs; ++pr)
     for (int c = 0; c < hm.n_instr; ++c) {
       const int q = json_of_canon[c];
@@ -306,7 +307,10 @@ PackedModel pack_model(const HostModel& hm) {
           double cc[4];
           hermite(h, hm.v1[base + iv], hm.v1[base + iv + 1], hm.d1[base + iv], hm.d1[base + iv + 1], cc);
           for (int p = 0; p < 4; ++p)
-            pm.spl1[(((static_cast<size_t>(pr) * nint + iv) * hm.n_instr + c) * C + k) * 4 + p] =
+            pm.spl1[((((static_cast<size_t>(pr) * nint + iv) * hm.n_instr + c) * 2 + p / 2) * (C / 2) + k / 2) * 4 +
+                    (p % 2) * 2 + k % 2] = static_cast<float>(cc[p]);
+          for (int p = 0; p < 4; ++p)
+            pm.spl1_fwd[(((static_cast<size_t>(pr) * nint + iv) * hm.n_instr + c) * C + k) * 4 + p] =
                 static_cast<float>(cc[p]);
         }
       }

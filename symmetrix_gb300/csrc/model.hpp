@@ -79,7 +79,10 @@ struct PackedModel {
   int S, C, L_max, nLM, n_lme, n_instr, n_p, nint, npairs;
   float h, r_cut;
   std::vector<float> spl0;     // [S*S][nint][4 (l)][C][4 (coef)]  folded, ordered pair ti*S+tj
-  std::vector<float> spl1;     // [npairs][nint][n_instr][C][4]     canonical instruction order
+  // [npairs][nint][n_instr][2][C/2][4], canonical instruction order; channel pairs
+  // (2c, 2c+1): plane 0 = (c0, c0', c1, c1'), plane 1 = (c2, c2', c3, c3')
+  std::vector<float> spl1;
+  std::vector<float> spl1_fwd;  // [npairs][nint][n_instr][C][4]: one float4 cubic per channel
   std::vector<int> mono0;      // packed a | b<<8 | c<<16 (16 = constant one), per LM contiguous
   std::vector<int> mono0_off;  // [nLM + 1]
   int T0 = 0;                  // max monomials per LM (coefficient stride)

@@ -55,6 +55,8 @@ extern "C" {
 #define SMX_ERR_TIMEOUT 5   /* a bounded device-side wait gave up */
 
 #define SMX_PRECISION_FP32 0 /* plain form: float32 throughout, float64 outputs */
+#define SMX_PRECISION_BF16 1 /* precision form: channel-mixing GEMMs in bf16 on the tensor cores
+                                (tcgen05, float32 accumulation); everything else as the plain form */
 
 typedef struct smx_engine smx_engine;
 

@@ -1,7 +1,7 @@
 """Command-line utilities for the GB300 engine.
 
     python -m symmetrix_gb300.cli gen-model --config fp32_4096 --seed 1 --zbl out.json
-    python -m symmetrix_gb300.cli eval --model out.json --atoms 4096 --density 0.10 --evals 3
+    python -m symmetrix_gb300.cli eval --model out.json --atoms 4096 --density 0.10 --evals 3 [--precision bfloat16]
 
 `gen-model` writes a seeded synthetic model in libsymmetrix's JSON format;
 `eval` builds a seeded random periodic box of the model's species and runs E+F
@@ -34,7 +34,7 @@ def evaluate(args):
     from .synth.structures import neighbor_list, random_box
 
     build()
-    eng = MACE(args.model, device=args.device)
+    eng = MACE(args.model, device=args.device, precision=args.precision)
     pos, L, species = random_box(args.atoms, args.density, args.min_dist, eng.num_elements, seed=args.seed)
     nl = neighbor_list(pos, eng.r_cut, L)
     N, E = args.atoms, len(nl["r"])
@@ -81,6 +81,7 @@ def main(argv=None):
     e.add_argument("--seed", type=int, default=2)
     e.add_argument("--evals", type=int, default=3)
     e.add_argument("--device", type=int, default=0)
+    e.add_argument("--precision", default="float32", choices=["float32", "bfloat16"])
     args = ap.parse_args(argv)
     if args.cmd == "gen-model":
         gen_model(args)

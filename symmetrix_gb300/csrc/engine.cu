@@ -42,7 +42,7 @@ smx_engine* smx_create(const char* model_path, int precision, int device) {
     fail(SMX_ERR_INVALID, "model_path is NULL");
     return nullptr;
   }
-  if (precision != SMX_PRECISION_FP32) {
+  if (precision != SMX_PRECISION_FP32 && precision != SMX_PRECISION_BF16) {
     fail(SMX_ERR_INVALID, "unsupported precision mode");
     return nullptr;
   }
@@ -55,6 +55,11 @@ smx_engine* smx_create(const char* model_path, int precision, int device) {
     eng->device = device;
     eng->precision = precision;
     check(cudaStreamCreateWithFlags(&eng->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    check(cudaHostAlloc(reinterpret_cast<void**>(&eng->status_host), sizeof(unsigned), cudaHostAllocMapped),
+          "cudaHostAlloc");
+    *eng->status_host = 0;
+    check(cudaHostGetDevicePointer(reinterpret_cast<void**>(&eng->status_dev), eng->status_host, 0),
+          "cudaHostGetDevicePointer");
     eng->load(model_path);
     check(cudaDeviceSynchronize(), "model upload");
   } catch (const CudaError& e) {
@@ -78,6 +83,7 @@ void smx_destroy(smx_engine* eng) {
   if (eng->stream) cudaStreamDestroy(eng->stream);
   for (auto& e : eng->ev)
     if (e) cudaEventDestroy(e);
+  if (eng->status_host) cudaFreeHost(eng->status_host);
   delete eng;
 }
 
@@ -103,6 +109,20 @@ int smx_set_option(smx_engine* eng, const char* key, long value) {
   }
   if (std::strcmp(key, "profile") == 0) {
     eng->profile = value != 0;
+    return SMX_OK;
+  }
+  if (std::strcmp(key, "tc_terms") == 0) {  // precision form: bf16 split terms of the GEMMs
+    if (value < 1 || value > 3) return fail(SMX_ERR_INVALID, "tc_terms must be 1, 2 or 3");
+    if (eng->precision != SMX_PRECISION_BF16) return fail(SMX_ERR_INVALID, "tc_terms applies to the bf16 form");
+    try {
+      cudaSetDevice(eng->device);
+      cudaStreamSynchronize(eng->stream);
+      eng->tc_terms = static_cast<int>(value);
+      eng->setup_tc_weights();
+      eng->free_workspace();  // operand buffers are sized by the term count
+    } catch (const std::exception& e) {
+      return fail(SMX_ERR_CUDA, e.what());
+    }
     return SMX_OK;
   }
   return fail(SMX_ERR_INVALID, std::string("unknown option '") + key + "'");
@@ -158,6 +178,7 @@ int smx_compute_node_energies_forces(smx_engine* eng, int num_nodes, const int* 
   } catch (const std::exception& e) {
     return fail(SMX_ERR_CUDA, e.what());
   }
+  if (eng->take_status() != SMX_OK) return fail(SMX_ERR_TIMEOUT, "a device-side wait timed out; results are invalid");
   return SMX_OK;
 }
 

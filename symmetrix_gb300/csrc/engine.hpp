@@ -1,9 +1,12 @@
 // Engine object shared by the C ABI translation units (engine.cu, md.cu).
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdint>
+#include <cstring>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -20,6 +23,14 @@ struct CudaError : std::runtime_error {
 };
 inline void check(cudaError_t e, const char* what) {
   if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
+}
+// float -> bf16 bit pattern, round to nearest even (NaN kept quiet)
+inline uint16_t bf16_bits(float f) {
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  if ((u & 0x7fffffffu) > 0x7f800000u) return 0x7fc0;
+  u += 0x7fffu + ((u >> 16) & 1u);
+  return static_cast<uint16_t>(u >> 16);
 }
 template <typename T>
 T* dalloc(size_t n) {
@@ -41,6 +52,18 @@ struct smx_engine {
   smx::DevModel dm{};
   std::vector<void*> model_mem;
   cudaStream_t stream = nullptr;
+  // status word of the bounded device waits (mapped pinned host memory: the host
+  // reads it after a synchronisation without a copy)
+  unsigned* status_host = nullptr;
+  unsigned* status_dev = nullptr;
+  // precision form: bf16 B operands (K contiguous) of the tensor-core GEMMs
+  // (K contiguous, `tc_terms` bf16 split terms concatenated along K: see tc_operand)
+  const __nv_bfloat16 *W_H1 = nullptr, *W_M0adj = nullptr, *W_A1[4] = {}, *W_Phi1adj[4] = {};
+  bool tc_H1 = false, tc_A1[4] = {}, tc_Phi1adj[4] = {};
+  // 1: bf16 operands; 2: weights split hi + lo (x_hi W_hi + x_hi W_lo); 3: both
+  // split (x_hi W_hi + x_lo W_hi + x_hi W_lo: close to float32 operand precision)
+  int tc_terms = 3;
+  std::vector<float> hw_H1W, hw_H1W_T, hw_A1W[4], hw_A1W_T[4];  // float32 host copies
   bool keep_stages = false;
   // optional per-stage CUDA-event timing of the last evaluation
   static constexpr int kStages = 9;
@@ -55,10 +78,45 @@ struct smx_engine {
   float *A0_adj = nullptr, *M0_adj = nullptr, *H1_adj = nullptr, *Phi1_adj = nullptr, *A1_adj = nullptr;
   float *M1_adj = nullptr, *H2_adj = nullptr;
   double* f1 = nullptr;  // layer-1 edge forces (float64 accumulation)
+  // precision form: bf16 GEMM operands (M0 and H1_adj as [N*nLM][C]; Phi1 and A1_adj
+  // regrouped per l as [N*(2l+1)][n_eta*C] and [N*(2l+1)][C])
+  __nv_bfloat16 *M0_bf = nullptr, *Phi1_bf = nullptr, *A1adj_bf = nullptr, *H1adj_bf = nullptr;
   float* zbl_e = nullptr;  // per-node ZBL energy
   int *first = nullptr, *ntype = nullptr, *nidx = nullptr, *ntype_e = nullptr;
   double *xyz = nullptr, *r = nullptr, *energies = nullptr, *forces = nullptr;
   int lastN = 0;
+
+  // B operand of a tensor-core GEMM from a row-major float [nrows][K] matrix: row n
+  // holds (W_hi), (W_hi | W_lo) or (W_hi | W_hi | W_lo) for 1, 2, 3 terms,
+  // W_lo = bf16(W - W_hi).
+  const __nv_bfloat16* tc_operand(const std::vector<float>& W, int nrows, int K) {
+    const int T = tc_terms;
+    std::vector<uint16_t> b(static_cast<size_t>(nrows) * K * T);
+    for (int n = 0; n < nrows; ++n)
+      for (int k = 0; k < K; ++k) {
+        const float w = W[static_cast<size_t>(n) * K + k];
+        const uint16_t hi = smx::bf16_bits(w);
+        uint32_t hu = static_cast<uint32_t>(hi) << 16;
+        float hf;
+        std::memcpy(&hf, &hu, 4);
+        const uint16_t lo = smx::bf16_bits(w - hf);
+        for (int t = 0; t < T; ++t)
+          b[(static_cast<size_t>(n) * T + t) * K + k] = (t == T - 1 && T > 1) ? lo : hi;
+      }
+    return reinterpret_cast<const __nv_bfloat16*>(upload(b));
+  }
+
+  void setup_tc_weights() {
+    const int C = dm.C;
+    if (tc_H1) {
+      W_H1 = tc_operand(hw_H1W_T, 2 * C, C);   // [L][k'][k]: B of H1 = M0 . H1W[L]
+      W_M0adj = tc_operand(hw_H1W, 2 * C, C);  // [L][k][k']: B of M0_adj = H1_adj . H1W[L]^T
+    }
+    for (int l = 0; l < 4; ++l) {
+      if (tc_A1[l]) W_A1[l] = tc_operand(hw_A1W_T[l], C, dm.num_e[l] * C);             // [k'][e k]
+      if (tc_Phi1adj[l]) W_Phi1adj[l] = tc_operand(hw_A1W[l], dm.num_e[l] * C, C);     // [e k][k']
+    }
+  }
 
   template <typename T>
   const T* upload(const std::vector<T>& v) {
@@ -123,6 +181,23 @@ struct smx_engine {
     for (int q = 0; q < 4; ++q) m.zbl_c[q] = pm.zbl_c[q];
     m.zbl_pair = pm.has_zbl ? reinterpret_cast<const float4*>(upload(pm.zbl_pair)) : nullptr;
     check(smx::init_edge_kernels(dm), "cudaFuncSetAttribute");
+    if (precision == SMX_PRECISION_BF16) {
+      check(smx::init_umma_kernels(), "cudaFuncSetAttribute");
+      const int C = pm.C;
+      tc_H1 = smx::umma_supported(C, C) && pm.L_max == 1;
+      for (int l = 0; l < 4; ++l) {
+        if (pm.num_e[l] == 0) continue;
+        tc_A1[l] = smx::umma_supported(pm.num_e[l] * C, C);
+        tc_Phi1adj[l] = smx::umma_supported(C, C);
+      }
+      hw_H1W = pm.H1W;
+      hw_H1W_T = pm.H1W_T;
+      for (int l = 0; l < 4; ++l) {
+        hw_A1W[l] = pm.A1W[l];
+        hw_A1W_T[l] = pm.A1W_T[l];
+      }
+      setup_tc_weights();
+    }
     if (hm.L_max != 1) throw std::invalid_argument("model file: this build supports L_max = 1 (hidden irreps 0e + 1o)");
     if (hm.A0_scaled || hm.A1_scaled)
       throw std::invalid_argument("model file: density-scaled interaction blocks are not supported by this build");
@@ -130,10 +205,11 @@ struct smx_engine {
 
   void free_workspace() {
     void* ps[] = {A0, M0, H1, Phi1, A1, M1, H2, A0_adj, M0_adj, H1_adj, Phi1_adj, A1_adj, M1_adj, H2_adj, f1,
-                  first, ntype, nidx, ntype_e, xyz, r, energies, forces};
+                  first, ntype, nidx, ntype_e, xyz, r, energies, forces, M0_bf, Phi1_bf, A1adj_bf, H1adj_bf};
     for (void* p : ps)
       if (p) cudaFree(p);
     A0 = M0 = H1 = Phi1 = A1 = M1 = H2 = A0_adj = M0_adj = H1_adj = Phi1_adj = A1_adj = M1_adj = H2_adj = nullptr;
+    M0_bf = Phi1_bf = A1adj_bf = H1adj_bf = nullptr;
     f1 = nullptr;
     if (zbl_e) cudaFree(zbl_e);
     zbl_e = nullptr;
@@ -171,6 +247,13 @@ struct smx_engine {
     r = dalloc<double>(nE);
     energies = dalloc<double>(nN);
     forces = dalloc<double>(3 * nE);
+    if (precision == SMX_PRECISION_BF16) {
+      const long T = tc_terms;
+      M0_bf = dalloc<__nv_bfloat16>(T * nN * dm.nLM * C);
+      Phi1_bf = dalloc<__nv_bfloat16>(T * nN * dm.n_lme * C);
+      A1adj_bf = dalloc<__nv_bfloat16>(T * nN * 16 * C);
+      H1adj_bf = dalloc<__nv_bfloat16>(T * nN * dm.nLM * C);
+    }
     capN = nN;
     capE = nE;
   }
@@ -199,10 +282,21 @@ struct smx_engine {
     if (profile) check(cudaEventRecord(ev[q], s), "cudaEventRecord");
   }
 
+  // SMX_ERR_TIMEOUT if a bounded device wait gave up since the last check (call after
+  // synchronising the work in question); clears the word.
+  int take_status() {
+    if (!status_host) return SMX_OK;
+    const unsigned v = *reinterpret_cast<volatile unsigned*>(status_host);
+    if (v == 0) return SMX_OK;
+    *reinterpret_cast<volatile unsigned*>(status_host) = 0;
+    return SMX_ERR_TIMEOUT;
+  }
+
   // The full forward + adjoint pass on device-resident inputs.
   void run(const smx::EdgeIn& in, double* out_e, double* out_f, cudaStream_t s) {
     const int N = in.N;
     const int C = dm.C;
+    const int T = tc_terms;
     lastN = N;
     if (N == 0) return;
     if (profile && !ev[0])
@@ -211,7 +305,11 @@ struct smx_engine {
     mark(0, s);
     smx::launch_layer0_fwd(dm, in, A0, M0, dm.has_zbl ? zbl_e : nullptr, s);
     mark(1, s);
-    {  // H1 = M0 @ H1W[L]  (mace.cpp:397-423)
+    if (tc_H1) {  // H1 = M0 @ H1W[L]  (mace.cpp:397-423), tensor cores
+      smx::launch_rows_to_bf16(M0, M0_bf, static_cast<long>(N) * dm.nLM, C, 1, C, 0, 0, T, s);
+      smx::UmmaOut o{H1, static_cast<long>(N) * dm.nLM, dm.nLM, static_cast<long>(dm.nLM) * C, 0, C, 1};
+      smx::launch_umma_gemm(M0_bf, static_cast<long>(N) * dm.nLM, T * C, W_H1, 2 * C, C, o, status_dev, s);
+    } else {  // H1 = M0 @ H1W[L]  (mace.cpp:397-423)
       smx::GemmBatch b{};
       for (int L = 0; L <= dm.L_max; ++L)
         b.s[b.n++] = seg_rows(M0, H1, dm.H1W + static_cast<size_t>(L) * C * C, N, 2 * L + 1, C, C,
@@ -222,9 +320,19 @@ struct smx_engine {
     smx::launch_layer1_fwd(dm, in, H1, Phi1, s);
     mark(3, s);
     {  // A1 = Phi1 @ A1W[l]  (mace.cpp:607-642)
+      for (int l = 0; l < 4; ++l)
+        if (dm.num_e[l] > 0 && tc_A1[l]) {  // tensor cores on the per-l regrouped bf16 rows
+          const long rows = static_cast<long>(N) * (2 * l + 1);
+          const int K = dm.num_e[l] * C;
+          __nv_bfloat16* X = Phi1_bf + static_cast<size_t>(T) * N * dm.lme_off[l] * C;
+          smx::launch_rows_to_bf16(Phi1, X, rows, K, 2 * l + 1, static_cast<long>(dm.n_lme) * C, dm.lme_off[l] * C, K,
+                                   T, s);
+          smx::UmmaOut o{A1, rows, 2 * l + 1, 16L * C, l * l * C, C, 0};
+          smx::launch_umma_gemm(X, rows, T * K, W_A1[l], C, C, o, status_dev, s);
+        }
       smx::GemmBatch b{};
       for (int l = 0; l < 4; ++l)
-        if (dm.num_e[l] > 0)
+        if (dm.num_e[l] > 0 && !tc_A1[l])
           b.s[b.n++] = seg_rows(Phi1, A1, dm.A1W[l], N, 2 * l + 1, dm.num_e[l] * C, C,
                                 static_cast<long>(dm.n_lme) * C, dm.lme_off[l] * C, dm.num_e[l] * C,
                                 16L * C, l * l * C, C);
@@ -235,9 +343,18 @@ struct smx_engine {
                           dm.has_zbl ? zbl_e : nullptr, out_e, s);
     mark(5, s);
     {  // Phi1_adj = A1_adj @ A1W[l]^T  (mace.cpp:644-679)
+      for (int l = 0; l < 4; ++l)
+        if (dm.num_e[l] > 0 && tc_Phi1adj[l]) {  // tensor cores, one N-tile per eta
+          const long rows = static_cast<long>(N) * (2 * l + 1);
+          __nv_bfloat16* X = A1adj_bf + static_cast<size_t>(T) * N * l * l * C;
+          smx::launch_rows_to_bf16(A1_adj, X, rows, C, 2 * l + 1, 16L * C, l * l * C, C, T, s);
+          smx::UmmaOut o{Phi1_adj, rows, 2 * l + 1, static_cast<long>(dm.n_lme) * C, dm.lme_off[l] * C,
+                         dm.num_e[l] * C, 0};
+          smx::launch_umma_gemm(X, rows, T * C, W_Phi1adj[l], dm.num_e[l] * C, C, o, status_dev, s);
+        }
       smx::GemmBatch b{};
       for (int l = 0; l < 4; ++l)
-        if (dm.num_e[l] > 0)
+        if (dm.num_e[l] > 0 && !tc_Phi1adj[l])
           b.s[b.n++] = seg_rows(A1_adj, Phi1_adj, dm.A1W_T[l], N, 2 * l + 1, C, dm.num_e[l] * C, 16L * C, l * l * C,
                                 C, static_cast<long>(dm.n_lme) * C, dm.lme_off[l] * C, dm.num_e[l] * C);
       smx::launch_gemm(b, s);
@@ -245,7 +362,11 @@ struct smx_engine {
     mark(6, s);
     smx::launch_layer1_rev(dm, in, H1, Phi1_adj, H1_adj, f1, s);
     mark(7, s);
-    {  // M0_adj = H1_adj @ H1W[L]^T  (mace.cpp:425-451)
+    if (tc_H1) {  // M0_adj = H1_adj @ H1W[L]^T  (mace.cpp:425-451), tensor cores
+      smx::launch_rows_to_bf16(H1_adj, H1adj_bf, static_cast<long>(N) * dm.nLM, C, 1, C, 0, 0, T, s);
+      smx::UmmaOut o{M0_adj, static_cast<long>(N) * dm.nLM, dm.nLM, static_cast<long>(dm.nLM) * C, 0, C, 1};
+      smx::launch_umma_gemm(H1adj_bf, static_cast<long>(N) * dm.nLM, T * C, W_M0adj, 2 * C, C, o, status_dev, s);
+    } else {  // M0_adj = H1_adj @ H1W[L]^T  (mace.cpp:425-451)
       smx::GemmBatch b{};
       for (int L = 0; L <= dm.L_max; ++L)
         b.s[b.n++] = seg_rows(H1_adj, M0_adj, dm.H1W_T + static_cast<size_t>(L) * C * C, N, 2 * L + 1, C, C,

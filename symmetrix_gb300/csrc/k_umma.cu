@@ -1,0 +1,260 @@
+// Channel-mixing GEMMs on the tcgen05 tensor cores (the BF16 precision form).
+//
+//   Y[rows, N] = X[rows, K] . B[N, K]^T     X, B bf16 (K contiguous), Y f32
+//
+// One CTA per 128-row x NT-column tile.  Thread 0 streams 64-wide k-blocks of the X
+// tile and the B tile with TMA (128-byte swizzled boxes) through a ring of up to four
+// shared-memory stages (full/empty mbarriers); thread 32 issues four tcgen05.mma
+// (M=128, N=NT, K=16) per k-block into an f32 accumulator in tensor memory and
+// releases each stage with tcgen05.commit; after the last commit the four warps read
+// their 32 accumulator lanes back with tcgen05.ld and store them through an affine row
+// map straight into the engine's feature layouts.
+//
+// These GEMMs restate compute_H1, compute_A1, reverse_A1 and reverse_H1
+// (libsymmetrix/source/mace.cpp:397-451, :607-679) with bf16 operands and f32
+// accumulation.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+
+#include "kernels.h"
+#include "sm100.cuh"
+
+namespace smx {
+
+namespace {
+
+constexpr int kBoxK = 64;      // bf16 elements per TMA box row (128 B: one swizzle atom row)
+constexpr int kTileM = 128;
+
+__device__ __forceinline__ void record_timeout(unsigned* status) {
+  if (status) atomicOr(status, 1u);
+}
+
+constexpr int kStages = 4;     // shared-memory ring depth (k-blocks in flight)
+
+__global__ void __launch_bounds__(128, 1) k_umma_gemm(const __grid_constant__ CUtensorMap ta,
+                                                      const __grid_constant__ CUtensorMap tb, UmmaOut o, int K,
+                                                      int NT, unsigned* status) {
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ uint64_t full[kStages], empty[kStages], bar_mma;
+  __shared__ uint32_t tmem_base;
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  const int KB = K / kBoxK;
+  const int S = KB < kStages ? KB : kStages;
+  const uint32_t a_bytes = kTileM * kBoxK * 2, b_bytes = static_cast<uint32_t>(NT) * kBoxK * 2;
+  const uint32_t stage_bytes = a_bytes + b_bytes;  // stage = A box then B box (both 1024-B multiples)
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.x * kTileM, n0 = blockIdx.y * NT;
+  const uint32_t ncols = NT <= 32 ? 32u : (NT <= 64 ? 64u : (NT <= 128 ? 128u : 256u));
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < S; ++s) {
+      sm100::mbar_init(&full[s], 1);
+      sm100::mbar_init(&empty[s], 1);
+    }
+    sm100::mbar_init(&bar_mma, 1);
+    sm100::fence_mbar_init();
+  }
+  if (warp == 0) {
+    sm100::tmem_alloc(&tmem_base, ncols);
+    sm100::tmem_relinquish();
+  }
+  sm100::tc_fence_before();
+  __syncthreads();
+  sm100::tc_fence_after();
+  const uint32_t tmem = tmem_base;
+
+  // producer: k-block kb goes to stage kb % S once the MMAs of k-block kb - S released it
+  int loads = 0;
+  bool prod_ok = true;
+  if (threadIdx.x == 0) {
+    for (int kb = 0; kb < KB; ++kb) {
+      const int s = kb % S;
+      if (kb >= S && !sm100::mbar_wait(&empty[s], ((kb / S) - 1) & 1)) {
+        prod_ok = false;
+        break;
+      }
+      uint8_t* st = smem + static_cast<size_t>(s) * stage_bytes;
+      sm100::mbar_arrive_expect_tx(&full[s], stage_bytes);
+      sm100::tma_load_2d(st, &ta, kb * kBoxK, m0, &full[s]);
+      sm100::tma_load_2d(st + a_bytes, &tb, kb * kBoxK, n0, &full[s]);
+      ++loads;
+    }
+  }
+  // MMA issuer
+  bool issued = false, mma_ok = true;
+  if (threadIdx.x == 32) {
+    const uint32_t idesc = sm100::idesc_bf16_f32(kTileM, NT);
+    for (int kb = 0; kb < KB; ++kb) {
+      const int s = kb % S;
+      if (!sm100::mbar_wait(&full[s], (kb / S) & 1)) {
+        mma_ok = false;
+        break;
+      }
+      sm100::tc_fence_after();
+      const uint32_t a0 = sm100::smem_u32(smem + static_cast<size_t>(s) * stage_bytes), b0 = a0 + a_bytes;
+#pragma unroll
+      for (int k = 0; k < kBoxK / 16; ++k)  // 16 elements (32 B) per MMA inside the 128-B swizzled row
+        sm100::umma_bf16(tmem, sm100::sdesc_sw128(a0 + k * 32), sm100::sdesc_sw128(b0 + k * 32), idesc,
+                         (kb | k) != 0 ? 1u : 0u);
+      sm100::umma_commit(&empty[s]);
+      issued = true;
+    }
+    // bar_mma: every MMA issued above has completed (also on the error path)
+    if (issued) sm100::umma_commit(&bar_mma);
+  }
+  const int ok = __syncthreads_and((prod_ok && mma_ok) ? 1 : 0);
+  const int any_mma = __syncthreads_or(issued ? 1 : 0);
+  bool done = false;
+  if (any_mma) done = sm100::mbar_wait(&bar_mma, 0);
+  const int all_done = __syncthreads_and((done && ok) ? 1 : 0);
+  sm100::tc_fence_after();
+  if (all_done) {
+    const int r = m0 + warp * 32 + lane;
+    const bool row_ok = r < o.rows;
+    long base = 0;
+    bool write = row_ok;
+    if (row_ok) {
+      base = static_cast<long>(r / o.rpn) * o.y_ns + o.y_off + static_cast<long>(r % o.rpn) * o.y_rs +
+             (o.select ? 0 : n0);
+      if (o.select) write = ((r % o.rpn) == 0) == (blockIdx.y == 0);
+    }
+    for (int c0 = 0; c0 < NT; c0 += 32) {
+      float v[32];
+      sm100::tmem_ld32(tmem + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(c0), v);
+      if (write) {
+        float4* dst = reinterpret_cast<float4*>(o.Y + base + c0);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) dst[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+      }
+    }
+  } else if (threadIdx.x == 0) {
+    record_timeout(status);
+    // no TMA copy may still be landing in shared memory when the CTA exits: wait for
+    // the last load issued into each stage
+    for (int kb = loads - S > 0 ? loads - S : 0; kb < loads; ++kb) sm100::mbar_wait(&full[kb % S], (kb / S) & 1);
+  }
+  sm100::tc_fence_before();
+  __syncthreads();
+  if (warp == 0) sm100::tmem_dealloc(tmem, ncols);
+}
+
+// Split of x into bf16 terms: hi = bf16(x), lo = bf16(x - hi).  Row r of dst holds
+// `terms` blocks of `width`: (hi), (hi | hi) or (hi | lo | hi), matching B operands
+// (W_hi), (W_hi | W_lo) or (W_hi | W_hi | W_lo), so that one GEMM over terms*width
+// sums x_hi W_hi (+ x_hi W_lo) or x_hi W_hi + x_lo W_hi + x_hi W_lo.
+// Source element c of row r: src[(r / rpn) * s_ns + s_off + (r % rpn) * s_rs + c].
+__global__ void k_rows_to_bf16(const float* __restrict__ src, __nv_bfloat16* __restrict__ dst, long rows, int width,
+                               int rpn, long s_ns, int s_off, int s_rs, int terms) {
+  const int w4 = width >> 2;
+  const long n = rows * w4;
+  const long pitch = static_cast<long>(terms) * width;
+  for (long t = blockIdx.x * static_cast<long>(blockDim.x) + threadIdx.x; t < n;
+       t += static_cast<long>(gridDim.x) * blockDim.x) {
+    const long r = t / w4;
+    const int c = static_cast<int>(t - r * w4) * 4;
+    const float4 v = *reinterpret_cast<const float4*>(src + (r / rpn) * s_ns + s_off + (r % rpn) * s_rs + c);
+    const __nv_bfloat162 h0 = __floats2bfloat162_rn(v.x, v.y), h1 = __floats2bfloat162_rn(v.z, v.w);
+    __nv_bfloat162* d = reinterpret_cast<__nv_bfloat162*>(dst + r * pitch + c);
+    d[0] = h0;
+    d[1] = h1;
+    if (terms == 2) {
+      __nv_bfloat162* dh = reinterpret_cast<__nv_bfloat162*>(dst + r * pitch + width + c);
+      dh[0] = h0;
+      dh[1] = h1;
+    }
+    if (terms == 3) {
+      const float2 f0 = __bfloat1622float2(h0), f1 = __bfloat1622float2(h1);
+      __nv_bfloat162* dl = reinterpret_cast<__nv_bfloat162*>(dst + r * pitch + width + c);
+      dl[0] = __floats2bfloat162_rn(v.x - f0.x, v.y - f0.y);
+      dl[1] = __floats2bfloat162_rn(v.z - f1.x, v.w - f1.y);
+    }
+    if (terms > 2) {
+      __nv_bfloat162* dh = reinterpret_cast<__nv_bfloat162*>(dst + r * pitch + 2 * width + c);
+      dh[0] = h0;
+      dh[1] = h1;
+    }
+  }
+}
+
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encoder() {
+  static std::once_flag once;
+  static EncodeTiledFn fn = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  });
+  if (!fn) throw std::runtime_error("cuTensorMapEncodeTiled is not available from the driver");
+  return fn;
+}
+
+// 2-D bf16 tensor map over a row-major [rows][K] matrix, box = 64 x box_rows, 128-B swizzle.
+CUtensorMap make_map(const void* base, long rows, int K, int box_rows) {
+  if (reinterpret_cast<uintptr_t>(base) % 16 != 0) throw std::invalid_argument("tensor map base not 16-byte aligned");
+  if (K % kBoxK != 0) throw std::invalid_argument("GEMM K must be a multiple of 64");
+  CUtensorMap m;
+  std::memset(&m, 0, sizeof(m));
+  const cuuint64_t dims[2] = {static_cast<cuuint64_t>(K), static_cast<cuuint64_t>(rows)};
+  const cuuint64_t strides[1] = {static_cast<cuuint64_t>(K) * 2};
+  const cuuint32_t box[2] = {static_cast<cuuint32_t>(kBoxK), static_cast<cuuint32_t>(box_rows)};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = encoder()(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box,
+                               estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) throw std::runtime_error("cuTensorMapEncodeTiled failed (" + std::to_string(r) + ")");
+  return m;
+}
+
+}  // namespace
+
+size_t umma_smem_bytes(int K, int NT) {
+  const int stages = std::min(K / kBoxK, kStages);
+  return static_cast<size_t>(stages) * (kTileM + NT) * kBoxK * 2 + 1024;
+}
+
+// dynamic shared memory available next to the kernel's few static words
+constexpr size_t kMaxDynSmem = 226 * 1024;
+
+bool umma_supported(int K, int NT) {
+  return K % kBoxK == 0 && NT % 32 == 0 && NT >= 32 && NT <= 256 && umma_smem_bytes(K, NT) <= kMaxDynSmem;
+}
+
+cudaError_t init_umma_kernels() {
+  return cudaFuncSetAttribute(k_umma_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              static_cast<int>(kMaxDynSmem));
+}
+
+void launch_umma_gemm(const __nv_bfloat16* X, long rows, int K, const __nv_bfloat16* B, int nb_rows, int NT,
+                      const UmmaOut& o, unsigned* status, cudaStream_t s) {
+  if (rows <= 0) return;
+  if (!umma_supported(K, NT) || nb_rows % NT != 0) throw std::invalid_argument("unsupported tensor-core GEMM shape");
+  const CUtensorMap ta = make_map(X, rows, K, kTileM);
+  const CUtensorMap tb = make_map(B, nb_rows, K, NT);
+  const dim3 grid(static_cast<unsigned>((rows + kTileM - 1) / kTileM), static_cast<unsigned>(nb_rows / NT));
+  k_umma_gemm<<<grid, 128, umma_smem_bytes(K, NT), s>>>(ta, tb, o, K, NT, status);
+}
+
+void launch_rows_to_bf16(const float* src, __nv_bfloat16* dst, long rows, int width, int rpn, long s_ns, int s_off,
+                         int s_rs, int terms, cudaStream_t s) {
+  if (rows <= 0) return;
+  const long n = rows * (width / 4);
+  const int blocks = static_cast<int>(std::min<long>((n + 255) / 256, 152L * 16));
+  k_rows_to_bf16<<<blocks, 256, 0, s>>>(src, dst, rows, width, rpn, s_ns, s_off, s_rs, terms);
+}
+
+}  // namespace smx

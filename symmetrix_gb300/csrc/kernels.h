@@ -1,6 +1,7 @@
 // Kernel launchers of the GB300 MACE engine (host-callable).
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include "device.cuh"
@@ -45,6 +46,29 @@ void launch_node_tail(const DevModel& m, const int* node_type, int N, const floa
                       float* H2, float* A1_adj, float* H1_adj, float* M1_adj, float* H2_adj, const float* zbl_e,
                       double* energies, cudaStream_t s);
 void launch_scan_first(const int* num_neigh, int N, int* first, cudaStream_t s);
+
+// k_umma.cu: Y = X . B^T on the tcgen05 tensor cores (bf16 operands, f32 accumulation).
+// Row r of the GEMM, column c of N-tile y lands at
+//   Y + (r / rpn) * y_ns + y_off + (r % rpn) * y_rs + (select ? 0 : y * NT) + c;
+// with select, N-tile y is written only for rows with (r % rpn == 0) == (y == 0) (the
+// L = 0 and L = 1 weight blocks of the H1 and M0_adj GEMMs, computed as two N-tiles).
+struct UmmaOut {
+  float* Y;
+  long rows;
+  int rpn;
+  long y_ns;
+  int y_off, y_rs;
+  int select;
+};
+cudaError_t init_umma_kernels();
+size_t umma_smem_bytes(int K, int NT);
+bool umma_supported(int K, int NT);
+void launch_umma_gemm(const __nv_bfloat16* X, long rows, int K, const __nv_bfloat16* B, int nb_rows, int NT,
+                      const UmmaOut& o, unsigned* status, cudaStream_t s);
+// Row r of dst (pitch terms*width): the bf16 split terms (hi), (hi | hi) or (hi | lo | hi) of
+// src[(r / rpn) * s_ns + s_off + (r % rpn) * s_rs + c], c < width (multiple of 4)
+void launch_rows_to_bf16(const float* src, __nv_bfloat16* dst, long rows, int width, int rpn, long s_ns, int s_off,
+                         int s_rs, int terms, cudaStream_t s);
 
 // k_md.cu
 void launch_wrap(int N, double3 box, int3 periodic, double* pos, cudaStream_t s);

@@ -22,12 +22,17 @@ def _ptr(a):
     return ctypes.c_void_p(a.ctypes.data) if a is not None and a.size else None
 
 
+# precision names -> SMX_PRECISION_* (include/smx_gb300.h)
+PRECISIONS = {"float32": 0, "fp32": 0, "bfloat16": 1, "bf16": 1}
+
+
 class MACE:
     def __init__(self, filename, device=0, precision="float32", keep_stages=False):
         self._lib = _lib.load()
-        if precision not in ("float32",):
+        if precision not in PRECISIONS:
             raise ValueError(f"unsupported precision '{precision}'")
-        h = self._lib.smx_create(str(filename).encode(), 0, int(device))
+        self.precision = "bfloat16" if PRECISIONS[precision] == 1 else "float32"
+        h = self._lib.smx_create(str(filename).encode(), PRECISIONS[precision], int(device))
         if not h:
             msg = self._lib.smx_last_error().decode(errors="replace")
             raise RuntimeError(msg)

@@ -1,0 +1,130 @@
+"""GPU precision form (SMX_PRECISION_BF16): the channel-mixing GEMMs on the tcgen05
+tensor cores with bf16 operands and float32 accumulation.
+
+* GEMM exactness: the tensor-core H1 and A1 stages equal a float64 product of the
+  bf16 split operands (1, 2 or 3 terms of the engine's own float32 M0 / Phi1 and the
+  JSON weights) to float32 accumulation error (relative 2e-5 of the stage's scale).
+* Adjoint GEMMs (Phi1_adj, M0_adj) against the plain form: within bf16 operand
+  rounding (2e-2 of scale).
+* End to end against the float64 oracle: force error at most 10 meV/A per edge and
+  per atom, energy error per atom at most 5 meV with both operands split (three bf16
+  products, the default); the one- and two-term errors are printed.
+"""
+import json
+
+import numpy as np
+import pytest
+
+from helpers import atomic_forces, edge_args
+from oracle.pyoracle import Evaluator
+from symmetrix_gb300.synth.model import CONFIGS, make_model, write_model
+from symmetrix_gb300.synth.structures import neighbor_list, random_box
+
+pytestmark = pytest.mark.gpu
+
+F_TOL_BF16 = 0.010  # eV/A
+E_TOL_BF16 = 0.005  # eV per atom
+
+
+def bf16(x):
+    """Round to the nearest bf16 (ties to even), returned as float64."""
+    u = np.asarray(x, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    u = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return u.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+@pytest.fixture(scope="module")
+def wide(tmp_path_factory):
+    cfg = dict(CONFIGS["fp32_4096"], num_knots=50)
+    path = write_model(make_model(**cfg, seed=7), str(tmp_path_factory.mktemp("bf16") / "wide.json"))
+    pos, L, species = random_box(160, 0.10, 0.9, 4, seed=9)
+    nl = neighbor_list(pos, 5.0, L)
+    return path, species, nl
+
+
+def _run(path, species, nl, precision, terms=None):
+    from symmetrix_gb300 import MACE
+    m = MACE(path, precision=precision, keep_stages=True)
+    if terms is not None:
+        m.set_option("tc_terms", terms)
+    m.compute_node_energies_forces(*edge_args(species, nl))
+    return m
+
+
+def split_product(X, W, terms):
+    """float64 value of the tensor-core product with `terms` bf16 split terms."""
+    Xh, Wh = bf16(X), bf16(W)
+    out = Xh @ Wh
+    if terms > 1:
+        out += Xh @ bf16(np.asarray(W, np.float64) - Wh)
+    if terms > 2:
+        out += bf16(np.asarray(X, np.float64) - Xh) @ Wh
+    return out
+
+
+def _rel(a, b):
+    return np.abs(np.asarray(a) - np.asarray(b)).max() / max(np.abs(b).max(), 1e-30)
+
+
+@pytest.mark.parametrize("terms", [1, 2, 3])
+def test_tensor_core_gemms_are_exact_bf16_products(engine_lib, wide, terms):
+    path, species, nl = wide
+    m = _run(path, species, nl, "bf16", terms)
+    d = json.load(open(path))
+    C = d["num_channels"]
+    N = len(species)
+    # H1[i, lm, :] = M0[i, lm, :] . H1W[L(lm)] with split bf16 operands
+    W = np.asarray(d["H1_weights"], dtype=np.float64).reshape(2, C, C)
+    M0 = m.stage("M0").reshape(N, 4, C)
+    H1 = m.stage("H1").reshape(N, 4, C)
+    ref = np.empty_like(H1)
+    ref[:, 0] = split_product(M0[:, 0], W[0].astype(np.float32), terms)
+    ref[:, 1:] = split_product(M0[:, 1:], W[1].astype(np.float32), terms)
+    print(f"terms={terms} H1 rel", _rel(H1, ref))
+    assert _rel(H1, ref) < 2e-5
+    # A1[i, l^2 + m, :] = sum_e Phi1[i, (l, m, e), :] . A1W[l][e]
+    n_e = [len(v) // (C * C) for v in d["A1_weights"]]
+    Phi1 = m.stage("Phi1").reshape(N, -1, C)
+    A1 = m.stage("A1").reshape(N, 16, C)
+    off = 0
+    for l in range(4):
+        if n_e[l] == 0:
+            continue
+        Wl = np.asarray(d["A1_weights"][l], dtype=np.float64).reshape(n_e[l] * C, C).astype(np.float32)
+        X = Phi1[:, off:off + (2 * l + 1) * n_e[l]].reshape(N, 2 * l + 1, n_e[l] * C)
+        ref = split_product(X, Wl, terms)
+        got = A1[:, l * l:(l + 1) ** 2]
+        print(f"terms={terms} A1 l={l} rel", _rel(got, ref))
+        assert _rel(got, ref) < 2e-5
+        off += (2 * l + 1) * n_e[l]
+
+
+def test_adjoint_gemms_close_to_plain_form(engine_lib, wide):
+    path, species, nl = wide
+    mb = _run(path, species, nl, "bf16")
+    mf = _run(path, species, nl, "fp32")
+    for s in ("H1", "A1", "Phi1_adj", "H1_adj", "M0_adj", "A0_adj"):
+        r = _rel(mb.stage(s), mf.stage(s))
+        print(f"{s}: rel {r:.3e}")
+        assert r < 2e-2, s
+
+
+@pytest.mark.parametrize("terms", [1, 2, 3])
+def test_bf16_form_force_error_vs_fp64_oracle(engine_lib, wide, terms):
+    path, species, nl = wide
+    mb = _run(path, species, nl, "bf16", terms)
+    ref = Evaluator(path, "port")
+    ref.compute_node_energies_forces(*edge_args(species, nl))
+    N = len(species)
+    de = np.abs(mb.node_energies - ref.node_energies).max()
+    df = np.abs(mb.node_forces - ref.node_forces).max()
+    F = atomic_forces(N, nl["i"], nl["neigh_indices"], mb.node_forces)
+    Fr = atomic_forces(N, nl["i"], nl["neigh_indices"], ref.node_forces)
+    dF = np.abs(F - Fr)
+    print(f"bf16 form, {terms} term(s): max|dE_i|={de:.3e} eV  max|df_edge|={df:.3e}  max|dF|={dF.max():.3e} "
+          f"rms|dF|={np.sqrt((dF ** 2).mean()):.3e} eV/A  |F|max={np.abs(Fr).max():.2f}")
+    if terms < 3:
+        return  # fewer terms: reported, not held to the 10 meV/A bar
+    assert de < E_TOL_BF16
+    assert df < F_TOL_BF16
+    assert dF.max() < F_TOL_BF16

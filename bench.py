@@ -1,5 +1,5 @@
 #!/usr/bin/env python3
-"""Throughput of the GB300 MACE engine on the 4096-atom FP32 workload.
+"""Throughput of the GB300 MACE engine on the 4096-atom workload, BF16-mixed vs FP32.
 
 Workload (the single-GPU configuration the headline metric is quoted on): a
 periodic cubic box of 4096 atoms at 0.10 atoms/A^3 (H/C/N/O uniform, minimum pair
@@ -18,6 +18,10 @@ pass), scatter to atomic forces and both half-kicks, with the neighbour list
 as one captured CUDA graph.  `value` is atoms x steps / device time (CUDA events on
 the engine's stream).  No L2 flush between steps: the working set of a step (spline
 tables, node features and adjoints, edge arrays) is several times the 129 MB L2.
+Both forms run the same MD: `value` is the BF16-mixed form (channel-mixing GEMMs on
+the tcgen05 tensor cores with bf16 split operands), `forms` holds both forms'
+throughput and their energy / force / virial errors against the float64 oracle on a
+256-atom box of the same model (the CPU baseline's sample).
 `e2e` is the same metric through the host-pointer C ABI evaluator call a LAMMPS/ASE
 caller makes every step (host->device copy of the neighbour list and device->host
 copy of energies and forces inside the timed region).  Per-kernel times for the
@@ -189,7 +193,8 @@ def cpu_evaluators(path, threads):
 
 
 def cpu_rate(path, threads, repeats, n_atoms):
-    """atom-steps/s of `threads` independent evaluations of an n_atoms sub-box."""
+    """atom-steps/s of `threads` independent evaluations of an n_atoms sub-box; also the
+    sub-box and the float64 result (the error reference of the GPU forms)."""
     kind, evs = cpu_evaluators(path, threads)
     pos, L, species, nl = structure(n_atoms, WORKLOAD["struct_seed"] + 100)
     args = (n_atoms, species, nl["num_neigh"], nl["neigh_indices"], species[nl["neigh_indices"]], nl["xyz"], nl["r"])
@@ -208,7 +213,34 @@ def cpu_rate(path, threads, repeats, n_atoms):
         if rep > 0:
             times.append(time.perf_counter() - t)
     dt = statistics.median(times)
-    return kind, threads * n_atoms / dt, dt, len(nl["r"])
+    ref = {"node_energies": np.array(evs[0].node_energies), "node_forces": np.array(evs[0].node_forces)}
+    return kind, threads * n_atoms / dt, dt, len(nl["r"]), (args, nl, ref)
+
+
+def form_errors(eng, sample):
+    """Errors of one GPU form against the float64 oracle on the CPU sample box."""
+    args, nl, ref = sample
+    eng.compute_node_energies_forces(*args)
+    n = args[0]
+    e, f = np.asarray(eng.node_energies), np.asarray(eng.node_forces).reshape(-1, 3)
+    er, fr = ref["node_energies"], ref["node_forces"].reshape(-1, 3)
+
+    def atomic(fe):
+        F = np.zeros((n, 3))
+        np.add.at(F, nl["i"], -fe)
+        np.add.at(F, nl["neigh_indices"], fe)
+        return F
+
+    def virial(fe):  # W_ab = -sum_e x_a f_b over directed edges (force on j from edge i->j is f)
+        x = nl["xyz"].reshape(-1, 3)
+        return -(x[:, :, None] * fe[:, None, :]).sum(0)
+
+    dF = np.abs(atomic(f) - atomic(fr))
+    return {"energy_per_atom_eV": abs(e.sum() - er.sum()) / n, "max_node_energy_eV": float(np.abs(e - er).max()),
+            "max_force_eV_per_A": float(dF.max()), "rms_force_eV_per_A": float(np.sqrt((dF ** 2).mean())),
+            "max_edge_force_eV_per_A": float(np.abs(f - fr).max()),
+            "max_virial_eV": float(np.abs(virial(f) - virial(fr)).max()),
+            "sample": f"{n}-atom box of the same model, density and species mix, vs the float64 oracle"}
 
 
 def reference_arm(args, rank, world):
@@ -252,34 +284,12 @@ def reference_arm(args, rank, world):
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
-def gpu_arm(args, rank, world, local_rank):
-    import ctypes
-
+def time_md(eng, pos, species, masses, L, vel, args, dist, estream):
+    """The timed region: `args.steps` MD steps after `args.warmup` untimed ones."""
     import torch
 
-    from symmetrix_gb300 import MACE, _lib
-    from symmetrix_gb300.build import build
     from symmetrix_gb300.md import MD
-    from symmetrix_gb300.synth.structures import maxwell_boltzmann, species_masses
-
-    torch.cuda.set_device(local_rank)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
-    build()
-    path = model_path()
-    N = WORKLOAD["n_atoms"]
-    pos, L, species, nl = structure(N, WORKLOAD["struct_seed"] + rank)
-    E = len(nl["r"])
-    eng = MACE(path, device=local_rank)
-    dims = model_dims(eng, path)
-    dev = torch.device("cuda", local_rank)
-    estream = torch.cuda.ExternalStream(eng.stream, device=dev)
-
-    # ---- MD: the timed region ----
-    masses = species_masses(eng.atomic_numbers, species)
-    vel = maxwell_boltzmann(masses, 300.0, np.random.default_rng(WORKLOAD["struct_seed"] + rank))
+    N = len(species)
     md = MD(eng, pos, species, masses, box=L, velocities=vel, dt=0.5, skin=1.0, rebuild_every=10)
     st0 = md.state()
     md.run(args.warmup)
@@ -303,10 +313,9 @@ def gpu_arm(args, rank, world, local_rank):
     clk = clocks.stop()
     T = e0.elapsed_time(e1) / 1e3
     if dist:
-        tt = torch.tensor([T], device=dev)
+        tt = torch.tensor([T], device=torch.device("cuda", torch.cuda.current_device()))
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         T = tt.item()
-    value = world * N * args.steps / T
     st1 = md.state()
     acc = 9.648533212331e-3
     ke = lambda v: 0.5 * float((masses[:, None] * v ** 2).sum()) / acc
@@ -314,8 +323,12 @@ def gpu_arm(args, rank, world, local_rank):
                 "E_total_end": st1["potential_energy"] + ke(st1["velocities"]),
                 "T_end_K": 2 * ke(st1["velocities"]) / (3 * N * 8.617333262e-5), "edges_skin_list": md.num_edges}
     del md
+    return T, t_wall, clk, md_check
 
-    # ---- per-kernel device times: evaluation steps with engine CUDA events ----
+
+def stage_profile(eng, N, E, species, nl, n_prof, dev):
+    """Per-stage device times (engine CUDA events) over n_prof evaluations, L2 flushed."""
+    import torch
     eng.set_option("profile", 1)
     t_types = torch.as_tensor(species, dtype=torch.int32, device=dev)
     t_nn = torch.as_tensor(nl["num_neigh"], dtype=torch.int32, device=dev)
@@ -333,7 +346,6 @@ def gpu_arm(args, rank, world, local_rank):
                            t_xyz.data_ptr(), t_r.data_ptr(), t_e.data_ptr(), t_f.data_ptr(), stream.cuda_stream)
 
     stage_tot, eval_ms = {}, []
-    n_prof = max(5, min(args.steps, 20))
     with torch.cuda.stream(stream):
         for _ in range(3):
             flush.fill_(1)
@@ -350,8 +362,47 @@ def gpu_arm(args, rank, world, local_rank):
     torch.cuda.synchronize()
     eval_ms = [a.elapsed_time(b) for a, b in eval_ms]
     eng.set_option("profile", 0)
+    return {n_: v / n_prof for n_, v in stage_tot.items()}, statistics.median(eval_ms)
 
-    # ---- e2e: the host-pointer C ABI with pinned host buffers ----
+
+def gpu_arm(args, rank, world, local_rank):
+    import ctypes
+
+    import torch
+
+    from symmetrix_gb300 import MACE, _lib
+    from symmetrix_gb300.build import build
+    from symmetrix_gb300.synth.structures import maxwell_boltzmann, species_masses
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    build()
+    path = model_path()
+    N = WORKLOAD["n_atoms"]
+    pos, L, species, nl = structure(N, WORKLOAD["struct_seed"] + rank)
+    E = len(nl["r"])
+    dev = torch.device("cuda", local_rank)
+    n_prof = max(5, min(args.steps, 20))
+
+    # ---- both forms: MD timed region, per-stage times ----
+    forms = {}
+    for form in ("fp32", "bf16"):
+        eng = MACE(path, device=local_rank, precision=form)
+        dims = model_dims(eng, path)
+        estream = torch.cuda.ExternalStream(eng.stream, device=dev)
+        masses = species_masses(eng.atomic_numbers, species)
+        vel = maxwell_boltzmann(masses, 300.0, np.random.default_rng(WORKLOAD["struct_seed"] + rank))
+        T, t_wall, clk, md_check = time_md(eng, pos, species, masses, L, vel, args, dist, estream)
+        avg, eval_ms = stage_profile(eng, N, E, species, nl, n_prof, dev)
+        forms[form] = {"eng": eng, "T": T, "t_wall": t_wall, "clk": clk, "md_check": md_check, "stages": avg,
+                       "eval_ms": eval_ms, "value": world * N * args.steps / T}
+    head = forms["bf16"]
+    eng = head["eng"]
+
+    # ---- e2e: the host-pointer C ABI with pinned host buffers (headline form) ----
     lib = _lib.load()
     pin = lambda a, dt: torch.as_tensor(np.ascontiguousarray(a), dtype=dt).pin_memory()
     h = [pin(species, torch.int32), pin(nl["num_neigh"], torch.int32), pin(nl["neigh_indices"], torch.int32),
@@ -380,16 +431,24 @@ def gpu_arm(args, rank, world, local_rank):
         t_e2e = tt.item()
     e2e = {"value": world * N * args.steps / t_e2e, "unit": UNIT,
            "h2d_bytes_per_step": 4 * N + 4 * (N + 1) + E * (4 + 4 + 24 + 8), "d2h_bytes_per_step": 8 * N + 24 * E,
-           "step": "one smx_compute_node_energies_forces call on host arrays (the pair-style call)"}
+           "step": "one smx_compute_node_energies_forces call on host arrays (the pair-style call), BF16-mixed form"}
 
     if rank != 0:
         if dist:
             dist.destroy_process_group()
         return
 
-    # ---- roofline of the dominant kernel ----
+    # ---- CPU baseline (the oracle, one thread, bounded sample) and the error report ----
+    kind, cpu_val, cpu_dt, cpu_edges, sample = cpu_rate(path, 1, 2, WORKLOAD["cpu_sample_atoms"])
+    cpu = {"value": cpu_val, "unit": UNIT, "cores": 1, "kind": kind,
+           "sample": f"median of 2 E+F evaluations of a {WORKLOAD['cpu_sample_atoms']}-atom box of the same model, "
+                     f"density and species mix ({cpu_edges} edges), float64, 1 thread"}
+    for form in forms.values():
+        form["errors"] = form_errors(form["eng"], sample)
+
+    # ---- roofline of the dominant kernel (headline form) ----
     costs = stage_costs(dims, N, E)
-    avg = {n_: v / n_prof for n_, v in stage_tot.items()}
+    avg = head["stages"]
     dom = max(avg, key=avg.get)
     flops, bytes_ = costs[dom]
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -400,6 +459,7 @@ def gpu_arm(args, rank, world, local_rank):
         hbm, peak_src = 6800.0, "fallback"
     t_dom = avg[dom] / 1e3
     achieved = bytes_ / t_dom / 1e9
+    clk = head["clk"]
     sm_mhz = clk.get("sm_mhz") or 2070.0
     fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
@@ -408,41 +468,50 @@ def gpu_arm(args, rank, world, local_rank):
                 "fp32_simt": {"achieved_tflops": flops / t_dom / 1e12, "peak_tflops": fp32_peak,
                               "frac": flops / t_dom / 1e12 / fp32_peak,
                               "peak_source": "152 SMs x 128 FP32 lanes x 2 x median SM clock under load"}}
-    per_stage = {n_: {"ms": avg[n_], "gflop": costs[n_][0] / 1e9, "tflops": costs[n_][0] / (avg[n_] / 1e3) / 1e12,
-                      "gbs": costs[n_][1] / (avg[n_] / 1e3) / 1e9} for n_ in avg}
 
-    # ---- CPU baseline: the oracle, one thread, bounded sample ----
-    kind, cpu_val, cpu_dt, cpu_edges = cpu_rate(path, 1, 2, WORKLOAD["cpu_sample_atoms"])
-    cpu = {"value": cpu_val, "unit": UNIT, "cores": 1, "kind": kind,
-           "sample": f"median of 2 E+F evaluations of a {WORKLOAD['cpu_sample_atoms']}-atom box of the same model, "
-                     f"density and species mix ({cpu_edges} edges), float64, 1 thread"}
+    def per_stage(a):
+        return {n_: {"ms": a[n_], "gflop": costs[n_][0] / 1e9, "tflops": costs[n_][0] / (a[n_] / 1e3) / 1e12,
+                     "gbs": costs[n_][1] / (a[n_] / 1e3) / 1e9} for n_ in a}
 
-    # kernels per MD step: vv_first, edge_geometry, 9 evaluation kernels, atom_forces, vv_second;
-    # plus per rebuild: wrap, 4 cell-list kernels, 2 neighbour passes, scan, reverse map
+    # kernels per MD step of the BF16 form: vv_first, edge_geometry, atom_forces, vv_second and 26
+    # evaluation kernels (layer0_fwd, layer1_fwd, node_tail, layer1_rev, contract0_rev, layer0_rev,
+    # and 10 tensor-core GEMMs each with its operand conversion: H1, A1 per l (4), Phi1_adj per l (4),
+    # M0_adj); plus per rebuild: wrap, 4 cell-list kernels, 2 neighbour passes, scan, reverse map
     rebuilds = (args.warmup + args.steps + 9) // 10 - (args.warmup + 9) // 10
-    launches = 13 * args.steps + 9 * rebuilds
+    launches = 30 * args.steps + 9 * rebuilds
+    fp = forms["fp32"]
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": T / args.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic",
+        "metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": head["T"] / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
         "config": {"workload": "fp32_4096: periodic box, 4096 atoms, 0.10 atoms/A^3, H/C/N/O, "
                                "128x0e+128x1o, l_max 3, correlation 3, r_cut 5 A, 200 spline knots, ZBL",
-                   "atoms": N, "edges_r_cut": E, "form": "FP32 plain",
+                   "atoms": N, "edges_r_cut": E,
+                   "form": "BF16-mixed: channel-mixing GEMMs on tcgen05 with bf16 split operands (3 terms) and "
+                           "f32 accumulation; radials, Y_lm, contractions and adjoint in f32; f64 sums",
                    "step": "velocity-Verlet MD step: E+F evaluation + integration; neighbour list rebuilt on the "
                            "GPU every 10 steps (1 A skin); steps between rebuilds in one CUDA graph",
                    "dt_fs": 0.5, "T0_K": 300,
                    "l2": "no flush: per-step working set (>400 MB of tables, node features, adjoints) exceeds L2",
                    "replicas_per_gpu": 1},
+        "forms": {
+            "bf16": {"value": head["value"], "ms_per_step": head["T"] / args.steps * 1e3, "errors": head["errors"],
+                     "ms_per_eval": head["eval_ms"]},
+            "fp32": {"value": fp["value"], "ms_per_step": fp["T"] / args.steps * 1e3, "errors": fp["errors"],
+                     "ms_per_eval": fp["eval_ms"], "md_check": fp["md_check"], "clocks": fp["clk"]},
+            "bf16_over_fp32": head["value"] / fp["value"],
+        },
         "roofline": roofline,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": launches,
         "clocks": clk,
-        "eval_only": {"ms_per_eval": statistics.median(eval_ms), "atom_evals_per_s": N / (statistics.median(eval_ms) / 1e3),
+        "eval_only": {"ms_per_eval": head["eval_ms"], "atom_evals_per_s": N / (head["eval_ms"] / 1e3),
                       "l2": "flushed between evaluations"},
-        "stages_ms": per_stage,
-        "md_check": md_check,
-        "wall_s_timed_region": t_wall,
+        "stages_ms": per_stage(avg),
+        "stages_ms_fp32": per_stage(fp["stages"]),
+        "md_check": head["md_check"],
+        "wall_s_timed_region": head["t_wall"],
     }
     print(json.dumps(line), flush=True)
     if dist:

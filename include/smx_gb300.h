@@ -156,6 +156,28 @@ void smx_md_destroy(smx_md* md);
 int smx_energy_virial_device_noalloc(int num_nodes, long num_edges, const double* node_energies, const double* xyz,
                                      const double* node_forces, double* out, void* stream);
 
+/* ---- LAMMPS pair-style adapter -------------------------------------------
+ * One compute() of pair_style symmetrix/mace in its no-domain-decomposition mode:
+ * replaces PairSymmetrixMACE::compute_no_domain_decomposition
+ * (pair_symmetrix/pair_symmetrix_mace.cpp:242-372), with the same inputs taken
+ * straight from LAMMPS: the full neighbour list (list->inum, ilist, numneigh,
+ * firstneigh, NEIGHMASK), atom->x[0] (x[nall][3] of local and ghost atoms),
+ * atom->type (1-based, nall), local_of[j] = atom->map(atom->tag[j]) and the
+ * LAMMPS-type -> model-species map mace_types[ntypes] set by pair_coeff.  Edges are
+ * the candidates with r < r_cut; results are ADDED like the reference: f[nall][3]
+ * (F_i -= f_e, F_local_of[j] += f_e), *eng_vdwl (eflag_global), eatom[inum]
+ * (eflag_atom, overwritten), virial[6] = xx yy zz xy xz yz of sum_e xyz (x) f_e
+ * (vflag_global).  neigh_changed != 0 re-uploads the list topology, types and owners
+ * (LAMMPS re-neighbouring); otherwise only x moves.  Filtering, evaluation and force
+ * scatter run on the GPU; synchronous.  One adapter per engine; not thread-safe. */
+typedef struct smx_pair smx_pair;
+smx_pair* smx_pair_create(smx_engine* eng);
+void smx_pair_destroy(smx_pair* pair);
+int smx_pair_compute(smx_pair* pair, int inum, int nall, const int* ilist, const int* numneigh,
+                     const int* const* firstneigh, int neighmask, int neigh_changed, const double* x,
+                     const int* type, const int* local_of, const int* mace_types, int ntypes, int eflag_global,
+                     int eflag_atom, int vflag_global, double* f, double* eng_vdwl, double* eatom, double* virial);
+
 #ifdef __cplusplus
 }
 #endif

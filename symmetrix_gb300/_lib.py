@@ -43,6 +43,9 @@ SIGNATURES = [
     ("smx_md_num_edges", _L, [_P]),
     ("smx_md_destroy", None, [_P]),
     ("smx_energy_virial_device_noalloc", _I, [_I, _L, _P, _P, _P, _P, _P]),
+    ("smx_pair_create", _P, [_P]),
+    ("smx_pair_destroy", None, [_P]),
+    ("smx_pair_compute", _I, [_P, _I, _I, _P, _P, _P, _I, _I, _P, _P, _P, _P, _I, _I, _I, _I, _P, _P, _P, _P]),
 ]
 
 STAGE_NAMES = ("layer0_fwd", "gemm_H1", "layer1_fwd", "gemm_A1", "node_tail", "gemm_Phi1_adj", "layer1_rev",

@@ -60,7 +60,15 @@ extern "C" {
 
 typedef struct smx_engine smx_engine;
 
-/* Load a libsymmetrix JSON model onto CUDA device `device`.  NULL on failure. */
+/* Parse a model (JSON, or a cache file) once and write it as a binary model cache:
+ * the packed device-layout tables in one file that smx_create then loads in place of
+ * the JSON without parsing it.  Host only (no GPU).  No counterpart in the reference,
+ * whose MACE(std::string) parses the JSON on every construction
+ * (libsymmetrix/source/mace.cpp:12-15, :905-1030). */
+int smx_save_model_cache(const char* model_path, const char* cache_path);
+
+/* Load a libsymmetrix JSON model (or a model cache written by smx_save_model_cache)
+ * onto CUDA device `device`.  NULL on failure. */
 smx_engine* smx_create(const char* model_path, int precision, int device);
 void smx_destroy(smx_engine* eng);
 const char* smx_last_error(void);

@@ -5,6 +5,6 @@ include/smx_gb300.h; the kernels are hand-written CUDA for sm_103a
 (symmetrix_gb300/csrc).  `symmetrix_gb300.synth` generates seeded synthetic models
 in the reference's JSON format and synthetic structures.
 """
-from .mace import MACE  # noqa: F401
+from .mace import MACE, save_model_cache  # noqa: F401
 
 __version__ = "0.1.0"

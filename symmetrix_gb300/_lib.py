@@ -19,6 +19,7 @@ _L = ctypes.c_long
 _D = ctypes.c_double
 _S = ctypes.c_char_p
 SIGNATURES = [
+    ("smx_save_model_cache", _I, [_S, _S]),
     ("smx_create", _P, [_S, _I, _I]),
     ("smx_destroy", None, [_P]),
     ("smx_last_error", _S, []),

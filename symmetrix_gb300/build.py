@@ -22,7 +22,7 @@ CU_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcom
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-I", SRC, "-I", os.path.join(ROOT, "include")]
 
 CU_SOURCES = ["k_edge.cu", "k_layer1.cu", "k_umma.cu", "k_node.cu", "k_md.cu", "engine.cu", "md.cu", "noalloc.cu", "pair.cu"]
-CXX_SOURCES = ["model.cpp"]
+CXX_SOURCES = ["model.cpp", "model_cache.cpp"]
 
 
 def _deps():

@@ -3,10 +3,13 @@
     python -m symmetrix_gb300.cli gen-model --config fp32_4096 --seed 1 --zbl out.json
     python -m symmetrix_gb300.cli eval --model out.json --atoms 4096 --density 0.10 --evals 3 [--precision bfloat16]
 
+    python -m symmetrix_gb300.cli cache model.json model.smxb
+
 `gen-model` writes a seeded synthetic model in libsymmetrix's JSON format;
 `eval` builds a seeded random periodic box of the model's species and runs E+F
 evaluations of it through the device-pointer C ABI (the call a GPU-resident caller
-makes), printing per-evaluation device times.  `eval` is also the small, fixed target
+makes), printing per-evaluation device times.  `cache` writes the binary model cache
+that MACE() (smx_create) loads without parsing the JSON.  `eval` is also the small, fixed target
 used for ncu captures of single kernels.
 """
 import argparse
@@ -64,6 +67,15 @@ def evaluate(args):
     print(json.dumps({"atoms": N, "edges": E, "ms_per_eval": ms, "energy": float(e_out.sum().item())}))
 
 
+def cache(args):
+    from . import save_model_cache
+    from .build import build
+    build()
+    t = time.time()
+    save_model_cache(args.model, args.out)
+    print(f"wrote {args.out} ({os.path.getsize(args.out) / 1e6:.1f} MB) in {time.time() - t:.1f} s")
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(prog="python -m symmetrix_gb300.cli")
     sub = ap.add_subparsers(dest="cmd", required=True)
@@ -82,9 +94,14 @@ def main(argv=None):
     e.add_argument("--evals", type=int, default=3)
     e.add_argument("--device", type=int, default=0)
     e.add_argument("--precision", default="float32", choices=["float32", "bfloat16"])
+    c = sub.add_parser("cache")
+    c.add_argument("model")
+    c.add_argument("out")
     args = ap.parse_args(argv)
     if args.cmd == "gen-model":
         gen_model(args)
+    elif args.cmd == "cache":
+        cache(args)
     else:
         evaluate(args)
 

@@ -37,6 +37,19 @@ extern "C" {
 
 const char* smx_last_error(void) { return smx::g_last_error.c_str(); }
 
+int smx_save_model_cache(const char* model_path, const char* cache_path) {
+  if (!model_path || !cache_path) return fail(SMX_ERR_INVALID, "NULL path");
+  try {
+    smx::HostModel hm;
+    smx::PackedModel pm;
+    smx::load_model(model_path, hm, pm);
+    smx::save_model_cache(cache_path, hm, pm);
+  } catch (const std::exception& e) {
+    return fail(SMX_ERR_MODEL, e.what());
+  }
+  return SMX_OK;
+}
+
 smx_engine* smx_create(const char* model_path, int precision, int device) {
   if (!model_path) {
     fail(SMX_ERR_INVALID, "model_path is NULL");

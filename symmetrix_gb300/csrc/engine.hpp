@@ -127,8 +127,8 @@ struct smx_engine {
   }
 
   void load(const std::string& path) {
-    hm.load_json(path);
-    smx::PackedModel pm = smx::pack_model(hm);
+    smx::PackedModel pm;
+    smx::load_model(path, hm, pm);
     auto& m = dm;
     m.S = pm.S;
     m.C = pm.C;

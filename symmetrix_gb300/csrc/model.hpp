@@ -119,4 +119,20 @@ struct PackedModel {
 
 PackedModel pack_model(const HostModel& hm);
 
+// Binary model cache (model_cache.cpp): the packed model plus the HostModel scalars
+// the engine reads; load fills only those HostModel fields.
+bool is_model_cache(const std::string& path);
+void save_model_cache(const std::string& path, const HostModel& hm, const PackedModel& pm);
+void load_model_cache(const std::string& path, HostModel& hm, PackedModel& pm);
+
+// JSON or cache file -> (hm, pm)
+inline void load_model(const std::string& path, HostModel& hm, PackedModel& pm) {
+  if (is_model_cache(path)) {
+    load_model_cache(path, hm, pm);
+  } else {
+    hm.load_json(path);
+    pm = pack_model(hm);
+  }
+}
+
 }  // namespace smx

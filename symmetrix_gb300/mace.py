@@ -22,6 +22,12 @@ def _ptr(a):
     return ctypes.c_void_p(a.ctypes.data) if a is not None and a.size else None
 
 
+def save_model_cache(model_path, cache_path):
+    """Parse a JSON model once and write the binary model cache that MACE() loads in its place."""
+    lib = _lib.load()
+    _lib.raise_for(lib.smx_save_model_cache(str(model_path).encode(), str(cache_path).encode()), lib)
+
+
 # precision names -> SMX_PRECISION_* (include/smx_gb300.h)
 PRECISIONS = {"float32": 0, "fp32": 0, "bfloat16": 1, "bf16": 1}
 

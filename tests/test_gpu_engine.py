@@ -199,3 +199,18 @@ def test_polynomial_paths(engine_lib, small_model_path, small_golden, tmp_path, 
     ref.compute_node_energies_forces(*edge_args(species, nl))
     assert _report("E_i", m.node_energies, ref.node_energies) < E_TOL
     assert _report("f_edge", m.node_forces, ref.node_forces) < F_TOL
+
+
+def test_model_cache_gives_identical_results(engine_lib, small_model_path, small_golden, tmp_path):
+    from symmetrix_gb300 import save_model_cache
+    g = small_golden
+    species = g["species"].astype(np.int32)
+    nl = {k: g[k] for k in ("num_neigh", "neigh_indices", "xyz", "r")}
+    cache = str(tmp_path / "small.smxb")
+    save_model_cache(small_model_path, cache)
+    a, b = _engine(small_model_path), _engine(cache)
+    a.compute_node_energies_forces(*edge_args(species, nl))
+    b.compute_node_energies_forces(*edge_args(species, nl))
+    assert b.atomic_numbers == a.atomic_numbers and b.r_cut == a.r_cut
+    assert np.array_equal(a.node_energies, b.node_energies)
+    assert np.array_equal(a.node_forces, b.node_forces)

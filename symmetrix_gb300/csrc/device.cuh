@@ -47,6 +47,14 @@ struct DevModel {
   int has_zbl, zbl_p;
   float zbl_c[4];
   const float4* zbl_pair;  // [S*S]: (1/a, 0.5*14.3996*Zu*Zv, r_max, 0)
+  // density-normalised blocks: layer 0 / 1 spline tables [npairs][nint][4] (or nullptr)
+  const float4* dens_spl[2];
+  int dens_nint[2];
+  float dens_h[2], dens_inv_h[2];
+  // and their per-node workspace (set by the engine with its buffers): the factor
+  // s_i = 1 + sum_j s(r_ij) and c_i = (dE/dA_scaled . A_scaled) / s_i
+  float* dens_s[2];
+  float* dens_c[2];
 };
 
 // ZBL energy of one directed edge and its r-derivative, as zbl.cpp:22-94
@@ -215,5 +223,49 @@ __device__ __forceinline__ float warp_sum(float v) {
 }
 
 inline int ceil_div(long a, long b) { return static_cast<int>((a + b - 1) / b); }
+
+// Density-normalisation spline of `layer` for the unordered pair (ti, tj) at r: value
+// and r-derivative (CubicSpline::evaluate_deriv, libsymmetrix/source/cubic_spline.cpp:29-41).
+__device__ __forceinline__ void dens_eval(const DevModel& m, int layer, int ti, int tj, float r, float& v,
+                                          float& d) {
+  const int a = ti < tj ? ti : tj, b = ti < tj ? tj : ti;
+  const int pr = a * (2 * m.S - a - 1) / 2 + b;
+  int iv = static_cast<int>(r * m.dens_inv_h[layer]);
+  iv = iv < 0 ? 0 : (iv >= m.dens_nint[layer] ? m.dens_nint[layer] - 1 : iv);
+  const float x = r - static_cast<float>(iv) * m.dens_h[layer];
+  const float4 c = __ldg(m.dens_spl[layer] + static_cast<size_t>(pr) * m.dens_nint[layer] + iv);
+  v = spline_val(c, x);
+  d = spline_der(c, x);
+}
+
+// Sum of v over the block (blockDim a multiple of 32, at most 1024 threads); every
+// thread gets the total.  Contains __syncthreads: call from uniform control flow.
+__device__ __forceinline__ float block_sum(float v) {
+  __shared__ float red[33];
+  v = warp_sum(v);
+  const int nw = blockDim.x >> 5;
+  __syncthreads();  // red may still be read by a previous call
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float t = 0.0f;
+    for (int w = 0; w < nw; ++w) t += red[w];
+    red[32] = t;
+  }
+  __syncthreads();
+  return red[32];
+}
+
+// s_i = 1 + sum over the node's edges of the density spline (compute_A0_scaled /
+// compute_A1_scaled, libsymmetrix/source/mace.cpp:273-297, :681-705).
+__device__ __forceinline__ float dens_factor(const DevModel& m, int layer, const EdgeIn& in, int i, int ti) {
+  float z = 0.0f;
+  for (int e = in.first[i] + threadIdx.x; e < in.first[i + 1]; e += blockDim.x) {
+    float v, d;
+    dens_eval(m, layer, ti, in.ntype_e[e], static_cast<float>(in.r[e]), v, d);
+    z += v;
+  }
+  return 1.0f + block_sum(z);
+}
 
 }  // namespace smx

@@ -180,6 +180,14 @@ struct smx_engine {
     m.zbl_p = pm.zbl_p;
     for (int q = 0; q < 4; ++q) m.zbl_c[q] = pm.zbl_c[q];
     m.zbl_pair = pm.has_zbl ? reinterpret_cast<const float4*>(upload(pm.zbl_pair)) : nullptr;
+    for (int layer = 0; layer < 2; ++layer) {  // density-normalised interaction blocks
+      m.dens_spl[layer] =
+          pm.dens_scaled[layer] ? reinterpret_cast<const float4*>(upload(pm.dens_spl[layer])) : nullptr;
+      m.dens_nint[layer] = pm.dens_nint[layer];
+      m.dens_h[layer] = pm.dens_h[layer];
+      m.dens_inv_h[layer] = pm.dens_scaled[layer] ? 1.0f / pm.dens_h[layer] : 0.0f;
+      m.dens_s[layer] = m.dens_c[layer] = nullptr;
+    }
     check(smx::init_edge_kernels(dm), "cudaFuncSetAttribute");
     if (precision == SMX_PRECISION_BF16) {
       check(smx::init_umma_kernels(), "cudaFuncSetAttribute");
@@ -199,8 +207,7 @@ struct smx_engine {
       setup_tc_weights();
     }
     if (hm.L_max != 1) throw std::invalid_argument("model file: this build supports L_max = 1 (hidden irreps 0e + 1o)");
-    if (hm.A0_scaled || hm.A1_scaled)
-      throw std::invalid_argument("model file: density-scaled interaction blocks are not supported by this build");
+
   }
 
   void free_workspace() {
@@ -210,6 +217,11 @@ struct smx_engine {
       if (p) cudaFree(p);
     A0 = M0 = H1 = Phi1 = A1 = M1 = H2 = A0_adj = M0_adj = H1_adj = Phi1_adj = A1_adj = M1_adj = H2_adj = nullptr;
     M0_bf = Phi1_bf = A1adj_bf = H1adj_bf = nullptr;
+    for (int layer = 0; layer < 2; ++layer) {
+      if (dm.dens_s[layer]) cudaFree(dm.dens_s[layer]);
+      if (dm.dens_c[layer]) cudaFree(dm.dens_c[layer]);
+      dm.dens_s[layer] = dm.dens_c[layer] = nullptr;
+    }
     f1 = nullptr;
     if (zbl_e) cudaFree(zbl_e);
     zbl_e = nullptr;
@@ -254,6 +266,11 @@ struct smx_engine {
       A1adj_bf = dalloc<__nv_bfloat16>(T * nN * 16 * C);
       H1adj_bf = dalloc<__nv_bfloat16>(T * nN * dm.nLM * C);
     }
+    for (int layer = 0; layer < 2; ++layer)
+      if (dm.dens_spl[layer]) {
+        dm.dens_s[layer] = dalloc<float>(nN);
+        dm.dens_c[layer] = dalloc<float>(nN);
+      }
     capN = nN;
     capE = nE;
   }

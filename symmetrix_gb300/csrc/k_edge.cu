@@ -129,6 +129,12 @@ __global__ void __launch_bounds__(256) k_layer0_fwd(DevModel m, EdgeIn in, float
       zbl_e[i] = t;
     }
   }
+  if (m.dens_spl[0]) {  // density-normalised A0: A0 /= 1 + sum_j s(r_ij)  (mace.cpp:273-297)
+    const float S = dens_factor(m, 0, in, i, ti);
+    if (threadIdx.x == 0) m.dens_s[0][i] = S;
+#pragma unroll
+    for (int q = 0; q < 16; ++q) acc[q] /= S;
+  }
 #pragma unroll
   for (int q = 0; q < 16; ++q) A0[(static_cast<size_t>(i) * 16 + q) * C + k] = acc[q];
   if (m.poly_canon) {  // generated straight-line polynomials, A0 column in registers
@@ -212,6 +218,16 @@ __global__ void __launch_bounds__(256) k_contract0_rev(DevModel m, const int* __
 #pragma unroll
     for (int q = 0; q < 16; ++q) dA[q] = sGd[q * C + k];
   }
+  if (m.dens_spl[0]) {  // reverse_A0_scaled (mace.cpp:299-346): c_i = dA . A0 / s_i, dA /= s_i
+    float dot = 0.0f;
+#pragma unroll
+    for (int q = 0; q < 16; ++q) dot = fmaf(dA[q], A0[(static_cast<size_t>(i) * 16 + q) * C + k], dot);
+    dot = block_sum(dot);
+    const float S = m.dens_s[0][i];
+    if (threadIdx.x == 0) m.dens_c[0][i] = dot / S;
+#pragma unroll
+    for (int q = 0; q < 16; ++q) dA[q] /= S;
+  }
 #pragma unroll
   for (int q = 0; q < 16; ++q) A0_adj[(static_cast<size_t>(i) * 16 + q) * C + k] = dA[q];
 }
@@ -281,6 +297,13 @@ __global__ void __launch_bounds__(256) k_layer0_rev(DevModel m, EdgeIn in, const
         const double r = in.r[e];
         zbl_edge(m, m.zbl_pair[ti * m.S + in.ntype_e[e]], static_cast<float>(r), V, dV);
         for (int a = 0; a < 3; ++a) s[a] += in.xyz[3 * e + a] / r * static_cast<double>(dV);
+      }
+      if (m.dens_spl[0]) {  // dE/dx through the layer-0 density factor (mace.cpp:334-339)
+        float v, d;
+        const double r = in.r[e];
+        dens_eval(m, 0, ti, in.ntype_e[e], static_cast<float>(r), v, d);
+        const double g = static_cast<double>(m.dens_c[0][i]) * static_cast<double>(d) / r;
+        for (int a = 0; a < 3; ++a) s[a] -= g * in.xyz[3 * e + a];
       }
       for (int a = 0; a < 3; ++a) forces[3 * e + a] = -(s[a] + f1[3 * e + a]);
     }

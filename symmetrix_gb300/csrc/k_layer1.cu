@@ -360,6 +360,10 @@ __global__ void __launch_bounds__(256) k_layer1_fwd(DevModel m, EdgeIn in, const
       });
     }
   }
+  if (m.dens_spl[1]) {  // layer-1 density factor for node_tail (mace.cpp:681-705)
+    const float S = dens_factor(m, 1, in, i, ti);
+    if (threadIdx.x == 0) m.dens_s[1][i] = S;
+  }
   float* sP = dyn;  // [NP][C]: this thread's Phi1r column
 #pragma unroll
   for (int p = 0; p < NP; ++p) sP[p * C + k] = acc[p];
@@ -423,10 +427,18 @@ __global__ void __launch_bounds__(256) k_layer1_rev(DevModel m, EdgeIn in, const
     __syncthreads();
     for (int t = threadIdx.x; t < ne; t += blockDim.x) {
       double s[3] = {0.0, 0.0, 0.0};
+      const long e = static_cast<long>(eb) + t;
       if (st.row[t] >= 0)
         for (int w = 0; w < nwarp; ++w)
           for (int c = 0; c < 3; ++c) s[c] += static_cast<double>(sF[t][w][c]);
-      for (int c = 0; c < 3; ++c) f1[3 * (static_cast<long>(eb) + t) + c] = s[c];
+      if (m.dens_spl[1]) {  // dE/dx through the layer-1 density factor (mace.cpp:744-749)
+        float v, d;
+        const double r = in.r[e];
+        dens_eval(m, 1, ti, in.ntype_e[e], static_cast<float>(r), v, d);
+        const double g = static_cast<double>(m.dens_c[1][i]) * static_cast<double>(d) / r;
+        for (int c = 0; c < 3; ++c) s[c] -= g * in.xyz[3 * e + c];
+      }
+      for (int c = 0; c < 3; ++c) f1[3 * e + c] = s[c];
     }
   }
 }

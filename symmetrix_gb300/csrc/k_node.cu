@@ -95,7 +95,7 @@ void launch_gemm(const GemmBatch& b, cudaStream_t s) {
 //   dE/dH2 (MLP gradient), H1_adj[i,0,:] = w1 + W_H1[ti] dE/dH2 (other rows 0),
 //   M1_adj = W_M1 dE/dH2, A1_adj[i,lm,k] = dM1/dA1[lm] * M1_adj[k].
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_node_tail(DevModel m, const int* __restrict__ ntype, const float* __restrict__ A1,
+__global__ void __launch_bounds__(256) k_node_tail(DevModel m, const int* __restrict__ ntype, float* __restrict__ A1,
                                                    const float* __restrict__ H1, float* __restrict__ M1o,
                                                    float* __restrict__ H2o, float* __restrict__ A1_adj,
                                                    float* __restrict__ H1_adj, float* __restrict__ M1_adj_o,
@@ -116,6 +116,12 @@ __global__ void __launch_bounds__(256) k_node_tail(DevModel m, const int* __rest
   float* sS = sRed + 33 * 8;    // [33]
   float f = 0.0f;
   const float* cf = m.coef1 + static_cast<size_t>(ti) * m.T1 * C + k;
+  const bool dens = m.dens_spl[1] != nullptr;
+  const float S1 = dens ? m.dens_s[1][i] : 1.0f;
+  if (dens) {  // density-normalised A1, kept scaled (compute_A1_scaled, mace.cpp:681-705)
+#pragma unroll
+    for (int q = 0; q < 16; ++q) A1[(static_cast<size_t>(i) * 16 + q) * C + k] /= S1;
+  }
   if (m.poly_canon) {  // generated straight-line M1 polynomial and gradient
     float x[16], g[16];
 #pragma unroll
@@ -195,8 +201,15 @@ __global__ void __launch_bounds__(256) k_node_tail(DevModel m, const int* __rest
     ha = fmaf(__ldg(WT + static_cast<size_t>(c) * C), d, ha);
     m1a = fmaf(__ldg(m.H2W_M1_T + static_cast<size_t>(c) * C + k), d, m1a);
   }
+  if (dens) {  // reverse_A1_scaled (mace.cpp:707-757): c_i = dA1 . A1 / s_i, dA1 /= s_i
+    float dot = 0.0f;
 #pragma unroll
-  for (int q = 0; q < 16; ++q) A1_adj[(static_cast<size_t>(i) * 16 + q) * C + k] = sG[q * C + k] * m1a;
+    for (int q = 0; q < 16; ++q) dot = fmaf(sG[q * C + k] * m1a, A1[(static_cast<size_t>(i) * 16 + q) * C + k], dot);
+    dot = block_sum(dot);
+    if (k == 0) m.dens_c[1][i] = dot / S1;
+  }
+#pragma unroll
+  for (int q = 0; q < 16; ++q) A1_adj[(static_cast<size_t>(i) * 16 + q) * C + k] = sG[q * C + k] * m1a / S1;
   H1_adj[static_cast<size_t>(i) * m.nLM * C + k] = ha;
   for (int LM = 1; LM < m.nLM; ++LM) H1_adj[(static_cast<size_t>(i) * m.nLM + LM) * C + k] = 0.0f;
   M1o[static_cast<size_t>(i) * C + k] = f;
@@ -205,7 +218,7 @@ __global__ void __launch_bounds__(256) k_node_tail(DevModel m, const int* __rest
   H2_adj_o[static_cast<size_t>(i) * C + k] = dh2;
 }
 
-void launch_node_tail(const DevModel& m, const int* node_type, int N, const float* A1, const float* H1, float* M1,
+void launch_node_tail(const DevModel& m, const int* node_type, int N, float* A1, const float* H1, float* M1,
                       float* H2, float* A1_adj, float* H1_adj, float* M1_adj, float* H2_adj, const float* zbl_e,
                       double* energies, cudaStream_t s) {
   if (N <= 0) return;

@@ -42,7 +42,7 @@ struct GemmBatch {
 };
 void launch_gemm(const GemmBatch& b, cudaStream_t s);
 
-void launch_node_tail(const DevModel& m, const int* node_type, int N, const float* A1, const float* H1, float* M1,
+void launch_node_tail(const DevModel& m, const int* node_type, int N, float* A1, const float* H1, float* M1,
                       float* H2, float* A1_adj, float* H1_adj, float* M1_adj, float* H2_adj, const float* zbl_e,
                       double* energies, cudaStream_t s);
 void launch_scan_first(const int* num_neigh, int N, int* first, cudaStream_t s);

@@ -461,6 +461,28 @@ PackedModel pack_model(const HostModel& hm) {
   pm.n_hidden = hm.n_hidden;
   pm.e0 = f32(hm.e0);
   pm.Z = hm.Z;
+  // density-normalisation splines
+  for (int layer = 0; layer < 2; ++layer) {
+    const bool on = layer == 0 ? hm.A0_scaled : hm.A1_scaled;
+    if (!on) continue;
+    const double dh = layer == 0 ? hm.A0_h : hm.A1_h;
+    const int dK = layer == 0 ? hm.A0_K : hm.A1_K;
+    const std::vector<double>& sv = layer == 0 ? hm.A0_sv : hm.A1_sv;
+    const std::vector<double>& sd = layer == 0 ? hm.A0_sd : hm.A1_sd;
+    require(dK >= 2 && dh > 0.0, "density spline knots");
+    pm.dens_scaled[layer] = 1;
+    pm.dens_nint[layer] = dK - 1;
+    pm.dens_h[layer] = static_cast<float>(dh);
+    pm.dens_spl[layer].assign(static_cast<size_t>(hm.npairs) * (dK - 1) * 4, 0.0f);
+    for (int pr = 0; pr < hm.npairs; ++pr)
+      for (int iv = 0; iv < dK - 1; ++iv) {
+        const size_t b = static_cast<size_t>(pr) * dK + iv;
+        double c[4];
+        hermite(dh, sv[b], sv[b + 1], sd[b], sd[b + 1], c);
+        for (int q = 0; q < 4; ++q)
+          pm.dens_spl[layer][(static_cast<size_t>(pr) * (dK - 1) + iv) * 4 + q] = static_cast<float>(c[q]);
+      }
+  }
   if (hm.has_zbl) {
     pm.has_zbl = 1;
     pm.zbl_p = hm.zbl_p;

@@ -111,6 +111,11 @@ struct PackedModel {
   int n_hidden;
   std::vector<float> e0;
   std::vector<int> Z;
+  // density-normalised blocks (mace.cpp:273-346, :681-757): per unordered species pair
+  // one cubic per interval, [npairs][nint][4], on knots of spacing dens_h[layer]
+  int dens_scaled[2] = {0, 0}, dens_nint[2] = {0, 0};
+  float dens_h[2] = {0, 0};
+  std::vector<float> dens_spl[2];
   // ZBL pair repulsion (zbl.cpp): per ordered species pair (1/a, 0.5 * 14.3996 Zu Zv, r_max, 0)
   int has_zbl = 0, zbl_p = 0;
   float zbl_c[4] = {0, 0, 0, 0};

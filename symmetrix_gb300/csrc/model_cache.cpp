@@ -21,7 +21,7 @@ namespace smx {
 namespace {
 
 constexpr char kMagic[8] = {'S', 'M', 'X', 'G', 'B', '3', '0', '0'};
-constexpr uint32_t kVersion = 1;
+constexpr uint32_t kVersion = 2;
 
 struct Out {
   std::ofstream f;
@@ -73,7 +73,8 @@ bool is_model_cache(const std::string& path) {
   V(pm.cg_fwd_v) V(pm.cg_rev_off) V(pm.cg_rev_lme) V(pm.cg_rev_v) X(pm.lme_off) X(pm.num_e) V(pm.A1W[0])      \
   V(pm.A1W[1]) V(pm.A1W[2]) V(pm.A1W[3]) V(pm.A1W_T[0]) V(pm.A1W_T[1]) V(pm.A1W_T[2]) V(pm.A1W_T[3])         \
   V(pm.H2W_H1) V(pm.H2W_H1_T) V(pm.H2W_M1) V(pm.H2W_M1_T) V(pm.ro1) V(pm.ro2_w1) V(pm.ro2_w2)                \
-  X(pm.ro2_scale) X(pm.n_hidden) V(pm.e0) V(pm.Z) X(pm.has_zbl) X(pm.zbl_p) X(pm.zbl_c) V(pm.zbl_pair)
+  X(pm.ro2_scale) X(pm.n_hidden) V(pm.e0) V(pm.Z) X(pm.has_zbl) X(pm.zbl_p) X(pm.zbl_c) V(pm.zbl_pair) \
+  X(pm.dens_scaled) X(pm.dens_nint) X(pm.dens_h) V(pm.dens_spl[0]) V(pm.dens_spl[1])
 
 void save_model_cache(const std::string& path, const HostModel& hm, const PackedModel& pm) {
   Out o;

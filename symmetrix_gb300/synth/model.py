@@ -78,8 +78,15 @@ def _spline_tables(r_knots, values):
 def make_model(num_channels=32, species=("H", "C", "O"), r_cut=5.0, L_max=1, correlation=3,
                num_bessel=8, envelope_p=5, num_knots=200, avg_num_neighbors=None, seed=0,
                radial_hidden=(64, 64), l_max=3, a0_gain=7.0, a1_gain=12.0, energy_scale=0.35, zbl=False,
-               core=(0.8, 1.3)):
-    """Return a dict in libsymmetrix's MACE JSON layout for a random two-layer MACE."""
+               core=(0.8, 1.3), density_scaled=False):
+    """Return a dict in libsymmetrix's MACE JSON layout for a random two-layer MACE.
+
+    density_scaled: density-normalised interaction blocks (A0_scaled / A1_scaled,
+    libsymmetrix/source/mace.cpp:273-346, :681-757): A is divided by 1 + sum_j s(r_ij)
+    with one spline s per unordered species pair and layer, s(r) = w tanh(b(r).v)^2 on
+    the Bessel-envelope basis b (non-negative, zero at r_cut, as MACE's density
+    blocks); drawn from a separate stream so the other weights equal the unscaled
+    model's of the same seed."""
     if l_max != 3:
         raise ValueError("the evaluator supports l_max = 3 only")
     if correlation > 3:
@@ -202,6 +209,23 @@ def make_model(num_channels=32, species=("H", "C", "O"), r_cut=5.0, L_max=1, cor
     out["readout_2_weights_1"] = (rng.normal(size=(16, C)) / np.sqrt(C)).flatten().tolist()
     out["readout_2_weights_2"] = (energy_scale * rng.normal(size=16) / 4.0).tolist()
     out["readout_2_scale_factor"] = 1.679
+
+    if density_scaled:
+        drng = np.random.default_rng(seed + 7919)
+        for layer in ("A0", "A1"):
+            vals, ders = [], []
+            for a in range(S):
+                for b in range(a, S):
+                    v = drng.normal(size=num_bessel) * 2.0
+                    w = 0.05 * (1.0 + drng.random())
+                    dens = w * np.tanh(emb @ v) ** 2
+                    vv, dd = _spline_tables(r_knots, dens[:, None])
+                    vals.append(vv[0].tolist())
+                    ders.append(dd[0].tolist())
+            out[f"{layer}_scaled"] = True
+            out[f"{layer}_spline_h"] = float(h)
+            out[f"{layer}_spline_values"] = vals
+            out[f"{layer}_spline_derivs"] = ders
     return out
 
 

@@ -12,10 +12,16 @@ import pytest
 from symmetrix_gb300 import _lib, save_model_cache
 
 
-def test_cache_round_trip_is_exact(engine_lib, small_model_path, tmp_path):
+@pytest.mark.parametrize("variant", ["plain", "density_zbl"])
+def test_cache_round_trip_is_exact(engine_lib, small_model_path, tmp_path, variant):
+    from symmetrix_gb300.synth.model import CONFIGS, make_model, write_model
+    src = small_model_path
+    if variant == "density_zbl":
+        src = write_model(make_model(**dict(CONFIGS["small"], num_knots=40), seed=2, density_scaled=True, zbl=True),
+                          str(tmp_path / "dz.json"))
     a, b = str(tmp_path / "a.smxb"), str(tmp_path / "b.smxb")
     t = time.time()
-    save_model_cache(small_model_path, a)
+    save_model_cache(src, a)
     t_json = time.time() - t
     t = time.time()
     save_model_cache(a, b)

@@ -164,6 +164,20 @@ void smx_md_destroy(smx_md* md);
 int smx_energy_virial_device_noalloc(int num_nodes, long num_edges, const double* node_energies, const double* xyz,
                                      const double* node_forces, double* out, void* stream);
 
+/* ---- batching form: many independent non-periodic molecules ---------------
+ * Molecule m holds atoms [mol_first[m], mol_first[m+1]) (mol_first[0] = 0,
+ * mol_first[n_mol] = number of atoms).  One neighbour build, one launch per engine
+ * stage for the whole batch; edges only join atoms of the same molecule, wherever
+ * the molecules sit in space.  Per-molecule energies, per-atom energies and forces.
+ * The reference evaluates one structure per MACE::compute_node_energies_forces call
+ * (libsymmetrix/source/mace.cpp:17-64); this batches what its callers would loop over. */
+int smx_compute_molecules(smx_engine* eng, int n_mol, const int* mol_first, const double* positions,
+                          const int* species, double* mol_energies, double* node_energies, double* forces);
+/* velocity-Verlet MD of such a batch (as smx_md_create with no box) */
+smx_md* smx_md_create_molecules(smx_engine* eng, int n_mol, const int* mol_first, const double* positions,
+                                const double* velocities, const int* species, const double* masses, double dt_fs,
+                                double skin, int rebuild_every);
+
 /* ---- LAMMPS pair-style adapter -------------------------------------------
  * One compute() of pair_style symmetrix/mace in its no-domain-decomposition mode:
  * replaces PairSymmetrixMACE::compute_no_domain_decomposition

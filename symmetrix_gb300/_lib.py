@@ -44,6 +44,8 @@ SIGNATURES = [
     ("smx_md_num_edges", _L, [_P]),
     ("smx_md_destroy", None, [_P]),
     ("smx_energy_virial_device_noalloc", _I, [_I, _L, _P, _P, _P, _P, _P]),
+    ("smx_compute_molecules", _I, [_P, _I, _P, _P, _P, _P, _P, _P]),
+    ("smx_md_create_molecules", _P, [_P, _I, _P, _P, _P, _P, _P, _D, _D, _I]),
     ("smx_pair_create", _P, [_P]),
     ("smx_pair_destroy", None, [_P]),
     ("smx_pair_compute", _I, [_P, _I, _I, _P, _P, _P, _I, _I, _P, _P, _P, _P, _I, _I, _I, _I, _P, _P, _P, _P]),

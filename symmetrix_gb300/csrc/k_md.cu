@@ -124,15 +124,18 @@ __global__ void k_neigh_cells(const double* __restrict__ pos, const int* __restr
 // Small or non-periodic systems: all pairs over the periodic images in range.
 template <bool FILL>
 __global__ void k_neigh_brute(const double* __restrict__ pos, const int* __restrict__ species, int N, double3 box,
-                              int3 nimg, double rl2, int* __restrict__ num_neigh, const int* __restrict__ first,
-                              int* __restrict__ nidx, int* __restrict__ ntype_e, int* __restrict__ edge_i,
-                              char4* __restrict__ shift, long cap) {
+                              int3 nimg, double rl2, const int* __restrict__ seg_of, const int* __restrict__ seg_first,
+                              int* __restrict__ num_neigh, const int* __restrict__ first, int* __restrict__ nidx,
+                              int* __restrict__ ntype_e, int* __restrict__ edge_i, char4* __restrict__ shift,
+                              long cap) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
   const double xi = pos[3 * i], yi = pos[3 * i + 1], zi = pos[3 * i + 2];
   int count = 0;
   long slot = FILL ? first[i] : 0;
-  for (int j = 0; j < N; ++j)
+  // with segments (a batch of molecules), only atoms of i's own segment are candidates
+  const int j0 = seg_of ? seg_first[seg_of[i]] : 0, j1 = seg_of ? seg_first[seg_of[i] + 1] : N;
+  for (int j = j0; j < j1; ++j)
     for (int sx = -nimg.x; sx <= nimg.x; ++sx)
       for (int sy = -nimg.y; sy <= nimg.y; ++sy)
         for (int sz = -nimg.z; sz <= nimg.z; ++sz) {
@@ -286,17 +289,18 @@ void launch_cell_list(const double* pos, int N, double3 box, int3 nc, int* cell,
 
 void launch_neigh_pass(bool fill, bool brute, const double* pos, const int* species, int N, double3 box, int3 nc,
                        int3 periodic, int3 nimg, double rl, const int* cell, const int* cell_start,
-                       const int* cell_atoms, int* num_neigh, const int* first, int* nidx, int* ntype_e, int* edge_i,
-                       char4* shift, long cap, cudaStream_t s) {
+                       const int* cell_atoms, const int* seg_of, const int* seg_first, int* num_neigh,
+                       const int* first, int* nidx, int* ntype_e, int* edge_i, char4* shift, long cap,
+                       cudaStream_t s) {
   const double rl2 = rl * rl;
   const int g = ceil_div(N, 128);
-  if (brute) {
+  if (brute || seg_of) {
     if (fill)
-      k_neigh_brute<true><<<g, 128, 0, s>>>(pos, species, N, box, nimg, rl2, num_neigh, first, nidx, ntype_e, edge_i,
-                                            shift, cap);
+      k_neigh_brute<true><<<g, 128, 0, s>>>(pos, species, N, box, nimg, rl2, seg_of, seg_first, num_neigh, first,
+                                            nidx, ntype_e, edge_i, shift, cap);
     else
-      k_neigh_brute<false><<<g, 128, 0, s>>>(pos, species, N, box, nimg, rl2, num_neigh, first, nidx, ntype_e,
-                                             edge_i, shift, cap);
+      k_neigh_brute<false><<<g, 128, 0, s>>>(pos, species, N, box, nimg, rl2, seg_of, seg_first, num_neigh, first,
+                                             nidx, ntype_e, edge_i, shift, cap);
   } else {
     if (fill)
       k_neigh_cells<true><<<g, 128, 0, s>>>(pos, species, N, box, nc, periodic, rl2, cell, cell_start, cell_atoms,

@@ -76,8 +76,9 @@ void launch_cell_list(const double* pos, int N, double3 box, int3 nc, int* cell,
                       int* cell_fill, int* cell_atoms, cudaStream_t s);
 void launch_neigh_pass(bool fill, bool brute, const double* pos, const int* species, int N, double3 box, int3 nc,
                        int3 periodic, int3 nimg, double rl, const int* cell, const int* cell_start,
-                       const int* cell_atoms, int* num_neigh, const int* first, int* nidx, int* ntype_e, int* edge_i,
-                       char4* shift, long cap, cudaStream_t s);
+                       const int* cell_atoms, const int* seg_of, const int* seg_first, int* num_neigh,
+                       const int* first, int* nidx, int* ntype_e, int* edge_i, char4* shift, long cap,
+                       cudaStream_t s);
 void launch_reverse_edges(long cap, int N, const int* first, const int* nidx, const int* edge_i, const char4* shift,
                           int* rev, cudaStream_t s);
 void launch_edge_geometry(long cap, int N, const int* first, const double* pos, double3 box, const int* nidx,

@@ -80,8 +80,11 @@ struct NeighList {
     realloc_happened = true;
   }
 
-  // Build the list for positions pos (wrapped in place for periodic axes).
-  void build(double* pos, const int* species, int N, double3 box, int3 periodic, double rl, cudaStream_t s) {
+  // Build the list for positions pos (wrapped in place for periodic axes).  With
+  // segments (seg_of[atom], seg_first[segment]: a batch of non-periodic molecules) only
+  // atoms of the same segment are neighbours.
+  void build(double* pos, const int* species, int N, double3 box, int3 periodic, double rl, cudaStream_t s,
+             const int* seg_of = nullptr, const int* seg_first = nullptr) {
     const double L[3] = {box.x, box.y, box.z};
     const int per[3] = {periodic.x, periodic.y, periodic.z};
     int n[3];
@@ -98,7 +101,7 @@ struct NeighList {
       *img[d] = static_cast<int>(std::ceil(rl / L[d]));
       if (n[d] < 3) brute = true;
     }
-    if (brute && N > 200000)
+    if (brute && !seg_of && N > 200000)
       throw std::invalid_argument("non-periodic or small-box neighbour search is limited to 200000 atoms");
     const int3 nc = make_int3(n[0], n[1], n[2]);
     reserve_nodes(N, nc.x * nc.y * nc.z);
@@ -106,7 +109,7 @@ struct NeighList {
     if (!brute)
       smx::launch_cell_list(pos, N, box, nc, cell, cell_count, cell_start, cell_fill, cell_atoms, s);
     smx::launch_neigh_pass(false, brute, pos, species, N, box, nc, periodic, nimg, rl, cell, cell_start, cell_atoms,
-                           num_neigh, first, nidx, ntype_e, edge_i, shift, capE, s);
+                           seg_of, seg_first, num_neigh, first, nidx, ntype_e, edge_i, shift, capE, s);
     smx::launch_scan_first(num_neigh, N, first, s);
     int total = 0;
     check(cudaMemcpyAsync(&total, first + N, sizeof(int), cudaMemcpyDeviceToHost, s), "D2H");
@@ -114,7 +117,7 @@ struct NeighList {
     E = total;
     reserve_edges(E);
     smx::launch_neigh_pass(true, brute, pos, species, N, box, nc, periodic, nimg, rl, cell, cell_start, cell_atoms,
-                           num_neigh, first, nidx, ntype_e, edge_i, shift, capE, s);
+                           seg_of, seg_first, num_neigh, first, nidx, ntype_e, edge_i, shift, capE, s);
     smx::launch_reverse_edges(capE, N, first, nidx, edge_i, shift, rev, s);
   }
 };
@@ -128,6 +131,24 @@ void box_args(const double* box_lengths, double3& box, int3& periodic) {
     box = make_double3(1.0, 1.0, 1.0);
     periodic = make_int3(0, 0, 0);
   }
+}
+
+// Molecule offsets (mol_first[0] = 0 <= ... <= mol_first[n_mol] = n_atoms) -> the
+// atom -> molecule map.
+std::vector<int> molecule_of(int n_mol, const int* mol_first, int n_atoms) {
+  if (n_mol < 0 || (n_mol > 0 && !mol_first)) throw std::invalid_argument("bad molecule offsets");
+  if (n_mol == 0) {
+    if (n_atoms != 0) throw std::invalid_argument("atoms outside every molecule");
+    return {};
+  }
+  if (mol_first[0] != 0 || mol_first[n_mol] != n_atoms)
+    throw std::invalid_argument("molecule offsets must start at 0 and end at n_atoms");
+  std::vector<int> of(n_atoms);
+  for (int m = 0; m < n_mol; ++m) {
+    if (mol_first[m + 1] < mol_first[m]) throw std::invalid_argument("molecule offsets must not decrease");
+    for (int a = mol_first[m]; a < mol_first[m + 1]; ++a) of[a] = m;
+  }
+  return of;
 }
 
 }  // namespace
@@ -147,6 +168,7 @@ struct smx_md {
   double *pos = nullptr, *vel = nullptr, *F = nullptr, *inv_m = nullptr, *energies = nullptr, *partial = nullptr,
          *reduced = nullptr;
   int* species = nullptr;
+  int *seg_of = nullptr, *seg_first = nullptr;  // molecule batch: atom -> molecule, molecule atom offsets
   NeighList nl;
   cudaGraphExec_t graph = nullptr;
   int graph_steps = 0;
@@ -154,7 +176,7 @@ struct smx_md {
 
   ~smx_md() {
     if (graph) cudaGraphExecDestroy(graph);
-    void* ps[] = {pos, vel, F, inv_m, energies, partial, reduced, species};
+    void* ps[] = {pos, vel, F, inv_m, energies, partial, reduced, species, seg_of, seg_first};
     for (void* p : ps)
       if (p) cudaFree(p);
   }
@@ -178,12 +200,22 @@ struct smx_md {
 
   void rebuild(cudaStream_t s) {
     nl.realloc_happened = false;
-    nl.build(pos, species, N, box, periodic, eng->hm.r_cut + skin, s);
+    nl.build(pos, species, N, box, periodic, eng->hm.r_cut + skin, s, seg_of, seg_first);
     eng->reserve(N, nl.capE);
     if (nl.realloc_happened && graph) {
       cudaGraphExecDestroy(graph);
       graph = nullptr;
     }
+  }
+
+  // a batch of independent non-periodic molecules: neighbours only inside a molecule
+  void set_molecules(int n_mol, const int* mol_first, cudaStream_t s) {
+    const std::vector<int> of = molecule_of(n_mol, mol_first, N);
+    seg_of = dalloc<int>(N);
+    seg_first = dalloc<int>(n_mol + 1);
+    check(cudaMemcpyAsync(seg_of, of.data(), sizeof(int) * N, cudaMemcpyHostToDevice, s), "H2D");
+    check(cudaMemcpyAsync(seg_first, mol_first, sizeof(int) * (n_mol + 1), cudaMemcpyHostToDevice, s), "H2D");
+    check(cudaStreamSynchronize(s), "molecule upload");  // `of` goes out of scope
   }
 
   void run(int steps) {
@@ -219,9 +251,13 @@ struct smx_md {
 
 extern "C" {
 
-int smx_compute_atoms(smx_engine* eng, int n_atoms, const double* positions, const int* species,
-                      const double* box_lengths, double* energy, double* node_energies, double* forces,
-                      double* virial) {
+}  // extern "C"
+
+namespace {
+
+int compute_atoms_impl(smx_engine* eng, int n_atoms, const double* positions, const int* species,
+                       const double* box_lengths, int n_mol, const int* mol_first, double* energy,
+                       double* node_energies, double* forces, double* virial) {
   if (!eng) return fail(SMX_ERR_INVALID, "engine is NULL");
   if (n_atoms < 0 || (n_atoms > 0 && (!positions || !species || !forces)))
     return fail(SMX_ERR_INVALID, "bad atom arrays");
@@ -252,6 +288,7 @@ int smx_compute_atoms(smx_engine* eng, int n_atoms, const double* positions, con
     md.reduced = dalloc<double>(10);
     check(cudaMemcpyAsync(md.pos, positions, sizeof(double) * 3 * n_atoms, cudaMemcpyHostToDevice, s), "H2D");
     check(cudaMemcpyAsync(md.species, species, sizeof(int) * n_atoms, cudaMemcpyHostToDevice, s), "H2D");
+    if (mol_first) md.set_molecules(n_mol, mol_first, s);
     md.rebuild(s);
     md.forces(s);
     smx::launch_reduce(n_atoms, md.nl.first, md.energies, md.nl.xyz, md.nl.forces, md.partial, smx_md::kReduceBlocks,
@@ -270,12 +307,13 @@ int smx_compute_atoms(smx_engine* eng, int n_atoms, const double* positions, con
   } catch (const std::exception& e) {
     return fail(SMX_ERR_INVALID, e.what());
   }
+  if (eng->take_status() != SMX_OK) return fail(SMX_ERR_TIMEOUT, "a device-side wait timed out; results are invalid");
   return SMX_OK;
 }
 
-smx_md* smx_md_create(smx_engine* eng, int n_atoms, const double* positions, const double* velocities,
-                      const int* species, const double* masses, const double* box_lengths, double dt_fs, double skin,
-                      int rebuild_every) {
+smx_md* md_create_impl(smx_engine* eng, int n_atoms, const double* positions, const double* velocities,
+                       const int* species, const double* masses, const double* box_lengths, int n_mol,
+                       const int* mol_first, double dt_fs, double skin, int rebuild_every) {
   if (!eng || n_atoms <= 0 || !positions || !species || !masses || rebuild_every < 1 || !(dt_fs > 0) ||
       !(skin >= 0)) {
     fail(SMX_ERR_INVALID, "bad MD arguments");
@@ -312,6 +350,7 @@ smx_md* smx_md_create(smx_engine* eng, int n_atoms, const double* positions, con
     check(cudaMemcpyAsync(md->vel, v.data(), sizeof(double) * 3 * n_atoms, cudaMemcpyHostToDevice, s), "H2D");
     check(cudaMemcpyAsync(md->inv_m, inv.data(), sizeof(double) * n_atoms, cudaMemcpyHostToDevice, s), "H2D");
     check(cudaMemcpyAsync(md->species, species, sizeof(int) * n_atoms, cudaMemcpyHostToDevice, s), "H2D");
+    if (mol_first) md->set_molecules(n_mol, mol_first, s);
     md->rebuild(s);
     md->forces(s);
     check(cudaStreamSynchronize(s), "initial forces");
@@ -323,6 +362,53 @@ smx_md* smx_md_create(smx_engine* eng, int n_atoms, const double* positions, con
     return nullptr;
   }
   return md.release();
+}
+
+}  // namespace
+
+extern "C" {
+
+int smx_compute_atoms(smx_engine* eng, int n_atoms, const double* positions, const int* species,
+                      const double* box_lengths, double* energy, double* node_energies, double* forces,
+                      double* virial) {
+  return compute_atoms_impl(eng, n_atoms, positions, species, box_lengths, 0, nullptr, energy, node_energies, forces,
+                            virial);
+}
+
+int smx_compute_molecules(smx_engine* eng, int n_mol, const int* mol_first, const double* positions,
+                          const int* species, double* mol_energies, double* node_energies, double* forces) {
+  if (n_mol < 0 || (n_mol > 0 && !mol_first)) return fail(SMX_ERR_INVALID, "bad molecule offsets");
+  const int n_atoms = n_mol > 0 ? mol_first[n_mol] : 0;
+  std::vector<double> ne(static_cast<size_t>(n_atoms));
+  const int code = compute_atoms_impl(eng, n_atoms, positions, species, nullptr, n_mol, n_mol > 0 ? mol_first : nullptr,
+                                      nullptr, ne.data(), forces, nullptr);
+  if (code != SMX_OK) return code;
+  if (node_energies && n_atoms > 0) std::memcpy(node_energies, ne.data(), sizeof(double) * n_atoms);
+  if (mol_energies)
+    for (int m = 0; m < n_mol; ++m) {
+      double e = 0.0;
+      for (int a = mol_first[m]; a < mol_first[m + 1]; ++a) e += ne[a];
+      mol_energies[m] = e;
+    }
+  return SMX_OK;
+}
+
+smx_md* smx_md_create(smx_engine* eng, int n_atoms, const double* positions, const double* velocities,
+                      const int* species, const double* masses, const double* box_lengths, double dt_fs, double skin,
+                      int rebuild_every) {
+  return md_create_impl(eng, n_atoms, positions, velocities, species, masses, box_lengths, 0, nullptr, dt_fs, skin,
+                        rebuild_every);
+}
+
+smx_md* smx_md_create_molecules(smx_engine* eng, int n_mol, const int* mol_first, const double* positions,
+                                const double* velocities, const int* species, const double* masses, double dt_fs,
+                                double skin, int rebuild_every) {
+  if (n_mol <= 0 || !mol_first) {
+    fail(SMX_ERR_INVALID, "bad molecule offsets");
+    return nullptr;
+  }
+  return md_create_impl(eng, mol_first[n_mol], positions, velocities, species, masses, nullptr, n_mol, mol_first,
+                        dt_fs, skin, rebuild_every);
 }
 
 int smx_md_run(smx_md* md, int steps) {

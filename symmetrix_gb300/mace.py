@@ -113,6 +113,28 @@ class MACE:
         _lib.raise_for(code, self._lib)
         return e.value, node_e, forces, virial.reshape(3, 3)
 
+    def compute_molecules(self, molecules):
+        """Batching form: evaluate many independent non-periodic molecules in one pass.
+
+        molecules: sequence of (positions (n, 3), species (n,)).  Returns (energies per
+        molecule, list of node-energy arrays, list of force arrays)."""
+        pos = [np.asarray(p, dtype=np.float64).reshape(-1, 3) for p, _ in molecules]
+        sp = [np.asarray(s, dtype=np.int32).reshape(-1) for _, s in molecules]
+        counts = np.array([len(p) for p in pos], dtype=np.int64)
+        if any(len(a) != len(b) for a, b in zip(pos, sp)):
+            raise ValueError("species and positions differ in length")
+        first = np.concatenate([[0], np.cumsum(counts)]).astype(np.int32)
+        X = np.ascontiguousarray(np.concatenate(pos) if pos else np.zeros((0, 3)))
+        S = np.ascontiguousarray(np.concatenate(sp) if sp else np.zeros(0, np.int32))
+        n = len(X)
+        e_mol = np.zeros(len(pos))
+        node_e = np.zeros(n)
+        F = np.zeros((n, 3))
+        code = self._lib.smx_compute_molecules(self._h, len(pos), _ptr(first), _ptr(X), _ptr(S), _ptr(e_mol),
+                                               _ptr(node_e), _ptr(F))
+        _lib.raise_for(code, self._lib)
+        return e_mol, np.split(node_e, first[1:-1]), np.split(F, first[1:-1])
+
     @property
     def stream(self):
         """Address of the engine's CUDA stream (host-pointer calls and MD run on it)."""

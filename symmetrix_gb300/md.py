@@ -13,7 +13,9 @@ from .mace import _ptr
 
 class MD:
     def __init__(self, engine, positions, species, masses, box=None, velocities=None, dt=0.5, skin=1.0,
-                 rebuild_every=10):
+                 rebuild_every=10, mol_first=None):
+        """mol_first: optional molecule offsets (batching form): the atoms form independent
+        non-periodic molecules [mol_first[m], mol_first[m+1]); box must then be None."""
         self._lib = _lib.load()
         self.engine = engine  # keeps the engine alive
         pos = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
@@ -22,8 +24,15 @@ class MD:
         m = np.ascontiguousarray(masses, dtype=np.float64)
         v = None if velocities is None else np.ascontiguousarray(velocities, dtype=np.float64).reshape(-1, 3)
         bx = None if box is None else np.ascontiguousarray(np.broadcast_to(box, 3), dtype=np.float64)
-        h = self._lib.smx_md_create(engine._h, self.n, _ptr(pos), _ptr(v), _ptr(sp), _ptr(m), _ptr(bx), float(dt),
-                                    float(skin), int(rebuild_every))
+        if mol_first is not None:
+            if box is not None:
+                raise ValueError("a batch of molecules is non-periodic: box must be None")
+            mf = np.ascontiguousarray(mol_first, dtype=np.int32)
+            h = self._lib.smx_md_create_molecules(engine._h, len(mf) - 1, _ptr(mf), _ptr(pos), _ptr(v), _ptr(sp),
+                                                  _ptr(m), float(dt), float(skin), int(rebuild_every))
+        else:
+            h = self._lib.smx_md_create(engine._h, self.n, _ptr(pos), _ptr(v), _ptr(sp), _ptr(m), _ptr(bx),
+                                        float(dt), float(skin), int(rebuild_every))
         if not h:
             raise RuntimeError(self._lib.smx_last_error().decode(errors="replace"))
         self._h = ctypes.c_void_p(h)

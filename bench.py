@@ -518,12 +518,86 @@ def gpu_arm(args, rank, world, local_rank):
         dist.destroy_process_group()
 
 
+# ---------------------------------------------------------------------------
+# batching form (--workload molecules): not the headline line
+# ---------------------------------------------------------------------------
+MOLECULES = dict(name="molecules_2048", n_mol=2048, sizes=(8, 120), density=0.08, min_dist=0.95, seed=4,
+                 species=("H", "C", "N", "O", "F", "S", "Cl"), probs=(0.45, 0.30, 0.08, 0.10, 0.03, 0.02, 0.02))
+
+
+def molecules_arm(args):
+    import torch
+
+    from symmetrix_gb300 import MACE
+    from symmetrix_gb300.build import build
+    from symmetrix_gb300.md import MD
+    from symmetrix_gb300.synth.model import CONFIGS, make_model, write_model
+    from symmetrix_gb300.synth.structures import maxwell_boltzmann, random_molecule, species_masses
+
+    build()
+    os.makedirs(CACHE, exist_ok=True)
+    path = os.path.join(CACHE, "model_molecules_zbl_s1.json")
+    if not os.path.exists(path):
+        write_model(make_model(**CONFIGS["molecules"], seed=1, zbl=True), path + ".tmp")
+        os.replace(path + ".tmp", path)
+    W = MOLECULES
+    sfile = os.path.join(CACHE, f"{W['name']}_s{W['seed']}.npz")
+    if os.path.exists(sfile):
+        z = np.load(sfile)
+        pos, sp, first = z["pos"], z["sp"], z["first"]
+    else:
+        rng = np.random.default_rng(W["seed"])
+        P, S_, counts = [], [], []
+        for m in range(W["n_mol"]):
+            k = int(rng.integers(W["sizes"][0], W["sizes"][1] + 1))
+            p, s_ = random_molecule(k, W["density"], W["min_dist"], len(W["species"]), rng, probs=W["probs"])
+            # molecules on a 40 A grid (independence is by molecule, not by distance)
+            P.append(p + 40.0 * np.array([m % 16, (m // 16) % 16, m // 256]))
+            S_.append(s_)
+            counts.append(k)
+        pos, sp = np.concatenate(P), np.concatenate(S_).astype(np.int32)
+        first = np.concatenate([[0], np.cumsum(counts)]).astype(np.int32)
+        np.savez(sfile, pos=pos, sp=sp, first=first)
+    N = len(pos)
+    dev = torch.device("cuda", 0)
+    out = {}
+    for form in ("fp32", "bf16"):
+        eng = MACE(path, precision=form)
+        estream = torch.cuda.ExternalStream(eng.stream, device=dev)
+        masses = species_masses(eng.atomic_numbers, sp)
+        vel = maxwell_boltzmann(masses, 300.0, np.random.default_rng(7))
+        md = MD(eng, pos, sp, masses, velocities=vel, dt=0.5, skin=1.0, rebuild_every=10, mol_first=first)
+        md.run(args.warmup)
+        md.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(estream)
+        md.run(args.steps)
+        e1.record(estream)
+        md.sync()
+        T = e0.elapsed_time(e1) / 1e3
+        out[form] = {"value": N * args.steps / T, "ms_per_step": T / args.steps * 1e3, "edges": md.num_edges}
+        del md, eng
+    print(json.dumps({
+        "metric": METRIC, "value": out["bf16"]["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": out["bf16"]["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+        "config": {"workload": f"{W['name']}: {W['n_mol']} non-periodic molecules of {W['sizes'][0]}-{W['sizes'][1]} "
+                               f"atoms ({N} atoms), 64x0e+64x1o, r_cut 5 A, H/C/N/O/F/S/Cl, ZBL; batch MD, dt 0.5 fs, "
+                               "neighbour list per molecule rebuilt every 10 steps, CUDA graph between rebuilds",
+                   "atoms": N},
+        "forms": out, "bf16_over_fp32": out["bf16"]["value"] / out["fp32"]["value"],
+    }), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="fp32_4096", choices=["fp32_4096", "molecules"],
+                    help="fp32_4096: the headline line; molecules: the batching form (2048 molecules)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -532,6 +606,9 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", 0))
     if args.impl == "reference":
         reference_arm(args, rank, world)
+    elif args.workload == "molecules":
+        if rank == 0:
+            molecules_arm(args)
     else:
         gpu_arm(args, rank, world, local_rank)
 

@@ -22,47 +22,6 @@ namespace smx {
 
 namespace {
 
-// Stage the geometry of edges [eb, eb+ne) of centre node i into shared memory.
-// base[t] = spline row (pair * nint + interval) * stride, or -1 if r >= r_cut.
-template <bool GRAD>
-__device__ __forceinline__ void stage_edges(const DevModel& m, const EdgeIn& in, int ti, int eb, int ne,
-                                            bool ordered_pair, int stride, float (*sY)[kEdgeChunk],
-                                            float (*sG)[kEdgeChunk], float (*su)[kEdgeChunk], float* sx,
-                                            int* sbase, int* sj) {
-  for (int t = threadIdx.x; t < ne; t += blockDim.x) {
-    const long e = static_cast<long>(eb) + t;
-    const float vx = static_cast<float>(in.xyz[3 * e]);
-    const float vy = static_cast<float>(in.xyz[3 * e + 1]);
-    const float vz = static_cast<float>(in.xyz[3 * e + 2]);
-    const float rr = static_cast<float>(in.r[e]);
-    float Y[16], G[48];
-    sph_harm16<GRAD>(vx, vy, vz, Y, G);
-#pragma unroll
-    for (int q = 0; q < 16; ++q) sY[q][t] = Y[q];
-    if constexpr (GRAD) {
-#pragma unroll
-      for (int q = 0; q < 48; ++q) sG[q][t] = G[q];
-      const float inv = 1.0f / rr;
-      su[0][t] = vx * inv;
-      su[1][t] = vy * inv;
-      su[2][t] = vz * inv;
-    }
-    int iv = static_cast<int>(rr * m.inv_h);
-    iv = iv < 0 ? 0 : (iv >= m.nint ? m.nint - 1 : iv);
-    sx[t] = rr - static_cast<float>(iv) * m.h;
-    const int tj = in.ntype_e[e];
-    int pr;
-    if (ordered_pair) {
-      pr = ti * m.S + tj;
-    } else {
-      const int a = ti < tj ? ti : tj, b = ti < tj ? tj : ti;
-      pr = a * (2 * m.S - a - 1) / 2 + b;
-    }
-    sbase[t] = (rr < m.r_cut) ? (pr * m.nint + iv) * stride : -1;
-    if (sj) sj[t] = in.nidx[e];
-  }
-}
-
 // Sum a per-thread 3-vector over the block's channels for edge t: float32 warp
 // shuffles (float64 arithmetic is slow on this part), then one partial per warp into
 // sF, summed across warps in float64 after the chunk.
@@ -78,6 +37,57 @@ __device__ __forceinline__ void block_reduce3(float fx, float fy, float fz, floa
 
 }  // namespace
 
+namespace {
+
+// Edge chunk staged for the layer-0 kernels: Y_lm (and, for the adjoint, dY/dx, dY/dy,
+// dY/dz) packed as float4 rows, the ordered-pair spline row of the folded layer-0 table, and the
+// compacted list of active edges (r < r_cut).
+template <bool GRAD>
+struct L0Stage {
+  float4 Y[kEdgeChunk][4];
+  float4 G[GRAD ? kEdgeChunk : 1][16];  // (dY_lm/dx, dY_lm/dy, dY_lm/dz, 0)
+  float4 u[GRAD ? kEdgeChunk : 1];
+  float x[kEdgeChunk];
+  int row[kEdgeChunk];  // (ti * S + tj) * nint + interval, or -1
+  int act[kEdgeChunk];
+  int nact;
+};
+
+template <bool GRAD>
+__device__ __forceinline__ void stage_l0(const DevModel& m, const EdgeIn& in, int ti, int eb, int ne,
+                                         L0Stage<GRAD>& st) {
+  if (threadIdx.x >= 32) return;
+  const int t = threadIdx.x;
+  bool active = false;
+  if (t < ne) {
+    const long e = static_cast<long>(eb) + t;
+    const float vx = static_cast<float>(in.xyz[3 * e]);
+    const float vy = static_cast<float>(in.xyz[3 * e + 1]);
+    const float vz = static_cast<float>(in.xyz[3 * e + 2]);
+    const float rr = static_cast<float>(in.r[e]);
+    float Y[16], G[GRAD ? 48 : 1];
+    sph_harm16<GRAD>(vx, vy, vz, Y, G);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) st.Y[t][q] = make_float4(Y[4 * q], Y[4 * q + 1], Y[4 * q + 2], Y[4 * q + 3]);
+    if constexpr (GRAD) {
+#pragma unroll
+      for (int c = 0; c < 16; ++c) st.G[t][c] = make_float4(G[c], G[16 + c], G[32 + c], 0.0f);
+      const float inv = 1.0f / rr;
+      st.u[t] = make_float4(vx * inv, vy * inv, vz * inv, 0.0f);
+    }
+    int iv = static_cast<int>(rr * m.inv_h);
+    iv = iv < 0 ? 0 : (iv >= m.nint ? m.nint - 1 : iv);
+    st.x[t] = rr - static_cast<float>(iv) * m.h;
+    active = rr < m.r_cut;
+    st.row[t] = active ? (ti * m.S + in.ntype_e[e]) * m.nint + iv : -1;
+  }
+  const unsigned ball = __ballot_sync(0xffffffffu, active);
+  if (active) st.act[__popc(ball & ((1u << t) - 1u))] = t;
+  if (t == 0) st.nact = __popc(ball);
+}
+
+}  // namespace
+
 // ---------------------------------------------------------------------------
 // Layer 0 forward: A0[i,lm,k] = sum_j Y_lm(x_ij) R0'_{ti,tj,l}(r_ij)[k] with the
 // folded ordered-pair splines, then M0[i,LM,k] = P_{ti,LM,k}(A0[i,:,k]).
@@ -85,9 +95,7 @@ __device__ __forceinline__ void block_reduce3(float fx, float fy, float fz, floa
 __global__ void __launch_bounds__(256) k_layer0_fwd(DevModel m, EdgeIn in, float* __restrict__ A0,
                                                     float* __restrict__ M0, float* __restrict__ zbl_e) {
   extern __shared__ float dyn[];
-  __shared__ float sY[16][kEdgeChunk];
-  __shared__ float sx[kEdgeChunk];
-  __shared__ int sbase[kEdgeChunk];
+  __shared__ L0Stage<false> st;
   const int C = m.C, k = threadIdx.x, i = blockIdx.x;
   const int ti = in.node_type[i];
   const int e0 = in.first[i], e1 = in.first[i + 1];
@@ -97,18 +105,37 @@ __global__ void __launch_bounds__(256) k_layer0_fwd(DevModel m, EdgeIn in, float
   for (int eb = e0; eb < e1; eb += kEdgeChunk) {
     const int ne = min(kEdgeChunk, e1 - eb);
     __syncthreads();
-    stage_edges<false>(m, in, ti, eb, ne, true, 4, sY, nullptr, nullptr, sx, sbase, nullptr);
+    stage_l0<false>(m, in, ti, eb, ne, st);
     __syncthreads();
-    for (int t = 0; t < ne; ++t) {
-      const int base = sbase[t];
-      if (base < 0) continue;
-      const float4* c = m.spl0 + static_cast<size_t>(base) * C + k;
-      const float x = sx[t];
+    // active edges; the next edge's four cubics load while this one accumulates
+    const int na = st.nact;
+    float4 c[4];
+    if (na > 0) {
+      const float4* cp = m.spl0 + static_cast<size_t>(st.row[st.act[0]]) * 4 * C + k;
 #pragma unroll
-      for (int l = 0; l < 4; ++l) {
-        const float R = spline_val(__ldg(c + l * C), x);
+      for (int l = 0; l < 4; ++l) c[l] = __ldg(cp + l * C);
+    }
+    for (int a = 0; a < na; ++a) {
+      const int t = st.act[a];
+      const float x = st.x[t];
+      float R[4];
 #pragma unroll
-        for (int q = l * l; q < (l + 1) * (l + 1); ++q) acc[q] = fmaf(R, sY[q][t], acc[q]);
+      for (int l = 0; l < 4; ++l) R[l] = spline_val(c[l], x);
+      if (a + 1 < na) {
+        const float4* cp = m.spl0 + static_cast<size_t>(st.row[st.act[a + 1]]) * 4 * C + k;
+#pragma unroll
+        for (int l = 0; l < 4; ++l) c[l] = __ldg(cp + l * C);
+      }
+#pragma unroll
+      for (int q4 = 0; q4 < 4; ++q4) {
+        const float4 y = st.Y[t][q4];
+        const float yy[4] = {y.x, y.y, y.z, y.w};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int q = 4 * q4 + j;
+          const int l = q < 1 ? 0 : (q < 4 ? 1 : (q < 9 ? 2 : 3));
+          acc[q] = fmaf(R[l], yy[j], acc[q]);
+        }
       }
     }
   }
@@ -232,18 +259,17 @@ __global__ void __launch_bounds__(256) k_contract0_rev(DevModel m, const int* __
   for (int q = 0; q < 16; ++q) A0_adj[(static_cast<size_t>(i) * 16 + q) * C + k] = dA[q];
 }
 
+
+
 // ---------------------------------------------------------------------------
-// Layer 0 edge adjoint, from dA0 (k_contract0_rev):
-//   dE/dx_ij = sum_k sum_lm dA0[lm] (R0'_l'(r) u Y_lm + R0'_l(r) dY_lm/dx)
-// and node_forces[e] = -(layer-0 + layer-1 contributions), in float64.
+// Layer-0 edge adjoint (mace.cpp:203-271): dE/dx_ij from A0_adj through the folded
+// radial splines and Y_lm; ZBL and the density factor add their terms; forces =
+// -(layer 0 + layer 1).  The next active edge's four spline cubics are loaded while
+// this edge computes.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_layer0_rev(DevModel m, EdgeIn in, const float* __restrict__ A0_adj,
                                                     const double* __restrict__ f1, double* __restrict__ forces) {
-  __shared__ float sY[16][kEdgeChunk];
-  __shared__ float sG[48][kEdgeChunk];
-  __shared__ float su[3][kEdgeChunk];
-  __shared__ float sx[kEdgeChunk];
-  __shared__ int sbase[kEdgeChunk];
+  __shared__ L0Stage<true> st;
   __shared__ float sF[kEdgeChunk][8][3];
   const int C = m.C, k = threadIdx.x, i = blockIdx.x;
   const int nwarp = C >> 5;
@@ -255,43 +281,63 @@ __global__ void __launch_bounds__(256) k_layer0_rev(DevModel m, EdgeIn in, const
   for (int eb = e0; eb < e1; eb += kEdgeChunk) {
     const int ne = min(kEdgeChunk, e1 - eb);
     __syncthreads();
-    stage_edges<true>(m, in, ti, eb, ne, true, 4, sY, sG, su, sx, sbase, nullptr);
+    stage_l0<true>(m, in, ti, eb, ne, st);
     __syncthreads();
-    for (int t = 0; t < ne; ++t) {
-      const int base = sbase[t];
-      if (base < 0) {
-        if ((threadIdx.x & 31) == 0) sF[t][threadIdx.x >> 5][0] = sF[t][threadIdx.x >> 5][1] = sF[t][threadIdx.x >> 5][2] = 0.0f;
-        continue;
+    const int na = st.nact;
+    float4 c[4];
+    if (na > 0) {
+      const float4* cp = m.spl0 + static_cast<size_t>(st.row[st.act[0]]) * 4 * C + k;
+#pragma unroll
+      for (int l = 0; l < 4; ++l) c[l] = __ldg(cp + l * C);
+    }
+    for (int a = 0; a < na; ++a) {
+      const int t = st.act[a];
+      const float x = st.x[t];
+      float R[4], Rd[4];
+#pragma unroll
+      for (int l = 0; l < 4; ++l) {
+        R[l] = spline_val(c[l], x);
+        Rd[l] = spline_der(c[l], x);
       }
-      const float4* c = m.spl0 + static_cast<size_t>(base) * C + k;
-      const float x = sx[t];
+      if (a + 1 < na) {
+        const float4* cp = m.spl0 + static_cast<size_t>(st.row[st.act[a + 1]]) * 4 * C + k;
+#pragma unroll
+        for (int l = 0; l < 4; ++l) c[l] = __ldg(cp + l * C);
+      }
+      float Y[16];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const float4 v = st.Y[t][q];
+        Y[4 * q] = v.x; Y[4 * q + 1] = v.y; Y[4 * q + 2] = v.z; Y[4 * q + 3] = v.w;
+      }
       float dr = 0.0f, fx = 0.0f, fy = 0.0f, fz = 0.0f;
 #pragma unroll
       for (int l = 0; l < 4; ++l) {
-        const float4 cc = __ldg(c + l * C);
-        const float R = spline_val(cc, x), Rd = spline_der(cc, x);
         float dRl = 0.0f;
 #pragma unroll
         for (int q = l * l; q < (l + 1) * (l + 1); ++q) {
-          dRl = fmaf(dA[q], sY[q][t], dRl);
-          const float w = dA[q] * R;
-          fx = fmaf(w, sG[q][t], fx);
-          fy = fmaf(w, sG[16 + q][t], fy);
-          fz = fmaf(w, sG[32 + q][t], fz);
+          dRl = fmaf(dA[q], Y[q], dRl);
+          const float w = dA[q] * R[l];
+          const float4 g = st.G[t][q];
+          fx = fmaf(w, g.x, fx);
+          fy = fmaf(w, g.y, fy);
+          fz = fmaf(w, g.z, fz);
         }
-        dr = fmaf(dRl, Rd, dr);
+        dr = fmaf(dRl, Rd[l], dr);
       }
-      fx = fmaf(dr, su[0][t], fx);
-      fy = fmaf(dr, su[1][t], fy);
-      fz = fmaf(dr, su[2][t], fz);
+      const float4 u = st.u[t];
+      fx = fmaf(dr, u.x, fx);
+      fy = fmaf(dr, u.y, fy);
+      fz = fmaf(dr, u.z, fz);
       block_reduce3(fx, fy, fz, sF, t);
     }
     __syncthreads();
     for (int t = threadIdx.x; t < ne; t += blockDim.x) {
       const long e = static_cast<long>(eb) + t;
       double s[3] = {0.0, 0.0, 0.0};
-      for (int w = 0; w < nwarp; ++w)
-        for (int a = 0; a < 3; ++a) s[a] += static_cast<double>(sF[t][w][a]);
+      if (st.row[t] >= 0)
+        for (int w = 0; w < nwarp; ++w)
+          for (int a = 0; a < 3; ++a) s[a] += static_cast<double>(sF[t][w][a]);
       if (m.has_zbl) {  // node_forces -= xyz / r * dV_ZBL/dr (zbl.cpp:118-121)
         float V, dV;
         const double r = in.r[e];

@@ -76,12 +76,15 @@ __global__ void k_neigh_cells(const double* __restrict__ pos, const int* __restr
                               int* __restrict__ num_neigh, const int* __restrict__ first, int* __restrict__ nidx,
                               int* __restrict__ ntype_e, int* __restrict__ edge_i, char4* __restrict__ shift,
                               long cap) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  // one warp per atom: the lanes test 32 candidates of a cell at a time and a ballot
+  // keeps the hits in candidate order, so the list order is the sequential one
+  const int i = static_cast<int>((static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
   if (i >= N) return;
+  const unsigned below = (1u << lane) - 1u;
   const double xi = pos[3 * i], yi = pos[3 * i + 1], zi = pos[3 * i + 2];
   const int ci = cell[i];
   const int cz = ci % nc.z, cy = (ci / nc.z) % nc.y, cx = ci / (nc.z * nc.y);
-  int count = 0;
   long slot = FILL ? first[i] : 0;
   for (int dx = -1; dx <= 1; ++dx) {
     int qx = cx + dx, sx = 0;
@@ -97,28 +100,34 @@ __global__ void k_neigh_cells(const double* __restrict__ pos, const int* __restr
         if (qz >= nc.z) { if (!periodic.z) continue; qz -= nc.z; sz = 1; }
         const int q = (qx * nc.y + qy) * nc.z + qz;
         const double ox = sx * box.x, oy = sy * box.y, oz = sz * box.z;
-        for (int w = cell_start[q]; w < cell_start[q + 1]; ++w) {
-          const int j = cell_atoms[w];
-          if (j == i && sx == 0 && sy == 0 && sz == 0) continue;
-          const double ddx = pos[3 * j] + ox - xi, ddy = pos[3 * j + 1] + oy - yi, ddz = pos[3 * j + 2] + oz - zi;
-          if (ddx * ddx + ddy * ddy + ddz * ddz < rl2) {
-            if (FILL) {
-              if (slot < cap) {
-                nidx[slot] = j;
-                ntype_e[slot] = species[j];
-                edge_i[slot] = i;
-                shift[slot] = make_char4(sx, sy, sz, 0);
-              }
-              ++slot;
-            } else {
-              ++count;
+        const int w1 = cell_start[q + 1];
+        for (int w0 = cell_start[q]; w0 < w1; w0 += 32) {
+          const int w = w0 + lane;
+          int j = -1;
+          bool hit = false;
+          if (w < w1) {
+            j = cell_atoms[w];
+            if (!(j == i && sx == 0 && sy == 0 && sz == 0)) {
+              const double ddx = pos[3 * j] + ox - xi, ddy = pos[3 * j + 1] + oy - yi, ddz = pos[3 * j + 2] + oz - zi;
+              hit = ddx * ddx + ddy * ddy + ddz * ddz < rl2;
             }
           }
+          const unsigned ball = __ballot_sync(0xffffffffu, hit);
+          if (FILL && hit) {
+            const long sl = slot + __popc(ball & below);
+            if (sl < cap) {
+              nidx[sl] = j;
+              ntype_e[sl] = species[j];
+              edge_i[sl] = i;
+              shift[sl] = make_char4(sx, sy, sz, 0);
+            }
+          }
+          slot += __popc(ball);
         }
       }
     }
   }
-  if (!FILL) num_neigh[i] = count;
+  if (!FILL && lane == 0) num_neigh[i] = static_cast<int>(slot);
 }
 
 // Small or non-periodic systems: all pairs over the periodic images in range.
@@ -128,35 +137,41 @@ __global__ void k_neigh_brute(const double* __restrict__ pos, const int* __restr
                               int* __restrict__ num_neigh, const int* __restrict__ first, int* __restrict__ nidx,
                               int* __restrict__ ntype_e, int* __restrict__ edge_i, char4* __restrict__ shift,
                               long cap) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  // one warp per atom, 32 candidates per ballot (order: candidate chunk, image, lane)
+  const int i = static_cast<int>((static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
   if (i >= N) return;
+  const unsigned below = (1u << lane) - 1u;
   const double xi = pos[3 * i], yi = pos[3 * i + 1], zi = pos[3 * i + 2];
-  int count = 0;
   long slot = FILL ? first[i] : 0;
   // with segments (a batch of molecules), only atoms of i's own segment are candidates
   const int j0 = seg_of ? seg_first[seg_of[i]] : 0, j1 = seg_of ? seg_first[seg_of[i] + 1] : N;
-  for (int j = j0; j < j1; ++j)
+  for (int jb = j0; jb < j1; jb += 32) {
+    const int j = jb + lane;
+    const bool live = j < j1;
     for (int sx = -nimg.x; sx <= nimg.x; ++sx)
       for (int sy = -nimg.y; sy <= nimg.y; ++sy)
         for (int sz = -nimg.z; sz <= nimg.z; ++sz) {
-          if (j == i && sx == 0 && sy == 0 && sz == 0) continue;
-          const double ddx = pos[3 * j] + sx * box.x - xi, ddy = pos[3 * j + 1] + sy * box.y - yi,
-                       ddz = pos[3 * j + 2] + sz * box.z - zi;
-          if (ddx * ddx + ddy * ddy + ddz * ddz < rl2) {
-            if (FILL) {
-              if (slot < cap) {
-                nidx[slot] = j;
-                ntype_e[slot] = species[j];
-                edge_i[slot] = i;
-                shift[slot] = make_char4(sx, sy, sz, 0);
-              }
-              ++slot;
-            } else {
-              ++count;
+          bool hit = false;
+          if (live && !(j == i && sx == 0 && sy == 0 && sz == 0)) {
+            const double ddx = pos[3 * j] + sx * box.x - xi, ddy = pos[3 * j + 1] + sy * box.y - yi,
+                         ddz = pos[3 * j + 2] + sz * box.z - zi;
+            hit = ddx * ddx + ddy * ddy + ddz * ddz < rl2;
+          }
+          const unsigned ball = __ballot_sync(0xffffffffu, hit);
+          if (FILL && hit) {
+            const long sl = slot + __popc(ball & below);
+            if (sl < cap) {
+              nidx[sl] = j;
+              ntype_e[sl] = species[j];
+              edge_i[sl] = i;
+              shift[sl] = make_char4(sx, sy, sz, 0);
             }
           }
+          slot += __popc(ball);
         }
-  if (!FILL) num_neigh[i] = count;
+  }
+  if (!FILL && lane == 0) num_neigh[i] = static_cast<int>(slot);
 }
 
 // Wrap positions into the periodic box (done before each neighbour build; positions
@@ -211,14 +226,19 @@ __global__ void k_edge_geometry(long cap, int N, const int* __restrict__ first, 
 // F_a = sum_{e in out(a)} (f[rev e] - f[e]); one thread per atom, no atomics
 __global__ void k_atom_forces(int N, const int* __restrict__ first, const int* __restrict__ rev,
                               const double* __restrict__ f, double* __restrict__ F) {
-  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  // one warp per atom; fixed lane assignment and reduction tree: deterministic
+  const int a = static_cast<int>((static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
   if (a >= N) return;
   double s[3] = {0.0, 0.0, 0.0};
-  for (int e = first[a]; e < first[a + 1]; ++e) {
+  for (int e = first[a] + lane; e < first[a + 1]; e += 32) {
     const int q = rev[e];
     for (int c = 0; c < 3; ++c) s[c] += (q >= 0 ? f[3 * static_cast<long>(q) + c] : 0.0) - f[3 * static_cast<long>(e) + c];
   }
-  for (int c = 0; c < 3; ++c) F[3 * a + c] = s[c];
+  for (int o = 16; o > 0; o >>= 1)
+    for (int c = 0; c < 3; ++c) s[c] += __shfl_xor_sync(0xffffffffu, s[c], o);
+  if (lane == 0)
+    for (int c = 0; c < 3; ++c) F[3 * a + c] = s[c];
 }
 
 // Deterministic float64 reduction of the energy (slot 0) and the 9 virial
@@ -293,7 +313,7 @@ void launch_neigh_pass(bool fill, bool brute, const double* pos, const int* spec
                        const int* first, int* nidx, int* ntype_e, int* edge_i, char4* shift, long cap,
                        cudaStream_t s) {
   const double rl2 = rl * rl;
-  const int g = ceil_div(N, 128);
+  const int g = ceil_div(N, 4);  // 128-thread blocks, one warp per atom
   if (brute || seg_of) {
     if (fill)
       k_neigh_brute<true><<<g, 128, 0, s>>>(pos, species, N, box, nimg, rl2, seg_of, seg_first, num_neigh, first,
@@ -326,7 +346,7 @@ void launch_edge_geometry(long cap, int N, const int* first, const double* pos, 
 }
 
 void launch_atom_forces(int N, const int* first, const int* rev, const double* f, double* F, cudaStream_t s) {
-  if (N > 0) k_atom_forces<<<ceil_div(N, 128), 128, 0, s>>>(N, first, rev, f, F);
+  if (N > 0) k_atom_forces<<<ceil_div(N, 4), 128, 0, s>>>(N, first, rev, f, F);  // one warp per atom
 }
 
 void launch_reduce(int N, const int* first, const double* energies, const double* xyz, const double* f,

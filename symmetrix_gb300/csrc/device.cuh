@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <type_traits>
@@ -55,7 +56,29 @@ struct DevModel {
   // s_i = 1 + sum_j s(r_ij) and c_i = (dE/dA_scaled . A_scaled) / s_i
   float* dens_s[2];
   float* dens_c[2];
+  // BF16 form: the producers also write the tensor-core GEMM X operands as `tc_terms`
+  // bf16 split terms per row (see write_split); nullptr in the FP32 form.
+  //   op_m0    [N*nLM][T*C]                rows (node, LM)              (H1 GEMM)
+  //   op_phi1  per l: [N(2l+1)][T*n_e*C]   at T*N*lme_off[l]*C          (A1 GEMM)
+  //   op_a1adj per l: [N(2l+1)][T*C]       at T*N*l*l*C                 (Phi1_adj GEMM)
+  __nv_bfloat16* op_m0;
+  __nv_bfloat16* op_phi1;
+  __nv_bfloat16* op_a1adj;
+  int tc_terms;
 };
+
+// Element `col` of a GEMM operand row of width K as bf16 split terms: (hi), (hi | hi)
+// or (hi | lo | hi) for 1, 2, 3 terms, hi = bf16(v), lo = bf16(v - hi); the B operand
+// rows carry (W_hi), (W_hi | W_lo), (W_hi | W_hi | W_lo).
+__device__ __forceinline__ void write_split(__nv_bfloat16* row, int K, int T, int col, float v) {
+  const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+  row[col] = hi;
+  if (T == 2) row[K + col] = hi;
+  if (T == 3) {
+    row[K + col] = __float2bfloat16_rn(v - __bfloat162float(hi));
+    row[2 * K + col] = hi;
+  }
+}
 
 // ZBL energy of one directed edge and its r-derivative, as zbl.cpp:22-94
 // (energy 0.5 * v(r) * envelope(r); each pair appears as two directed edges).

@@ -131,6 +131,7 @@ int smx_set_option(smx_engine* eng, const char* key, long value) {
       cudaSetDevice(eng->device);
       cudaStreamSynchronize(eng->stream);
       eng->tc_terms = static_cast<int>(value);
+      eng->dm.tc_terms = eng->tc_terms;
       eng->setup_tc_weights();
       eng->free_workspace();  // operand buffers are sized by the term count
     } catch (const std::exception& e) {

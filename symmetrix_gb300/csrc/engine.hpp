@@ -177,6 +177,8 @@ struct smx_engine {
     m.ro2_w2 = upload(pm.ro2_w2);
     m.e0 = upload(pm.e0);
     m.has_zbl = pm.has_zbl;
+    m.op_m0 = m.op_phi1 = m.op_a1adj = nullptr;
+    m.tc_terms = tc_terms;
     m.zbl_p = pm.zbl_p;
     for (int q = 0; q < 4; ++q) m.zbl_c[q] = pm.zbl_c[q];
     m.zbl_pair = pm.has_zbl ? reinterpret_cast<const float4*>(upload(pm.zbl_pair)) : nullptr;
@@ -217,6 +219,7 @@ struct smx_engine {
       if (p) cudaFree(p);
     A0 = M0 = H1 = Phi1 = A1 = M1 = H2 = A0_adj = M0_adj = H1_adj = Phi1_adj = A1_adj = M1_adj = H2_adj = nullptr;
     M0_bf = Phi1_bf = A1adj_bf = H1adj_bf = nullptr;
+    dm.op_m0 = dm.op_phi1 = dm.op_a1adj = nullptr;
     for (int layer = 0; layer < 2; ++layer) {
       if (dm.dens_s[layer]) cudaFree(dm.dens_s[layer]);
       if (dm.dens_c[layer]) cudaFree(dm.dens_c[layer]);
@@ -265,6 +268,9 @@ struct smx_engine {
       Phi1_bf = dalloc<__nv_bfloat16>(T * nN * dm.n_lme * C);
       A1adj_bf = dalloc<__nv_bfloat16>(T * nN * 16 * C);
       H1adj_bf = dalloc<__nv_bfloat16>(T * nN * dm.nLM * C);
+      dm.op_m0 = tc_H1 ? M0_bf : nullptr;
+      dm.op_phi1 = Phi1_bf;
+      dm.op_a1adj = A1adj_bf;
     }
     for (int layer = 0; layer < 2; ++layer)
       if (dm.dens_spl[layer]) {
@@ -323,9 +329,11 @@ struct smx_engine {
     smx::launch_layer0_fwd(dm, in, A0, M0, dm.has_zbl ? zbl_e : nullptr, s);
     mark(1, s);
     if (tc_H1) {  // H1 = M0 @ H1W[L]  (mace.cpp:397-423), tensor cores
-      smx::launch_rows_to_bf16(M0, M0_bf, static_cast<long>(N) * dm.nLM, C, 1, C, 0, 0, T, s);
-      smx::UmmaOut o{H1, static_cast<long>(N) * dm.nLM, dm.nLM, static_cast<long>(dm.nLM) * C, 0, C, 1};
-      smx::launch_umma_gemm(M0_bf, static_cast<long>(N) * dm.nLM, T * C, W_H1, 2 * C, C, o, status_dev, s);
+      // (layer0_fwd wrote M0 as split bf16 rows into M0_bf)
+      const smx::UmmaGemm g{M0_bf, static_cast<long>(N) * dm.nLM, T * C, W_H1, 2 * C, C,
+                            smx::UmmaOut{H1, static_cast<long>(N) * dm.nLM, dm.nLM, static_cast<long>(dm.nLM) * C, 0,
+                                         C, 1}};
+      smx::launch_umma_gemms(&g, 1, status_dev, s);
     } else {  // H1 = M0 @ H1W[L]  (mace.cpp:397-423)
       smx::GemmBatch b{};
       for (int L = 0; L <= dm.L_max; ++L)
@@ -337,16 +345,17 @@ struct smx_engine {
     smx::launch_layer1_fwd(dm, in, H1, Phi1, s);
     mark(3, s);
     {  // A1 = Phi1 @ A1W[l]  (mace.cpp:607-642)
+      // tensor cores on the per-l regrouped split bf16 rows layer1_fwd wrote, one launch
+      smx::UmmaGemm g[4];
+      int ng = 0;
       for (int l = 0; l < 4; ++l)
-        if (dm.num_e[l] > 0 && tc_A1[l]) {  // tensor cores on the per-l regrouped bf16 rows
+        if (dm.num_e[l] > 0 && tc_A1[l]) {
           const long rows = static_cast<long>(N) * (2 * l + 1);
           const int K = dm.num_e[l] * C;
-          __nv_bfloat16* X = Phi1_bf + static_cast<size_t>(T) * N * dm.lme_off[l] * C;
-          smx::launch_rows_to_bf16(Phi1, X, rows, K, 2 * l + 1, static_cast<long>(dm.n_lme) * C, dm.lme_off[l] * C, K,
-                                   T, s);
-          smx::UmmaOut o{A1, rows, 2 * l + 1, 16L * C, l * l * C, C, 0};
-          smx::launch_umma_gemm(X, rows, T * K, W_A1[l], C, C, o, status_dev, s);
+          g[ng++] = smx::UmmaGemm{Phi1_bf + static_cast<size_t>(T) * N * dm.lme_off[l] * C, rows, T * K, W_A1[l], C,
+                                  C, smx::UmmaOut{A1, rows, 2 * l + 1, 16L * C, l * l * C, C, 0}};
         }
+      if (ng) smx::launch_umma_gemms(g, ng, status_dev, s);
       smx::GemmBatch b{};
       for (int l = 0; l < 4; ++l)
         if (dm.num_e[l] > 0 && !tc_A1[l])
@@ -360,15 +369,18 @@ struct smx_engine {
                           dm.has_zbl ? zbl_e : nullptr, out_e, s);
     mark(5, s);
     {  // Phi1_adj = A1_adj @ A1W[l]^T  (mace.cpp:644-679)
+      // tensor cores on the split rows node_tail wrote, one N-tile per eta, one launch
+      smx::UmmaGemm g[4];
+      int ng = 0;
       for (int l = 0; l < 4; ++l)
-        if (dm.num_e[l] > 0 && tc_Phi1adj[l]) {  // tensor cores, one N-tile per eta
+        if (dm.num_e[l] > 0 && tc_Phi1adj[l]) {
           const long rows = static_cast<long>(N) * (2 * l + 1);
-          __nv_bfloat16* X = A1adj_bf + static_cast<size_t>(T) * N * l * l * C;
-          smx::launch_rows_to_bf16(A1_adj, X, rows, C, 2 * l + 1, 16L * C, l * l * C, C, T, s);
-          smx::UmmaOut o{Phi1_adj, rows, 2 * l + 1, static_cast<long>(dm.n_lme) * C, dm.lme_off[l] * C,
-                         dm.num_e[l] * C, 0};
-          smx::launch_umma_gemm(X, rows, T * C, W_Phi1adj[l], dm.num_e[l] * C, C, o, status_dev, s);
+          g[ng++] = smx::UmmaGemm{A1adj_bf + static_cast<size_t>(T) * N * l * l * C, rows, T * C, W_Phi1adj[l],
+                                  dm.num_e[l] * C, C,
+                                  smx::UmmaOut{Phi1_adj, rows, 2 * l + 1, static_cast<long>(dm.n_lme) * C,
+                                               dm.lme_off[l] * C, dm.num_e[l] * C, 0}};
         }
+      if (ng) smx::launch_umma_gemms(g, ng, status_dev, s);
       smx::GemmBatch b{};
       for (int l = 0; l < 4; ++l)
         if (dm.num_e[l] > 0 && !tc_Phi1adj[l])
@@ -381,8 +393,10 @@ struct smx_engine {
     mark(7, s);
     if (tc_H1) {  // M0_adj = H1_adj @ H1W[L]^T  (mace.cpp:425-451), tensor cores
       smx::launch_rows_to_bf16(H1_adj, H1adj_bf, static_cast<long>(N) * dm.nLM, C, 1, C, 0, 0, T, s);
-      smx::UmmaOut o{M0_adj, static_cast<long>(N) * dm.nLM, dm.nLM, static_cast<long>(dm.nLM) * C, 0, C, 1};
-      smx::launch_umma_gemm(H1adj_bf, static_cast<long>(N) * dm.nLM, T * C, W_M0adj, 2 * C, C, o, status_dev, s);
+      const smx::UmmaGemm g{H1adj_bf, static_cast<long>(N) * dm.nLM, T * C, W_M0adj, 2 * C, C,
+                            smx::UmmaOut{M0_adj, static_cast<long>(N) * dm.nLM, dm.nLM,
+                                         static_cast<long>(dm.nLM) * C, 0, C, 1}};
+      smx::launch_umma_gemms(&g, 1, status_dev, s);
     } else {  // M0_adj = H1_adj @ H1W[L]^T  (mace.cpp:425-451)
       smx::GemmBatch b{};
       for (int L = 0; L <= dm.L_max; ++L)

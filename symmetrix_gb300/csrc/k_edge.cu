@@ -168,10 +168,14 @@ __global__ void __launch_bounds__(256) k_layer0_fwd(DevModel m, EdgeIn in, float
     const float* cf = m.coef0 + static_cast<size_t>(ti * m.nLM) * m.T0 * C + k;
     const size_t st = static_cast<size_t>(m.T0) * C;
     float* out = M0 + static_cast<size_t>(i) * m.nLM * C + k;
-    out[0] = poly::value_LM0(acc, cf, C);
-    out[C] = poly::value_LM1(acc, cf + st, C);
-    out[2 * C] = poly::value_LM2(acc, cf + 2 * st, C);
-    out[3 * C] = poly::value_LM3(acc, cf + 3 * st, C);
+    const float v[4] = {poly::value_LM0(acc, cf, C), poly::value_LM1(acc, cf + st, C),
+                        poly::value_LM2(acc, cf + 2 * st, C), poly::value_LM3(acc, cf + 3 * st, C)};
+#pragma unroll
+    for (int LM = 0; LM < 4; ++LM) {
+      out[LM * C] = v[LM];
+      if (m.op_m0)  // BF16 form: the H1 GEMM's split operand
+        write_split(m.op_m0 + (static_cast<size_t>(i) * m.nLM + LM) * m.tc_terms * C, C, m.tc_terms, k, v[LM]);
+    }
     return;
   }
   float* sA = dyn;  // [17][C]: this thread's A0 column (+ constant one) for the contraction
@@ -188,6 +192,8 @@ __global__ void __launch_bounds__(256) k_layer0_fwd(DevModel m, EdgeIn in, float
       f = fmaf(__ldg(cf + static_cast<size_t>(t - t0) * C), xa * xb * xc, f);
     }
     M0[(static_cast<size_t>(i) * m.nLM + LM) * C + k] = f;
+    if (m.op_m0)
+      write_split(m.op_m0 + (static_cast<size_t>(i) * m.nLM + LM) * m.tc_terms * C, C, m.tc_terms, k, f);
   }
 }
 

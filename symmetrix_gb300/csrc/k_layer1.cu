@@ -367,12 +367,25 @@ __global__ void __launch_bounds__(256) k_layer1_fwd(DevModel m, EdgeIn in, const
   float* sP = dyn;  // [NP][C]: this thread's Phi1r column
 #pragma unroll
   for (int p = 0; p < NP; ++p) sP[p * C + k] = acc[p];
-  for (int lme = 0; lme < m.n_lme; ++lme) {
-    float s = 0.0f;
-    const int p1 = __ldg(m.cg_fwd_off + lme + 1);
-    for (int p = __ldg(m.cg_fwd_off + lme); p < p1; ++p)
-      s = fmaf(__ldg(m.cg_fwd_v + p), sP[__ldg(m.cg_fwd_p + p) * C + k], s);
-    Phi1[(static_cast<size_t>(i) * m.n_lme + lme) * C + k] = s;
+  // Phi1 rows are [l][m][e] (lme = lme_off[l] + m n_e + e); the BF16 form also writes
+  // them as the A1 GEMM's split operand, regrouped per l
+  const int T = m.tc_terms;
+  for (int l = 0; l < 4; ++l) {
+    const int ne = m.num_e[l], Kl = ne * C;
+    for (int mm = 0; mm < 2 * l + 1; ++mm)
+      for (int e = 0; e < ne; ++e) {
+        const int lme = m.lme_off[l] + mm * ne + e;
+        float s = 0.0f;
+        const int p1 = __ldg(m.cg_fwd_off + lme + 1);
+        for (int p = __ldg(m.cg_fwd_off + lme); p < p1; ++p)
+          s = fmaf(__ldg(m.cg_fwd_v + p), sP[__ldg(m.cg_fwd_p + p) * C + k], s);
+        Phi1[(static_cast<size_t>(i) * m.n_lme + lme) * C + k] = s;
+        if (m.op_phi1) {
+          __nv_bfloat16* row = m.op_phi1 + static_cast<size_t>(T) * in.N * m.lme_off[l] * C +
+                               (static_cast<size_t>(i) * (2 * l + 1) + mm) * T * Kl;
+          write_split(row, Kl, T, e * C + k, s);
+        }
+      }
   }
 }
 

@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(256) k_node_tail(DevModel m, const int* __rest
                                                    float* __restrict__ H2o, float* __restrict__ A1_adj,
                                                    float* __restrict__ H1_adj, float* __restrict__ M1_adj_o,
                                                    float* __restrict__ H2_adj_o, const float* __restrict__ zbl_e,
-                                                   double* __restrict__ energies) {
+                                                   double* __restrict__ energies, int N) {
   extern __shared__ float dyn[];
   const int C = m.C, k = threadIdx.x, i = blockIdx.x;
   const int nwarp = C >> 5, lane = k & 31, warp = k >> 5;
@@ -210,6 +210,17 @@ __global__ void __launch_bounds__(256) k_node_tail(DevModel m, const int* __rest
   }
 #pragma unroll
   for (int q = 0; q < 16; ++q) A1_adj[(static_cast<size_t>(i) * 16 + q) * C + k] = sG[q * C + k] * m1a / S1;
+  if (m.op_a1adj) {  // BF16 form: the Phi1_adj GEMM's split operand, rows (node, m) per l
+    const int T = m.tc_terms;
+    for (int l = 0; l < 4; ++l) {
+      if (m.num_e[l] == 0) continue;
+      for (int mm = 0; mm < 2 * l + 1; ++mm) {
+        __nv_bfloat16* row = m.op_a1adj + static_cast<size_t>(T) * N * l * l * C +
+                             (static_cast<size_t>(i) * (2 * l + 1) + mm) * T * C;
+        write_split(row, C, T, k, sG[(l * l + mm) * C + k] * m1a / S1);
+      }
+    }
+  }
   H1_adj[static_cast<size_t>(i) * m.nLM * C + k] = ha;
   for (int LM = 1; LM < m.nLM; ++LM) H1_adj[(static_cast<size_t>(i) * m.nLM + LM) * C + k] = 0.0f;
   M1o[static_cast<size_t>(i) * C + k] = f;
@@ -223,7 +234,7 @@ void launch_node_tail(const DevModel& m, const int* node_type, int N, float* A1,
                       double* energies, cudaStream_t s) {
   if (N <= 0) return;
   const size_t smem = sizeof(float) * (34 * m.C + 4 * m.C + 33 * 8 + 33);
-  k_node_tail<<<N, m.C, smem, s>>>(m, node_type, A1, H1, M1, H2, A1_adj, H1_adj, M1_adj, H2_adj, zbl_e, energies);
+  k_node_tail<<<N, m.C, smem, s>>>(m, node_type, A1, H1, M1, H2, A1_adj, H1_adj, M1_adj, H2_adj, zbl_e, energies, N);
 }
 
 // first[0] = 0, first[i+1] = first[i] + num_neigh[i]; one block, sequential tiles.

@@ -40,9 +40,24 @@ __device__ __forceinline__ void record_timeout(unsigned* status) {
 
 constexpr int kStages = 4;     // shared-memory ring depth (k-blocks in flight)
 
-__global__ void __launch_bounds__(128, 1) k_umma_gemm(const __grid_constant__ CUtensorMap ta,
-                                                      const __grid_constant__ CUtensorMap tb, UmmaOut o, int K,
-                                                      int NT, unsigned* status) {
+// Up to four independent GEMMs in one launch (blockIdx.z selects the segment; the
+// blocks beyond a segment's tile counts return at once).
+struct UmmaSegDev {
+  CUtensorMap ta, tb;
+  UmmaOut o;
+  int K, NT, tiles_m, tiles_n;
+};
+struct UmmaGroupDev {
+  UmmaSegDev s[4];
+};
+
+__global__ void __launch_bounds__(128, 1) k_umma_gemm(const __grid_constant__ UmmaGroupDev grp, unsigned* status) {
+  const UmmaSegDev& seg = grp.s[blockIdx.z];
+  if (static_cast<int>(blockIdx.x) >= seg.tiles_m || static_cast<int>(blockIdx.y) >= seg.tiles_n) return;
+  const CUtensorMap& ta = seg.ta;
+  const CUtensorMap& tb = seg.tb;
+  const UmmaOut& o = seg.o;
+  const int K = seg.K, NT = seg.NT;
   extern __shared__ uint8_t smem_raw[];
   __shared__ uint64_t full[kStages], empty[kStages], bar_mma;
   __shared__ uint32_t tmem_base;
@@ -239,14 +254,32 @@ cudaError_t init_umma_kernels() {
                               static_cast<int>(kMaxDynSmem));
 }
 
-void launch_umma_gemm(const __nv_bfloat16* X, long rows, int K, const __nv_bfloat16* B, int nb_rows, int NT,
-                      const UmmaOut& o, unsigned* status, cudaStream_t s) {
-  if (rows <= 0) return;
-  if (!umma_supported(K, NT) || nb_rows % NT != 0) throw std::invalid_argument("unsupported tensor-core GEMM shape");
-  const CUtensorMap ta = make_map(X, rows, K, kTileM);
-  const CUtensorMap tb = make_map(B, nb_rows, K, NT);
-  const dim3 grid(static_cast<unsigned>((rows + kTileM - 1) / kTileM), static_cast<unsigned>(nb_rows / NT));
-  k_umma_gemm<<<grid, 128, umma_smem_bytes(K, NT), s>>>(ta, tb, o, K, NT, status);
+void launch_umma_gemms(const UmmaGemm* g, int n, unsigned* status, cudaStream_t s) {
+  if (n < 1 || n > 4) throw std::invalid_argument("1 to 4 tensor-core GEMMs per launch");
+  UmmaGroupDev grp;
+  std::memset(&grp, 0, sizeof(grp));
+  unsigned gx = 0, gy = 0;
+  size_t smem = 0;
+  int used = 0;
+  for (int q = 0; q < n; ++q) {
+    const UmmaGemm& a = g[q];
+    if (!umma_supported(a.K, a.NT) || a.nb_rows % a.NT != 0)
+      throw std::invalid_argument("unsupported tensor-core GEMM shape");
+    if (a.rows <= 0) continue;
+    UmmaSegDev& d = grp.s[used++];
+    d.ta = make_map(a.X, a.rows, a.K, kTileM);
+    d.tb = make_map(a.B, a.nb_rows, a.K, a.NT);
+    d.o = a.o;
+    d.K = a.K;
+    d.NT = a.NT;
+    d.tiles_m = static_cast<int>((a.rows + kTileM - 1) / kTileM);
+    d.tiles_n = a.nb_rows / a.NT;
+    gx = std::max(gx, static_cast<unsigned>(d.tiles_m));
+    gy = std::max(gy, static_cast<unsigned>(d.tiles_n));
+    smem = std::max(smem, umma_smem_bytes(a.K, a.NT));
+  }
+  if (used == 0) return;
+  k_umma_gemm<<<dim3(gx, gy, used), 128, smem, s>>>(grp, status);
 }
 
 void launch_rows_to_bf16(const float* src, __nv_bfloat16* dst, long rows, int width, int rpn, long s_ns, int s_off,

@@ -63,8 +63,17 @@ struct UmmaOut {
 cudaError_t init_umma_kernels();
 size_t umma_smem_bytes(int K, int NT);
 bool umma_supported(int K, int NT);
-void launch_umma_gemm(const __nv_bfloat16* X, long rows, int K, const __nv_bfloat16* B, int nb_rows, int NT,
-                      const UmmaOut& o, unsigned* status, cudaStream_t s);
+// One GEMM: X [rows][K] bf16, B [nb_rows][K] bf16 (N-tiles of NT rows), output map o.
+struct UmmaGemm {
+  const __nv_bfloat16* X;
+  long rows;
+  int K;
+  const __nv_bfloat16* B;
+  int nb_rows, NT;
+  UmmaOut o;
+};
+// 1 to 4 GEMMs in one launch.
+void launch_umma_gemms(const UmmaGemm* g, int n, unsigned* status, cudaStream_t s);
 // Row r of dst (pitch terms*width): the bf16 split terms (hi), (hi | hi) or (hi | lo | hi) of
 // src[(r / rpn) * s_ns + s_off + (r % rpn) * s_rs + c], c < width (multiple of 4)
 void launch_rows_to_bf16(const float* src, __nv_bfloat16* dst, long rows, int width, int rpn, long s_ns, int s_off,

@@ -208,7 +208,8 @@ struct smx_engine {
       }
       setup_tc_weights();
     }
-    if (hm.L_max != 1) throw std::invalid_argument("model file: this build supports L_max = 1 (hidden irreps 0e + 1o)");
+    if (hm.L_max == 2 && hm.C > 128)
+      throw std::invalid_argument("model file: L_max = 2 models are supported up to 128 channels");
 
   }
 

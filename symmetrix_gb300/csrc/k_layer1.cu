@@ -456,6 +456,312 @@ __global__ void __launch_bounds__(256) k_layer1_rev(DevModel m, EdgeIn in, const
   }
 }
 
+// ===========================================================================
+// L_max = 2 (hidden irreps up to 2e: 17 instructions, 243 CG paths).  The paths do not
+// fit one thread's registers, so the instructions are split over four thread groups
+// per channel ({11,13,15,16}, {1,4,5,8,12}, {0,2,6,10}, {3,7,9,14}: exhaustive local
+// search for equal scalar work, 202/201/196/202 FMAs per edge, and 62/57/62/62 paths);
+// one channel per thread, scalar FMAs.  Block = 4 groups x C threads.
+// ===========================================================================
+namespace {
+
+constexpr int kL2Groups = 4;
+__host__ __device__ constexpr int l2_count(int g) { return g == 1 ? 5 : 4; }
+__host__ __device__ constexpr int l2_ins(int g, int i) {
+  constexpr int t0[4] = {11, 13, 15, 16}, t1[5] = {1, 4, 5, 8, 12}, t2[4] = {0, 2, 6, 10}, t3[4] = {3, 7, 9, 14};
+  return g == 0 ? t0[i] : (g == 1 ? t1[i] : (g == 2 ? t2[i] : t3[i]));
+}
+template <int G>
+__host__ __device__ constexpr int l2_goff(int i) {
+  int s = 0;
+  for (int w = 0; w < i; ++w) s += ins_paths(2, l2_ins(G, w));
+  return s;
+}
+template <int G>
+__host__ __device__ constexpr int l2_np() {
+  return l2_goff<G>(l2_count(G));
+}
+template <int G>
+__host__ __device__ constexpr bool l2_uses_y(int c) {
+  for (int w = 0; w < l2_count(G); ++w) {
+    const int l1 = ins_l1(2, l2_ins(G, w));
+    if (c >= l1 * l1 && c < (l1 + 1) * (l1 + 1)) return true;
+  }
+  return false;
+}
+constexpr int kL2MaxNp = 62;
+
+// block-wide sum of a 3-vector per edge for up to 32 warps
+__device__ __forceinline__ void block_reduce3_w32(float fx, float fy, float fz, float (*sF)[32][3], int t) {
+  const float x = warp_sum(fx), y = warp_sum(fy), z = warp_sum(fz);
+  if ((threadIdx.x & 31) == 0) {
+    const int w = threadIdx.x >> 5;
+    sF[t][w][0] = x;
+    sF[t][w][1] = y;
+    sF[t][w][2] = z;
+  }
+}
+
+// Forward, group G, one staged chunk: acc[local path] += R_q Y_{l1 m1} H1[j, l2 m2, k].
+template <int G>
+__device__ __forceinline__ void l2_fwd_chunk(const DevModel& m, const float* __restrict__ H1,
+                                             const L1Stage<false>& st, int C, int k, float* acc) {
+  constexpr int NL2 = 9, NI = 17;
+  const int na = st.nact;
+  for (int a = 0; a < na; ++a) {
+    const int t = st.act[a];
+    const float x = st.x[t];
+    float hv[NL2];
+    const float* hj = H1 + static_cast<size_t>(st.j[t]) * NL2 * C + k;
+#pragma unroll
+    for (int b = 0; b < NL2; ++b) hv[b] = __ldg(hj + b * C);
+    const float4* cp = m.spl1_fwd + static_cast<size_t>(st.row[t]) * NI * C + k;
+    static_for<l2_count(G)>([&](auto ic) {
+      constexpr int i = decltype(ic)::value;
+      constexpr int q = l2_ins(G, i);
+      constexpr int l1 = ins_l1(2, q), l2 = ins_l2(2, q), g0 = l2_goff<G>(i);
+      const float R = spline_val(__ldg(cp + q * C), x);
+#pragma unroll
+      for (int a1 = 0; a1 < 2 * l1 + 1; ++a1) {
+        const float ry = R * st.Y2[t][l1 * l1 + a1].x;
+#pragma unroll
+        for (int b = 0; b < 2 * l2 + 1; ++b)
+          acc[g0 + a1 * (2 * l2 + 1) + b] = fmaf(ry, hv[l2 * l2 + b], acc[g0 + a1 * (2 * l2 + 1) + b]);
+      }
+    });
+  }
+}
+
+template <int G>
+__device__ __forceinline__ void l2_store(float* sP, int C, int k, const float* acc) {
+  static_for<l2_count(G)>([&](auto ic) {
+    constexpr int i = decltype(ic)::value;
+    constexpr int q = l2_ins(G, i);
+    constexpr int np = ins_paths(2, q), p0 = ins_poff(2, q), g0 = l2_goff<G>(i);
+#pragma unroll
+    for (int p = 0; p < np; ++p) sP[(p0 + p) * C + k] = acc[g0 + p];
+  });
+}
+
+template <int G>
+__device__ __forceinline__ void l2_load_g(const float* sP, int C, int k, float* g) {
+  static_for<l2_count(G)>([&](auto ic) {
+    constexpr int i = decltype(ic)::value;
+    constexpr int q = l2_ins(G, i);
+    constexpr int np = ins_paths(2, q), p0 = ins_poff(2, q), g0 = l2_goff<G>(i);
+#pragma unroll
+    for (int p = 0; p < np; ++p) g[g0 + p] = sP[(p0 + p) * C + k];
+  });
+}
+
+}  // namespace
+
+// Layer-1 forward, L_max = 2.
+__global__ void __launch_bounds__(512, 1) k_layer1_fwd_l2(DevModel m, EdgeIn in, const float* __restrict__ H1,
+                                                          float* __restrict__ Phi1) {
+  extern __shared__ float dyn[];
+  __shared__ L1Stage<false> st;
+  const int C = m.C, CP = (C + 31) & ~31, i = blockIdx.x;
+  const int grp = threadIdx.x / CP, kk = threadIdx.x - grp * CP;
+  const bool live = kk < C;
+  const int k = live ? kk : 0;
+  const int ti = in.node_type[i];
+  const int e0 = in.first[i], e1 = in.first[i + 1];
+  float acc[kL2MaxNp];
+#pragma unroll
+  for (int p = 0; p < kL2MaxNp; ++p) acc[p] = 0.0f;
+  for (int eb = e0; eb < e1; eb += kEdgeChunk) {
+    const int ne = min(kEdgeChunk, e1 - eb);
+    __syncthreads();
+    stage_l1<false>(m, in, ti, eb, ne, st);
+    __syncthreads();
+    switch (grp) {
+      case 0: l2_fwd_chunk<0>(m, H1, st, C, k, acc); break;
+      case 1: l2_fwd_chunk<1>(m, H1, st, C, k, acc); break;
+      case 2: l2_fwd_chunk<2>(m, H1, st, C, k, acc); break;
+      default: l2_fwd_chunk<3>(m, H1, st, C, k, acc); break;
+    }
+  }
+  if (m.dens_spl[1]) {
+    const float S = dens_factor(m, 1, in, i, ti);
+    if (threadIdx.x == 0) m.dens_s[1][i] = S;
+  }
+  float* sP = dyn;  // [NP][C]
+  if (live) {
+    switch (grp) {
+      case 0: l2_store<0>(sP, C, k, acc); break;
+      case 1: l2_store<1>(sP, C, k, acc); break;
+      case 2: l2_store<2>(sP, C, k, acc); break;
+      default: l2_store<3>(sP, C, k, acc); break;
+    }
+  }
+  __syncthreads();
+  const int T = m.tc_terms;
+  for (int kc = threadIdx.x; kc < C; kc += blockDim.x)
+    for (int l = 0; l < 4; ++l) {
+      const int ne = m.num_e[l], Kl = ne * C;
+      for (int mm = 0; mm < 2 * l + 1; ++mm)
+        for (int e = 0; e < ne; ++e) {
+          const int lme = m.lme_off[l] + mm * ne + e;
+          float s = 0.0f;
+          const int p1 = __ldg(m.cg_fwd_off + lme + 1);
+          for (int p = __ldg(m.cg_fwd_off + lme); p < p1; ++p)
+            s = fmaf(__ldg(m.cg_fwd_v + p), sP[__ldg(m.cg_fwd_p + p) * C + kc], s);
+          Phi1[(static_cast<size_t>(i) * m.n_lme + lme) * C + kc] = s;
+          if (m.op_phi1) {
+            __nv_bfloat16* row = m.op_phi1 + static_cast<size_t>(T) * in.N * m.lme_off[l] * C +
+                                 (static_cast<size_t>(i) * (2 * l + 1) + mm) * T * Kl;
+            write_split(row, Kl, T, e * C + kc, s);
+          }
+        }
+    }
+}
+
+namespace {
+
+template <int G>
+__host__ __device__ constexpr bool l2_uses_l2(int l2) {
+  for (int w = 0; w < l2_count(G); ++w)
+    if (ins_l2(2, l2_ins(G, w)) == l2) return true;
+  return false;
+}
+
+// Adjoint, group G, one staged chunk (as l1_rev_edge, scalar, this group's paths).
+template <int G>
+__device__ __forceinline__ void l2_rev_chunk(const DevModel& m, const float* __restrict__ H1,
+                                             float* __restrict__ H1_adj, const L1Stage<true>& st, int C, int k,
+                                             bool live, const float* g, float (*sF)[32][3]) {
+  constexpr int NL2 = 9, NI = 17;
+  const int na = st.nact;
+  for (int a = 0; a < na; ++a) {
+    const int t = st.act[a];
+    const float x = st.x[t];
+    const int j = st.j[t];
+    float hv[NL2];
+    const float* hj = H1 + static_cast<size_t>(j) * NL2 * C + k;
+#pragma unroll
+    for (int b = 0; b < NL2; ++b) hv[b] = __ldg(hj + b * C);
+    const float4* cp = m.spl1_fwd + static_cast<size_t>(st.row[t]) * NI * C + k;
+    float dY[16], hadj[NL2], dr = 0.0f;
+#pragma unroll
+    for (int c = 0; c < 16; ++c) dY[c] = 0.0f;
+#pragma unroll
+    for (int b = 0; b < NL2; ++b) hadj[b] = 0.0f;
+    static_for<l2_count(G)>([&](auto ic) {
+      constexpr int i = decltype(ic)::value;
+      constexpr int q = l2_ins(G, i);
+      constexpr int l1 = ins_l1(2, q), l2 = ins_l2(2, q), g0 = l2_goff<G>(i), nb = 2 * l2 + 1;
+      const float4 cc = __ldg(cp + q * C);
+      const float R = spline_val(cc, x), Rd = spline_der(cc, x);
+      float dRq = 0.0f;
+#pragma unroll
+      for (int a1 = 0; a1 < 2 * l1 + 1; ++a1) {
+        const float y = st.Y2[t][l1 * l1 + a1].x;
+        float gs = 0.0f;
+#pragma unroll
+        for (int b = 0; b < nb; ++b) gs = fmaf(g[g0 + a1 * nb + b], hv[l2 * l2 + b], gs);
+        dRq = fmaf(gs, y, dRq);
+        dY[l1 * l1 + a1] = fmaf(R, gs, dY[l1 * l1 + a1]);
+        const float ry = R * y;
+#pragma unroll
+        for (int b = 0; b < nb; ++b) hadj[l2 * l2 + b] = fmaf(ry, g[g0 + a1 * nb + b], hadj[l2 * l2 + b]);
+      }
+      dr = fmaf(dRq, Rd, dr);
+    });
+    const float4 u = st.u[t];
+    float fx = dr * u.x, fy = dr * u.y, fz = dr * u.z;
+    static_for<16>([&](auto cc) {
+      constexpr int c = decltype(cc)::value;
+      if constexpr (l2_uses_y<G>(c)) {
+        const float4 gc = st.G[t][c];
+        fx = fmaf(dY[c], gc.x, fx);
+        fy = fmaf(dY[c], gc.y, fy);
+        fz = fmaf(dY[c], gc.z, fz);
+      }
+    });
+    if (!live) fx = fy = fz = 0.0f;
+    block_reduce3_w32(fx, fy, fz, sF, t);
+    if (live) {
+      float* dst = H1_adj + static_cast<size_t>(j) * NL2 * C + k;
+      static_for<3>([&](auto lc) {
+        constexpr int l2 = decltype(lc)::value;
+        if constexpr (l2_uses_l2<G>(l2)) {
+#pragma unroll
+          for (int b = 0; b < 2 * l2 + 1; ++b) atomicAdd(dst + (l2 * l2 + b) * C, hadj[l2 * l2 + b]);
+        }
+      });
+    }
+  }
+}
+
+}  // namespace
+
+// Layer-1 adjoint, L_max = 2.
+__global__ void __launch_bounds__(512, 1) k_layer1_rev_l2(DevModel m, EdgeIn in, const float* __restrict__ H1,
+                                                          const float* __restrict__ dPhi1,
+                                                          float* __restrict__ H1_adj, double* __restrict__ f1) {
+  constexpr int NP = 243;
+  extern __shared__ float dyn[];
+  __shared__ L1Stage<true> st;
+  __shared__ float sF[kEdgeChunk][32][3];
+  const int C = m.C, CP = (C + 31) & ~31, i = blockIdx.x;
+  const int grp = threadIdx.x / CP, kk = threadIdx.x - grp * CP;
+  const bool live = kk < C;
+  const int k = live ? kk : 0;
+  const int nwarp = blockDim.x >> 5;
+  const int ti = in.node_type[i];
+  const int e0 = in.first[i], e1 = in.first[i + 1];
+  float* sD = dyn;                 // [n_lme][C]
+  float* sP = dyn + m.n_lme * C;   // [NP][C]
+  for (int kc = threadIdx.x; kc < C; kc += blockDim.x) {
+    for (int lme = 0; lme < m.n_lme; ++lme)
+      sD[lme * C + kc] = dPhi1[(static_cast<size_t>(i) * m.n_lme + lme) * C + kc];
+    for (int p = 0; p < NP; ++p) {
+      float s = 0.0f;
+      const int q1 = __ldg(m.cg_rev_off + p + 1);
+      for (int q = __ldg(m.cg_rev_off + p); q < q1; ++q)
+        s = fmaf(__ldg(m.cg_rev_v + q), sD[__ldg(m.cg_rev_lme + q) * C + kc], s);
+      sP[p * C + kc] = s;
+    }
+  }
+  __syncthreads();
+  float g[kL2MaxNp];
+  switch (grp) {
+    case 0: l2_load_g<0>(sP, C, k, g); break;
+    case 1: l2_load_g<1>(sP, C, k, g); break;
+    case 2: l2_load_g<2>(sP, C, k, g); break;
+    default: l2_load_g<3>(sP, C, k, g); break;
+  }
+  for (int eb = e0; eb < e1; eb += kEdgeChunk) {
+    const int ne = min(kEdgeChunk, e1 - eb);
+    __syncthreads();
+    stage_l1<true>(m, in, ti, eb, ne, st);
+    __syncthreads();
+    switch (grp) {
+      case 0: l2_rev_chunk<0>(m, H1, H1_adj, st, C, k, live, g, sF); break;
+      case 1: l2_rev_chunk<1>(m, H1, H1_adj, st, C, k, live, g, sF); break;
+      case 2: l2_rev_chunk<2>(m, H1, H1_adj, st, C, k, live, g, sF); break;
+      default: l2_rev_chunk<3>(m, H1, H1_adj, st, C, k, live, g, sF); break;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < ne; t += blockDim.x) {
+      double s[3] = {0.0, 0.0, 0.0};
+      const long e = static_cast<long>(eb) + t;
+      if (st.row[t] >= 0)
+        for (int w = 0; w < nwarp; ++w)
+          for (int c = 0; c < 3; ++c) s[c] += static_cast<double>(sF[t][w][c]);
+      if (m.dens_spl[1]) {
+        float v, d;
+        const double r = in.r[e];
+        dens_eval(m, 1, ti, in.ntype_e[e], static_cast<float>(r), v, d);
+        const double gg = static_cast<double>(m.dens_c[1][i]) * static_cast<double>(d) / r;
+        for (int c = 0; c < 3; ++c) s[c] -= gg * in.xyz[3 * e + c];
+      }
+      for (int c = 0; c < 3; ++c) f1[3 * e + c] = s[c];
+    }
+  }
+}
+
 // threads per block of the layer-1 kernels: two warp-aligned groups of C/2
 int layer1_block(int C) { return 2 * (((C >> 1) + 31) & ~31); }
 
@@ -485,6 +791,13 @@ void dispatch_c(int C, F&& f) {
 }  // namespace
 
 cudaError_t init_layer1_kernels(const DevModel& m) {
+  if (m.L_max == 2) {
+    cudaError_t e = cudaFuncSetAttribute(k_layer1_fwd_l2, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(sizeof(float) * ins_np(2) * m.C));
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_layer1_rev_l2, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                static_cast<int>(sizeof(float) * (m.n_lme + ins_np(2)) * m.C));
+  }
   cudaError_t e = cudaSuccess;
   dispatch_c(m.C, [&](auto ct) { e = set_smem<decltype(ct)::value>(m); });
   return e;
@@ -492,6 +805,10 @@ cudaError_t init_layer1_kernels(const DevModel& m) {
 
 void launch_layer1_fwd(const DevModel& m, const EdgeIn& in, const float* H1, float* Phi1, cudaStream_t s) {
   if (in.N <= 0) return;
+  if (m.L_max == 2) {
+    k_layer1_fwd_l2<<<in.N, kL2Groups * ((m.C + 31) & ~31), sizeof(float) * ins_np(2) * m.C, s>>>(m, in, H1, Phi1);
+    return;
+  }
   const size_t smem = sizeof(float) * ins_np(1) * m.C;
   dispatch_c(m.C, [&](auto ct) {
     k_layer1_fwd<1, decltype(ct)::value><<<in.N, m.C, smem, s>>>(m, in, H1, Phi1);
@@ -501,6 +818,11 @@ void launch_layer1_fwd(const DevModel& m, const EdgeIn& in, const float* H1, flo
 void launch_layer1_rev(const DevModel& m, const EdgeIn& in, const float* H1, const float* dPhi1, float* H1_adj,
                        double* f1, cudaStream_t s) {
   if (in.N <= 0) return;
+  if (m.L_max == 2) {
+    k_layer1_rev_l2<<<in.N, kL2Groups * ((m.C + 31) & ~31), sizeof(float) * (m.n_lme + ins_np(2)) * m.C, s>>>(
+        m, in, H1, dPhi1, H1_adj, f1);
+    return;
+  }
   const size_t smem = sizeof(float) * (m.n_lme + ins_np(1)) * m.C;
   dispatch_c(m.C, [&](auto ct) {
     k_layer1_rev<1, decltype(ct)::value><<<in.N, layer1_block(m.C), smem, s>>>(m, in, H1, dPhi1, H1_adj, f1);

@@ -235,3 +235,42 @@ def test_density_scaled_model_matches_oracle(engine_lib, tmp_path, zbl):
     for s in ("A0", "A1", "A0_adj", "A1_adj", "Phi1_adj"):
         a, b = m.stage(s), ref.get(s)
         assert _report(s, a, b) <= 1e-4 * max(np.abs(b).max(), 1e-30), s
+
+
+@pytest.mark.parametrize("variant", ["plain", "density_zbl"])
+def test_lmax2_model_matches_oracle(engine_lib, tmp_path, variant):
+    """L_max = 2 hidden irreps (17 layer-1 instructions, 243 paths, nine LM outputs):
+    energies, edge forces and stage buffers against the oracle."""
+    extra = dict(density_scaled=True, zbl=True) if variant == "density_zbl" else {}
+    path = write_model(make_model(num_channels=32, species=("H", "C", "O"), r_cut=5.0, L_max=2, num_knots=60,
+                                  seed=3, **extra), str(tmp_path / "l2.json"))
+    pos, L, species = random_box(64, 0.064, 0.9, 3, seed=4)
+    nl = neighbor_list(pos, 5.0, L)
+    m = _engine(path, keep_stages=True)
+    assert m.L_max == 2 and m.num_LM == 9
+    m.compute_node_energies_forces(*edge_args(species, nl))
+    ref = Evaluator(path, "port")
+    ref.compute_node_energies_forces(*edge_args(species, nl))
+    assert _report("E_i", m.node_energies, ref.node_energies) < E_TOL
+    assert _report("f_edge", m.node_forces, ref.node_forces) < F_TOL
+    for s in ("M0", "H1", "Phi1", "A1", "H1_adj", "Phi1_adj", "M0_adj", "A0_adj"):
+        a, b = m.stage(s), ref.get(s)
+        assert a.shape == b.shape, s
+        assert _report(s, a, b) <= 1e-4 * max(np.abs(b).max(), 1e-30), s
+
+
+def test_lmax2_wide_model(engine_lib, tmp_path):
+    """L_max = 2 at 128 channels (the precision-form shape), both forms against the oracle."""
+    path = write_model(make_model(num_channels=128, species=("H", "C", "N", "O"), r_cut=5.0, L_max=2,
+                                  num_knots=40, seed=8), str(tmp_path / "l2w.json"))
+    pos, L, species = random_box(96, 0.09, 0.9, 4, seed=6)
+    nl = neighbor_list(pos, 5.0, L)
+    ref = Evaluator(path, "port")
+    ref.compute_node_energies_forces(*edge_args(species, nl))
+    Fr = atomic_forces(96, nl["i"], nl["neigh_indices"], ref.node_forces)
+    for precision, tol in (("float32", F_TOL), ("bfloat16", 1e-2)):
+        m = _engine(path, precision=precision)
+        m.compute_node_energies_forces(*edge_args(species, nl))
+        F = atomic_forces(96, nl["i"], nl["neigh_indices"], m.node_forces)
+        assert _report(f"{precision} E_i", m.node_energies, ref.node_energies) < (E_TOL if tol == F_TOL else 5e-3)
+        assert _report(f"{precision} F_atom", F, Fr) < tol

@@ -49,8 +49,20 @@ import numpy as np  # noqa: E402
 
 METRIC = "atom-steps/s (E+F) on 1 GB300: BF16-mixed vs FP32 at <=10 meV/A force error"
 UNIT = "atom-steps/s"
-WORKLOAD = dict(name="fp32_4096", n_atoms=4096, density=0.10, min_dist=0.9, model_seed=1, struct_seed=2,
-                cpu_sample_atoms=256)
+WORKLOADS = {
+    # the headline: 4096 atoms, 128x0e+128x1o, H/C/N/O, r_cut 5
+    "fp32_4096": dict(name="fp32_4096", config="fp32_4096", n_atoms=4096, density=0.10, min_dist=0.9, n_species=4,
+                      r_cut=5.0, model_seed=1, struct_seed=2, cpu_sample_atoms=256,
+                      text="fp32_4096: periodic box, 4096 atoms, 0.10 atoms/A^3, H/C/N/O, 128x0e+128x1o, l_max 3, "
+                           "correlation 3, r_cut 5 A, 200 spline knots, ZBL"),
+    # the precision-form shape: 32768 atoms, 128x0e+128x1o+128x2e, 10 species, r_cut 6
+    "precision_32768": dict(name="precision_32768", config="bf16_32768", n_atoms=32768, density=0.09, min_dist=0.9,
+                            n_species=10, r_cut=6.0, model_seed=1, struct_seed=2, cpu_sample_atoms=128,
+                            text="precision_32768: periodic box, 32768 atoms, 0.09 atoms/A^3, 10 species, "
+                                 "128x0e+128x1o+128x2e (L_max 2), l_max 3, correlation 3, r_cut 6 A, 200 spline "
+                                 "knots, ZBL"),
+}
+WORKLOAD = WORKLOADS["fp32_4096"]
 CACHE = os.path.join(tempfile.gettempdir(), "smx_bench")
 
 
@@ -67,22 +79,44 @@ def model_path():
     path = os.path.join(CACHE, f"model_{WORKLOAD['name']}_zbl_s{WORKLOAD['model_seed']}.json")
     if not os.path.exists(path):
         t = time.time()
-        write_model(make_model(**CONFIGS["fp32_4096"], seed=WORKLOAD["model_seed"], zbl=True), path + ".tmp")
+        model = make_model(**CONFIGS[WORKLOAD["config"]], seed=WORKLOAD["model_seed"], zbl=True)
+        json.dump(dims_of(model), open(path + ".dims.json", "w"))
+        write_model(model, path + ".tmp")
+        del model
         os.replace(path + ".tmp", path)
         log(f"model written in {time.time() - t:.1f} s")
     return path
 
 
+def engine_model_path(path):
+    """The engine loads a binary cache of the model (written once next to the JSON)."""
+    from symmetrix_gb300 import save_model_cache
+    cache = path[:-5] + ".smxb"
+    if not os.path.exists(cache):
+        save_model_cache(path, cache + ".tmp")
+        os.replace(cache + ".tmp", cache)
+    return cache
+
+
 def structure(n_atoms, seed):
     from symmetrix_gb300.synth.structures import neighbor_list, random_box
-    pos, L, species = random_box(n_atoms, WORKLOAD["density"], WORKLOAD["min_dist"], 4, seed=seed)
-    nl = neighbor_list(pos, 5.0, L)
+    pos, L, species = random_box(n_atoms, WORKLOAD["density"], WORKLOAD["min_dist"], WORKLOAD["n_species"], seed=seed)
+    nl = neighbor_list(pos, WORKLOAD["r_cut"], L)
     return pos, L, species, nl
 
 
 def model_dims(eng, path):
+    dims_path = path + ".dims.json"
+    if os.path.exists(dims_path):
+        return json.load(open(dims_path))
     with open(path) as f:
         m = json.load(f)
+    d = dims_of(m)
+    json.dump(d, open(dims_path, "w"))
+    return d
+
+
+def dims_of(m):
     C = m["num_channels"]
     L_max = m["L_max"]
     n_e = [sum(1 for l in m["Phi1_l"] if l == ll) for ll in range(4)]
@@ -381,6 +415,7 @@ def gpu_arm(args, rank, world, local_rank):
         dist.init_process_group("nccl")
     build()
     path = model_path()
+    epath = engine_model_path(path)
     N = WORKLOAD["n_atoms"]
     pos, L, species, nl = structure(N, WORKLOAD["struct_seed"] + rank)
     E = len(nl["r"])
@@ -390,7 +425,7 @@ def gpu_arm(args, rank, world, local_rank):
     # ---- both forms: MD timed region, per-stage times ----
     forms = {}
     for form in ("fp32", "bf16"):
-        eng = MACE(path, device=local_rank, precision=form)
+        eng = MACE(epath, device=local_rank, precision=form)
         dims = model_dims(eng, path)
         estream = torch.cuda.ExternalStream(eng.stream, device=dev)
         masses = species_masses(eng.atomic_numbers, species)
@@ -484,8 +519,7 @@ def gpu_arm(args, rank, world, local_rank):
         "metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": head["T"] / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
-        "config": {"workload": "fp32_4096: periodic box, 4096 atoms, 0.10 atoms/A^3, H/C/N/O, "
-                               "128x0e+128x1o, l_max 3, correlation 3, r_cut 5 A, 200 spline knots, ZBL",
+        "config": {"workload": WORKLOAD["text"],
                    "atoms": N, "edges_r_cut": E,
                    "form": "BF16-mixed: channel-mixing GEMMs on tcgen05 with bf16 split operands (3 terms) and "
                            "f32 accumulation; radials, Y_lm, contractions and adjoint in f32; f64 sums",
@@ -596,9 +630,13 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="fp32_4096", choices=["fp32_4096", "molecules"],
-                    help="fp32_4096: the headline line; molecules: the batching form (2048 molecules)")
+    ap.add_argument("--workload", default="fp32_4096", choices=["fp32_4096", "precision_32768", "molecules"],
+                    help="fp32_4096: the headline line; precision_32768: L_max 2, 10 species, 32768 atoms; "
+                         "molecules: the batching form (2048 molecules)")
     args = ap.parse_args()
+    global WORKLOAD
+    if args.workload in WORKLOADS:
+        WORKLOAD = WORKLOADS[args.workload]
     if args.warmup < 3:
         args.warmup = 3
     rank = int(os.environ.get("RANK", 0))

@@ -56,6 +56,11 @@ WORKLOADS = {
                       text="fp32_4096: periodic box, 4096 atoms, 0.10 atoms/A^3, H/C/N/O, 128x0e+128x1o, l_max 3, "
                            "correlation 3, r_cut 5 A, 200 spline knots, ZBL"),
     # the precision-form shape: 32768 atoms, 128x0e+128x1o+128x2e, 10 species, r_cut 6
+    # the large single system: 1,048,576 atoms, 128x0e+128x1o, 10 species, r_cut 5 (MD only)
+    "large_1m": dict(name="large_1m", config="large_1m", n_atoms=1048576, density=0.10, min_dist=0.9, n_species=10,
+                     r_cut=5.0, model_seed=1, struct_seed=2, cpu_sample_atoms=128,
+                     text="large_1m: periodic box, 1,048,576 atoms, 0.10 atoms/A^3, 10 species, 128x0e+128x1o, "
+                          "l_max 3, correlation 3, r_cut 5 A, 200 spline knots, ZBL"),
     "precision_32768": dict(name="precision_32768", config="bf16_32768", n_atoms=32768, density=0.09, min_dist=0.9,
                             n_species=10, r_cut=6.0, model_seed=1, struct_seed=2, cpu_sample_atoms=128,
                             text="precision_32768: periodic box, 32768 atoms, 0.09 atoms/A^3, 10 species, "
@@ -624,13 +629,71 @@ def molecules_arm(args):
     }), flush=True)
 
 
+def large_arm(args):
+    """MD of the 1,048,576-atom box in both forms (one engine alive at a time: the node
+    features of one form take ~90 GB)."""
+    import gc
+
+    import torch
+
+    from symmetrix_gb300 import MACE
+    from symmetrix_gb300.build import build
+    from symmetrix_gb300.md import MD
+    from symmetrix_gb300.synth.structures import maxwell_boltzmann, random_box, species_masses
+
+    build()
+    path = engine_model_path(model_path())
+    W = WORKLOAD
+    sfile = os.path.join(CACHE, f"{W['name']}_s{W['struct_seed']}.npz")
+    if os.path.exists(sfile):
+        z = np.load(sfile)
+        pos, L, species = z["pos"], float(z["L"]), z["species"]
+    else:
+        t = time.time()
+        pos, L, species = random_box(W["n_atoms"], W["density"], W["min_dist"], W["n_species"], seed=W["struct_seed"])
+        np.savez(sfile, pos=pos, L=L, species=species)
+        log(f"structure built in {time.time() - t:.0f} s")
+    N = len(pos)
+    dev = torch.device("cuda", 0)
+    out = {}
+    for form in ("fp32", "bf16"):
+        eng = MACE(path, precision=form)
+        estream = torch.cuda.ExternalStream(eng.stream, device=dev)
+        masses = species_masses(eng.atomic_numbers, species)
+        vel = maxwell_boltzmann(masses, 300.0, np.random.default_rng(3))
+        md = MD(eng, pos, species, masses, box=L, velocities=vel, dt=0.5, skin=1.0, rebuild_every=10)
+        md.run(args.warmup)
+        md.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(estream)
+        md.run(args.steps)
+        e1.record(estream)
+        md.sync()
+        T = e0.elapsed_time(e1) / 1e3
+        st = md.state()
+        out[form] = {"value": N * args.steps / T, "ms_per_step": T / args.steps * 1e3, "edges_skin_list": md.num_edges,
+                     "potential_energy_per_atom": st["potential_energy"] / N}
+        del md, eng
+        gc.collect()
+    print(json.dumps({
+        "metric": METRIC, "value": out["bf16"]["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": out["bf16"]["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+        "config": {"workload": W["text"] + "; MD dt 0.5 fs, neighbour list rebuilt every 10 steps (1 A skin), CUDA "
+                   "graph between rebuilds", "atoms": N},
+        "forms": out, "bf16_over_fp32": out["bf16"]["value"] / out["fp32"]["value"],
+    }), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="fp32_4096", choices=["fp32_4096", "precision_32768", "molecules"],
+    ap.add_argument("--workload", default="fp32_4096",
+                    choices=["fp32_4096", "precision_32768", "large_1m", "molecules"],
                     help="fp32_4096: the headline line; precision_32768: L_max 2, 10 species, 32768 atoms; "
                          "molecules: the batching form (2048 molecules)")
     args = ap.parse_args()
@@ -647,6 +710,9 @@ def main():
     elif args.workload == "molecules":
         if rank == 0:
             molecules_arm(args)
+    elif args.workload == "large_1m":
+        if rank == 0:
+            large_arm(args)
     else:
         gpu_arm(args, rank, world, local_rank)
 

@@ -244,6 +244,9 @@ CONFIGS = {
     # 10 species, 128x0e+128x1o+128x2e, r_cut 6
     "bf16_32768": dict(num_channels=128, species=("H", "C", "N", "O", "F", "Na", "Mg", "Al", "Si", "S"),
                        r_cut=6.0, L_max=2, num_knots=200),
+    # 10 species, 128x0e+128x1o, the 1,048,576-atom box
+    "large_1m": dict(num_channels=128, species=("H", "C", "N", "O", "F", "Na", "Mg", "Al", "Si", "S"), r_cut=5.0,
+                     L_max=1, num_knots=200),
     # 7 species, 64x0e+64x1o molecules
     "molecules": dict(num_channels=64, species=("H", "C", "N", "O", "F", "S", "Cl"), r_cut=5.0, L_max=1,
                       num_knots=200),

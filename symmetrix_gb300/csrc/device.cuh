@@ -17,7 +17,7 @@ struct DevModel {
   int S, C, L_max, nLM, n_lme, n_instr, n_p, nint, T0, T1, n_hidden;
   int poly_canon;  // coefficients in canonical order: use the generated polynomials
   float h, inv_h, r_cut, ro2_scale;
-  const float4* spl0;  // [S*S][nint][4][C]
+  const float4* spl0;  // [S*S][nint][4][2][C/2]: channel-pair planes
   const float4* spl1;      // [npairs][nint][n_instr][2][C/2]: channel-pair planes (adjoint)
   const float4* spl1_fwd;  // [npairs][nint][n_instr][C]: per-channel cubics (forward)
   const int* mono0;
@@ -246,6 +246,39 @@ __device__ __forceinline__ float warp_sum(float v) {
 }
 
 inline int ceil_div(long a, long b) { return static_cast<int>((a + b - 1) / b); }
+
+// ---- channel-pair helpers: packed FP32 (sm_100 and later: two FMAs per instruction) ----
+template <typename F, int... I>
+__device__ __forceinline__ void static_for_impl(F&& f, std::integer_sequence<int, I...>) {
+  (f(std::integral_constant<int, I>{}), ...);
+}
+// f(std::integral_constant<int, i>) for i in [0, N)
+template <int N, typename F>
+__device__ __forceinline__ void static_for(F&& f) {
+  static_for_impl(f, std::make_integer_sequence<int, N>{});
+}
+
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+
+// Cubic of a channel pair at offset x2 = (x, x) inside its interval, value only.
+__device__ __forceinline__ float2 spline2_val(float4 lo, float4 hi, float2 x2) {
+  const float2 c0 = make_float2(lo.x, lo.y), c1 = make_float2(lo.z, lo.w);
+  const float2 c2 = make_float2(hi.x, hi.y), c3 = make_float2(hi.z, hi.w);
+  return fma2(fma2(fma2(c3, x2, c2), x2, c1), x2, c0);
+}
+// Value and derivative by the two-row Horner scheme (5 packed FMAs).
+__device__ __forceinline__ void spline2(float4 lo, float4 hi, float2 x2, float2& R, float2& Rd) {
+  const float2 c0 = make_float2(lo.x, lo.y), c1 = make_float2(lo.z, lo.w);
+  const float2 c2 = make_float2(hi.x, hi.y), c3 = make_float2(hi.z, hi.w);
+  float2 p = fma2(c3, x2, c2);
+  float2 d = fma2(c3, x2, p);
+  p = fma2(p, x2, c1);
+  d = fma2(d, x2, p);
+  R = fma2(p, x2, c0);
+  Rd = d;
+}
+
 
 // Density-normalisation spline of `layer` for the unordered pair (ti, tj) at r: value
 // and r-derivative (CubicSpline::evaluate_deriv, libsymmetrix/source/cubic_spline.cpp:29-41).

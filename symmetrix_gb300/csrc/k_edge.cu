@@ -44,7 +44,7 @@ namespace {
 // compacted list of active edges (r < r_cut).
 template <bool GRAD>
 struct L0Stage {
-  float4 Y[kEdgeChunk][4];
+  float2 Y2[kEdgeChunk][16];  // (Y_lm, Y_lm): operand of the packed FMAs
   float4 G[GRAD ? kEdgeChunk : 1][16];  // (dY_lm/dx, dY_lm/dy, dY_lm/dz, 0)
   float4 u[GRAD ? kEdgeChunk : 1];
   float x[kEdgeChunk];
@@ -68,7 +68,7 @@ __device__ __forceinline__ void stage_l0(const DevModel& m, const EdgeIn& in, in
     float Y[16], G[GRAD ? 48 : 1];
     sph_harm16<GRAD>(vx, vy, vz, Y, G);
 #pragma unroll
-    for (int q = 0; q < 4; ++q) st.Y[t][q] = make_float4(Y[4 * q], Y[4 * q + 1], Y[4 * q + 2], Y[4 * q + 3]);
+    for (int q = 0; q < 16; ++q) st.Y2[t][q] = make_float2(Y[q], Y[q]);
     if constexpr (GRAD) {
 #pragma unroll
       for (int c = 0; c < 16; ++c) st.G[t][c] = make_float4(G[c], G[16 + c], G[32 + c], 0.0f);
@@ -94,106 +94,110 @@ __device__ __forceinline__ void stage_l0(const DevModel& m, const EdgeIn& in, in
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_layer0_fwd(DevModel m, EdgeIn in, float* __restrict__ A0,
                                                     float* __restrict__ M0, float* __restrict__ zbl_e) {
-  extern __shared__ float dyn[];
+  extern __shared__ float dyn[];  // [17][C]: A0 columns (+ constant one) for the contraction
   __shared__ L0Stage<false> st;
-  const int C = m.C, k = threadIdx.x, i = blockIdx.x;
+  const int C = m.C, C2 = C >> 1, BW = (C2 + 31) & ~31, i = blockIdx.x;
+  // two groups of channel-pair threads, each taking every other active edge
+  const int half = static_cast<int>(threadIdx.x) >= BW ? 1 : 0;
+  const int lt = threadIdx.x - half * BW;
+  const bool live = lt < C2;
+  const int cp = live ? lt : 0, kc = 2 * cp;
   const int ti = in.node_type[i];
   const int e0 = in.first[i], e1 = in.first[i + 1];
-  float acc[16];
+  float2 acc[16];
 #pragma unroll
-  for (int q = 0; q < 16; ++q) acc[q] = 0.0f;
+  for (int q = 0; q < 16; ++q) acc[q] = make_float2(0.0f, 0.0f);
   for (int eb = e0; eb < e1; eb += kEdgeChunk) {
     const int ne = min(kEdgeChunk, e1 - eb);
     __syncthreads();
     stage_l0<false>(m, in, ti, eb, ne, st);
     __syncthreads();
-    // active edges; the next edge's four cubics load while this one accumulates
+    // this group's active edges; the next one's cubics load while this one accumulates
     const int na = st.nact;
-    float4 c[4];
-    if (na > 0) {
-      const float4* cp = m.spl0 + static_cast<size_t>(st.row[st.act[0]]) * 4 * C + k;
+    float4 c[8];
+    auto fetch = [&](int a) {
+      const float4* p = m.spl0 + static_cast<size_t>(st.row[st.act[a]]) * 4 * C + cp;
 #pragma unroll
-      for (int l = 0; l < 4; ++l) c[l] = __ldg(cp + l * C);
-    }
-    for (int a = 0; a < na; ++a) {
+      for (int q = 0; q < 8; ++q) c[q] = __ldg(p + q * C2);
+    };
+    if (half < na) fetch(half);
+    for (int a = half; a < na; a += 2) {
       const int t = st.act[a];
-      const float x = st.x[t];
-      float R[4];
+      const float2 x2 = make_float2(st.x[t], st.x[t]);
+      float2 R[4];
 #pragma unroll
-      for (int l = 0; l < 4; ++l) R[l] = spline_val(c[l], x);
-      if (a + 1 < na) {
-        const float4* cp = m.spl0 + static_cast<size_t>(st.row[st.act[a + 1]]) * 4 * C + k;
+      for (int l = 0; l < 4; ++l) R[l] = spline2_val(c[2 * l], c[2 * l + 1], x2);
+      if (a + 2 < na) fetch(a + 2);
 #pragma unroll
-        for (int l = 0; l < 4; ++l) c[l] = __ldg(cp + l * C);
-      }
-#pragma unroll
-      for (int q4 = 0; q4 < 4; ++q4) {
-        const float4 y = st.Y[t][q4];
-        const float yy[4] = {y.x, y.y, y.z, y.w};
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const int q = 4 * q4 + j;
-          const int l = q < 1 ? 0 : (q < 4 ? 1 : (q < 9 ? 2 : 3));
-          acc[q] = fmaf(R[l], yy[j], acc[q]);
-        }
+      for (int q = 0; q < 16; ++q) {
+        const int l = q < 1 ? 0 : (q < 4 ? 1 : (q < 9 ? 2 : 3));
+        acc[q] = fma2(R[l], st.Y2[t][q], acc[q]);
       }
     }
   }
   if (m.has_zbl) {  // ZBL energy of node i: sum over its directed edges (zbl.cpp:96-125)
-    __shared__ float sz[8];
     float z = 0.0f;
     for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
       float V, dV;
       zbl_edge(m, m.zbl_pair[ti * m.S + in.ntype_e[e]], static_cast<float>(in.r[e]), V, dV);
       z += V;
     }
-    z = warp_sum(z);
-    if ((threadIdx.x & 31) == 0) sz[threadIdx.x >> 5] = z;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      float t = 0.0f;
-      for (int w = 0; w < (C >> 5); ++w) t += sz[w];
-      zbl_e[i] = t;
-    }
+    z = block_sum(z);
+    if (threadIdx.x == 0) zbl_e[i] = z;
   }
+  float S = 1.0f;
   if (m.dens_spl[0]) {  // density-normalised A0: A0 /= 1 + sum_j s(r_ij)  (mace.cpp:273-297)
-    const float S = dens_factor(m, 0, in, i, ti);
+    S = dens_factor(m, 0, in, i, ti);
     if (threadIdx.x == 0) m.dens_s[0][i] = S;
-#pragma unroll
-    for (int q = 0; q < 16; ++q) acc[q] /= S;
   }
+  float* sA = dyn;
+  if (half == 1 && live)
 #pragma unroll
-  for (int q = 0; q < 16; ++q) A0[(static_cast<size_t>(i) * 16 + q) * C + k] = acc[q];
-  if (m.poly_canon) {  // generated straight-line polynomials, A0 column in registers
-    const float* cf = m.coef0 + static_cast<size_t>(ti * m.nLM) * m.T0 * C + k;
-    const size_t st = static_cast<size_t>(m.T0) * C;
-    float* out = M0 + static_cast<size_t>(i) * m.nLM * C + k;
-    const float v[4] = {poly::value_LM0(acc, cf, C), poly::value_LM1(acc, cf + st, C),
-                        poly::value_LM2(acc, cf + 2 * st, C), poly::value_LM3(acc, cf + 3 * st, C)};
+    for (int q = 0; q < 16; ++q) *reinterpret_cast<float2*>(sA + q * C + kc) = acc[q];
+  __syncthreads();
+  if (half == 0 && live) {
 #pragma unroll
-    for (int LM = 0; LM < 4; ++LM) {
-      out[LM * C] = v[LM];
-      if (m.op_m0)  // BF16 form: the H1 GEMM's split operand
-        write_split(m.op_m0 + (static_cast<size_t>(i) * m.nLM + LM) * m.tc_terms * C, C, m.tc_terms, k, v[LM]);
+    for (int q = 0; q < 16; ++q) {
+      const float2 o = *reinterpret_cast<const float2*>(sA + q * C + kc);
+      const float2 v = make_float2((acc[q].x + o.x) / S, (acc[q].y + o.y) / S);
+      *reinterpret_cast<float2*>(sA + q * C + kc) = v;
+      *reinterpret_cast<float2*>(A0 + (static_cast<size_t>(i) * 16 + q) * C + kc) = v;
     }
-    return;
   }
-  float* sA = dyn;  // [17][C]: this thread's A0 column (+ constant one) for the contraction
+  for (int k = threadIdx.x; k < C; k += blockDim.x) sA[16 * C + k] = 1.0f;
+  __syncthreads();
+  // the symmetric contraction, one thread per channel
+  for (int k = threadIdx.x; k < C; k += blockDim.x) {
+    if (m.poly_canon) {  // generated straight-line polynomials, A0 column in registers
+      float x[16];
 #pragma unroll
-  for (int q = 0; q < 16; ++q) sA[q * C + k] = acc[q];
-  sA[16 * C + k] = 1.0f;
-  for (int LM = 0; LM < m.nLM; ++LM) {
-    const int t0 = m.mono0_off[LM], t1 = m.mono0_off[LM + 1];
-    const float* cf = m.coef0 + (static_cast<size_t>(ti * m.nLM + LM) * m.T0) * C + k;
-    float f = 0.0f;
-    for (int t = t0; t < t1; ++t) {
-      const int pk = __ldg(m.mono0 + t);
-      const float xa = sA[(pk & 255) * C + k], xb = sA[((pk >> 8) & 255) * C + k], xc = sA[(pk >> 16) * C + k];
-      f = fmaf(__ldg(cf + static_cast<size_t>(t - t0) * C), xa * xb * xc, f);
+      for (int q = 0; q < 16; ++q) x[q] = sA[q * C + k];
+      const float* cf = m.coef0 + static_cast<size_t>(ti * m.nLM) * m.T0 * C + k;
+      const size_t sst = static_cast<size_t>(m.T0) * C;
+      float* out = M0 + static_cast<size_t>(i) * m.nLM * C + k;
+      const float v[4] = {poly::value_LM0(x, cf, C), poly::value_LM1(x, cf + sst, C),
+                          poly::value_LM2(x, cf + 2 * sst, C), poly::value_LM3(x, cf + 3 * sst, C)};
+#pragma unroll
+      for (int LM = 0; LM < 4; ++LM) {
+        out[LM * C] = v[LM];
+        if (m.op_m0)  // BF16 form: the H1 GEMM's split operand
+          write_split(m.op_m0 + (static_cast<size_t>(i) * m.nLM + LM) * m.tc_terms * C, C, m.tc_terms, k, v[LM]);
+      }
+      continue;
     }
-    M0[(static_cast<size_t>(i) * m.nLM + LM) * C + k] = f;
-    if (m.op_m0)
-      write_split(m.op_m0 + (static_cast<size_t>(i) * m.nLM + LM) * m.tc_terms * C, C, m.tc_terms, k, f);
+    for (int LM = 0; LM < m.nLM; ++LM) {
+      const int t0 = m.mono0_off[LM], t1 = m.mono0_off[LM + 1];
+      const float* cf = m.coef0 + (static_cast<size_t>(ti * m.nLM + LM) * m.T0) * C + k;
+      float f = 0.0f;
+      for (int t = t0; t < t1; ++t) {
+        const int pk = __ldg(m.mono0 + t);
+        const float xa = sA[(pk & 255) * C + k], xb = sA[((pk >> 8) & 255) * C + k], xc = sA[(pk >> 16) * C + k];
+        f = fmaf(__ldg(cf + static_cast<size_t>(t - t0) * C), xa * xb * xc, f);
+      }
+      M0[(static_cast<size_t>(i) * m.nLM + LM) * C + k] = f;
+      if (m.op_m0)
+        write_split(m.op_m0 + (static_cast<size_t>(i) * m.nLM + LM) * m.tc_terms * C, C, m.tc_terms, k, f);
+    }
   }
 }
 
@@ -273,68 +277,63 @@ __global__ void __launch_bounds__(256) k_contract0_rev(DevModel m, const int* __
 // -(layer 0 + layer 1).  The next active edge's four spline cubics are loaded while
 // this edge computes.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_layer0_rev(DevModel m, EdgeIn in, const float* __restrict__ A0_adj,
+__global__ void __launch_bounds__(128) k_layer0_rev(DevModel m, EdgeIn in, const float* __restrict__ A0_adj,
                                                     const double* __restrict__ f1, double* __restrict__ forces) {
   __shared__ L0Stage<true> st;
   __shared__ float sF[kEdgeChunk][8][3];
-  const int C = m.C, k = threadIdx.x, i = blockIdx.x;
-  const int nwarp = C >> 5;
+  const int C = m.C, C2 = C >> 1, i = blockIdx.x;
+  const bool live = static_cast<int>(threadIdx.x) < C2;
+  const int cp = live ? threadIdx.x : 0, kc = 2 * cp;  // this thread's channel pair
+  const int nwarp = blockDim.x >> 5;
   const int ti = in.node_type[i];
   const int e0 = in.first[i], e1 = in.first[i + 1];
-  float dA[16];
+  float2 dA[16];
 #pragma unroll
-  for (int q = 0; q < 16; ++q) dA[q] = A0_adj[(static_cast<size_t>(i) * 16 + q) * C + k];
+  for (int q = 0; q < 16; ++q)
+    dA[q] = *reinterpret_cast<const float2*>(A0_adj + (static_cast<size_t>(i) * 16 + q) * C + kc);
   for (int eb = e0; eb < e1; eb += kEdgeChunk) {
     const int ne = min(kEdgeChunk, e1 - eb);
     __syncthreads();
     stage_l0<true>(m, in, ti, eb, ne, st);
     __syncthreads();
     const int na = st.nact;
-    float4 c[4];
-    if (na > 0) {
-      const float4* cp = m.spl0 + static_cast<size_t>(st.row[st.act[0]]) * 4 * C + k;
+    float4 c[8];
+    auto fetch = [&](int a) {
+      const float4* p = m.spl0 + static_cast<size_t>(st.row[st.act[a]]) * 4 * C + cp;
 #pragma unroll
-      for (int l = 0; l < 4; ++l) c[l] = __ldg(cp + l * C);
-    }
+      for (int q = 0; q < 8; ++q) c[q] = __ldg(p + q * C2);
+    };
+    if (na > 0) fetch(0);
     for (int a = 0; a < na; ++a) {
       const int t = st.act[a];
-      const float x = st.x[t];
-      float R[4], Rd[4];
+      const float2 x2 = make_float2(st.x[t], st.x[t]);
+      float2 R[4], Rd[4];
+#pragma unroll
+      for (int l = 0; l < 4; ++l) spline2(c[2 * l], c[2 * l + 1], x2, R[l], Rd[l]);
+      if (a + 1 < na) fetch(a + 1);
+      float2 dr = make_float2(0.0f, 0.0f);
+      float fx = 0.0f, fy = 0.0f, fz = 0.0f;
 #pragma unroll
       for (int l = 0; l < 4; ++l) {
-        R[l] = spline_val(c[l], x);
-        Rd[l] = spline_der(c[l], x);
-      }
-      if (a + 1 < na) {
-        const float4* cp = m.spl0 + static_cast<size_t>(st.row[st.act[a + 1]]) * 4 * C + k;
-#pragma unroll
-        for (int l = 0; l < 4; ++l) c[l] = __ldg(cp + l * C);
-      }
-      float Y[16];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const float4 v = st.Y[t][q];
-        Y[4 * q] = v.x; Y[4 * q + 1] = v.y; Y[4 * q + 2] = v.z; Y[4 * q + 3] = v.w;
-      }
-      float dr = 0.0f, fx = 0.0f, fy = 0.0f, fz = 0.0f;
-#pragma unroll
-      for (int l = 0; l < 4; ++l) {
-        float dRl = 0.0f;
+        float2 dRl = make_float2(0.0f, 0.0f);
 #pragma unroll
         for (int q = l * l; q < (l + 1) * (l + 1); ++q) {
-          dRl = fmaf(dA[q], Y[q], dRl);
-          const float w = dA[q] * R[l];
+          dRl = fma2(dA[q], st.Y2[t][q], dRl);
+          const float2 w = mul2(dA[q], R[l]);
+          const float s = w.x + w.y;
           const float4 g = st.G[t][q];
-          fx = fmaf(w, g.x, fx);
-          fy = fmaf(w, g.y, fy);
-          fz = fmaf(w, g.z, fz);
+          fx = fmaf(s, g.x, fx);
+          fy = fmaf(s, g.y, fy);
+          fz = fmaf(s, g.z, fz);
         }
-        dr = fmaf(dRl, Rd[l], dr);
+        dr = fma2(dRl, Rd[l], dr);
       }
+      const float d = dr.x + dr.y;
       const float4 u = st.u[t];
-      fx = fmaf(dr, u.x, fx);
-      fy = fmaf(dr, u.y, fy);
-      fz = fmaf(dr, u.z, fz);
+      fx = fmaf(d, u.x, fx);
+      fy = fmaf(d, u.y, fy);
+      fz = fmaf(d, u.z, fz);
+      if (!live) fx = fy = fz = 0.0f;
       block_reduce3(fx, fy, fz, sF, t);
     }
     __syncthreads();
@@ -369,17 +368,20 @@ __global__ void __launch_bounds__(256) k_layer0_rev(DevModel m, EdgeIn in, const
 // any stream capture).
 cudaError_t init_edge_kernels(const DevModel& m) { return init_layer1_kernels(m); }
 
+// layer-0 edge kernels: one thread per channel pair, whole warps
+int layer0_block(int C) { return ((C >> 1) + 31) & ~31; }
+
 void launch_layer0_fwd(const DevModel& m, const EdgeIn& in, float* A0, float* M0, float* zbl_e, cudaStream_t s) {
   if (in.N <= 0) return;
   const size_t smem = 17 * sizeof(float) * m.C;
-  k_layer0_fwd<<<in.N, m.C, smem, s>>>(m, in, A0, M0, zbl_e);
+  k_layer0_fwd<<<in.N, 2 * layer0_block(m.C), smem, s>>>(m, in, A0, M0, zbl_e);
 }
 
 void launch_layer0_rev(const DevModel& m, const EdgeIn& in, const float* A0, const float* M0_adj, const double* f1,
                        float* A0_adj, double* forces, cudaStream_t s) {
   if (in.N <= 0) return;
   k_contract0_rev<<<in.N, m.C, m.poly_canon ? 0 : 34 * sizeof(float) * m.C, s>>>(m, in.node_type, A0, M0_adj, A0_adj);
-  k_layer0_rev<<<in.N, m.C, 0, s>>>(m, in, A0_adj, f1, forces);
+  k_layer0_rev<<<in.N, layer0_block(m.C), 0, s>>>(m, in, A0_adj, f1, forces);
 }
 
 }  // namespace smx

@@ -63,37 +63,6 @@ __host__ __device__ constexpr bool half_uses_y(int c) {
   return false;
 }
 
-template <typename F, int... I>
-__device__ __forceinline__ void static_for_impl(F&& f, std::integer_sequence<int, I...>) {
-  (f(std::integral_constant<int, I>{}), ...);
-}
-// f(std::integral_constant<int, i>) for i in [0, N)
-template <int N, typename F>
-__device__ __forceinline__ void static_for(F&& f) {
-  static_for_impl(f, std::make_integer_sequence<int, N>{});
-}
-
-__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
-
-// Cubic of a channel pair at offset x2 = (x, x) inside its interval, value only.
-__device__ __forceinline__ float2 spline2_val(float4 lo, float4 hi, float2 x2) {
-  const float2 c0 = make_float2(lo.x, lo.y), c1 = make_float2(lo.z, lo.w);
-  const float2 c2 = make_float2(hi.x, hi.y), c3 = make_float2(hi.z, hi.w);
-  return fma2(fma2(fma2(c3, x2, c2), x2, c1), x2, c0);
-}
-// Value and derivative by the two-row Horner scheme (5 packed FMAs).
-__device__ __forceinline__ void spline2(float4 lo, float4 hi, float2 x2, float2& R, float2& Rd) {
-  const float2 c0 = make_float2(lo.x, lo.y), c1 = make_float2(lo.z, lo.w);
-  const float2 c2 = make_float2(hi.x, hi.y), c3 = make_float2(hi.z, hi.w);
-  float2 p = fma2(c3, x2, c2);
-  float2 d = fma2(c3, x2, p);
-  p = fma2(p, x2, c1);
-  d = fma2(d, x2, p);
-  R = fma2(p, x2, c0);
-  Rd = d;
-}
-
 // Sum a per-thread 3-vector over the block for edge t (float32 shuffles; one
 // partial per warp into sF, summed across warps in float64 after the chunk).
 __device__ __forceinline__ void block_reduce3(float fx, float fy, float fz, float (*sF)[8][3], int t) {

@@ -271,8 +271,8 @@ PackedModel pack_model(const HostModel& hm) {
           for (int iv = 0; iv < nint; ++iv)
             for (int k = 0; k < C; ++k)
               for (int p = 0; p < 4; ++p)
-                pm.spl0[((((static_cast<size_t>(ti) * S + tj) * nint + iv) * 4 + l) * C + k) * 4 + p] =
-                    static_cast<float>(out[(static_cast<size_t>(iv) * 4 + p) * C + k]);
+                pm.spl0[(((((static_cast<size_t>(ti) * S + tj) * nint + iv) * 4 + l) * 2 + p / 2) * (C / 2) + k / 2) * 4 +
+                        (p % 2) * 2 + k % 2] = static_cast<float>(out[(static_cast<size_t>(iv) * 4 + p) * C + k]);
         }
       }
   }

@@ -78,7 +78,9 @@ std::vector<std::array<int, 3>> canonical_instructions(int L_max);
 struct PackedModel {
   int S, C, L_max, nLM, n_lme, n_instr, n_p, nint, npairs;
   float h, r_cut;
-  std::vector<float> spl0;     // [S*S][nint][4 (l)][C][4 (coef)]  folded, ordered pair ti*S+tj
+  // folded, ordered pair ti*S+tj: [S*S][nint][4 (l)][2][C/2][4], channel pairs (2c, 2c+1):
+  // plane 0 = (c0, c0', c1, c1'), plane 1 = (c2, c2', c3, c3')
+  std::vector<float> spl0;
   // [npairs][nint][n_instr][2][C/2][4], canonical instruction order; channel pairs
   // (2c, 2c+1): plane 0 = (c0, c0', c1, c1'), plane 1 = (c2, c2', c3, c3')
   std::vector<float> spl1;

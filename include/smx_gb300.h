@@ -105,8 +105,16 @@ int smx_compute_node_energies_forces_device(smx_engine* eng, int num_nodes, cons
 long smx_get_stage(smx_engine* eng, const char* name, double* out, long cap);
 
 /* Options: "keep_stages" (keep A0_adj for smx_get_stage), "profile" (record CUDA
- * events between the kernels of every evaluation). */
+ * events between the kernels of every evaluation); BF16 form: "tc_terms" (1, 2 or 3
+ * bf16 split terms of the GEMM operands, default 3; set before the first evaluation),
+ * "autotune" (1, the default: the first evaluation outside a stream capture times the
+ * candidate N-tile widths and TMA ring depths of each tensor-core GEMM group on its own
+ * operands and keeps the fastest; setting it again re-tunes; 0 keeps the defaults).
+ * No counterpart in the reference (its MACE object has no options). */
 int smx_set_option(smx_engine* eng, const char* key, long value);
+/* Read an option or a tuned schedule entry ("tc_nt_<G>", "tc_stages_<G>",
+ * "tc_tuned_ns_<G>" for G in H1, A1, Phi1_adj, M0_adj); -1 if unknown. */
+long smx_get_option(const smx_engine* eng, const char* key);
 
 /* The engine's own CUDA stream (a cudaStream_t): host-pointer calls and the MD driver
  * run on it, so callers can order their work or record CUDA events against it. */

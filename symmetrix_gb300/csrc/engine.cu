@@ -124,6 +124,11 @@ int smx_set_option(smx_engine* eng, const char* key, long value) {
     eng->profile = value != 0;
     return SMX_OK;
   }
+  if (std::strcmp(key, "autotune") == 0) {  // precision form: (re)tune the GEMM schedule on the next evaluation
+    eng->autotune = value != 0;
+    for (bool& t : eng->tc_tuned) t = false;
+    return SMX_OK;
+  }
   if (std::strcmp(key, "tc_terms") == 0) {  // precision form: bf16 split terms of the GEMMs
     if (value < 1 || value > 3) return fail(SMX_ERR_INVALID, "tc_terms must be 1, 2 or 3");
     if (eng->precision != SMX_PRECISION_BF16) return fail(SMX_ERR_INVALID, "tc_terms applies to the bf16 form");
@@ -140,6 +145,23 @@ int smx_set_option(smx_engine* eng, const char* key, long value) {
     return SMX_OK;
   }
   return fail(SMX_ERR_INVALID, std::string("unknown option '") + key + "'");
+}
+
+long smx_get_option(const smx_engine* eng, const char* key) {
+  if (!eng || !key) return -1;
+  const std::string k(key);
+  if (k == "keep_stages") return eng->keep_stages;
+  if (k == "profile") return eng->profile;
+  if (k == "precision") return eng->precision;
+  if (k == "tc_terms") return eng->tc_terms;
+  if (k == "autotune") return eng->autotune;
+  static const char* groups[4] = {"H1", "A1", "Phi1_adj", "M0_adj"};
+  for (int q = 0; q < 4; ++q) {
+    if (k == std::string("tc_nt_") + groups[q]) return eng->tc_cfg[q].NT ? eng->tc_cfg[q].NT : eng->dm.C;
+    if (k == std::string("tc_stages_") + groups[q]) return eng->tc_cfg[q].stages;
+    if (k == std::string("tc_tuned_ns_") + groups[q]) return static_cast<long>(eng->tc_tuned_us[q] * 1000.0f);
+  }
+  return -1;
 }
 
 int smx_compute_node_energies_forces(smx_engine* eng, int num_nodes, const int* node_types, const int* num_neigh,

@@ -306,6 +306,77 @@ struct smx_engine {
     if (profile) check(cudaEventRecord(ev[q], s), "cudaEventRecord");
   }
 
+  // ---- tensor-core GEMM schedule (BF16 form) and its autotuner ----
+  // Groups: 0 H1, 1 A1 (one launch for all l), 2 Phi1_adj (ditto), 3 M0_adj.  The N-tile
+  // width (A1, Phi1_adj; the H1/M0_adj tiles are the two L blocks, so N-tile = C) and the
+  // TMA ring depth are picked by timing the candidates on the first evaluation's own
+  // operands (CUDA events, one warm-up and three timed launches each), then kept.
+  struct TcCfg {
+    int NT = 0;  // 0: C
+    int stages = 4;
+  };
+  TcCfg tc_cfg[4];
+  bool tc_tuned[4] = {false, false, false, false};
+  bool autotune = true;
+  float tc_tuned_us[4] = {0, 0, 0, 0};
+
+  void tc_apply(const TcCfg& c, smx::UmmaGemm* g, int ng, bool tile_n) const {
+    for (int q = 0; q < ng; ++q) {
+      if (tile_n) g[q].NT = c.NT ? c.NT : dm.C;
+      g[q].stages = c.stages;
+    }
+  }
+
+  void tc_tune(int gid, smx::UmmaGemm* g, int ng, bool tile_n, cudaStream_t s) {
+    const int C = dm.C;
+    std::vector<TcCfg> cand;
+    for (int nt : {C, C / 2, 2 * C}) {
+      if (!tile_n && nt != C) continue;
+      bool ok = nt >= 64 && nt <= 256;
+      for (int q = 0; q < ng && ok; ++q) ok = g[q].nb_rows % nt == 0 && smx::umma_supported(g[q].K, nt);
+      if (!ok) continue;
+      for (int st : {2, 3, 4}) cand.push_back(TcCfg{nt == C ? 0 : nt, st});
+    }
+    cudaEvent_t a, b;
+    check(cudaEventCreate(&a), "cudaEventCreate");
+    check(cudaEventCreate(&b), "cudaEventCreate");
+    float best = 1e30f;
+    TcCfg bestc = tc_cfg[gid];
+    smx::UmmaGemm w[4];
+    for (const TcCfg& c : cand) {
+      std::copy(g, g + ng, w);
+      tc_apply(c, w, ng, tile_n);
+      smx::launch_umma_gemms(w, ng, status_dev, s);  // warm-up
+      check(cudaEventRecord(a, s), "cudaEventRecord");
+      for (int r = 0; r < 3; ++r) smx::launch_umma_gemms(w, ng, status_dev, s);
+      check(cudaEventRecord(b, s), "cudaEventRecord");
+      check(cudaEventSynchronize(b), "autotune");
+      float ms = 0.0f;
+      check(cudaEventElapsedTime(&ms, a, b), "cudaEventElapsedTime");
+      if (ms < best) {
+        best = ms;
+        bestc = c;
+      }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    tc_cfg[gid] = bestc;
+    tc_tuned[gid] = true;
+    tc_tuned_us[gid] = best * 1000.0f / 3.0f;
+  }
+
+  // launch one GEMM group with its tuned schedule (tuning it first if due)
+  void run_tc(int gid, smx::UmmaGemm* g, int ng, bool tile_n, cudaStream_t s) {
+    if (ng == 0) return;
+    if (autotune && !tc_tuned[gid]) {
+      cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+      check(cudaStreamIsCapturing(s, &cs), "cudaStreamIsCapturing");
+      if (cs == cudaStreamCaptureStatusNone) tc_tune(gid, g, ng, tile_n, s);
+    }
+    tc_apply(tc_cfg[gid], g, ng, tile_n);
+    smx::launch_umma_gemms(g, ng, status_dev, s);
+  }
+
   // SMX_ERR_TIMEOUT if a bounded device wait gave up since the last check (call after
   // synchronising the work in question); clears the word.
   int take_status() {
@@ -331,10 +402,10 @@ struct smx_engine {
     mark(1, s);
     if (tc_H1) {  // H1 = M0 @ H1W[L]  (mace.cpp:397-423), tensor cores
       // (layer0_fwd wrote M0 as split bf16 rows into M0_bf)
-      const smx::UmmaGemm g{M0_bf, static_cast<long>(N) * dm.nLM, T * C, W_H1, 2 * C, C,
-                            smx::UmmaOut{H1, static_cast<long>(N) * dm.nLM, dm.nLM, static_cast<long>(dm.nLM) * C, 0,
-                                         C, 1}};
-      smx::launch_umma_gemms(&g, 1, status_dev, s);
+      smx::UmmaGemm g{M0_bf, static_cast<long>(N) * dm.nLM, T * C, W_H1, 2 * C, C,
+                       smx::UmmaOut{H1, static_cast<long>(N) * dm.nLM, dm.nLM, static_cast<long>(dm.nLM) * C, 0, C,
+                                    1}};
+      run_tc(0, &g, 1, false, s);
     } else {  // H1 = M0 @ H1W[L]  (mace.cpp:397-423)
       smx::GemmBatch b{};
       for (int L = 0; L <= dm.L_max; ++L)
@@ -356,7 +427,7 @@ struct smx_engine {
           g[ng++] = smx::UmmaGemm{Phi1_bf + static_cast<size_t>(T) * N * dm.lme_off[l] * C, rows, T * K, W_A1[l], C,
                                   C, smx::UmmaOut{A1, rows, 2 * l + 1, 16L * C, l * l * C, C, 0}};
         }
-      if (ng) smx::launch_umma_gemms(g, ng, status_dev, s);
+      run_tc(1, g, ng, true, s);
       smx::GemmBatch b{};
       for (int l = 0; l < 4; ++l)
         if (dm.num_e[l] > 0 && !tc_A1[l])
@@ -381,7 +452,7 @@ struct smx_engine {
                                   smx::UmmaOut{Phi1_adj, rows, 2 * l + 1, static_cast<long>(dm.n_lme) * C,
                                                dm.lme_off[l] * C, dm.num_e[l] * C, 0}};
         }
-      if (ng) smx::launch_umma_gemms(g, ng, status_dev, s);
+      run_tc(2, g, ng, true, s);
       smx::GemmBatch b{};
       for (int l = 0; l < 4; ++l)
         if (dm.num_e[l] > 0 && !tc_Phi1adj[l])
@@ -394,10 +465,10 @@ struct smx_engine {
     mark(7, s);
     if (tc_H1) {  // M0_adj = H1_adj @ H1W[L]^T  (mace.cpp:425-451), tensor cores
       smx::launch_rows_to_bf16(H1_adj, H1adj_bf, static_cast<long>(N) * dm.nLM, C, 1, C, 0, 0, T, s);
-      const smx::UmmaGemm g{H1adj_bf, static_cast<long>(N) * dm.nLM, T * C, W_M0adj, 2 * C, C,
-                            smx::UmmaOut{M0_adj, static_cast<long>(N) * dm.nLM, dm.nLM,
-                                         static_cast<long>(dm.nLM) * C, 0, C, 1}};
-      smx::launch_umma_gemms(&g, 1, status_dev, s);
+      smx::UmmaGemm g{H1adj_bf, static_cast<long>(N) * dm.nLM, T * C, W_M0adj, 2 * C, C,
+                       smx::UmmaOut{M0_adj, static_cast<long>(N) * dm.nLM, dm.nLM, static_cast<long>(dm.nLM) * C, 0,
+                                    C, 1}};
+      run_tc(3, &g, 1, false, s);
     } else {  // M0_adj = H1_adj @ H1W[L]^T  (mace.cpp:425-451)
       smx::GemmBatch b{};
       for (int L = 0; L <= dm.L_max; ++L)

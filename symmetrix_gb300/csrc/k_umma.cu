@@ -38,14 +38,14 @@ __device__ __forceinline__ void record_timeout(unsigned* status) {
   if (status) atomicOr(status, 1u);
 }
 
-constexpr int kStages = 4;     // shared-memory ring depth (k-blocks in flight)
+constexpr int kStages = 4;     // maximum shared-memory ring depth (k-blocks in flight)
 
 // Up to four independent GEMMs in one launch (blockIdx.z selects the segment; the
 // blocks beyond a segment's tile counts return at once).
 struct UmmaSegDev {
   CUtensorMap ta, tb;
   UmmaOut o;
-  int K, NT, tiles_m, tiles_n;
+  int K, NT, tiles_m, tiles_n, stages;
 };
 struct UmmaGroupDev {
   UmmaSegDev s[4];
@@ -59,11 +59,11 @@ __global__ void __launch_bounds__(128, 1) k_umma_gemm(const __grid_constant__ Um
   const UmmaOut& o = seg.o;
   const int K = seg.K, NT = seg.NT;
   extern __shared__ uint8_t smem_raw[];
-  __shared__ uint64_t full[kStages], empty[kStages], bar_mma;
+  __shared__ uint64_t full[kStages], empty[kStages], bar_mma;  // kStages >= seg.stages
   __shared__ uint32_t tmem_base;
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const int KB = K / kBoxK;
-  const int S = KB < kStages ? KB : kStages;
+  const int S = KB < seg.stages ? KB : seg.stages;
   const uint32_t a_bytes = kTileM * kBoxK * 2, b_bytes = static_cast<uint32_t>(NT) * kBoxK * 2;
   const uint32_t stage_bytes = a_bytes + b_bytes;  // stage = A box then B box (both 1024-B multiples)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -237,8 +237,8 @@ CUtensorMap make_map(const void* base, long rows, int K, int box_rows) {
 
 }  // namespace
 
-size_t umma_smem_bytes(int K, int NT) {
-  const int stages = std::min(K / kBoxK, kStages);
+size_t umma_smem_bytes(int K, int NT, int stages) {
+  stages = std::min(K / kBoxK, std::min(stages, kStages));
   return static_cast<size_t>(stages) * (kTileM + NT) * kBoxK * 2 + 1024;
 }
 
@@ -246,7 +246,7 @@ size_t umma_smem_bytes(int K, int NT) {
 constexpr size_t kMaxDynSmem = 226 * 1024;
 
 bool umma_supported(int K, int NT) {
-  return K % kBoxK == 0 && NT % 32 == 0 && NT >= 32 && NT <= 256 && umma_smem_bytes(K, NT) <= kMaxDynSmem;
+  return K % kBoxK == 0 && NT % 32 == 0 && NT >= 32 && NT <= 256 && umma_smem_bytes(K, NT, kStages) <= kMaxDynSmem;
 }
 
 cudaError_t init_umma_kernels() {
@@ -274,9 +274,10 @@ void launch_umma_gemms(const UmmaGemm* g, int n, unsigned* status, cudaStream_t 
     d.NT = a.NT;
     d.tiles_m = static_cast<int>((a.rows + kTileM - 1) / kTileM);
     d.tiles_n = a.nb_rows / a.NT;
+    d.stages = a.stages >= 1 && a.stages <= kStages ? a.stages : kStages;
     gx = std::max(gx, static_cast<unsigned>(d.tiles_m));
     gy = std::max(gy, static_cast<unsigned>(d.tiles_n));
-    smem = std::max(smem, umma_smem_bytes(a.K, a.NT));
+    smem = std::max(smem, umma_smem_bytes(a.K, a.NT, d.stages));
   }
   if (used == 0) return;
   k_umma_gemm<<<dim3(gx, gy, used), 128, smem, s>>>(grp, status);

@@ -61,7 +61,7 @@ struct UmmaOut {
   int select;
 };
 cudaError_t init_umma_kernels();
-size_t umma_smem_bytes(int K, int NT);
+size_t umma_smem_bytes(int K, int NT, int stages);
 bool umma_supported(int K, int NT);
 // One GEMM: X [rows][K] bf16, B [nb_rows][K] bf16 (N-tiles of NT rows), output map o.
 struct UmmaGemm {
@@ -71,6 +71,7 @@ struct UmmaGemm {
   const __nv_bfloat16* B;
   int nb_rows, NT;
   UmmaOut o;
+  int stages = 4;  // shared-memory ring depth, 1..4
 };
 // 1 to 4 GEMMs in one launch.
 void launch_umma_gemms(const UmmaGemm* g, int n, unsigned* status, cudaStream_t s);

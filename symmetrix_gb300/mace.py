@@ -143,6 +143,14 @@ class MACE:
     def set_option(self, key, value):
         _lib.raise_for(self._lib.smx_set_option(self._h, key.encode(), int(value)), self._lib)
 
+    def get_option(self, key):
+        return self._lib.smx_get_option(self._h, key.encode())
+
+    def gemm_schedule(self):
+        """The tensor-core GEMM schedule the autotuner picked (BF16 form)."""
+        return {g: {"NT": self.get_option(f"tc_nt_{g}"), "stages": self.get_option(f"tc_stages_{g}"),
+                    "us": self.get_option(f"tc_tuned_ns_{g}") / 1e3} for g in ("H1", "A1", "Phi1_adj", "M0_adj")}
+
     def stage_times(self):
         """Per-stage device times (ms) of the last evaluation; needs set_option('profile', 1)."""
         out = np.zeros(16)

@@ -365,6 +365,18 @@ def time_md(eng, pos, species, masses, L, vel, args, dist, estream):
     return T, t_wall, clk, md_check
 
 
+ATOM_KERNELS = ("layer0_fwd", "contract0_rev", "layer0_rev", "layer1_fwd", "layer1_rev", "node_tail")
+
+
+def schedule_of(eng):
+    """The autotuned schedule the engine ran with: per-atom kernels on persistent grids, GEMM tiles."""
+    mask = eng.get_option("persistent")
+    out = {"persistent_kernels": [k for b, k in enumerate(ATOM_KERNELS) if mask >> b & 1]}
+    if eng.precision == "bfloat16":
+        out["gemm"] = eng.gemm_schedule()
+    return out
+
+
 def stage_profile(eng, N, E, species, nl, n_prof, dev):
     """Per-stage device times (engine CUDA events) over n_prof evaluations, L2 flushed."""
     import torch
@@ -438,7 +450,7 @@ def gpu_arm(args, rank, world, local_rank):
         T, t_wall, clk, md_check = time_md(eng, pos, species, masses, L, vel, args, dist, estream)
         avg, eval_ms = stage_profile(eng, N, E, species, nl, n_prof, dev)
         forms[form] = {"eng": eng, "T": T, "t_wall": t_wall, "clk": clk, "md_check": md_check, "stages": avg,
-                       "eval_ms": eval_ms, "value": world * N * args.steps / T}
+                       "eval_ms": eval_ms, "value": world * N * args.steps / T, "schedule": schedule_of(eng)}
     head = forms["bf16"]
     eng = head["eng"]
 
@@ -535,9 +547,10 @@ def gpu_arm(args, rank, world, local_rank):
                    "replicas_per_gpu": 1},
         "forms": {
             "bf16": {"value": head["value"], "ms_per_step": head["T"] / args.steps * 1e3, "errors": head["errors"],
-                     "ms_per_eval": head["eval_ms"]},
+                     "ms_per_eval": head["eval_ms"], "schedule": head["schedule"]},
             "fp32": {"value": fp["value"], "ms_per_step": fp["T"] / args.steps * 1e3, "errors": fp["errors"],
-                     "ms_per_eval": fp["eval_ms"], "md_check": fp["md_check"], "clocks": fp["clk"]},
+                     "ms_per_eval": fp["eval_ms"], "md_check": fp["md_check"], "clocks": fp["clk"],
+                     "schedule": fp["schedule"]},
             "bf16_over_fp32": head["value"] / fp["value"],
         },
         "roofline": roofline,
@@ -615,7 +628,8 @@ def molecules_arm(args):
         e1.record(estream)
         md.sync()
         T = e0.elapsed_time(e1) / 1e3
-        out[form] = {"value": N * args.steps / T, "ms_per_step": T / args.steps * 1e3, "edges": md.num_edges}
+        out[form] = {"value": N * args.steps / T, "ms_per_step": T / args.steps * 1e3, "edges": md.num_edges,
+                     "schedule": schedule_of(eng)}
         del md, eng
     print(json.dumps({
         "metric": METRIC, "value": out["bf16"]["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,

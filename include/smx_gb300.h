@@ -105,15 +105,21 @@ int smx_compute_node_energies_forces_device(smx_engine* eng, int num_nodes, cons
 long smx_get_stage(smx_engine* eng, const char* name, double* out, long cap);
 
 /* Options: "keep_stages" (keep A0_adj for smx_get_stage), "profile" (record CUDA
- * events between the kernels of every evaluation); BF16 form: "tc_terms" (1, 2 or 3
- * bf16 split terms of the GEMM operands, default 3; set before the first evaluation),
- * "autotune" (1, the default: the first evaluation outside a stream capture times the
- * candidate N-tile widths and TMA ring depths of each tensor-core GEMM group on its own
- * operands and keeps the fastest; setting it again re-tunes; 0 keeps the defaults).
+ * events between the kernels of every evaluation); "autotune" (1, the default: the
+ * first evaluation outside a stream capture picks, per per-atom kernel, one block per
+ * atom or a persistent grid of resident blocks claiming atoms from a counter, by timing
+ * whole passes in both, and in the BF16 form times the candidate N-tile widths and TMA
+ * ring depths of each tensor-core GEMM group on its own operands; setting it again
+ * re-tunes; 0 keeps the defaults: one block per atom, default GEMM schedule);
+ * "persistent" (-1: tuned as above, 0: one block per atom, 1: persistent grids);
+ * BF16 form: "tc_terms" (1, 2 or 3 bf16 split terms of the GEMM operands, default 3;
+ * set before the first evaluation).
  * No counterpart in the reference (its MACE object has no options). */
 int smx_set_option(smx_engine* eng, const char* key, long value);
 /* Read an option or a tuned schedule entry ("tc_nt_<G>", "tc_stages_<G>",
- * "tc_tuned_ns_<G>" for G in H1, A1, Phi1_adj, M0_adj); -1 if unknown. */
+ * "tc_tuned_ns_<G>" for G in H1, A1, Phi1_adj, M0_adj; "persistent": bit k set when
+ * per-atom kernel k (layer0_fwd, contract0_rev, layer0_rev, layer1_fwd, layer1_rev,
+ * node_tail) runs as a persistent grid); -1 if unknown. */
 long smx_get_option(const smx_engine* eng, const char* key);
 
 /* The engine's own CUDA stream (a cudaStream_t): host-pointer calls and the MD driver

@@ -65,7 +65,66 @@ struct DevModel {
   __nv_bfloat16* op_phi1;
   __nv_bfloat16* op_a1adj;
   int tc_terms;
+  // Centre-atom schedule of the per-atom kernels (AtomCursor): pgrid[k] > 0 runs kernel k
+  // as a persistent grid of that many blocks claiming atoms from the counter pair
+  // sched[0..1]; 0 launches one block per atom.  pgrid is read on the host only.
+  int* sched;
+  int pgrid[8];
 };
+
+// Per-atom kernels, indices into DevModel::pgrid.
+enum AtomKernel { kAkLayer0Fwd = 0, kAkContract0Rev, kAkLayer0Rev, kAkLayer1Fwd, kAkLayer1Rev, kAkNodeTail,
+                  kAkCount };
+
+// The centre atoms a block of a per-atom kernel works on.  Without a counter (one block
+// per atom) the block takes atom blockIdx.x.  With one (a persistent grid sized to the
+// resident blocks) blocks claim atoms in order from sched[0]; thread 0 claims the next
+// atom while the block works on the current one, so the atomic's latency is hidden.  The
+// last block to finish resets the counters for the next launch on the stream, which
+// keeps the launch self-contained (graph replays need no memset).
+struct AtomCursor {
+  int* sched;
+  int n;
+  int ahead;  // thread 0: the atom claimed for after the current one
+  __device__ __forceinline__ int first() {
+    if (!sched) return blockIdx.x;
+    __shared__ int slot;
+    if (threadIdx.x == 0) {
+      slot = atomicAdd(sched, 1);
+      ahead = atomicAdd(sched, 1);
+    }
+    __syncthreads();
+    return slot;
+  }
+  // call from uniform control flow after the block is done with the current atom
+  __device__ __forceinline__ int next() {
+    if (!sched) return n;
+    __shared__ int slot;
+    __syncthreads();  // every thread has finished the current atom (and read slot)
+    if (threadIdx.x == 0) {
+      slot = ahead;
+      ahead = ahead < n ? atomicAdd(sched, 1) : ahead;
+    }
+    __syncthreads();
+    return slot;
+  }
+  __device__ __forceinline__ void done() const {
+    if (!sched || threadIdx.x != 0) return;
+    __threadfence();
+    if (atomicAdd(sched + 1, 1) == static_cast<int>(gridDim.x) - 1) {
+      sched[0] = 0;
+      sched[1] = 0;
+    }
+  }
+};
+
+// Host side: the kernel's model copy and grid for n atoms under the current schedule.
+inline int atom_grid(const DevModel& m, int k, int n, DevModel& mk) {
+  mk = m;
+  if (m.sched && m.pgrid[k] > 0) return m.pgrid[k] < n ? m.pgrid[k] : n;
+  mk.sched = nullptr;
+  return n;
+}
 
 // Element `col` of a GEMM operand row of width K as bf16 split terms: (hi), (hi | hi)
 // or (hi | lo | hi) for 1, 2, 3 terms, hi = bf16(v), lo = bf16(v - hi); the B operand

@@ -124,9 +124,18 @@ int smx_set_option(smx_engine* eng, const char* key, long value) {
     eng->profile = value != 0;
     return SMX_OK;
   }
-  if (std::strcmp(key, "autotune") == 0) {  // precision form: (re)tune the GEMM schedule on the next evaluation
+  if (std::strcmp(key, "autotune") == 0) {  // (re)tune the GEMM and atom schedules on the next evaluation
     eng->autotune = value != 0;
     for (bool& t : eng->tc_tuned) t = false;
+    eng->sched_tuned = false;
+    if (!eng->autotune && eng->sched_force < 0) eng->sched_set(0);
+    return SMX_OK;
+  }
+  if (std::strcmp(key, "persistent") == 0) {  // atom schedule: -1 tuned, 0 one block per atom, 1 persistent
+    if (value < -1 || value > 1) return fail(SMX_ERR_INVALID, "persistent must be -1, 0 or 1");
+    eng->sched_force = static_cast<int>(value);
+    eng->sched_tuned = false;
+    eng->sched_set(value == 1 ? 1 : 0);
     return SMX_OK;
   }
   if (std::strcmp(key, "tc_terms") == 0) {  // precision form: bf16 split terms of the GEMMs
@@ -155,6 +164,7 @@ long smx_get_option(const smx_engine* eng, const char* key) {
   if (k == "precision") return eng->precision;
   if (k == "tc_terms") return eng->tc_terms;
   if (k == "autotune") return eng->autotune;
+  if (k == "persistent") return eng->sched_mask();  // bit k: per-atom kernel k runs persistent
   static const char* groups[4] = {"H1", "A1", "Phi1_adj", "M0_adj"};
   for (int q = 0; q < 4; ++q) {
     if (k == std::string("tc_nt_") + groups[q]) return eng->tc_cfg[q].NT ? eng->tc_cfg[q].NT : eng->dm.C;

@@ -191,6 +191,22 @@ struct smx_engine {
       m.dens_s[layer] = m.dens_c[layer] = nullptr;
     }
     check(smx::init_edge_kernels(dm), "cudaFuncSetAttribute");
+    {  // persistent grids of the per-atom kernels: resident blocks per SM x SMs
+      int* sc = dalloc<int>(2);
+      model_mem.push_back(sc);
+      check(cudaMemset(sc, 0, 2 * sizeof(int)), "cudaMemset");
+      m.sched = sc;
+      int nsm = 0, per_sm[smx::kAkCount] = {};
+      check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device), "cudaDeviceGetAttribute");
+      smx::layer0_residency(m, per_sm);
+      smx::layer1_residency(m, per_sm);
+      smx::node_tail_residency(m, per_sm);
+      check(cudaGetLastError(), "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+      for (int k = 0; k < smx::kAkCount; ++k) {
+        pfull[k] = per_sm[k] * nsm;
+        m.pgrid[k] = sched_force == 1 ? pfull[k] : 0;
+      }
+    }
     if (precision == SMX_PRECISION_BF16) {
       check(smx::init_umma_kernels(), "cudaFuncSetAttribute");
       const int C = pm.C;
@@ -377,6 +393,56 @@ struct smx_engine {
     smx::launch_umma_gemms(g, ng, status_dev, s);
   }
 
+  // ---- centre-atom schedule of the per-atom kernels and its autotuner ----
+  // Each per-atom kernel runs either one block per atom or as a persistent grid (its
+  // resident blocks on every SM) claiming atoms from a counter (smx::AtomCursor).  The
+  // first evaluation outside a stream capture times whole passes in both schedules
+  // (alternating, two passes each, per-stage CUDA events) and keeps the faster per
+  // kernel; the two layer-0 adjoint kernels share one stage and are switched together.
+  int pfull[smx::kAkCount] = {};
+  int sched_force = -1;  // -1: tune; 0: one block per atom; 1: persistent
+  bool sched_tuned = false;
+  float sched_stage_us[2][kStages] = {};
+
+  void sched_set(int mode) {
+    for (int k = 0; k < smx::kAkCount; ++k) dm.pgrid[k] = mode ? pfull[k] : 0;
+  }
+
+  void tune_sched(const smx::EdgeIn& in, double* out_e, double* out_f, cudaStream_t s) {
+    static constexpr int kStageOf[smx::kAkCount] = {0, 8, 8, 2, 6, 4};  // stage index of each kernel
+    const bool prof = profile;
+    profile = true;
+    float best[2][kStages];
+    for (auto& b : best)
+      for (float& v : b) v = 1e30f;
+    for (int rep = 0; rep < 2; ++rep)
+      for (int mode = 0; mode < 2; ++mode) {
+        sched_set(mode);
+        run_pass(in, out_e, out_f, s);
+        check(cudaEventSynchronize(ev[kStages]), "autotune");
+        for (int q = 0; q < kStages; ++q) {
+          float ms = 0.0f;
+          check(cudaEventElapsedTime(&ms, ev[q], ev[q + 1]), "cudaEventElapsedTime");
+          best[mode][q] = std::min(best[mode][q], ms);
+        }
+      }
+    for (int k = 0; k < smx::kAkCount; ++k) {
+      const int q = kStageOf[k];
+      dm.pgrid[k] = best[1][q] < best[0][q] ? pfull[k] : 0;
+    }
+    for (int mode = 0; mode < 2; ++mode)
+      for (int q = 0; q < kStages; ++q) sched_stage_us[mode][q] = best[mode][q] * 1000.0f;
+    profile = prof;
+    sched_tuned = true;
+  }
+
+  long sched_mask() const {
+    long mask = 0;
+    for (int k = 0; k < smx::kAkCount; ++k)
+      if (dm.pgrid[k] > 0) mask |= 1L << k;
+    return mask;
+  }
+
   // SMX_ERR_TIMEOUT if a bounded device wait gave up since the last check (call after
   // synchronising the work in question); clears the word.
   int take_status() {
@@ -387,8 +453,18 @@ struct smx_engine {
     return SMX_ERR_TIMEOUT;
   }
 
-  // The full forward + adjoint pass on device-resident inputs.
+  // The full forward + adjoint pass on device-resident inputs (tuning the atom schedule
+  // first when due).
   void run(const smx::EdgeIn& in, double* out_e, double* out_f, cudaStream_t s) {
+    if (autotune && sched_force < 0 && !sched_tuned && in.N > 0) {
+      cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+      check(cudaStreamIsCapturing(s, &cs), "cudaStreamIsCapturing");
+      if (cs == cudaStreamCaptureStatusNone) tune_sched(in, out_e, out_f, s);
+    }
+    run_pass(in, out_e, out_f, s);
+  }
+
+  void run_pass(const smx::EdgeIn& in, double* out_e, double* out_f, cudaStream_t s) {
     const int N = in.N;
     const int C = dm.C;
     const int T = tc_terms;

@@ -92,11 +92,11 @@ __device__ __forceinline__ void stage_l0(const DevModel& m, const EdgeIn& in, in
 // Layer 0 forward: A0[i,lm,k] = sum_j Y_lm(x_ij) R0'_{ti,tj,l}(r_ij)[k] with the
 // folded ordered-pair splines, then M0[i,LM,k] = P_{ti,LM,k}(A0[i,:,k]).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_layer0_fwd(DevModel m, EdgeIn in, float* __restrict__ A0,
-                                                    float* __restrict__ M0, float* __restrict__ zbl_e) {
+__device__ __forceinline__ void layer0_fwd_atom(const DevModel& m, const EdgeIn& in, float* __restrict__ A0,
+                                                float* __restrict__ M0, float* __restrict__ zbl_e, int i) {
   extern __shared__ float dyn[];  // [17][C]: A0 columns (+ constant one) for the contraction
   __shared__ L0Stage<false> st;
-  const int C = m.C, C2 = C >> 1, BW = (C2 + 31) & ~31, i = blockIdx.x;
+  const int C = m.C, C2 = C >> 1, BW = (C2 + 31) & ~31;
   // two groups of channel-pair threads, each taking every other active edge
   const int half = static_cast<int>(threadIdx.x) >= BW ? 1 : 0;
   const int lt = threadIdx.x - half * BW;
@@ -201,17 +201,25 @@ __global__ void __launch_bounds__(256) k_layer0_fwd(DevModel m, EdgeIn in, float
   }
 }
 
+template <bool P>
+__global__ void __launch_bounds__(256) k_layer0_fwd(DevModel m, EdgeIn in, float* __restrict__ A0,
+                                                    float* __restrict__ M0, float* __restrict__ zbl_e) {
+  AtomCursor cur{P ? m.sched : nullptr, in.N, 0};
+  for (int i = cur.first(); i < in.N; i = cur.next()) layer0_fwd_atom(m, in, A0, M0, zbl_e, i);
+  cur.done();
+}
+
 // ---------------------------------------------------------------------------
 // Layer-0 contraction adjoint (mace.cpp:372-395):
 //   A0_adj[i,:,k] = sum_LM M0_adj[i,LM,k] grad P_{ti,LM,k}(A0[i,:,k]).
 // Its own kernel, so its register-heavy generated code does not limit the occupancy
 // of the layer-0 edge adjoint.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_contract0_rev(DevModel m, const int* __restrict__ node_type,
-                                                       const float* __restrict__ A0, const float* __restrict__ M0_adj,
-                                                       float* __restrict__ A0_adj) {
+__device__ __forceinline__ void contract0_rev_atom(const DevModel& m, const int* __restrict__ node_type,
+                                                   const float* __restrict__ A0, const float* __restrict__ M0_adj,
+                                                   float* __restrict__ A0_adj, int i) {
   extern __shared__ float dyn[];
-  const int C = m.C, k = threadIdx.x, i = blockIdx.x;
+  const int C = m.C, k = threadIdx.x;
   const int ti = node_type[i];
   float dA[16];
   if (m.poly_canon) {  // dA0 = sum_LM dM0[LM] grad P_LM, generated code, registers only
@@ -269,6 +277,15 @@ __global__ void __launch_bounds__(256) k_contract0_rev(DevModel m, const int* __
   for (int q = 0; q < 16; ++q) A0_adj[(static_cast<size_t>(i) * 16 + q) * C + k] = dA[q];
 }
 
+template <bool P>
+__global__ void __launch_bounds__(256) k_contract0_rev(DevModel m, const int* __restrict__ node_type,
+                                                       const float* __restrict__ A0, const float* __restrict__ M0_adj,
+                                                       float* __restrict__ A0_adj, int N) {
+  AtomCursor cur{P ? m.sched : nullptr, N, 0};
+  for (int i = cur.first(); i < N; i = cur.next()) contract0_rev_atom(m, node_type, A0, M0_adj, A0_adj, i);
+  cur.done();
+}
+
 
 
 // ---------------------------------------------------------------------------
@@ -277,11 +294,11 @@ __global__ void __launch_bounds__(256) k_contract0_rev(DevModel m, const int* __
 // -(layer 0 + layer 1).  The next active edge's four spline cubics are loaded while
 // this edge computes.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_layer0_rev(DevModel m, EdgeIn in, const float* __restrict__ A0_adj,
-                                                    const double* __restrict__ f1, double* __restrict__ forces) {
+__device__ __forceinline__ void layer0_rev_atom(const DevModel& m, const EdgeIn& in, const float* __restrict__ A0_adj,
+                                                const double* __restrict__ f1, double* __restrict__ forces, int i) {
   __shared__ L0Stage<true> st;
   __shared__ float sF[kEdgeChunk][8][3];
-  const int C = m.C, C2 = C >> 1, i = blockIdx.x;
+  const int C = m.C, C2 = C >> 1;
   const bool live = static_cast<int>(threadIdx.x) < C2;
   const int cp = live ? threadIdx.x : 0, kc = 2 * cp;  // this thread's channel pair
   const int nwarp = blockDim.x >> 5;
@@ -361,6 +378,14 @@ __global__ void __launch_bounds__(128) k_layer0_rev(DevModel m, EdgeIn in, const
   }
 }
 
+template <bool P>
+__global__ void __launch_bounds__(128) k_layer0_rev(DevModel m, EdgeIn in, const float* __restrict__ A0_adj,
+                                                    const double* __restrict__ f1, double* __restrict__ forces) {
+  AtomCursor cur{P ? m.sched : nullptr, in.N, 0};
+  for (int i = cur.first(); i < in.N; i = cur.next()) layer0_rev_atom(m, in, A0_adj, f1, forces, i);
+  cur.done();
+}
+
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
@@ -374,14 +399,38 @@ int layer0_block(int C) { return ((C >> 1) + 31) & ~31; }
 void launch_layer0_fwd(const DevModel& m, const EdgeIn& in, float* A0, float* M0, float* zbl_e, cudaStream_t s) {
   if (in.N <= 0) return;
   const size_t smem = 17 * sizeof(float) * m.C;
-  k_layer0_fwd<<<in.N, 2 * layer0_block(m.C), smem, s>>>(m, in, A0, M0, zbl_e);
+  DevModel mk;
+  const int grid = atom_grid(m, kAkLayer0Fwd, in.N, mk);
+  if (mk.sched)
+    k_layer0_fwd<true><<<grid, 2 * layer0_block(m.C), smem, s>>>(mk, in, A0, M0, zbl_e);
+  else
+    k_layer0_fwd<false><<<grid, 2 * layer0_block(m.C), smem, s>>>(mk, in, A0, M0, zbl_e);
 }
 
 void launch_layer0_rev(const DevModel& m, const EdgeIn& in, const float* A0, const float* M0_adj, const double* f1,
                        float* A0_adj, double* forces, cudaStream_t s) {
   if (in.N <= 0) return;
-  k_contract0_rev<<<in.N, m.C, m.poly_canon ? 0 : 34 * sizeof(float) * m.C, s>>>(m, in.node_type, A0, M0_adj, A0_adj);
-  k_layer0_rev<<<in.N, layer0_block(m.C), 0, s>>>(m, in, A0_adj, f1, forces);
+  DevModel mk;
+  int grid = atom_grid(m, kAkContract0Rev, in.N, mk);
+  const size_t smem = m.poly_canon ? 0 : 34 * sizeof(float) * m.C;
+  if (mk.sched)
+    k_contract0_rev<true><<<grid, m.C, smem, s>>>(mk, in.node_type, A0, M0_adj, A0_adj, in.N);
+  else
+    k_contract0_rev<false><<<grid, m.C, smem, s>>>(mk, in.node_type, A0, M0_adj, A0_adj, in.N);
+  grid = atom_grid(m, kAkLayer0Rev, in.N, mk);
+  if (mk.sched)
+    k_layer0_rev<true><<<grid, layer0_block(m.C), 0, s>>>(mk, in, A0_adj, f1, forces);
+  else
+    k_layer0_rev<false><<<grid, layer0_block(m.C), 0, s>>>(mk, in, A0_adj, f1, forces);
+}
+
+// resident blocks per SM of the persistent layer-0 kernels at this model's launch shapes
+void layer0_residency(const DevModel& m, int* per_sm) {
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[kAkLayer0Fwd], k_layer0_fwd<true>, 2 * layer0_block(m.C),
+                                                17 * sizeof(float) * m.C);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[kAkContract0Rev], k_contract0_rev<true>, m.C,
+                                                m.poly_canon ? 0 : 34 * sizeof(float) * m.C);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[kAkLayer0Rev], k_layer0_rev<true>, layer0_block(m.C), 0);
 }
 
 }  // namespace smx

@@ -286,15 +286,15 @@ __device__ __forceinline__ Lane2 lane2(const int C, int& half) {
 // registers, four blocks of 128 threads per SM) rather than for the packed FMAs.
 // ---------------------------------------------------------------------------
 template <int LMAX, int CT>
-__global__ void __launch_bounds__(256) k_layer1_fwd(DevModel m, EdgeIn in, const float* __restrict__ H1,
-                                                    float* __restrict__ Phi1) {
+__device__ __forceinline__ void layer1_fwd_atom(const DevModel& m, const EdgeIn& in, const float* __restrict__ H1,
+                                                float* __restrict__ Phi1, int i) {
   constexpr int NL2 = (LMAX + 1) * (LMAX + 1);
   constexpr int NI = ins_count(LMAX);
   constexpr int NP = ins_np(LMAX);
   extern __shared__ float dyn[];
   __shared__ L1Stage<false> st;
   const int C = CT > 0 ? CT : m.C;
-  const int k = threadIdx.x, i = blockIdx.x;
+  const int k = threadIdx.x;
   const int ti = in.node_type[i];
   const int e0 = in.first[i], e1 = in.first[i + 1];
   float acc[NP];
@@ -358,21 +358,29 @@ __global__ void __launch_bounds__(256) k_layer1_fwd(DevModel m, EdgeIn in, const
   }
 }
 
+template <int LMAX, int CT, bool P>
+__global__ void __launch_bounds__(256) k_layer1_fwd(DevModel m, EdgeIn in, const float* __restrict__ H1,
+                                                    float* __restrict__ Phi1) {
+  AtomCursor cur{P ? m.sched : nullptr, in.N, 0};
+  for (int i = cur.first(); i < in.N; i = cur.next()) layer1_fwd_atom<LMAX, CT>(m, in, H1, Phi1, i);
+  cur.done();
+}
+
 // ---------------------------------------------------------------------------
 // Layer 1 adjoint.  g (this thread's half of the CG-contracted dPhi1 paths, channel
 // pair) stays in registers across the node's edges; f1[e] receives dE/dx_ij.
 // ---------------------------------------------------------------------------
 template <int LMAX, int CT>
-__global__ void __launch_bounds__(256) k_layer1_rev(DevModel m, EdgeIn in, const float* __restrict__ H1,
-                                                    const float* __restrict__ dPhi1, float* __restrict__ H1_adj,
-                                                    double* __restrict__ f1) {
+__device__ __forceinline__ void layer1_rev_atom(const DevModel& m, const EdgeIn& in, const float* __restrict__ H1,
+                                                const float* __restrict__ dPhi1, float* __restrict__ H1_adj,
+                                                double* __restrict__ f1, int i) {
   static_assert(LMAX == 1, "instruction halves are tabulated for L_max = 1");
   constexpr int NP = ins_np(LMAX);
   constexpr int NG = half_np<LMAX, 0>() > half_np<LMAX, 1>() ? half_np<LMAX, 0>() : half_np<LMAX, 1>();
   extern __shared__ float dyn[];
   __shared__ L1Stage<true> st;
   __shared__ float sF[kEdgeChunk][8][3];
-  const int C = CT > 0 ? CT : m.C, i = blockIdx.x;
+  const int C = CT > 0 ? CT : m.C;
   int half;
   const Lane2 L = lane2(C, half);
   const int nwarp = blockDim.x >> 5;
@@ -423,6 +431,15 @@ __global__ void __launch_bounds__(256) k_layer1_rev(DevModel m, EdgeIn in, const
       for (int c = 0; c < 3; ++c) f1[3 * e + c] = s[c];
     }
   }
+}
+
+template <int LMAX, int CT, bool P>
+__global__ void __launch_bounds__(256) k_layer1_rev(DevModel m, EdgeIn in, const float* __restrict__ H1,
+                                                    const float* __restrict__ dPhi1, float* __restrict__ H1_adj,
+                                                    double* __restrict__ f1) {
+  AtomCursor cur{P ? m.sched : nullptr, in.N, 0};
+  for (int i = cur.first(); i < in.N; i = cur.next()) layer1_rev_atom<LMAX, CT>(m, in, H1, dPhi1, H1_adj, f1, i);
+  cur.done();
 }
 
 // ===========================================================================
@@ -526,11 +543,11 @@ __device__ __forceinline__ void l2_load_g(const float* sP, int C, int k, float* 
 }  // namespace
 
 // Layer-1 forward, L_max = 2.
-__global__ void __launch_bounds__(512, 1) k_layer1_fwd_l2(DevModel m, EdgeIn in, const float* __restrict__ H1,
-                                                          float* __restrict__ Phi1) {
+__device__ __forceinline__ void layer1_fwd_l2_atom(const DevModel& m, const EdgeIn& in, const float* __restrict__ H1,
+                                                   float* __restrict__ Phi1, int i) {
   extern __shared__ float dyn[];
   __shared__ L1Stage<false> st;
-  const int C = m.C, CP = (C + 31) & ~31, i = blockIdx.x;
+  const int C = m.C, CP = (C + 31) & ~31;
   const int grp = threadIdx.x / CP, kk = threadIdx.x - grp * CP;
   const bool live = kk < C;
   const int k = live ? kk : 0;
@@ -584,6 +601,14 @@ __global__ void __launch_bounds__(512, 1) k_layer1_fwd_l2(DevModel m, EdgeIn in,
           }
         }
     }
+}
+
+template <bool P>
+__global__ void __launch_bounds__(512, 1) k_layer1_fwd_l2(DevModel m, EdgeIn in, const float* __restrict__ H1,
+                                                          float* __restrict__ Phi1) {
+  AtomCursor cur{P ? m.sched : nullptr, in.N, 0};
+  for (int i = cur.first(); i < in.N; i = cur.next()) layer1_fwd_l2_atom(m, in, H1, Phi1, i);
+  cur.done();
 }
 
 namespace {
@@ -666,14 +691,14 @@ __device__ __forceinline__ void l2_rev_chunk(const DevModel& m, const float* __r
 }  // namespace
 
 // Layer-1 adjoint, L_max = 2.
-__global__ void __launch_bounds__(512, 1) k_layer1_rev_l2(DevModel m, EdgeIn in, const float* __restrict__ H1,
-                                                          const float* __restrict__ dPhi1,
-                                                          float* __restrict__ H1_adj, double* __restrict__ f1) {
+__device__ __forceinline__ void layer1_rev_l2_atom(const DevModel& m, const EdgeIn& in, const float* __restrict__ H1,
+                                                   const float* __restrict__ dPhi1, float* __restrict__ H1_adj,
+                                                   double* __restrict__ f1, int i) {
   constexpr int NP = 243;
   extern __shared__ float dyn[];
   __shared__ L1Stage<true> st;
   __shared__ float sF[kEdgeChunk][32][3];
-  const int C = m.C, CP = (C + 31) & ~31, i = blockIdx.x;
+  const int C = m.C, CP = (C + 31) & ~31;
   const int grp = threadIdx.x / CP, kk = threadIdx.x - grp * CP;
   const bool live = kk < C;
   const int k = live ? kk : 0;
@@ -731,18 +756,36 @@ __global__ void __launch_bounds__(512, 1) k_layer1_rev_l2(DevModel m, EdgeIn in,
   }
 }
 
+template <bool P>
+__global__ void __launch_bounds__(512, 1) k_layer1_rev_l2(DevModel m, EdgeIn in, const float* __restrict__ H1,
+                                                          const float* __restrict__ dPhi1,
+                                                          float* __restrict__ H1_adj, double* __restrict__ f1) {
+  AtomCursor cur{P ? m.sched : nullptr, in.N, 0};
+  for (int i = cur.first(); i < in.N; i = cur.next()) layer1_rev_l2_atom(m, in, H1, dPhi1, H1_adj, f1, i);
+  cur.done();
+}
+
 // threads per block of the layer-1 kernels: two warp-aligned groups of C/2
 int layer1_block(int C) { return 2 * (((C >> 1) + 31) & ~31); }
 
 namespace {
 
-template <int CT>
+template <int CT, bool P>
 cudaError_t set_smem(const DevModel& m) {
-  cudaError_t e = cudaFuncSetAttribute(k_layer1_fwd<1, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaError_t e = cudaFuncSetAttribute(k_layer1_fwd<1, CT, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(sizeof(float) * ins_np(1) * m.C));
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_layer1_rev<1, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  return cudaFuncSetAttribute(k_layer1_rev<1, CT, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               static_cast<int>(sizeof(float) * (m.n_lme + ins_np(1)) * m.C));
+}
+
+template <bool P>
+cudaError_t set_smem_l2(const DevModel& m) {
+  cudaError_t e = cudaFuncSetAttribute(k_layer1_fwd_l2<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(sizeof(float) * ins_np(2) * m.C));
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_layer1_rev_l2<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              static_cast<int>(sizeof(float) * (m.n_lme + ins_np(2)) * m.C));
 }
 
 // Channel counts with a compile-time specialisation (addresses fold to immediates).
@@ -757,45 +800,86 @@ void dispatch_c(int C, F&& f) {
   }
 }
 
+// the one-block-per-atom (false) or persistent (true) instantiation
+template <typename F>
+void dispatch_p(bool persistent, F&& f) {
+  if (persistent)
+    f(std::true_type{});
+  else
+    f(std::false_type{});
+}
+
 }  // namespace
 
 cudaError_t init_layer1_kernels(const DevModel& m) {
-  if (m.L_max == 2) {
-    cudaError_t e = cudaFuncSetAttribute(k_layer1_fwd_l2, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(sizeof(float) * ins_np(2) * m.C));
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_layer1_rev_l2, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                static_cast<int>(sizeof(float) * (m.n_lme + ins_np(2)) * m.C));
-  }
   cudaError_t e = cudaSuccess;
-  dispatch_c(m.C, [&](auto ct) { e = set_smem<decltype(ct)::value>(m); });
+  for (bool p : {false, true}) {
+    if (m.L_max == 2)
+      dispatch_p(p, [&](auto pc) { e = set_smem_l2<decltype(pc)::value>(m); });
+    else
+      dispatch_c(m.C, [&](auto ct) {
+        dispatch_p(p, [&](auto pc) { e = set_smem<decltype(ct)::value, decltype(pc)::value>(m); });
+      });
+    if (e != cudaSuccess) return e;
+  }
   return e;
 }
 
 void launch_layer1_fwd(const DevModel& m, const EdgeIn& in, const float* H1, float* Phi1, cudaStream_t s) {
   if (in.N <= 0) return;
-  if (m.L_max == 2) {
-    k_layer1_fwd_l2<<<in.N, kL2Groups * ((m.C + 31) & ~31), sizeof(float) * ins_np(2) * m.C, s>>>(m, in, H1, Phi1);
-    return;
-  }
-  const size_t smem = sizeof(float) * ins_np(1) * m.C;
-  dispatch_c(m.C, [&](auto ct) {
-    k_layer1_fwd<1, decltype(ct)::value><<<in.N, m.C, smem, s>>>(m, in, H1, Phi1);
+  DevModel mk;
+  const int grid = atom_grid(m, kAkLayer1Fwd, in.N, mk);
+  dispatch_p(mk.sched != nullptr, [&](auto pc) {
+    constexpr bool P = decltype(pc)::value;
+    if (m.L_max == 2) {
+      k_layer1_fwd_l2<P><<<grid, kL2Groups * ((m.C + 31) & ~31), sizeof(float) * ins_np(2) * m.C, s>>>(mk, in, H1,
+                                                                                                     Phi1);
+      return;
+    }
+    const size_t smem = sizeof(float) * ins_np(1) * m.C;
+    dispatch_c(m.C, [&](auto ct) {
+      k_layer1_fwd<1, decltype(ct)::value, P><<<grid, m.C, smem, s>>>(mk, in, H1, Phi1);
+    });
   });
 }
 
 void launch_layer1_rev(const DevModel& m, const EdgeIn& in, const float* H1, const float* dPhi1, float* H1_adj,
                        double* f1, cudaStream_t s) {
   if (in.N <= 0) return;
-  if (m.L_max == 2) {
-    k_layer1_rev_l2<<<in.N, kL2Groups * ((m.C + 31) & ~31), sizeof(float) * (m.n_lme + ins_np(2)) * m.C, s>>>(
-        m, in, H1, dPhi1, H1_adj, f1);
-    return;
-  }
-  const size_t smem = sizeof(float) * (m.n_lme + ins_np(1)) * m.C;
-  dispatch_c(m.C, [&](auto ct) {
-    k_layer1_rev<1, decltype(ct)::value><<<in.N, layer1_block(m.C), smem, s>>>(m, in, H1, dPhi1, H1_adj, f1);
+  DevModel mk;
+  const int grid = atom_grid(m, kAkLayer1Rev, in.N, mk);
+  dispatch_p(mk.sched != nullptr, [&](auto pc) {
+    constexpr bool P = decltype(pc)::value;
+    if (m.L_max == 2) {
+      k_layer1_rev_l2<P><<<grid, kL2Groups * ((m.C + 31) & ~31), sizeof(float) * (m.n_lme + ins_np(2)) * m.C, s>>>(
+          mk, in, H1, dPhi1, H1_adj, f1);
+      return;
+    }
+    const size_t smem = sizeof(float) * (m.n_lme + ins_np(1)) * m.C;
+    dispatch_c(m.C, [&](auto ct) {
+      k_layer1_rev<1, decltype(ct)::value, P><<<grid, layer1_block(m.C), smem, s>>>(mk, in, H1, dPhi1, H1_adj, f1);
+    });
   });
+}
+
+// resident blocks per SM of the persistent layer-1 kernels at this model's launch shapes
+void layer1_residency(const DevModel& m, int* per_sm) {
+  int f = 0, r = 0;
+  if (m.L_max == 2) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f, k_layer1_fwd_l2<true>, kL2Groups * ((m.C + 31) & ~31),
+                                                  sizeof(float) * ins_np(2) * m.C);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_layer1_rev_l2<true>, kL2Groups * ((m.C + 31) & ~31),
+                                                  sizeof(float) * (m.n_lme + ins_np(2)) * m.C);
+  } else {
+    dispatch_c(m.C, [&](auto ct) {
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f, k_layer1_fwd<1, decltype(ct)::value, true>, m.C,
+                                                    sizeof(float) * ins_np(1) * m.C);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_layer1_rev<1, decltype(ct)::value, true>,
+                                                    layer1_block(m.C), sizeof(float) * (m.n_lme + ins_np(1)) * m.C);
+    });
+  }
+  per_sm[kAkLayer1Fwd] = f;
+  per_sm[kAkLayer1Rev] = r;
 }
 
 }  // namespace smx

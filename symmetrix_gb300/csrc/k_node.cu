@@ -95,14 +95,14 @@ void launch_gemm(const GemmBatch& b, cudaStream_t s) {
 //   dE/dH2 (MLP gradient), H1_adj[i,0,:] = w1 + W_H1[ti] dE/dH2 (other rows 0),
 //   M1_adj = W_M1 dE/dH2, A1_adj[i,lm,k] = dM1/dA1[lm] * M1_adj[k].
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_node_tail(DevModel m, const int* __restrict__ ntype, float* __restrict__ A1,
-                                                   const float* __restrict__ H1, float* __restrict__ M1o,
-                                                   float* __restrict__ H2o, float* __restrict__ A1_adj,
-                                                   float* __restrict__ H1_adj, float* __restrict__ M1_adj_o,
-                                                   float* __restrict__ H2_adj_o, const float* __restrict__ zbl_e,
-                                                   double* __restrict__ energies, int N) {
+__device__ __forceinline__ void node_tail_atom(const DevModel& m, const int* __restrict__ ntype, float* __restrict__ A1,
+                                               const float* __restrict__ H1, float* __restrict__ M1o,
+                                               float* __restrict__ H2o, float* __restrict__ A1_adj,
+                                               float* __restrict__ H1_adj, float* __restrict__ M1_adj_o,
+                                               float* __restrict__ H2_adj_o, const float* __restrict__ zbl_e,
+                                               double* __restrict__ energies, int N, int i) {
   extern __shared__ float dyn[];
-  const int C = m.C, k = threadIdx.x, i = blockIdx.x;
+  const int C = m.C, k = threadIdx.x;
   const int nwarp = C >> 5, lane = k & 31, warp = k >> 5;
   const int ti = ntype[i];
   const int nh = m.n_hidden;
@@ -229,12 +229,37 @@ __global__ void __launch_bounds__(256) k_node_tail(DevModel m, const int* __rest
   H2_adj_o[static_cast<size_t>(i) * C + k] = dh2;
 }
 
+template <bool P>
+__global__ void __launch_bounds__(256) k_node_tail(DevModel m, const int* __restrict__ ntype, float* __restrict__ A1,
+                                                   const float* __restrict__ H1, float* __restrict__ M1o,
+                                                   float* __restrict__ H2o, float* __restrict__ A1_adj,
+                                                   float* __restrict__ H1_adj, float* __restrict__ M1_adj_o,
+                                                   float* __restrict__ H2_adj_o, const float* __restrict__ zbl_e,
+                                                   double* __restrict__ energies, int N) {
+  AtomCursor cur{P ? m.sched : nullptr, N, 0};
+  for (int i = cur.first(); i < N; i = cur.next())
+    node_tail_atom(m, ntype, A1, H1, M1o, H2o, A1_adj, H1_adj, M1_adj_o, H2_adj_o, zbl_e, energies, N, i);
+  cur.done();
+}
+
+size_t node_tail_smem(const DevModel& m) { return sizeof(float) * (34 * m.C + 4 * m.C + 33 * 8 + 33); }
+
 void launch_node_tail(const DevModel& m, const int* node_type, int N, float* A1, const float* H1, float* M1,
                       float* H2, float* A1_adj, float* H1_adj, float* M1_adj, float* H2_adj, const float* zbl_e,
                       double* energies, cudaStream_t s) {
   if (N <= 0) return;
-  const size_t smem = sizeof(float) * (34 * m.C + 4 * m.C + 33 * 8 + 33);
-  k_node_tail<<<N, m.C, smem, s>>>(m, node_type, A1, H1, M1, H2, A1_adj, H1_adj, M1_adj, H2_adj, zbl_e, energies, N);
+  DevModel mk;
+  const int grid = atom_grid(m, kAkNodeTail, N, mk);
+  if (mk.sched)
+    k_node_tail<true><<<grid, m.C, node_tail_smem(m), s>>>(mk, node_type, A1, H1, M1, H2, A1_adj, H1_adj, M1_adj,
+                                                           H2_adj, zbl_e, energies, N);
+  else
+    k_node_tail<false><<<grid, m.C, node_tail_smem(m), s>>>(mk, node_type, A1, H1, M1, H2, A1_adj, H1_adj, M1_adj,
+                                                            H2_adj, zbl_e, energies, N);
+}
+
+void node_tail_residency(const DevModel& m, int* per_sm) {
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[kAkNodeTail], k_node_tail<true>, m.C, node_tail_smem(m));
 }
 
 // first[0] = 0, first[i+1] = first[i] + num_neigh[i]; one block, sequential tiles.

@@ -10,6 +10,11 @@ namespace smx {
 
 // k_edge.cu
 cudaError_t init_edge_kernels(const DevModel& m);
+// resident blocks per SM of each per-atom kernel (indexed by AtomKernel) at the launch
+// shapes of this model: the persistent grid is this times the SM count
+void layer0_residency(const DevModel& m, int* per_sm);
+void layer1_residency(const DevModel& m, int* per_sm);
+void node_tail_residency(const DevModel& m, int* per_sm);
 void launch_layer0_fwd(const DevModel& m, const EdgeIn& in, float* A0, float* M0, float* zbl_e, cudaStream_t s);
 void launch_layer0_rev(const DevModel& m, const EdgeIn& in, const float* A0, const float* M0_adj, const double* f1,
                        float* A0_adj, double* forces, cudaStream_t s);

@@ -274,3 +274,40 @@ def test_lmax2_wide_model(engine_lib, tmp_path):
         F = atomic_forces(96, nl["i"], nl["neigh_indices"], m.node_forces)
         assert _report(f"{precision} E_i", m.node_energies, ref.node_energies) < (E_TOL if tol == F_TOL else 5e-3)
         assert _report(f"{precision} F_atom", F, Fr) < tol
+
+
+@pytest.mark.parametrize("L_max", [1, 2])
+def test_persistent_atom_schedule(engine_lib, tmp_path, L_max):
+    """The per-atom kernels as persistent grids claiming atoms from a counter: the same
+    energies as one block per atom (bitwise: the forward pass is deterministic), forces
+    against the oracle, and the counter is reset between launches (repeat evaluations).
+    The tuned schedule is a mask over the six per-atom kernels."""
+    path = write_model(make_model(num_channels=32, species=("H", "C", "O"), r_cut=5.0, L_max=L_max, num_knots=60,
+                                  seed=5), str(tmp_path / "m.json"))
+    pos, L, species = random_box(300, 0.08, 0.9, 3, seed=12)
+    nl = neighbor_list(pos, 5.0, L)
+    ref = Evaluator(path, "port")
+    ref.compute_node_energies_forces(*edge_args(species, nl))
+    m = _engine(path)
+    m.set_option("persistent", 0)
+    m.compute_node_energies_forces(*edge_args(species, nl))
+    e_block = m.node_energies.copy()
+    assert m.get_option("persistent") == 0
+    m.set_option("persistent", 1)
+    assert m.get_option("persistent") == 63
+    for rep in range(3):
+        m.compute_node_energies_forces(*edge_args(species, nl))
+        assert np.array_equal(m.node_energies, e_block), rep
+        assert _report("f_edge", m.node_forces, ref.node_forces) < F_TOL
+    m.set_option("persistent", -1)  # tuned on the next evaluation
+    m.compute_node_energies_forces(*edge_args(species, nl))
+    assert 0 <= m.get_option("persistent") <= 63
+    assert np.array_equal(m.node_energies, e_block)
+    assert _report("f_edge", m.node_forces, ref.node_forces) < F_TOL
+    # fewer atoms than the persistent grid has blocks
+    sub = neighbor_list(pos[:7], 5.0)
+    m.set_option("persistent", 1)
+    m.compute_node_energies_forces(*edge_args(species[:7], sub))
+    ref.compute_node_energies_forces(*edge_args(species[:7], sub))
+    assert _report("E_i small", m.node_energies, ref.node_energies) < E_TOL
+    assert _report("f_edge small", m.node_forces, ref.node_forces) < F_TOL

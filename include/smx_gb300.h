@@ -112,6 +112,9 @@ long smx_get_stage(smx_engine* eng, const char* name, double* out, long cap);
  * ring depths of each tensor-core GEMM group on its own operands; setting it again
  * re-tunes; 0 keeps the defaults: one block per atom, default GEMM schedule);
  * "persistent" (-1: tuned as above, 0: one block per atom, 1: persistent grids);
+ * "species_order" (-1, the default: the edge kernels take the centre atoms sorted by
+ * species when a layer's spline table exceeds 64 MB, so the rows in use stay in L2;
+ * 0: input order; 1: always sorted; results do not depend on it);
  * BF16 form: "tc_terms" (1, 2 or 3 bf16 split terms of the GEMM operands, default 3;
  * set before the first evaluation).
  * No counterpart in the reference (its MACE object has no options). */
@@ -119,7 +122,8 @@ int smx_set_option(smx_engine* eng, const char* key, long value);
 /* Read an option or a tuned schedule entry ("tc_nt_<G>", "tc_stages_<G>",
  * "tc_tuned_ns_<G>" for G in H1, A1, Phi1_adj, M0_adj; "persistent": bit k set when
  * per-atom kernel k (layer0_fwd, contract0_rev, layer0_rev, layer1_fwd, layer1_rev,
- * node_tail) runs as a persistent grid); -1 if unknown. */
+ * node_tail) runs as a persistent grid; "species_order": 1 when the sorted order is in
+ * effect); -1 if unknown. */
 long smx_get_option(const smx_engine* eng, const char* key);
 
 /* The engine's own CUDA stream (a cudaStream_t): host-pointer calls and the MD driver

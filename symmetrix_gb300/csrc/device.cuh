@@ -181,6 +181,11 @@ struct EdgeIn {
   const double* xyz;     // [E][3]
   const double* r;       // [E]
   int N;
+  // Processing order of the centre atoms (block b works on atom order[b]); nullptr: the
+  // identity.  A species-sorted order keeps the spline rows the blocks in flight gather
+  // (the pairs of one centre species) inside L2 when the whole table is larger.
+  const int* order = nullptr;
+  __device__ __forceinline__ int atom_at(int b) const { return order ? order[b] : b; }
 };
 
 // Canonical layer-1 tensor-product instructions (l1 from Y_lm, l2 from H1),

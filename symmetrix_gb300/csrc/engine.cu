@@ -131,6 +131,11 @@ int smx_set_option(smx_engine* eng, const char* key, long value) {
     if (!eng->autotune && eng->sched_force < 0) eng->sched_set(0);
     return SMX_OK;
   }
+  if (std::strcmp(key, "species_order") == 0) {  // -1 by table size, 0 input order, 1 species-sorted
+    if (value < -1 || value > 1) return fail(SMX_ERR_INVALID, "species_order must be -1, 0 or 1");
+    eng->species_order = static_cast<int>(value);
+    return SMX_OK;
+  }
   if (std::strcmp(key, "persistent") == 0) {  // atom schedule: -1 tuned, 0 one block per atom, 1 persistent
     if (value < -1 || value > 1) return fail(SMX_ERR_INVALID, "persistent must be -1, 0 or 1");
     eng->sched_force = static_cast<int>(value);
@@ -164,7 +169,8 @@ long smx_get_option(const smx_engine* eng, const char* key) {
   if (k == "precision") return eng->precision;
   if (k == "tc_terms") return eng->tc_terms;
   if (k == "autotune") return eng->autotune;
-  if (k == "persistent") return eng->sched_mask();  // bit k: per-atom kernel k runs persistent
+  if (k == "persistent") return eng->sched_mask();
+  if (k == "species_order") return eng->order_species() ? 1 : 0;  // in effect  // bit k: per-atom kernel k runs persistent
   static const char* groups[4] = {"H1", "A1", "Phi1_adj", "M0_adj"};
   for (int q = 0; q < 4; ++q) {
     if (k == std::string("tc_nt_") + groups[q]) return eng->tc_cfg[q].NT ? eng->tc_cfg[q].NT : eng->dm.C;

@@ -83,6 +83,7 @@ struct smx_engine {
   __nv_bfloat16 *M0_bf = nullptr, *Phi1_bf = nullptr, *A1adj_bf = nullptr, *H1adj_bf = nullptr;
   float* zbl_e = nullptr;  // per-node ZBL energy
   int *first = nullptr, *ntype = nullptr, *nidx = nullptr, *ntype_e = nullptr;
+  int* atom_order = nullptr;  // centre atoms sorted by species (when species_order is on)
   double *xyz = nullptr, *r = nullptr, *energies = nullptr, *forces = nullptr;
   int lastN = 0;
 
@@ -231,7 +232,8 @@ struct smx_engine {
 
   void free_workspace() {
     void* ps[] = {A0, M0, H1, Phi1, A1, M1, H2, A0_adj, M0_adj, H1_adj, Phi1_adj, A1_adj, M1_adj, H2_adj, f1,
-                  first, ntype, nidx, ntype_e, xyz, r, energies, forces, M0_bf, Phi1_bf, A1adj_bf, H1adj_bf};
+                  first, ntype, nidx, ntype_e, xyz, r, energies, forces, M0_bf, Phi1_bf, A1adj_bf, H1adj_bf,
+                  atom_order};
     for (void* p : ps)
       if (p) cudaFree(p);
     A0 = M0 = H1 = Phi1 = A1 = M1 = H2 = A0_adj = M0_adj = H1_adj = Phi1_adj = A1_adj = M1_adj = H2_adj = nullptr;
@@ -245,7 +247,7 @@ struct smx_engine {
     f1 = nullptr;
     if (zbl_e) cudaFree(zbl_e);
     zbl_e = nullptr;
-    first = ntype = nidx = ntype_e = nullptr;
+    first = ntype = nidx = ntype_e = atom_order = nullptr;
     xyz = r = energies = forces = nullptr;
     capN = capE = 0;
   }
@@ -279,6 +281,7 @@ struct smx_engine {
     r = dalloc<double>(nE);
     energies = dalloc<double>(nN);
     forces = dalloc<double>(3 * nE);
+    atom_order = dalloc<int>(nN);
     if (precision == SMX_PRECISION_BF16) {
       const long T = tc_terms;
       M0_bf = dalloc<__nv_bfloat16>(T * nN * dm.nLM * C);
@@ -393,6 +396,20 @@ struct smx_engine {
     smx::launch_umma_gemms(g, ng, status_dev, s);
   }
 
+  // ---- centre-atom order of the edge kernels ----
+  // -1: species-sorted when a layer's spline table exceeds kOrderTableBytes (then the
+  // rows of all pairs do not stay in L2, the rows of one centre species do); 0: input
+  // order; 1: species-sorted.
+  static constexpr double kOrderTableBytes = 64.0 * 1024 * 1024;
+  int species_order = -1;
+  bool order_species() const {
+    if (species_order >= 0) return species_order == 1;
+    const double npairs = 0.5 * dm.S * (dm.S + 1);
+    const double fwd = npairs * dm.nint * dm.n_instr * dm.C * 16.0;
+    const double l0 = static_cast<double>(dm.S) * dm.S * dm.nint * 4 * dm.C * 16.0;
+    return dm.S > 1 && (fwd > kOrderTableBytes || l0 > kOrderTableBytes);
+  }
+
   // ---- centre-atom schedule of the per-atom kernels and its autotuner ----
   // Each per-atom kernel runs either one block per atom or as a persistent grid (its
   // resident blocks on every SM) claiming atoms from a counter (smx::AtomCursor).  The
@@ -464,8 +481,13 @@ struct smx_engine {
     run_pass(in, out_e, out_f, s);
   }
 
-  void run_pass(const smx::EdgeIn& in, double* out_e, double* out_f, cudaStream_t s) {
+  void run_pass(const smx::EdgeIn& in_, double* out_e, double* out_f, cudaStream_t s) {
+    smx::EdgeIn in = in_;
     const int N = in.N;
+    if (N > 0 && order_species()) {
+      smx::launch_species_order(in.node_type, N, dm.S, atom_order, s);
+      in.order = atom_order;
+    }
     const int C = dm.C;
     const int T = tc_terms;
     lastN = N;

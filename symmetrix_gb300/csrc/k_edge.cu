@@ -205,7 +205,8 @@ template <bool P>
 __global__ void __launch_bounds__(256) k_layer0_fwd(DevModel m, EdgeIn in, float* __restrict__ A0,
                                                     float* __restrict__ M0, float* __restrict__ zbl_e) {
   AtomCursor cur{P ? m.sched : nullptr, in.N, 0};
-  for (int i = cur.first(); i < in.N; i = cur.next()) layer0_fwd_atom(m, in, A0, M0, zbl_e, i);
+  for (int b = cur.first(); b < in.N; b = cur.next())
+    layer0_fwd_atom(m, in, A0, M0, zbl_e, in.atom_at(b));
   cur.done();
 }
 
@@ -382,7 +383,8 @@ template <bool P>
 __global__ void __launch_bounds__(128) k_layer0_rev(DevModel m, EdgeIn in, const float* __restrict__ A0_adj,
                                                     const double* __restrict__ f1, double* __restrict__ forces) {
   AtomCursor cur{P ? m.sched : nullptr, in.N, 0};
-  for (int i = cur.first(); i < in.N; i = cur.next()) layer0_rev_atom(m, in, A0_adj, f1, forces, i);
+  for (int b = cur.first(); b < in.N; b = cur.next())
+    layer0_rev_atom(m, in, A0_adj, f1, forces, in.atom_at(b));
   cur.done();
 }
 

@@ -362,7 +362,8 @@ template <int LMAX, int CT, bool P>
 __global__ void __launch_bounds__(256) k_layer1_fwd(DevModel m, EdgeIn in, const float* __restrict__ H1,
                                                     float* __restrict__ Phi1) {
   AtomCursor cur{P ? m.sched : nullptr, in.N, 0};
-  for (int i = cur.first(); i < in.N; i = cur.next()) layer1_fwd_atom<LMAX, CT>(m, in, H1, Phi1, i);
+  for (int b = cur.first(); b < in.N; b = cur.next())
+    layer1_fwd_atom<LMAX, CT>(m, in, H1, Phi1, in.atom_at(b));
   cur.done();
 }
 
@@ -438,7 +439,8 @@ __global__ void __launch_bounds__(256) k_layer1_rev(DevModel m, EdgeIn in, const
                                                     const float* __restrict__ dPhi1, float* __restrict__ H1_adj,
                                                     double* __restrict__ f1) {
   AtomCursor cur{P ? m.sched : nullptr, in.N, 0};
-  for (int i = cur.first(); i < in.N; i = cur.next()) layer1_rev_atom<LMAX, CT>(m, in, H1, dPhi1, H1_adj, f1, i);
+  for (int b = cur.first(); b < in.N; b = cur.next())
+    layer1_rev_atom<LMAX, CT>(m, in, H1, dPhi1, H1_adj, f1, in.atom_at(b));
   cur.done();
 }
 
@@ -607,7 +609,8 @@ template <bool P>
 __global__ void __launch_bounds__(512, 1) k_layer1_fwd_l2(DevModel m, EdgeIn in, const float* __restrict__ H1,
                                                           float* __restrict__ Phi1) {
   AtomCursor cur{P ? m.sched : nullptr, in.N, 0};
-  for (int i = cur.first(); i < in.N; i = cur.next()) layer1_fwd_l2_atom(m, in, H1, Phi1, i);
+  for (int b = cur.first(); b < in.N; b = cur.next())
+    layer1_fwd_l2_atom(m, in, H1, Phi1, in.atom_at(b));
   cur.done();
 }
 
@@ -761,7 +764,8 @@ __global__ void __launch_bounds__(512, 1) k_layer1_rev_l2(DevModel m, EdgeIn in,
                                                           const float* __restrict__ dPhi1,
                                                           float* __restrict__ H1_adj, double* __restrict__ f1) {
   AtomCursor cur{P ? m.sched : nullptr, in.N, 0};
-  for (int i = cur.first(); i < in.N; i = cur.next()) layer1_rev_l2_atom(m, in, H1, dPhi1, H1_adj, f1, i);
+  for (int b = cur.first(); b < in.N; b = cur.next())
+    layer1_rev_l2_atom(m, in, H1, dPhi1, H1_adj, f1, in.atom_at(b));
   cur.done();
 }
 

@@ -262,6 +262,33 @@ void node_tail_residency(const DevModel& m, int* per_sm) {
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[kAkNodeTail], k_node_tail<true>, m.C, node_tail_smem(m));
 }
 
+// Centre atoms sorted by species (a counting sort; the order inside a species is
+// arbitrary: every atom's results are computed the same way whichever block takes it).
+// One block.
+__global__ void __launch_bounds__(1024) k_species_order(const int* __restrict__ ntype, int N, int S,
+                                                        int* __restrict__ order) {
+  extern __shared__ int cnt[];  // [S]: counts, then scatter cursors
+  for (int t = threadIdx.x; t < S; t += blockDim.x) cnt[t] = 0;
+  __syncthreads();
+  for (int i = threadIdx.x; i < N; i += blockDim.x) atomicAdd(&cnt[ntype[i]], 1);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int o = 0;
+    for (int t = 0; t < S; ++t) {
+      const int c = cnt[t];
+      cnt[t] = o;
+      o += c;
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < N; i += blockDim.x) order[atomicAdd(&cnt[ntype[i]], 1)] = i;
+}
+
+void launch_species_order(const int* node_type, int N, int S, int* order, cudaStream_t s) {
+  if (N <= 0) return;
+  k_species_order<<<1, 1024, sizeof(int) * S, s>>>(node_type, N, S, order);
+}
+
 // first[0] = 0, first[i+1] = first[i] + num_neigh[i]; one block, sequential tiles.
 __global__ void __launch_bounds__(1024) k_scan_first(const int* __restrict__ num_neigh, int N, int* __restrict__ first) {
   __shared__ int sw[32];

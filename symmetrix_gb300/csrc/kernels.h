@@ -51,6 +51,8 @@ void launch_node_tail(const DevModel& m, const int* node_type, int N, float* A1,
                       float* H2, float* A1_adj, float* H1_adj, float* M1_adj, float* H2_adj, const float* zbl_e,
                       double* energies, cudaStream_t s);
 void launch_scan_first(const int* num_neigh, int N, int* first, cudaStream_t s);
+// order[N]: the atoms sorted by species (node_type in [0, S))
+void launch_species_order(const int* node_type, int N, int S, int* order, cudaStream_t s);
 
 // k_umma.cu: Y = X . B^T on the tcgen05 tensor cores (bf16 operands, f32 accumulation).
 // Row r of the GEMM, column c of N-tile y lands at

@@ -311,3 +311,26 @@ def test_persistent_atom_schedule(engine_lib, tmp_path, L_max):
     ref.compute_node_energies_forces(*edge_args(species[:7], sub))
     assert _report("E_i small", m.node_energies, ref.node_energies) < E_TOL
     assert _report("f_edge small", m.node_forces, ref.node_forces) < F_TOL
+
+
+def test_species_sorted_atom_order(engine_lib, tmp_path):
+    """Centre atoms taken in species order (the layout for tables larger than L2): the
+    same energies as the input order, bitwise, and forces against the oracle."""
+    path = write_model(make_model(num_channels=32, species=("H", "C", "N", "O"), r_cut=5.0, L_max=1, num_knots=60,
+                                  seed=6, zbl=True), str(tmp_path / "m.json"))
+    pos, L, species = random_box(250, 0.09, 0.9, 4, seed=13)
+    nl = neighbor_list(pos, 5.0, L)
+    ref = Evaluator(path, "port")
+    ref.compute_node_energies_forces(*edge_args(species, nl))
+    m = _engine(path)
+    m.set_option("species_order", 0)
+    assert m.get_option("species_order") == 0  # a small table: input order by default too
+    m.compute_node_energies_forces(*edge_args(species, nl))
+    e0 = m.node_energies.copy()
+    m.set_option("species_order", 1)
+    assert m.get_option("species_order") == 1
+    for persistent in (0, 1):
+        m.set_option("persistent", persistent)
+        m.compute_node_energies_forces(*edge_args(species, nl))
+        assert np.array_equal(m.node_energies, e0), persistent
+        assert _report("f_edge", m.node_forces, ref.node_forces) < F_TOL

@@ -123,7 +123,8 @@ int smx_set_option(smx_engine* eng, const char* key, long value);
  * "tc_tuned_ns_<G>" for G in H1, A1, Phi1_adj, M0_adj; "persistent": bit k set when
  * per-atom kernel k (layer0_fwd, contract0_rev, layer0_rev, layer1_fwd, layer1_rev,
  * node_tail) runs as a persistent grid; "species_order": 1 when the sorted order is in
- * effect); -1 if unknown. */
+ * effect; "poly_canon": 1 when the model's symmetric-contraction monomials are the
+ * canonical sets and run as generated code, 0 for the data-driven path); -1 if unknown. */
 long smx_get_option(const smx_engine* eng, const char* key);
 
 /* The engine's own CUDA stream (a cudaStream_t): host-pointer calls and the MD driver

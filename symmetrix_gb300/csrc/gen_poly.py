@@ -18,7 +18,7 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
 from symmetrix_gb300.synth.equivariant import equivariant_polynomial_basis  # noqa: E402
 
-L_MAX = 1  # hidden irreps 0e + 1o: LM = 0..3
+L_MAX = 2  # hidden irreps up to 0e + 1o + 2e: LM = 0..8 (an L_max = 1 model uses LM = 0..3)
 
 
 def canonical(L, M):
@@ -102,9 +102,8 @@ def main():
     t = ["// Generated by gen_poly.py: canonical symmetric-contraction monomial tables (l_max 3,",
          "// degree <= 3), shared by host and device code.  Do not edit; rerun the script.",
          "#pragma once", "", "namespace smx {", "namespace poly {", "",
-         f"constexpr int kNumLM = {nLM};  // L_max = {L_MAX}",
+         f"constexpr int kNumLM = {nLM};  // LM = 0 .. (L_max + 1)^2 - 1 for L_max up to {L_MAX}",
          f"constexpr int kOffset[{nLM + 1}] = {{{', '.join(map(str, offs))}}};",
-         f"constexpr int kMaxCount = {max(len(x) for x in lists)};",
          "// packed a | b << 8 | c << 16, 16 = constant one; LM-major, canonical order",
          f"constexpr int kMono[{len(flat)}] = {{{', '.join(map(str, flat))}}};", "",
          "}  // namespace poly", "}  // namespace smx", ""]

@@ -92,6 +92,7 @@ __device__ __forceinline__ void stage_l0(const DevModel& m, const EdgeIn& in, in
 // Layer 0 forward: A0[i,lm,k] = sum_j Y_lm(x_ij) R0'_{ti,tj,l}(r_ij)[k] with the
 // folded ordered-pair splines, then M0[i,LM,k] = P_{ti,LM,k}(A0[i,:,k]).
 // ---------------------------------------------------------------------------
+template <int NLM>
 __device__ __forceinline__ void layer0_fwd_atom(const DevModel& m, const EdgeIn& in, float* __restrict__ A0,
                                                 float* __restrict__ M0, float* __restrict__ zbl_e, int i) {
   extern __shared__ float dyn[];  // [17][C]: A0 columns (+ constant one) for the contraction
@@ -175,10 +176,20 @@ __device__ __forceinline__ void layer0_fwd_atom(const DevModel& m, const EdgeIn&
       const float* cf = m.coef0 + static_cast<size_t>(ti * m.nLM) * m.T0 * C + k;
       const size_t sst = static_cast<size_t>(m.T0) * C;
       float* out = M0 + static_cast<size_t>(i) * m.nLM * C + k;
-      const float v[4] = {poly::value_LM0(x, cf, C), poly::value_LM1(x, cf + sst, C),
-                          poly::value_LM2(x, cf + 2 * sst, C), poly::value_LM3(x, cf + 3 * sst, C)};
+      float v[9];
+      v[0] = poly::value_LM0(x, cf, C);
+      v[1] = poly::value_LM1(x, cf + sst, C);
+      v[2] = poly::value_LM2(x, cf + 2 * sst, C);
+      v[3] = poly::value_LM3(x, cf + 3 * sst, C);
+      if constexpr (NLM == 9) {  // L_max = 2: the five l = 2 outputs
+        v[4] = poly::value_LM4(x, cf + 4 * sst, C);
+        v[5] = poly::value_LM5(x, cf + 5 * sst, C);
+        v[6] = poly::value_LM6(x, cf + 6 * sst, C);
+        v[7] = poly::value_LM7(x, cf + 7 * sst, C);
+        v[8] = poly::value_LM8(x, cf + 8 * sst, C);
+      }
 #pragma unroll
-      for (int LM = 0; LM < 4; ++LM) {
+      for (int LM = 0; LM < NLM; ++LM) {
         out[LM * C] = v[LM];
         if (m.op_m0)  // BF16 form: the H1 GEMM's split operand
           write_split(m.op_m0 + (static_cast<size_t>(i) * m.nLM + LM) * m.tc_terms * C, C, m.tc_terms, k, v[LM]);
@@ -201,12 +212,12 @@ __device__ __forceinline__ void layer0_fwd_atom(const DevModel& m, const EdgeIn&
   }
 }
 
-template <bool P>
+template <bool P, int NLM>
 __global__ void __launch_bounds__(256) k_layer0_fwd(DevModel m, EdgeIn in, float* __restrict__ A0,
                                                     float* __restrict__ M0, float* __restrict__ zbl_e) {
   AtomCursor cur{P ? m.sched : nullptr, in.N, 0};
   for (int b = cur.first(); b < in.N; b = cur.next())
-    layer0_fwd_atom(m, in, A0, M0, zbl_e, in.atom_at(b));
+    layer0_fwd_atom<NLM>(m, in, A0, M0, zbl_e, in.atom_at(b));
   cur.done();
 }
 
@@ -216,6 +227,7 @@ __global__ void __launch_bounds__(256) k_layer0_fwd(DevModel m, EdgeIn in, float
 // Its own kernel, so its register-heavy generated code does not limit the occupancy
 // of the layer-0 edge adjoint.
 // ---------------------------------------------------------------------------
+template <int NLM>
 __device__ __forceinline__ void contract0_rev_atom(const DevModel& m, const int* __restrict__ node_type,
                                                    const float* __restrict__ A0, const float* __restrict__ M0_adj,
                                                    float* __restrict__ A0_adj, int i) {
@@ -237,6 +249,13 @@ __device__ __forceinline__ void contract0_rev_atom(const DevModel& m, const int*
     poly::grad_LM1(x, w[C], cf + st, C, dA);
     poly::grad_LM2(x, w[2 * C], cf + 2 * st, C, dA);
     poly::grad_LM3(x, w[3 * C], cf + 3 * st, C, dA);
+    if constexpr (NLM == 9) {  // L_max = 2: the five l = 2 outputs
+      poly::grad_LM4(x, w[4 * C], cf + 4 * st, C, dA);
+      poly::grad_LM5(x, w[5 * C], cf + 5 * st, C, dA);
+      poly::grad_LM6(x, w[6 * C], cf + 6 * st, C, dA);
+      poly::grad_LM7(x, w[7 * C], cf + 7 * st, C, dA);
+      poly::grad_LM8(x, w[8 * C], cf + 8 * st, C, dA);
+    }
   } else {  // data-driven monomial lists, this thread's columns in shared memory
     float* sA = dyn;            // [17][C] A0 column
     float* sGd = dyn + 17 * C;  // [17][C] gradient column (row 16 absorbs the constant slot)
@@ -278,12 +297,12 @@ __device__ __forceinline__ void contract0_rev_atom(const DevModel& m, const int*
   for (int q = 0; q < 16; ++q) A0_adj[(static_cast<size_t>(i) * 16 + q) * C + k] = dA[q];
 }
 
-template <bool P>
+template <bool P, int NLM>
 __global__ void __launch_bounds__(256) k_contract0_rev(DevModel m, const int* __restrict__ node_type,
                                                        const float* __restrict__ A0, const float* __restrict__ M0_adj,
                                                        float* __restrict__ A0_adj, int N) {
   AtomCursor cur{P ? m.sched : nullptr, N, 0};
-  for (int i = cur.first(); i < N; i = cur.next()) contract0_rev_atom(m, node_type, A0, M0_adj, A0_adj, i);
+  for (int i = cur.first(); i < N; i = cur.next()) contract0_rev_atom<NLM>(m, node_type, A0, M0_adj, A0_adj, i);
   cur.done();
 }
 
@@ -398,15 +417,28 @@ cudaError_t init_edge_kernels(const DevModel& m) { return init_layer1_kernels(m)
 // layer-0 edge kernels: one thread per channel pair, whole warps
 int layer0_block(int C) { return ((C >> 1) + 31) & ~31; }
 
+// the canonical polynomial outputs compiled into the layer-0 kernels: 9 (L_max = 2) or 4
+// (L_max = 1, and every model on the data-driven polynomial path)
+template <typename F>
+void dispatch_nlm(const DevModel& m, F&& f) {
+  if (m.poly_canon && m.nLM == 9)
+    f(std::integral_constant<int, 9>{});
+  else
+    f(std::integral_constant<int, 4>{});
+}
+
 void launch_layer0_fwd(const DevModel& m, const EdgeIn& in, float* A0, float* M0, float* zbl_e, cudaStream_t s) {
   if (in.N <= 0) return;
   const size_t smem = 17 * sizeof(float) * m.C;
   DevModel mk;
   const int grid = atom_grid(m, kAkLayer0Fwd, in.N, mk);
-  if (mk.sched)
-    k_layer0_fwd<true><<<grid, 2 * layer0_block(m.C), smem, s>>>(mk, in, A0, M0, zbl_e);
-  else
-    k_layer0_fwd<false><<<grid, 2 * layer0_block(m.C), smem, s>>>(mk, in, A0, M0, zbl_e);
+  dispatch_nlm(m, [&](auto nc) {
+    constexpr int NLM = decltype(nc)::value;
+    if (mk.sched)
+      k_layer0_fwd<true, NLM><<<grid, 2 * layer0_block(m.C), smem, s>>>(mk, in, A0, M0, zbl_e);
+    else
+      k_layer0_fwd<false, NLM><<<grid, 2 * layer0_block(m.C), smem, s>>>(mk, in, A0, M0, zbl_e);
+  });
 }
 
 void launch_layer0_rev(const DevModel& m, const EdgeIn& in, const float* A0, const float* M0_adj, const double* f1,
@@ -415,10 +447,13 @@ void launch_layer0_rev(const DevModel& m, const EdgeIn& in, const float* A0, con
   DevModel mk;
   int grid = atom_grid(m, kAkContract0Rev, in.N, mk);
   const size_t smem = m.poly_canon ? 0 : 34 * sizeof(float) * m.C;
-  if (mk.sched)
-    k_contract0_rev<true><<<grid, m.C, smem, s>>>(mk, in.node_type, A0, M0_adj, A0_adj, in.N);
-  else
-    k_contract0_rev<false><<<grid, m.C, smem, s>>>(mk, in.node_type, A0, M0_adj, A0_adj, in.N);
+  dispatch_nlm(m, [&](auto nc) {
+    constexpr int NLM = decltype(nc)::value;
+    if (mk.sched)
+      k_contract0_rev<true, NLM><<<grid, m.C, smem, s>>>(mk, in.node_type, A0, M0_adj, A0_adj, in.N);
+    else
+      k_contract0_rev<false, NLM><<<grid, m.C, smem, s>>>(mk, in.node_type, A0, M0_adj, A0_adj, in.N);
+  });
   grid = atom_grid(m, kAkLayer0Rev, in.N, mk);
   if (mk.sched)
     k_layer0_rev<true><<<grid, layer0_block(m.C), 0, s>>>(mk, in, A0_adj, f1, forces);
@@ -428,10 +463,13 @@ void launch_layer0_rev(const DevModel& m, const EdgeIn& in, const float* A0, con
 
 // resident blocks per SM of the persistent layer-0 kernels at this model's launch shapes
 void layer0_residency(const DevModel& m, int* per_sm) {
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[kAkLayer0Fwd], k_layer0_fwd<true>, 2 * layer0_block(m.C),
-                                                17 * sizeof(float) * m.C);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[kAkContract0Rev], k_contract0_rev<true>, m.C,
-                                                m.poly_canon ? 0 : 34 * sizeof(float) * m.C);
+  dispatch_nlm(m, [&](auto nc) {
+    constexpr int NLM = decltype(nc)::value;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[kAkLayer0Fwd], k_layer0_fwd<true, NLM>,
+                                                  2 * layer0_block(m.C), 17 * sizeof(float) * m.C);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[kAkContract0Rev], k_contract0_rev<true, NLM>, m.C,
+                                                  m.poly_canon ? 0 : 34 * sizeof(float) * m.C);
+  });
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[kAkLayer0Rev], k_layer0_rev<true>, layer0_block(m.C), 0);
 }
 

@@ -386,7 +386,9 @@ PackedModel pack_model(const HostModel& hm) {
     }
     return true;
   };
-  pm.poly_canon = (hm.L_max == 1 && hm.nLM == poly::kNumLM) ? 1 : 0;
+  pm.poly_canon =
+      ((hm.L_max == 1 || hm.L_max == 2) && hm.nLM == (hm.L_max + 1) * (hm.L_max + 1) && hm.nLM <= poly::kNumLM) ? 1
+                                                                                                            : 0;
   std::vector<std::vector<int>> cmap0(hm.nLM);
   std::vector<int> cmap1;
   if (pm.poly_canon) {
@@ -401,7 +403,10 @@ PackedModel pack_model(const HostModel& hm) {
     pm.mono0_off[LM + 1] = static_cast<int>(pm.mono0.size());
     pm.T0 = std::max<int>(pm.T0, hm.M0_mono[LM].size());
   }
-  if (pm.poly_canon) pm.T0 = poly::kMaxCount;
+  if (pm.poly_canon) {  // coefficient slots: the longest canonical list among the model's LM
+    pm.T0 = 0;
+    for (int LM = 0; LM < hm.nLM; ++LM) pm.T0 = std::max(pm.T0, poly::kOffset[LM + 1] - poly::kOffset[LM]);
+  }
   pm.coef0.assign(static_cast<size_t>(S) * hm.nLM * std::max(pm.T0, 1) * C, 0.0f);
   for (int s = 0; s < S; ++s)
     for (int LM = 0; LM < hm.nLM; ++LM)

@@ -248,6 +248,7 @@ def test_lmax2_model_matches_oracle(engine_lib, tmp_path, variant):
     nl = neighbor_list(pos, 5.0, L)
     m = _engine(path, keep_stages=True)
     assert m.L_max == 2 and m.num_LM == 9
+    assert m.get_option("poly_canon") == 1  # generated polynomial kernels for LM = 0..8
     m.compute_node_energies_forces(*edge_args(species, nl))
     ref = Evaluator(path, "port")
     ref.compute_node_energies_forces(*edge_args(species, nl))
@@ -334,3 +335,29 @@ def test_species_sorted_atom_order(engine_lib, tmp_path):
         m.compute_node_energies_forces(*edge_args(species, nl))
         assert np.array_equal(m.node_energies, e0), persistent
         assert _report("f_edge", m.node_forces, ref.node_forces) < F_TOL
+
+
+def test_lmax2_data_driven_polynomials(engine_lib, tmp_path):
+    """An L_max = 2 model with a monomial outside the canonical sets runs the data-driven
+    polynomial kernels; energies and forces against the oracle."""
+    import json
+    path = write_model(make_model(num_channels=32, species=("H", "C", "O"), r_cut=5.0, L_max=2, num_knots=60,
+                                  seed=9), str(tmp_path / "l2.json"))
+    with open(path) as f:
+        model = json.load(f)
+    rng = np.random.default_rng(4)
+    model["M0_monomials"]["5"].append([0, 1, 4])
+    for s in model["M0_weights"]:
+        for k in model["M0_weights"][s]["5"]:
+            model["M0_weights"][s]["5"][k].append(float(rng.normal() * 0.1))
+    with open(path, "w") as f:
+        json.dump(model, f)
+    pos, L, species = random_box(64, 0.064, 0.9, 3, seed=5)
+    nl = neighbor_list(pos, 5.0, L)
+    m = _engine(path)
+    assert m.get_option("poly_canon") == 0
+    m.compute_node_energies_forces(*edge_args(species, nl))
+    ref = Evaluator(path, "port")
+    ref.compute_node_energies_forces(*edge_args(species, nl))
+    assert _report("E_i", m.node_energies, ref.node_energies) < E_TOL
+    assert _report("f_edge", m.node_forces, ref.node_forces) < F_TOL

@@ -70,6 +70,10 @@ struct DevModel {
   // sched[0..1]; 0 launches one block per atom.  pgrid is read on the host only.
   int* sched;
   int pgrid[8];
+  // L_max = 2 layer-1 kernels: channel slices per node (one block each) and the offset
+  // between the per-slice partial edge forces in f1 (0: one slice)
+  int l2_split;
+  long f1_stride;
 };
 
 // Per-atom kernels, indices into DevModel::pgrid.

@@ -180,6 +180,10 @@ struct smx_engine {
     m.has_zbl = pm.has_zbl;
     m.op_m0 = m.op_phi1 = m.op_a1adj = nullptr;
     m.tc_terms = tc_terms;
+    // two blocks per node (half the channels each) let two L_max = 2 layer-1 blocks share
+    // an SM: one computes while the other waits at a barrier
+    m.l2_split = (pm.L_max == 2 && pm.C >= 64) ? 2 : 1;
+    m.f1_stride = 0;
     m.zbl_p = pm.zbl_p;
     for (int q = 0; q < 4; ++q) m.zbl_c[q] = pm.zbl_c[q];
     m.zbl_pair = pm.has_zbl ? reinterpret_cast<const float4*>(upload(pm.zbl_pair)) : nullptr;
@@ -271,7 +275,9 @@ struct smx_engine {
     A1_adj = dalloc<float>(nN * 16 * C);
     M1_adj = dalloc<float>(nN * C);
     H2_adj = dalloc<float>(nN * C);
-    f1 = dalloc<double>(3 * nE);
+    // L_max = 2 with two channel slices: one f1 slice each
+    dm.f1_stride = dm.l2_split > 1 ? 3 * nE : 0;
+    f1 = dalloc<double>(3 * nE * dm.l2_split);
     zbl_e = dalloc<float>(nN);
     first = dalloc<int>(nN + 1);
     ntype = dalloc<int>(nN);

@@ -393,7 +393,11 @@ __device__ __forceinline__ void layer0_rev_atom(const DevModel& m, const EdgeIn&
         const double g = static_cast<double>(m.dens_c[0][i]) * static_cast<double>(d) / r;
         for (int a = 0; a < 3; ++a) s[a] -= g * in.xyz[3 * e + a];
       }
-      for (int a = 0; a < 3; ++a) forces[3 * e + a] = -(s[a] + f1[3 * e + a]);
+      for (int a = 0; a < 3; ++a) {
+        double f = f1[3 * e + a];
+        if (m.f1_stride) f += f1[m.f1_stride + 3 * e + a];  // second channel slice (L_max = 2)
+        forces[3 * e + a] = -(s[a] + f);
+      }
     }
   }
 }

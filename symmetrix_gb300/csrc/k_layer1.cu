@@ -454,6 +454,10 @@ __global__ void __launch_bounds__(256) k_layer1_rev(DevModel m, EdgeIn in, const
 namespace {
 
 constexpr int kL2Groups = 4;
+// channels per block of the L_max = 2 layer-1 kernels (a warp multiple)
+__host__ __device__ inline int l2_slice_width(const DevModel& m) {
+  return ((m.C + m.l2_split - 1) / m.l2_split + 31) & ~31;
+}
 __host__ __device__ constexpr int l2_count(int g) { return g == 1 ? 5 : 4; }
 __host__ __device__ constexpr int l2_ins(int g, int i) {
   constexpr int t0[4] = {11, 13, 15, 16}, t1[5] = {1, 4, 5, 8, 12}, t2[4] = {0, 2, 6, 10}, t3[4] = {3, 7, 9, 14};
@@ -479,8 +483,8 @@ __host__ __device__ constexpr bool l2_uses_y(int c) {
 }
 constexpr int kL2MaxNp = 62;
 
-// block-wide sum of a 3-vector per edge for up to 32 warps
-__device__ __forceinline__ void block_reduce3_w32(float fx, float fy, float fz, float (*sF)[32][3], int t) {
+// block-wide sum of a 3-vector per edge for up to 16 warps
+__device__ __forceinline__ void block_reduce3_w16(float fx, float fy, float fz, float (*sF)[16][3], int t) {
   const float x = warp_sum(fx), y = warp_sum(fy), z = warp_sum(fz);
   if ((threadIdx.x & 31) == 0) {
     const int w = threadIdx.x >> 5;
@@ -544,15 +548,17 @@ __device__ __forceinline__ void l2_load_g(const float* sP, int C, int k, float* 
 
 }  // namespace
 
-// Layer-1 forward, L_max = 2.
+// Layer-1 forward, L_max = 2: slice h of the channels of node i (channels h*CH ..
+// h*CH + CH - 1, CH = l2_slice_width(C)); four groups of CH threads, group G running the
+// instructions of group G.
 __device__ __forceinline__ void layer1_fwd_l2_atom(const DevModel& m, const EdgeIn& in, const float* __restrict__ H1,
-                                                   float* __restrict__ Phi1, int i) {
+                                                   float* __restrict__ Phi1, int i, int h) {
   extern __shared__ float dyn[];
   __shared__ L1Stage<false> st;
-  const int C = m.C, CP = (C + 31) & ~31;
-  const int grp = threadIdx.x / CP, kk = threadIdx.x - grp * CP;
-  const bool live = kk < C;
-  const int k = live ? kk : 0;
+  const int C = m.C, CH = l2_slice_width(m);
+  const int grp = threadIdx.x / CH, kk = threadIdx.x - grp * CH;
+  const bool live = kk < CH && h * CH + kk < C;
+  const int k = live ? h * CH + kk : 0;
   const int ti = in.node_type[i];
   const int e0 = in.first[i], e1 = in.first[i + 1];
   float acc[kL2MaxNp];
@@ -572,45 +578,49 @@ __device__ __forceinline__ void layer1_fwd_l2_atom(const DevModel& m, const Edge
   }
   if (m.dens_spl[1]) {
     const float S = dens_factor(m, 1, in, i, ti);
-    if (threadIdx.x == 0) m.dens_s[1][i] = S;
+    if (threadIdx.x == 0 && h == 0) m.dens_s[1][i] = S;
   }
-  float* sP = dyn;  // [NP][C]
+  float* sP = dyn;  // [NP][CH]: Phi1r of the slice
   if (live) {
     switch (grp) {
-      case 0: l2_store<0>(sP, C, k, acc); break;
-      case 1: l2_store<1>(sP, C, k, acc); break;
-      case 2: l2_store<2>(sP, C, k, acc); break;
-      default: l2_store<3>(sP, C, k, acc); break;
+      case 0: l2_store<0>(sP, CH, kk, acc); break;
+      case 1: l2_store<1>(sP, CH, kk, acc); break;
+      case 2: l2_store<2>(sP, CH, kk, acc); break;
+      default: l2_store<3>(sP, CH, kk, acc); break;
     }
   }
   __syncthreads();
+  // Phi1 rows of the slice, group G taking the rows lme = G (mod 4)
+  if (!live) return;
   const int T = m.tc_terms;
-  for (int kc = threadIdx.x; kc < C; kc += blockDim.x)
-    for (int l = 0; l < 4; ++l) {
-      const int ne = m.num_e[l], Kl = ne * C;
-      for (int mm = 0; mm < 2 * l + 1; ++mm)
-        for (int e = 0; e < ne; ++e) {
-          const int lme = m.lme_off[l] + mm * ne + e;
-          float s = 0.0f;
-          const int p1 = __ldg(m.cg_fwd_off + lme + 1);
-          for (int p = __ldg(m.cg_fwd_off + lme); p < p1; ++p)
-            s = fmaf(__ldg(m.cg_fwd_v + p), sP[__ldg(m.cg_fwd_p + p) * C + kc], s);
-          Phi1[(static_cast<size_t>(i) * m.n_lme + lme) * C + kc] = s;
-          if (m.op_phi1) {
-            __nv_bfloat16* row = m.op_phi1 + static_cast<size_t>(T) * in.N * m.lme_off[l] * C +
-                                 (static_cast<size_t>(i) * (2 * l + 1) + mm) * T * Kl;
-            write_split(row, Kl, T, e * C + kc, s);
-          }
+  for (int l = 0; l < 4; ++l) {
+    const int ne = m.num_e[l], Kl = ne * C;
+    for (int mm = 0; mm < 2 * l + 1; ++mm)
+      for (int e = 0; e < ne; ++e) {
+        const int lme = m.lme_off[l] + mm * ne + e;
+        if ((lme & (kL2Groups - 1)) != grp) continue;
+        float sum = 0.0f;
+        const int p1 = __ldg(m.cg_fwd_off + lme + 1);
+        for (int p = __ldg(m.cg_fwd_off + lme); p < p1; ++p)
+          sum = fmaf(__ldg(m.cg_fwd_v + p), sP[__ldg(m.cg_fwd_p + p) * CH + kk], sum);
+        Phi1[(static_cast<size_t>(i) * m.n_lme + lme) * C + k] = sum;
+        if (m.op_phi1) {
+          __nv_bfloat16* row = m.op_phi1 + static_cast<size_t>(T) * in.N * m.lme_off[l] * C +
+                               (static_cast<size_t>(i) * (2 * l + 1) + mm) * T * Kl;
+          write_split(row, Kl, T, e * C + k, sum);
         }
-    }
+      }
+  }
 }
 
+// work item b = (atom, channel slice); the return in the atom body above happens after
+// its last barrier
 template <bool P>
 __global__ void __launch_bounds__(512, 1) k_layer1_fwd_l2(DevModel m, EdgeIn in, const float* __restrict__ H1,
                                                           float* __restrict__ Phi1) {
-  AtomCursor cur{P ? m.sched : nullptr, in.N, 0};
-  for (int b = cur.first(); b < in.N; b = cur.next())
-    layer1_fwd_l2_atom(m, in, H1, Phi1, in.atom_at(b));
+  const int ns = m.l2_split, n = in.N * ns;
+  AtomCursor cur{P ? m.sched : nullptr, n, 0};
+  for (int b = cur.first(); b < n; b = cur.next()) layer1_fwd_l2_atom(m, in, H1, Phi1, in.atom_at(b / ns), b % ns);
   cur.done();
 }
 
@@ -627,7 +637,7 @@ __host__ __device__ constexpr bool l2_uses_l2(int l2) {
 template <int G>
 __device__ __forceinline__ void l2_rev_chunk(const DevModel& m, const float* __restrict__ H1,
                                              float* __restrict__ H1_adj, const L1Stage<true>& st, int C, int k,
-                                             bool live, const float* g, float (*sF)[32][3]) {
+                                             bool live, const float* g, float (*sF)[16][3]) {
   constexpr int NL2 = 9, NI = 17;
   const int na = st.nact;
   for (int a = 0; a < na; ++a) {
@@ -677,7 +687,7 @@ __device__ __forceinline__ void l2_rev_chunk(const DevModel& m, const float* __r
       }
     });
     if (!live) fx = fy = fz = 0.0f;
-    block_reduce3_w32(fx, fy, fz, sF, t);
+    block_reduce3_w16(fx, fy, fz, sF, t);
     if (live) {
       float* dst = H1_adj + static_cast<size_t>(j) * NL2 * C + k;
       static_for<3>([&](auto lc) {
@@ -693,42 +703,47 @@ __device__ __forceinline__ void l2_rev_chunk(const DevModel& m, const float* __r
 
 }  // namespace
 
-// Layer-1 adjoint, L_max = 2.
+// Layer-1 adjoint, L_max = 2, channel slice h of node i (as the forward).  Each slice
+// writes its partial per-edge forces to its own f1 slice (f1 + h * f1_stride); the
+// layer-0 adjoint adds the slices.
 __device__ __forceinline__ void layer1_rev_l2_atom(const DevModel& m, const EdgeIn& in, const float* __restrict__ H1,
                                                    const float* __restrict__ dPhi1, float* __restrict__ H1_adj,
-                                                   double* __restrict__ f1, int i) {
+                                                   double* __restrict__ f1, int i, int h) {
   constexpr int NP = 243;
   extern __shared__ float dyn[];
   __shared__ L1Stage<true> st;
-  __shared__ float sF[kEdgeChunk][32][3];
-  const int C = m.C, CP = (C + 31) & ~31;
-  const int grp = threadIdx.x / CP, kk = threadIdx.x - grp * CP;
-  const bool live = kk < C;
-  const int k = live ? kk : 0;
+  __shared__ float sF[kEdgeChunk][16][3];  // up to 16 warps (512 threads)
+  const int C = m.C, CH = l2_slice_width(m);
+  const int grp = threadIdx.x / CH, kk = threadIdx.x - grp * CH;
+  const bool live = kk < CH && h * CH + kk < C;
+  const int k = live ? h * CH + kk : 0;
   const int nwarp = blockDim.x >> 5;
   const int ti = in.node_type[i];
   const int e0 = in.first[i], e1 = in.first[i + 1];
-  float* sD = dyn;                 // [n_lme][C]
-  float* sP = dyn + m.n_lme * C;   // [NP][C]
-  for (int kc = threadIdx.x; kc < C; kc += blockDim.x) {
-    for (int lme = 0; lme < m.n_lme; ++lme)
-      sD[lme * C + kc] = dPhi1[(static_cast<size_t>(i) * m.n_lme + lme) * C + kc];
-    for (int p = 0; p < NP; ++p) {
-      float s = 0.0f;
+  float* sD = dyn;                  // [n_lme][CH]
+  float* sP = dyn + m.n_lme * CH;   // [NP][CH]
+  // sP[p][k] = sum_lme CG[lme,p] dPhi1[i,lme,k]: rows split over the four groups
+  if (live)
+    for (int lme = grp; lme < m.n_lme; lme += kL2Groups)
+      sD[lme * CH + kk] = dPhi1[(static_cast<size_t>(i) * m.n_lme + lme) * C + k];
+  __syncthreads();
+  if (live)
+    for (int p = grp; p < NP; p += kL2Groups) {
+      float sum = 0.0f;
       const int q1 = __ldg(m.cg_rev_off + p + 1);
       for (int q = __ldg(m.cg_rev_off + p); q < q1; ++q)
-        s = fmaf(__ldg(m.cg_rev_v + q), sD[__ldg(m.cg_rev_lme + q) * C + kc], s);
-      sP[p * C + kc] = s;
+        sum = fmaf(__ldg(m.cg_rev_v + q), sD[__ldg(m.cg_rev_lme + q) * CH + kk], sum);
+      sP[p * CH + kk] = sum;
     }
-  }
   __syncthreads();
   float g[kL2MaxNp];
   switch (grp) {
-    case 0: l2_load_g<0>(sP, C, k, g); break;
-    case 1: l2_load_g<1>(sP, C, k, g); break;
-    case 2: l2_load_g<2>(sP, C, k, g); break;
-    default: l2_load_g<3>(sP, C, k, g); break;
+    case 0: l2_load_g<0>(sP, CH, kk, g); break;
+    case 1: l2_load_g<1>(sP, CH, kk, g); break;
+    case 2: l2_load_g<2>(sP, CH, kk, g); break;
+    default: l2_load_g<3>(sP, CH, kk, g); break;
   }
+  double* f1h = f1 + h * m.f1_stride;
   for (int eb = e0; eb < e1; eb += kEdgeChunk) {
     const int ne = min(kEdgeChunk, e1 - eb);
     __syncthreads();
@@ -742,19 +757,19 @@ __device__ __forceinline__ void layer1_rev_l2_atom(const DevModel& m, const Edge
     }
     __syncthreads();
     for (int t = threadIdx.x; t < ne; t += blockDim.x) {
-      double s[3] = {0.0, 0.0, 0.0};
+      double sum[3] = {0.0, 0.0, 0.0};
       const long e = static_cast<long>(eb) + t;
       if (st.row[t] >= 0)
         for (int w = 0; w < nwarp; ++w)
-          for (int c = 0; c < 3; ++c) s[c] += static_cast<double>(sF[t][w][c]);
-      if (m.dens_spl[1]) {
+          for (int c = 0; c < 3; ++c) sum[c] += static_cast<double>(sF[t][w][c]);
+      if (m.dens_spl[1] && h == 0) {
         float v, d;
         const double r = in.r[e];
         dens_eval(m, 1, ti, in.ntype_e[e], static_cast<float>(r), v, d);
         const double gg = static_cast<double>(m.dens_c[1][i]) * static_cast<double>(d) / r;
-        for (int c = 0; c < 3; ++c) s[c] -= gg * in.xyz[3 * e + c];
+        for (int c = 0; c < 3; ++c) sum[c] -= gg * in.xyz[3 * e + c];
       }
-      for (int c = 0; c < 3; ++c) f1[3 * e + c] = s[c];
+      for (int c = 0; c < 3; ++c) f1h[3 * e + c] = sum[c];
     }
   }
 }
@@ -763,9 +778,10 @@ template <bool P>
 __global__ void __launch_bounds__(512, 1) k_layer1_rev_l2(DevModel m, EdgeIn in, const float* __restrict__ H1,
                                                           const float* __restrict__ dPhi1,
                                                           float* __restrict__ H1_adj, double* __restrict__ f1) {
-  AtomCursor cur{P ? m.sched : nullptr, in.N, 0};
-  for (int b = cur.first(); b < in.N; b = cur.next())
-    layer1_rev_l2_atom(m, in, H1, dPhi1, H1_adj, f1, in.atom_at(b));
+  const int ns = m.l2_split, n = in.N * ns;
+  AtomCursor cur{P ? m.sched : nullptr, n, 0};
+  for (int b = cur.first(); b < n; b = cur.next())
+    layer1_rev_l2_atom(m, in, H1, dPhi1, H1_adj, f1, in.atom_at(b / ns), b % ns);
   cur.done();
 }
 
@@ -832,12 +848,12 @@ cudaError_t init_layer1_kernels(const DevModel& m) {
 void launch_layer1_fwd(const DevModel& m, const EdgeIn& in, const float* H1, float* Phi1, cudaStream_t s) {
   if (in.N <= 0) return;
   DevModel mk;
-  const int grid = atom_grid(m, kAkLayer1Fwd, in.N, mk);
+  const int grid = atom_grid(m, kAkLayer1Fwd, m.L_max == 2 ? in.N * m.l2_split : in.N, mk);
   dispatch_p(mk.sched != nullptr, [&](auto pc) {
     constexpr bool P = decltype(pc)::value;
     if (m.L_max == 2) {
-      k_layer1_fwd_l2<P><<<grid, kL2Groups * ((m.C + 31) & ~31), sizeof(float) * ins_np(2) * m.C, s>>>(mk, in, H1,
-                                                                                                     Phi1);
+      k_layer1_fwd_l2<P><<<grid, kL2Groups * l2_slice_width(m), sizeof(float) * ins_np(2) * l2_slice_width(m), s>>>(
+          mk, in, H1, Phi1);
       return;
     }
     const size_t smem = sizeof(float) * ins_np(1) * m.C;
@@ -851,12 +867,12 @@ void launch_layer1_rev(const DevModel& m, const EdgeIn& in, const float* H1, con
                        double* f1, cudaStream_t s) {
   if (in.N <= 0) return;
   DevModel mk;
-  const int grid = atom_grid(m, kAkLayer1Rev, in.N, mk);
+  const int grid = atom_grid(m, kAkLayer1Rev, m.L_max == 2 ? in.N * m.l2_split : in.N, mk);
   dispatch_p(mk.sched != nullptr, [&](auto pc) {
     constexpr bool P = decltype(pc)::value;
     if (m.L_max == 2) {
-      k_layer1_rev_l2<P><<<grid, kL2Groups * ((m.C + 31) & ~31), sizeof(float) * (m.n_lme + ins_np(2)) * m.C, s>>>(
-          mk, in, H1, dPhi1, H1_adj, f1);
+      k_layer1_rev_l2<P><<<grid, kL2Groups * l2_slice_width(m),
+                           sizeof(float) * (m.n_lme + ins_np(2)) * l2_slice_width(m), s>>>(mk, in, H1, dPhi1, H1_adj, f1);
       return;
     }
     const size_t smem = sizeof(float) * (m.n_lme + ins_np(1)) * m.C;
@@ -870,10 +886,10 @@ void launch_layer1_rev(const DevModel& m, const EdgeIn& in, const float* H1, con
 void layer1_residency(const DevModel& m, int* per_sm) {
   int f = 0, r = 0;
   if (m.L_max == 2) {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f, k_layer1_fwd_l2<true>, kL2Groups * ((m.C + 31) & ~31),
-                                                  sizeof(float) * ins_np(2) * m.C);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_layer1_rev_l2<true>, kL2Groups * ((m.C + 31) & ~31),
-                                                  sizeof(float) * (m.n_lme + ins_np(2)) * m.C);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f, k_layer1_fwd_l2<true>, kL2Groups * l2_slice_width(m),
+                                                  sizeof(float) * ins_np(2) * l2_slice_width(m));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_layer1_rev_l2<true>, kL2Groups * l2_slice_width(m),
+                                                  sizeof(float) * (m.n_lme + ins_np(2)) * l2_slice_width(m));
   } else {
     dispatch_c(m.C, [&](auto ct) {
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f, k_layer1_fwd<1, decltype(ct)::value, true>, m.C,

@@ -283,8 +283,9 @@ def test_persistent_atom_schedule(engine_lib, tmp_path, L_max):
     energies as one block per atom (bitwise: the forward pass is deterministic), forces
     against the oracle, and the counter is reset between launches (repeat evaluations).
     The tuned schedule is a mask over the six per-atom kernels."""
-    path = write_model(make_model(num_channels=32, species=("H", "C", "O"), r_cut=5.0, L_max=L_max, num_knots=60,
-                                  seed=5), str(tmp_path / "m.json"))
+    # 64 channels at L_max = 2: the layer-1 kernels run two channel slices per node
+    path = write_model(make_model(num_channels=32 * L_max, species=("H", "C", "O"), r_cut=5.0, L_max=L_max,
+                                  num_knots=60, seed=5), str(tmp_path / "m.json"))
     pos, L, species = random_box(300, 0.08, 0.9, 3, seed=12)
     nl = neighbor_list(pos, 5.0, L)
     ref = Evaluator(path, "port")

@@ -395,7 +395,7 @@ __device__ __forceinline__ void layer0_rev_atom(const DevModel& m, const EdgeIn&
       }
       for (int a = 0; a < 3; ++a) {
         double f = f1[3 * e + a];
-        if (m.f1_stride) f += f1[m.f1_stride + 3 * e + a];  // second channel slice (L_max = 2)
+        for (int h = 1; h < m.l2_split; ++h) f += f1[h * m.f1_stride + 3 * e + a];  // channel slices (L_max = 2)
         forces[3 * e + a] = -(s[a] + f);
       }
     }

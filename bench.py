@@ -365,6 +365,11 @@ def time_md(eng, pos, species, masses, L, vel, args, dist, estream):
     return T, t_wall, clk, md_check
 
 
+# (workload, stage) -> (DRAM bytes per launch, the ncu summary it comes from)
+NCU_TRAFFIC = {
+    ("fp32_4096", "layer1_rev"): (156.1e6 + 10.8e6, "profiles/layer1_rev_fp32_4096.md (ncu --set full, 1 launch)"),
+}
+
 ATOM_KERNELS = ("layer0_fwd", "contract0_rev", "layer0_rev", "layer1_fwd", "layer1_rev", "node_tail")
 
 
@@ -514,8 +519,12 @@ def gpu_arm(args, rank, world, local_rank):
     clk = head["clk"]
     sm_mhz = clk.get("sm_mhz") or 2070.0
     fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    # DRAM bytes per launch of the dominant kernel from one ncu capture of this build
+    # (dram__bytes_read.sum + dram__bytes_write.sum), where one exists for the workload
+    traffic = NCU_TRAFFIC.get((WORKLOAD["name"], dom))
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": achieved / hbm, "peak_source": peak_src, "traffic": None,
+                "frac": achieved / hbm, "peak_source": peak_src,
+                "traffic": traffic[0] if traffic else None, "traffic_source": traffic[1] if traffic else None,
                 "algorithmic_bytes_per_launch": bytes_, "avg_launch_ms": avg[dom],
                 "fp32_simt": {"achieved_tflops": flops / t_dom / 1e12, "peak_tflops": fp32_peak,
                               "frac": flops / t_dom / 1e12 / fp32_peak,

@@ -73,6 +73,11 @@ smx_engine* smx_create(const char* model_path, int precision, int device) {
     *eng->status_host = 0;
     check(cudaHostGetDevicePointer(reinterpret_cast<void**>(&eng->status_dev), eng->status_host, 0),
           "cudaHostGetDevicePointer");
+    check(cudaHostAlloc(reinterpret_cast<void**>(&eng->check_host), sizeof(unsigned), cudaHostAllocMapped),
+          "cudaHostAlloc");
+    *eng->check_host = 0;
+    check(cudaHostGetDevicePointer(reinterpret_cast<void**>(&eng->check_dev), eng->check_host, 0),
+          "cudaHostGetDevicePointer");
     eng->load(model_path);
     check(cudaDeviceSynchronize(), "model upload");
   } catch (const CudaError& e) {
@@ -97,6 +102,7 @@ void smx_destroy(smx_engine* eng) {
   for (auto& e : eng->ev)
     if (e) cudaEventDestroy(e);
   if (eng->status_host) cudaFreeHost(eng->status_host);
+  if (eng->check_host) cudaFreeHost(eng->check_host);
   delete eng;
 }
 
@@ -193,34 +199,38 @@ int smx_compute_node_energies_forces(smx_engine* eng, int num_nodes, const int* 
     return fail(SMX_ERR_INVALID, "NULL edge array");
   const int S = eng->hm.S;
   const double rc = eng->hm.r_cut;
-  // host-side validation and CSR offsets (the reference trusts its caller here)
-  std::vector<int> first(static_cast<size_t>(num_nodes) + 1, 0);
-  for (int i = 0; i < num_nodes; ++i) {
-    if (node_types[i] < 0 || node_types[i] >= S) return fail(SMX_ERR_INVALID, "node_types out of range");
-    if (num_neigh[i] < 0) return fail(SMX_ERR_INVALID, "negative num_neigh");
-    first[i + 1] = first[i] + num_neigh[i];
-  }
-  if (first[num_nodes] != num_edges) return fail(SMX_ERR_INVALID, "sum(num_neigh) != num_edges");
-  for (long e = 0; e < num_edges; ++e) {
-    if (neigh_indices[e] < 0 || neigh_indices[e] >= num_nodes)
-      return fail(SMX_ERR_INVALID, "neigh_indices out of range (must be < num_nodes)");
-    if (neigh_types[e] < 0 || neigh_types[e] >= S) return fail(SMX_ERR_INVALID, "neigh_types out of range");
-    if (!(r[e] > 0.0 && r[e] < rc) || !is_finite_d(xyz[3 * e]) || !is_finite_d(xyz[3 * e + 1]) || !is_finite_d(xyz[3 * e + 2]))
-      return fail(SMX_ERR_INVALID, "edge length outside (0, r_cut) or non-finite edge vector");
-  }
+  // The inputs are checked on the device after the copies (the reference trusts its
+  // caller here); nothing is evaluated until the check has passed.
   try {
     check(cudaSetDevice(eng->device), "cudaSetDevice");
     eng->reserve(num_nodes, num_edges);
     cudaStream_t s = eng->stream;
-    check(cudaMemcpyAsync(eng->first, first.data(), sizeof(int) * (num_nodes + 1), cudaMemcpyHostToDevice, s), "H2D");
-    if (num_nodes > 0)
+    if (num_nodes > 0) {
       check(cudaMemcpyAsync(eng->ntype, node_types, sizeof(int) * num_nodes, cudaMemcpyHostToDevice, s), "H2D");
+      check(cudaMemcpyAsync(eng->nneigh, num_neigh, sizeof(int) * num_nodes, cudaMemcpyHostToDevice, s), "H2D");
+    }
     if (num_edges > 0) {
       check(cudaMemcpyAsync(eng->nidx, neigh_indices, sizeof(int) * num_edges, cudaMemcpyHostToDevice, s), "H2D");
       check(cudaMemcpyAsync(eng->ntype_e, neigh_types, sizeof(int) * num_edges, cudaMemcpyHostToDevice, s), "H2D");
       check(cudaMemcpyAsync(eng->xyz, xyz, sizeof(double) * 3 * num_edges, cudaMemcpyHostToDevice, s), "H2D");
       check(cudaMemcpyAsync(eng->r, r, sizeof(double) * num_edges, cudaMemcpyHostToDevice, s), "H2D");
     }
+    if (num_nodes > 0)
+      smx::launch_scan_first(eng->nneigh, num_nodes, eng->first, s);
+    else
+      check(cudaMemsetAsync(eng->first, 0, sizeof(int), s), "cudaMemsetAsync");
+    *reinterpret_cast<volatile unsigned*>(eng->check_host) = 0;
+    smx::launch_validate_inputs(num_nodes, num_edges, S, rc, eng->ntype, eng->nneigh, eng->first, eng->nidx,
+                                eng->ntype_e, eng->xyz, eng->r, eng->check_dev, s);
+    check(cudaStreamSynchronize(s), "input check");
+    const unsigned bad = *reinterpret_cast<volatile unsigned*>(eng->check_host);
+    if (bad & smx::kBadNodeType) return fail(SMX_ERR_INVALID, "node_types out of range");
+    if (bad & smx::kBadNumNeigh) return fail(SMX_ERR_INVALID, "negative num_neigh");
+    if (bad & smx::kBadEdgeCount) return fail(SMX_ERR_INVALID, "sum(num_neigh) != num_edges");
+    if (bad & smx::kBadNeighIndex) return fail(SMX_ERR_INVALID, "neigh_indices out of range (must be < num_nodes)");
+    if (bad & smx::kBadNeighType) return fail(SMX_ERR_INVALID, "neigh_types out of range");
+    if (bad & smx::kBadEdge)
+      return fail(SMX_ERR_INVALID, "edge length outside (0, r_cut) or non-finite edge vector");
     smx::EdgeIn in{eng->first, eng->ntype, eng->nidx, eng->ntype_e, eng->xyz, eng->r, num_nodes};
     eng->run(in, eng->energies, eng->forces, s);
     if (num_nodes > 0)

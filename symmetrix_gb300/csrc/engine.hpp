@@ -56,6 +56,9 @@ struct smx_engine {
   // reads it after a synchronisation without a copy)
   unsigned* status_host = nullptr;
   unsigned* status_dev = nullptr;
+  // flags of the device-side input check of the host-pointer call (mapped, as above)
+  unsigned* check_host = nullptr;
+  unsigned* check_dev = nullptr;
   // precision form: bf16 B operands (K contiguous) of the tensor-core GEMMs
   // (K contiguous, `tc_terms` bf16 split terms concatenated along K: see tc_operand)
   const __nv_bfloat16 *W_H1 = nullptr, *W_M0adj = nullptr, *W_A1[4] = {}, *W_Phi1adj[4] = {};
@@ -84,6 +87,7 @@ struct smx_engine {
   float* zbl_e = nullptr;  // per-node ZBL energy
   int *first = nullptr, *ntype = nullptr, *nidx = nullptr, *ntype_e = nullptr;
   int* atom_order = nullptr;  // centre atoms sorted by species (when species_order is on)
+  int* nneigh = nullptr;      // num_neigh of the host-pointer call
   double *xyz = nullptr, *r = nullptr, *energies = nullptr, *forces = nullptr;
   int lastN = 0;
 
@@ -237,7 +241,7 @@ struct smx_engine {
   void free_workspace() {
     void* ps[] = {A0, M0, H1, Phi1, A1, M1, H2, A0_adj, M0_adj, H1_adj, Phi1_adj, A1_adj, M1_adj, H2_adj, f1,
                   first, ntype, nidx, ntype_e, xyz, r, energies, forces, M0_bf, Phi1_bf, A1adj_bf, H1adj_bf,
-                  atom_order};
+                  atom_order, nneigh};
     for (void* p : ps)
       if (p) cudaFree(p);
     A0 = M0 = H1 = Phi1 = A1 = M1 = H2 = A0_adj = M0_adj = H1_adj = Phi1_adj = A1_adj = M1_adj = H2_adj = nullptr;
@@ -251,7 +255,7 @@ struct smx_engine {
     f1 = nullptr;
     if (zbl_e) cudaFree(zbl_e);
     zbl_e = nullptr;
-    first = ntype = nidx = ntype_e = atom_order = nullptr;
+    first = ntype = nidx = ntype_e = atom_order = nneigh = nullptr;
     xyz = r = energies = forces = nullptr;
     capN = capE = 0;
   }
@@ -288,6 +292,7 @@ struct smx_engine {
     energies = dalloc<double>(nN);
     forces = dalloc<double>(3 * nE);
     atom_order = dalloc<int>(nN);
+    nneigh = dalloc<int>(nN);
     if (precision == SMX_PRECISION_BF16) {
       const long T = tc_terms;
       M0_bf = dalloc<__nv_bfloat16>(T * nN * dm.nLM * C);

@@ -8,6 +8,8 @@
 //                  reverse_H2 (:834-874), reverse_M1 (:779-794)
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "device.cuh"
 #include "kernels.h"
 #include "poly_canon.h"
@@ -287,6 +289,43 @@ __global__ void __launch_bounds__(1024) k_species_order(const int* __restrict__ 
 void launch_species_order(const int* node_type, int N, int S, int* order, cudaStream_t s) {
   if (N <= 0) return;
   k_species_order<<<1, 1024, sizeof(int) * S, s>>>(node_type, N, S, order);
+}
+
+// The host API's input check, on the device: flags (a mapped host word) receive one bit
+// per violated condition (kBad* in kernels.h); first[] must already be the scan of
+// num_neigh.  Grid-stride over max(N, E).
+__global__ void k_validate_inputs(int N, long E, int S, double r_cut, const int* __restrict__ node_types,
+                                  const int* __restrict__ num_neigh, const int* __restrict__ first,
+                                  const int* __restrict__ nidx, const int* __restrict__ ntype_e,
+                                  const double* __restrict__ xyz, const double* __restrict__ r,
+                                  unsigned* __restrict__ flags) {
+  unsigned bad = 0;
+  const long n = E > N ? E : N;
+  for (long t = blockIdx.x * static_cast<long>(blockDim.x) + threadIdx.x; t < n;
+       t += static_cast<long>(gridDim.x) * blockDim.x) {
+    if (t < N) {
+      if (node_types[t] < 0 || node_types[t] >= S) bad |= kBadNodeType;
+      if (num_neigh[t] < 0) bad |= kBadNumNeigh;
+    }
+    if (t < E) {
+      if (nidx[t] < 0 || nidx[t] >= N) bad |= kBadNeighIndex;
+      if (ntype_e[t] < 0 || ntype_e[t] >= S) bad |= kBadNeighType;
+      const double re = r[t];
+      if (!(re > 0.0 && re < r_cut) || !isfinite(xyz[3 * t]) || !isfinite(xyz[3 * t + 1]) || !isfinite(xyz[3 * t + 2]))
+        bad |= kBadEdge;
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0 && static_cast<long>(first[N]) != E) bad |= kBadEdgeCount;
+  bad = __reduce_or_sync(0xffffffffu, bad);
+  if ((threadIdx.x & 31) == 0 && bad) atomicOr(flags, bad);
+}
+
+void launch_validate_inputs(int N, long E, int S, double r_cut, const int* node_types, const int* num_neigh,
+                            const int* first, const int* nidx, const int* ntype_e, const double* xyz, const double* r,
+                            unsigned* flags, cudaStream_t s) {
+  const long n = E > N ? E : N;
+  const int grid = static_cast<int>(std::min<long>(ceil_div(n > 0 ? n : 1, 256), 152L * 8));
+  k_validate_inputs<<<grid, 256, 0, s>>>(N, E, S, r_cut, node_types, num_neigh, first, nidx, ntype_e, xyz, r, flags);
 }
 
 // first[0] = 0, first[i+1] = first[i] + num_neigh[i]; one block, sequential tiles.

@@ -51,6 +51,12 @@ void launch_node_tail(const DevModel& m, const int* node_type, int N, float* A1,
                       float* H2, float* A1_adj, float* H1_adj, float* M1_adj, float* H2_adj, const float* zbl_e,
                       double* energies, cudaStream_t s);
 void launch_scan_first(const int* num_neigh, int N, int* first, cudaStream_t s);
+// input check of the host API (bits of the flags word)
+constexpr unsigned kBadNodeType = 1, kBadNumNeigh = 2, kBadEdgeCount = 4, kBadNeighIndex = 8, kBadNeighType = 16,
+                   kBadEdge = 32;
+void launch_validate_inputs(int N, long E, int S, double r_cut, const int* node_types, const int* num_neigh,
+                            const int* first, const int* nidx, const int* ntype_e, const double* xyz, const double* r,
+                            unsigned* flags, cudaStream_t s);
 // order[N]: the atoms sorted by species (node_type in [0, S))
 void launch_species_order(const int* node_type, int N, int S, int* order, cudaStream_t s);
 

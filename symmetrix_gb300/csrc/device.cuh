@@ -189,7 +189,11 @@ struct EdgeIn {
   // identity.  A species-sorted order keeps the spline rows the blocks in flight gather
   // (the pairs of one centre species) inside L2 when the whole table is larger.
   const int* order = nullptr;
+  // End of each centre atom's edges (nullptr: first[i + 1]): a list whose segments are
+  // only partly filled, e.g. the in-cut-off edges packed at the front of a skin list's.
+  const int* last = nullptr;
   __device__ __forceinline__ int atom_at(int b) const { return order ? order[b] : b; }
+  __device__ __forceinline__ int end(int i) const { return last ? last[i] : first[i + 1]; }
 };
 
 // Canonical layer-1 tensor-product instructions (l1 from Y_lm, l2 from H1),
@@ -384,7 +388,7 @@ __device__ __forceinline__ float block_sum(float v) {
 // compute_A1_scaled, libsymmetrix/source/mace.cpp:273-297, :681-705).
 __device__ __forceinline__ float dens_factor(const DevModel& m, int layer, const EdgeIn& in, int i, int ti) {
   float z = 0.0f;
-  for (int e = in.first[i] + threadIdx.x; e < in.first[i + 1]; e += blockDim.x) {
+  for (int e = in.first[i] + threadIdx.x; e < in.end(i); e += blockDim.x) {
     float v, d;
     dens_eval(m, layer, ti, in.ntype_e[e], static_cast<float>(in.r[e]), v, d);
     z += v;

@@ -104,7 +104,7 @@ __device__ __forceinline__ void layer0_fwd_atom(const DevModel& m, const EdgeIn&
   const bool live = lt < C2;
   const int cp = live ? lt : 0, kc = 2 * cp;
   const int ti = in.node_type[i];
-  const int e0 = in.first[i], e1 = in.first[i + 1];
+  const int e0 = in.first[i], e1 = in.end(i);
   float2 acc[16];
 #pragma unroll
   for (int q = 0; q < 16; ++q) acc[q] = make_float2(0.0f, 0.0f);
@@ -323,7 +323,7 @@ __device__ __forceinline__ void layer0_rev_atom(const DevModel& m, const EdgeIn&
   const int cp = live ? threadIdx.x : 0, kc = 2 * cp;  // this thread's channel pair
   const int nwarp = blockDim.x >> 5;
   const int ti = in.node_type[i];
-  const int e0 = in.first[i], e1 = in.first[i + 1];
+  const int e0 = in.first[i], e1 = in.end(i);
   float2 dA[16];
 #pragma unroll
   for (int q = 0; q < 16; ++q)

@@ -296,7 +296,7 @@ __device__ __forceinline__ void layer1_fwd_atom(const DevModel& m, const EdgeIn&
   const int C = CT > 0 ? CT : m.C;
   const int k = threadIdx.x;
   const int ti = in.node_type[i];
-  const int e0 = in.first[i], e1 = in.first[i + 1];
+  const int e0 = in.first[i], e1 = in.end(i);
   float acc[NP];
 #pragma unroll
   for (int p = 0; p < NP; ++p) acc[p] = 0.0f;
@@ -386,7 +386,7 @@ __device__ __forceinline__ void layer1_rev_atom(const DevModel& m, const EdgeIn&
   const Lane2 L = lane2(C, half);
   const int nwarp = blockDim.x >> 5;
   const int ti = in.node_type[i];
-  const int e0 = in.first[i], e1 = in.first[i + 1];
+  const int e0 = in.first[i], e1 = in.end(i);
   // sP[p][k] = sum_lme CG[lme,p] dPhi1[i,lme,k], one channel per thread
   float* sD = dyn;                 // [n_lme][C]
   float* sP = dyn + m.n_lme * C;   // [NP][C]
@@ -560,7 +560,7 @@ __device__ __forceinline__ void layer1_fwd_l2_atom(const DevModel& m, const Edge
   const bool live = kk < CH && h * CH + kk < C;
   const int k = live ? h * CH + kk : 0;
   const int ti = in.node_type[i];
-  const int e0 = in.first[i], e1 = in.first[i + 1];
+  const int e0 = in.first[i], e1 = in.end(i);
   float acc[kL2MaxNp];
 #pragma unroll
   for (int p = 0; p < kL2MaxNp; ++p) acc[p] = 0.0f;
@@ -719,7 +719,7 @@ __device__ __forceinline__ void layer1_rev_l2_atom(const DevModel& m, const Edge
   const int k = live ? h * CH + kk : 0;
   const int nwarp = blockDim.x >> 5;
   const int ti = in.node_type[i];
-  const int e0 = in.first[i], e1 = in.first[i + 1];
+  const int e0 = in.first[i], e1 = in.end(i);
   float* sD = dyn;                  // [n_lme][CH]
   float* sP = dyn + m.n_lme * CH;   // [NP][CH]
   // sP[p][k] = sum_lme CG[lme,p] dPhi1[i,lme,k]: rows split over the four groups

@@ -223,6 +223,72 @@ __global__ void k_edge_geometry(long cap, int N, const int* __restrict__ first, 
   r[e] = sqrt(dx * dx + dy * dy + dz * dz);
 }
 
+// Edge geometry of a skin list at the current positions, and its in-cut-off edges
+// packed to the front of each centre atom's segment: one warp per atom, ballot ranks
+// (list order kept, deterministic).  Atom a's packed edges are [first[a], last[a]) of
+// the packed arrays (emap: their skin-list index); the skin-list forces of edges at or
+// beyond r_cut are zeroed here, those inside are scattered back after the evaluation.
+__global__ void k_edge_geometry_packed(int N, const int* __restrict__ first, const double* __restrict__ pos,
+                                       double3 box, const int* __restrict__ nidx, const int* __restrict__ ntype_e,
+                                       const char4* __restrict__ shift, double r_cut, double* __restrict__ xyz,
+                                       double* __restrict__ r, double* __restrict__ f_skin, int* __restrict__ last,
+                                       int* __restrict__ emap, int* __restrict__ nidx_p, int* __restrict__ ntype_p,
+                                       double* __restrict__ xyz_p, double* __restrict__ r_p) {
+  const int a = static_cast<int>((static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (a >= N) return;
+  const int e0 = first[a], e1 = first[a + 1];
+  const double px = pos[3 * a], py = pos[3 * a + 1], pz = pos[3 * a + 2];
+  int count = 0;
+  for (int base = e0; base < e1; base += 32) {
+    const int e = base + lane;
+    bool active = false;
+    double dx = 0.0, dy = 0.0, dz = 0.0, re = 0.0;
+    int j = 0;
+    if (e < e1) {
+      j = nidx[e];
+      const char4 sh = shift[e];
+      dx = pos[3 * j] + sh.x * box.x - px;
+      dy = pos[3 * j + 1] + sh.y * box.y - py;
+      dz = pos[3 * j + 2] + sh.z * box.z - pz;
+      re = sqrt(dx * dx + dy * dy + dz * dz);
+      xyz[3 * static_cast<long>(e)] = dx;
+      xyz[3 * static_cast<long>(e) + 1] = dy;
+      xyz[3 * static_cast<long>(e) + 2] = dz;
+      r[e] = re;
+      active = re < r_cut;
+      if (!active)
+        for (int c = 0; c < 3; ++c) f_skin[3 * static_cast<long>(e) + c] = 0.0;
+    }
+    const unsigned ball = __ballot_sync(0xffffffffu, active);
+    if (active) {
+      const long q = e0 + count + __popc(ball & ((1u << lane) - 1u));
+      emap[q] = e;
+      nidx_p[q] = j;
+      ntype_p[q] = ntype_e[e];
+      xyz_p[3 * q] = dx;
+      xyz_p[3 * q + 1] = dy;
+      xyz_p[3 * q + 2] = dz;
+      r_p[q] = re;
+    }
+    count += __popc(ball);
+  }
+  if (lane == 0) last[a] = e0 + count;
+}
+
+// skin-list forces of the packed edges: f_skin[emap[e]] = f_p[e]; one warp per atom
+__global__ void k_scatter_packed_forces(int N, const int* __restrict__ first, const int* __restrict__ last,
+                                        const int* __restrict__ emap, const double* __restrict__ f_p,
+                                        double* __restrict__ f_skin) {
+  const int a = static_cast<int>((static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (a >= N) return;
+  for (int e = first[a] + lane; e < last[a]; e += 32) {
+    const long q = emap[e];
+    for (int c = 0; c < 3; ++c) f_skin[3 * q + c] = f_p[3 * static_cast<long>(e) + c];
+  }
+}
+
 // F_a = sum_{e in out(a)} (f[rev e] - f[e]); one thread per atom, no atomics
 __global__ void k_atom_forces(int N, const int* __restrict__ first, const int* __restrict__ rev,
                               const double* __restrict__ f, double* __restrict__ F) {
@@ -343,6 +409,20 @@ void launch_reverse_edges(long cap, int N, const int* first, const int* nidx, co
 void launch_edge_geometry(long cap, int N, const int* first, const double* pos, double3 box, const int* nidx,
                           const int* edge_i, const char4* shift, double* xyz, double* r, cudaStream_t s) {
   if (cap > 0) k_edge_geometry<<<ceil_div(cap, 256), 256, 0, s>>>(cap, N, first, pos, box, nidx, edge_i, shift, xyz, r);
+}
+
+void launch_edge_geometry_packed(int N, const int* first, const double* pos, double3 box, const int* nidx,
+                                 const int* ntype_e, const char4* shift, double r_cut, double* xyz, double* r,
+                                 double* f_skin, int* last, int* emap, int* nidx_p, int* ntype_p, double* xyz_p,
+                                 double* r_p, cudaStream_t s) {
+  if (N > 0)
+    k_edge_geometry_packed<<<ceil_div(N, 4), 128, 0, s>>>(N, first, pos, box, nidx, ntype_e, shift, r_cut, xyz, r,
+                                                          f_skin, last, emap, nidx_p, ntype_p, xyz_p, r_p);
+}
+
+void launch_scatter_packed_forces(int N, const int* first, const int* last, const int* emap, const double* f_p,
+                                  double* f_skin, cudaStream_t s) {
+  if (N > 0) k_scatter_packed_forces<<<ceil_div(N, 4), 128, 0, s>>>(N, first, last, emap, f_p, f_skin);
 }
 
 void launch_atom_forces(int N, const int* first, const int* rev, const double* f, double* F, cudaStream_t s) {

@@ -106,6 +106,13 @@ void launch_reverse_edges(long cap, int N, const int* first, const int* nidx, co
                           int* rev, cudaStream_t s);
 void launch_edge_geometry(long cap, int N, const int* first, const double* pos, double3 box, const int* nidx,
                           const int* edge_i, const char4* shift, double* xyz, double* r, cudaStream_t s);
+// skin-list geometry plus the in-cut-off edges packed per centre atom (see k_md.cu)
+void launch_edge_geometry_packed(int N, const int* first, const double* pos, double3 box, const int* nidx,
+                                 const int* ntype_e, const char4* shift, double r_cut, double* xyz, double* r,
+                                 double* f_skin, int* last, int* emap, int* nidx_p, int* ntype_p, double* xyz_p,
+                                 double* r_p, cudaStream_t s);
+void launch_scatter_packed_forces(int N, const int* first, const int* last, const int* emap, const double* f_p,
+                                  double* f_skin, cudaStream_t s);
 void launch_atom_forces(int N, const int* first, const int* rev, const double* f, double* F, cudaStream_t s);
 void launch_reduce(int N, const int* first, const double* energies, const double* xyz, const double* f,
                    double* partial, int nblocks, double* out, cudaStream_t s);

@@ -27,28 +27,34 @@ struct NeighList {
   int *num_neigh = nullptr, *first = nullptr, *nidx = nullptr, *ntype_e = nullptr, *edge_i = nullptr, *rev = nullptr;
   char4* shift = nullptr;
   double *xyz = nullptr, *r = nullptr, *forces = nullptr;
+  // the edges inside the cut-off, packed per centre atom each step (a skin list)
+  int *last = nullptr, *emap = nullptr, *nidx_p = nullptr, *ntype_p = nullptr;
+  double *xyz_p = nullptr, *r_p = nullptr, *forces_p = nullptr;
   long E = 0;
   bool realloc_happened = false;
 
   ~NeighList() { release(); }
   void release() {
-    void* ps[] = {cell, cell_count, cell_start, cell_fill, cell_atoms, num_neigh, first, nidx, ntype_e, edge_i, rev,
-                  shift, xyz, r, forces};
+    void* ps[] = {cell,  cell_count, cell_start, cell_fill, cell_atoms, num_neigh, first, nidx,  ntype_e,
+                  edge_i, rev,       shift,      xyz,       r,          forces,    last,  emap,  nidx_p,
+                  ntype_p, xyz_p,    r_p,        forces_p};
     for (void* p : ps)
       if (p) cudaFree(p);
     cell = cell_count = cell_start = cell_fill = cell_atoms = num_neigh = first = nidx = ntype_e = edge_i = rev = nullptr;
+    last = emap = nidx_p = ntype_p = nullptr;
     shift = nullptr;
-    xyz = r = forces = nullptr;
+    xyz = r = forces = xyz_p = r_p = forces_p = nullptr;
     capN = ncell_cap = 0;
     capE = 0;
   }
   void reserve_nodes(int N, int ncell) {
     if (N > capN) {
-      for (int** p : {&cell, &num_neigh, &first})
+      for (int** p : {&cell, &num_neigh, &first, &last})
         if (*p) cudaFree(*p);
       cell = dalloc<int>(N);
       num_neigh = dalloc<int>(N);
       first = dalloc<int>(N + 1);
+      last = dalloc<int>(N);
       capN = N;
       realloc_happened = true;
     }
@@ -65,7 +71,7 @@ struct NeighList {
   void reserve_edges(long E_) {
     if (E_ <= capE) return;
     const long nE = static_cast<long>(E_ * 1.25) + 1024;
-    void* ps[] = {nidx, ntype_e, edge_i, rev, shift, xyz, r, forces};
+    void* ps[] = {nidx, ntype_e, edge_i, rev, shift, xyz, r, forces, emap, nidx_p, ntype_p, xyz_p, r_p, forces_p};
     for (void* p : ps)
       if (p) cudaFree(p);
     nidx = dalloc<int>(nE);
@@ -76,6 +82,12 @@ struct NeighList {
     xyz = dalloc<double>(3 * nE);
     r = dalloc<double>(nE);
     forces = dalloc<double>(3 * nE);
+    emap = dalloc<int>(nE);
+    nidx_p = dalloc<int>(nE);
+    ntype_p = dalloc<int>(nE);
+    xyz_p = dalloc<double>(3 * nE);
+    r_p = dalloc<double>(nE);
+    forces_p = dalloc<double>(3 * nE);
     capE = nE;
     realloc_happened = true;
   }
@@ -185,10 +197,22 @@ struct smx_md {
     return smx::EdgeIn{nl.first, species, nl.nidx, nl.ntype_e, nl.xyz, nl.r, N};
   }
 
-  // forces at the current positions (geometry + evaluator + scatter); graph-capturable
+  // forces at the current positions (geometry + evaluator + scatter); graph-capturable.
+  // With a skin the evaluator sees only the edges inside the cut-off, packed per atom
+  // (the skin edges would cost it ~5% of its time), and their forces go back to the
+  // skin list, whose reverse-edge map gives the atomic forces.
   void forces(cudaStream_t s) {
-    smx::launch_edge_geometry(nl.capE, N, nl.first, pos, box, nl.nidx, nl.edge_i, nl.shift, nl.xyz, nl.r, s);
-    eng->run(edges(), energies, nl.forces, s);
+    if (skin > 0.0) {
+      smx::launch_edge_geometry_packed(N, nl.first, pos, box, nl.nidx, nl.ntype_e, nl.shift, eng->hm.r_cut, nl.xyz,
+                                       nl.r, nl.forces, nl.last, nl.emap, nl.nidx_p, nl.ntype_p, nl.xyz_p, nl.r_p, s);
+      smx::EdgeIn in{nl.first, species, nl.nidx_p, nl.ntype_p, nl.xyz_p, nl.r_p, N};
+      in.last = nl.last;
+      eng->run(in, energies, nl.forces_p, s);
+      smx::launch_scatter_packed_forces(N, nl.first, nl.last, nl.emap, nl.forces_p, nl.forces, s);
+    } else {
+      smx::launch_edge_geometry(nl.capE, N, nl.first, pos, box, nl.nidx, nl.edge_i, nl.shift, nl.xyz, nl.r, s);
+      eng->run(edges(), energies, nl.forces, s);
+    }
     smx::launch_atom_forces(N, nl.first, nl.rev, nl.forces, F, s);
   }
 

@@ -534,13 +534,14 @@ def gpu_arm(args, rank, world, local_rank):
         return {n_: {"ms": a[n_], "gflop": costs[n_][0] / 1e9, "tflops": costs[n_][0] / (a[n_] / 1e3) / 1e12,
                      "gbs": costs[n_][1] / (a[n_] / 1e3) / 1e9} for n_ in a}
 
-    # kernels per MD step of the BF16 form: vv_first, edge_geometry, atom_forces, vv_second and 11
+    # kernels per MD step of the BF16 form: vv_first, edge geometry with the in-cut-off packing,
+    # the scatter of the packed forces, atom_forces, vv_second and 11
     # evaluation kernels (layer0_fwd, layer1_fwd, node_tail, layer1_rev, contract0_rev, layer0_rev,
     # four grouped tcgen05 GEMM launches: H1, A1 (all l), Phi1_adj (all l), M0_adj, and the bf16
     # conversion of H1_adj), one more when the centre atoms are species-sorted; plus per rebuild:
     # wrap, 4 cell-list kernels, 2 neighbour passes, scan, reverse map
     rebuilds = (args.warmup + args.steps + 9) // 10 - (args.warmup + 9) // 10
-    per_step = 4 + 11 + (1 if eng.get_option("species_order") == 1 else 0)
+    per_step = 5 + 11 + (1 if eng.get_option("species_order") == 1 else 0)
     launches = per_step * args.steps + 9 * rebuilds
     fp = forms["fp32"]
     line = {

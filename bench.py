@@ -282,6 +282,22 @@ def form_errors(eng, sample):
             "sample": f"{n}-atom box of the same model, density and species mix, vs the float64 oracle"}
 
 
+def cpu_model():
+    """The host CPU as /proc/cpuinfo names it (model name, or implementer/part on Arm)."""
+    import platform
+    fields = {}
+    try:
+        for line in open("/proc/cpuinfo"):
+            if ":" in line:
+                k, v = (x.strip() for x in line.split(":", 1))
+                fields.setdefault(k, v)
+    except OSError:
+        pass
+    name = fields.get("model name") or " ".join(f"{k} {fields[k]}" for k in ("CPU implementer", "CPU part")
+                                                if k in fields)
+    return f"{platform.machine()} {name}".strip()
+
+
 def reference_arm(args, rank, world):
     if rank != 0:
         return
@@ -315,7 +331,8 @@ def reference_arm(args, rank, world):
         "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD["name"], "atoms_per_step": n * threads, "threads": threads},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample,
+                         "cpu": cpu_model()},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
 
@@ -497,7 +514,7 @@ def gpu_arm(args, rank, world, local_rank):
 
     # ---- CPU baseline (the oracle, one thread, bounded sample) and the error report ----
     kind, cpu_val, cpu_dt, cpu_edges, sample = cpu_rate(path, 1, 2, WORKLOAD["cpu_sample_atoms"])
-    cpu = {"value": cpu_val, "unit": UNIT, "cores": 1, "kind": kind,
+    cpu = {"value": cpu_val, "unit": UNIT, "cores": 1, "kind": kind, "cpu": cpu_model(),
            "sample": f"median of 2 E+F evaluations of a {WORKLOAD['cpu_sample_atoms']}-atom box of the same model, "
                      f"density and species mix ({cpu_edges} edges), float64, 1 thread"}
     for form in forms.values():

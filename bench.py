@@ -393,7 +393,8 @@ ATOM_KERNELS = ("layer0_fwd", "contract0_rev", "layer0_rev", "layer1_fwd", "laye
 def schedule_of(eng):
     """The autotuned schedule the engine ran with: per-atom kernels on persistent grids, GEMM tiles."""
     mask = eng.get_option("persistent")
-    out = {"persistent_kernels": [k for b, k in enumerate(ATOM_KERNELS) if mask >> b & 1]}
+    out = {"persistent_kernels": [k for b, k in enumerate(ATOM_KERNELS) if mask >> b & 1],
+           "species_order": eng.get_option("species_order"), "l2_channel_slices": eng.get_option("l2_split")}
     if eng.precision == "bfloat16":
         out["gemm"] = eng.gemm_schedule()
     return out

@@ -107,10 +107,12 @@ long smx_get_stage(smx_engine* eng, const char* name, double* out, long cap);
 /* Options: "keep_stages" (keep A0_adj for smx_get_stage), "profile" (record CUDA
  * events between the kernels of every evaluation); "autotune" (1, the default: the
  * first evaluation outside a stream capture picks, per per-atom kernel, one block per
- * atom or a persistent grid of resident blocks claiming atoms from a counter, by timing
- * whole passes in both, and in the BF16 form times the candidate N-tile widths and TMA
- * ring depths of each tensor-core GEMM group on its own operands; setting it again
- * re-tunes; 0 keeps the defaults: one block per atom, default GEMM schedule);
+ * atom or a persistent grid of resident blocks claiming atoms from a counter, and for
+ * L_max = 2 models of 64 or more channels one or two channel slices per node in the
+ * layer-1 kernels, by timing whole passes; in the BF16 form it times the candidate N-tile
+ * widths and TMA ring depths of each tensor-core GEMM group on its own operands; setting
+ * it again re-tunes; 0 keeps the defaults: one block per atom, two channel slices,
+ * default GEMM schedule);
  * "persistent" (-1: tuned as above, 0: one block per atom, 1: persistent grids);
  * "species_order" (-1, the default: the edge kernels take the centre atoms sorted by
  * species when a layer's spline table exceeds 64 MB, so the rows in use stay in L2;
@@ -124,7 +126,9 @@ int smx_set_option(smx_engine* eng, const char* key, long value);
  * per-atom kernel k (layer0_fwd, contract0_rev, layer0_rev, layer1_fwd, layer1_rev,
  * node_tail) runs as a persistent grid; "species_order": 1 when the sorted order is in
  * effect; "poly_canon": 1 when the model's symmetric-contraction monomials are the
- * canonical sets and run as generated code, 0 for the data-driven path); -1 if unknown. */
+ * canonical sets and run as generated code, 0 for the data-driven path; "l2_split": channel
+ * slices per node of the L_max = 2 layer-1 kernels, 1 or 2, picked by the autotuner); -1 if
+ * unknown. */
 long smx_get_option(const smx_engine* eng, const char* key);
 
 /* The engine's own CUDA stream (a cudaStream_t): host-pointer calls and the MD driver

@@ -178,6 +178,7 @@ long smx_get_option(const smx_engine* eng, const char* key) {
   if (k == "persistent") return eng->sched_mask();  // bit k: per-atom kernel k runs persistent
   if (k == "species_order") return eng->order_species() ? 1 : 0;  // in effect
   if (k == "poly_canon") return eng->dm.poly_canon;  // 1: generated polynomial kernels
+  if (k == "l2_split") return eng->dm.l2_split;       // channel slices of the L_max = 2 layer-1 kernels
   static const char* groups[4] = {"H1", "A1", "Phi1_adj", "M0_adj"};
   for (int q = 0; q < 4; ++q) {
     if (k == std::string("tc_nt_") + groups[q]) return eng->tc_cfg[q].NT ? eng->tc_cfg[q].NT : eng->dm.C;

@@ -186,7 +186,8 @@ struct smx_engine {
     m.tc_terms = tc_terms;
     // two blocks per node (half the channels each) let two L_max = 2 layer-1 blocks share
     // an SM: one computes while the other waits at a barrier
-    m.l2_split = (pm.L_max == 2 && pm.C >= 64) ? 2 : 1;
+    l2_split_max = (pm.L_max == 2 && pm.C >= 64) ? 2 : 1;
+    m.l2_split = l2_split_max;
     m.f1_stride = 0;
     m.zbl_p = pm.zbl_p;
     for (int q = 0; q < 4; ++q) m.zbl_c[q] = pm.zbl_c[q];
@@ -280,8 +281,8 @@ struct smx_engine {
     M1_adj = dalloc<float>(nN * C);
     H2_adj = dalloc<float>(nN * C);
     // L_max = 2 with two channel slices: one f1 slice each
-    dm.f1_stride = dm.l2_split > 1 ? 3 * nE : 0;
-    f1 = dalloc<double>(3 * nE * dm.l2_split);
+    dm.f1_stride = l2_split_max > 1 ? 3 * nE : 0;
+    f1 = dalloc<double>(3 * nE * l2_split_max);
     zbl_e = dalloc<float>(nN);
     first = dalloc<int>(nN + 1);
     ntype = dalloc<int>(nN);
@@ -428,12 +429,27 @@ struct smx_engine {
   // (alternating, two passes each, per-stage CUDA events) and keeps the faster per
   // kernel; the two layer-0 adjoint kernels share one stage and are switched together.
   int pfull[smx::kAkCount] = {};
+  // L_max = 2 layer-1 kernels: channel slices per node, 1 or (from 64 channels) 2, tuned
+  int l2_split_max = 1;
   int sched_force = -1;  // -1: tune; 0: one block per atom; 1: persistent
   bool sched_tuned = false;
   float sched_stage_us[2][kStages] = {};
 
   void sched_set(int mode) {
     for (int k = 0; k < smx::kAkCount; ++k) dm.pgrid[k] = mode ? pfull[k] : 0;
+  }
+
+  // the persistent grids of the layer-1 kernels follow their block shape
+  void set_l2_split(int ns) {
+    dm.l2_split = ns;
+    int nsm = 0, per_sm[smx::kAkCount] = {};
+    check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device), "cudaDeviceGetAttribute");
+    smx::layer1_residency(dm, per_sm);
+    for (int k : {smx::kAkLayer1Fwd, smx::kAkLayer1Rev}) {
+      const bool on = dm.pgrid[k] > 0;
+      pfull[k] = per_sm[k] * nsm;
+      if (on) dm.pgrid[k] = pfull[k];
+    }
   }
 
   void tune_sched(const smx::EdgeIn& in, double* out_e, double* out_f, cudaStream_t s) {
@@ -460,6 +476,20 @@ struct smx_engine {
     }
     for (int mode = 0; mode < 2; ++mode)
       for (int q = 0; q < kStages; ++q) sched_stage_us[mode][q] = best[mode][q] * 1000.0f;
+    if (l2_split_max > 1) {  // channel slices of the L_max = 2 layer-1 kernels: stages 2 and 6
+      float t[3] = {1e30f, 1e30f, 1e30f};
+      for (int rep = 0; rep < 2; ++rep)
+        for (int ns = 1; ns <= l2_split_max; ++ns) {
+          set_l2_split(ns);
+          run_pass(in, out_e, out_f, s);
+          check(cudaEventSynchronize(ev[kStages]), "autotune");
+          float a = 0.0f, b = 0.0f;
+          check(cudaEventElapsedTime(&a, ev[2], ev[3]), "cudaEventElapsedTime");
+          check(cudaEventElapsedTime(&b, ev[6], ev[7]), "cudaEventElapsedTime");
+          t[ns] = std::min(t[ns], a + b);
+        }
+      set_l2_split(t[1] <= t[2] ? 1 : 2);
+    }
     profile = prof;
     sched_tuned = true;
   }

@@ -272,6 +272,7 @@ def test_lmax2_wide_model(engine_lib, tmp_path):
     for precision, tol in (("float32", F_TOL), ("bfloat16", 1e-2)):
         m = _engine(path, precision=precision)
         m.compute_node_energies_forces(*edge_args(species, nl))
+        assert m.get_option("l2_split") in (1, 2)  # tuned on the first evaluation
         F = atomic_forces(96, nl["i"], nl["neigh_indices"], m.node_forces)
         assert _report(f"{precision} E_i", m.node_energies, ref.node_energies) < (E_TOL if tol == F_TOL else 5e-3)
         assert _report(f"{precision} F_atom", F, Fr) < tol

@@ -4,7 +4,10 @@
 //   k_layer1_fwd : compute_R1 + compute_Phi1 (:92-116, :453-502)
 //   k_layer1_rev : reverse_Phi1 (:504-605)
 //
-// The adjoint (the costlier kernel): one thread block per centre node i.  A thread owns a channel pair (2c, 2c+1) and
+// Every kernel works on one centre node at a time: one block per node, or a persistent
+// grid claiming nodes (AtomCursor), in the order EdgeIn::atom_at gives.
+//
+// The adjoint (the costlier kernel): a thread owns a channel pair (2c, 2c+1) and
 // one half of the layer-1 instructions: the block is two groups of HW threads
 // (HW = C/2 rounded up to a warp), group 0 runs the instructions of half 0 and
 // group 1 those of half 1, so the split is warp-uniform.  All per-channel
@@ -17,6 +20,10 @@
 // instruction, two planes of C/2 float4: plane 0 = (c0, c0', c1, c1') and plane 1 =
 // (c2, c2', c3, c3'), ' marking the odd channel of the pair, so that every cubic
 // coefficient pair is one aligned float2 operand.
+//
+// L_max = 2 (17 instructions, 243 paths): four instruction groups, one channel per
+// thread, scalar FMAs; from 64 channels each node's channels are split over two blocks
+// (DevModel::l2_split) so that two blocks share an SM.
 #include <cuda_runtime.h>
 
 #include "device.cuh"
@@ -549,7 +556,7 @@ __device__ __forceinline__ void l2_load_g(const float* sP, int C, int k, float* 
 }  // namespace
 
 // Layer-1 forward, L_max = 2: slice h of the channels of node i (channels h*CH ..
-// h*CH + CH - 1, CH = l2_slice_width(C)); four groups of CH threads, group G running the
+// h*CH + CH - 1, CH = l2_slice_width(m)); four groups of CH threads, group G running the
 // instructions of group G.
 __device__ __forceinline__ void layer1_fwd_l2_atom(const DevModel& m, const EdgeIn& in, const float* __restrict__ H1,
                                                    float* __restrict__ Phi1, int i, int h) {

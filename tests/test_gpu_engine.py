@@ -363,3 +363,27 @@ def test_lmax2_data_driven_polynomials(engine_lib, tmp_path):
     ref.compute_node_energies_forces(*edge_args(species, nl))
     assert _report("E_i", m.node_energies, ref.node_energies) < E_TOL
     assert _report("f_edge", m.node_forces, ref.node_forces) < F_TOL
+
+
+@pytest.mark.parametrize("L_max", [1, 2])
+def test_rotation_invariance_on_gpu(engine_lib, tmp_path, L_max):
+    """The CUDA path: energies invariant and atomic forces covariant under O(3) (float32
+    tolerances), for both hidden-irrep sizes."""
+    from helpers import random_rotation
+    path = write_model(make_model(num_channels=32, species=("H", "C", "O"), r_cut=5.0, L_max=L_max, num_knots=60,
+                                  seed=11), str(tmp_path / "m.json"))
+    rng = np.random.default_rng(8)
+    pos = rng.normal(size=(40, 3)) * 2.2
+    species = rng.integers(0, 3, size=40).astype(np.int32)
+    m = _engine(path)
+    out = []
+    for Q in (np.eye(3), random_rotation(rng), -random_rotation(rng)):
+        nl = neighbor_list(pos @ Q.T, 5.0)
+        m.compute_node_energies_forces(*edge_args(species, nl))
+        F = atomic_forces(40, nl["i"], nl["neigh_indices"], m.node_forces)
+        out.append((m.node_energies.copy(), F @ Q))
+    scale_e = max(1.0, np.abs(out[0][0]).max())
+    scale_f = max(1.0, np.abs(out[0][1]).max())
+    for e, F in out[1:]:
+        assert _report("E_i rotated", e, out[0][0]) < 1e-5 * scale_e
+        assert _report("F rotated", F, out[0][1]) < 1e-5 * scale_f

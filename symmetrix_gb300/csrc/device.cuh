@@ -33,6 +33,9 @@ struct DevModel {
   const int* cg_rev_off;
   const int* cg_rev_lme;
   const float* cg_rev_v;
+  // the same table padded to two terms per path, (lme, float bits of the value), zero
+  // terms as (0, 0); nullptr when some path has more terms
+  const int2* cg_rev_pad;
   int lme_off[4], num_e[4];
   const float* A1W[4];
   const float* A1W_T[4];

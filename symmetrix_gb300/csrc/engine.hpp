@@ -167,6 +167,24 @@ struct smx_engine {
     m.cg_rev_off = upload(pm.cg_rev_off);
     m.cg_rev_lme = upload(pm.cg_rev_lme);
     m.cg_rev_v = upload(pm.cg_rev_v);
+    {  // two-term padded copy: the adjoint kernels then gather g with independent loads
+      const int np = static_cast<int>(pm.cg_rev_off.size()) - 1;
+      bool fits = np > 0;
+      for (int p = 0; p < np && fits; ++p) fits = pm.cg_rev_off[p + 1] - pm.cg_rev_off[p] <= 2;
+      m.cg_rev_pad = nullptr;
+      if (fits) {
+        std::vector<int> pad(static_cast<size_t>(4) * np, 0);
+        for (int p = 0; p < np; ++p)
+          for (int q = pm.cg_rev_off[p], t = 0; q < pm.cg_rev_off[p + 1]; ++q, ++t) {
+            float v = pm.cg_rev_v[q];
+            int bits;
+            std::memcpy(&bits, &v, sizeof(bits));
+            pad[4 * p + 2 * t] = pm.cg_rev_lme[q];
+            pad[4 * p + 2 * t + 1] = bits;
+          }
+        m.cg_rev_pad = reinterpret_cast<const int2*>(upload(pad));
+      }
+    }
     for (int l = 0; l < 4; ++l) {
       m.lme_off[l] = pm.lme_off[l];
       m.num_e[l] = pm.num_e[l];

@@ -395,16 +395,24 @@ __device__ __forceinline__ void layer1_rev_atom(const DevModel& m, const EdgeIn&
   const int ti = in.node_type[i];
   const int e0 = in.first[i], e1 = in.end(i);
   // sP[p][k] = sum_lme CG[lme,p] dPhi1[i,lme,k], one channel per thread
-  float* sD = dyn;                 // [n_lme][C]
-  float* sP = dyn + m.n_lme * C;   // [NP][C]
+  float* sD = dyn;                // [n_lme][C]
+  float* sP = dyn + m.n_lme * C;  // [NP][C]
   for (int k = threadIdx.x; k < C; k += blockDim.x) {
     for (int lme = 0; lme < m.n_lme; ++lme) sD[lme * C + k] = dPhi1[(static_cast<size_t>(i) * m.n_lme + lme) * C + k];
-    for (int p = 0; p < NP; ++p) {
-      float s = 0.0f;
-      const int q1 = __ldg(m.cg_rev_off + p + 1);
-      for (int q = __ldg(m.cg_rev_off + p); q < q1; ++q)
-        s = fmaf(__ldg(m.cg_rev_v + q), sD[__ldg(m.cg_rev_lme + q) * C + k], s);
-      sP[p * C + k] = s;
+    if (m.cg_rev_pad) {  // two terms per path: eight paths' loads in flight at a time
+#pragma unroll 8
+      for (int p = 0; p < NP; ++p) {
+        const int2 t0 = __ldg(m.cg_rev_pad + 2 * p), t1 = __ldg(m.cg_rev_pad + 2 * p + 1);
+        sP[p * C + k] = fmaf(__int_as_float(t1.y), sD[t1.x * C + k], __int_as_float(t0.y) * sD[t0.x * C + k]);
+      }
+    } else {  // any number of terms: a chain of dependent loads per path
+      for (int p = 0; p < NP; ++p) {
+        float s = 0.0f;
+        const int q1 = __ldg(m.cg_rev_off + p + 1);
+        for (int q = __ldg(m.cg_rev_off + p); q < q1; ++q)
+          s = fmaf(__ldg(m.cg_rev_v + q), sD[__ldg(m.cg_rev_lme + q) * C + k], s);
+        sP[p * C + k] = s;
+      }
     }
   }
   __syncthreads();

@@ -117,6 +117,8 @@ long smx_get_stage(smx_engine* eng, const char* name, double* out, long cap);
  * "species_order" (-1, the default: the edge kernels take the centre atoms sorted by
  * species when a layer's spline table exceeds 64 MB, so the rows in use stay in L2;
  * 0: input order; 1: always sorted; results do not depend on it);
+ * "cg_padded" (1, the default: the layer-1 Clebsch-Gordan contractions read tables padded
+ * to a fixed number of terms per row, with independent loads; 0: the compressed rows);
  * BF16 form: "tc_terms" (1, 2 or 3 bf16 split terms of the GEMM operands, default 3;
  * set before the first evaluation).
  * No counterpart in the reference (its MACE object has no options). */

@@ -30,6 +30,10 @@ struct DevModel {
   const int* cg_fwd_off;
   const int* cg_fwd_p;
   const float* cg_fwd_v;
+  // the same table padded to cg_fwd_kp terms per output row (<= 8), (p, float bits of the
+  // value), zero terms as (0, 0); nullptr (kp 0) when some row has more terms
+  const int2* cg_fwd_pad;
+  int cg_fwd_kp;
   const int* cg_rev_off;
   const int* cg_rev_lme;
   const float* cg_rev_v;

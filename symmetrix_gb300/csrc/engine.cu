@@ -137,6 +137,10 @@ int smx_set_option(smx_engine* eng, const char* key, long value) {
     if (!eng->autotune && eng->sched_force < 0) eng->sched_set(0);
     return SMX_OK;
   }
+  if (std::strcmp(key, "cg_padded") == 0) {  // 1 (default): padded CG tables; 0: compressed rows
+    eng->use_cg_padded(value != 0);
+    return SMX_OK;
+  }
   if (std::strcmp(key, "species_order") == 0) {  // -1 by table size, 0 input order, 1 species-sorted
     if (value < -1 || value > 1) return fail(SMX_ERR_INVALID, "species_order must be -1, 0 or 1");
     eng->species_order = static_cast<int>(value);
@@ -178,6 +182,7 @@ long smx_get_option(const smx_engine* eng, const char* key) {
   if (k == "persistent") return eng->sched_mask();  // bit k: per-atom kernel k runs persistent
   if (k == "species_order") return eng->order_species() ? 1 : 0;  // in effect
   if (k == "poly_canon") return eng->dm.poly_canon;  // 1: generated polynomial kernels
+  if (k == "cg_padded") return eng->dm.cg_rev_pad != nullptr || eng->dm.cg_fwd_pad != nullptr;
   if (k == "l2_split") return eng->dm.l2_split;       // channel slices of the L_max = 2 layer-1 kernels
   static const char* groups[4] = {"H1", "A1", "Phi1_adj", "M0_adj"};
   for (int q = 0; q < 4; ++q) {

@@ -167,6 +167,28 @@ struct smx_engine {
     m.cg_rev_off = upload(pm.cg_rev_off);
     m.cg_rev_lme = upload(pm.cg_rev_lme);
     m.cg_rev_v = upload(pm.cg_rev_v);
+    {  // forward table padded to its longest row (up to 8 terms): independent loads
+      const int nr = static_cast<int>(pm.cg_fwd_off.size()) - 1;
+      int kp = 0;
+      for (int r = 0; r < nr; ++r) kp = std::max(kp, pm.cg_fwd_off[r + 1] - pm.cg_fwd_off[r]);
+      m.cg_fwd_pad = nullptr;
+      m.cg_fwd_kp = 0;
+      if (nr > 0 && kp >= 1 && kp <= 8) {
+        std::vector<int> pad(static_cast<size_t>(2) * kp * nr, 0);
+        for (int r = 0; r < nr; ++r)
+          for (int q = pm.cg_fwd_off[r], t = 0; q < pm.cg_fwd_off[r + 1]; ++q, ++t) {
+            float v = pm.cg_fwd_v[q];
+            int bits;
+            std::memcpy(&bits, &v, sizeof(bits));
+            pad[2 * (static_cast<size_t>(r) * kp + t)] = pm.cg_fwd_p[q];
+            pad[2 * (static_cast<size_t>(r) * kp + t) + 1] = bits;
+          }
+        m.cg_fwd_pad = reinterpret_cast<const int2*>(upload(pad));
+        m.cg_fwd_kp = kp;
+      }
+      cg_fwd_pad_keep = m.cg_fwd_pad;
+      cg_fwd_kp_keep = m.cg_fwd_kp;
+    }
     {  // two-term padded copy: the adjoint kernels then gather g with independent loads
       const int np = static_cast<int>(pm.cg_rev_off.size()) - 1;
       bool fits = np > 0;
@@ -184,6 +206,7 @@ struct smx_engine {
           }
         m.cg_rev_pad = reinterpret_cast<const int2*>(upload(pad));
       }
+      cg_rev_pad_keep = m.cg_rev_pad;
     }
     for (int l = 0; l < 4; ++l) {
       m.lme_off[l] = pm.lme_off[l];
@@ -424,6 +447,16 @@ struct smx_engine {
     }
     tc_apply(tc_cfg[gid], g, ng, tile_n);
     smx::launch_umma_gemms(g, ng, status_dev, s);
+  }
+
+  // padded Clebsch-Gordan tables (option "cg_padded" 0 switches the kernels to the
+  // compressed-row walk, which models with longer rows always use)
+  const int2 *cg_fwd_pad_keep = nullptr, *cg_rev_pad_keep = nullptr;
+  int cg_fwd_kp_keep = 0;
+  void use_cg_padded(bool on) {
+    dm.cg_fwd_pad = on ? cg_fwd_pad_keep : nullptr;
+    dm.cg_fwd_kp = on ? cg_fwd_kp_keep : 0;
+    dm.cg_rev_pad = on ? cg_rev_pad_keep : nullptr;
   }
 
   // ---- centre-atom order of the edge kernels ----

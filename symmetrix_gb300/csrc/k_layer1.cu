@@ -82,6 +82,67 @@ __device__ __forceinline__ void block_reduce3(float fx, float fy, float fz, floa
   }
 }
 
+// sum_p CG[lme,p] sP[p][k] over row lme of the padded forward table, KF terms, all loads
+// independent
+template <int KF>
+__device__ __forceinline__ float cg_row(const int2* __restrict__ row, const float* sP, int stride, int k) {
+  int2 t[KF];
+#pragma unroll
+  for (int u = 0; u < KF; ++u) t[u] = __ldg(row + u);
+  float s = 0.0f;
+#pragma unroll
+  for (int u = 0; u < KF; ++u) s = fmaf(__int_as_float(t[u].y), sP[t[u].x * stride + k], s);
+  return s;
+}
+
+// f(std::integral_constant<int, KF>) for the padded forward table's row length, KF = 0
+// for the compressed-row walk (no padded table)
+template <typename F>
+__device__ __forceinline__ void dispatch_kf(int kp, F&& f) {
+  switch (kp) {
+    case 1: f(std::integral_constant<int, 1>{}); break;
+    case 2: f(std::integral_constant<int, 2>{}); break;
+    case 3: f(std::integral_constant<int, 3>{}); break;
+    case 4: f(std::integral_constant<int, 4>{}); break;
+    case 5: f(std::integral_constant<int, 5>{}); break;
+    case 6: f(std::integral_constant<int, 6>{}); break;
+    case 7: f(std::integral_constant<int, 7>{}); break;
+    case 8: f(std::integral_constant<int, 8>{}); break;
+    default: f(std::integral_constant<int, 0>{}); break;
+  }
+}
+
+// Phi1[i,lme,k] = sum_p CG[lme,p] sP[p][k] for the rows lme with (lme mod nrow_groups) ==
+// row_group (the BF16 form also writes them as the A1 GEMM's split operand, regrouped per
+// l); sP holds this block's channels with row stride `stride`, k is the global channel
+template <int KF>
+__device__ __forceinline__ void l1_fwd_epilogue(const DevModel& m, int N, int i, const float* sP, int stride, int kk,
+                                                int k, int row_group, int nrow_groups, float* __restrict__ Phi1) {
+  const int C = m.C, T = m.tc_terms;
+  for (int l = 0; l < 4; ++l) {
+    const int ne = m.num_e[l], Kl = ne * C;
+    for (int mm = 0; mm < 2 * l + 1; ++mm)
+      for (int e = 0; e < ne; ++e) {
+        const int lme = m.lme_off[l] + mm * ne + e;
+        if (lme % nrow_groups != row_group) continue;
+        float s = 0.0f;
+        if constexpr (KF > 0) {
+          s = cg_row<KF>(m.cg_fwd_pad + static_cast<size_t>(lme) * KF, sP, stride, kk);
+        } else {
+          const int p1 = __ldg(m.cg_fwd_off + lme + 1);
+          for (int p = __ldg(m.cg_fwd_off + lme); p < p1; ++p)
+            s = fmaf(__ldg(m.cg_fwd_v + p), sP[__ldg(m.cg_fwd_p + p) * stride + kk], s);
+        }
+        Phi1[(static_cast<size_t>(i) * m.n_lme + lme) * C + k] = s;
+        if (m.op_phi1) {
+          __nv_bfloat16* row = m.op_phi1 + static_cast<size_t>(T) * N * m.lme_off[l] * C +
+                               (static_cast<size_t>(i) * (2 * l + 1) + mm) * T * Kl;
+          write_split(row, Kl, T, e * C + k, s);
+        }
+      }
+  }
+}
+
 // Edge chunk staged for the layer-1 kernels.
 template <bool GRAD>
 struct L1Stage {
@@ -343,26 +404,11 @@ __device__ __forceinline__ void layer1_fwd_atom(const DevModel& m, const EdgeIn&
   float* sP = dyn;  // [NP][C]: this thread's Phi1r column
 #pragma unroll
   for (int p = 0; p < NP; ++p) sP[p * C + k] = acc[p];
-  // Phi1 rows are [l][m][e] (lme = lme_off[l] + m n_e + e); the BF16 form also writes
-  // them as the A1 GEMM's split operand, regrouped per l
-  const int T = m.tc_terms;
-  for (int l = 0; l < 4; ++l) {
-    const int ne = m.num_e[l], Kl = ne * C;
-    for (int mm = 0; mm < 2 * l + 1; ++mm)
-      for (int e = 0; e < ne; ++e) {
-        const int lme = m.lme_off[l] + mm * ne + e;
-        float s = 0.0f;
-        const int p1 = __ldg(m.cg_fwd_off + lme + 1);
-        for (int p = __ldg(m.cg_fwd_off + lme); p < p1; ++p)
-          s = fmaf(__ldg(m.cg_fwd_v + p), sP[__ldg(m.cg_fwd_p + p) * C + k], s);
-        Phi1[(static_cast<size_t>(i) * m.n_lme + lme) * C + k] = s;
-        if (m.op_phi1) {
-          __nv_bfloat16* row = m.op_phi1 + static_cast<size_t>(T) * in.N * m.lme_off[l] * C +
-                               (static_cast<size_t>(i) * (2 * l + 1) + mm) * T * Kl;
-          write_split(row, Kl, T, e * C + k, s);
-        }
-      }
-  }
+  // Phi1 rows are [l][m][e] (lme = lme_off[l] + m n_e + e); each thread reads back only its
+  // own column of sP
+  dispatch_kf(m.cg_fwd_kp, [&](auto kc) {
+    l1_fwd_epilogue<decltype(kc)::value>(m, in.N, i, sP, C, k, k, 0, 1, Phi1);
+  });
 }
 
 template <int LMAX, int CT, bool P>
@@ -607,25 +653,9 @@ __device__ __forceinline__ void layer1_fwd_l2_atom(const DevModel& m, const Edge
   __syncthreads();
   // Phi1 rows of the slice, group G taking the rows lme = G (mod 4)
   if (!live) return;
-  const int T = m.tc_terms;
-  for (int l = 0; l < 4; ++l) {
-    const int ne = m.num_e[l], Kl = ne * C;
-    for (int mm = 0; mm < 2 * l + 1; ++mm)
-      for (int e = 0; e < ne; ++e) {
-        const int lme = m.lme_off[l] + mm * ne + e;
-        if ((lme & (kL2Groups - 1)) != grp) continue;
-        float sum = 0.0f;
-        const int p1 = __ldg(m.cg_fwd_off + lme + 1);
-        for (int p = __ldg(m.cg_fwd_off + lme); p < p1; ++p)
-          sum = fmaf(__ldg(m.cg_fwd_v + p), sP[__ldg(m.cg_fwd_p + p) * CH + kk], sum);
-        Phi1[(static_cast<size_t>(i) * m.n_lme + lme) * C + k] = sum;
-        if (m.op_phi1) {
-          __nv_bfloat16* row = m.op_phi1 + static_cast<size_t>(T) * in.N * m.lme_off[l] * C +
-                               (static_cast<size_t>(i) * (2 * l + 1) + mm) * T * Kl;
-          write_split(row, Kl, T, e * C + k, sum);
-        }
-      }
-  }
+  dispatch_kf(m.cg_fwd_kp, [&](auto kc) {
+    l1_fwd_epilogue<decltype(kc)::value>(m, in.N, i, sP, CH, kk, k, grp, kL2Groups, Phi1);
+  });
 }
 
 // work item b = (atom, channel slice); the return in the atom body above happens after
@@ -742,14 +772,23 @@ __device__ __forceinline__ void layer1_rev_l2_atom(const DevModel& m, const Edge
     for (int lme = grp; lme < m.n_lme; lme += kL2Groups)
       sD[lme * CH + kk] = dPhi1[(static_cast<size_t>(i) * m.n_lme + lme) * C + k];
   __syncthreads();
-  if (live)
-    for (int p = grp; p < NP; p += kL2Groups) {
-      float sum = 0.0f;
-      const int q1 = __ldg(m.cg_rev_off + p + 1);
-      for (int q = __ldg(m.cg_rev_off + p); q < q1; ++q)
-        sum = fmaf(__ldg(m.cg_rev_v + q), sD[__ldg(m.cg_rev_lme + q) * CH + kk], sum);
-      sP[p * CH + kk] = sum;
+  if (live) {
+    if (m.cg_rev_pad) {  // two terms per path: several paths' loads in flight
+#pragma unroll 4
+      for (int p = grp; p < NP; p += kL2Groups) {
+        const int2 t0 = __ldg(m.cg_rev_pad + 2 * p), t1 = __ldg(m.cg_rev_pad + 2 * p + 1);
+        sP[p * CH + kk] = fmaf(__int_as_float(t1.y), sD[t1.x * CH + kk], __int_as_float(t0.y) * sD[t0.x * CH + kk]);
+      }
+    } else {
+      for (int p = grp; p < NP; p += kL2Groups) {
+        float sum = 0.0f;
+        const int q1 = __ldg(m.cg_rev_off + p + 1);
+        for (int q = __ldg(m.cg_rev_off + p); q < q1; ++q)
+          sum = fmaf(__ldg(m.cg_rev_v + q), sD[__ldg(m.cg_rev_lme + q) * CH + kk], sum);
+        sP[p * CH + kk] = sum;
+      }
     }
+  }
   __syncthreads();
   float g[kL2MaxNp];
   switch (grp) {

@@ -387,3 +387,22 @@ def test_rotation_invariance_on_gpu(engine_lib, tmp_path, L_max):
     for e, F in out[1:]:
         assert _report("E_i rotated", e, out[0][0]) < 1e-5 * scale_e
         assert _report("F rotated", F, out[0][1]) < 1e-5 * scale_f
+
+
+@pytest.mark.parametrize("L_max", [1, 2])
+def test_cg_table_forms_agree(engine_lib, tmp_path, L_max):
+    """The layer-1 Clebsch-Gordan contractions through the padded tables (default) and
+    through the compressed rows: the same energies and forces to float32 rounding."""
+    path = write_model(make_model(num_channels=32 * L_max, species=("H", "C", "O"), r_cut=5.0, L_max=L_max,
+                                  num_knots=60, seed=12), str(tmp_path / "m.json"))
+    pos, L, species = random_box(120, 0.08, 0.9, 3, seed=14)
+    nl = neighbor_list(pos, 5.0, L)
+    m = _engine(path)
+    assert m.get_option("cg_padded") == 1
+    m.compute_node_energies_forces(*edge_args(species, nl))
+    e_pad, f_pad = m.node_energies.copy(), m.node_forces.copy()
+    m.set_option("cg_padded", 0)
+    assert m.get_option("cg_padded") == 0
+    m.compute_node_energies_forces(*edge_args(species, nl))
+    assert _report("E_i", m.node_energies, e_pad) < 1e-5 * max(1.0, np.abs(e_pad).max())
+    assert _report("f_edge", m.node_forces, f_pad) < 1e-5 * max(1.0, np.abs(f_pad).max())

@@ -41,11 +41,12 @@ def term(m):
 
 
 def value_fn(name, monos):
+    # four partial sums (terms taken round-robin): four short dependent FMA chains
     out = [f"__device__ __forceinline__ float {name}(const float* x, const float* __restrict__ cf, int C) {{",
-           "  float f = 0.0f;"]
+           "  float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f, f3 = 0.0f;"]
     for t, m in enumerate(monos):
-        out.append(f"  f = fmaf(__ldg(cf + {t} * C), {term(m)}, f);")
-    out += ["  return f;", "}"]
+        out.append(f"  f{t % 4} = fmaf(__ldg(cf + {t} * C), {term(m)}, f{t % 4});")
+    out += ["  return (f0 + f1) + (f2 + f3);", "}"]
     return "\n".join(out)
 
 
@@ -74,10 +75,10 @@ def grad_fn(name, monos):
 
 def value_grad_fn(name, monos):
     out = [f"__device__ __forceinline__ float {name}(const float* x, const float* __restrict__ cf, int C, "
-           f"float* g) {{", "  float f = 0.0f;"]
+           f"float* g) {{", "  float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f, f3 = 0.0f;"]
     for t, m in enumerate(monos):
         out.append(f"  {{ const float q = __ldg(cf + {t} * C);")
-        out.append(f"    f = fmaf(q, {term(m)}, f);")
+        out.append(f"    f{t % 4} = fmaf(q, {term(m)}, f{t % 4});")
         if len(m) == 1:
             out.append(f"    g[{m[0]}] += q;")
         else:
@@ -85,7 +86,7 @@ def value_grad_fn(name, monos):
                 rest = [b for j, b in enumerate(m) if j != i]
                 out.append(f"    g[{a}] = fmaf(q, {term(rest)}, g[{a}]);")
         out.append("  }")
-    out += ["  return f;", "}"]
+    out += ["  return (f0 + f1) + (f2 + f3);", "}"]
     return "\n".join(out)
 
 

@@ -157,14 +157,22 @@ __device__ __forceinline__ void node_tail_atom(const DevModel& m, const int* __r
   const float h10 = H1[static_cast<size_t>(i) * m.nLM * C + k];
   sH10[k] = h10;
   __syncthreads();
-  float h2 = 0.0f;
+  // H2 = W_H1[ti]^T H1[i,0,:] + W_M1^T M1: four partial sums, eight rows' loads in flight
   const float* W = m.H2W_H1 + static_cast<size_t>(ti) * C * C + k;
-  for (int r = 0; r < C; ++r) {
-    h2 = fmaf(sH10[r], __ldg(W + static_cast<size_t>(r) * C), h2);
-    h2 = fmaf(sM1[r], __ldg(m.H2W_M1 + static_cast<size_t>(r) * C + k), h2);
+  const float* WM = m.H2W_M1 + k;
+  float hp0 = 0.0f, hp1 = 0.0f, hp2 = 0.0f, hp3 = 0.0f;  // C is a multiple of 32
+#pragma unroll 2
+  for (int r = 0; r < C; r += 4) {
+    const size_t o = static_cast<size_t>(r) * C;
+    hp0 = fmaf(sM1[r], __ldg(WM + o), fmaf(sH10[r], __ldg(W + o), hp0));
+    hp1 = fmaf(sM1[r + 1], __ldg(WM + o + C), fmaf(sH10[r + 1], __ldg(W + o + C), hp1));
+    hp2 = fmaf(sM1[r + 2], __ldg(WM + o + 2 * C), fmaf(sH10[r + 2], __ldg(W + o + 2 * C), hp2));
+    hp3 = fmaf(sM1[r + 3], __ldg(WM + o + 3 * C), fmaf(sH10[r + 3], __ldg(W + o + 3 * C), hp3));
   }
+  const float h2 = (hp0 + hp1) + (hp2 + hp3);
   sH2[k] = h2;
   // hidden pre-activations s_u = W1[u,:] . H2 and the linear readout w1 . H1[i,0,:] (slot nh)
+#pragma unroll 4
   for (int u = 0; u <= nh; ++u) {
     float v = (u < nh) ? __ldg(m.ro2_w1 + static_cast<size_t>(u) * C + k) * h2 : __ldg(m.ro1 + k) * h10;
     v = warp_sum(v);
@@ -196,13 +204,21 @@ __device__ __forceinline__ void node_tail_atom(const DevModel& m, const int* __r
     energies[i] = e;
   }
   __syncthreads();
-  float ha = __ldg(m.ro1 + k), m1a = 0.0f;
+  // H1_adj[i,0,:] = w1 + W_H1[ti] dE/dH2 and M1_adj = W_M1 dE/dH2: as above
   const float* WT = m.H2W_H1_T + static_cast<size_t>(ti) * C * C + k;
-  for (int c = 0; c < C; ++c) {
-    const float d = sdH2[c];
-    ha = fmaf(__ldg(WT + static_cast<size_t>(c) * C), d, ha);
-    m1a = fmaf(__ldg(m.H2W_M1_T + static_cast<size_t>(c) * C + k), d, m1a);
+  const float* WMT = m.H2W_M1_T + k;
+  float ha0 = 0.0f, ha1 = 0.0f, ma0 = 0.0f, ma1 = 0.0f;
+#pragma unroll 4
+  for (int c = 0; c < C; c += 2) {
+    const size_t o = static_cast<size_t>(c) * C;
+    const float d0 = sdH2[c], d1 = sdH2[c + 1];
+    ha0 = fmaf(__ldg(WT + o), d0, ha0);
+    ma0 = fmaf(__ldg(WMT + o), d0, ma0);
+    ha1 = fmaf(__ldg(WT + o + C), d1, ha1);
+    ma1 = fmaf(__ldg(WMT + o + C), d1, ma1);
   }
+  const float ha = __ldg(m.ro1 + k) + (ha0 + ha1);
+  const float m1a = ma0 + ma1;
   if (dens) {  // reverse_A1_scaled (mace.cpp:707-757): c_i = dA1 . A1 / s_i, dA1 /= s_i
     float dot = 0.0f;
 #pragma unroll

@@ -17,12 +17,6 @@
 
 namespace smx {
 
-namespace {
-
-__device__ __forceinline__ int wrapi(int c, int n) { return c < 0 ? c + n : (c >= n ? c - n : c); }
-
-}  // namespace
-
 // ---- cell list ----
 __global__ void k_cell_assign(const double* __restrict__ pos, int N, double3 box, int3 nc, int* __restrict__ cell,
                               int* __restrict__ cell_count) {
@@ -51,19 +45,19 @@ __global__ void k_cell_fill(const int* __restrict__ cell, int N, const int* __re
   cell_atoms[cell_start[c] + atomicAdd(cell_fill + c, 1)] = a;
 }
 
-// one thread per cell: insertion sort of the cell's atoms by index (cells hold tens of atoms)
-__global__ void k_cell_sort(int ncell, const int* __restrict__ cell_start, int* __restrict__ cell_atoms) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+// one warp per cell: each atom's rank among the cell's atoms (by index) is its place in
+// the sorted list (cells hold tens of atoms; O(n^2 / 32) per cell)
+__global__ void k_cell_sort(int ncell, const int* __restrict__ cell_start, const int* __restrict__ unsorted,
+                            int* __restrict__ cell_atoms) {
+  const int c = static_cast<int>((static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
   if (c >= ncell) return;
-  const int b = cell_start[c], e = cell_start[c + 1];
-  for (int q = b + 1; q < e; ++q) {
-    const int v = cell_atoms[q];
-    int w = q - 1;
-    while (w >= b && cell_atoms[w] > v) {
-      cell_atoms[w + 1] = cell_atoms[w];
-      --w;
-    }
-    cell_atoms[w + 1] = v;
+  const int b = cell_start[c], n = cell_start[c + 1] - b;
+  for (int u = lane; u < n; u += 32) {
+    const int v = unsorted[b + u];
+    int rank = 0;
+    for (int x = 0; x < n; ++x) rank += unsorted[b + x] < v;
+    cell_atoms[b + rank] = v;
   }
 }
 
@@ -186,23 +180,30 @@ __global__ void k_wrap(int N, double3 box, int3 periodic, double* __restrict__ p
 }
 
 // rev[e] = index of the reverse edge (j -> i, -shift) of e = (i -> j, shift); -1 if absent.
-// The edge count is read from first[N] on the device, so launches do not depend on it.
-__global__ void k_reverse_edges(long cap, int N, const int* __restrict__ first, const int* __restrict__ nidx,
-                                const int* __restrict__ edge_i, const char4* __restrict__ shift, int* __restrict__ rev) {
-  const long e = static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x;
-  const long E = first[N] < cap ? first[N] : cap;
-  if (e >= E) return;
-  const int i = edge_i[e], j = nidx[e];
-  const char4 s = shift[e];
-  int found = -1;
-  for (int w = first[j]; w < first[j + 1]; ++w) {
-    const char4 t = shift[w];
-    if (nidx[w] == i && t.x == -s.x && t.y == -s.y && t.z == -s.z) {
-      found = w;
-      break;
+// One warp per centre atom i: for each of its edges the lanes scan j's list 32 entries at
+// a time (the first match in list order, as a sequential scan would find).
+__global__ void k_reverse_edges(int N, const int* __restrict__ first, const int* __restrict__ nidx,
+                                const char4* __restrict__ shift, int* __restrict__ rev) {
+  const int i = static_cast<int>((static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (i >= N) return;
+  for (int e = first[i]; e < first[i + 1]; ++e) {
+    const int j = nidx[e];
+    const char4 sh = shift[e];
+    const int w1 = first[j + 1];
+    int found = -1;
+    for (int w0 = first[j]; w0 < w1 && found < 0; w0 += 32) {
+      const int w = w0 + lane;
+      bool match = false;
+      if (w < w1) {
+        const char4 t = shift[w];
+        match = nidx[w] == i && t.x == -sh.x && t.y == -sh.y && t.z == -sh.z;
+      }
+      const unsigned ball = __ballot_sync(0xffffffffu, match);
+      if (ball) found = w0 + __ffs(ball) - 1;
     }
+    if (lane == 0) rev[e] = found;
   }
-  rev[e] = found;
 }
 
 // xyz_e = x_j + shift_e * box - x_i, r_e = |xyz_e|
@@ -362,15 +363,17 @@ __global__ void k_vv_second(int N, double dt, const double* __restrict__ F, cons
 }
 
 // ---- launchers ----
+// atoms binned (atomic fill into cell_tmp), then each cell's atoms sorted by index into
+// cell_atoms: the list order does not depend on the order of the atomics
 void launch_cell_list(const double* pos, int N, double3 box, int3 nc, int* cell, int* cell_count, int* cell_start,
-                      int* cell_fill, int* cell_atoms, cudaStream_t s) {
+                      int* cell_fill, int* cell_tmp, int* cell_atoms, cudaStream_t s) {
   const int ncell = nc.x * nc.y * nc.z;
   cudaMemsetAsync(cell_count, 0, sizeof(int) * ncell, s);
   cudaMemsetAsync(cell_fill, 0, sizeof(int) * ncell, s);
   k_cell_assign<<<ceil_div(N, 256), 256, 0, s>>>(pos, N, box, nc, cell, cell_count);
   launch_scan_first(cell_count, ncell, cell_start, s);
-  k_cell_fill<<<ceil_div(N, 256), 256, 0, s>>>(cell, N, cell_start, cell_fill, cell_atoms);
-  k_cell_sort<<<ceil_div(ncell, 128), 128, 0, s>>>(ncell, cell_start, cell_atoms);
+  k_cell_fill<<<ceil_div(N, 256), 256, 0, s>>>(cell, N, cell_start, cell_fill, cell_tmp);
+  k_cell_sort<<<ceil_div(ncell, 4), 128, 0, s>>>(ncell, cell_start, cell_tmp, cell_atoms);  // one warp per cell
 }
 
 void launch_neigh_pass(bool fill, bool brute, const double* pos, const int* species, int N, double3 box, int3 nc,
@@ -403,7 +406,7 @@ void launch_wrap(int N, double3 box, int3 periodic, double* pos, cudaStream_t s)
 
 void launch_reverse_edges(long cap, int N, const int* first, const int* nidx, const int* edge_i, const char4* shift,
                           int* rev, cudaStream_t s) {
-  if (cap > 0) k_reverse_edges<<<ceil_div(cap, 256), 256, 0, s>>>(cap, N, first, nidx, edge_i, shift, rev);
+  if (cap > 0 && N > 0) k_reverse_edges<<<ceil_div(N, 4), 128, 0, s>>>(N, first, nidx, shift, rev);  // warp per atom
 }
 
 void launch_edge_geometry(long cap, int N, const int* first, const double* pos, double3 box, const int* nidx,

@@ -96,7 +96,7 @@ void launch_rows_to_bf16(const float* src, __nv_bfloat16* dst, long rows, int wi
 // k_md.cu
 void launch_wrap(int N, double3 box, int3 periodic, double* pos, cudaStream_t s);
 void launch_cell_list(const double* pos, int N, double3 box, int3 nc, int* cell, int* cell_count, int* cell_start,
-                      int* cell_fill, int* cell_atoms, cudaStream_t s);
+                      int* cell_fill, int* cell_tmp, int* cell_atoms, cudaStream_t s);
 void launch_neigh_pass(bool fill, bool brute, const double* pos, const int* species, int N, double3 box, int3 nc,
                        int3 periodic, int3 nimg, double rl, const int* cell, const int* cell_start,
                        const int* cell_atoms, const int* seg_of, const int* seg_first, int* num_neigh,

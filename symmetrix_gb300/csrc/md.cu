@@ -21,9 +21,10 @@ namespace {
 
 // Full directed neighbour list on the device with a skin, CSR by centre atom.
 struct NeighList {
-  int capN = 0, ncell_cap = 0;
+  int capN = 0, ncell_cap = 0, cell_atoms_cap = 0;
   long capE = 0;
   int *cell = nullptr, *cell_count = nullptr, *cell_start = nullptr, *cell_fill = nullptr, *cell_atoms = nullptr;
+  int* cell_tmp = nullptr;  // the binned atoms before each cell is sorted
   int *num_neigh = nullptr, *first = nullptr, *nidx = nullptr, *ntype_e = nullptr, *edge_i = nullptr, *rev = nullptr;
   char4* shift = nullptr;
   double *xyz = nullptr, *r = nullptr, *forces = nullptr;
@@ -37,14 +38,14 @@ struct NeighList {
   void release() {
     void* ps[] = {cell,  cell_count, cell_start, cell_fill, cell_atoms, num_neigh, first, nidx,  ntype_e,
                   edge_i, rev,       shift,      xyz,       r,          forces,    last,  emap,  nidx_p,
-                  ntype_p, xyz_p,    r_p,        forces_p};
+                  ntype_p, xyz_p,    r_p,        forces_p,  cell_tmp};
     for (void* p : ps)
       if (p) cudaFree(p);
     cell = cell_count = cell_start = cell_fill = cell_atoms = num_neigh = first = nidx = ntype_e = edge_i = rev = nullptr;
-    last = emap = nidx_p = ntype_p = nullptr;
+    last = emap = nidx_p = ntype_p = cell_tmp = nullptr;
     shift = nullptr;
     xyz = r = forces = xyz_p = r_p = forces_p = nullptr;
-    capN = ncell_cap = 0;
+    capN = ncell_cap = cell_atoms_cap = 0;
     capE = 0;
   }
   void reserve_nodes(int N, int ncell) {
@@ -66,7 +67,13 @@ struct NeighList {
       cell_fill = dalloc<int>(ncell + 1);
       ncell_cap = ncell + 1;
     }
-    if (!cell_atoms) cell_atoms = dalloc<int>(N);
+    if (N > cell_atoms_cap) {
+      for (int** p : {&cell_atoms, &cell_tmp})
+        if (*p) cudaFree(*p);
+      cell_atoms = dalloc<int>(N);
+      cell_tmp = dalloc<int>(N);
+      cell_atoms_cap = N;
+    }
   }
   void reserve_edges(long E_) {
     if (E_ <= capE) return;
@@ -119,7 +126,7 @@ struct NeighList {
     reserve_nodes(N, nc.x * nc.y * nc.z);
     smx::launch_wrap(N, box, periodic, pos, s);
     if (!brute)
-      smx::launch_cell_list(pos, N, box, nc, cell, cell_count, cell_start, cell_fill, cell_atoms, s);
+      smx::launch_cell_list(pos, N, box, nc, cell, cell_count, cell_start, cell_fill, cell_tmp, cell_atoms, s);
     smx::launch_neigh_pass(false, brute, pos, species, N, box, nc, periodic, nimg, rl, cell, cell_start, cell_atoms,
                            seg_of, seg_first, num_neigh, first, nidx, ntype_e, edge_i, shift, capE, s);
     smx::launch_scan_first(num_neigh, N, first, s);

@@ -588,7 +588,19 @@ struct smx_engine {
       for (auto& e : ev) check(cudaEventCreate(&e), "cudaEventCreate");
     prof_stream = s;
     mark(0, s);
-    smx::launch_layer0_fwd(dm, in, A0, M0, dm.has_zbl ? zbl_e : nullptr, s);
+    // The BF16 form's GEMMs read the producers' split bf16 rows; the float32 copies of
+    // M0, Phi1 and A1_adj are then written only for inspection or a SIMT fallback.
+    bool all_A1 = true, all_Phi1adj = true;
+    for (int l = 0; l < 4; ++l)
+      if (dm.num_e[l] > 0) {
+        all_A1 = all_A1 && tc_A1[l];
+        all_Phi1adj = all_Phi1adj && tc_Phi1adj[l];
+      }
+    const bool f32_rows = keep_stages || precision != SMX_PRECISION_BF16;
+    float* M0_out = (f32_rows || !tc_H1) ? M0 : nullptr;
+    float* Phi1_out = (f32_rows || !all_A1) ? Phi1 : nullptr;
+    float* A1adj_out = (f32_rows || !all_Phi1adj) ? A1_adj : nullptr;
+    smx::launch_layer0_fwd(dm, in, A0, M0_out, dm.has_zbl ? zbl_e : nullptr, s);
     mark(1, s);
     if (tc_H1) {  // H1 = M0 @ H1W[L]  (mace.cpp:397-423), tensor cores
       // (layer0_fwd wrote M0 as split bf16 rows into M0_bf)
@@ -604,7 +616,7 @@ struct smx_engine {
       smx::launch_gemm(b, s);
     }
     mark(2, s);
-    smx::launch_layer1_fwd(dm, in, H1, Phi1, s);
+    smx::launch_layer1_fwd(dm, in, H1, Phi1_out, s);
     mark(3, s);
     {  // A1 = Phi1 @ A1W[l]  (mace.cpp:607-642)
       // tensor cores on the per-l regrouped split bf16 rows layer1_fwd wrote, one launch
@@ -627,7 +639,7 @@ struct smx_engine {
       smx::launch_gemm(b, s);
     }
     mark(4, s);
-    smx::launch_node_tail(dm, in.node_type, N, A1, H1, M1, H2, A1_adj, H1_adj, M1_adj, H2_adj,
+    smx::launch_node_tail(dm, in.node_type, N, A1, H1, M1, H2, A1adj_out, H1_adj, M1_adj, H2_adj,
                           dm.has_zbl ? zbl_e : nullptr, out_e, s);
     mark(5, s);
     {  // Phi1_adj = A1_adj @ A1W[l]^T  (mace.cpp:644-679)

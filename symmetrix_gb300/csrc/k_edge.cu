@@ -190,7 +190,7 @@ __device__ __forceinline__ void layer0_fwd_atom(const DevModel& m, const EdgeIn&
       }
 #pragma unroll
       for (int LM = 0; LM < NLM; ++LM) {
-        out[LM * C] = v[LM];
+        if (M0) out[LM * C] = v[LM];  // nullptr: only the split rows are consumed
         if (m.op_m0)  // BF16 form: the H1 GEMM's split operand
           write_split(m.op_m0 + (static_cast<size_t>(i) * m.nLM + LM) * m.tc_terms * C, C, m.tc_terms, k, v[LM]);
       }
@@ -205,7 +205,7 @@ __device__ __forceinline__ void layer0_fwd_atom(const DevModel& m, const EdgeIn&
         const float xa = sA[(pk & 255) * C + k], xb = sA[((pk >> 8) & 255) * C + k], xc = sA[(pk >> 16) * C + k];
         f = fmaf(__ldg(cf + static_cast<size_t>(t - t0) * C), xa * xb * xc, f);
       }
-      M0[(static_cast<size_t>(i) * m.nLM + LM) * C + k] = f;
+      if (M0) M0[(static_cast<size_t>(i) * m.nLM + LM) * C + k] = f;
       if (m.op_m0)
         write_split(m.op_m0 + (static_cast<size_t>(i) * m.nLM + LM) * m.tc_terms * C, C, m.tc_terms, k, f);
     }

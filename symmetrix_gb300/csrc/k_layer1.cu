@@ -133,7 +133,7 @@ __device__ __forceinline__ void l1_fwd_epilogue(const DevModel& m, int N, int i,
           for (int p = __ldg(m.cg_fwd_off + lme); p < p1; ++p)
             s = fmaf(__ldg(m.cg_fwd_v + p), sP[__ldg(m.cg_fwd_p + p) * stride + kk], s);
         }
-        Phi1[(static_cast<size_t>(i) * m.n_lme + lme) * C + k] = s;
+        if (Phi1) Phi1[(static_cast<size_t>(i) * m.n_lme + lme) * C + k] = s;  // nullptr: split rows only
         if (m.op_phi1) {
           __nv_bfloat16* row = m.op_phi1 + static_cast<size_t>(T) * N * m.lme_off[l] * C +
                                (static_cast<size_t>(i) * (2 * l + 1) + mm) * T * Kl;

@@ -226,8 +226,9 @@ __device__ __forceinline__ void node_tail_atom(const DevModel& m, const int* __r
     dot = block_sum(dot);
     if (k == 0) m.dens_c[1][i] = dot / S1;
   }
+  if (A1_adj)  // nullptr: only the split rows below are consumed
 #pragma unroll
-  for (int q = 0; q < 16; ++q) A1_adj[(static_cast<size_t>(i) * 16 + q) * C + k] = sG[q * C + k] * m1a / S1;
+    for (int q = 0; q < 16; ++q) A1_adj[(static_cast<size_t>(i) * 16 + q) * C + k] = sG[q * C + k] * m1a / S1;
   if (m.op_a1adj) {  // BF16 form: the Phi1_adj GEMM's split operand, rows (node, m) per l
     const int T = m.tc_terms;
     for (int l = 0; l < 4; ++l) {

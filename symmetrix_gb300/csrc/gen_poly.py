@@ -41,12 +41,13 @@ def term(m):
 
 
 def value_fn(name, monos):
-    # four partial sums (terms taken round-robin): four short dependent FMA chains
+    # one sum: the layer-0 kernel evaluates several of these side by side (four partial
+    # sums each measured slower there); the node tail's value_grad uses four
     out = [f"__device__ __forceinline__ float {name}(const float* x, const float* __restrict__ cf, int C) {{",
-           "  float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f, f3 = 0.0f;"]
+           "  float f = 0.0f;"]
     for t, m in enumerate(monos):
-        out.append(f"  f{t % 4} = fmaf(__ldg(cf + {t} * C), {term(m)}, f{t % 4});")
-    out += ["  return (f0 + f1) + (f2 + f3);", "}"]
+        out.append(f"  f = fmaf(__ldg(cf + {t} * C), {term(m)}, f);")
+    out += ["  return f;", "}"]
     return "\n".join(out)
 
 

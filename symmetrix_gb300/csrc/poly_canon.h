@@ -8,102 +8,102 @@ namespace smx {
 namespace poly {
 
 __device__ __forceinline__ float value_LM0(const float* x, const float* __restrict__ cf, int C) {
-  float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f, f3 = 0.0f;
-  f0 = fmaf(__ldg(cf + 0 * C), x[0], f0);
-  f1 = fmaf(__ldg(cf + 1 * C), x[0]*x[0], f1);
-  f2 = fmaf(__ldg(cf + 2 * C), x[1]*x[1], f2);
-  f3 = fmaf(__ldg(cf + 3 * C), x[2]*x[2], f3);
-  f0 = fmaf(__ldg(cf + 4 * C), x[3]*x[3], f0);
-  f1 = fmaf(__ldg(cf + 5 * C), x[4]*x[4], f1);
-  f2 = fmaf(__ldg(cf + 6 * C), x[5]*x[5], f2);
-  f3 = fmaf(__ldg(cf + 7 * C), x[6]*x[6], f3);
-  f0 = fmaf(__ldg(cf + 8 * C), x[7]*x[7], f0);
-  f1 = fmaf(__ldg(cf + 9 * C), x[8]*x[8], f1);
-  f2 = fmaf(__ldg(cf + 10 * C), x[9]*x[9], f2);
-  f3 = fmaf(__ldg(cf + 11 * C), x[10]*x[10], f3);
-  f0 = fmaf(__ldg(cf + 12 * C), x[11]*x[11], f0);
-  f1 = fmaf(__ldg(cf + 13 * C), x[12]*x[12], f1);
-  f2 = fmaf(__ldg(cf + 14 * C), x[13]*x[13], f2);
-  f3 = fmaf(__ldg(cf + 15 * C), x[14]*x[14], f3);
-  f0 = fmaf(__ldg(cf + 16 * C), x[15]*x[15], f0);
-  f1 = fmaf(__ldg(cf + 17 * C), x[0]*x[0]*x[0], f1);
-  f2 = fmaf(__ldg(cf + 18 * C), x[0]*x[1]*x[1], f2);
-  f3 = fmaf(__ldg(cf + 19 * C), x[0]*x[2]*x[2], f3);
-  f0 = fmaf(__ldg(cf + 20 * C), x[0]*x[3]*x[3], f0);
-  f1 = fmaf(__ldg(cf + 21 * C), x[0]*x[4]*x[4], f1);
-  f2 = fmaf(__ldg(cf + 22 * C), x[0]*x[5]*x[5], f2);
-  f3 = fmaf(__ldg(cf + 23 * C), x[0]*x[6]*x[6], f3);
-  f0 = fmaf(__ldg(cf + 24 * C), x[0]*x[7]*x[7], f0);
-  f1 = fmaf(__ldg(cf + 25 * C), x[0]*x[8]*x[8], f1);
-  f2 = fmaf(__ldg(cf + 26 * C), x[0]*x[9]*x[9], f2);
-  f3 = fmaf(__ldg(cf + 27 * C), x[0]*x[10]*x[10], f3);
-  f0 = fmaf(__ldg(cf + 28 * C), x[0]*x[11]*x[11], f0);
-  f1 = fmaf(__ldg(cf + 29 * C), x[0]*x[12]*x[12], f1);
-  f2 = fmaf(__ldg(cf + 30 * C), x[0]*x[13]*x[13], f2);
-  f3 = fmaf(__ldg(cf + 31 * C), x[0]*x[14]*x[14], f3);
-  f0 = fmaf(__ldg(cf + 32 * C), x[0]*x[15]*x[15], f0);
-  f1 = fmaf(__ldg(cf + 33 * C), x[1]*x[1]*x[6], f1);
-  f2 = fmaf(__ldg(cf + 34 * C), x[1]*x[1]*x[8], f2);
-  f3 = fmaf(__ldg(cf + 35 * C), x[1]*x[2]*x[5], f3);
-  f0 = fmaf(__ldg(cf + 36 * C), x[1]*x[3]*x[4], f0);
-  f1 = fmaf(__ldg(cf + 37 * C), x[1]*x[4]*x[13], f1);
-  f2 = fmaf(__ldg(cf + 38 * C), x[1]*x[4]*x[15], f2);
-  f3 = fmaf(__ldg(cf + 39 * C), x[1]*x[5]*x[12], f3);
-  f0 = fmaf(__ldg(cf + 40 * C), x[1]*x[5]*x[14], f0);
-  f1 = fmaf(__ldg(cf + 41 * C), x[1]*x[6]*x[11], f1);
-  f2 = fmaf(__ldg(cf + 42 * C), x[1]*x[7]*x[10], f2);
-  f3 = fmaf(__ldg(cf + 43 * C), x[1]*x[8]*x[9], f3);
-  f0 = fmaf(__ldg(cf + 44 * C), x[1]*x[8]*x[11], f0);
-  f1 = fmaf(__ldg(cf + 45 * C), x[2]*x[2]*x[6], f1);
-  f2 = fmaf(__ldg(cf + 46 * C), x[2]*x[3]*x[7], f2);
-  f3 = fmaf(__ldg(cf + 47 * C), x[2]*x[4]*x[10], f3);
-  f0 = fmaf(__ldg(cf + 48 * C), x[2]*x[5]*x[11], f0);
-  f1 = fmaf(__ldg(cf + 49 * C), x[2]*x[6]*x[12], f1);
-  f2 = fmaf(__ldg(cf + 50 * C), x[2]*x[7]*x[13], f2);
-  f3 = fmaf(__ldg(cf + 51 * C), x[2]*x[8]*x[14], f3);
-  f0 = fmaf(__ldg(cf + 52 * C), x[3]*x[3]*x[6], f0);
-  f1 = fmaf(__ldg(cf + 53 * C), x[3]*x[3]*x[8], f1);
-  f2 = fmaf(__ldg(cf + 54 * C), x[3]*x[4]*x[9], f2);
-  f3 = fmaf(__ldg(cf + 55 * C), x[3]*x[4]*x[11], f3);
-  f0 = fmaf(__ldg(cf + 56 * C), x[3]*x[5]*x[10], f0);
-  f1 = fmaf(__ldg(cf + 57 * C), x[3]*x[6]*x[13], f1);
-  f2 = fmaf(__ldg(cf + 58 * C), x[3]*x[7]*x[12], f2);
-  f3 = fmaf(__ldg(cf + 59 * C), x[3]*x[7]*x[14], f3);
-  f0 = fmaf(__ldg(cf + 60 * C), x[3]*x[8]*x[13], f0);
-  f1 = fmaf(__ldg(cf + 61 * C), x[3]*x[8]*x[15], f1);
-  f2 = fmaf(__ldg(cf + 62 * C), x[4]*x[4]*x[6], f2);
-  f3 = fmaf(__ldg(cf + 63 * C), x[4]*x[5]*x[7], f3);
-  f0 = fmaf(__ldg(cf + 64 * C), x[4]*x[9]*x[13], f0);
-  f1 = fmaf(__ldg(cf + 65 * C), x[4]*x[10]*x[12], f1);
-  f2 = fmaf(__ldg(cf + 66 * C), x[4]*x[11]*x[13], f2);
-  f3 = fmaf(__ldg(cf + 67 * C), x[4]*x[11]*x[15], f3);
-  f0 = fmaf(__ldg(cf + 68 * C), x[5]*x[5]*x[6], f0);
-  f1 = fmaf(__ldg(cf + 69 * C), x[5]*x[5]*x[8], f1);
-  f2 = fmaf(__ldg(cf + 70 * C), x[5]*x[9]*x[14], f2);
-  f3 = fmaf(__ldg(cf + 71 * C), x[5]*x[10]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 72 * C), x[5]*x[10]*x[15], f0);
-  f1 = fmaf(__ldg(cf + 73 * C), x[5]*x[11]*x[12], f1);
-  f2 = fmaf(__ldg(cf + 74 * C), x[5]*x[11]*x[14], f2);
-  f3 = fmaf(__ldg(cf + 75 * C), x[6]*x[6]*x[6], f3);
-  f0 = fmaf(__ldg(cf + 76 * C), x[6]*x[7]*x[7], f0);
-  f1 = fmaf(__ldg(cf + 77 * C), x[6]*x[8]*x[8], f1);
-  f2 = fmaf(__ldg(cf + 78 * C), x[6]*x[9]*x[9], f2);
-  f3 = fmaf(__ldg(cf + 79 * C), x[6]*x[11]*x[11], f3);
-  f0 = fmaf(__ldg(cf + 80 * C), x[6]*x[12]*x[12], f0);
-  f1 = fmaf(__ldg(cf + 81 * C), x[6]*x[13]*x[13], f1);
-  f2 = fmaf(__ldg(cf + 82 * C), x[6]*x[15]*x[15], f2);
-  f3 = fmaf(__ldg(cf + 83 * C), x[7]*x[7]*x[8], f3);
-  f0 = fmaf(__ldg(cf + 84 * C), x[7]*x[9]*x[10], f0);
-  f1 = fmaf(__ldg(cf + 85 * C), x[7]*x[10]*x[11], f1);
-  f2 = fmaf(__ldg(cf + 86 * C), x[7]*x[12]*x[13], f2);
-  f3 = fmaf(__ldg(cf + 87 * C), x[7]*x[13]*x[14], f3);
-  f0 = fmaf(__ldg(cf + 88 * C), x[7]*x[14]*x[15], f0);
-  f1 = fmaf(__ldg(cf + 89 * C), x[8]*x[9]*x[11], f1);
-  f2 = fmaf(__ldg(cf + 90 * C), x[8]*x[11]*x[11], f2);
-  f3 = fmaf(__ldg(cf + 91 * C), x[8]*x[12]*x[14], f3);
-  f0 = fmaf(__ldg(cf + 92 * C), x[8]*x[13]*x[13], f0);
-  f1 = fmaf(__ldg(cf + 93 * C), x[8]*x[13]*x[15], f1);
-  return (f0 + f1) + (f2 + f3);
+  float f = 0.0f;
+  f = fmaf(__ldg(cf + 0 * C), x[0], f);
+  f = fmaf(__ldg(cf + 1 * C), x[0]*x[0], f);
+  f = fmaf(__ldg(cf + 2 * C), x[1]*x[1], f);
+  f = fmaf(__ldg(cf + 3 * C), x[2]*x[2], f);
+  f = fmaf(__ldg(cf + 4 * C), x[3]*x[3], f);
+  f = fmaf(__ldg(cf + 5 * C), x[4]*x[4], f);
+  f = fmaf(__ldg(cf + 6 * C), x[5]*x[5], f);
+  f = fmaf(__ldg(cf + 7 * C), x[6]*x[6], f);
+  f = fmaf(__ldg(cf + 8 * C), x[7]*x[7], f);
+  f = fmaf(__ldg(cf + 9 * C), x[8]*x[8], f);
+  f = fmaf(__ldg(cf + 10 * C), x[9]*x[9], f);
+  f = fmaf(__ldg(cf + 11 * C), x[10]*x[10], f);
+  f = fmaf(__ldg(cf + 12 * C), x[11]*x[11], f);
+  f = fmaf(__ldg(cf + 13 * C), x[12]*x[12], f);
+  f = fmaf(__ldg(cf + 14 * C), x[13]*x[13], f);
+  f = fmaf(__ldg(cf + 15 * C), x[14]*x[14], f);
+  f = fmaf(__ldg(cf + 16 * C), x[15]*x[15], f);
+  f = fmaf(__ldg(cf + 17 * C), x[0]*x[0]*x[0], f);
+  f = fmaf(__ldg(cf + 18 * C), x[0]*x[1]*x[1], f);
+  f = fmaf(__ldg(cf + 19 * C), x[0]*x[2]*x[2], f);
+  f = fmaf(__ldg(cf + 20 * C), x[0]*x[3]*x[3], f);
+  f = fmaf(__ldg(cf + 21 * C), x[0]*x[4]*x[4], f);
+  f = fmaf(__ldg(cf + 22 * C), x[0]*x[5]*x[5], f);
+  f = fmaf(__ldg(cf + 23 * C), x[0]*x[6]*x[6], f);
+  f = fmaf(__ldg(cf + 24 * C), x[0]*x[7]*x[7], f);
+  f = fmaf(__ldg(cf + 25 * C), x[0]*x[8]*x[8], f);
+  f = fmaf(__ldg(cf + 26 * C), x[0]*x[9]*x[9], f);
+  f = fmaf(__ldg(cf + 27 * C), x[0]*x[10]*x[10], f);
+  f = fmaf(__ldg(cf + 28 * C), x[0]*x[11]*x[11], f);
+  f = fmaf(__ldg(cf + 29 * C), x[0]*x[12]*x[12], f);
+  f = fmaf(__ldg(cf + 30 * C), x[0]*x[13]*x[13], f);
+  f = fmaf(__ldg(cf + 31 * C), x[0]*x[14]*x[14], f);
+  f = fmaf(__ldg(cf + 32 * C), x[0]*x[15]*x[15], f);
+  f = fmaf(__ldg(cf + 33 * C), x[1]*x[1]*x[6], f);
+  f = fmaf(__ldg(cf + 34 * C), x[1]*x[1]*x[8], f);
+  f = fmaf(__ldg(cf + 35 * C), x[1]*x[2]*x[5], f);
+  f = fmaf(__ldg(cf + 36 * C), x[1]*x[3]*x[4], f);
+  f = fmaf(__ldg(cf + 37 * C), x[1]*x[4]*x[13], f);
+  f = fmaf(__ldg(cf + 38 * C), x[1]*x[4]*x[15], f);
+  f = fmaf(__ldg(cf + 39 * C), x[1]*x[5]*x[12], f);
+  f = fmaf(__ldg(cf + 40 * C), x[1]*x[5]*x[14], f);
+  f = fmaf(__ldg(cf + 41 * C), x[1]*x[6]*x[11], f);
+  f = fmaf(__ldg(cf + 42 * C), x[1]*x[7]*x[10], f);
+  f = fmaf(__ldg(cf + 43 * C), x[1]*x[8]*x[9], f);
+  f = fmaf(__ldg(cf + 44 * C), x[1]*x[8]*x[11], f);
+  f = fmaf(__ldg(cf + 45 * C), x[2]*x[2]*x[6], f);
+  f = fmaf(__ldg(cf + 46 * C), x[2]*x[3]*x[7], f);
+  f = fmaf(__ldg(cf + 47 * C), x[2]*x[4]*x[10], f);
+  f = fmaf(__ldg(cf + 48 * C), x[2]*x[5]*x[11], f);
+  f = fmaf(__ldg(cf + 49 * C), x[2]*x[6]*x[12], f);
+  f = fmaf(__ldg(cf + 50 * C), x[2]*x[7]*x[13], f);
+  f = fmaf(__ldg(cf + 51 * C), x[2]*x[8]*x[14], f);
+  f = fmaf(__ldg(cf + 52 * C), x[3]*x[3]*x[6], f);
+  f = fmaf(__ldg(cf + 53 * C), x[3]*x[3]*x[8], f);
+  f = fmaf(__ldg(cf + 54 * C), x[3]*x[4]*x[9], f);
+  f = fmaf(__ldg(cf + 55 * C), x[3]*x[4]*x[11], f);
+  f = fmaf(__ldg(cf + 56 * C), x[3]*x[5]*x[10], f);
+  f = fmaf(__ldg(cf + 57 * C), x[3]*x[6]*x[13], f);
+  f = fmaf(__ldg(cf + 58 * C), x[3]*x[7]*x[12], f);
+  f = fmaf(__ldg(cf + 59 * C), x[3]*x[7]*x[14], f);
+  f = fmaf(__ldg(cf + 60 * C), x[3]*x[8]*x[13], f);
+  f = fmaf(__ldg(cf + 61 * C), x[3]*x[8]*x[15], f);
+  f = fmaf(__ldg(cf + 62 * C), x[4]*x[4]*x[6], f);
+  f = fmaf(__ldg(cf + 63 * C), x[4]*x[5]*x[7], f);
+  f = fmaf(__ldg(cf + 64 * C), x[4]*x[9]*x[13], f);
+  f = fmaf(__ldg(cf + 65 * C), x[4]*x[10]*x[12], f);
+  f = fmaf(__ldg(cf + 66 * C), x[4]*x[11]*x[13], f);
+  f = fmaf(__ldg(cf + 67 * C), x[4]*x[11]*x[15], f);
+  f = fmaf(__ldg(cf + 68 * C), x[5]*x[5]*x[6], f);
+  f = fmaf(__ldg(cf + 69 * C), x[5]*x[5]*x[8], f);
+  f = fmaf(__ldg(cf + 70 * C), x[5]*x[9]*x[14], f);
+  f = fmaf(__ldg(cf + 71 * C), x[5]*x[10]*x[13], f);
+  f = fmaf(__ldg(cf + 72 * C), x[5]*x[10]*x[15], f);
+  f = fmaf(__ldg(cf + 73 * C), x[5]*x[11]*x[12], f);
+  f = fmaf(__ldg(cf + 74 * C), x[5]*x[11]*x[14], f);
+  f = fmaf(__ldg(cf + 75 * C), x[6]*x[6]*x[6], f);
+  f = fmaf(__ldg(cf + 76 * C), x[6]*x[7]*x[7], f);
+  f = fmaf(__ldg(cf + 77 * C), x[6]*x[8]*x[8], f);
+  f = fmaf(__ldg(cf + 78 * C), x[6]*x[9]*x[9], f);
+  f = fmaf(__ldg(cf + 79 * C), x[6]*x[11]*x[11], f);
+  f = fmaf(__ldg(cf + 80 * C), x[6]*x[12]*x[12], f);
+  f = fmaf(__ldg(cf + 81 * C), x[6]*x[13]*x[13], f);
+  f = fmaf(__ldg(cf + 82 * C), x[6]*x[15]*x[15], f);
+  f = fmaf(__ldg(cf + 83 * C), x[7]*x[7]*x[8], f);
+  f = fmaf(__ldg(cf + 84 * C), x[7]*x[9]*x[10], f);
+  f = fmaf(__ldg(cf + 85 * C), x[7]*x[10]*x[11], f);
+  f = fmaf(__ldg(cf + 86 * C), x[7]*x[12]*x[13], f);
+  f = fmaf(__ldg(cf + 87 * C), x[7]*x[13]*x[14], f);
+  f = fmaf(__ldg(cf + 88 * C), x[7]*x[14]*x[15], f);
+  f = fmaf(__ldg(cf + 89 * C), x[8]*x[9]*x[11], f);
+  f = fmaf(__ldg(cf + 90 * C), x[8]*x[11]*x[11], f);
+  f = fmaf(__ldg(cf + 91 * C), x[8]*x[12]*x[14], f);
+  f = fmaf(__ldg(cf + 92 * C), x[8]*x[13]*x[13], f);
+  f = fmaf(__ldg(cf + 93 * C), x[8]*x[13]*x[15], f);
+  return f;
 }
 
 __device__ __forceinline__ void grad_LM0(const float* x, float w, const float* __restrict__ cf, int C, float* g) {
@@ -562,120 +562,120 @@ __device__ __forceinline__ void grad_LM0(const float* x, float w, const float* _
 }
 
 __device__ __forceinline__ float value_LM1(const float* x, const float* __restrict__ cf, int C) {
-  float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f, f3 = 0.0f;
-  f0 = fmaf(__ldg(cf + 0 * C), x[1], f0);
-  f1 = fmaf(__ldg(cf + 1 * C), x[0]*x[1], f1);
-  f2 = fmaf(__ldg(cf + 2 * C), x[1]*x[6], f2);
-  f3 = fmaf(__ldg(cf + 3 * C), x[1]*x[8], f3);
-  f0 = fmaf(__ldg(cf + 4 * C), x[2]*x[5], f0);
-  f1 = fmaf(__ldg(cf + 5 * C), x[3]*x[4], f1);
-  f2 = fmaf(__ldg(cf + 6 * C), x[4]*x[13], f2);
-  f3 = fmaf(__ldg(cf + 7 * C), x[4]*x[15], f3);
-  f0 = fmaf(__ldg(cf + 8 * C), x[5]*x[12], f0);
-  f1 = fmaf(__ldg(cf + 9 * C), x[5]*x[14], f1);
-  f2 = fmaf(__ldg(cf + 10 * C), x[6]*x[11], f2);
-  f3 = fmaf(__ldg(cf + 11 * C), x[7]*x[10], f3);
-  f0 = fmaf(__ldg(cf + 12 * C), x[8]*x[9], f0);
-  f1 = fmaf(__ldg(cf + 13 * C), x[8]*x[11], f1);
-  f2 = fmaf(__ldg(cf + 14 * C), x[0]*x[0]*x[1], f2);
-  f3 = fmaf(__ldg(cf + 15 * C), x[0]*x[1]*x[6], f3);
-  f0 = fmaf(__ldg(cf + 16 * C), x[0]*x[1]*x[8], f0);
-  f1 = fmaf(__ldg(cf + 17 * C), x[0]*x[2]*x[5], f1);
-  f2 = fmaf(__ldg(cf + 18 * C), x[0]*x[3]*x[4], f2);
-  f3 = fmaf(__ldg(cf + 19 * C), x[0]*x[4]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 20 * C), x[0]*x[4]*x[15], f0);
-  f1 = fmaf(__ldg(cf + 21 * C), x[0]*x[5]*x[12], f1);
-  f2 = fmaf(__ldg(cf + 22 * C), x[0]*x[5]*x[14], f2);
-  f3 = fmaf(__ldg(cf + 23 * C), x[0]*x[6]*x[11], f3);
-  f0 = fmaf(__ldg(cf + 24 * C), x[0]*x[7]*x[10], f0);
-  f1 = fmaf(__ldg(cf + 25 * C), x[0]*x[8]*x[9], f1);
-  f2 = fmaf(__ldg(cf + 26 * C), x[0]*x[8]*x[11], f2);
-  f3 = fmaf(__ldg(cf + 27 * C), x[1]*x[1]*x[1], f3);
-  f0 = fmaf(__ldg(cf + 28 * C), x[1]*x[1]*x[9], f0);
-  f1 = fmaf(__ldg(cf + 29 * C), x[1]*x[1]*x[11], f1);
-  f2 = fmaf(__ldg(cf + 30 * C), x[1]*x[2]*x[2], f2);
-  f3 = fmaf(__ldg(cf + 31 * C), x[1]*x[2]*x[12], f3);
-  f0 = fmaf(__ldg(cf + 32 * C), x[1]*x[2]*x[14], f0);
-  f1 = fmaf(__ldg(cf + 33 * C), x[1]*x[3]*x[3], f1);
-  f2 = fmaf(__ldg(cf + 34 * C), x[1]*x[3]*x[13], f2);
-  f3 = fmaf(__ldg(cf + 35 * C), x[1]*x[3]*x[15], f3);
-  f0 = fmaf(__ldg(cf + 36 * C), x[1]*x[4]*x[4], f0);
-  f1 = fmaf(__ldg(cf + 37 * C), x[1]*x[5]*x[5], f1);
-  f2 = fmaf(__ldg(cf + 38 * C), x[1]*x[6]*x[6], f2);
-  f3 = fmaf(__ldg(cf + 39 * C), x[1]*x[6]*x[8], f3);
-  f0 = fmaf(__ldg(cf + 40 * C), x[1]*x[7]*x[7], f0);
-  f1 = fmaf(__ldg(cf + 41 * C), x[1]*x[8]*x[8], f1);
-  f2 = fmaf(__ldg(cf + 42 * C), x[1]*x[9]*x[9], f2);
-  f3 = fmaf(__ldg(cf + 43 * C), x[1]*x[9]*x[11], f3);
-  f0 = fmaf(__ldg(cf + 44 * C), x[1]*x[10]*x[10], f0);
-  f1 = fmaf(__ldg(cf + 45 * C), x[1]*x[11]*x[11], f1);
-  f2 = fmaf(__ldg(cf + 46 * C), x[1]*x[12]*x[12], f2);
-  f3 = fmaf(__ldg(cf + 47 * C), x[1]*x[12]*x[14], f3);
-  f0 = fmaf(__ldg(cf + 48 * C), x[1]*x[13]*x[13], f0);
-  f1 = fmaf(__ldg(cf + 49 * C), x[1]*x[13]*x[15], f1);
-  f2 = fmaf(__ldg(cf + 50 * C), x[1]*x[14]*x[14], f2);
-  f3 = fmaf(__ldg(cf + 51 * C), x[1]*x[15]*x[15], f3);
-  f0 = fmaf(__ldg(cf + 52 * C), x[2]*x[2]*x[11], f0);
-  f1 = fmaf(__ldg(cf + 53 * C), x[2]*x[3]*x[10], f1);
-  f2 = fmaf(__ldg(cf + 54 * C), x[2]*x[4]*x[7], f2);
-  f3 = fmaf(__ldg(cf + 55 * C), x[2]*x[5]*x[6], f3);
-  f0 = fmaf(__ldg(cf + 56 * C), x[2]*x[5]*x[8], f0);
-  f1 = fmaf(__ldg(cf + 57 * C), x[2]*x[9]*x[14], f1);
-  f2 = fmaf(__ldg(cf + 58 * C), x[2]*x[10]*x[13], f2);
-  f3 = fmaf(__ldg(cf + 59 * C), x[2]*x[10]*x[15], f3);
-  f0 = fmaf(__ldg(cf + 60 * C), x[2]*x[11]*x[12], f0);
-  f1 = fmaf(__ldg(cf + 61 * C), x[2]*x[11]*x[14], f1);
-  f2 = fmaf(__ldg(cf + 62 * C), x[3]*x[3]*x[9], f2);
-  f3 = fmaf(__ldg(cf + 63 * C), x[3]*x[3]*x[11], f3);
-  f0 = fmaf(__ldg(cf + 64 * C), x[3]*x[4]*x[6], f0);
-  f1 = fmaf(__ldg(cf + 65 * C), x[3]*x[5]*x[7], f1);
-  f2 = fmaf(__ldg(cf + 66 * C), x[3]*x[9]*x[13], f2);
-  f3 = fmaf(__ldg(cf + 67 * C), x[3]*x[10]*x[12], f3);
-  f0 = fmaf(__ldg(cf + 68 * C), x[3]*x[11]*x[13], f0);
-  f1 = fmaf(__ldg(cf + 69 * C), x[3]*x[11]*x[15], f1);
-  f2 = fmaf(__ldg(cf + 70 * C), x[4]*x[4]*x[9], f2);
-  f3 = fmaf(__ldg(cf + 71 * C), x[4]*x[4]*x[11], f3);
-  f0 = fmaf(__ldg(cf + 72 * C), x[4]*x[5]*x[10], f0);
-  f1 = fmaf(__ldg(cf + 73 * C), x[4]*x[6]*x[13], f1);
-  f2 = fmaf(__ldg(cf + 74 * C), x[4]*x[6]*x[15], f2);
-  f3 = fmaf(__ldg(cf + 75 * C), x[4]*x[7]*x[12], f3);
-  f0 = fmaf(__ldg(cf + 76 * C), x[4]*x[7]*x[14], f0);
-  f1 = fmaf(__ldg(cf + 77 * C), x[4]*x[8]*x[15], f1);
-  f2 = fmaf(__ldg(cf + 78 * C), x[5]*x[5]*x[9], f2);
-  f3 = fmaf(__ldg(cf + 79 * C), x[5]*x[5]*x[11], f3);
-  f0 = fmaf(__ldg(cf + 80 * C), x[5]*x[6]*x[12], f0);
-  f1 = fmaf(__ldg(cf + 81 * C), x[5]*x[6]*x[14], f1);
-  f2 = fmaf(__ldg(cf + 82 * C), x[5]*x[7]*x[13], f2);
-  f3 = fmaf(__ldg(cf + 83 * C), x[5]*x[7]*x[15], f3);
-  f0 = fmaf(__ldg(cf + 84 * C), x[5]*x[8]*x[12], f0);
-  f1 = fmaf(__ldg(cf + 85 * C), x[5]*x[8]*x[14], f1);
-  f2 = fmaf(__ldg(cf + 86 * C), x[6]*x[6]*x[11], f2);
-  f3 = fmaf(__ldg(cf + 87 * C), x[6]*x[7]*x[10], f3);
-  f0 = fmaf(__ldg(cf + 88 * C), x[6]*x[8]*x[9], f0);
-  f1 = fmaf(__ldg(cf + 89 * C), x[6]*x[8]*x[11], f1);
-  f2 = fmaf(__ldg(cf + 90 * C), x[7]*x[7]*x[9], f2);
-  f3 = fmaf(__ldg(cf + 91 * C), x[7]*x[7]*x[11], f3);
-  f0 = fmaf(__ldg(cf + 92 * C), x[7]*x[8]*x[10], f0);
-  f1 = fmaf(__ldg(cf + 93 * C), x[8]*x[8]*x[9], f1);
-  f2 = fmaf(__ldg(cf + 94 * C), x[8]*x[8]*x[11], f2);
-  f3 = fmaf(__ldg(cf + 95 * C), x[9]*x[9]*x[11], f3);
-  f0 = fmaf(__ldg(cf + 96 * C), x[9]*x[10]*x[10], f0);
-  f1 = fmaf(__ldg(cf + 97 * C), x[9]*x[11]*x[11], f1);
-  f2 = fmaf(__ldg(cf + 98 * C), x[9]*x[12]*x[14], f2);
-  f3 = fmaf(__ldg(cf + 99 * C), x[9]*x[13]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 100 * C), x[9]*x[14]*x[14], f0);
-  f1 = fmaf(__ldg(cf + 101 * C), x[10]*x[10]*x[11], f1);
-  f2 = fmaf(__ldg(cf + 102 * C), x[10]*x[12]*x[13], f2);
-  f3 = fmaf(__ldg(cf + 103 * C), x[10]*x[12]*x[15], f3);
-  f0 = fmaf(__ldg(cf + 104 * C), x[10]*x[14]*x[15], f0);
-  f1 = fmaf(__ldg(cf + 105 * C), x[11]*x[11]*x[11], f1);
-  f2 = fmaf(__ldg(cf + 106 * C), x[11]*x[12]*x[12], f2);
-  f3 = fmaf(__ldg(cf + 107 * C), x[11]*x[12]*x[14], f3);
-  f0 = fmaf(__ldg(cf + 108 * C), x[11]*x[13]*x[13], f0);
-  f1 = fmaf(__ldg(cf + 109 * C), x[11]*x[13]*x[15], f1);
-  f2 = fmaf(__ldg(cf + 110 * C), x[11]*x[14]*x[14], f2);
-  f3 = fmaf(__ldg(cf + 111 * C), x[11]*x[15]*x[15], f3);
-  return (f0 + f1) + (f2 + f3);
+  float f = 0.0f;
+  f = fmaf(__ldg(cf + 0 * C), x[1], f);
+  f = fmaf(__ldg(cf + 1 * C), x[0]*x[1], f);
+  f = fmaf(__ldg(cf + 2 * C), x[1]*x[6], f);
+  f = fmaf(__ldg(cf + 3 * C), x[1]*x[8], f);
+  f = fmaf(__ldg(cf + 4 * C), x[2]*x[5], f);
+  f = fmaf(__ldg(cf + 5 * C), x[3]*x[4], f);
+  f = fmaf(__ldg(cf + 6 * C), x[4]*x[13], f);
+  f = fmaf(__ldg(cf + 7 * C), x[4]*x[15], f);
+  f = fmaf(__ldg(cf + 8 * C), x[5]*x[12], f);
+  f = fmaf(__ldg(cf + 9 * C), x[5]*x[14], f);
+  f = fmaf(__ldg(cf + 10 * C), x[6]*x[11], f);
+  f = fmaf(__ldg(cf + 11 * C), x[7]*x[10], f);
+  f = fmaf(__ldg(cf + 12 * C), x[8]*x[9], f);
+  f = fmaf(__ldg(cf + 13 * C), x[8]*x[11], f);
+  f = fmaf(__ldg(cf + 14 * C), x[0]*x[0]*x[1], f);
+  f = fmaf(__ldg(cf + 15 * C), x[0]*x[1]*x[6], f);
+  f = fmaf(__ldg(cf + 16 * C), x[0]*x[1]*x[8], f);
+  f = fmaf(__ldg(cf + 17 * C), x[0]*x[2]*x[5], f);
+  f = fmaf(__ldg(cf + 18 * C), x[0]*x[3]*x[4], f);
+  f = fmaf(__ldg(cf + 19 * C), x[0]*x[4]*x[13], f);
+  f = fmaf(__ldg(cf + 20 * C), x[0]*x[4]*x[15], f);
+  f = fmaf(__ldg(cf + 21 * C), x[0]*x[5]*x[12], f);
+  f = fmaf(__ldg(cf + 22 * C), x[0]*x[5]*x[14], f);
+  f = fmaf(__ldg(cf + 23 * C), x[0]*x[6]*x[11], f);
+  f = fmaf(__ldg(cf + 24 * C), x[0]*x[7]*x[10], f);
+  f = fmaf(__ldg(cf + 25 * C), x[0]*x[8]*x[9], f);
+  f = fmaf(__ldg(cf + 26 * C), x[0]*x[8]*x[11], f);
+  f = fmaf(__ldg(cf + 27 * C), x[1]*x[1]*x[1], f);
+  f = fmaf(__ldg(cf + 28 * C), x[1]*x[1]*x[9], f);
+  f = fmaf(__ldg(cf + 29 * C), x[1]*x[1]*x[11], f);
+  f = fmaf(__ldg(cf + 30 * C), x[1]*x[2]*x[2], f);
+  f = fmaf(__ldg(cf + 31 * C), x[1]*x[2]*x[12], f);
+  f = fmaf(__ldg(cf + 32 * C), x[1]*x[2]*x[14], f);
+  f = fmaf(__ldg(cf + 33 * C), x[1]*x[3]*x[3], f);
+  f = fmaf(__ldg(cf + 34 * C), x[1]*x[3]*x[13], f);
+  f = fmaf(__ldg(cf + 35 * C), x[1]*x[3]*x[15], f);
+  f = fmaf(__ldg(cf + 36 * C), x[1]*x[4]*x[4], f);
+  f = fmaf(__ldg(cf + 37 * C), x[1]*x[5]*x[5], f);
+  f = fmaf(__ldg(cf + 38 * C), x[1]*x[6]*x[6], f);
+  f = fmaf(__ldg(cf + 39 * C), x[1]*x[6]*x[8], f);
+  f = fmaf(__ldg(cf + 40 * C), x[1]*x[7]*x[7], f);
+  f = fmaf(__ldg(cf + 41 * C), x[1]*x[8]*x[8], f);
+  f = fmaf(__ldg(cf + 42 * C), x[1]*x[9]*x[9], f);
+  f = fmaf(__ldg(cf + 43 * C), x[1]*x[9]*x[11], f);
+  f = fmaf(__ldg(cf + 44 * C), x[1]*x[10]*x[10], f);
+  f = fmaf(__ldg(cf + 45 * C), x[1]*x[11]*x[11], f);
+  f = fmaf(__ldg(cf + 46 * C), x[1]*x[12]*x[12], f);
+  f = fmaf(__ldg(cf + 47 * C), x[1]*x[12]*x[14], f);
+  f = fmaf(__ldg(cf + 48 * C), x[1]*x[13]*x[13], f);
+  f = fmaf(__ldg(cf + 49 * C), x[1]*x[13]*x[15], f);
+  f = fmaf(__ldg(cf + 50 * C), x[1]*x[14]*x[14], f);
+  f = fmaf(__ldg(cf + 51 * C), x[1]*x[15]*x[15], f);
+  f = fmaf(__ldg(cf + 52 * C), x[2]*x[2]*x[11], f);
+  f = fmaf(__ldg(cf + 53 * C), x[2]*x[3]*x[10], f);
+  f = fmaf(__ldg(cf + 54 * C), x[2]*x[4]*x[7], f);
+  f = fmaf(__ldg(cf + 55 * C), x[2]*x[5]*x[6], f);
+  f = fmaf(__ldg(cf + 56 * C), x[2]*x[5]*x[8], f);
+  f = fmaf(__ldg(cf + 57 * C), x[2]*x[9]*x[14], f);
+  f = fmaf(__ldg(cf + 58 * C), x[2]*x[10]*x[13], f);
+  f = fmaf(__ldg(cf + 59 * C), x[2]*x[10]*x[15], f);
+  f = fmaf(__ldg(cf + 60 * C), x[2]*x[11]*x[12], f);
+  f = fmaf(__ldg(cf + 61 * C), x[2]*x[11]*x[14], f);
+  f = fmaf(__ldg(cf + 62 * C), x[3]*x[3]*x[9], f);
+  f = fmaf(__ldg(cf + 63 * C), x[3]*x[3]*x[11], f);
+  f = fmaf(__ldg(cf + 64 * C), x[3]*x[4]*x[6], f);
+  f = fmaf(__ldg(cf + 65 * C), x[3]*x[5]*x[7], f);
+  f = fmaf(__ldg(cf + 66 * C), x[3]*x[9]*x[13], f);
+  f = fmaf(__ldg(cf + 67 * C), x[3]*x[10]*x[12], f);
+  f = fmaf(__ldg(cf + 68 * C), x[3]*x[11]*x[13], f);
+  f = fmaf(__ldg(cf + 69 * C), x[3]*x[11]*x[15], f);
+  f = fmaf(__ldg(cf + 70 * C), x[4]*x[4]*x[9], f);
+  f = fmaf(__ldg(cf + 71 * C), x[4]*x[4]*x[11], f);
+  f = fmaf(__ldg(cf + 72 * C), x[4]*x[5]*x[10], f);
+  f = fmaf(__ldg(cf + 73 * C), x[4]*x[6]*x[13], f);
+  f = fmaf(__ldg(cf + 74 * C), x[4]*x[6]*x[15], f);
+  f = fmaf(__ldg(cf + 75 * C), x[4]*x[7]*x[12], f);
+  f = fmaf(__ldg(cf + 76 * C), x[4]*x[7]*x[14], f);
+  f = fmaf(__ldg(cf + 77 * C), x[4]*x[8]*x[15], f);
+  f = fmaf(__ldg(cf + 78 * C), x[5]*x[5]*x[9], f);
+  f = fmaf(__ldg(cf + 79 * C), x[5]*x[5]*x[11], f);
+  f = fmaf(__ldg(cf + 80 * C), x[5]*x[6]*x[12], f);
+  f = fmaf(__ldg(cf + 81 * C), x[5]*x[6]*x[14], f);
+  f = fmaf(__ldg(cf + 82 * C), x[5]*x[7]*x[13], f);
+  f = fmaf(__ldg(cf + 83 * C), x[5]*x[7]*x[15], f);
+  f = fmaf(__ldg(cf + 84 * C), x[5]*x[8]*x[12], f);
+  f = fmaf(__ldg(cf + 85 * C), x[5]*x[8]*x[14], f);
+  f = fmaf(__ldg(cf + 86 * C), x[6]*x[6]*x[11], f);
+  f = fmaf(__ldg(cf + 87 * C), x[6]*x[7]*x[10], f);
+  f = fmaf(__ldg(cf + 88 * C), x[6]*x[8]*x[9], f);
+  f = fmaf(__ldg(cf + 89 * C), x[6]*x[8]*x[11], f);
+  f = fmaf(__ldg(cf + 90 * C), x[7]*x[7]*x[9], f);
+  f = fmaf(__ldg(cf + 91 * C), x[7]*x[7]*x[11], f);
+  f = fmaf(__ldg(cf + 92 * C), x[7]*x[8]*x[10], f);
+  f = fmaf(__ldg(cf + 93 * C), x[8]*x[8]*x[9], f);
+  f = fmaf(__ldg(cf + 94 * C), x[8]*x[8]*x[11], f);
+  f = fmaf(__ldg(cf + 95 * C), x[9]*x[9]*x[11], f);
+  f = fmaf(__ldg(cf + 96 * C), x[9]*x[10]*x[10], f);
+  f = fmaf(__ldg(cf + 97 * C), x[9]*x[11]*x[11], f);
+  f = fmaf(__ldg(cf + 98 * C), x[9]*x[12]*x[14], f);
+  f = fmaf(__ldg(cf + 99 * C), x[9]*x[13]*x[13], f);
+  f = fmaf(__ldg(cf + 100 * C), x[9]*x[14]*x[14], f);
+  f = fmaf(__ldg(cf + 101 * C), x[10]*x[10]*x[11], f);
+  f = fmaf(__ldg(cf + 102 * C), x[10]*x[12]*x[13], f);
+  f = fmaf(__ldg(cf + 103 * C), x[10]*x[12]*x[15], f);
+  f = fmaf(__ldg(cf + 104 * C), x[10]*x[14]*x[15], f);
+  f = fmaf(__ldg(cf + 105 * C), x[11]*x[11]*x[11], f);
+  f = fmaf(__ldg(cf + 106 * C), x[11]*x[12]*x[12], f);
+  f = fmaf(__ldg(cf + 107 * C), x[11]*x[12]*x[14], f);
+  f = fmaf(__ldg(cf + 108 * C), x[11]*x[13]*x[13], f);
+  f = fmaf(__ldg(cf + 109 * C), x[11]*x[13]*x[15], f);
+  f = fmaf(__ldg(cf + 110 * C), x[11]*x[14]*x[14], f);
+  f = fmaf(__ldg(cf + 111 * C), x[11]*x[15]*x[15], f);
+  return f;
 }
 
 __device__ __forceinline__ void grad_LM1(const float* x, float w, const float* __restrict__ cf, int C, float* g) {
@@ -1227,100 +1227,100 @@ __device__ __forceinline__ void grad_LM1(const float* x, float w, const float* _
 }
 
 __device__ __forceinline__ float value_LM2(const float* x, const float* __restrict__ cf, int C) {
-  float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f, f3 = 0.0f;
-  f0 = fmaf(__ldg(cf + 0 * C), x[2], f0);
-  f1 = fmaf(__ldg(cf + 1 * C), x[0]*x[2], f1);
-  f2 = fmaf(__ldg(cf + 2 * C), x[1]*x[5], f2);
-  f3 = fmaf(__ldg(cf + 3 * C), x[2]*x[6], f3);
-  f0 = fmaf(__ldg(cf + 4 * C), x[3]*x[7], f0);
-  f1 = fmaf(__ldg(cf + 5 * C), x[4]*x[10], f1);
-  f2 = fmaf(__ldg(cf + 6 * C), x[5]*x[11], f2);
-  f3 = fmaf(__ldg(cf + 7 * C), x[6]*x[12], f3);
-  f0 = fmaf(__ldg(cf + 8 * C), x[7]*x[13], f0);
-  f1 = fmaf(__ldg(cf + 9 * C), x[8]*x[14], f1);
-  f2 = fmaf(__ldg(cf + 10 * C), x[0]*x[0]*x[2], f2);
-  f3 = fmaf(__ldg(cf + 11 * C), x[0]*x[1]*x[5], f3);
-  f0 = fmaf(__ldg(cf + 12 * C), x[0]*x[2]*x[6], f0);
-  f1 = fmaf(__ldg(cf + 13 * C), x[0]*x[3]*x[7], f1);
-  f2 = fmaf(__ldg(cf + 14 * C), x[0]*x[4]*x[10], f2);
-  f3 = fmaf(__ldg(cf + 15 * C), x[0]*x[5]*x[11], f3);
-  f0 = fmaf(__ldg(cf + 16 * C), x[0]*x[6]*x[12], f0);
-  f1 = fmaf(__ldg(cf + 17 * C), x[0]*x[7]*x[13], f1);
-  f2 = fmaf(__ldg(cf + 18 * C), x[0]*x[8]*x[14], f2);
-  f3 = fmaf(__ldg(cf + 19 * C), x[1]*x[1]*x[2], f3);
-  f0 = fmaf(__ldg(cf + 20 * C), x[1]*x[1]*x[12], f0);
-  f1 = fmaf(__ldg(cf + 21 * C), x[1]*x[1]*x[14], f1);
-  f2 = fmaf(__ldg(cf + 22 * C), x[1]*x[2]*x[11], f2);
-  f3 = fmaf(__ldg(cf + 23 * C), x[1]*x[3]*x[10], f3);
-  f0 = fmaf(__ldg(cf + 24 * C), x[1]*x[4]*x[7], f0);
-  f1 = fmaf(__ldg(cf + 25 * C), x[1]*x[5]*x[6], f1);
-  f2 = fmaf(__ldg(cf + 26 * C), x[1]*x[5]*x[8], f2);
-  f3 = fmaf(__ldg(cf + 27 * C), x[1]*x[9]*x[14], f3);
-  f0 = fmaf(__ldg(cf + 28 * C), x[1]*x[10]*x[13], f0);
-  f1 = fmaf(__ldg(cf + 29 * C), x[1]*x[10]*x[15], f1);
-  f2 = fmaf(__ldg(cf + 30 * C), x[1]*x[11]*x[12], f2);
-  f3 = fmaf(__ldg(cf + 31 * C), x[1]*x[11]*x[14], f3);
-  f0 = fmaf(__ldg(cf + 32 * C), x[2]*x[2]*x[2], f0);
-  f1 = fmaf(__ldg(cf + 33 * C), x[2]*x[2]*x[12], f1);
-  f2 = fmaf(__ldg(cf + 34 * C), x[2]*x[3]*x[3], f2);
-  f3 = fmaf(__ldg(cf + 35 * C), x[2]*x[3]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 36 * C), x[2]*x[4]*x[4], f0);
-  f1 = fmaf(__ldg(cf + 37 * C), x[2]*x[5]*x[5], f1);
-  f2 = fmaf(__ldg(cf + 38 * C), x[2]*x[6]*x[6], f2);
-  f3 = fmaf(__ldg(cf + 39 * C), x[2]*x[7]*x[7], f3);
-  f0 = fmaf(__ldg(cf + 40 * C), x[2]*x[8]*x[8], f0);
-  f1 = fmaf(__ldg(cf + 41 * C), x[2]*x[9]*x[9], f1);
-  f2 = fmaf(__ldg(cf + 42 * C), x[2]*x[10]*x[10], f2);
-  f3 = fmaf(__ldg(cf + 43 * C), x[2]*x[11]*x[11], f3);
-  f0 = fmaf(__ldg(cf + 44 * C), x[2]*x[12]*x[12], f0);
-  f1 = fmaf(__ldg(cf + 45 * C), x[2]*x[13]*x[13], f1);
-  f2 = fmaf(__ldg(cf + 46 * C), x[2]*x[14]*x[14], f2);
-  f3 = fmaf(__ldg(cf + 47 * C), x[2]*x[15]*x[15], f3);
-  f0 = fmaf(__ldg(cf + 48 * C), x[3]*x[3]*x[12], f0);
-  f1 = fmaf(__ldg(cf + 49 * C), x[3]*x[3]*x[14], f1);
-  f2 = fmaf(__ldg(cf + 50 * C), x[3]*x[4]*x[5], f2);
-  f3 = fmaf(__ldg(cf + 51 * C), x[3]*x[6]*x[7], f3);
-  f0 = fmaf(__ldg(cf + 52 * C), x[3]*x[7]*x[8], f0);
-  f1 = fmaf(__ldg(cf + 53 * C), x[3]*x[9]*x[10], f1);
-  f2 = fmaf(__ldg(cf + 54 * C), x[3]*x[10]*x[11], f2);
-  f3 = fmaf(__ldg(cf + 55 * C), x[3]*x[12]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 56 * C), x[3]*x[13]*x[14], f0);
-  f1 = fmaf(__ldg(cf + 57 * C), x[3]*x[14]*x[15], f1);
-  f2 = fmaf(__ldg(cf + 58 * C), x[4]*x[4]*x[12], f2);
-  f3 = fmaf(__ldg(cf + 59 * C), x[4]*x[5]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 60 * C), x[4]*x[5]*x[15], f0);
-  f1 = fmaf(__ldg(cf + 61 * C), x[4]*x[6]*x[10], f1);
-  f2 = fmaf(__ldg(cf + 62 * C), x[4]*x[7]*x[9], f2);
-  f3 = fmaf(__ldg(cf + 63 * C), x[4]*x[7]*x[11], f3);
-  f0 = fmaf(__ldg(cf + 64 * C), x[5]*x[5]*x[12], f0);
-  f1 = fmaf(__ldg(cf + 65 * C), x[5]*x[5]*x[14], f1);
-  f2 = fmaf(__ldg(cf + 66 * C), x[5]*x[6]*x[11], f2);
-  f3 = fmaf(__ldg(cf + 67 * C), x[5]*x[7]*x[10], f3);
-  f0 = fmaf(__ldg(cf + 68 * C), x[5]*x[8]*x[9], f0);
-  f1 = fmaf(__ldg(cf + 69 * C), x[5]*x[8]*x[11], f1);
-  f2 = fmaf(__ldg(cf + 70 * C), x[6]*x[6]*x[12], f2);
-  f3 = fmaf(__ldg(cf + 71 * C), x[6]*x[7]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 72 * C), x[6]*x[8]*x[14], f0);
-  f1 = fmaf(__ldg(cf + 73 * C), x[7]*x[7]*x[12], f1);
-  f2 = fmaf(__ldg(cf + 74 * C), x[7]*x[7]*x[14], f2);
-  f3 = fmaf(__ldg(cf + 75 * C), x[7]*x[8]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 76 * C), x[7]*x[8]*x[15], f0);
-  f1 = fmaf(__ldg(cf + 77 * C), x[8]*x[8]*x[12], f1);
-  f2 = fmaf(__ldg(cf + 78 * C), x[9]*x[9]*x[12], f2);
-  f3 = fmaf(__ldg(cf + 79 * C), x[9]*x[10]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 80 * C), x[9]*x[11]*x[14], f0);
-  f1 = fmaf(__ldg(cf + 81 * C), x[10]*x[10]*x[12], f1);
-  f2 = fmaf(__ldg(cf + 82 * C), x[10]*x[11]*x[13], f2);
-  f3 = fmaf(__ldg(cf + 83 * C), x[10]*x[11]*x[15], f3);
-  f0 = fmaf(__ldg(cf + 84 * C), x[11]*x[11]*x[12], f0);
-  f1 = fmaf(__ldg(cf + 85 * C), x[11]*x[11]*x[14], f1);
-  f2 = fmaf(__ldg(cf + 86 * C), x[12]*x[12]*x[12], f2);
-  f3 = fmaf(__ldg(cf + 87 * C), x[12]*x[13]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 88 * C), x[12]*x[14]*x[14], f0);
-  f1 = fmaf(__ldg(cf + 89 * C), x[12]*x[15]*x[15], f1);
-  f2 = fmaf(__ldg(cf + 90 * C), x[13]*x[13]*x[14], f2);
-  f3 = fmaf(__ldg(cf + 91 * C), x[13]*x[14]*x[15], f3);
-  return (f0 + f1) + (f2 + f3);
+  float f = 0.0f;
+  f = fmaf(__ldg(cf + 0 * C), x[2], f);
+  f = fmaf(__ldg(cf + 1 * C), x[0]*x[2], f);
+  f = fmaf(__ldg(cf + 2 * C), x[1]*x[5], f);
+  f = fmaf(__ldg(cf + 3 * C), x[2]*x[6], f);
+  f = fmaf(__ldg(cf + 4 * C), x[3]*x[7], f);
+  f = fmaf(__ldg(cf + 5 * C), x[4]*x[10], f);
+  f = fmaf(__ldg(cf + 6 * C), x[5]*x[11], f);
+  f = fmaf(__ldg(cf + 7 * C), x[6]*x[12], f);
+  f = fmaf(__ldg(cf + 8 * C), x[7]*x[13], f);
+  f = fmaf(__ldg(cf + 9 * C), x[8]*x[14], f);
+  f = fmaf(__ldg(cf + 10 * C), x[0]*x[0]*x[2], f);
+  f = fmaf(__ldg(cf + 11 * C), x[0]*x[1]*x[5], f);
+  f = fmaf(__ldg(cf + 12 * C), x[0]*x[2]*x[6], f);
+  f = fmaf(__ldg(cf + 13 * C), x[0]*x[3]*x[7], f);
+  f = fmaf(__ldg(cf + 14 * C), x[0]*x[4]*x[10], f);
+  f = fmaf(__ldg(cf + 15 * C), x[0]*x[5]*x[11], f);
+  f = fmaf(__ldg(cf + 16 * C), x[0]*x[6]*x[12], f);
+  f = fmaf(__ldg(cf + 17 * C), x[0]*x[7]*x[13], f);
+  f = fmaf(__ldg(cf + 18 * C), x[0]*x[8]*x[14], f);
+  f = fmaf(__ldg(cf + 19 * C), x[1]*x[1]*x[2], f);
+  f = fmaf(__ldg(cf + 20 * C), x[1]*x[1]*x[12], f);
+  f = fmaf(__ldg(cf + 21 * C), x[1]*x[1]*x[14], f);
+  f = fmaf(__ldg(cf + 22 * C), x[1]*x[2]*x[11], f);
+  f = fmaf(__ldg(cf + 23 * C), x[1]*x[3]*x[10], f);
+  f = fmaf(__ldg(cf + 24 * C), x[1]*x[4]*x[7], f);
+  f = fmaf(__ldg(cf + 25 * C), x[1]*x[5]*x[6], f);
+  f = fmaf(__ldg(cf + 26 * C), x[1]*x[5]*x[8], f);
+  f = fmaf(__ldg(cf + 27 * C), x[1]*x[9]*x[14], f);
+  f = fmaf(__ldg(cf + 28 * C), x[1]*x[10]*x[13], f);
+  f = fmaf(__ldg(cf + 29 * C), x[1]*x[10]*x[15], f);
+  f = fmaf(__ldg(cf + 30 * C), x[1]*x[11]*x[12], f);
+  f = fmaf(__ldg(cf + 31 * C), x[1]*x[11]*x[14], f);
+  f = fmaf(__ldg(cf + 32 * C), x[2]*x[2]*x[2], f);
+  f = fmaf(__ldg(cf + 33 * C), x[2]*x[2]*x[12], f);
+  f = fmaf(__ldg(cf + 34 * C), x[2]*x[3]*x[3], f);
+  f = fmaf(__ldg(cf + 35 * C), x[2]*x[3]*x[13], f);
+  f = fmaf(__ldg(cf + 36 * C), x[2]*x[4]*x[4], f);
+  f = fmaf(__ldg(cf + 37 * C), x[2]*x[5]*x[5], f);
+  f = fmaf(__ldg(cf + 38 * C), x[2]*x[6]*x[6], f);
+  f = fmaf(__ldg(cf + 39 * C), x[2]*x[7]*x[7], f);
+  f = fmaf(__ldg(cf + 40 * C), x[2]*x[8]*x[8], f);
+  f = fmaf(__ldg(cf + 41 * C), x[2]*x[9]*x[9], f);
+  f = fmaf(__ldg(cf + 42 * C), x[2]*x[10]*x[10], f);
+  f = fmaf(__ldg(cf + 43 * C), x[2]*x[11]*x[11], f);
+  f = fmaf(__ldg(cf + 44 * C), x[2]*x[12]*x[12], f);
+  f = fmaf(__ldg(cf + 45 * C), x[2]*x[13]*x[13], f);
+  f = fmaf(__ldg(cf + 46 * C), x[2]*x[14]*x[14], f);
+  f = fmaf(__ldg(cf + 47 * C), x[2]*x[15]*x[15], f);
+  f = fmaf(__ldg(cf + 48 * C), x[3]*x[3]*x[12], f);
+  f = fmaf(__ldg(cf + 49 * C), x[3]*x[3]*x[14], f);
+  f = fmaf(__ldg(cf + 50 * C), x[3]*x[4]*x[5], f);
+  f = fmaf(__ldg(cf + 51 * C), x[3]*x[6]*x[7], f);
+  f = fmaf(__ldg(cf + 52 * C), x[3]*x[7]*x[8], f);
+  f = fmaf(__ldg(cf + 53 * C), x[3]*x[9]*x[10], f);
+  f = fmaf(__ldg(cf + 54 * C), x[3]*x[10]*x[11], f);
+  f = fmaf(__ldg(cf + 55 * C), x[3]*x[12]*x[13], f);
+  f = fmaf(__ldg(cf + 56 * C), x[3]*x[13]*x[14], f);
+  f = fmaf(__ldg(cf + 57 * C), x[3]*x[14]*x[15], f);
+  f = fmaf(__ldg(cf + 58 * C), x[4]*x[4]*x[12], f);
+  f = fmaf(__ldg(cf + 59 * C), x[4]*x[5]*x[13], f);
+  f = fmaf(__ldg(cf + 60 * C), x[4]*x[5]*x[15], f);
+  f = fmaf(__ldg(cf + 61 * C), x[4]*x[6]*x[10], f);
+  f = fmaf(__ldg(cf + 62 * C), x[4]*x[7]*x[9], f);
+  f = fmaf(__ldg(cf + 63 * C), x[4]*x[7]*x[11], f);
+  f = fmaf(__ldg(cf + 64 * C), x[5]*x[5]*x[12], f);
+  f = fmaf(__ldg(cf + 65 * C), x[5]*x[5]*x[14], f);
+  f = fmaf(__ldg(cf + 66 * C), x[5]*x[6]*x[11], f);
+  f = fmaf(__ldg(cf + 67 * C), x[5]*x[7]*x[10], f);
+  f = fmaf(__ldg(cf + 68 * C), x[5]*x[8]*x[9], f);
+  f = fmaf(__ldg(cf + 69 * C), x[5]*x[8]*x[11], f);
+  f = fmaf(__ldg(cf + 70 * C), x[6]*x[6]*x[12], f);
+  f = fmaf(__ldg(cf + 71 * C), x[6]*x[7]*x[13], f);
+  f = fmaf(__ldg(cf + 72 * C), x[6]*x[8]*x[14], f);
+  f = fmaf(__ldg(cf + 73 * C), x[7]*x[7]*x[12], f);
+  f = fmaf(__ldg(cf + 74 * C), x[7]*x[7]*x[14], f);
+  f = fmaf(__ldg(cf + 75 * C), x[7]*x[8]*x[13], f);
+  f = fmaf(__ldg(cf + 76 * C), x[7]*x[8]*x[15], f);
+  f = fmaf(__ldg(cf + 77 * C), x[8]*x[8]*x[12], f);
+  f = fmaf(__ldg(cf + 78 * C), x[9]*x[9]*x[12], f);
+  f = fmaf(__ldg(cf + 79 * C), x[9]*x[10]*x[13], f);
+  f = fmaf(__ldg(cf + 80 * C), x[9]*x[11]*x[14], f);
+  f = fmaf(__ldg(cf + 81 * C), x[10]*x[10]*x[12], f);
+  f = fmaf(__ldg(cf + 82 * C), x[10]*x[11]*x[13], f);
+  f = fmaf(__ldg(cf + 83 * C), x[10]*x[11]*x[15], f);
+  f = fmaf(__ldg(cf + 84 * C), x[11]*x[11]*x[12], f);
+  f = fmaf(__ldg(cf + 85 * C), x[11]*x[11]*x[14], f);
+  f = fmaf(__ldg(cf + 86 * C), x[12]*x[12]*x[12], f);
+  f = fmaf(__ldg(cf + 87 * C), x[12]*x[13]*x[13], f);
+  f = fmaf(__ldg(cf + 88 * C), x[12]*x[14]*x[14], f);
+  f = fmaf(__ldg(cf + 89 * C), x[12]*x[15]*x[15], f);
+  f = fmaf(__ldg(cf + 90 * C), x[13]*x[13]*x[14], f);
+  f = fmaf(__ldg(cf + 91 * C), x[13]*x[14]*x[15], f);
+  return f;
 }
 
 __device__ __forceinline__ void grad_LM2(const float* x, float w, const float* __restrict__ cf, int C, float* g) {
@@ -1776,120 +1776,120 @@ __device__ __forceinline__ void grad_LM2(const float* x, float w, const float* _
 }
 
 __device__ __forceinline__ float value_LM3(const float* x, const float* __restrict__ cf, int C) {
-  float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f, f3 = 0.0f;
-  f0 = fmaf(__ldg(cf + 0 * C), x[3], f0);
-  f1 = fmaf(__ldg(cf + 1 * C), x[0]*x[3], f1);
-  f2 = fmaf(__ldg(cf + 2 * C), x[1]*x[4], f2);
-  f3 = fmaf(__ldg(cf + 3 * C), x[2]*x[7], f3);
-  f0 = fmaf(__ldg(cf + 4 * C), x[3]*x[6], f0);
-  f1 = fmaf(__ldg(cf + 5 * C), x[3]*x[8], f1);
-  f2 = fmaf(__ldg(cf + 6 * C), x[4]*x[9], f2);
-  f3 = fmaf(__ldg(cf + 7 * C), x[4]*x[11], f3);
-  f0 = fmaf(__ldg(cf + 8 * C), x[5]*x[10], f0);
-  f1 = fmaf(__ldg(cf + 9 * C), x[6]*x[13], f1);
-  f2 = fmaf(__ldg(cf + 10 * C), x[7]*x[12], f2);
-  f3 = fmaf(__ldg(cf + 11 * C), x[7]*x[14], f3);
-  f0 = fmaf(__ldg(cf + 12 * C), x[8]*x[13], f0);
-  f1 = fmaf(__ldg(cf + 13 * C), x[8]*x[15], f1);
-  f2 = fmaf(__ldg(cf + 14 * C), x[0]*x[0]*x[3], f2);
-  f3 = fmaf(__ldg(cf + 15 * C), x[0]*x[1]*x[4], f3);
-  f0 = fmaf(__ldg(cf + 16 * C), x[0]*x[2]*x[7], f0);
-  f1 = fmaf(__ldg(cf + 17 * C), x[0]*x[3]*x[6], f1);
-  f2 = fmaf(__ldg(cf + 18 * C), x[0]*x[3]*x[8], f2);
-  f3 = fmaf(__ldg(cf + 19 * C), x[0]*x[4]*x[9], f3);
-  f0 = fmaf(__ldg(cf + 20 * C), x[0]*x[4]*x[11], f0);
-  f1 = fmaf(__ldg(cf + 21 * C), x[0]*x[5]*x[10], f1);
-  f2 = fmaf(__ldg(cf + 22 * C), x[0]*x[6]*x[13], f2);
-  f3 = fmaf(__ldg(cf + 23 * C), x[0]*x[7]*x[12], f3);
-  f0 = fmaf(__ldg(cf + 24 * C), x[0]*x[7]*x[14], f0);
-  f1 = fmaf(__ldg(cf + 25 * C), x[0]*x[8]*x[13], f1);
-  f2 = fmaf(__ldg(cf + 26 * C), x[0]*x[8]*x[15], f2);
-  f3 = fmaf(__ldg(cf + 27 * C), x[1]*x[1]*x[3], f3);
-  f0 = fmaf(__ldg(cf + 28 * C), x[1]*x[1]*x[13], f0);
-  f1 = fmaf(__ldg(cf + 29 * C), x[1]*x[1]*x[15], f1);
-  f2 = fmaf(__ldg(cf + 30 * C), x[1]*x[2]*x[10], f2);
-  f3 = fmaf(__ldg(cf + 31 * C), x[1]*x[3]*x[9], f3);
-  f0 = fmaf(__ldg(cf + 32 * C), x[1]*x[3]*x[11], f0);
-  f1 = fmaf(__ldg(cf + 33 * C), x[1]*x[4]*x[6], f1);
-  f2 = fmaf(__ldg(cf + 34 * C), x[1]*x[5]*x[7], f2);
-  f3 = fmaf(__ldg(cf + 35 * C), x[1]*x[9]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 36 * C), x[1]*x[10]*x[12], f0);
-  f1 = fmaf(__ldg(cf + 37 * C), x[1]*x[11]*x[13], f1);
-  f2 = fmaf(__ldg(cf + 38 * C), x[1]*x[11]*x[15], f2);
-  f3 = fmaf(__ldg(cf + 39 * C), x[2]*x[2]*x[3], f3);
-  f0 = fmaf(__ldg(cf + 40 * C), x[2]*x[2]*x[13], f0);
-  f1 = fmaf(__ldg(cf + 41 * C), x[2]*x[3]*x[12], f1);
-  f2 = fmaf(__ldg(cf + 42 * C), x[2]*x[3]*x[14], f2);
-  f3 = fmaf(__ldg(cf + 43 * C), x[2]*x[4]*x[5], f3);
-  f0 = fmaf(__ldg(cf + 44 * C), x[2]*x[6]*x[7], f0);
-  f1 = fmaf(__ldg(cf + 45 * C), x[2]*x[7]*x[8], f1);
-  f2 = fmaf(__ldg(cf + 46 * C), x[2]*x[9]*x[10], f2);
-  f3 = fmaf(__ldg(cf + 47 * C), x[2]*x[10]*x[11], f3);
-  f0 = fmaf(__ldg(cf + 48 * C), x[2]*x[12]*x[13], f0);
-  f1 = fmaf(__ldg(cf + 49 * C), x[2]*x[13]*x[14], f1);
-  f2 = fmaf(__ldg(cf + 50 * C), x[2]*x[14]*x[15], f2);
-  f3 = fmaf(__ldg(cf + 51 * C), x[3]*x[3]*x[3], f3);
-  f0 = fmaf(__ldg(cf + 52 * C), x[3]*x[3]*x[13], f0);
-  f1 = fmaf(__ldg(cf + 53 * C), x[3]*x[3]*x[15], f1);
-  f2 = fmaf(__ldg(cf + 54 * C), x[3]*x[4]*x[4], f2);
-  f3 = fmaf(__ldg(cf + 55 * C), x[3]*x[5]*x[5], f3);
-  f0 = fmaf(__ldg(cf + 56 * C), x[3]*x[6]*x[6], f0);
-  f1 = fmaf(__ldg(cf + 57 * C), x[3]*x[6]*x[8], f1);
-  f2 = fmaf(__ldg(cf + 58 * C), x[3]*x[7]*x[7], f2);
-  f3 = fmaf(__ldg(cf + 59 * C), x[3]*x[8]*x[8], f3);
-  f0 = fmaf(__ldg(cf + 60 * C), x[3]*x[9]*x[9], f0);
-  f1 = fmaf(__ldg(cf + 61 * C), x[3]*x[9]*x[11], f1);
-  f2 = fmaf(__ldg(cf + 62 * C), x[3]*x[10]*x[10], f2);
-  f3 = fmaf(__ldg(cf + 63 * C), x[3]*x[11]*x[11], f3);
-  f0 = fmaf(__ldg(cf + 64 * C), x[3]*x[12]*x[12], f0);
-  f1 = fmaf(__ldg(cf + 65 * C), x[3]*x[12]*x[14], f1);
-  f2 = fmaf(__ldg(cf + 66 * C), x[3]*x[13]*x[13], f2);
-  f3 = fmaf(__ldg(cf + 67 * C), x[3]*x[13]*x[15], f3);
-  f0 = fmaf(__ldg(cf + 68 * C), x[3]*x[14]*x[14], f0);
-  f1 = fmaf(__ldg(cf + 69 * C), x[3]*x[15]*x[15], f1);
-  f2 = fmaf(__ldg(cf + 70 * C), x[4]*x[4]*x[13], f2);
-  f3 = fmaf(__ldg(cf + 71 * C), x[4]*x[4]*x[15], f3);
-  f0 = fmaf(__ldg(cf + 72 * C), x[4]*x[5]*x[12], f0);
-  f1 = fmaf(__ldg(cf + 73 * C), x[4]*x[5]*x[14], f1);
-  f2 = fmaf(__ldg(cf + 74 * C), x[4]*x[6]*x[9], f2);
-  f3 = fmaf(__ldg(cf + 75 * C), x[4]*x[6]*x[11], f3);
-  f0 = fmaf(__ldg(cf + 76 * C), x[4]*x[7]*x[10], f0);
-  f1 = fmaf(__ldg(cf + 77 * C), x[4]*x[8]*x[9], f1);
-  f2 = fmaf(__ldg(cf + 78 * C), x[5]*x[5]*x[13], f2);
-  f3 = fmaf(__ldg(cf + 79 * C), x[5]*x[5]*x[15], f3);
-  f0 = fmaf(__ldg(cf + 80 * C), x[5]*x[6]*x[10], f0);
-  f1 = fmaf(__ldg(cf + 81 * C), x[5]*x[7]*x[9], f1);
-  f2 = fmaf(__ldg(cf + 82 * C), x[5]*x[7]*x[11], f2);
-  f3 = fmaf(__ldg(cf + 83 * C), x[5]*x[8]*x[10], f3);
-  f0 = fmaf(__ldg(cf + 84 * C), x[6]*x[6]*x[13], f0);
-  f1 = fmaf(__ldg(cf + 85 * C), x[6]*x[7]*x[12], f1);
-  f2 = fmaf(__ldg(cf + 86 * C), x[6]*x[7]*x[14], f2);
-  f3 = fmaf(__ldg(cf + 87 * C), x[6]*x[8]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 88 * C), x[6]*x[8]*x[15], f0);
-  f1 = fmaf(__ldg(cf + 89 * C), x[7]*x[7]*x[13], f1);
-  f2 = fmaf(__ldg(cf + 90 * C), x[7]*x[7]*x[15], f2);
-  f3 = fmaf(__ldg(cf + 91 * C), x[7]*x[8]*x[12], f3);
-  f0 = fmaf(__ldg(cf + 92 * C), x[7]*x[8]*x[14], f0);
-  f1 = fmaf(__ldg(cf + 93 * C), x[8]*x[8]*x[13], f1);
-  f2 = fmaf(__ldg(cf + 94 * C), x[8]*x[8]*x[15], f2);
-  f3 = fmaf(__ldg(cf + 95 * C), x[9]*x[9]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 96 * C), x[9]*x[10]*x[12], f0);
-  f1 = fmaf(__ldg(cf + 97 * C), x[9]*x[10]*x[14], f1);
-  f2 = fmaf(__ldg(cf + 98 * C), x[9]*x[11]*x[13], f2);
-  f3 = fmaf(__ldg(cf + 99 * C), x[10]*x[10]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 100 * C), x[10]*x[10]*x[15], f0);
-  f1 = fmaf(__ldg(cf + 101 * C), x[10]*x[11]*x[12], f1);
-  f2 = fmaf(__ldg(cf + 102 * C), x[11]*x[11]*x[13], f2);
-  f3 = fmaf(__ldg(cf + 103 * C), x[11]*x[11]*x[15], f3);
-  f0 = fmaf(__ldg(cf + 104 * C), x[12]*x[12]*x[13], f0);
-  f1 = fmaf(__ldg(cf + 105 * C), x[12]*x[13]*x[14], f1);
-  f2 = fmaf(__ldg(cf + 106 * C), x[12]*x[14]*x[15], f2);
-  f3 = fmaf(__ldg(cf + 107 * C), x[13]*x[13]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 108 * C), x[13]*x[13]*x[15], f0);
-  f1 = fmaf(__ldg(cf + 109 * C), x[13]*x[14]*x[14], f1);
-  f2 = fmaf(__ldg(cf + 110 * C), x[13]*x[15]*x[15], f2);
-  f3 = fmaf(__ldg(cf + 111 * C), x[14]*x[14]*x[15], f3);
-  return (f0 + f1) + (f2 + f3);
+  float f = 0.0f;
+  f = fmaf(__ldg(cf + 0 * C), x[3], f);
+  f = fmaf(__ldg(cf + 1 * C), x[0]*x[3], f);
+  f = fmaf(__ldg(cf + 2 * C), x[1]*x[4], f);
+  f = fmaf(__ldg(cf + 3 * C), x[2]*x[7], f);
+  f = fmaf(__ldg(cf + 4 * C), x[3]*x[6], f);
+  f = fmaf(__ldg(cf + 5 * C), x[3]*x[8], f);
+  f = fmaf(__ldg(cf + 6 * C), x[4]*x[9], f);
+  f = fmaf(__ldg(cf + 7 * C), x[4]*x[11], f);
+  f = fmaf(__ldg(cf + 8 * C), x[5]*x[10], f);
+  f = fmaf(__ldg(cf + 9 * C), x[6]*x[13], f);
+  f = fmaf(__ldg(cf + 10 * C), x[7]*x[12], f);
+  f = fmaf(__ldg(cf + 11 * C), x[7]*x[14], f);
+  f = fmaf(__ldg(cf + 12 * C), x[8]*x[13], f);
+  f = fmaf(__ldg(cf + 13 * C), x[8]*x[15], f);
+  f = fmaf(__ldg(cf + 14 * C), x[0]*x[0]*x[3], f);
+  f = fmaf(__ldg(cf + 15 * C), x[0]*x[1]*x[4], f);
+  f = fmaf(__ldg(cf + 16 * C), x[0]*x[2]*x[7], f);
+  f = fmaf(__ldg(cf + 17 * C), x[0]*x[3]*x[6], f);
+  f = fmaf(__ldg(cf + 18 * C), x[0]*x[3]*x[8], f);
+  f = fmaf(__ldg(cf + 19 * C), x[0]*x[4]*x[9], f);
+  f = fmaf(__ldg(cf + 20 * C), x[0]*x[4]*x[11], f);
+  f = fmaf(__ldg(cf + 21 * C), x[0]*x[5]*x[10], f);
+  f = fmaf(__ldg(cf + 22 * C), x[0]*x[6]*x[13], f);
+  f = fmaf(__ldg(cf + 23 * C), x[0]*x[7]*x[12], f);
+  f = fmaf(__ldg(cf + 24 * C), x[0]*x[7]*x[14], f);
+  f = fmaf(__ldg(cf + 25 * C), x[0]*x[8]*x[13], f);
+  f = fmaf(__ldg(cf + 26 * C), x[0]*x[8]*x[15], f);
+  f = fmaf(__ldg(cf + 27 * C), x[1]*x[1]*x[3], f);
+  f = fmaf(__ldg(cf + 28 * C), x[1]*x[1]*x[13], f);
+  f = fmaf(__ldg(cf + 29 * C), x[1]*x[1]*x[15], f);
+  f = fmaf(__ldg(cf + 30 * C), x[1]*x[2]*x[10], f);
+  f = fmaf(__ldg(cf + 31 * C), x[1]*x[3]*x[9], f);
+  f = fmaf(__ldg(cf + 32 * C), x[1]*x[3]*x[11], f);
+  f = fmaf(__ldg(cf + 33 * C), x[1]*x[4]*x[6], f);
+  f = fmaf(__ldg(cf + 34 * C), x[1]*x[5]*x[7], f);
+  f = fmaf(__ldg(cf + 35 * C), x[1]*x[9]*x[13], f);
+  f = fmaf(__ldg(cf + 36 * C), x[1]*x[10]*x[12], f);
+  f = fmaf(__ldg(cf + 37 * C), x[1]*x[11]*x[13], f);
+  f = fmaf(__ldg(cf + 38 * C), x[1]*x[11]*x[15], f);
+  f = fmaf(__ldg(cf + 39 * C), x[2]*x[2]*x[3], f);
+  f = fmaf(__ldg(cf + 40 * C), x[2]*x[2]*x[13], f);
+  f = fmaf(__ldg(cf + 41 * C), x[2]*x[3]*x[12], f);
+  f = fmaf(__ldg(cf + 42 * C), x[2]*x[3]*x[14], f);
+  f = fmaf(__ldg(cf + 43 * C), x[2]*x[4]*x[5], f);
+  f = fmaf(__ldg(cf + 44 * C), x[2]*x[6]*x[7], f);
+  f = fmaf(__ldg(cf + 45 * C), x[2]*x[7]*x[8], f);
+  f = fmaf(__ldg(cf + 46 * C), x[2]*x[9]*x[10], f);
+  f = fmaf(__ldg(cf + 47 * C), x[2]*x[10]*x[11], f);
+  f = fmaf(__ldg(cf + 48 * C), x[2]*x[12]*x[13], f);
+  f = fmaf(__ldg(cf + 49 * C), x[2]*x[13]*x[14], f);
+  f = fmaf(__ldg(cf + 50 * C), x[2]*x[14]*x[15], f);
+  f = fmaf(__ldg(cf + 51 * C), x[3]*x[3]*x[3], f);
+  f = fmaf(__ldg(cf + 52 * C), x[3]*x[3]*x[13], f);
+  f = fmaf(__ldg(cf + 53 * C), x[3]*x[3]*x[15], f);
+  f = fmaf(__ldg(cf + 54 * C), x[3]*x[4]*x[4], f);
+  f = fmaf(__ldg(cf + 55 * C), x[3]*x[5]*x[5], f);
+  f = fmaf(__ldg(cf + 56 * C), x[3]*x[6]*x[6], f);
+  f = fmaf(__ldg(cf + 57 * C), x[3]*x[6]*x[8], f);
+  f = fmaf(__ldg(cf + 58 * C), x[3]*x[7]*x[7], f);
+  f = fmaf(__ldg(cf + 59 * C), x[3]*x[8]*x[8], f);
+  f = fmaf(__ldg(cf + 60 * C), x[3]*x[9]*x[9], f);
+  f = fmaf(__ldg(cf + 61 * C), x[3]*x[9]*x[11], f);
+  f = fmaf(__ldg(cf + 62 * C), x[3]*x[10]*x[10], f);
+  f = fmaf(__ldg(cf + 63 * C), x[3]*x[11]*x[11], f);
+  f = fmaf(__ldg(cf + 64 * C), x[3]*x[12]*x[12], f);
+  f = fmaf(__ldg(cf + 65 * C), x[3]*x[12]*x[14], f);
+  f = fmaf(__ldg(cf + 66 * C), x[3]*x[13]*x[13], f);
+  f = fmaf(__ldg(cf + 67 * C), x[3]*x[13]*x[15], f);
+  f = fmaf(__ldg(cf + 68 * C), x[3]*x[14]*x[14], f);
+  f = fmaf(__ldg(cf + 69 * C), x[3]*x[15]*x[15], f);
+  f = fmaf(__ldg(cf + 70 * C), x[4]*x[4]*x[13], f);
+  f = fmaf(__ldg(cf + 71 * C), x[4]*x[4]*x[15], f);
+  f = fmaf(__ldg(cf + 72 * C), x[4]*x[5]*x[12], f);
+  f = fmaf(__ldg(cf + 73 * C), x[4]*x[5]*x[14], f);
+  f = fmaf(__ldg(cf + 74 * C), x[4]*x[6]*x[9], f);
+  f = fmaf(__ldg(cf + 75 * C), x[4]*x[6]*x[11], f);
+  f = fmaf(__ldg(cf + 76 * C), x[4]*x[7]*x[10], f);
+  f = fmaf(__ldg(cf + 77 * C), x[4]*x[8]*x[9], f);
+  f = fmaf(__ldg(cf + 78 * C), x[5]*x[5]*x[13], f);
+  f = fmaf(__ldg(cf + 79 * C), x[5]*x[5]*x[15], f);
+  f = fmaf(__ldg(cf + 80 * C), x[5]*x[6]*x[10], f);
+  f = fmaf(__ldg(cf + 81 * C), x[5]*x[7]*x[9], f);
+  f = fmaf(__ldg(cf + 82 * C), x[5]*x[7]*x[11], f);
+  f = fmaf(__ldg(cf + 83 * C), x[5]*x[8]*x[10], f);
+  f = fmaf(__ldg(cf + 84 * C), x[6]*x[6]*x[13], f);
+  f = fmaf(__ldg(cf + 85 * C), x[6]*x[7]*x[12], f);
+  f = fmaf(__ldg(cf + 86 * C), x[6]*x[7]*x[14], f);
+  f = fmaf(__ldg(cf + 87 * C), x[6]*x[8]*x[13], f);
+  f = fmaf(__ldg(cf + 88 * C), x[6]*x[8]*x[15], f);
+  f = fmaf(__ldg(cf + 89 * C), x[7]*x[7]*x[13], f);
+  f = fmaf(__ldg(cf + 90 * C), x[7]*x[7]*x[15], f);
+  f = fmaf(__ldg(cf + 91 * C), x[7]*x[8]*x[12], f);
+  f = fmaf(__ldg(cf + 92 * C), x[7]*x[8]*x[14], f);
+  f = fmaf(__ldg(cf + 93 * C), x[8]*x[8]*x[13], f);
+  f = fmaf(__ldg(cf + 94 * C), x[8]*x[8]*x[15], f);
+  f = fmaf(__ldg(cf + 95 * C), x[9]*x[9]*x[13], f);
+  f = fmaf(__ldg(cf + 96 * C), x[9]*x[10]*x[12], f);
+  f = fmaf(__ldg(cf + 97 * C), x[9]*x[10]*x[14], f);
+  f = fmaf(__ldg(cf + 98 * C), x[9]*x[11]*x[13], f);
+  f = fmaf(__ldg(cf + 99 * C), x[10]*x[10]*x[13], f);
+  f = fmaf(__ldg(cf + 100 * C), x[10]*x[10]*x[15], f);
+  f = fmaf(__ldg(cf + 101 * C), x[10]*x[11]*x[12], f);
+  f = fmaf(__ldg(cf + 102 * C), x[11]*x[11]*x[13], f);
+  f = fmaf(__ldg(cf + 103 * C), x[11]*x[11]*x[15], f);
+  f = fmaf(__ldg(cf + 104 * C), x[12]*x[12]*x[13], f);
+  f = fmaf(__ldg(cf + 105 * C), x[12]*x[13]*x[14], f);
+  f = fmaf(__ldg(cf + 106 * C), x[12]*x[14]*x[15], f);
+  f = fmaf(__ldg(cf + 107 * C), x[13]*x[13]*x[13], f);
+  f = fmaf(__ldg(cf + 108 * C), x[13]*x[13]*x[15], f);
+  f = fmaf(__ldg(cf + 109 * C), x[13]*x[14]*x[14], f);
+  f = fmaf(__ldg(cf + 110 * C), x[13]*x[15]*x[15], f);
+  f = fmaf(__ldg(cf + 111 * C), x[14]*x[14]*x[15], f);
+  return f;
 }
 
 __device__ __forceinline__ void grad_LM3(const float* x, float w, const float* __restrict__ cf, int C, float* g) {
@@ -2441,98 +2441,98 @@ __device__ __forceinline__ void grad_LM3(const float* x, float w, const float* _
 }
 
 __device__ __forceinline__ float value_LM4(const float* x, const float* __restrict__ cf, int C) {
-  float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f, f3 = 0.0f;
-  f0 = fmaf(__ldg(cf + 0 * C), x[4], f0);
-  f1 = fmaf(__ldg(cf + 1 * C), x[0]*x[4], f1);
-  f2 = fmaf(__ldg(cf + 2 * C), x[1]*x[3], f2);
-  f3 = fmaf(__ldg(cf + 3 * C), x[1]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 4 * C), x[1]*x[15], f0);
-  f1 = fmaf(__ldg(cf + 5 * C), x[2]*x[10], f1);
-  f2 = fmaf(__ldg(cf + 6 * C), x[3]*x[9], f2);
-  f3 = fmaf(__ldg(cf + 7 * C), x[3]*x[11], f3);
-  f0 = fmaf(__ldg(cf + 8 * C), x[4]*x[6], f0);
-  f1 = fmaf(__ldg(cf + 9 * C), x[5]*x[7], f1);
-  f2 = fmaf(__ldg(cf + 10 * C), x[9]*x[13], f2);
-  f3 = fmaf(__ldg(cf + 11 * C), x[10]*x[12], f3);
-  f0 = fmaf(__ldg(cf + 12 * C), x[11]*x[13], f0);
-  f1 = fmaf(__ldg(cf + 13 * C), x[11]*x[15], f1);
-  f2 = fmaf(__ldg(cf + 14 * C), x[0]*x[0]*x[4], f2);
-  f3 = fmaf(__ldg(cf + 15 * C), x[0]*x[1]*x[3], f3);
-  f0 = fmaf(__ldg(cf + 16 * C), x[0]*x[1]*x[13], f0);
-  f1 = fmaf(__ldg(cf + 17 * C), x[0]*x[1]*x[15], f1);
-  f2 = fmaf(__ldg(cf + 18 * C), x[0]*x[2]*x[10], f2);
-  f3 = fmaf(__ldg(cf + 19 * C), x[0]*x[3]*x[9], f3);
-  f0 = fmaf(__ldg(cf + 20 * C), x[0]*x[3]*x[11], f0);
-  f1 = fmaf(__ldg(cf + 21 * C), x[0]*x[4]*x[6], f1);
-  f2 = fmaf(__ldg(cf + 22 * C), x[0]*x[5]*x[7], f2);
-  f3 = fmaf(__ldg(cf + 23 * C), x[0]*x[9]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 24 * C), x[0]*x[10]*x[12], f0);
-  f1 = fmaf(__ldg(cf + 25 * C), x[0]*x[11]*x[13], f1);
-  f2 = fmaf(__ldg(cf + 26 * C), x[0]*x[11]*x[15], f2);
-  f3 = fmaf(__ldg(cf + 27 * C), x[1]*x[1]*x[4], f3);
-  f0 = fmaf(__ldg(cf + 28 * C), x[1]*x[2]*x[7], f0);
-  f1 = fmaf(__ldg(cf + 29 * C), x[1]*x[3]*x[6], f1);
-  f2 = fmaf(__ldg(cf + 30 * C), x[1]*x[4]*x[9], f2);
-  f3 = fmaf(__ldg(cf + 31 * C), x[1]*x[4]*x[11], f3);
-  f0 = fmaf(__ldg(cf + 32 * C), x[1]*x[5]*x[10], f0);
-  f1 = fmaf(__ldg(cf + 33 * C), x[1]*x[6]*x[13], f1);
-  f2 = fmaf(__ldg(cf + 34 * C), x[1]*x[6]*x[15], f2);
-  f3 = fmaf(__ldg(cf + 35 * C), x[1]*x[7]*x[12], f3);
-  f0 = fmaf(__ldg(cf + 36 * C), x[1]*x[7]*x[14], f0);
-  f1 = fmaf(__ldg(cf + 37 * C), x[1]*x[8]*x[13], f1);
-  f2 = fmaf(__ldg(cf + 38 * C), x[1]*x[8]*x[15], f2);
-  f3 = fmaf(__ldg(cf + 39 * C), x[2]*x[2]*x[4], f3);
-  f0 = fmaf(__ldg(cf + 40 * C), x[2]*x[3]*x[5], f0);
-  f1 = fmaf(__ldg(cf + 41 * C), x[2]*x[4]*x[12], f1);
-  f2 = fmaf(__ldg(cf + 42 * C), x[2]*x[5]*x[13], f2);
-  f3 = fmaf(__ldg(cf + 43 * C), x[2]*x[5]*x[15], f3);
-  f0 = fmaf(__ldg(cf + 44 * C), x[2]*x[6]*x[10], f0);
-  f1 = fmaf(__ldg(cf + 45 * C), x[2]*x[7]*x[9], f1);
-  f2 = fmaf(__ldg(cf + 46 * C), x[2]*x[7]*x[11], f2);
-  f3 = fmaf(__ldg(cf + 47 * C), x[3]*x[3]*x[4], f3);
-  f0 = fmaf(__ldg(cf + 48 * C), x[3]*x[4]*x[13], f0);
-  f1 = fmaf(__ldg(cf + 49 * C), x[3]*x[4]*x[15], f1);
-  f2 = fmaf(__ldg(cf + 50 * C), x[3]*x[5]*x[12], f2);
-  f3 = fmaf(__ldg(cf + 51 * C), x[3]*x[5]*x[14], f3);
-  f0 = fmaf(__ldg(cf + 52 * C), x[3]*x[6]*x[9], f0);
-  f1 = fmaf(__ldg(cf + 53 * C), x[3]*x[6]*x[11], f1);
-  f2 = fmaf(__ldg(cf + 54 * C), x[3]*x[7]*x[10], f2);
-  f3 = fmaf(__ldg(cf + 55 * C), x[3]*x[8]*x[9], f3);
-  f0 = fmaf(__ldg(cf + 56 * C), x[3]*x[8]*x[11], f0);
-  f1 = fmaf(__ldg(cf + 57 * C), x[4]*x[4]*x[4], f1);
-  f2 = fmaf(__ldg(cf + 58 * C), x[4]*x[5]*x[5], f2);
-  f3 = fmaf(__ldg(cf + 59 * C), x[4]*x[6]*x[6], f3);
-  f0 = fmaf(__ldg(cf + 60 * C), x[4]*x[7]*x[7], f0);
-  f1 = fmaf(__ldg(cf + 61 * C), x[4]*x[8]*x[8], f1);
-  f2 = fmaf(__ldg(cf + 62 * C), x[4]*x[9]*x[9], f2);
-  f3 = fmaf(__ldg(cf + 63 * C), x[4]*x[9]*x[11], f3);
-  f0 = fmaf(__ldg(cf + 64 * C), x[4]*x[10]*x[10], f0);
-  f1 = fmaf(__ldg(cf + 65 * C), x[4]*x[11]*x[11], f1);
-  f2 = fmaf(__ldg(cf + 66 * C), x[4]*x[12]*x[12], f2);
-  f3 = fmaf(__ldg(cf + 67 * C), x[4]*x[13]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 68 * C), x[4]*x[13]*x[15], f0);
-  f1 = fmaf(__ldg(cf + 69 * C), x[4]*x[14]*x[14], f1);
-  f2 = fmaf(__ldg(cf + 70 * C), x[4]*x[15]*x[15], f2);
-  f3 = fmaf(__ldg(cf + 71 * C), x[5]*x[9]*x[10], f3);
-  f0 = fmaf(__ldg(cf + 72 * C), x[5]*x[10]*x[11], f0);
-  f1 = fmaf(__ldg(cf + 73 * C), x[5]*x[12]*x[13], f1);
-  f2 = fmaf(__ldg(cf + 74 * C), x[5]*x[12]*x[15], f2);
-  f3 = fmaf(__ldg(cf + 75 * C), x[5]*x[13]*x[14], f3);
-  f0 = fmaf(__ldg(cf + 76 * C), x[5]*x[14]*x[15], f0);
-  f1 = fmaf(__ldg(cf + 77 * C), x[6]*x[9]*x[13], f1);
-  f2 = fmaf(__ldg(cf + 78 * C), x[6]*x[10]*x[12], f2);
-  f3 = fmaf(__ldg(cf + 79 * C), x[6]*x[11]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 80 * C), x[6]*x[11]*x[15], f0);
-  f1 = fmaf(__ldg(cf + 81 * C), x[7]*x[9]*x[12], f1);
-  f2 = fmaf(__ldg(cf + 82 * C), x[7]*x[9]*x[14], f2);
-  f3 = fmaf(__ldg(cf + 83 * C), x[7]*x[10]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 84 * C), x[7]*x[10]*x[15], f0);
-  f1 = fmaf(__ldg(cf + 85 * C), x[7]*x[11]*x[12], f1);
-  f2 = fmaf(__ldg(cf + 86 * C), x[7]*x[11]*x[14], f2);
-  f3 = fmaf(__ldg(cf + 87 * C), x[8]*x[9]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 88 * C), x[8]*x[10]*x[14], f0);
-  f1 = fmaf(__ldg(cf + 89 * C), x[8]*x[11]*x[15], f1);
-  return (f0 + f1) + (f2 + f3);
+  float f = 0.0f;
+  f = fmaf(__ldg(cf + 0 * C), x[4], f);
+  f = fmaf(__ldg(cf + 1 * C), x[0]*x[4], f);
+  f = fmaf(__ldg(cf + 2 * C), x[1]*x[3], f);
+  f = fmaf(__ldg(cf + 3 * C), x[1]*x[13], f);
+  f = fmaf(__ldg(cf + 4 * C), x[1]*x[15], f);
+  f = fmaf(__ldg(cf + 5 * C), x[2]*x[10], f);
+  f = fmaf(__ldg(cf + 6 * C), x[3]*x[9], f);
+  f = fmaf(__ldg(cf + 7 * C), x[3]*x[11], f);
+  f = fmaf(__ldg(cf + 8 * C), x[4]*x[6], f);
+  f = fmaf(__ldg(cf + 9 * C), x[5]*x[7], f);
+  f = fmaf(__ldg(cf + 10 * C), x[9]*x[13], f);
+  f = fmaf(__ldg(cf + 11 * C), x[10]*x[12], f);
+  f = fmaf(__ldg(cf + 12 * C), x[11]*x[13], f);
+  f = fmaf(__ldg(cf + 13 * C), x[11]*x[15], f);
+  f = fmaf(__ldg(cf + 14 * C), x[0]*x[0]*x[4], f);
+  f = fmaf(__ldg(cf + 15 * C), x[0]*x[1]*x[3], f);
+  f = fmaf(__ldg(cf + 16 * C), x[0]*x[1]*x[13], f);
+  f = fmaf(__ldg(cf + 17 * C), x[0]*x[1]*x[15], f);
+  f = fmaf(__ldg(cf + 18 * C), x[0]*x[2]*x[10], f);
+  f = fmaf(__ldg(cf + 19 * C), x[0]*x[3]*x[9], f);
+  f = fmaf(__ldg(cf + 20 * C), x[0]*x[3]*x[11], f);
+  f = fmaf(__ldg(cf + 21 * C), x[0]*x[4]*x[6], f);
+  f = fmaf(__ldg(cf + 22 * C), x[0]*x[5]*x[7], f);
+  f = fmaf(__ldg(cf + 23 * C), x[0]*x[9]*x[13], f);
+  f = fmaf(__ldg(cf + 24 * C), x[0]*x[10]*x[12], f);
+  f = fmaf(__ldg(cf + 25 * C), x[0]*x[11]*x[13], f);
+  f = fmaf(__ldg(cf + 26 * C), x[0]*x[11]*x[15], f);
+  f = fmaf(__ldg(cf + 27 * C), x[1]*x[1]*x[4], f);
+  f = fmaf(__ldg(cf + 28 * C), x[1]*x[2]*x[7], f);
+  f = fmaf(__ldg(cf + 29 * C), x[1]*x[3]*x[6], f);
+  f = fmaf(__ldg(cf + 30 * C), x[1]*x[4]*x[9], f);
+  f = fmaf(__ldg(cf + 31 * C), x[1]*x[4]*x[11], f);
+  f = fmaf(__ldg(cf + 32 * C), x[1]*x[5]*x[10], f);
+  f = fmaf(__ldg(cf + 33 * C), x[1]*x[6]*x[13], f);
+  f = fmaf(__ldg(cf + 34 * C), x[1]*x[6]*x[15], f);
+  f = fmaf(__ldg(cf + 35 * C), x[1]*x[7]*x[12], f);
+  f = fmaf(__ldg(cf + 36 * C), x[1]*x[7]*x[14], f);
+  f = fmaf(__ldg(cf + 37 * C), x[1]*x[8]*x[13], f);
+  f = fmaf(__ldg(cf + 38 * C), x[1]*x[8]*x[15], f);
+  f = fmaf(__ldg(cf + 39 * C), x[2]*x[2]*x[4], f);
+  f = fmaf(__ldg(cf + 40 * C), x[2]*x[3]*x[5], f);
+  f = fmaf(__ldg(cf + 41 * C), x[2]*x[4]*x[12], f);
+  f = fmaf(__ldg(cf + 42 * C), x[2]*x[5]*x[13], f);
+  f = fmaf(__ldg(cf + 43 * C), x[2]*x[5]*x[15], f);
+  f = fmaf(__ldg(cf + 44 * C), x[2]*x[6]*x[10], f);
+  f = fmaf(__ldg(cf + 45 * C), x[2]*x[7]*x[9], f);
+  f = fmaf(__ldg(cf + 46 * C), x[2]*x[7]*x[11], f);
+  f = fmaf(__ldg(cf + 47 * C), x[3]*x[3]*x[4], f);
+  f = fmaf(__ldg(cf + 48 * C), x[3]*x[4]*x[13], f);
+  f = fmaf(__ldg(cf + 49 * C), x[3]*x[4]*x[15], f);
+  f = fmaf(__ldg(cf + 50 * C), x[3]*x[5]*x[12], f);
+  f = fmaf(__ldg(cf + 51 * C), x[3]*x[5]*x[14], f);
+  f = fmaf(__ldg(cf + 52 * C), x[3]*x[6]*x[9], f);
+  f = fmaf(__ldg(cf + 53 * C), x[3]*x[6]*x[11], f);
+  f = fmaf(__ldg(cf + 54 * C), x[3]*x[7]*x[10], f);
+  f = fmaf(__ldg(cf + 55 * C), x[3]*x[8]*x[9], f);
+  f = fmaf(__ldg(cf + 56 * C), x[3]*x[8]*x[11], f);
+  f = fmaf(__ldg(cf + 57 * C), x[4]*x[4]*x[4], f);
+  f = fmaf(__ldg(cf + 58 * C), x[4]*x[5]*x[5], f);
+  f = fmaf(__ldg(cf + 59 * C), x[4]*x[6]*x[6], f);
+  f = fmaf(__ldg(cf + 60 * C), x[4]*x[7]*x[7], f);
+  f = fmaf(__ldg(cf + 61 * C), x[4]*x[8]*x[8], f);
+  f = fmaf(__ldg(cf + 62 * C), x[4]*x[9]*x[9], f);
+  f = fmaf(__ldg(cf + 63 * C), x[4]*x[9]*x[11], f);
+  f = fmaf(__ldg(cf + 64 * C), x[4]*x[10]*x[10], f);
+  f = fmaf(__ldg(cf + 65 * C), x[4]*x[11]*x[11], f);
+  f = fmaf(__ldg(cf + 66 * C), x[4]*x[12]*x[12], f);
+  f = fmaf(__ldg(cf + 67 * C), x[4]*x[13]*x[13], f);
+  f = fmaf(__ldg(cf + 68 * C), x[4]*x[13]*x[15], f);
+  f = fmaf(__ldg(cf + 69 * C), x[4]*x[14]*x[14], f);
+  f = fmaf(__ldg(cf + 70 * C), x[4]*x[15]*x[15], f);
+  f = fmaf(__ldg(cf + 71 * C), x[5]*x[9]*x[10], f);
+  f = fmaf(__ldg(cf + 72 * C), x[5]*x[10]*x[11], f);
+  f = fmaf(__ldg(cf + 73 * C), x[5]*x[12]*x[13], f);
+  f = fmaf(__ldg(cf + 74 * C), x[5]*x[12]*x[15], f);
+  f = fmaf(__ldg(cf + 75 * C), x[5]*x[13]*x[14], f);
+  f = fmaf(__ldg(cf + 76 * C), x[5]*x[14]*x[15], f);
+  f = fmaf(__ldg(cf + 77 * C), x[6]*x[9]*x[13], f);
+  f = fmaf(__ldg(cf + 78 * C), x[6]*x[10]*x[12], f);
+  f = fmaf(__ldg(cf + 79 * C), x[6]*x[11]*x[13], f);
+  f = fmaf(__ldg(cf + 80 * C), x[6]*x[11]*x[15], f);
+  f = fmaf(__ldg(cf + 81 * C), x[7]*x[9]*x[12], f);
+  f = fmaf(__ldg(cf + 82 * C), x[7]*x[9]*x[14], f);
+  f = fmaf(__ldg(cf + 83 * C), x[7]*x[10]*x[13], f);
+  f = fmaf(__ldg(cf + 84 * C), x[7]*x[10]*x[15], f);
+  f = fmaf(__ldg(cf + 85 * C), x[7]*x[11]*x[12], f);
+  f = fmaf(__ldg(cf + 86 * C), x[7]*x[11]*x[14], f);
+  f = fmaf(__ldg(cf + 87 * C), x[8]*x[9]*x[13], f);
+  f = fmaf(__ldg(cf + 88 * C), x[8]*x[10]*x[14], f);
+  f = fmaf(__ldg(cf + 89 * C), x[8]*x[11]*x[15], f);
+  return f;
 }
 
 __device__ __forceinline__ void grad_LM4(const float* x, float w, const float* __restrict__ cf, int C, float* g) {
@@ -2974,105 +2974,105 @@ __device__ __forceinline__ void grad_LM4(const float* x, float w, const float* _
 }
 
 __device__ __forceinline__ float value_LM5(const float* x, const float* __restrict__ cf, int C) {
-  float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f, f3 = 0.0f;
-  f0 = fmaf(__ldg(cf + 0 * C), x[5], f0);
-  f1 = fmaf(__ldg(cf + 1 * C), x[0]*x[5], f1);
-  f2 = fmaf(__ldg(cf + 2 * C), x[1]*x[2], f2);
-  f3 = fmaf(__ldg(cf + 3 * C), x[1]*x[12], f3);
-  f0 = fmaf(__ldg(cf + 4 * C), x[1]*x[14], f0);
-  f1 = fmaf(__ldg(cf + 5 * C), x[2]*x[11], f1);
-  f2 = fmaf(__ldg(cf + 6 * C), x[3]*x[10], f2);
-  f3 = fmaf(__ldg(cf + 7 * C), x[4]*x[7], f3);
-  f0 = fmaf(__ldg(cf + 8 * C), x[5]*x[6], f0);
-  f1 = fmaf(__ldg(cf + 9 * C), x[5]*x[8], f1);
-  f2 = fmaf(__ldg(cf + 10 * C), x[9]*x[14], f2);
-  f3 = fmaf(__ldg(cf + 11 * C), x[10]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 12 * C), x[10]*x[15], f0);
-  f1 = fmaf(__ldg(cf + 13 * C), x[11]*x[12], f1);
-  f2 = fmaf(__ldg(cf + 14 * C), x[11]*x[14], f2);
-  f3 = fmaf(__ldg(cf + 15 * C), x[0]*x[0]*x[5], f3);
-  f0 = fmaf(__ldg(cf + 16 * C), x[0]*x[1]*x[2], f0);
-  f1 = fmaf(__ldg(cf + 17 * C), x[0]*x[1]*x[12], f1);
-  f2 = fmaf(__ldg(cf + 18 * C), x[0]*x[1]*x[14], f2);
-  f3 = fmaf(__ldg(cf + 19 * C), x[0]*x[2]*x[11], f3);
-  f0 = fmaf(__ldg(cf + 20 * C), x[0]*x[3]*x[10], f0);
-  f1 = fmaf(__ldg(cf + 21 * C), x[0]*x[4]*x[7], f1);
-  f2 = fmaf(__ldg(cf + 22 * C), x[0]*x[5]*x[6], f2);
-  f3 = fmaf(__ldg(cf + 23 * C), x[0]*x[5]*x[8], f3);
-  f0 = fmaf(__ldg(cf + 24 * C), x[0]*x[9]*x[14], f0);
-  f1 = fmaf(__ldg(cf + 25 * C), x[0]*x[10]*x[13], f1);
-  f2 = fmaf(__ldg(cf + 26 * C), x[0]*x[10]*x[15], f2);
-  f3 = fmaf(__ldg(cf + 27 * C), x[0]*x[11]*x[12], f3);
-  f0 = fmaf(__ldg(cf + 28 * C), x[0]*x[11]*x[14], f0);
-  f1 = fmaf(__ldg(cf + 29 * C), x[1]*x[1]*x[5], f1);
-  f2 = fmaf(__ldg(cf + 30 * C), x[1]*x[2]*x[6], f2);
-  f3 = fmaf(__ldg(cf + 31 * C), x[1]*x[2]*x[8], f3);
-  f0 = fmaf(__ldg(cf + 32 * C), x[1]*x[3]*x[7], f0);
-  f1 = fmaf(__ldg(cf + 33 * C), x[1]*x[4]*x[10], f1);
-  f2 = fmaf(__ldg(cf + 34 * C), x[1]*x[5]*x[9], f2);
-  f3 = fmaf(__ldg(cf + 35 * C), x[1]*x[5]*x[11], f3);
-  f0 = fmaf(__ldg(cf + 36 * C), x[1]*x[6]*x[12], f0);
-  f1 = fmaf(__ldg(cf + 37 * C), x[1]*x[6]*x[14], f1);
-  f2 = fmaf(__ldg(cf + 38 * C), x[1]*x[7]*x[13], f2);
-  f3 = fmaf(__ldg(cf + 39 * C), x[1]*x[7]*x[15], f3);
-  f0 = fmaf(__ldg(cf + 40 * C), x[1]*x[8]*x[12], f0);
-  f1 = fmaf(__ldg(cf + 41 * C), x[1]*x[8]*x[14], f1);
-  f2 = fmaf(__ldg(cf + 42 * C), x[2]*x[2]*x[5], f2);
-  f3 = fmaf(__ldg(cf + 43 * C), x[2]*x[3]*x[4], f3);
-  f0 = fmaf(__ldg(cf + 44 * C), x[2]*x[4]*x[13], f0);
-  f1 = fmaf(__ldg(cf + 45 * C), x[2]*x[4]*x[15], f1);
-  f2 = fmaf(__ldg(cf + 46 * C), x[2]*x[5]*x[12], f2);
-  f3 = fmaf(__ldg(cf + 47 * C), x[2]*x[5]*x[14], f3);
-  f0 = fmaf(__ldg(cf + 48 * C), x[2]*x[6]*x[11], f0);
-  f1 = fmaf(__ldg(cf + 49 * C), x[2]*x[7]*x[10], f1);
-  f2 = fmaf(__ldg(cf + 50 * C), x[2]*x[8]*x[9], f2);
-  f3 = fmaf(__ldg(cf + 51 * C), x[2]*x[8]*x[11], f3);
-  f0 = fmaf(__ldg(cf + 52 * C), x[3]*x[3]*x[5], f0);
-  f1 = fmaf(__ldg(cf + 53 * C), x[3]*x[4]*x[12], f1);
-  f2 = fmaf(__ldg(cf + 54 * C), x[3]*x[4]*x[14], f2);
-  f3 = fmaf(__ldg(cf + 55 * C), x[3]*x[5]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 56 * C), x[3]*x[5]*x[15], f0);
-  f1 = fmaf(__ldg(cf + 57 * C), x[3]*x[6]*x[10], f1);
-  f2 = fmaf(__ldg(cf + 58 * C), x[3]*x[7]*x[9], f2);
-  f3 = fmaf(__ldg(cf + 59 * C), x[3]*x[7]*x[11], f3);
-  f0 = fmaf(__ldg(cf + 60 * C), x[3]*x[8]*x[10], f0);
-  f1 = fmaf(__ldg(cf + 61 * C), x[4]*x[4]*x[5], f1);
-  f2 = fmaf(__ldg(cf + 62 * C), x[4]*x[9]*x[10], f2);
-  f3 = fmaf(__ldg(cf + 63 * C), x[4]*x[10]*x[11], f3);
-  f0 = fmaf(__ldg(cf + 64 * C), x[4]*x[12]*x[13], f0);
-  f1 = fmaf(__ldg(cf + 65 * C), x[4]*x[12]*x[15], f1);
-  f2 = fmaf(__ldg(cf + 66 * C), x[4]*x[13]*x[14], f2);
-  f3 = fmaf(__ldg(cf + 67 * C), x[4]*x[14]*x[15], f3);
-  f0 = fmaf(__ldg(cf + 68 * C), x[5]*x[5]*x[5], f0);
-  f1 = fmaf(__ldg(cf + 69 * C), x[5]*x[6]*x[6], f1);
-  f2 = fmaf(__ldg(cf + 70 * C), x[5]*x[7]*x[7], f2);
-  f3 = fmaf(__ldg(cf + 71 * C), x[5]*x[8]*x[8], f3);
-  f0 = fmaf(__ldg(cf + 72 * C), x[5]*x[9]*x[9], f0);
-  f1 = fmaf(__ldg(cf + 73 * C), x[5]*x[9]*x[11], f1);
-  f2 = fmaf(__ldg(cf + 74 * C), x[5]*x[10]*x[10], f2);
-  f3 = fmaf(__ldg(cf + 75 * C), x[5]*x[11]*x[11], f3);
-  f0 = fmaf(__ldg(cf + 76 * C), x[5]*x[12]*x[12], f0);
-  f1 = fmaf(__ldg(cf + 77 * C), x[5]*x[12]*x[14], f1);
-  f2 = fmaf(__ldg(cf + 78 * C), x[5]*x[13]*x[13], f2);
-  f3 = fmaf(__ldg(cf + 79 * C), x[5]*x[13]*x[15], f3);
-  f0 = fmaf(__ldg(cf + 80 * C), x[5]*x[14]*x[14], f0);
-  f1 = fmaf(__ldg(cf + 81 * C), x[5]*x[15]*x[15], f1);
-  f2 = fmaf(__ldg(cf + 82 * C), x[6]*x[9]*x[14], f2);
-  f3 = fmaf(__ldg(cf + 83 * C), x[6]*x[10]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 84 * C), x[6]*x[10]*x[15], f0);
-  f1 = fmaf(__ldg(cf + 85 * C), x[6]*x[11]*x[12], f1);
-  f2 = fmaf(__ldg(cf + 86 * C), x[6]*x[11]*x[14], f2);
-  f3 = fmaf(__ldg(cf + 87 * C), x[7]*x[9]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 88 * C), x[7]*x[10]*x[12], f0);
-  f1 = fmaf(__ldg(cf + 89 * C), x[7]*x[11]*x[13], f1);
-  f2 = fmaf(__ldg(cf + 90 * C), x[7]*x[11]*x[15], f2);
-  f3 = fmaf(__ldg(cf + 91 * C), x[8]*x[9]*x[12], f3);
-  f0 = fmaf(__ldg(cf + 92 * C), x[8]*x[9]*x[14], f0);
-  f1 = fmaf(__ldg(cf + 93 * C), x[8]*x[10]*x[13], f1);
-  f2 = fmaf(__ldg(cf + 94 * C), x[8]*x[10]*x[15], f2);
-  f3 = fmaf(__ldg(cf + 95 * C), x[8]*x[11]*x[12], f3);
-  f0 = fmaf(__ldg(cf + 96 * C), x[8]*x[11]*x[14], f0);
-  return (f0 + f1) + (f2 + f3);
+  float f = 0.0f;
+  f = fmaf(__ldg(cf + 0 * C), x[5], f);
+  f = fmaf(__ldg(cf + 1 * C), x[0]*x[5], f);
+  f = fmaf(__ldg(cf + 2 * C), x[1]*x[2], f);
+  f = fmaf(__ldg(cf + 3 * C), x[1]*x[12], f);
+  f = fmaf(__ldg(cf + 4 * C), x[1]*x[14], f);
+  f = fmaf(__ldg(cf + 5 * C), x[2]*x[11], f);
+  f = fmaf(__ldg(cf + 6 * C), x[3]*x[10], f);
+  f = fmaf(__ldg(cf + 7 * C), x[4]*x[7], f);
+  f = fmaf(__ldg(cf + 8 * C), x[5]*x[6], f);
+  f = fmaf(__ldg(cf + 9 * C), x[5]*x[8], f);
+  f = fmaf(__ldg(cf + 10 * C), x[9]*x[14], f);
+  f = fmaf(__ldg(cf + 11 * C), x[10]*x[13], f);
+  f = fmaf(__ldg(cf + 12 * C), x[10]*x[15], f);
+  f = fmaf(__ldg(cf + 13 * C), x[11]*x[12], f);
+  f = fmaf(__ldg(cf + 14 * C), x[11]*x[14], f);
+  f = fmaf(__ldg(cf + 15 * C), x[0]*x[0]*x[5], f);
+  f = fmaf(__ldg(cf + 16 * C), x[0]*x[1]*x[2], f);
+  f = fmaf(__ldg(cf + 17 * C), x[0]*x[1]*x[12], f);
+  f = fmaf(__ldg(cf + 18 * C), x[0]*x[1]*x[14], f);
+  f = fmaf(__ldg(cf + 19 * C), x[0]*x[2]*x[11], f);
+  f = fmaf(__ldg(cf + 20 * C), x[0]*x[3]*x[10], f);
+  f = fmaf(__ldg(cf + 21 * C), x[0]*x[4]*x[7], f);
+  f = fmaf(__ldg(cf + 22 * C), x[0]*x[5]*x[6], f);
+  f = fmaf(__ldg(cf + 23 * C), x[0]*x[5]*x[8], f);
+  f = fmaf(__ldg(cf + 24 * C), x[0]*x[9]*x[14], f);
+  f = fmaf(__ldg(cf + 25 * C), x[0]*x[10]*x[13], f);
+  f = fmaf(__ldg(cf + 26 * C), x[0]*x[10]*x[15], f);
+  f = fmaf(__ldg(cf + 27 * C), x[0]*x[11]*x[12], f);
+  f = fmaf(__ldg(cf + 28 * C), x[0]*x[11]*x[14], f);
+  f = fmaf(__ldg(cf + 29 * C), x[1]*x[1]*x[5], f);
+  f = fmaf(__ldg(cf + 30 * C), x[1]*x[2]*x[6], f);
+  f = fmaf(__ldg(cf + 31 * C), x[1]*x[2]*x[8], f);
+  f = fmaf(__ldg(cf + 32 * C), x[1]*x[3]*x[7], f);
+  f = fmaf(__ldg(cf + 33 * C), x[1]*x[4]*x[10], f);
+  f = fmaf(__ldg(cf + 34 * C), x[1]*x[5]*x[9], f);
+  f = fmaf(__ldg(cf + 35 * C), x[1]*x[5]*x[11], f);
+  f = fmaf(__ldg(cf + 36 * C), x[1]*x[6]*x[12], f);
+  f = fmaf(__ldg(cf + 37 * C), x[1]*x[6]*x[14], f);
+  f = fmaf(__ldg(cf + 38 * C), x[1]*x[7]*x[13], f);
+  f = fmaf(__ldg(cf + 39 * C), x[1]*x[7]*x[15], f);
+  f = fmaf(__ldg(cf + 40 * C), x[1]*x[8]*x[12], f);
+  f = fmaf(__ldg(cf + 41 * C), x[1]*x[8]*x[14], f);
+  f = fmaf(__ldg(cf + 42 * C), x[2]*x[2]*x[5], f);
+  f = fmaf(__ldg(cf + 43 * C), x[2]*x[3]*x[4], f);
+  f = fmaf(__ldg(cf + 44 * C), x[2]*x[4]*x[13], f);
+  f = fmaf(__ldg(cf + 45 * C), x[2]*x[4]*x[15], f);
+  f = fmaf(__ldg(cf + 46 * C), x[2]*x[5]*x[12], f);
+  f = fmaf(__ldg(cf + 47 * C), x[2]*x[5]*x[14], f);
+  f = fmaf(__ldg(cf + 48 * C), x[2]*x[6]*x[11], f);
+  f = fmaf(__ldg(cf + 49 * C), x[2]*x[7]*x[10], f);
+  f = fmaf(__ldg(cf + 50 * C), x[2]*x[8]*x[9], f);
+  f = fmaf(__ldg(cf + 51 * C), x[2]*x[8]*x[11], f);
+  f = fmaf(__ldg(cf + 52 * C), x[3]*x[3]*x[5], f);
+  f = fmaf(__ldg(cf + 53 * C), x[3]*x[4]*x[12], f);
+  f = fmaf(__ldg(cf + 54 * C), x[3]*x[4]*x[14], f);
+  f = fmaf(__ldg(cf + 55 * C), x[3]*x[5]*x[13], f);
+  f = fmaf(__ldg(cf + 56 * C), x[3]*x[5]*x[15], f);
+  f = fmaf(__ldg(cf + 57 * C), x[3]*x[6]*x[10], f);
+  f = fmaf(__ldg(cf + 58 * C), x[3]*x[7]*x[9], f);
+  f = fmaf(__ldg(cf + 59 * C), x[3]*x[7]*x[11], f);
+  f = fmaf(__ldg(cf + 60 * C), x[3]*x[8]*x[10], f);
+  f = fmaf(__ldg(cf + 61 * C), x[4]*x[4]*x[5], f);
+  f = fmaf(__ldg(cf + 62 * C), x[4]*x[9]*x[10], f);
+  f = fmaf(__ldg(cf + 63 * C), x[4]*x[10]*x[11], f);
+  f = fmaf(__ldg(cf + 64 * C), x[4]*x[12]*x[13], f);
+  f = fmaf(__ldg(cf + 65 * C), x[4]*x[12]*x[15], f);
+  f = fmaf(__ldg(cf + 66 * C), x[4]*x[13]*x[14], f);
+  f = fmaf(__ldg(cf + 67 * C), x[4]*x[14]*x[15], f);
+  f = fmaf(__ldg(cf + 68 * C), x[5]*x[5]*x[5], f);
+  f = fmaf(__ldg(cf + 69 * C), x[5]*x[6]*x[6], f);
+  f = fmaf(__ldg(cf + 70 * C), x[5]*x[7]*x[7], f);
+  f = fmaf(__ldg(cf + 71 * C), x[5]*x[8]*x[8], f);
+  f = fmaf(__ldg(cf + 72 * C), x[5]*x[9]*x[9], f);
+  f = fmaf(__ldg(cf + 73 * C), x[5]*x[9]*x[11], f);
+  f = fmaf(__ldg(cf + 74 * C), x[5]*x[10]*x[10], f);
+  f = fmaf(__ldg(cf + 75 * C), x[5]*x[11]*x[11], f);
+  f = fmaf(__ldg(cf + 76 * C), x[5]*x[12]*x[12], f);
+  f = fmaf(__ldg(cf + 77 * C), x[5]*x[12]*x[14], f);
+  f = fmaf(__ldg(cf + 78 * C), x[5]*x[13]*x[13], f);
+  f = fmaf(__ldg(cf + 79 * C), x[5]*x[13]*x[15], f);
+  f = fmaf(__ldg(cf + 80 * C), x[5]*x[14]*x[14], f);
+  f = fmaf(__ldg(cf + 81 * C), x[5]*x[15]*x[15], f);
+  f = fmaf(__ldg(cf + 82 * C), x[6]*x[9]*x[14], f);
+  f = fmaf(__ldg(cf + 83 * C), x[6]*x[10]*x[13], f);
+  f = fmaf(__ldg(cf + 84 * C), x[6]*x[10]*x[15], f);
+  f = fmaf(__ldg(cf + 85 * C), x[6]*x[11]*x[12], f);
+  f = fmaf(__ldg(cf + 86 * C), x[6]*x[11]*x[14], f);
+  f = fmaf(__ldg(cf + 87 * C), x[7]*x[9]*x[13], f);
+  f = fmaf(__ldg(cf + 88 * C), x[7]*x[10]*x[12], f);
+  f = fmaf(__ldg(cf + 89 * C), x[7]*x[11]*x[13], f);
+  f = fmaf(__ldg(cf + 90 * C), x[7]*x[11]*x[15], f);
+  f = fmaf(__ldg(cf + 91 * C), x[8]*x[9]*x[12], f);
+  f = fmaf(__ldg(cf + 92 * C), x[8]*x[9]*x[14], f);
+  f = fmaf(__ldg(cf + 93 * C), x[8]*x[10]*x[13], f);
+  f = fmaf(__ldg(cf + 94 * C), x[8]*x[10]*x[15], f);
+  f = fmaf(__ldg(cf + 95 * C), x[8]*x[11]*x[12], f);
+  f = fmaf(__ldg(cf + 96 * C), x[8]*x[11]*x[14], f);
+  return f;
 }
 
 __device__ __forceinline__ void grad_LM5(const float* x, float w, const float* __restrict__ cf, int C, float* g) {
@@ -3548,103 +3548,103 @@ __device__ __forceinline__ void grad_LM5(const float* x, float w, const float* _
 }
 
 __device__ __forceinline__ float value_LM6(const float* x, const float* __restrict__ cf, int C) {
-  float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f, f3 = 0.0f;
-  f0 = fmaf(__ldg(cf + 0 * C), x[6], f0);
-  f1 = fmaf(__ldg(cf + 1 * C), x[0]*x[6], f1);
-  f2 = fmaf(__ldg(cf + 2 * C), x[1]*x[1], f2);
-  f3 = fmaf(__ldg(cf + 3 * C), x[1]*x[11], f3);
-  f0 = fmaf(__ldg(cf + 4 * C), x[2]*x[2], f0);
-  f1 = fmaf(__ldg(cf + 5 * C), x[2]*x[12], f1);
-  f2 = fmaf(__ldg(cf + 6 * C), x[3]*x[3], f2);
-  f3 = fmaf(__ldg(cf + 7 * C), x[3]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 8 * C), x[4]*x[4], f0);
-  f1 = fmaf(__ldg(cf + 9 * C), x[5]*x[5], f1);
-  f2 = fmaf(__ldg(cf + 10 * C), x[6]*x[6], f2);
-  f3 = fmaf(__ldg(cf + 11 * C), x[7]*x[7], f3);
-  f0 = fmaf(__ldg(cf + 12 * C), x[8]*x[8], f0);
-  f1 = fmaf(__ldg(cf + 13 * C), x[9]*x[9], f1);
-  f2 = fmaf(__ldg(cf + 14 * C), x[11]*x[11], f2);
-  f3 = fmaf(__ldg(cf + 15 * C), x[12]*x[12], f3);
-  f0 = fmaf(__ldg(cf + 16 * C), x[13]*x[13], f0);
-  f1 = fmaf(__ldg(cf + 17 * C), x[15]*x[15], f1);
-  f2 = fmaf(__ldg(cf + 18 * C), x[0]*x[0]*x[6], f2);
-  f3 = fmaf(__ldg(cf + 19 * C), x[0]*x[1]*x[1], f3);
-  f0 = fmaf(__ldg(cf + 20 * C), x[0]*x[1]*x[11], f0);
-  f1 = fmaf(__ldg(cf + 21 * C), x[0]*x[2]*x[2], f1);
-  f2 = fmaf(__ldg(cf + 22 * C), x[0]*x[2]*x[12], f2);
-  f3 = fmaf(__ldg(cf + 23 * C), x[0]*x[3]*x[3], f3);
-  f0 = fmaf(__ldg(cf + 24 * C), x[0]*x[3]*x[13], f0);
-  f1 = fmaf(__ldg(cf + 25 * C), x[0]*x[4]*x[4], f1);
-  f2 = fmaf(__ldg(cf + 26 * C), x[0]*x[5]*x[5], f2);
-  f3 = fmaf(__ldg(cf + 27 * C), x[0]*x[6]*x[6], f3);
-  f0 = fmaf(__ldg(cf + 28 * C), x[0]*x[7]*x[7], f0);
-  f1 = fmaf(__ldg(cf + 29 * C), x[0]*x[8]*x[8], f1);
-  f2 = fmaf(__ldg(cf + 30 * C), x[0]*x[9]*x[9], f2);
-  f3 = fmaf(__ldg(cf + 31 * C), x[0]*x[11]*x[11], f3);
-  f0 = fmaf(__ldg(cf + 32 * C), x[0]*x[12]*x[12], f0);
-  f1 = fmaf(__ldg(cf + 33 * C), x[0]*x[13]*x[13], f1);
-  f2 = fmaf(__ldg(cf + 34 * C), x[0]*x[15]*x[15], f2);
-  f3 = fmaf(__ldg(cf + 35 * C), x[1]*x[1]*x[6], f3);
-  f0 = fmaf(__ldg(cf + 36 * C), x[1]*x[1]*x[8], f0);
-  f1 = fmaf(__ldg(cf + 37 * C), x[1]*x[2]*x[5], f1);
-  f2 = fmaf(__ldg(cf + 38 * C), x[1]*x[3]*x[4], f2);
-  f3 = fmaf(__ldg(cf + 39 * C), x[1]*x[4]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 40 * C), x[1]*x[4]*x[15], f0);
-  f1 = fmaf(__ldg(cf + 41 * C), x[1]*x[5]*x[12], f1);
-  f2 = fmaf(__ldg(cf + 42 * C), x[1]*x[5]*x[14], f2);
-  f3 = fmaf(__ldg(cf + 43 * C), x[1]*x[6]*x[11], f3);
-  f0 = fmaf(__ldg(cf + 44 * C), x[1]*x[7]*x[10], f0);
-  f1 = fmaf(__ldg(cf + 45 * C), x[1]*x[8]*x[9], f1);
-  f2 = fmaf(__ldg(cf + 46 * C), x[1]*x[8]*x[11], f2);
-  f3 = fmaf(__ldg(cf + 47 * C), x[2]*x[2]*x[6], f3);
-  f0 = fmaf(__ldg(cf + 48 * C), x[2]*x[3]*x[7], f0);
-  f1 = fmaf(__ldg(cf + 49 * C), x[2]*x[4]*x[10], f1);
-  f2 = fmaf(__ldg(cf + 50 * C), x[2]*x[5]*x[11], f2);
-  f3 = fmaf(__ldg(cf + 51 * C), x[2]*x[6]*x[12], f3);
-  f0 = fmaf(__ldg(cf + 52 * C), x[2]*x[7]*x[13], f0);
-  f1 = fmaf(__ldg(cf + 53 * C), x[2]*x[8]*x[14], f1);
-  f2 = fmaf(__ldg(cf + 54 * C), x[3]*x[3]*x[6], f2);
-  f3 = fmaf(__ldg(cf + 55 * C), x[3]*x[3]*x[8], f3);
-  f0 = fmaf(__ldg(cf + 56 * C), x[3]*x[4]*x[9], f0);
-  f1 = fmaf(__ldg(cf + 57 * C), x[3]*x[4]*x[11], f1);
-  f2 = fmaf(__ldg(cf + 58 * C), x[3]*x[5]*x[10], f2);
-  f3 = fmaf(__ldg(cf + 59 * C), x[3]*x[6]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 60 * C), x[3]*x[7]*x[12], f0);
-  f1 = fmaf(__ldg(cf + 61 * C), x[3]*x[7]*x[14], f1);
-  f2 = fmaf(__ldg(cf + 62 * C), x[3]*x[8]*x[13], f2);
-  f3 = fmaf(__ldg(cf + 63 * C), x[3]*x[8]*x[15], f3);
-  f0 = fmaf(__ldg(cf + 64 * C), x[4]*x[4]*x[6], f0);
-  f1 = fmaf(__ldg(cf + 65 * C), x[4]*x[9]*x[13], f1);
-  f2 = fmaf(__ldg(cf + 66 * C), x[4]*x[10]*x[12], f2);
-  f3 = fmaf(__ldg(cf + 67 * C), x[4]*x[11]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 68 * C), x[4]*x[11]*x[15], f0);
-  f1 = fmaf(__ldg(cf + 69 * C), x[5]*x[5]*x[6], f1);
-  f2 = fmaf(__ldg(cf + 70 * C), x[5]*x[9]*x[14], f2);
-  f3 = fmaf(__ldg(cf + 71 * C), x[5]*x[10]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 72 * C), x[5]*x[10]*x[15], f0);
-  f1 = fmaf(__ldg(cf + 73 * C), x[5]*x[11]*x[12], f1);
-  f2 = fmaf(__ldg(cf + 74 * C), x[5]*x[11]*x[14], f2);
-  f3 = fmaf(__ldg(cf + 75 * C), x[6]*x[6]*x[6], f3);
-  f0 = fmaf(__ldg(cf + 76 * C), x[6]*x[7]*x[7], f0);
-  f1 = fmaf(__ldg(cf + 77 * C), x[6]*x[8]*x[8], f1);
-  f2 = fmaf(__ldg(cf + 78 * C), x[6]*x[9]*x[9], f2);
-  f3 = fmaf(__ldg(cf + 79 * C), x[6]*x[10]*x[10], f3);
-  f0 = fmaf(__ldg(cf + 80 * C), x[6]*x[11]*x[11], f0);
-  f1 = fmaf(__ldg(cf + 81 * C), x[6]*x[12]*x[12], f1);
-  f2 = fmaf(__ldg(cf + 82 * C), x[6]*x[13]*x[13], f2);
-  f3 = fmaf(__ldg(cf + 83 * C), x[6]*x[14]*x[14], f3);
-  f0 = fmaf(__ldg(cf + 84 * C), x[6]*x[15]*x[15], f0);
-  f1 = fmaf(__ldg(cf + 85 * C), x[7]*x[9]*x[10], f1);
-  f2 = fmaf(__ldg(cf + 86 * C), x[7]*x[10]*x[11], f2);
-  f3 = fmaf(__ldg(cf + 87 * C), x[7]*x[12]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 88 * C), x[7]*x[13]*x[14], f0);
-  f1 = fmaf(__ldg(cf + 89 * C), x[7]*x[14]*x[15], f1);
-  f2 = fmaf(__ldg(cf + 90 * C), x[8]*x[9]*x[11], f2);
-  f3 = fmaf(__ldg(cf + 91 * C), x[8]*x[11]*x[11], f3);
-  f0 = fmaf(__ldg(cf + 92 * C), x[8]*x[12]*x[14], f0);
-  f1 = fmaf(__ldg(cf + 93 * C), x[8]*x[13]*x[13], f1);
-  f2 = fmaf(__ldg(cf + 94 * C), x[8]*x[13]*x[15], f2);
-  return (f0 + f1) + (f2 + f3);
+  float f = 0.0f;
+  f = fmaf(__ldg(cf + 0 * C), x[6], f);
+  f = fmaf(__ldg(cf + 1 * C), x[0]*x[6], f);
+  f = fmaf(__ldg(cf + 2 * C), x[1]*x[1], f);
+  f = fmaf(__ldg(cf + 3 * C), x[1]*x[11], f);
+  f = fmaf(__ldg(cf + 4 * C), x[2]*x[2], f);
+  f = fmaf(__ldg(cf + 5 * C), x[2]*x[12], f);
+  f = fmaf(__ldg(cf + 6 * C), x[3]*x[3], f);
+  f = fmaf(__ldg(cf + 7 * C), x[3]*x[13], f);
+  f = fmaf(__ldg(cf + 8 * C), x[4]*x[4], f);
+  f = fmaf(__ldg(cf + 9 * C), x[5]*x[5], f);
+  f = fmaf(__ldg(cf + 10 * C), x[6]*x[6], f);
+  f = fmaf(__ldg(cf + 11 * C), x[7]*x[7], f);
+  f = fmaf(__ldg(cf + 12 * C), x[8]*x[8], f);
+  f = fmaf(__ldg(cf + 13 * C), x[9]*x[9], f);
+  f = fmaf(__ldg(cf + 14 * C), x[11]*x[11], f);
+  f = fmaf(__ldg(cf + 15 * C), x[12]*x[12], f);
+  f = fmaf(__ldg(cf + 16 * C), x[13]*x[13], f);
+  f = fmaf(__ldg(cf + 17 * C), x[15]*x[15], f);
+  f = fmaf(__ldg(cf + 18 * C), x[0]*x[0]*x[6], f);
+  f = fmaf(__ldg(cf + 19 * C), x[0]*x[1]*x[1], f);
+  f = fmaf(__ldg(cf + 20 * C), x[0]*x[1]*x[11], f);
+  f = fmaf(__ldg(cf + 21 * C), x[0]*x[2]*x[2], f);
+  f = fmaf(__ldg(cf + 22 * C), x[0]*x[2]*x[12], f);
+  f = fmaf(__ldg(cf + 23 * C), x[0]*x[3]*x[3], f);
+  f = fmaf(__ldg(cf + 24 * C), x[0]*x[3]*x[13], f);
+  f = fmaf(__ldg(cf + 25 * C), x[0]*x[4]*x[4], f);
+  f = fmaf(__ldg(cf + 26 * C), x[0]*x[5]*x[5], f);
+  f = fmaf(__ldg(cf + 27 * C), x[0]*x[6]*x[6], f);
+  f = fmaf(__ldg(cf + 28 * C), x[0]*x[7]*x[7], f);
+  f = fmaf(__ldg(cf + 29 * C), x[0]*x[8]*x[8], f);
+  f = fmaf(__ldg(cf + 30 * C), x[0]*x[9]*x[9], f);
+  f = fmaf(__ldg(cf + 31 * C), x[0]*x[11]*x[11], f);
+  f = fmaf(__ldg(cf + 32 * C), x[0]*x[12]*x[12], f);
+  f = fmaf(__ldg(cf + 33 * C), x[0]*x[13]*x[13], f);
+  f = fmaf(__ldg(cf + 34 * C), x[0]*x[15]*x[15], f);
+  f = fmaf(__ldg(cf + 35 * C), x[1]*x[1]*x[6], f);
+  f = fmaf(__ldg(cf + 36 * C), x[1]*x[1]*x[8], f);
+  f = fmaf(__ldg(cf + 37 * C), x[1]*x[2]*x[5], f);
+  f = fmaf(__ldg(cf + 38 * C), x[1]*x[3]*x[4], f);
+  f = fmaf(__ldg(cf + 39 * C), x[1]*x[4]*x[13], f);
+  f = fmaf(__ldg(cf + 40 * C), x[1]*x[4]*x[15], f);
+  f = fmaf(__ldg(cf + 41 * C), x[1]*x[5]*x[12], f);
+  f = fmaf(__ldg(cf + 42 * C), x[1]*x[5]*x[14], f);
+  f = fmaf(__ldg(cf + 43 * C), x[1]*x[6]*x[11], f);
+  f = fmaf(__ldg(cf + 44 * C), x[1]*x[7]*x[10], f);
+  f = fmaf(__ldg(cf + 45 * C), x[1]*x[8]*x[9], f);
+  f = fmaf(__ldg(cf + 46 * C), x[1]*x[8]*x[11], f);
+  f = fmaf(__ldg(cf + 47 * C), x[2]*x[2]*x[6], f);
+  f = fmaf(__ldg(cf + 48 * C), x[2]*x[3]*x[7], f);
+  f = fmaf(__ldg(cf + 49 * C), x[2]*x[4]*x[10], f);
+  f = fmaf(__ldg(cf + 50 * C), x[2]*x[5]*x[11], f);
+  f = fmaf(__ldg(cf + 51 * C), x[2]*x[6]*x[12], f);
+  f = fmaf(__ldg(cf + 52 * C), x[2]*x[7]*x[13], f);
+  f = fmaf(__ldg(cf + 53 * C), x[2]*x[8]*x[14], f);
+  f = fmaf(__ldg(cf + 54 * C), x[3]*x[3]*x[6], f);
+  f = fmaf(__ldg(cf + 55 * C), x[3]*x[3]*x[8], f);
+  f = fmaf(__ldg(cf + 56 * C), x[3]*x[4]*x[9], f);
+  f = fmaf(__ldg(cf + 57 * C), x[3]*x[4]*x[11], f);
+  f = fmaf(__ldg(cf + 58 * C), x[3]*x[5]*x[10], f);
+  f = fmaf(__ldg(cf + 59 * C), x[3]*x[6]*x[13], f);
+  f = fmaf(__ldg(cf + 60 * C), x[3]*x[7]*x[12], f);
+  f = fmaf(__ldg(cf + 61 * C), x[3]*x[7]*x[14], f);
+  f = fmaf(__ldg(cf + 62 * C), x[3]*x[8]*x[13], f);
+  f = fmaf(__ldg(cf + 63 * C), x[3]*x[8]*x[15], f);
+  f = fmaf(__ldg(cf + 64 * C), x[4]*x[4]*x[6], f);
+  f = fmaf(__ldg(cf + 65 * C), x[4]*x[9]*x[13], f);
+  f = fmaf(__ldg(cf + 66 * C), x[4]*x[10]*x[12], f);
+  f = fmaf(__ldg(cf + 67 * C), x[4]*x[11]*x[13], f);
+  f = fmaf(__ldg(cf + 68 * C), x[4]*x[11]*x[15], f);
+  f = fmaf(__ldg(cf + 69 * C), x[5]*x[5]*x[6], f);
+  f = fmaf(__ldg(cf + 70 * C), x[5]*x[9]*x[14], f);
+  f = fmaf(__ldg(cf + 71 * C), x[5]*x[10]*x[13], f);
+  f = fmaf(__ldg(cf + 72 * C), x[5]*x[10]*x[15], f);
+  f = fmaf(__ldg(cf + 73 * C), x[5]*x[11]*x[12], f);
+  f = fmaf(__ldg(cf + 74 * C), x[5]*x[11]*x[14], f);
+  f = fmaf(__ldg(cf + 75 * C), x[6]*x[6]*x[6], f);
+  f = fmaf(__ldg(cf + 76 * C), x[6]*x[7]*x[7], f);
+  f = fmaf(__ldg(cf + 77 * C), x[6]*x[8]*x[8], f);
+  f = fmaf(__ldg(cf + 78 * C), x[6]*x[9]*x[9], f);
+  f = fmaf(__ldg(cf + 79 * C), x[6]*x[10]*x[10], f);
+  f = fmaf(__ldg(cf + 80 * C), x[6]*x[11]*x[11], f);
+  f = fmaf(__ldg(cf + 81 * C), x[6]*x[12]*x[12], f);
+  f = fmaf(__ldg(cf + 82 * C), x[6]*x[13]*x[13], f);
+  f = fmaf(__ldg(cf + 83 * C), x[6]*x[14]*x[14], f);
+  f = fmaf(__ldg(cf + 84 * C), x[6]*x[15]*x[15], f);
+  f = fmaf(__ldg(cf + 85 * C), x[7]*x[9]*x[10], f);
+  f = fmaf(__ldg(cf + 86 * C), x[7]*x[10]*x[11], f);
+  f = fmaf(__ldg(cf + 87 * C), x[7]*x[12]*x[13], f);
+  f = fmaf(__ldg(cf + 88 * C), x[7]*x[13]*x[14], f);
+  f = fmaf(__ldg(cf + 89 * C), x[7]*x[14]*x[15], f);
+  f = fmaf(__ldg(cf + 90 * C), x[8]*x[9]*x[11], f);
+  f = fmaf(__ldg(cf + 91 * C), x[8]*x[11]*x[11], f);
+  f = fmaf(__ldg(cf + 92 * C), x[8]*x[12]*x[14], f);
+  f = fmaf(__ldg(cf + 93 * C), x[8]*x[13]*x[13], f);
+  f = fmaf(__ldg(cf + 94 * C), x[8]*x[13]*x[15], f);
+  return f;
 }
 
 __device__ __forceinline__ void grad_LM6(const float* x, float w, const float* __restrict__ cf, int C, float* g) {
@@ -4107,105 +4107,105 @@ __device__ __forceinline__ void grad_LM6(const float* x, float w, const float* _
 }
 
 __device__ __forceinline__ float value_LM7(const float* x, const float* __restrict__ cf, int C) {
-  float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f, f3 = 0.0f;
-  f0 = fmaf(__ldg(cf + 0 * C), x[7], f0);
-  f1 = fmaf(__ldg(cf + 1 * C), x[0]*x[7], f1);
-  f2 = fmaf(__ldg(cf + 2 * C), x[1]*x[10], f2);
-  f3 = fmaf(__ldg(cf + 3 * C), x[2]*x[3], f3);
-  f0 = fmaf(__ldg(cf + 4 * C), x[2]*x[13], f0);
-  f1 = fmaf(__ldg(cf + 5 * C), x[3]*x[12], f1);
-  f2 = fmaf(__ldg(cf + 6 * C), x[3]*x[14], f2);
-  f3 = fmaf(__ldg(cf + 7 * C), x[4]*x[5], f3);
-  f0 = fmaf(__ldg(cf + 8 * C), x[6]*x[7], f0);
-  f1 = fmaf(__ldg(cf + 9 * C), x[7]*x[8], f1);
-  f2 = fmaf(__ldg(cf + 10 * C), x[9]*x[10], f2);
-  f3 = fmaf(__ldg(cf + 11 * C), x[10]*x[11], f3);
-  f0 = fmaf(__ldg(cf + 12 * C), x[12]*x[13], f0);
-  f1 = fmaf(__ldg(cf + 13 * C), x[13]*x[14], f1);
-  f2 = fmaf(__ldg(cf + 14 * C), x[14]*x[15], f2);
-  f3 = fmaf(__ldg(cf + 15 * C), x[0]*x[0]*x[7], f3);
-  f0 = fmaf(__ldg(cf + 16 * C), x[0]*x[1]*x[10], f0);
-  f1 = fmaf(__ldg(cf + 17 * C), x[0]*x[2]*x[3], f1);
-  f2 = fmaf(__ldg(cf + 18 * C), x[0]*x[2]*x[13], f2);
-  f3 = fmaf(__ldg(cf + 19 * C), x[0]*x[3]*x[12], f3);
-  f0 = fmaf(__ldg(cf + 20 * C), x[0]*x[3]*x[14], f0);
-  f1 = fmaf(__ldg(cf + 21 * C), x[0]*x[4]*x[5], f1);
-  f2 = fmaf(__ldg(cf + 22 * C), x[0]*x[6]*x[7], f2);
-  f3 = fmaf(__ldg(cf + 23 * C), x[0]*x[7]*x[8], f3);
-  f0 = fmaf(__ldg(cf + 24 * C), x[0]*x[9]*x[10], f0);
-  f1 = fmaf(__ldg(cf + 25 * C), x[0]*x[10]*x[11], f1);
-  f2 = fmaf(__ldg(cf + 26 * C), x[0]*x[12]*x[13], f2);
-  f3 = fmaf(__ldg(cf + 27 * C), x[0]*x[13]*x[14], f3);
-  f0 = fmaf(__ldg(cf + 28 * C), x[0]*x[14]*x[15], f0);
-  f1 = fmaf(__ldg(cf + 29 * C), x[1]*x[1]*x[7], f1);
-  f2 = fmaf(__ldg(cf + 30 * C), x[1]*x[2]*x[4], f2);
-  f3 = fmaf(__ldg(cf + 31 * C), x[1]*x[3]*x[5], f3);
-  f0 = fmaf(__ldg(cf + 32 * C), x[1]*x[4]*x[12], f0);
-  f1 = fmaf(__ldg(cf + 33 * C), x[1]*x[4]*x[14], f1);
-  f2 = fmaf(__ldg(cf + 34 * C), x[1]*x[5]*x[13], f2);
-  f3 = fmaf(__ldg(cf + 35 * C), x[1]*x[5]*x[15], f3);
-  f0 = fmaf(__ldg(cf + 36 * C), x[1]*x[6]*x[10], f0);
-  f1 = fmaf(__ldg(cf + 37 * C), x[1]*x[7]*x[9], f1);
-  f2 = fmaf(__ldg(cf + 38 * C), x[1]*x[7]*x[11], f2);
-  f3 = fmaf(__ldg(cf + 39 * C), x[1]*x[8]*x[10], f3);
-  f0 = fmaf(__ldg(cf + 40 * C), x[2]*x[2]*x[7], f0);
-  f1 = fmaf(__ldg(cf + 41 * C), x[2]*x[3]*x[6], f1);
-  f2 = fmaf(__ldg(cf + 42 * C), x[2]*x[3]*x[8], f2);
-  f3 = fmaf(__ldg(cf + 43 * C), x[2]*x[4]*x[9], f3);
-  f0 = fmaf(__ldg(cf + 44 * C), x[2]*x[4]*x[11], f0);
-  f1 = fmaf(__ldg(cf + 45 * C), x[2]*x[5]*x[10], f1);
-  f2 = fmaf(__ldg(cf + 46 * C), x[2]*x[6]*x[13], f2);
-  f3 = fmaf(__ldg(cf + 47 * C), x[2]*x[7]*x[12], f3);
-  f0 = fmaf(__ldg(cf + 48 * C), x[2]*x[7]*x[14], f0);
-  f1 = fmaf(__ldg(cf + 49 * C), x[2]*x[8]*x[13], f1);
-  f2 = fmaf(__ldg(cf + 50 * C), x[2]*x[8]*x[15], f2);
-  f3 = fmaf(__ldg(cf + 51 * C), x[3]*x[3]*x[7], f3);
-  f0 = fmaf(__ldg(cf + 52 * C), x[3]*x[4]*x[10], f0);
-  f1 = fmaf(__ldg(cf + 53 * C), x[3]*x[5]*x[9], f1);
-  f2 = fmaf(__ldg(cf + 54 * C), x[3]*x[5]*x[11], f2);
-  f3 = fmaf(__ldg(cf + 55 * C), x[3]*x[6]*x[12], f3);
-  f0 = fmaf(__ldg(cf + 56 * C), x[3]*x[6]*x[14], f0);
-  f1 = fmaf(__ldg(cf + 57 * C), x[3]*x[7]*x[13], f1);
-  f2 = fmaf(__ldg(cf + 58 * C), x[3]*x[7]*x[15], f2);
-  f3 = fmaf(__ldg(cf + 59 * C), x[3]*x[8]*x[12], f3);
-  f0 = fmaf(__ldg(cf + 60 * C), x[3]*x[8]*x[14], f0);
-  f1 = fmaf(__ldg(cf + 61 * C), x[4]*x[4]*x[7], f1);
-  f2 = fmaf(__ldg(cf + 62 * C), x[4]*x[9]*x[12], f2);
-  f3 = fmaf(__ldg(cf + 63 * C), x[4]*x[9]*x[14], f3);
-  f0 = fmaf(__ldg(cf + 64 * C), x[4]*x[10]*x[13], f0);
-  f1 = fmaf(__ldg(cf + 65 * C), x[4]*x[10]*x[15], f1);
-  f2 = fmaf(__ldg(cf + 66 * C), x[4]*x[11]*x[12], f2);
-  f3 = fmaf(__ldg(cf + 67 * C), x[4]*x[11]*x[14], f3);
-  f0 = fmaf(__ldg(cf + 68 * C), x[5]*x[5]*x[7], f0);
-  f1 = fmaf(__ldg(cf + 69 * C), x[5]*x[9]*x[13], f1);
-  f2 = fmaf(__ldg(cf + 70 * C), x[5]*x[10]*x[12], f2);
-  f3 = fmaf(__ldg(cf + 71 * C), x[5]*x[11]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 72 * C), x[5]*x[11]*x[15], f0);
-  f1 = fmaf(__ldg(cf + 73 * C), x[6]*x[6]*x[7], f1);
-  f2 = fmaf(__ldg(cf + 74 * C), x[6]*x[9]*x[10], f2);
-  f3 = fmaf(__ldg(cf + 75 * C), x[6]*x[10]*x[11], f3);
-  f0 = fmaf(__ldg(cf + 76 * C), x[6]*x[12]*x[13], f0);
-  f1 = fmaf(__ldg(cf + 77 * C), x[6]*x[13]*x[14], f1);
-  f2 = fmaf(__ldg(cf + 78 * C), x[6]*x[14]*x[15], f2);
-  f3 = fmaf(__ldg(cf + 79 * C), x[7]*x[7]*x[7], f3);
-  f0 = fmaf(__ldg(cf + 80 * C), x[7]*x[8]*x[8], f0);
-  f1 = fmaf(__ldg(cf + 81 * C), x[7]*x[9]*x[9], f1);
-  f2 = fmaf(__ldg(cf + 82 * C), x[7]*x[9]*x[11], f2);
-  f3 = fmaf(__ldg(cf + 83 * C), x[7]*x[10]*x[10], f3);
-  f0 = fmaf(__ldg(cf + 84 * C), x[7]*x[11]*x[11], f0);
-  f1 = fmaf(__ldg(cf + 85 * C), x[7]*x[12]*x[12], f1);
-  f2 = fmaf(__ldg(cf + 86 * C), x[7]*x[12]*x[14], f2);
-  f3 = fmaf(__ldg(cf + 87 * C), x[7]*x[13]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 88 * C), x[7]*x[13]*x[15], f0);
-  f1 = fmaf(__ldg(cf + 89 * C), x[7]*x[14]*x[14], f1);
-  f2 = fmaf(__ldg(cf + 90 * C), x[7]*x[15]*x[15], f2);
-  f3 = fmaf(__ldg(cf + 91 * C), x[8]*x[9]*x[10], f3);
-  f0 = fmaf(__ldg(cf + 92 * C), x[8]*x[10]*x[11], f0);
-  f1 = fmaf(__ldg(cf + 93 * C), x[8]*x[12]*x[13], f1);
-  f2 = fmaf(__ldg(cf + 94 * C), x[8]*x[12]*x[15], f2);
-  f3 = fmaf(__ldg(cf + 95 * C), x[8]*x[13]*x[14], f3);
-  f0 = fmaf(__ldg(cf + 96 * C), x[8]*x[14]*x[15], f0);
-  return (f0 + f1) + (f2 + f3);
+  float f = 0.0f;
+  f = fmaf(__ldg(cf + 0 * C), x[7], f);
+  f = fmaf(__ldg(cf + 1 * C), x[0]*x[7], f);
+  f = fmaf(__ldg(cf + 2 * C), x[1]*x[10], f);
+  f = fmaf(__ldg(cf + 3 * C), x[2]*x[3], f);
+  f = fmaf(__ldg(cf + 4 * C), x[2]*x[13], f);
+  f = fmaf(__ldg(cf + 5 * C), x[3]*x[12], f);
+  f = fmaf(__ldg(cf + 6 * C), x[3]*x[14], f);
+  f = fmaf(__ldg(cf + 7 * C), x[4]*x[5], f);
+  f = fmaf(__ldg(cf + 8 * C), x[6]*x[7], f);
+  f = fmaf(__ldg(cf + 9 * C), x[7]*x[8], f);
+  f = fmaf(__ldg(cf + 10 * C), x[9]*x[10], f);
+  f = fmaf(__ldg(cf + 11 * C), x[10]*x[11], f);
+  f = fmaf(__ldg(cf + 12 * C), x[12]*x[13], f);
+  f = fmaf(__ldg(cf + 13 * C), x[13]*x[14], f);
+  f = fmaf(__ldg(cf + 14 * C), x[14]*x[15], f);
+  f = fmaf(__ldg(cf + 15 * C), x[0]*x[0]*x[7], f);
+  f = fmaf(__ldg(cf + 16 * C), x[0]*x[1]*x[10], f);
+  f = fmaf(__ldg(cf + 17 * C), x[0]*x[2]*x[3], f);
+  f = fmaf(__ldg(cf + 18 * C), x[0]*x[2]*x[13], f);
+  f = fmaf(__ldg(cf + 19 * C), x[0]*x[3]*x[12], f);
+  f = fmaf(__ldg(cf + 20 * C), x[0]*x[3]*x[14], f);
+  f = fmaf(__ldg(cf + 21 * C), x[0]*x[4]*x[5], f);
+  f = fmaf(__ldg(cf + 22 * C), x[0]*x[6]*x[7], f);
+  f = fmaf(__ldg(cf + 23 * C), x[0]*x[7]*x[8], f);
+  f = fmaf(__ldg(cf + 24 * C), x[0]*x[9]*x[10], f);
+  f = fmaf(__ldg(cf + 25 * C), x[0]*x[10]*x[11], f);
+  f = fmaf(__ldg(cf + 26 * C), x[0]*x[12]*x[13], f);
+  f = fmaf(__ldg(cf + 27 * C), x[0]*x[13]*x[14], f);
+  f = fmaf(__ldg(cf + 28 * C), x[0]*x[14]*x[15], f);
+  f = fmaf(__ldg(cf + 29 * C), x[1]*x[1]*x[7], f);
+  f = fmaf(__ldg(cf + 30 * C), x[1]*x[2]*x[4], f);
+  f = fmaf(__ldg(cf + 31 * C), x[1]*x[3]*x[5], f);
+  f = fmaf(__ldg(cf + 32 * C), x[1]*x[4]*x[12], f);
+  f = fmaf(__ldg(cf + 33 * C), x[1]*x[4]*x[14], f);
+  f = fmaf(__ldg(cf + 34 * C), x[1]*x[5]*x[13], f);
+  f = fmaf(__ldg(cf + 35 * C), x[1]*x[5]*x[15], f);
+  f = fmaf(__ldg(cf + 36 * C), x[1]*x[6]*x[10], f);
+  f = fmaf(__ldg(cf + 37 * C), x[1]*x[7]*x[9], f);
+  f = fmaf(__ldg(cf + 38 * C), x[1]*x[7]*x[11], f);
+  f = fmaf(__ldg(cf + 39 * C), x[1]*x[8]*x[10], f);
+  f = fmaf(__ldg(cf + 40 * C), x[2]*x[2]*x[7], f);
+  f = fmaf(__ldg(cf + 41 * C), x[2]*x[3]*x[6], f);
+  f = fmaf(__ldg(cf + 42 * C), x[2]*x[3]*x[8], f);
+  f = fmaf(__ldg(cf + 43 * C), x[2]*x[4]*x[9], f);
+  f = fmaf(__ldg(cf + 44 * C), x[2]*x[4]*x[11], f);
+  f = fmaf(__ldg(cf + 45 * C), x[2]*x[5]*x[10], f);
+  f = fmaf(__ldg(cf + 46 * C), x[2]*x[6]*x[13], f);
+  f = fmaf(__ldg(cf + 47 * C), x[2]*x[7]*x[12], f);
+  f = fmaf(__ldg(cf + 48 * C), x[2]*x[7]*x[14], f);
+  f = fmaf(__ldg(cf + 49 * C), x[2]*x[8]*x[13], f);
+  f = fmaf(__ldg(cf + 50 * C), x[2]*x[8]*x[15], f);
+  f = fmaf(__ldg(cf + 51 * C), x[3]*x[3]*x[7], f);
+  f = fmaf(__ldg(cf + 52 * C), x[3]*x[4]*x[10], f);
+  f = fmaf(__ldg(cf + 53 * C), x[3]*x[5]*x[9], f);
+  f = fmaf(__ldg(cf + 54 * C), x[3]*x[5]*x[11], f);
+  f = fmaf(__ldg(cf + 55 * C), x[3]*x[6]*x[12], f);
+  f = fmaf(__ldg(cf + 56 * C), x[3]*x[6]*x[14], f);
+  f = fmaf(__ldg(cf + 57 * C), x[3]*x[7]*x[13], f);
+  f = fmaf(__ldg(cf + 58 * C), x[3]*x[7]*x[15], f);
+  f = fmaf(__ldg(cf + 59 * C), x[3]*x[8]*x[12], f);
+  f = fmaf(__ldg(cf + 60 * C), x[3]*x[8]*x[14], f);
+  f = fmaf(__ldg(cf + 61 * C), x[4]*x[4]*x[7], f);
+  f = fmaf(__ldg(cf + 62 * C), x[4]*x[9]*x[12], f);
+  f = fmaf(__ldg(cf + 63 * C), x[4]*x[9]*x[14], f);
+  f = fmaf(__ldg(cf + 64 * C), x[4]*x[10]*x[13], f);
+  f = fmaf(__ldg(cf + 65 * C), x[4]*x[10]*x[15], f);
+  f = fmaf(__ldg(cf + 66 * C), x[4]*x[11]*x[12], f);
+  f = fmaf(__ldg(cf + 67 * C), x[4]*x[11]*x[14], f);
+  f = fmaf(__ldg(cf + 68 * C), x[5]*x[5]*x[7], f);
+  f = fmaf(__ldg(cf + 69 * C), x[5]*x[9]*x[13], f);
+  f = fmaf(__ldg(cf + 70 * C), x[5]*x[10]*x[12], f);
+  f = fmaf(__ldg(cf + 71 * C), x[5]*x[11]*x[13], f);
+  f = fmaf(__ldg(cf + 72 * C), x[5]*x[11]*x[15], f);
+  f = fmaf(__ldg(cf + 73 * C), x[6]*x[6]*x[7], f);
+  f = fmaf(__ldg(cf + 74 * C), x[6]*x[9]*x[10], f);
+  f = fmaf(__ldg(cf + 75 * C), x[6]*x[10]*x[11], f);
+  f = fmaf(__ldg(cf + 76 * C), x[6]*x[12]*x[13], f);
+  f = fmaf(__ldg(cf + 77 * C), x[6]*x[13]*x[14], f);
+  f = fmaf(__ldg(cf + 78 * C), x[6]*x[14]*x[15], f);
+  f = fmaf(__ldg(cf + 79 * C), x[7]*x[7]*x[7], f);
+  f = fmaf(__ldg(cf + 80 * C), x[7]*x[8]*x[8], f);
+  f = fmaf(__ldg(cf + 81 * C), x[7]*x[9]*x[9], f);
+  f = fmaf(__ldg(cf + 82 * C), x[7]*x[9]*x[11], f);
+  f = fmaf(__ldg(cf + 83 * C), x[7]*x[10]*x[10], f);
+  f = fmaf(__ldg(cf + 84 * C), x[7]*x[11]*x[11], f);
+  f = fmaf(__ldg(cf + 85 * C), x[7]*x[12]*x[12], f);
+  f = fmaf(__ldg(cf + 86 * C), x[7]*x[12]*x[14], f);
+  f = fmaf(__ldg(cf + 87 * C), x[7]*x[13]*x[13], f);
+  f = fmaf(__ldg(cf + 88 * C), x[7]*x[13]*x[15], f);
+  f = fmaf(__ldg(cf + 89 * C), x[7]*x[14]*x[14], f);
+  f = fmaf(__ldg(cf + 90 * C), x[7]*x[15]*x[15], f);
+  f = fmaf(__ldg(cf + 91 * C), x[8]*x[9]*x[10], f);
+  f = fmaf(__ldg(cf + 92 * C), x[8]*x[10]*x[11], f);
+  f = fmaf(__ldg(cf + 93 * C), x[8]*x[12]*x[13], f);
+  f = fmaf(__ldg(cf + 94 * C), x[8]*x[12]*x[15], f);
+  f = fmaf(__ldg(cf + 95 * C), x[8]*x[13]*x[14], f);
+  f = fmaf(__ldg(cf + 96 * C), x[8]*x[14]*x[15], f);
+  return f;
 }
 
 __device__ __forceinline__ void grad_LM7(const float* x, float w, const float* __restrict__ cf, int C, float* g) {
@@ -4681,106 +4681,106 @@ __device__ __forceinline__ void grad_LM7(const float* x, float w, const float* _
 }
 
 __device__ __forceinline__ float value_LM8(const float* x, const float* __restrict__ cf, int C) {
-  float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f, f3 = 0.0f;
-  f0 = fmaf(__ldg(cf + 0 * C), x[8], f0);
-  f1 = fmaf(__ldg(cf + 1 * C), x[0]*x[8], f1);
-  f2 = fmaf(__ldg(cf + 2 * C), x[1]*x[1], f2);
-  f3 = fmaf(__ldg(cf + 3 * C), x[1]*x[9], f3);
-  f0 = fmaf(__ldg(cf + 4 * C), x[1]*x[11], f0);
-  f1 = fmaf(__ldg(cf + 5 * C), x[2]*x[14], f1);
-  f2 = fmaf(__ldg(cf + 6 * C), x[3]*x[3], f2);
-  f3 = fmaf(__ldg(cf + 7 * C), x[3]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 8 * C), x[3]*x[15], f0);
-  f1 = fmaf(__ldg(cf + 9 * C), x[5]*x[5], f1);
-  f2 = fmaf(__ldg(cf + 10 * C), x[6]*x[8], f2);
-  f3 = fmaf(__ldg(cf + 11 * C), x[7]*x[7], f3);
-  f0 = fmaf(__ldg(cf + 12 * C), x[9]*x[11], f0);
-  f1 = fmaf(__ldg(cf + 13 * C), x[11]*x[11], f1);
-  f2 = fmaf(__ldg(cf + 14 * C), x[12]*x[14], f2);
-  f3 = fmaf(__ldg(cf + 15 * C), x[13]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 16 * C), x[13]*x[15], f0);
-  f1 = fmaf(__ldg(cf + 17 * C), x[0]*x[0]*x[8], f1);
-  f2 = fmaf(__ldg(cf + 18 * C), x[0]*x[1]*x[1], f2);
-  f3 = fmaf(__ldg(cf + 19 * C), x[0]*x[1]*x[9], f3);
-  f0 = fmaf(__ldg(cf + 20 * C), x[0]*x[1]*x[11], f0);
-  f1 = fmaf(__ldg(cf + 21 * C), x[0]*x[2]*x[14], f1);
-  f2 = fmaf(__ldg(cf + 22 * C), x[0]*x[3]*x[3], f2);
-  f3 = fmaf(__ldg(cf + 23 * C), x[0]*x[3]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 24 * C), x[0]*x[3]*x[15], f0);
-  f1 = fmaf(__ldg(cf + 25 * C), x[0]*x[5]*x[5], f1);
-  f2 = fmaf(__ldg(cf + 26 * C), x[0]*x[6]*x[8], f2);
-  f3 = fmaf(__ldg(cf + 27 * C), x[0]*x[7]*x[7], f3);
-  f0 = fmaf(__ldg(cf + 28 * C), x[0]*x[9]*x[11], f0);
-  f1 = fmaf(__ldg(cf + 29 * C), x[0]*x[11]*x[11], f1);
-  f2 = fmaf(__ldg(cf + 30 * C), x[0]*x[12]*x[14], f2);
-  f3 = fmaf(__ldg(cf + 31 * C), x[0]*x[13]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 32 * C), x[0]*x[13]*x[15], f0);
-  f1 = fmaf(__ldg(cf + 33 * C), x[1]*x[1]*x[6], f1);
-  f2 = fmaf(__ldg(cf + 34 * C), x[1]*x[1]*x[8], f2);
-  f3 = fmaf(__ldg(cf + 35 * C), x[1]*x[2]*x[5], f3);
-  f0 = fmaf(__ldg(cf + 36 * C), x[1]*x[4]*x[13], f0);
-  f1 = fmaf(__ldg(cf + 37 * C), x[1]*x[4]*x[15], f1);
-  f2 = fmaf(__ldg(cf + 38 * C), x[1]*x[5]*x[12], f2);
-  f3 = fmaf(__ldg(cf + 39 * C), x[1]*x[5]*x[14], f3);
-  f0 = fmaf(__ldg(cf + 40 * C), x[1]*x[6]*x[9], f0);
-  f1 = fmaf(__ldg(cf + 41 * C), x[1]*x[6]*x[11], f1);
-  f2 = fmaf(__ldg(cf + 42 * C), x[1]*x[7]*x[10], f2);
-  f3 = fmaf(__ldg(cf + 43 * C), x[1]*x[8]*x[9], f3);
-  f0 = fmaf(__ldg(cf + 44 * C), x[1]*x[8]*x[11], f0);
-  f1 = fmaf(__ldg(cf + 45 * C), x[2]*x[2]*x[8], f1);
-  f2 = fmaf(__ldg(cf + 46 * C), x[2]*x[3]*x[7], f2);
-  f3 = fmaf(__ldg(cf + 47 * C), x[2]*x[5]*x[9], f3);
-  f0 = fmaf(__ldg(cf + 48 * C), x[2]*x[5]*x[11], f0);
-  f1 = fmaf(__ldg(cf + 49 * C), x[2]*x[6]*x[14], f1);
-  f2 = fmaf(__ldg(cf + 50 * C), x[2]*x[7]*x[13], f2);
-  f3 = fmaf(__ldg(cf + 51 * C), x[2]*x[7]*x[15], f3);
-  f0 = fmaf(__ldg(cf + 52 * C), x[2]*x[8]*x[12], f0);
-  f1 = fmaf(__ldg(cf + 53 * C), x[3]*x[3]*x[6], f1);
-  f2 = fmaf(__ldg(cf + 54 * C), x[3]*x[3]*x[8], f2);
-  f3 = fmaf(__ldg(cf + 55 * C), x[3]*x[4]*x[9], f3);
-  f0 = fmaf(__ldg(cf + 56 * C), x[3]*x[4]*x[11], f0);
-  f1 = fmaf(__ldg(cf + 57 * C), x[3]*x[5]*x[10], f1);
-  f2 = fmaf(__ldg(cf + 58 * C), x[3]*x[6]*x[13], f2);
-  f3 = fmaf(__ldg(cf + 59 * C), x[3]*x[6]*x[15], f3);
-  f0 = fmaf(__ldg(cf + 60 * C), x[3]*x[7]*x[12], f0);
-  f1 = fmaf(__ldg(cf + 61 * C), x[3]*x[7]*x[14], f1);
-  f2 = fmaf(__ldg(cf + 62 * C), x[3]*x[8]*x[13], f2);
-  f3 = fmaf(__ldg(cf + 63 * C), x[3]*x[8]*x[15], f3);
-  f0 = fmaf(__ldg(cf + 64 * C), x[4]*x[4]*x[8], f0);
-  f1 = fmaf(__ldg(cf + 65 * C), x[4]*x[9]*x[13], f1);
-  f2 = fmaf(__ldg(cf + 66 * C), x[4]*x[10]*x[14], f2);
-  f3 = fmaf(__ldg(cf + 67 * C), x[4]*x[11]*x[15], f3);
-  f0 = fmaf(__ldg(cf + 68 * C), x[5]*x[5]*x[8], f0);
-  f1 = fmaf(__ldg(cf + 69 * C), x[5]*x[9]*x[12], f1);
-  f2 = fmaf(__ldg(cf + 70 * C), x[5]*x[9]*x[14], f2);
-  f3 = fmaf(__ldg(cf + 71 * C), x[5]*x[10]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 72 * C), x[5]*x[10]*x[15], f0);
-  f1 = fmaf(__ldg(cf + 73 * C), x[5]*x[11]*x[12], f1);
-  f2 = fmaf(__ldg(cf + 74 * C), x[5]*x[11]*x[14], f2);
-  f3 = fmaf(__ldg(cf + 75 * C), x[6]*x[6]*x[8], f3);
-  f0 = fmaf(__ldg(cf + 76 * C), x[6]*x[9]*x[11], f0);
-  f1 = fmaf(__ldg(cf + 77 * C), x[6]*x[11]*x[11], f1);
-  f2 = fmaf(__ldg(cf + 78 * C), x[6]*x[12]*x[14], f2);
-  f3 = fmaf(__ldg(cf + 79 * C), x[6]*x[13]*x[13], f3);
-  f0 = fmaf(__ldg(cf + 80 * C), x[6]*x[13]*x[15], f0);
-  f1 = fmaf(__ldg(cf + 81 * C), x[7]*x[7]*x[8], f1);
-  f2 = fmaf(__ldg(cf + 82 * C), x[7]*x[9]*x[10], f2);
-  f3 = fmaf(__ldg(cf + 83 * C), x[7]*x[10]*x[11], f3);
-  f0 = fmaf(__ldg(cf + 84 * C), x[7]*x[12]*x[13], f0);
-  f1 = fmaf(__ldg(cf + 85 * C), x[7]*x[12]*x[15], f1);
-  f2 = fmaf(__ldg(cf + 86 * C), x[7]*x[13]*x[14], f2);
-  f3 = fmaf(__ldg(cf + 87 * C), x[7]*x[14]*x[15], f3);
-  f0 = fmaf(__ldg(cf + 88 * C), x[8]*x[8]*x[8], f0);
-  f1 = fmaf(__ldg(cf + 89 * C), x[8]*x[9]*x[9], f1);
-  f2 = fmaf(__ldg(cf + 90 * C), x[8]*x[9]*x[11], f2);
-  f3 = fmaf(__ldg(cf + 91 * C), x[8]*x[10]*x[10], f3);
-  f0 = fmaf(__ldg(cf + 92 * C), x[8]*x[11]*x[11], f0);
-  f1 = fmaf(__ldg(cf + 93 * C), x[8]*x[12]*x[12], f1);
-  f2 = fmaf(__ldg(cf + 94 * C), x[8]*x[13]*x[13], f2);
-  f3 = fmaf(__ldg(cf + 95 * C), x[8]*x[13]*x[15], f3);
-  f0 = fmaf(__ldg(cf + 96 * C), x[8]*x[14]*x[14], f0);
-  f1 = fmaf(__ldg(cf + 97 * C), x[8]*x[15]*x[15], f1);
-  return (f0 + f1) + (f2 + f3);
+  float f = 0.0f;
+  f = fmaf(__ldg(cf + 0 * C), x[8], f);
+  f = fmaf(__ldg(cf + 1 * C), x[0]*x[8], f);
+  f = fmaf(__ldg(cf + 2 * C), x[1]*x[1], f);
+  f = fmaf(__ldg(cf + 3 * C), x[1]*x[9], f);
+  f = fmaf(__ldg(cf + 4 * C), x[1]*x[11], f);
+  f = fmaf(__ldg(cf + 5 * C), x[2]*x[14], f);
+  f = fmaf(__ldg(cf + 6 * C), x[3]*x[3], f);
+  f = fmaf(__ldg(cf + 7 * C), x[3]*x[13], f);
+  f = fmaf(__ldg(cf + 8 * C), x[3]*x[15], f);
+  f = fmaf(__ldg(cf + 9 * C), x[5]*x[5], f);
+  f = fmaf(__ldg(cf + 10 * C), x[6]*x[8], f);
+  f = fmaf(__ldg(cf + 11 * C), x[7]*x[7], f);
+  f = fmaf(__ldg(cf + 12 * C), x[9]*x[11], f);
+  f = fmaf(__ldg(cf + 13 * C), x[11]*x[11], f);
+  f = fmaf(__ldg(cf + 14 * C), x[12]*x[14], f);
+  f = fmaf(__ldg(cf + 15 * C), x[13]*x[13], f);
+  f = fmaf(__ldg(cf + 16 * C), x[13]*x[15], f);
+  f = fmaf(__ldg(cf + 17 * C), x[0]*x[0]*x[8], f);
+  f = fmaf(__ldg(cf + 18 * C), x[0]*x[1]*x[1], f);
+  f = fmaf(__ldg(cf + 19 * C), x[0]*x[1]*x[9], f);
+  f = fmaf(__ldg(cf + 20 * C), x[0]*x[1]*x[11], f);
+  f = fmaf(__ldg(cf + 21 * C), x[0]*x[2]*x[14], f);
+  f = fmaf(__ldg(cf + 22 * C), x[0]*x[3]*x[3], f);
+  f = fmaf(__ldg(cf + 23 * C), x[0]*x[3]*x[13], f);
+  f = fmaf(__ldg(cf + 24 * C), x[0]*x[3]*x[15], f);
+  f = fmaf(__ldg(cf + 25 * C), x[0]*x[5]*x[5], f);
+  f = fmaf(__ldg(cf + 26 * C), x[0]*x[6]*x[8], f);
+  f = fmaf(__ldg(cf + 27 * C), x[0]*x[7]*x[7], f);
+  f = fmaf(__ldg(cf + 28 * C), x[0]*x[9]*x[11], f);
+  f = fmaf(__ldg(cf + 29 * C), x[0]*x[11]*x[11], f);
+  f = fmaf(__ldg(cf + 30 * C), x[0]*x[12]*x[14], f);
+  f = fmaf(__ldg(cf + 31 * C), x[0]*x[13]*x[13], f);
+  f = fmaf(__ldg(cf + 32 * C), x[0]*x[13]*x[15], f);
+  f = fmaf(__ldg(cf + 33 * C), x[1]*x[1]*x[6], f);
+  f = fmaf(__ldg(cf + 34 * C), x[1]*x[1]*x[8], f);
+  f = fmaf(__ldg(cf + 35 * C), x[1]*x[2]*x[5], f);
+  f = fmaf(__ldg(cf + 36 * C), x[1]*x[4]*x[13], f);
+  f = fmaf(__ldg(cf + 37 * C), x[1]*x[4]*x[15], f);
+  f = fmaf(__ldg(cf + 38 * C), x[1]*x[5]*x[12], f);
+  f = fmaf(__ldg(cf + 39 * C), x[1]*x[5]*x[14], f);
+  f = fmaf(__ldg(cf + 40 * C), x[1]*x[6]*x[9], f);
+  f = fmaf(__ldg(cf + 41 * C), x[1]*x[6]*x[11], f);
+  f = fmaf(__ldg(cf + 42 * C), x[1]*x[7]*x[10], f);
+  f = fmaf(__ldg(cf + 43 * C), x[1]*x[8]*x[9], f);
+  f = fmaf(__ldg(cf + 44 * C), x[1]*x[8]*x[11], f);
+  f = fmaf(__ldg(cf + 45 * C), x[2]*x[2]*x[8], f);
+  f = fmaf(__ldg(cf + 46 * C), x[2]*x[3]*x[7], f);
+  f = fmaf(__ldg(cf + 47 * C), x[2]*x[5]*x[9], f);
+  f = fmaf(__ldg(cf + 48 * C), x[2]*x[5]*x[11], f);
+  f = fmaf(__ldg(cf + 49 * C), x[2]*x[6]*x[14], f);
+  f = fmaf(__ldg(cf + 50 * C), x[2]*x[7]*x[13], f);
+  f = fmaf(__ldg(cf + 51 * C), x[2]*x[7]*x[15], f);
+  f = fmaf(__ldg(cf + 52 * C), x[2]*x[8]*x[12], f);
+  f = fmaf(__ldg(cf + 53 * C), x[3]*x[3]*x[6], f);
+  f = fmaf(__ldg(cf + 54 * C), x[3]*x[3]*x[8], f);
+  f = fmaf(__ldg(cf + 55 * C), x[3]*x[4]*x[9], f);
+  f = fmaf(__ldg(cf + 56 * C), x[3]*x[4]*x[11], f);
+  f = fmaf(__ldg(cf + 57 * C), x[3]*x[5]*x[10], f);
+  f = fmaf(__ldg(cf + 58 * C), x[3]*x[6]*x[13], f);
+  f = fmaf(__ldg(cf + 59 * C), x[3]*x[6]*x[15], f);
+  f = fmaf(__ldg(cf + 60 * C), x[3]*x[7]*x[12], f);
+  f = fmaf(__ldg(cf + 61 * C), x[3]*x[7]*x[14], f);
+  f = fmaf(__ldg(cf + 62 * C), x[3]*x[8]*x[13], f);
+  f = fmaf(__ldg(cf + 63 * C), x[3]*x[8]*x[15], f);
+  f = fmaf(__ldg(cf + 64 * C), x[4]*x[4]*x[8], f);
+  f = fmaf(__ldg(cf + 65 * C), x[4]*x[9]*x[13], f);
+  f = fmaf(__ldg(cf + 66 * C), x[4]*x[10]*x[14], f);
+  f = fmaf(__ldg(cf + 67 * C), x[4]*x[11]*x[15], f);
+  f = fmaf(__ldg(cf + 68 * C), x[5]*x[5]*x[8], f);
+  f = fmaf(__ldg(cf + 69 * C), x[5]*x[9]*x[12], f);
+  f = fmaf(__ldg(cf + 70 * C), x[5]*x[9]*x[14], f);
+  f = fmaf(__ldg(cf + 71 * C), x[5]*x[10]*x[13], f);
+  f = fmaf(__ldg(cf + 72 * C), x[5]*x[10]*x[15], f);
+  f = fmaf(__ldg(cf + 73 * C), x[5]*x[11]*x[12], f);
+  f = fmaf(__ldg(cf + 74 * C), x[5]*x[11]*x[14], f);
+  f = fmaf(__ldg(cf + 75 * C), x[6]*x[6]*x[8], f);
+  f = fmaf(__ldg(cf + 76 * C), x[6]*x[9]*x[11], f);
+  f = fmaf(__ldg(cf + 77 * C), x[6]*x[11]*x[11], f);
+  f = fmaf(__ldg(cf + 78 * C), x[6]*x[12]*x[14], f);
+  f = fmaf(__ldg(cf + 79 * C), x[6]*x[13]*x[13], f);
+  f = fmaf(__ldg(cf + 80 * C), x[6]*x[13]*x[15], f);
+  f = fmaf(__ldg(cf + 81 * C), x[7]*x[7]*x[8], f);
+  f = fmaf(__ldg(cf + 82 * C), x[7]*x[9]*x[10], f);
+  f = fmaf(__ldg(cf + 83 * C), x[7]*x[10]*x[11], f);
+  f = fmaf(__ldg(cf + 84 * C), x[7]*x[12]*x[13], f);
+  f = fmaf(__ldg(cf + 85 * C), x[7]*x[12]*x[15], f);
+  f = fmaf(__ldg(cf + 86 * C), x[7]*x[13]*x[14], f);
+  f = fmaf(__ldg(cf + 87 * C), x[7]*x[14]*x[15], f);
+  f = fmaf(__ldg(cf + 88 * C), x[8]*x[8]*x[8], f);
+  f = fmaf(__ldg(cf + 89 * C), x[8]*x[9]*x[9], f);
+  f = fmaf(__ldg(cf + 90 * C), x[8]*x[9]*x[11], f);
+  f = fmaf(__ldg(cf + 91 * C), x[8]*x[10]*x[10], f);
+  f = fmaf(__ldg(cf + 92 * C), x[8]*x[11]*x[11], f);
+  f = fmaf(__ldg(cf + 93 * C), x[8]*x[12]*x[12], f);
+  f = fmaf(__ldg(cf + 94 * C), x[8]*x[13]*x[13], f);
+  f = fmaf(__ldg(cf + 95 * C), x[8]*x[13]*x[15], f);
+  f = fmaf(__ldg(cf + 96 * C), x[8]*x[14]*x[14], f);
+  f = fmaf(__ldg(cf + 97 * C), x[8]*x[15]*x[15], f);
+  return f;
 }
 
 __device__ __forceinline__ void grad_LM8(const float* x, float w, const float* __restrict__ cf, int C, float* g) {

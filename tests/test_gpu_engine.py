@@ -406,3 +406,25 @@ def test_cg_table_forms_agree(engine_lib, tmp_path, L_max):
     m.compute_node_energies_forces(*edge_args(species, nl))
     assert _report("E_i", m.node_energies, e_pad) < 1e-5 * max(1.0, np.abs(e_pad).max())
     assert _report("f_edge", m.node_forces, f_pad) < 1e-5 * max(1.0, np.abs(f_pad).max())
+
+
+@pytest.mark.parametrize("C,L_max", [(96, 1), (256, 1), (96, 2), (160, 1)])
+def test_channel_widths(engine_lib, tmp_path, C, L_max):
+    """Channel counts off the compile-time specialisations (96, 160: the generic kernels;
+    96 at L_max = 2: a partly filled second channel slice) and the widest (256), both
+    forms, against the oracle."""
+    path = write_model(make_model(num_channels=C, species=("H", "C", "O"), r_cut=5.0, L_max=L_max, num_knots=40,
+                                  seed=13), str(tmp_path / "m.json"))
+    pos, L, species = random_box(48, 0.07, 0.9, 3, seed=15)
+    nl = neighbor_list(pos, 5.0, L)
+    ref = Evaluator(path, "port")
+    ref.compute_node_energies_forces(*edge_args(species, nl))
+    Fr = atomic_forces(48, nl["i"], nl["neigh_indices"], ref.node_forces)
+    scale = max(1.0, np.abs(Fr).max())
+    for precision, tol in (("float32", F_TOL), ("bfloat16", 1e-3 * scale)):
+        m = _engine(path, precision=precision)
+        m.compute_node_energies_forces(*edge_args(species, nl))
+        F = atomic_forces(48, nl["i"], nl["neigh_indices"], m.node_forces)
+        assert _report(f"C={C} {precision} E_i", m.node_energies, ref.node_energies) < (
+            E_TOL if precision == "float32" else 1e-3 * max(1.0, np.abs(ref.node_energies).max()))
+        assert _report(f"C={C} {precision} F", F, Fr) < max(tol, F_TOL)

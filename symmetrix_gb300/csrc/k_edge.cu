@@ -45,7 +45,7 @@ namespace {
 template <bool GRAD>
 struct L0Stage {
   float2 Y2[kEdgeChunk][16];  // (Y_lm, Y_lm): operand of the packed FMAs
-  float4 G[GRAD ? kEdgeChunk : 1][16];  // (dY_lm/dx, dY_lm/dy, dY_lm/dz, 0)
+  float4 G[GRAD ? kEdgeChunk : 1][16];  // (dY_lm/dx, dY_lm/dy, dY_lm/dz, Y_lm): one load per lm
   float4 u[GRAD ? kEdgeChunk : 1];
   float x[kEdgeChunk];
   int row[kEdgeChunk];  // (ti * S + tj) * nint + interval, or -1
@@ -71,7 +71,7 @@ __device__ __forceinline__ void stage_l0(const DevModel& m, const EdgeIn& in, in
     for (int q = 0; q < 16; ++q) st.Y2[t][q] = make_float2(Y[q], Y[q]);
     if constexpr (GRAD) {
 #pragma unroll
-      for (int c = 0; c < 16; ++c) st.G[t][c] = make_float4(G[c], G[16 + c], G[32 + c], 0.0f);
+      for (int c = 0; c < 16; ++c) st.G[t][c] = make_float4(G[c], G[16 + c], G[32 + c], Y[c]);
       const float inv = 1.0f / rr;
       st.u[t] = make_float4(vx * inv, vy * inv, vz * inv, 0.0f);
     }
@@ -355,10 +355,10 @@ __device__ __forceinline__ void layer0_rev_atom(const DevModel& m, const EdgeIn&
         float2 dRl = make_float2(0.0f, 0.0f);
 #pragma unroll
         for (int q = l * l; q < (l + 1) * (l + 1); ++q) {
-          dRl = fma2(dA[q], st.Y2[t][q], dRl);
+          const float4 g = st.G[t][q];  // (dY/dx, dY/dy, dY/dz, Y)
+          dRl = fma2(dA[q], make_float2(g.w, g.w), dRl);
           const float2 w = mul2(dA[q], R[l]);
           const float s = w.x + w.y;
-          const float4 g = st.G[t][q];
           fx = fmaf(s, g.x, fx);
           fy = fmaf(s, g.y, fy);
           fz = fmaf(s, g.z, fz);

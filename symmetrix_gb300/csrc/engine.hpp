@@ -484,7 +484,6 @@ struct smx_engine {
   int l2_split_max = 1;
   int sched_force = -1;  // -1: tune; 0: one block per atom; 1: persistent
   bool sched_tuned = false;
-  float sched_stage_us[2][kStages] = {};
 
   void sched_set(int mode) {
     for (int k = 0; k < smx::kAkCount; ++k) dm.pgrid[k] = mode ? pfull[k] : 0;
@@ -525,8 +524,6 @@ struct smx_engine {
       const int q = kStageOf[k];
       dm.pgrid[k] = best[1][q] < best[0][q] ? pfull[k] : 0;
     }
-    for (int mode = 0; mode < 2; ++mode)
-      for (int q = 0; q < kStages; ++q) sched_stage_us[mode][q] = best[mode][q] * 1000.0f;
     if (l2_split_max > 1) {  // channel slices of the L_max = 2 layer-1 kernels: stages 2 and 6
       float t[3] = {1e30f, 1e30f, 1e30f};
       for (int rep = 0; rep < 2; ++rep)

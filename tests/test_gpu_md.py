@@ -97,3 +97,24 @@ def test_md_conserves_energy(engine_lib, small_model_path):
     drift = (max(tot) - min(tot)) / 256
     print(f"NVE: total energy range per atom over 50 steps of 0.1 fs = {drift:.3e} eV")
     assert drift < 1e-4
+
+
+@pytest.mark.parametrize("precision", ["float32", "bfloat16"])
+def test_gpu_forces_are_energy_gradients(engine_lib, small_model_path, precision):
+    """The reference's finite-difference check (symmetrix/test/test_mace.py:655-704) on the
+    GPU path: central differences of the GPU energy match the GPU forces (tolerance from
+    the float32 energy rounding over the step)."""
+    from symmetrix_gb300 import MACE
+    rng = np.random.default_rng(21)
+    pos = rng.normal(size=(20, 3)) * 1.8
+    species = rng.integers(0, 3, size=20).astype(np.int32)
+    m = MACE(small_model_path, precision=precision)
+    e0, _, F, _ = m.compute_atoms(pos, species)
+    h = 5e-3
+    for a in (0, 7, 13):
+        for c in range(3):
+            p, q = pos.copy(), pos.copy()
+            p[a, c] += h
+            q[a, c] -= h
+            fd = -(m.compute_atoms(p, species)[0] - m.compute_atoms(q, species)[0]) / (2 * h)
+            assert abs(fd - F[a, c]) < 5e-3 * max(1.0, abs(F[a, c])), (a, c, fd, F[a, c])

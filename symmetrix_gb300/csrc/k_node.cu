@@ -161,7 +161,7 @@ __device__ __forceinline__ void node_tail_atom(const DevModel& m, const int* __r
   const float* W = m.H2W_H1 + static_cast<size_t>(ti) * C * C + k;
   const float* WM = m.H2W_M1 + k;
   float hp0 = 0.0f, hp1 = 0.0f, hp2 = 0.0f, hp3 = 0.0f;  // C is a multiple of 32
-#pragma unroll 2
+#pragma unroll 4
   for (int r = 0; r < C; r += 4) {
     const size_t o = static_cast<size_t>(r) * C;
     hp0 = fmaf(sM1[r], __ldg(WM + o), fmaf(sH10[r], __ldg(W + o), hp0));
@@ -208,7 +208,7 @@ __device__ __forceinline__ void node_tail_atom(const DevModel& m, const int* __r
   const float* WT = m.H2W_H1_T + static_cast<size_t>(ti) * C * C + k;
   const float* WMT = m.H2W_M1_T + k;
   float ha0 = 0.0f, ha1 = 0.0f, ma0 = 0.0f, ma1 = 0.0f;
-#pragma unroll 4
+#pragma unroll 8
   for (int c = 0; c < C; c += 2) {
     const size_t o = static_cast<size_t>(c) * C;
     const float d0 = sdH2[c], d1 = sdH2[c + 1];

@@ -231,6 +231,25 @@ __device__ __forceinline__ void l1_load_g(const float* sP, const Lane2& L, float
   });
 }
 
+// g_p for this thread's channel pair straight from the node's staged dPhi1 rows (sD,
+// [n_lme][C]) through the two-term padded CG table
+template <int LMAX, int H>
+__device__ __forceinline__ void l1_load_g_sd(const DevModel& m, const float* sD, const Lane2& L, float2* g) {
+  static_for<half_count(H)>([&](auto ic) {
+    constexpr int i = decltype(ic)::value;
+    constexpr int q = half_ins(H, i);
+    constexpr int np = ins_paths(LMAX, q), p0 = ins_poff(LMAX, q), g0 = half_goff<LMAX, H>(i);
+#pragma unroll
+    for (int p = 0; p < np; ++p) {
+      const int2 t0 = __ldg(m.cg_rev_pad + 2 * (p0 + p)), t1 = __ldg(m.cg_rev_pad + 2 * (p0 + p) + 1);
+      const float2 d0 = *reinterpret_cast<const float2*>(sD + t0.x * L.C + L.kc);
+      const float2 d1 = *reinterpret_cast<const float2*>(sD + t1.x * L.C + L.kc);
+      const float v0 = __int_as_float(t0.y), v1 = __int_as_float(t1.y);
+      g[g0 + p] = make_float2(fmaf(v1, d1.x, v0 * d0.x), fmaf(v1, d1.y, v0 * d0.y));
+    }
+  });
+}
+
 // ---------------------------------------------------------------------------
 // Adjoint, one edge, half H.  With g_p = sum_lme CG[lme,p] dPhi1[i,lme,k]:
 //   dE/dx_ij += sum_k sum_p g_p h_{m2} (R1'_q u Y_{m1} + R1_q dY_{m1}/dx)
@@ -440,18 +459,14 @@ __device__ __forceinline__ void layer1_rev_atom(const DevModel& m, const EdgeIn&
   const int nwarp = blockDim.x >> 5;
   const int ti = in.node_type[i];
   const int e0 = in.first[i], e1 = in.end(i);
-  // sP[p][k] = sum_lme CG[lme,p] dPhi1[i,lme,k], one channel per thread
+  // g_p = sum_lme CG[lme,p] dPhi1[i,lme,k]: the node's dPhi1 rows staged in shared
+  // memory, then (padded table) each thread gathers its channel pair's g from them, or
+  // (compressed rows) sP[p][k] is formed first, one channel per thread
   float* sD = dyn;                // [n_lme][C]
   float* sP = dyn + m.n_lme * C;  // [NP][C]
   for (int k = threadIdx.x; k < C; k += blockDim.x) {
     for (int lme = 0; lme < m.n_lme; ++lme) sD[lme * C + k] = dPhi1[(static_cast<size_t>(i) * m.n_lme + lme) * C + k];
-    if (m.cg_rev_pad) {  // two terms per path: eight paths' loads in flight at a time
-#pragma unroll 8
-      for (int p = 0; p < NP; ++p) {
-        const int2 t0 = __ldg(m.cg_rev_pad + 2 * p), t1 = __ldg(m.cg_rev_pad + 2 * p + 1);
-        sP[p * C + k] = fmaf(__int_as_float(t1.y), sD[t1.x * C + k], __int_as_float(t0.y) * sD[t0.x * C + k]);
-      }
-    } else {  // any number of terms: a chain of dependent loads per path
+    if (!m.cg_rev_pad) {  // any number of terms: sP through a chain of dependent loads per path
       for (int p = 0; p < NP; ++p) {
         float s = 0.0f;
         const int q1 = __ldg(m.cg_rev_off + p + 1);
@@ -463,10 +478,16 @@ __device__ __forceinline__ void layer1_rev_atom(const DevModel& m, const EdgeIn&
   }
   __syncthreads();
   float2 g[NG];
-  if (half == 0)
+  if (m.cg_rev_pad) {
+    if (half == 0)
+      l1_load_g_sd<LMAX, 0>(m, sD, L, g);
+    else
+      l1_load_g_sd<LMAX, 1>(m, sD, L, g);
+  } else if (half == 0) {
     l1_load_g<LMAX, 0>(sP, L, g);
-  else
+  } else {
     l1_load_g<LMAX, 1>(sP, L, g);
+  }
   for (int eb = e0; eb < e1; eb += kEdgeChunk) {
     const int ne = min(kEdgeChunk, e1 - eb);
     __syncthreads();

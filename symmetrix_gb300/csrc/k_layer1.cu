@@ -628,6 +628,22 @@ __device__ __forceinline__ void l2_load_g(const float* sP, int C, int k, float* 
   });
 }
 
+// g of group G for channel kk straight from the staged dPhi1 rows sD ([n_lme][stride])
+// through the two-term padded CG table
+template <int G>
+__device__ __forceinline__ void l2_load_g_sd(const DevModel& m, const float* sD, int stride, int kk, float* g) {
+  static_for<l2_count(G)>([&](auto ic) {
+    constexpr int i = decltype(ic)::value;
+    constexpr int q = l2_ins(G, i);
+    constexpr int np = ins_paths(2, q), p0 = ins_poff(2, q), g0 = l2_goff<G>(i);
+#pragma unroll
+    for (int p = 0; p < np; ++p) {
+      const int2 t0 = __ldg(m.cg_rev_pad + 2 * (p0 + p)), t1 = __ldg(m.cg_rev_pad + 2 * (p0 + p) + 1);
+      g[g0 + p] = fmaf(__int_as_float(t1.y), sD[t1.x * stride + kk], __int_as_float(t0.y) * sD[t0.x * stride + kk]);
+    }
+  });
+}
+
 }  // namespace
 
 // Layer-1 forward, L_max = 2: slice h of the channels of node i (channels h*CH ..
@@ -788,19 +804,22 @@ __device__ __forceinline__ void layer1_rev_l2_atom(const DevModel& m, const Edge
   const int e0 = in.first[i], e1 = in.end(i);
   float* sD = dyn;                  // [n_lme][CH]
   float* sP = dyn + m.n_lme * CH;   // [NP][CH]
-  // sP[p][k] = sum_lme CG[lme,p] dPhi1[i,lme,k]: rows split over the four groups
+  // g_p = sum_lme CG[lme,p] dPhi1[i,lme,k] from the node's staged dPhi1 rows (staging
+  // split over the four groups)
   if (live)
     for (int lme = grp; lme < m.n_lme; lme += kL2Groups)
       sD[lme * CH + kk] = dPhi1[(static_cast<size_t>(i) * m.n_lme + lme) * C + k];
   __syncthreads();
-  if (live) {
-    if (m.cg_rev_pad) {  // two terms per path: several paths' loads in flight
-#pragma unroll 4
-      for (int p = grp; p < NP; p += kL2Groups) {
-        const int2 t0 = __ldg(m.cg_rev_pad + 2 * p), t1 = __ldg(m.cg_rev_pad + 2 * p + 1);
-        sP[p * CH + kk] = fmaf(__int_as_float(t1.y), sD[t1.x * CH + kk], __int_as_float(t0.y) * sD[t0.x * CH + kk]);
-      }
-    } else {
+  float g[kL2MaxNp];
+  if (m.cg_rev_pad) {  // each thread gathers its group's g from the staged rows
+    switch (grp) {
+      case 0: l2_load_g_sd<0>(m, sD, CH, kk, g); break;
+      case 1: l2_load_g_sd<1>(m, sD, CH, kk, g); break;
+      case 2: l2_load_g_sd<2>(m, sD, CH, kk, g); break;
+      default: l2_load_g_sd<3>(m, sD, CH, kk, g); break;
+    }
+  } else {  // sP first, rows split over the four groups, through the compressed rows
+    if (live)
       for (int p = grp; p < NP; p += kL2Groups) {
         float sum = 0.0f;
         const int q1 = __ldg(m.cg_rev_off + p + 1);
@@ -808,15 +827,13 @@ __device__ __forceinline__ void layer1_rev_l2_atom(const DevModel& m, const Edge
           sum = fmaf(__ldg(m.cg_rev_v + q), sD[__ldg(m.cg_rev_lme + q) * CH + kk], sum);
         sP[p * CH + kk] = sum;
       }
+    __syncthreads();
+    switch (grp) {
+      case 0: l2_load_g<0>(sP, CH, kk, g); break;
+      case 1: l2_load_g<1>(sP, CH, kk, g); break;
+      case 2: l2_load_g<2>(sP, CH, kk, g); break;
+      default: l2_load_g<3>(sP, CH, kk, g); break;
     }
-  }
-  __syncthreads();
-  float g[kL2MaxNp];
-  switch (grp) {
-    case 0: l2_load_g<0>(sP, CH, kk, g); break;
-    case 1: l2_load_g<1>(sP, CH, kk, g); break;
-    case 2: l2_load_g<2>(sP, CH, kk, g); break;
-    default: l2_load_g<3>(sP, CH, kk, g); break;
   }
   double* f1h = f1 + h * m.f1_stride;
   for (int eb = e0; eb < e1; eb += kEdgeChunk) {

@@ -180,14 +180,15 @@ __global__ void k_wrap(int N, double3 box, int3 periodic, double* __restrict__ p
 }
 
 // rev[e] = index of the reverse edge (j -> i, -shift) of e = (i -> j, shift); -1 if absent.
-// One warp per centre atom i: for each of its edges the lanes scan j's list 32 entries at
-// a time (the first match in list order, as a sequential scan would find).
+// One block per centre atom i, its warps taking every fourth edge: for each edge the
+// lanes scan j's list 32 entries at a time (the first match in list order, as a
+// sequential scan would find).
 __global__ void k_reverse_edges(int N, const int* __restrict__ first, const int* __restrict__ nidx,
                                 const char4* __restrict__ shift, int* __restrict__ rev) {
-  const int i = static_cast<int>((static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
-  const int lane = threadIdx.x & 31;
+  const int i = blockIdx.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   if (i >= N) return;
-  for (int e = first[i]; e < first[i + 1]; ++e) {
+  for (int e = first[i] + warp; e < first[i + 1]; e += nwarp) {
     const int j = nidx[e];
     const char4 sh = shift[e];
     const int w1 = first[j + 1];
@@ -406,7 +407,7 @@ void launch_wrap(int N, double3 box, int3 periodic, double* pos, cudaStream_t s)
 
 void launch_reverse_edges(long cap, int N, const int* first, const int* nidx, const int* edge_i, const char4* shift,
                           int* rev, cudaStream_t s) {
-  if (cap > 0 && N > 0) k_reverse_edges<<<ceil_div(N, 4), 128, 0, s>>>(N, first, nidx, shift, rev);  // warp per atom
+  if (cap > 0 && N > 0) k_reverse_edges<<<N, 128, 0, s>>>(N, first, nidx, shift, rev);  // block per atom
 }
 
 void launch_edge_geometry(long cap, int N, const int* first, const double* pos, double3 box, const int* nidx,

@@ -100,11 +100,16 @@ int smx_compute_node_energies_forces_device(smx_engine* eng, int num_nodes, cons
 
 /* Copies the last call's stage buffer `name` (A0, M0, H1, Phi1, A1, M1, H2, A0_adj,
  * M0_adj, H1_adj, Phi1_adj, A1_adj, M1_adj, H2_adj; reference layouts, see
- * libsymmetrix/source/mace.hpp) as float64.  Returns its length, -1 for an unknown
- * name.  A0_adj is kept only after smx_set_option(eng, "keep_stages", 1). */
+ * libsymmetrix/source/mace.hpp) as float64, after waiting for the device.  Returns its
+ * length (0 after an empty evaluation); -1 for an unknown name; -2 when the stage is
+ * not available: no evaluation has run yet, or the BF16 form skipped the float32 rows
+ * of M0, Phi1 or A1_adj (its tensor-core GEMMs read bf16 split rows instead), which it
+ * writes only after smx_set_option(eng, "keep_stages", 1); -3 on a CUDA error.
+ * smx_last_error() says which. */
 long smx_get_stage(smx_engine* eng, const char* name, double* out, long cap);
 
-/* Options: "keep_stages" (keep A0_adj for smx_get_stage), "profile" (record CUDA
+/* Options: "keep_stages" (the BF16 form also writes the float32 M0, Phi1 and A1_adj
+ * rows for smx_get_stage), "profile" (record CUDA
  * events between the kernels of every evaluation); "autotune" (1, the default: the
  * first evaluation outside a stream capture picks, per per-atom kernel, one block per
  * atom or a persistent grid of resident blocks claiming atoms from a counter, and for

@@ -287,15 +287,19 @@ int smx_stage_times(smx_engine* eng, double* out_ms, int cap) {
 }
 
 long smx_get_stage(smx_engine* eng, const char* name, double* out, long cap) {
-  if (!eng || !name) return -1;
+  if (!eng || !name) {
+    fail(SMX_ERR_INVALID, "NULL argument");
+    return -1;
+  }
   const long N = eng->lastN, C = eng->dm.C;
   const float* src = nullptr;
+  bool kept = true;
   long n = 0;
   const std::string s(name);
   if (s == "A0") { src = eng->A0; n = N * 16 * C; }
-  else if (s == "M0") { src = eng->M0; n = N * eng->dm.nLM * C; }
+  else if (s == "M0") { src = eng->M0; n = N * eng->dm.nLM * C; kept = eng->M0_kept; }
   else if (s == "H1") { src = eng->H1; n = N * eng->dm.nLM * C; }
-  else if (s == "Phi1") { src = eng->Phi1; n = N * eng->dm.n_lme * C; }
+  else if (s == "Phi1") { src = eng->Phi1; n = N * eng->dm.n_lme * C; kept = eng->Phi1_kept; }
   else if (s == "A1") { src = eng->A1; n = N * 16 * C; }
   else if (s == "M1") { src = eng->M1; n = N * C; }
   else if (s == "H2") { src = eng->H2; n = N * C; }
@@ -303,16 +307,32 @@ long smx_get_stage(smx_engine* eng, const char* name, double* out, long cap) {
   else if (s == "M0_adj") { src = eng->M0_adj; n = N * eng->dm.nLM * C; }
   else if (s == "H1_adj") { src = eng->H1_adj; n = N * eng->dm.nLM * C; }
   else if (s == "Phi1_adj") { src = eng->Phi1_adj; n = N * eng->dm.n_lme * C; }
-  else if (s == "A1_adj") { src = eng->A1_adj; n = N * 16 * C; }
+  else if (s == "A1_adj") { src = eng->A1_adj; n = N * 16 * C; kept = eng->A1adj_kept; }
   else if (s == "M1_adj") { src = eng->M1_adj; n = N * C; }
   else if (s == "H2_adj") { src = eng->H2_adj; n = N * C; }
-  else return -1;
-  if (!src) return fail(SMX_ERR_INVALID, "stage not kept (set keep_stages)") ? -1 : -1;
-  if (out && cap > 0 && n > 0) {
+  else {
+    fail(SMX_ERR_INVALID, std::string("unknown stage '") + name + "'");
+    return -1;
+  }
+  if (!eng->evaluated) {
+    fail(SMX_ERR_INVALID, "no evaluation has run since the engine's buffers were (re)allocated");
+    return -2;
+  }
+  if (n == 0) return 0;
+  if (!src || !kept) {
+    fail(SMX_ERR_INVALID, "stage " + s + " was not written by the last evaluation (set keep_stages)");
+    return -2;
+  }
+  if (out && cap > 0) {
     std::vector<float> tmp(static_cast<size_t>(n));
-    cudaSetDevice(eng->device);
-    cudaStreamSynchronize(eng->stream);
-    if (cudaMemcpy(tmp.data(), src, sizeof(float) * n, cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+    try {
+      check(cudaSetDevice(eng->device), "cudaSetDevice");
+      check(cudaDeviceSynchronize(), "cudaDeviceSynchronize");  // the last call may have run on a caller's stream
+      check(cudaMemcpy(tmp.data(), src, sizeof(float) * n, cudaMemcpyDeviceToHost), "D2H");
+    } catch (const std::exception& e) {
+      fail(SMX_ERR_CUDA, e.what());
+      return -3;
+    }
     for (long q = 0; q < n && q < cap; ++q) out[q] = tmp[q];
   }
   return n;

@@ -90,6 +90,8 @@ struct smx_engine {
   int* nneigh = nullptr;      // num_neigh of the host-pointer call
   double *xyz = nullptr, *r = nullptr, *energies = nullptr, *forces = nullptr;
   int lastN = 0;
+  bool evaluated = false;          // the workspace holds the stages of an evaluation
+  bool M0_kept = false, Phi1_kept = false, A1adj_kept = false;  // float32 rows written by it
 
   // B operand of a tensor-core GEMM from a row-major float [nrows][K] matrix: row n
   // holds (W_hi), (W_hi | W_lo) or (W_hi | W_hi | W_lo) for 1, 2, 3 terms,
@@ -300,6 +302,7 @@ struct smx_engine {
     first = ntype = nidx = ntype_e = atom_order = nneigh = nullptr;
     xyz = r = energies = forces = nullptr;
     capN = capE = 0;
+    evaluated = false;
   }
 
   void reserve(long N, long E) {
@@ -580,7 +583,10 @@ struct smx_engine {
     const int C = dm.C;
     const int T = tc_terms;
     lastN = N;
-    if (N == 0) return;
+    if (N == 0) {
+      evaluated = true;
+      return;
+    }
     if (profile && !ev[0])
       for (auto& e : ev) check(cudaEventCreate(&e), "cudaEventCreate");
     prof_stream = s;
@@ -597,6 +603,10 @@ struct smx_engine {
     float* M0_out = (f32_rows || !tc_H1) ? M0 : nullptr;
     float* Phi1_out = (f32_rows || !all_A1) ? Phi1 : nullptr;
     float* A1adj_out = (f32_rows || !all_Phi1adj) ? A1_adj : nullptr;
+    M0_kept = M0_out != nullptr;
+    Phi1_kept = Phi1_out != nullptr;
+    A1adj_kept = A1adj_out != nullptr;
+    evaluated = true;
     smx::launch_layer0_fwd(dm, in, A0, M0_out, dm.has_zbl ? zbl_e : nullptr, s);
     mark(1, s);
     if (tc_H1) {  // H1 = M0 @ H1W[L]  (mace.cpp:397-423), tensor cores

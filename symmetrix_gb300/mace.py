@@ -160,11 +160,15 @@ class MACE:
         return dict(zip(_lib.STAGE_NAMES, out[:n]))
 
     def stage(self, name):
+        """A stage buffer of the last evaluation as float64 (reference layout)."""
         n = self._lib.smx_get_stage(self._h, name.encode(), None, 0)
-        if n < 0:
+        if n == -1:
             raise KeyError(name)
+        if n < 0:
+            raise RuntimeError(self._lib.smx_last_error().decode(errors="replace"))
         out = np.zeros(n)
-        self._lib.smx_get_stage(self._h, name.encode(), _ptr(out), n)
+        if n > 0 and self._lib.smx_get_stage(self._h, name.encode(), _ptr(out), n) < 0:
+            raise RuntimeError(self._lib.smx_last_error().decode(errors="replace"))
         return out
 
     def __getattr__(self, name):

@@ -153,3 +153,31 @@ def test_autotuned_schedule_is_valid_and_exact(engine_lib, wide):
     assert np.array_equal(tuned.node_energies, plain.node_energies)
     # M0_adj's operand H1_adj is summed with float atomics in the layer-1 adjoint
     assert _rel(tuned.stage("M0_adj"), plain.stage("M0_adj")) < 1e-5
+
+
+def test_stage_rows_skipped_without_keep_stages(engine_lib, wide):
+    """The BF16 form writes no float32 M0 / Phi1 / A1_adj rows unless asked: reading
+    them then fails loudly instead of returning stale memory; the other stages and the
+    results do not depend on keep_stages."""
+    from symmetrix_gb300 import MACE
+    path, species, nl = wide
+    m = MACE(path, precision="bf16")
+    with pytest.raises(RuntimeError, match="no evaluation"):
+        m.stage("H1")
+    with pytest.raises(KeyError):
+        m.stage("no_such_stage")
+    m.compute_node_energies_forces(*edge_args(species, nl))
+    for s in ("M0", "Phi1", "A1_adj"):
+        with pytest.raises(RuntimeError, match="keep_stages"):
+            m.stage(s)
+    kept = _run(path, species, nl, "bf16")
+    for s in ("H1", "A1", "M1", "H2"):
+        assert np.array_equal(m.stage(s), kept.stage(s)), s
+    assert np.array_equal(m.node_energies, kept.node_energies)
+    # H1_adj, and what is computed from it, is summed with float atomics in the layer-1 adjoint
+    for s in ("H1_adj", "M0_adj", "A0_adj"):
+        assert _rel(m.stage(s), kept.stage(s)) < 1e-5, s
+    assert _rel(m.node_forces, kept.node_forces) < 1e-5
+    f32 = MACE(path, precision="fp32")
+    f32.compute_node_energies_forces(*edge_args(species, nl))
+    assert f32.stage("M0").size == len(species) * f32.num_LM * f32.num_channels

@@ -24,15 +24,26 @@ namespace {
 
 // Sum a per-thread 3-vector over the block's channels for edge t: float32 warp
 // shuffles (float64 arithmetic is slow on this part), then one partial per warp into
-// sF, summed across warps in float64 after the chunk.
+// sF, summed across warps in float64 after the chunk.  The lanes first trade halves of
+// the vector (x, y | z, 0) with their xor-1 and xor-2 partners, so each lane then holds
+// one component summed over its group of four lanes (lane & 3: 0 x, 1 z, 2 y, 3
+// nothing), and three butterfly steps sum the groups: six shuffles where three separate
+// warp sums take fifteen (k_layer0_rev 0.313 -> 0.283 ms on the 4096-atom workload).
+// The order of the additions is fixed, so results are reproducible.
 __device__ __forceinline__ void block_reduce3(float fx, float fy, float fz, float (*sF)[8][3], int t) {
-  const float x = warp_sum(fx), y = warp_sum(fy), z = warp_sum(fz);
-  if ((threadIdx.x & 31) == 0) {
-    const int w = threadIdx.x >> 5;
-    sF[t][w][0] = x;
-    sF[t][w][1] = y;
-    sF[t][w][2] = z;
-  }
+  constexpr unsigned kFull = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const bool b0 = lane & 1, b1 = lane & 2;
+  float k0 = b0 ? fz : fx, k1 = b0 ? 0.0f : fy;
+  const float s0 = b0 ? fx : fz, s1 = b0 ? fy : 0.0f;
+  k0 += __shfl_xor_sync(kFull, s0, 1);
+  k1 += __shfl_xor_sync(kFull, s1, 1);
+  float v = b1 ? k1 : k0;
+  v += __shfl_xor_sync(kFull, b1 ? k0 : k1, 2);
+  v += __shfl_xor_sync(kFull, v, 4);
+  v += __shfl_xor_sync(kFull, v, 8);
+  v += __shfl_xor_sync(kFull, v, 16);
+  if (lane < 3) sF[t][threadIdx.x >> 5][lane == 1 ? 2 : lane == 2 ? 1 : 0] = v;
 }
 
 }  // namespace

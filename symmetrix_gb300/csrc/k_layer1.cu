@@ -71,7 +71,9 @@ __host__ __device__ constexpr bool half_uses_y(int c) {
 }
 
 // Sum a per-thread 3-vector over the block for edge t (float32 shuffles; one
-// partial per warp into sF, summed across warps in float64 after the chunk).
+// partial per warp into sF, summed across warps in float64 after the chunk).  The
+// six-shuffle exchange form of k_edge.cu measured slower here (0.692 -> 0.709 ms on the
+// 4096-atom workload): three plain butterflies.
 __device__ __forceinline__ void block_reduce3(float fx, float fy, float fz, float (*sF)[8][3], int t) {
   const float x = warp_sum(fx), y = warp_sum(fy), z = warp_sum(fz);
   if ((threadIdx.x & 31) == 0) {

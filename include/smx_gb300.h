@@ -79,7 +79,7 @@ double smx_r_cut(const smx_engine* eng);
 int smx_l_max(const smx_engine* eng);
 int smx_L_max(const smx_engine* eng);
 int smx_num_LM(const smx_engine* eng);
-/* Copies up to cap atomic numbers; returns the number of species. */
+/* Copies up to cap atomic numbers (none when out is NULL); returns the number of species. */
 int smx_atomic_numbers(const smx_engine* eng, int* out, int cap);
 
 /* Host arrays in, host arrays out (node_energies[num_nodes], node_forces[3*num_edges]).

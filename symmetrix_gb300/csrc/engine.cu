@@ -114,7 +114,7 @@ int smx_L_max(const smx_engine* eng) { return eng ? eng->hm.L_max : -1; }
 int smx_num_LM(const smx_engine* eng) { return eng ? eng->hm.nLM : -1; }
 int smx_atomic_numbers(const smx_engine* eng, int* out, int cap) {
   if (!eng) return -1;
-  for (int q = 0; q < eng->hm.S && q < cap; ++q) out[q] = eng->hm.Z[q];
+  for (int q = 0; out && q < eng->hm.S && q < cap; ++q) out[q] = eng->hm.Z[q];
   return eng->hm.S;
 }
 

@@ -92,11 +92,18 @@ int smx_compute_node_energies_forces(smx_engine* eng, int num_nodes, const int* 
 /* Same, with every pointer in device memory of the engine's device; runs on
  * `stream` (a cudaStream_t, or NULL for the engine's own stream) and returns
  * without synchronising.  Inputs are not validated; edges with r >= r_cut
- * contribute nothing. */
+ * contribute nothing.  A bounded device-side wait that gave up is reported by
+ * the next smx_sync. */
 int smx_compute_node_energies_forces_device(smx_engine* eng, int num_nodes, const int* node_types,
                                             const int* num_neigh, const int* neigh_indices, const int* neigh_types,
                                             long num_edges, const double* xyz, const double* r,
                                             double* node_energies, double* node_forces, void* stream);
+
+/* Waits for `stream` (a cudaStream_t, or NULL for the engine's own stream) and
+ * returns SMX_ERR_TIMEOUT if a bounded device-side wait of the engine gave up since
+ * the last check (the results of that work are invalid), else SMX_OK.  The
+ * host-pointer calls and the MD sync/state calls make this check themselves. */
+int smx_sync(smx_engine* eng, void* stream);
 
 /* Copies the last call's stage buffer `name` (A0, M0, H1, Phi1, A1, M1, H2, A0_adj,
  * M0_adj, H1_adj, Phi1_adj, A1_adj, M1_adj, H2_adj; reference layouts, see

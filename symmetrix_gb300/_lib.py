@@ -32,6 +32,7 @@ SIGNATURES = [
     ("smx_atomic_numbers", _I, [_P, _P, _I]),
     ("smx_compute_node_energies_forces", _I, [_P, _I, _P, _P, _P, _P, _L, _P, _P, _P, _P]),
     ("smx_compute_node_energies_forces_device", _I, [_P, _I, _P, _P, _P, _P, _L, _P, _P, _P, _P, _P]),
+    ("smx_sync", _I, [_P, _P]),
     ("smx_get_stage", _L, [_P, _S, _P, _L]),
     ("smx_set_option", _I, [_P, _S, _L]),
     ("smx_get_option", _L, [_P, _S]),

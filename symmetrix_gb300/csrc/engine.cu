@@ -270,6 +270,18 @@ int smx_compute_node_energies_forces_device(smx_engine* eng, int num_nodes, cons
   return SMX_OK;
 }
 
+int smx_sync(smx_engine* eng, void* stream) {
+  if (!eng) return fail(SMX_ERR_INVALID, "engine is NULL");
+  try {
+    check(cudaSetDevice(eng->device), "cudaSetDevice");
+    check(cudaStreamSynchronize(stream ? static_cast<cudaStream_t>(stream) : eng->stream), "cudaStreamSynchronize");
+  } catch (const std::exception& e) {
+    return fail(SMX_ERR_CUDA, e.what());
+  }
+  if (eng->take_status() != SMX_OK) return fail(SMX_ERR_TIMEOUT, "a device-side wait timed out; results are invalid");
+  return SMX_OK;
+}
+
 int smx_stage_times(smx_engine* eng, double* out_ms, int cap) {
   if (!eng) return fail(SMX_ERR_INVALID, "engine is NULL");
   if (!eng->profile || !eng->ev[0]) return 0;

@@ -458,7 +458,9 @@ int smx_md_run(smx_md* md, int steps) {
 int smx_md_sync(smx_md* md) {
   if (!md) return fail(SMX_ERR_INVALID, "md is NULL");
   const cudaError_t e = cudaStreamSynchronize(md->eng->stream);
-  return e == cudaSuccess ? SMX_OK : fail(SMX_ERR_CUDA, cudaGetErrorString(e));
+  if (e != cudaSuccess) return fail(SMX_ERR_CUDA, cudaGetErrorString(e));
+  if (md->eng->take_status() != SMX_OK) return fail(SMX_ERR_TIMEOUT, "a device-side wait timed out; results are invalid");
+  return SMX_OK;
 }
 
 int smx_md_state(smx_md* md, double* positions, double* velocities, double* forces, double* potential_energy,
@@ -482,6 +484,7 @@ int smx_md_state(smx_md* md, double* positions, double* velocities, double* forc
   } catch (const std::exception& e) {
     return fail(SMX_ERR_CUDA, e.what());
   }
+  if (md->eng->take_status() != SMX_OK) return fail(SMX_ERR_TIMEOUT, "a device-side wait timed out; results are invalid");
   return SMX_OK;
 }
 

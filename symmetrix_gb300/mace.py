@@ -91,6 +91,11 @@ class MACE:
             node_energies, node_forces, stream)
         _lib.raise_for(code, self._lib)
 
+    def sync(self, stream=None):
+        """Wait for `stream` (default: the engine's) and raise TimeoutError if a bounded
+        device-side wait gave up in the work enqueued since the last check."""
+        _lib.raise_for(self._lib.smx_sync(self._h, stream), self._lib)
+
     def compute_atoms(self, positions, species, box=None):
         """Energy, node energies, atomic forces (n, 3) and virial (3, 3) of a structure.
 

@@ -32,3 +32,21 @@ def test_library_exports_every_declared_symbol():
 def test_binding_covers_the_header():
     bound = {n for n, _, _ in _lib.SIGNATURES}
     assert set(declared_functions()) <= bound
+
+
+def declared_arity():
+    """Parameter count of every smx_* declaration in include/*.h."""
+    out = {}
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
+        for name, params in re.findall(r"\b(smx_\w+)\s*\(([^)]*)\)\s*;", text):
+            params = params.strip()
+            out[name] = 0 if params in ("", "void") else len(params.split(","))
+    return out
+
+
+def test_binding_argument_counts_match_the_header():
+    arity = declared_arity()
+    assert len(arity) == len(declared_functions())
+    wrong = {n: (len(a), arity[n]) for n, _, a in _lib.SIGNATURES if n in arity and len(a) != arity[n]}
+    assert not wrong, wrong

@@ -58,6 +58,8 @@ void HostModel::load_json(const std::string& path) {
   r_cut = d.num(get("r_cut"));
   l_max = static_cast<int>(d.num(get("l_max")));
   L_max = static_cast<int>(d.num(get("L_max")));
+  require(S >= 1, "num_elements must be positive");
+  require(std::isfinite(r_cut) && r_cut > 0.0, "r_cut must be positive and finite");
   require(l_max == 3, "l_max must be 3");
   require(L_max >= 1 && L_max <= 2, "L_max must be 1 or 2");
   require(C >= 32 && C <= 256 && C % 32 == 0, "num_channels must be a multiple of 32 in [32, 256]");
@@ -94,6 +96,10 @@ void HostModel::load_json(const std::string& path) {
   require(npairs == S * (S + 1) / 2, "one spline set per unordered species pair");
   require(nspl0 == (l_max + 1) * C, "layer-0 radial set must have (l_max+1)*C splines");
   require(K >= 2, "at least two spline knots");
+  // the knots must reach r_cut: the reference reads past its table otherwise
+  // (cubic_spline_set.cpp:54 does no bounds check)
+  require(std::isfinite(spl_h) && spl_h > 0.0 && (K - 1) * spl_h >= r_cut * (1.0 - 1e-6),
+          "radial_spline_h must be positive, with (knots - 1) * h >= r_cut");
 
   H0 = numbers(d, get("H0_weights"));
   require(static_cast<int>(H0.size()) == S * C, "H0_weights size");

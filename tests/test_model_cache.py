@@ -39,3 +39,40 @@ def test_corrupt_cache_is_rejected(engine_lib, small_model_path, tmp_path):
         save_model_cache(bad, str(tmp_path / "c.smxb"))
     with pytest.raises(RuntimeError):
         save_model_cache(str(tmp_path / "missing.json"), str(tmp_path / "d.smxb"))
+
+
+MALFORMED = {
+    "missing key": (lambda m: m.pop("r_cut"), "missing key 'r_cut'"),
+    "r_cut zero": (lambda m: m.update(r_cut=0.0), "r_cut must be positive"),
+    "spline step negative": (lambda m: m.update(radial_spline_h=-0.1), "radial_spline_h"),
+    "knots short of r_cut": (lambda m: m.update(radial_spline_h=m["radial_spline_h"] * 0.5), "radial_spline_h"),
+    "ragged spline row": (lambda m: m["radial_spline_values_1"][0].pop(), "ragged array"),
+    "l_max": (lambda m: m.update(l_max=4), "l_max must be 3"),
+    "channels": (lambda m: m.update(num_channels=48), "num_channels"),
+    "species tables": (lambda m: m["atomic_energies"].pop(), "species table sizes"),
+    "H1_weights size": (lambda m: m["H1_weights"].pop(), "H1_weights size"),
+    "monomial variable": (lambda m: m["M0_monomials"]["0"][3].__setitem__(0, 99), "monomial variable out of range"),
+    "coupling index": (lambda m: m["Phi1_lme"].__setitem__(0, 999), "coupling index out of range"),
+    "readout size": (lambda m: m["readout_1_weights"].pop(), "readout_1_weights size"),
+}
+
+
+@pytest.mark.parametrize("case", sorted(MALFORMED))
+def test_malformed_model_is_rejected(engine_lib, small_model_path, tmp_path, case):
+    """The loader checks what the reference's load_from_json (mace.cpp:905-1030) trusts:
+    every malformation raises with a message naming it, before anything reaches a GPU."""
+    import json
+    mutate, message = MALFORMED[case]
+    m = json.load(open(small_model_path))
+    mutate(m)
+    bad = str(tmp_path / "bad.json")
+    json.dump(m, open(bad, "w"))
+    with pytest.raises(RuntimeError, match=message):
+        save_model_cache(bad, str(tmp_path / "bad.smxb"))
+
+
+def test_truncated_json_is_rejected(engine_lib, small_model_path, tmp_path):
+    bad = str(tmp_path / "cut.json")
+    open(bad, "w").write(open(small_model_path).read()[:1000])
+    with pytest.raises(RuntimeError, match="not valid JSON"):
+        save_model_cache(bad, str(tmp_path / "cut.smxb"))

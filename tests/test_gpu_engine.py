@@ -428,3 +428,33 @@ def test_channel_widths(engine_lib, tmp_path, C, L_max):
         assert _report(f"C={C} {precision} E_i", m.node_energies, ref.node_energies) < (
             E_TOL if precision == "float32" else 1e-3 * max(1.0, np.abs(ref.node_energies).max()))
         assert _report(f"C={C} {precision} F", F, Fr) < max(tol, F_TOL)
+
+
+@pytest.mark.parametrize("precision", ["float32", "bfloat16"])
+def test_twenty_species_model(engine_lib, tmp_path, precision):
+    """20 species, as the reference's high-entropy-alloy case
+    (pair_symmetrix/test/test_pair_symmetrix_mace.py:300-393): 210 unordered and 400 ordered
+    pair tables; every species present; against the oracle in both forms, and the same
+    results with the centre atoms taken in input or species-sorted order."""
+    Z = list(range(21, 31)) + list(range(39, 49))
+    path = write_model(make_model(num_channels=32, species=Z, num_knots=20, seed=20), str(tmp_path / "hea.json"))
+    pos, L, species = random_box(240, 0.08, 1.2, 20, seed=21)
+    assert len(np.unique(species)) == 20
+    nl = neighbor_list(pos, 5.0, L)
+    ref = Evaluator(path, "port")
+    ref.compute_node_energies_forces(*edge_args(species, nl))
+    out = {}
+    m = _engine(path, precision=precision)
+    for order in (0, 1):
+        m.set_option("species_order", order)
+        m.compute_node_energies_forces(*edge_args(species, nl))
+        out[order] = (m.node_energies.copy(), m.node_forces.copy())
+    e_tol, f_tol = (E_TOL, F_TOL) if precision == "float32" else (0.005, 0.010)
+    assert _report("E_i", out[1][0], ref.node_energies) < e_tol
+    assert _report("f_edge", out[1][1], ref.node_forces) < f_tol
+    F = atomic_forces(240, nl["i"], nl["neigh_indices"], out[1][1])
+    Fr = atomic_forces(240, nl["i"], nl["neigh_indices"], ref.node_forces)
+    assert _report("F_atom", F, Fr) < f_tol
+    # the forward pass does not depend on the order; the adjoint's atomics to float32 rounding
+    assert np.array_equal(out[0][0], out[1][0])
+    assert _report("order", out[0][1], out[1][1]) < 1e-6

@@ -15,6 +15,9 @@
  *                                   the same call on device-resident arrays, as the Kokkos
  *                                   pair style passes them (pair_symmetrix/
  *                                   pair_symmetrix_mace_kokkos.cpp:390-394)
+ *   smx_sync                        no counterpart: the reference's calls are synchronous;
+ *                                   it reports a timed-out device wait after the
+ *                                   device-pointer call
  *   smx_num_elements, smx_num_channels, smx_r_cut, smx_l_max, smx_L_max, smx_num_LM,
  *   smx_atomic_numbers              public fields of class MACE (mace.hpp:18-25)
  *   smx_get_stage                   the read-only stage buffers the Python binding exposes

@@ -180,3 +180,32 @@ class MACE:
         if name in STAGES:
             return self.stage(name)
         raise AttributeError(name)
+
+
+class MACEKokkos(MACE):
+    """The name of the reference's Kokkos evaluator class (symmetrix/source/cpp/mace_kokkos.cpp),
+    which the reference's calculator picks for dtype "float64" (symmetrix_calc.py:49): here the
+    FP32 plain form, the engine having no float64 GPU form (its forces are within 1e-5 eV/A
+    of the float64 evaluator)."""
+
+    def __init__(self, filename, device=0, keep_stages=False):
+        super().__init__(filename, device=device, precision="float32", keep_stages=keep_stages)
+
+
+class MACEKokkosFloat(MACEKokkos):
+    """The reference's single-precision Kokkos class name: the FP32 plain form."""
+
+
+_kokkos_ready = False
+
+
+def _init_kokkos():
+    """The reference initialises Kokkos once per process before building a Kokkos
+    evaluator (symmetrix_calc.py:47-48); the engine needs no runtime set-up, so this
+    only records the call."""
+    global _kokkos_ready
+    _kokkos_ready = True
+
+
+def _kokkos_is_initialized():
+    return _kokkos_ready

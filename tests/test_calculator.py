@@ -157,3 +157,13 @@ def test_orthorhombic_and_general_paths_agree():
     assert abs(fast["energy"] - slow["energy"]) < 1e-2 * abs(fast["energy"]) + 1e-6
     with pytest.raises(ValueError):
         evaluate_structure(ev, np.full(len(z), 26), pos, np.eye(3) * L, [True] * 3)
+
+
+def test_module_offers_the_reference_binding_names():
+    """Code written against the reference's `symmetrix` module finds the names its
+    calculator uses (symmetrix_calc.py:43-49) on this package, without a GPU."""
+    import symmetrix_gb300 as symmetrix
+    assert hasattr(symmetrix, "MACEKokkos") and issubclass(symmetrix.MACEKokkosFloat, symmetrix.MACE)
+    if not symmetrix._kokkos_is_initialized():
+        symmetrix._init_kokkos()
+    assert symmetrix._kokkos_is_initialized()

@@ -12,6 +12,7 @@
 // the reverse-edge map, in float64.
 #include <cuda_runtime.h>
 
+#include "compsum.h"
 #include "device.cuh"
 #include "kernels.h"
 
@@ -317,13 +318,13 @@ __global__ void k_reduce_partials(int N, const int* __restrict__ first, const do
                                   double* __restrict__ partial) {
   __shared__ double sh[10][256];
   const long E = first[N];
-  double acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  CompSum acc[10];
   const long stride = static_cast<long>(gridDim.x) * blockDim.x;
   for (long e = static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x; e < E; e += stride)
     for (int a = 0; a < 3; ++a)
-      for (int b = 0; b < 3; ++b) acc[1 + 3 * a + b] += xyz[3 * e + a] * f[3 * e + b];
-  for (long i = static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x; i < N; i += stride) acc[0] += energies[i];
-  for (int q = 0; q < 10; ++q) sh[q][threadIdx.x] = acc[q];
+      for (int b = 0; b < 3; ++b) acc[1 + 3 * a + b].add(xyz[3 * e + a] * f[3 * e + b]);
+  for (long i = static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x; i < N; i += stride) acc[0].add(energies[i]);
+  for (int q = 0; q < 10; ++q) sh[q][threadIdx.x] = acc[q].value();
   __syncthreads();
   for (int w = blockDim.x / 2; w > 0; w >>= 1) {
     if (threadIdx.x < w)
@@ -335,9 +336,9 @@ __global__ void k_reduce_partials(int N, const int* __restrict__ first, const do
 
 __global__ void k_reduce_final(int nblocks, const double* __restrict__ partial, double* __restrict__ out) {
   if (threadIdx.x < 10) {
-    double s = 0.0;
-    for (int b = 0; b < nblocks; ++b) s += partial[b * 10 + threadIdx.x];
-    out[threadIdx.x] = s;
+    CompSum s;
+    for (int b = 0; b < nblocks; ++b) s.add(partial[b * 10 + threadIdx.x]);
+    out[threadIdx.x] = s.value();
   }
 }
 

@@ -20,6 +20,7 @@
 #include <string>
 
 #include "../../include/smx_gb300.h"
+#include "compsum.h"
 
 namespace smx {
 int fail(int code, const std::string& msg);
@@ -64,13 +65,13 @@ __global__ void __launch_bounds__(256) k_partials_noalloc(int N, long E, const d
                                                           const double* __restrict__ f,
                                                           double* __restrict__ partial) {
   __shared__ double sh[10][256];
-  double acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  smx::CompSum acc[10];
   const long b0 = static_cast<long>(blockIdx.x) * kChunk;
   for (long e = b0 + threadIdx.x; e < b0 + kChunk && e < E; e += blockDim.x)
     for (int a = 0; a < 3; ++a)
-      for (int c = 0; c < 3; ++c) acc[1 + 3 * a + c] += xyz[3 * e + a] * f[3 * e + c];
-  for (long i = b0 + threadIdx.x; i < b0 + kChunk && i < N; i += blockDim.x) acc[0] += energies[i];
-  for (int q = 0; q < 10; ++q) sh[q][threadIdx.x] = acc[q];
+      for (int c = 0; c < 3; ++c) acc[1 + 3 * a + c].add(xyz[3 * e + a] * f[3 * e + c]);
+  for (long i = b0 + threadIdx.x; i < b0 + kChunk && i < N; i += blockDim.x) acc[0].add(energies[i]);
+  for (int q = 0; q < 10; ++q) sh[q][threadIdx.x] = acc[q].value();
   __syncthreads();
   for (int w = blockDim.x / 2; w > 0; w >>= 1) {
     if (threadIdx.x < w)
@@ -82,9 +83,9 @@ __global__ void __launch_bounds__(256) k_partials_noalloc(int N, long E, const d
 
 __global__ void k_final_noalloc(int nb, const double* __restrict__ partial, double* __restrict__ out) {
   if (threadIdx.x < 10) {
-    double s = 0.0;
-    for (int b = 0; b < nb; ++b) s += partial[static_cast<long>(b) * 10 + threadIdx.x];
-    out[threadIdx.x] = s;
+    smx::CompSum s;
+    for (int b = 0; b < nb; ++b) s.add(partial[static_cast<long>(b) * 10 + threadIdx.x]);
+    out[threadIdx.x] = s.value();
   }
 }
 

@@ -91,7 +91,7 @@ def value_grad_fn(name, monos):
     return "\n".join(out)
 
 
-def main():
+def main(out_dir=HERE):
     lists = []
     for L in range(L_MAX + 1):
         for M in range(2 * L + 1):
@@ -109,7 +109,7 @@ def main():
          "// packed a | b << 8 | c << 16, 16 = constant one; LM-major, canonical order",
          f"constexpr int kMono[{len(flat)}] = {{{', '.join(map(str, flat))}}};", "",
          "}  // namespace poly", "}  // namespace smx", ""]
-    with open(os.path.join(HERE, "poly_canon_tables.h"), "w") as f:
+    with open(os.path.join(out_dir, "poly_canon_tables.h"), "w") as f:
         f.write("\n".join(t))
     h = ["// Generated by gen_poly.py: canonical symmetric-contraction monomials (l_max 3,",
          "// degree <= 3) as straight-line code.  Do not edit; rerun the script.",
@@ -122,7 +122,7 @@ def main():
     h.append("// the layer-1 contraction is the LM = 0 set")
     h.append(value_grad_fn("value_grad_M1", lists[0]))
     h += ["", "}  // namespace poly", "}  // namespace smx", ""]
-    path = os.path.join(HERE, "poly_canon.h")
+    path = os.path.join(out_dir, "poly_canon.h")
     with open(path, "w") as f:
         f.write("\n".join(h))
     print(f"wrote {path}: {[len(x) for x in lists]} monomials")

@@ -26,7 +26,8 @@ CXX_SOURCES = ["model.cpp", "model_cache.cpp"]
 
 
 def _deps():
-    return [os.path.join(SRC, f) for f in os.listdir(SRC)] + [os.path.join(ROOT, "include", "smx_gb300.h")]
+    src = [f for f in os.listdir(SRC) if f.endswith((".cu", ".cuh", ".h", ".hpp", ".cpp"))]
+    return [os.path.join(SRC, f) for f in src] + [os.path.join(ROOT, "include", "smx_gb300.h")]
 
 
 def _stale():

@@ -76,3 +76,15 @@ def test_truncated_json_is_rejected(engine_lib, small_model_path, tmp_path):
     open(bad, "w").write(open(small_model_path).read()[:1000])
     with pytest.raises(RuntimeError, match="not valid JSON"):
         save_model_cache(bad, str(tmp_path / "cut.smxb"))
+
+
+def test_cli_generates_and_caches_a_model(engine_lib, tmp_path):
+    """`python -m symmetrix_gb300.cli gen-model` / `cache` (the commands the profile
+    summaries use) on the CPU: the cache of the generated JSON equals the cache of
+    the cache."""
+    from symmetrix_gb300.cli import main
+    js, a, b = str(tmp_path / "m.json"), str(tmp_path / "a.smxb"), str(tmp_path / "b.smxb")
+    main(["gen-model", js, "--config", "small", "--knots", "20", "--zbl"])
+    main(["cache", js, a])
+    main(["cache", a, b])
+    assert open(a, "rb").read() == open(b, "rb").read()

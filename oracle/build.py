@@ -41,8 +41,8 @@ def build_oracle(force=False):
     hdr = os.path.join(HERE, "shim", "include", "nlohmann", "json.hpp")
     if force or _stale(ORACLE_SO, [src, hdr]):
         os.makedirs(os.path.dirname(ORACLE_SO), exist_ok=True)
-        _run(["g++", "-std=c++20", "-O3", "-fPIC", "-shared", "-I", os.path.join(HERE, "shim", "include"),
-              src, "-o", ORACLE_SO])
+        _run(["g++", "-std=c++20", "-O3", "-fPIC", "-shared", "-pthread", "-I",
+              os.path.join(HERE, "shim", "include"), src, "-o", ORACLE_SO])
     return ORACLE_SO
 
 

@@ -13,7 +13,9 @@
 // Phi1[N][num_lme][C], M1/H2[N][C], node_energies[N], node_forces[3E]
 // (node_forces = -dE/dxyz per directed edge).
 //
-// Thread safety: one Oracle object per thread; objects share nothing.
+// Thread safety: one Oracle object per thread; objects share nothing.  One object may
+// itself split each stage over node ranges (orc_set_threads); its results are the same
+// bits whatever the thread count.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -21,6 +23,8 @@
 #include <map>
 #include <stdexcept>
 #include <string>
+#include <exception>
+#include <thread>
 #include <vector>
 
 #include "nlohmann/json.hpp"
@@ -325,6 +329,36 @@ struct Oracle {
     ro2_scale = j["readout_2_scale_factor"].get<double>();
   }
 
+  // ----- parallel loops over node ranges -----
+  // Every stage's work for node i (and its edges) is independent of the other nodes,
+  // except the H1_adj scatter of reverse_Phi1, which is done as a gather over each
+  // node's incoming edges in ascending edge order.  Each element is therefore computed
+  // by the same operations in the same order as in a serial run: results do not
+  // depend on the thread count, bit for bit.
+  int nthreads = 1;
+  std::vector<long> eoff;  // [N+1] first edge of each node
+  template <typename F>
+  void par_nodes(int N, F&& f) {  // f(i0, i1) over disjoint node ranges
+    const int T = std::max(1, std::min(nthreads, N / 4));
+    if (T <= 1) {
+      f(0, N);
+      return;
+    }
+    std::vector<std::thread> th;
+    std::vector<std::exception_ptr> err(T);
+    for (int t = 0; t < T; ++t)
+      th.emplace_back([&, t] {
+        try {
+          f(static_cast<int>(static_cast<long>(N) * t / T), static_cast<int>(static_cast<long>(N) * (t + 1) / T));
+        } catch (...) {
+          err[t] = std::current_exception();
+        }
+      });
+    for (auto& x : th) x.join();
+    for (auto& e : err)
+      if (e) std::rethrow_exception(e);
+  }
+
   // ----- forward + reverse (mace.cpp:17-64) -----
   void compute(int N, const int* ntype, const int* nneigh, const int* nidx, const int* ntypes_e, long E,
                const double* xyz, const double* r) {
@@ -333,341 +367,401 @@ struct Oracle {
     if (check != E) throw std::invalid_argument("sum(num_neigh) != number of edges");
     for (long e = 0; e < E; ++e)
       if (nidx[e] < 0 || nidx[e] >= N) throw std::invalid_argument("neighbor index out of range");
+    eoff.assign(N + 1, 0);
+    for (int i = 0; i < N; ++i) eoff[i + 1] = eoff[i] + nneigh[i];
     node_energies.assign(N, 0.0);
     node_forces.assign(3 * E, 0.0);
-    if (has_zbl) zbl_stage(N, ntype, nneigh, ntypes_e, xyz, r);
-    stage_Y(E, xyz);
-    stage_R(N, ntype, nneigh, ntypes_e, r, spl0, R0, R0_deriv);
-    stage_A0(N, ntype, nneigh, ntypes_e);
-    scale_fwd(N, ntype, nneigh, ntypes_e, r, A0_scaled, A0s, A0);
+    if (has_zbl) zbl_stage(N, ntype, ntypes_e, xyz, r);
+    stage_Y(N, E, xyz);
+    stage_R(N, ntype, ntypes_e, r, spl0, R0, R0_deriv);
+    stage_A0(N, ntype, ntypes_e);
+    scale_fwd(N, ntype, ntypes_e, r, A0_scaled, A0s, A0);
     stage_M0(N, ntype);
     stage_H1(N);
-    stage_R(N, ntype, nneigh, ntypes_e, r, spl1, R1, R1_deriv);
-    stage_Phi1(N, nneigh, nidx);
+    stage_R(N, ntype, ntypes_e, r, spl1, R1, R1_deriv);
+    stage_Phi1(N, nidx);
     stage_A1(N);
-    scale_fwd(N, ntype, nneigh, ntypes_e, r, A1_scaled, A1s, A1);
+    scale_fwd(N, ntype, ntypes_e, r, A1_scaled, A1s, A1);
     stage_M1(N, ntype);
     stage_H2(N, ntype);
     stage_readouts(N, ntype);
     reverse_H2(N, ntype);
     reverse_M1(N);
-    scale_rev(N, ntype, nneigh, ntypes_e, xyz, r, A1_scaled, A1s, A1, A1_adj);
+    scale_rev(N, ntype, ntypes_e, xyz, r, A1_scaled, A1s, A1, A1_adj);
     reverse_A1(N);
-    reverse_Phi1(N, nneigh, nidx, xyz, r);
+    reverse_Phi1(N, nidx, xyz, r);
     reverse_H1(N);
     reverse_M0(N);
-    scale_rev(N, ntype, nneigh, ntypes_e, xyz, r, A0_scaled, A0s, A0, A0_adj);
-    reverse_A0(N, ntype, nneigh, ntypes_e, xyz, r);
+    scale_rev(N, ntype, ntypes_e, xyz, r, A0_scaled, A0s, A0, A0_adj);
+    reverse_A0(N, ntype, ntypes_e, xyz, r);
   }
 
   // zbl.cpp:96-125
-  void zbl_stage(int N, const int* ntype, const int* nneigh, const int* te, const double* xyz, const double* r) {
-    long e = 0;
-    for (int i = 0; i < N; ++i)
-      for (int q = 0; q < nneigh[i]; ++q, ++e) {
-        double g = 0;
-        node_energies[i] += zbl.energy(Z[ntype[i]], Z[te[e]], r[e], &g);
-        for (int a = 0; a < 3; ++a) node_forces[3 * e + a] -= xyz[3 * e + a] / r[e] * g;
-      }
+  void zbl_stage(int N, const int* ntype, const int* te, const double* xyz, const double* r) {
+    par_nodes(N, [&](int i0, int i1) {
+      for (int i = i0; i < i1; ++i)
+        for (long e = eoff[i]; e < eoff[i + 1]; ++e) {
+          double g = 0;
+          node_energies[i] += zbl.energy(Z[ntype[i]], Z[te[e]], r[e], &g);
+          for (int a = 0; a < 3; ++a) node_forces[3 * e + a] -= xyz[3 * e + a] / r[e] * g;
+        }
+    });
   }
 
   // mace.cpp:118-148
-  void stage_Y(long E, const double* xyz) {
+  void stage_Y(int N, long E, const double* xyz) {
     Y.assign(E * nlm, 0.0);
     Y_grad.assign(3 * E * nlm, 0.0);
-    for (long e = 0; e < E; ++e) sph_harm(xyz + 3 * e, &Y[e * nlm], &Y_grad[3 * e * nlm]);
+    par_nodes(N, [&](int i0, int i1) {
+      for (long e = eoff[i0]; e < eoff[i1]; ++e) sph_harm(xyz + 3 * e, &Y[e * nlm], &Y_grad[3 * e * nlm]);
+    });
   }
 
   // mace.cpp:66-116
-  void stage_R(int N, const int* ntype, const int* nneigh, const int* te, const double* r,
-               const std::vector<SplineSet>& spl, vecd& R, vecd& Rd) {
+  void stage_R(int N, const int* ntype, const int* te, const double* r, const std::vector<SplineSet>& spl, vecd& R,
+               vecd& Rd) {
     const int ns = spl[0].ns;
-    long E = 0;
-    for (int i = 0; i < N; ++i) E += nneigh[i];
+    const long E = eoff[N];
     R.assign(E * ns, 0.0);
     Rd.assign(E * ns, 0.0);
-    long e = 0;
-    for (int i = 0; i < N; ++i)
-      for (int q = 0; q < nneigh[i]; ++q, ++e)
-        spl[pair_index(ntype[i], te[e])].eval(r[e], &R[e * ns], &Rd[e * ns]);
+    par_nodes(N, [&](int i0, int i1) {
+      for (int i = i0; i < i1; ++i)
+        for (long e = eoff[i]; e < eoff[i + 1]; ++e)
+          spl[pair_index(ntype[i], te[e])].eval(r[e], &R[e * ns], &Rd[e * ns]);
+    });
   }
 
   // mace.cpp:150-201: Phi0 = sum_j R0 Y H0[type_j], then per-l channel mixing
-  void stage_A0(int N, const int* ntype, const int* nneigh, const int* te) {
+  void stage_A0(int N, const int* ntype, const int* te) {
     A0.assign(static_cast<size_t>(N) * nlm * C, 0.0);
-    vecd phi0(nlm * C);
-    long e = 0;
-    for (int i = 0; i < N; ++i) {
-      std::fill(phi0.begin(), phi0.end(), 0.0);
-      for (int q = 0; q < nneigh[i]; ++q, ++e) {
-        const double* h0 = &H0w[te[e] * C];
-        for (int l = 0; l <= l_max; ++l) {
-          const double* rl = &R0[e * (l_max + 1) * C + l * C];
-          for (int lm = l * l; lm < (l + 1) * (l + 1); ++lm) {
-            const double y = Y[e * nlm + lm];
-            for (int k = 0; k < C; ++k) phi0[lm * C + k] += rl[k] * y * h0[k];
+    par_nodes(N, [&](int i0, int i1) {
+      vecd phi0(nlm * C);
+      for (int i = i0; i < i1; ++i) {
+        std::fill(phi0.begin(), phi0.end(), 0.0);
+        for (long e = eoff[i]; e < eoff[i + 1]; ++e) {
+          const double* h0 = &H0w[te[e] * C];
+          for (int l = 0; l <= l_max; ++l) {
+            const double* rl = &R0[e * (l_max + 1) * C + l * C];
+            for (int lm = l * l; lm < (l + 1) * (l + 1); ++lm) {
+              const double y = Y[e * nlm + lm];
+              for (int k = 0; k < C; ++k) phi0[lm * C + k] += rl[k] * y * h0[k];
+            }
           }
         }
+        for (int l = 0; l <= l_max; ++l) {
+          const double* W = A0w[ntype[i]][l].data();
+          for (int lm = l * l; lm < (l + 1) * (l + 1); ++lm)
+            for (int k = 0; k < C; ++k) {
+              double s = 0;
+              for (int kk = 0; kk < C; ++kk) s += phi0[lm * C + kk] * W[kk * C + k];
+              A0[(static_cast<size_t>(i) * nlm + lm) * C + k] = s;
+            }
+        }
       }
-      for (int l = 0; l <= l_max; ++l) {
-        const double* W = A0w[ntype[i]][l].data();
-        for (int lm = l * l; lm < (l + 1) * (l + 1); ++lm)
-          for (int k = 0; k < C; ++k) {
-            double s = 0;
-            for (int kk = 0; kk < C; ++kk) s += phi0[lm * C + kk] * W[kk * C + k];
-            A0[(static_cast<size_t>(i) * nlm + lm) * C + k] = s;
-          }
-      }
-    }
+    });
   }
 
   // mace.cpp:273-297 / :681-705
-  void scale_fwd(int N, const int* ntype, const int* nneigh, const int* te, const double* r, bool on,
-                 const std::vector<Spline1>& sp, vecd& A) {
+  void scale_fwd(int N, const int* ntype, const int* te, const double* r, bool on, const std::vector<Spline1>& sp,
+                 vecd& A) {
     if (!on) return;
-    long e = 0;
-    for (int i = 0; i < N; ++i) {
-      double s = 1.0;
-      for (int q = 0; q < nneigh[i]; ++q, ++e) {
-        double f, g;
-        sp[pair_index(ntype[i], te[e])].eval(r[e], f, g);
-        s += f;
+    par_nodes(N, [&](int i0, int i1) {
+      for (int i = i0; i < i1; ++i) {
+        double s = 1.0;
+        for (long e = eoff[i]; e < eoff[i + 1]; ++e) {
+          double f, g;
+          sp[pair_index(ntype[i], te[e])].eval(r[e], f, g);
+          s += f;
+        }
+        for (int x = 0; x < nlm * C; ++x) A[static_cast<size_t>(i) * nlm * C + x] /= s;
       }
-      for (int x = 0; x < nlm * C; ++x) A[static_cast<size_t>(i) * nlm * C + x] /= s;
-    }
+    });
   }
 
   // mace.cpp:299-346 / :707-757
-  void scale_rev(int N, const int* ntype, const int* nneigh, const int* te, const double* xyz, const double* r,
-                 bool on, const std::vector<Spline1>& sp, const vecd& A, vecd& Aadj) {
+  void scale_rev(int N, const int* ntype, const int* te, const double* xyz, const double* r, bool on,
+                 const std::vector<Spline1>& sp, const vecd& A, vecd& Aadj) {
     if (!on) return;
-    long e0i = 0;
-    for (int i = 0; i < N; ++i) {
-      double s = 1.0;
-      for (int q = 0; q < nneigh[i]; ++q) {
-        double f, g;
-        sp[pair_index(ntype[i], te[e0i + q])].eval(r[e0i + q], f, g);
-        s += f;
+    par_nodes(N, [&](int i0, int i1) {
+      for (int i = i0; i < i1; ++i) {
+        double s = 1.0;
+        for (long e = eoff[i]; e < eoff[i + 1]; ++e) {
+          double f, g;
+          sp[pair_index(ntype[i], te[e])].eval(r[e], f, g);
+          s += f;
+        }
+        double dot = 0;
+        for (int x = 0; x < nlm * C; ++x)
+          dot += Aadj[static_cast<size_t>(i) * nlm * C + x] * A[static_cast<size_t>(i) * nlm * C + x];
+        for (long e = eoff[i]; e < eoff[i + 1]; ++e) {
+          double f, g;
+          sp[pair_index(ntype[i], te[e])].eval(r[e], f, g);
+          for (int a = 0; a < 3; ++a) node_forces[3 * e + a] += dot / s * g * xyz[3 * e + a] / r[e];
+        }
+        for (int x = 0; x < nlm * C; ++x) Aadj[static_cast<size_t>(i) * nlm * C + x] /= s;
       }
-      double dot = 0;
-      for (int x = 0; x < nlm * C; ++x)
-        dot += Aadj[static_cast<size_t>(i) * nlm * C + x] * A[static_cast<size_t>(i) * nlm * C + x];
-      for (int q = 0; q < nneigh[i]; ++q) {
-        const long e = e0i + q;
-        double f, g;
-        sp[pair_index(ntype[i], te[e])].eval(r[e], f, g);
-        for (int a = 0; a < 3; ++a) node_forces[3 * e + a] += dot / s * g * xyz[3 * e + a] / r[e];
-      }
-      for (int x = 0; x < nlm * C; ++x) Aadj[static_cast<size_t>(i) * nlm * C + x] /= s;
-      e0i += nneigh[i];
-    }
+    });
   }
 
   // mace.cpp:348-370: per (i, LM, k) polynomial of A0[i, :, k], with gradient
   void stage_M0(int N, const int* ntype) {
     M0.assign(static_cast<size_t>(N) * nLM * C, 0.0);
     M0_grad.assign(static_cast<size_t>(N) * nLM * nlm * C, 0.0);
-    double x[16], g[16];
-    for (int i = 0; i < N; ++i)
-      for (int LM = 0; LM < nLM; ++LM)
-        for (int k = 0; k < C; ++k) {
-          for (int v = 0; v < nlm; ++v) x[v] = A0[(static_cast<size_t>(i) * nlm + v) * C + k];
-          const double* cf = &P0c[((static_cast<size_t>(ntype[i]) * nLM + LM) * C + k) * t_max0];
-          M0[(static_cast<size_t>(i) * nLM + LM) * C + k] = poly_eval(P0[LM], cf, x, g, nlm);
-          for (int v = 0; v < nlm; ++v)
-            M0_grad[((static_cast<size_t>(i) * nLM + LM) * nlm + v) * C + k] = g[v];
-        }
+    par_nodes(N, [&](int i0, int i1) {
+      double x[16], g[16];
+      for (int i = i0; i < i1; ++i)
+        for (int LM = 0; LM < nLM; ++LM)
+          for (int k = 0; k < C; ++k) {
+            for (int v = 0; v < nlm; ++v) x[v] = A0[(static_cast<size_t>(i) * nlm + v) * C + k];
+            const double* cf = &P0c[((static_cast<size_t>(ntype[i]) * nLM + LM) * C + k) * t_max0];
+            M0[(static_cast<size_t>(i) * nLM + LM) * C + k] = poly_eval(P0[LM], cf, x, g, nlm);
+            for (int v = 0; v < nlm; ++v)
+              M0_grad[((static_cast<size_t>(i) * nLM + LM) * nlm + v) * C + k] = g[v];
+          }
+    });
   }
 
   // mace.cpp:372-395
   void reverse_M0(int N) {
     A0_adj.assign(static_cast<size_t>(N) * nlm * C, 0.0);
-    for (int i = 0; i < N; ++i)
-      for (int v = 0; v < nlm; ++v)
-        for (int LM = 0; LM < nLM; ++LM)
-          for (int k = 0; k < C; ++k)
-            A0_adj[(static_cast<size_t>(i) * nlm + v) * C + k] +=
-                M0_grad[((static_cast<size_t>(i) * nLM + LM) * nlm + v) * C + k] *
-                M0_adj[(static_cast<size_t>(i) * nLM + LM) * C + k];
+    par_nodes(N, [&](int i0, int i1) {
+      for (int i = i0; i < i1; ++i)
+        for (int v = 0; v < nlm; ++v)
+          for (int LM = 0; LM < nLM; ++LM)
+            for (int k = 0; k < C; ++k)
+              A0_adj[(static_cast<size_t>(i) * nlm + v) * C + k] +=
+                  M0_grad[((static_cast<size_t>(i) * nLM + LM) * nlm + v) * C + k] *
+                  M0_adj[(static_cast<size_t>(i) * nLM + LM) * C + k];
+    });
   }
 
   // rows of block L of X[N][nLM][C] times W_L (C x C), optionally transposed (mace.cpp:397-451)
   void mix(int N, const vecd& X, vecd& Yo, const vecd& W, int Lmax, int nrows, bool trans) {
     Yo.assign(X.size(), 0.0);
-    for (int i = 0; i < N; ++i)
-      for (int L = 0; L <= Lmax; ++L) {
-        const double* w = &W[static_cast<size_t>(L) * C * C];
-        for (int LM = L * L; LM < (L + 1) * (L + 1); ++LM) {
-          const double* xr = &X[(static_cast<size_t>(i) * nrows + LM) * C];
-          double* yr = &Yo[(static_cast<size_t>(i) * nrows + LM) * C];
-          for (int k = 0; k < C; ++k) {
-            double s = 0;
-            for (int kk = 0; kk < C; ++kk) s += xr[kk] * (trans ? w[k * C + kk] : w[kk * C + k]);
-            yr[k] = s;
+    par_nodes(N, [&](int i0, int i1) {
+      for (int i = i0; i < i1; ++i)
+        for (int L = 0; L <= Lmax; ++L) {
+          const double* w = &W[static_cast<size_t>(L) * C * C];
+          for (int LM = L * L; LM < (L + 1) * (L + 1); ++LM) {
+            const double* xr = &X[(static_cast<size_t>(i) * nrows + LM) * C];
+            double* yr = &Yo[(static_cast<size_t>(i) * nrows + LM) * C];
+            for (int k = 0; k < C; ++k) {
+              double s = 0;
+              for (int kk = 0; kk < C; ++kk) s += xr[kk] * (trans ? w[k * C + kk] : w[kk * C + k]);
+              yr[k] = s;
+            }
           }
         }
-      }
+    });
   }
   void stage_H1(int N) { mix(N, M0, H1, H1w, L_max, nLM, false); }
   void reverse_H1(int N) { mix(N, H1_adj, M0_adj, H1w, L_max, nLM, true); }
 
   // mace.cpp:453-502
-  void stage_Phi1(int N, const int* nneigh, const int* nidx) {
+  void stage_Phi1(int N, const int* nidx) {
     const int ns1 = spl1[0].ns;
     Phi1r.assign(static_cast<size_t>(N) * n_p * C, 0.0);
-    long e = 0;
-    for (int i = 0; i < N; ++i) {
-      double* out = &Phi1r[static_cast<size_t>(i) * n_p * C];
-      for (int q = 0; q < nneigh[i]; ++q, ++e) {
-        const double* hj = &H1[static_cast<size_t>(nidx[e]) * nLM * C];
-        int p = 0;
-        for (size_t ins = 0; ins < phi_l.size(); ++ins) {
-          const double* R = &R1[e * ns1 + ins * C];
-          const int l1 = phi_l1[ins], l2 = phi_l2[ins];
-          for (int lm1 = l1 * l1; lm1 < (l1 + 1) * (l1 + 1); ++lm1) {
-            const double y = Y[e * nlm + lm1];
-            for (int lm2 = l2 * l2; lm2 < (l2 + 1) * (l2 + 1); ++lm2, ++p)
-              for (int k = 0; k < C; ++k) out[p * C + k] += R[k] * y * hj[lm2 * C + k];
+    Phi1.assign(static_cast<size_t>(N) * n_lme * C, 0.0);
+    par_nodes(N, [&](int i0, int i1) {
+      for (int i = i0; i < i1; ++i) {
+        double* out = &Phi1r[static_cast<size_t>(i) * n_p * C];
+        for (long e = eoff[i]; e < eoff[i + 1]; ++e) {
+          const double* hj = &H1[static_cast<size_t>(nidx[e]) * nLM * C];
+          int p = 0;
+          for (size_t ins = 0; ins < phi_l.size(); ++ins) {
+            const double* R = &R1[e * ns1 + ins * C];
+            const int l1 = phi_l1[ins], l2 = phi_l2[ins];
+            for (int lm1 = l1 * l1; lm1 < (l1 + 1) * (l1 + 1); ++lm1) {
+              const double y = Y[e * nlm + lm1];
+              for (int lm2 = l2 * l2; lm2 < (l2 + 1) * (l2 + 1); ++lm2, ++p)
+                for (int k = 0; k < C; ++k) out[p * C + k] += R[k] * y * hj[lm2 * C + k];
+            }
           }
         }
+        for (size_t t = 0; t < phi_cg.size(); ++t)
+          for (int k = 0; k < C; ++k)
+            Phi1[(static_cast<size_t>(i) * n_lme + phi_lme[t]) * C + k] +=
+                phi_cg[t] * Phi1r[(static_cast<size_t>(i) * n_p + phi_p[t]) * C + k];
       }
-    }
-    Phi1.assign(static_cast<size_t>(N) * n_lme * C, 0.0);
-    for (int i = 0; i < N; ++i)
-      for (size_t t = 0; t < phi_cg.size(); ++t)
-        for (int k = 0; k < C; ++k)
-          Phi1[(static_cast<size_t>(i) * n_lme + phi_lme[t]) * C + k] +=
-              phi_cg[t] * Phi1r[(static_cast<size_t>(i) * n_p + phi_p[t]) * C + k];
+    });
   }
 
-  // mace.cpp:504-605 (node_forces and H1_adj accumulate)
-  void reverse_Phi1(int N, const int* nneigh, const int* nidx, const double* xyz, const double* r) {
+  // mace.cpp:504-605: node_forces of every edge i->j, and H1_adj[j] += R1 Y dPhi1r[i].
+  // The H1_adj sums are formed per node j over its incoming edges in ascending edge
+  // order, the order a serial pass over the edges adds them in.
+  void reverse_Phi1(int N, const int* nidx, const double* xyz, const double* r) {
     const int ns1 = spl1[0].ns;
+    const long E = eoff[N];
     dPhi1r.assign(static_cast<size_t>(N) * n_p * C, 0.0);
+    par_nodes(N, [&](int i0, int i1) {
+      for (int i = i0; i < i1; ++i)
+        for (size_t t = 0; t < phi_cg.size(); ++t)
+          for (int k = 0; k < C; ++k)
+            dPhi1r[(static_cast<size_t>(i) * n_p + phi_p[t]) * C + k] +=
+                phi_cg[t] * dPhi1[(static_cast<size_t>(i) * n_lme + phi_lme[t]) * C + k];
+    });
+    par_nodes(N, [&](int i0, int i1) {
+      for (int i = i0; i < i1; ++i) {
+        const double* g = &dPhi1r[static_cast<size_t>(i) * n_p * C];
+        for (long e = eoff[i]; e < eoff[i + 1]; ++e) {
+          const double* hj = &H1[static_cast<size_t>(nidx[e]) * nLM * C];
+          const double* u = xyz + 3 * e;
+          double f[3] = {0, 0, 0};
+          int p = 0;
+          for (size_t ins = 0; ins < phi_l.size(); ++ins) {
+            const double* R = &R1[e * ns1 + ins * C];
+            const double* Rd = &R1_deriv[e * ns1 + ins * C];
+            const int l1 = phi_l1[ins], l2 = phi_l2[ins];
+            for (int lm1 = l1 * l1; lm1 < (l1 + 1) * (l1 + 1); ++lm1) {
+              const double y = Y[e * nlm + lm1];
+              const double gy[3] = {Y_grad[(3 * e + 0) * nlm + lm1], Y_grad[(3 * e + 1) * nlm + lm1],
+                                    Y_grad[(3 * e + 2) * nlm + lm1]};
+              for (int lm2 = l2 * l2; lm2 < (l2 + 1) * (l2 + 1); ++lm2, ++p)
+                for (int k = 0; k < C; ++k) {
+                  const double gh = g[p * C + k] * hj[lm2 * C + k];
+                  for (int a = 0; a < 3; ++a) f[a] -= gh * (u[a] / r[e] * Rd[k] * y + R[k] * gy[a]);
+                }
+            }
+          }
+          for (int a = 0; a < 3; ++a) node_forces[3 * e + a] += f[a];
+        }
+      }
+    });
+    // incoming edges of every node, ascending, and each edge's source node
+    std::vector<long> in_off(N + 1, 0), in_e(E);
+    std::vector<int> src(E);
     for (int i = 0; i < N; ++i)
-      for (size_t t = 0; t < phi_cg.size(); ++t)
-        for (int k = 0; k < C; ++k)
-          dPhi1r[(static_cast<size_t>(i) * n_p + phi_p[t]) * C + k] +=
-              phi_cg[t] * dPhi1[(static_cast<size_t>(i) * n_lme + phi_lme[t]) * C + k];
-    long e = 0;
-    for (int i = 0; i < N; ++i) {
-      const double* g = &dPhi1r[static_cast<size_t>(i) * n_p * C];
-      for (int q = 0; q < nneigh[i]; ++q, ++e) {
-        const double* hj = &H1[static_cast<size_t>(nidx[e]) * nLM * C];
-        double* aj = &H1_adj[static_cast<size_t>(nidx[e]) * nLM * C];
-        const double* u = xyz + 3 * e;
-        double f[3] = {0, 0, 0};
-        int p = 0;
-        for (size_t ins = 0; ins < phi_l.size(); ++ins) {
-          const double* R = &R1[e * ns1 + ins * C];
-          const double* Rd = &R1_deriv[e * ns1 + ins * C];
-          const int l1 = phi_l1[ins], l2 = phi_l2[ins];
-          for (int lm1 = l1 * l1; lm1 < (l1 + 1) * (l1 + 1); ++lm1) {
-            const double y = Y[e * nlm + lm1];
-            const double gy[3] = {Y_grad[(3 * e + 0) * nlm + lm1], Y_grad[(3 * e + 1) * nlm + lm1],
-                                  Y_grad[(3 * e + 2) * nlm + lm1]};
-            for (int lm2 = l2 * l2; lm2 < (l2 + 1) * (l2 + 1); ++lm2, ++p)
-              for (int k = 0; k < C; ++k) {
-                const double gh = g[p * C + k] * hj[lm2 * C + k];
-                for (int a = 0; a < 3; ++a) f[a] -= gh * (u[a] / r[e] * Rd[k] * y + R[k] * gy[a]);
-                aj[lm2 * C + k] += R[k] * y * g[p * C + k];
-              }
+      for (long e = eoff[i]; e < eoff[i + 1]; ++e) {
+        src[e] = i;
+        ++in_off[nidx[e] + 1];
+      }
+    for (int j = 0; j < N; ++j) in_off[j + 1] += in_off[j];
+    {
+      std::vector<long> fill(in_off.begin(), in_off.end() - 1);
+      for (long e = 0; e < E; ++e) in_e[fill[nidx[e]]++] = e;
+    }
+    par_nodes(N, [&](int j0, int j1) {
+      for (int j = j0; j < j1; ++j) {
+        double* aj = &H1_adj[static_cast<size_t>(j) * nLM * C];
+        for (long q = in_off[j]; q < in_off[j + 1]; ++q) {
+          const long e = in_e[q];
+          const double* g = &dPhi1r[static_cast<size_t>(src[e]) * n_p * C];
+          int p = 0;
+          for (size_t ins = 0; ins < phi_l.size(); ++ins) {
+            const double* R = &R1[e * ns1 + ins * C];
+            const int l1 = phi_l1[ins], l2 = phi_l2[ins];
+            for (int lm1 = l1 * l1; lm1 < (l1 + 1) * (l1 + 1); ++lm1) {
+              const double y = Y[e * nlm + lm1];
+              for (int lm2 = l2 * l2; lm2 < (l2 + 1) * (l2 + 1); ++lm2, ++p)
+                for (int k = 0; k < C; ++k) aj[lm2 * C + k] += R[k] * y * g[p * C + k];
+            }
           }
         }
-        for (int a = 0; a < 3; ++a) node_forces[3 * e + a] += f[a];
       }
-    }
+    });
   }
 
   // mace.cpp:607-679: per l, (2l+1) x (n_e C) times (n_e C) x C
   void stage_A1(int N) {
     A1.assign(static_cast<size_t>(N) * nlm * C, 0.0);
-    for (int i = 0; i < N; ++i) {
-      const double* ph = &Phi1[static_cast<size_t>(i) * n_lme * C];
-      double* a = &A1[static_cast<size_t>(i) * nlm * C];
-      for (int l = 0; l <= l_max; ++l) {
-        const int K = num_e[l] * C;
-        for (int m = 0; m < 2 * l + 1; ++m)
-          for (int k = 0; k < C; ++k) {
-            double s = 0;
-            for (int kk = 0; kk < K; ++kk) s += ph[m * K + kk] * A1w[l][static_cast<size_t>(kk) * C + k];
-            a[m * C + k] = s;
-          }
-        ph += (2 * l + 1) * K;
-        a += (2 * l + 1) * C;
+    par_nodes(N, [&](int i0, int i1) {
+      for (int i = i0; i < i1; ++i) {
+        const double* ph = &Phi1[static_cast<size_t>(i) * n_lme * C];
+        double* a = &A1[static_cast<size_t>(i) * nlm * C];
+        for (int l = 0; l <= l_max; ++l) {
+          const int K = num_e[l] * C;
+          for (int m = 0; m < 2 * l + 1; ++m)
+            for (int k = 0; k < C; ++k) {
+              double s = 0;
+              for (int kk = 0; kk < K; ++kk) s += ph[m * K + kk] * A1w[l][static_cast<size_t>(kk) * C + k];
+              a[m * C + k] = s;
+            }
+          ph += (2 * l + 1) * K;
+          a += (2 * l + 1) * C;
+        }
       }
-    }
+    });
   }
   void reverse_A1(int N) {
     dPhi1.assign(static_cast<size_t>(N) * n_lme * C, 0.0);
-    for (int i = 0; i < N; ++i) {
-      const double* a = &A1_adj[static_cast<size_t>(i) * nlm * C];
-      double* ph = &dPhi1[static_cast<size_t>(i) * n_lme * C];
-      for (int l = 0; l <= l_max; ++l) {
-        const int K = num_e[l] * C;
-        for (int m = 0; m < 2 * l + 1; ++m)
-          for (int kk = 0; kk < K; ++kk) {
-            double s = 0;
-            for (int k = 0; k < C; ++k) s += a[m * C + k] * A1w[l][static_cast<size_t>(kk) * C + k];
-            ph[m * K + kk] = s;
-          }
-        ph += (2 * l + 1) * K;
-        a += (2 * l + 1) * C;
+    par_nodes(N, [&](int i0, int i1) {
+      for (int i = i0; i < i1; ++i) {
+        const double* a = &A1_adj[static_cast<size_t>(i) * nlm * C];
+        double* ph = &dPhi1[static_cast<size_t>(i) * n_lme * C];
+        for (int l = 0; l <= l_max; ++l) {
+          const int K = num_e[l] * C;
+          for (int m = 0; m < 2 * l + 1; ++m)
+            for (int kk = 0; kk < K; ++kk) {
+              double s = 0;
+              for (int k = 0; k < C; ++k) s += a[m * C + k] * A1w[l][static_cast<size_t>(kk) * C + k];
+              ph[m * K + kk] = s;
+            }
+          ph += (2 * l + 1) * K;
+          a += (2 * l + 1) * C;
+        }
       }
-    }
+    });
   }
 
   // mace.cpp:759-794
   void stage_M1(int N, const int* ntype) {
     M1.assign(static_cast<size_t>(N) * C, 0.0);
     M1_grad.assign(static_cast<size_t>(N) * nlm * C, 0.0);
-    double x[16], g[16];
-    for (int i = 0; i < N; ++i)
-      for (int k = 0; k < C; ++k) {
-        for (int v = 0; v < nlm; ++v) x[v] = A1[(static_cast<size_t>(i) * nlm + v) * C + k];
-        const double* cf = &P1c[(static_cast<size_t>(ntype[i]) * C + k) * t_max1];
-        M1[static_cast<size_t>(i) * C + k] = poly_eval(P1, cf, x, g, nlm);
-        for (int v = 0; v < nlm; ++v) M1_grad[(static_cast<size_t>(i) * nlm + v) * C + k] = g[v];
-      }
+    par_nodes(N, [&](int i0, int i1) {
+      double x[16], g[16];
+      for (int i = i0; i < i1; ++i)
+        for (int k = 0; k < C; ++k) {
+          for (int v = 0; v < nlm; ++v) x[v] = A1[(static_cast<size_t>(i) * nlm + v) * C + k];
+          const double* cf = &P1c[(static_cast<size_t>(ntype[i]) * C + k) * t_max1];
+          M1[static_cast<size_t>(i) * C + k] = poly_eval(P1, cf, x, g, nlm);
+          for (int v = 0; v < nlm; ++v) M1_grad[(static_cast<size_t>(i) * nlm + v) * C + k] = g[v];
+        }
+    });
   }
   void reverse_M1(int N) {
     A1_adj.assign(static_cast<size_t>(N) * nlm * C, 0.0);
-    for (int i = 0; i < N; ++i)
-      for (int v = 0; v < nlm; ++v)
-        for (int k = 0; k < C; ++k)
-          A1_adj[(static_cast<size_t>(i) * nlm + v) * C + k] =
-              M1_grad[(static_cast<size_t>(i) * nlm + v) * C + k] * M1_adj[static_cast<size_t>(i) * C + k];
+    par_nodes(N, [&](int i0, int i1) {
+      for (int i = i0; i < i1; ++i)
+        for (int v = 0; v < nlm; ++v)
+          for (int k = 0; k < C; ++k)
+            A1_adj[(static_cast<size_t>(i) * nlm + v) * C + k] =
+                M1_grad[(static_cast<size_t>(i) * nlm + v) * C + k] * M1_adj[static_cast<size_t>(i) * C + k];
+    });
   }
 
   // mace.cpp:796-874: H2 = W_H1[type]^T H1[i,0,:] + W_M1^T M1[i]
   void stage_H2(int N, const int* ntype) {
     H2.assign(static_cast<size_t>(N) * C, 0.0);
-    for (int i = 0; i < N; ++i) {
-      const double* W = H2w_H1[ntype[i]].data();
-      for (int c = 0; c < C; ++c) {
-        double s = 0;
-        for (int rr = 0; rr < C; ++rr)
-          s += W[rr * C + c] * H1[static_cast<size_t>(i) * nLM * C + rr] +
-               H2w_M1[rr * C + c] * M1[static_cast<size_t>(i) * C + rr];
-        H2[static_cast<size_t>(i) * C + c] = s;
+    par_nodes(N, [&](int i0, int i1) {
+      for (int i = i0; i < i1; ++i) {
+        const double* W = H2w_H1[ntype[i]].data();
+        for (int c = 0; c < C; ++c) {
+          double s = 0;
+          for (int rr = 0; rr < C; ++rr)
+            s += W[rr * C + c] * H1[static_cast<size_t>(i) * nLM * C + rr] +
+                 H2w_M1[rr * C + c] * M1[static_cast<size_t>(i) * C + rr];
+          H2[static_cast<size_t>(i) * C + c] = s;
+        }
       }
-    }
+    });
   }
   void reverse_H2(int N, const int* ntype) {
     M1_adj.assign(static_cast<size_t>(N) * C, 0.0);
-    for (int i = 0; i < N; ++i) {
-      const double* W = H2w_H1[ntype[i]].data();
-      const double* g = &H2_adj[static_cast<size_t>(i) * C];
-      for (int rr = 0; rr < C; ++rr) {
-        double s1 = 0, s2 = 0;
-        for (int c = 0; c < C; ++c) {
-          s1 += W[rr * C + c] * g[c];
-          s2 += H2w_M1[rr * C + c] * g[c];
+    par_nodes(N, [&](int i0, int i1) {
+      for (int i = i0; i < i1; ++i) {
+        const double* W = H2w_H1[ntype[i]].data();
+        const double* g = &H2_adj[static_cast<size_t>(i) * C];
+        for (int rr = 0; rr < C; ++rr) {
+          double s1 = 0, s2 = 0;
+          for (int c = 0; c < C; ++c) {
+            s1 += W[rr * C + c] * g[c];
+            s2 += H2w_M1[rr * C + c] * g[c];
+          }
+          H1_adj[static_cast<size_t>(i) * nLM * C + rr] += s1;
+          M1_adj[static_cast<size_t>(i) * C + rr] = s2;
         }
-        H1_adj[static_cast<size_t>(i) * nLM * C + rr] += s1;
-        M1_adj[static_cast<size_t>(i) * C + rr] = s2;
       }
-    }
+    });
   }
 
   // mace.cpp:876-903 and multilayer_perceptron.cpp:76-150 (shape {C, 16, 1})
@@ -675,66 +769,69 @@ struct Oracle {
     H1_adj.assign(static_cast<size_t>(N) * nLM * C, 0.0);
     H2_adj.assign(static_cast<size_t>(N) * C, 0.0);
     const int nh = static_cast<int>(ro2_w2.size());
-    vecd hid(nh), act_d(nh);
-    for (int i = 0; i < N; ++i) {
-      double E = e0[ntype[i]];
-      for (int k = 0; k < C; ++k) {
-        E += ro1[k] * H1[static_cast<size_t>(i) * nLM * C + k];
-        H1_adj[static_cast<size_t>(i) * nLM * C + k] = ro1[k];
+    par_nodes(N, [&](int i0, int i1) {
+      vecd act_d(nh);
+      for (int i = i0; i < i1; ++i) {
+        double E = e0[ntype[i]];
+        for (int k = 0; k < C; ++k) {
+          E += ro1[k] * H1[static_cast<size_t>(i) * nLM * C + k];
+          H1_adj[static_cast<size_t>(i) * nLM * C + k] = ro1[k];
+        }
+        const double* x = &H2[static_cast<size_t>(i) * C];
+        double out = 0;
+        for (int u = 0; u < nh; ++u) {
+          double s = 0;
+          for (int k = 0; k < C; ++k) s += ro2_w1[u * C + k] * x[k];
+          const double sg = 1.0 / (1.0 + std::exp(-s));
+          out += ro2_w2[u] * ro2_scale * s * sg;
+          act_d[u] = ro2_w2[u] * (ro2_scale * sg + ro2_scale * s * sg * (1 - sg));
+        }
+        for (int k = 0; k < C; ++k) {
+          double g = 0;
+          for (int u = 0; u < nh; ++u) g += act_d[u] * ro2_w1[u * C + k];
+          H2_adj[static_cast<size_t>(i) * C + k] = g;
+        }
+        node_energies[i] += E + out;
       }
-      const double* x = &H2[static_cast<size_t>(i) * C];
-      double out = 0;
-      for (int u = 0; u < nh; ++u) {
-        double s = 0;
-        for (int k = 0; k < C; ++k) s += ro2_w1[u * C + k] * x[k];
-        const double sg = 1.0 / (1.0 + std::exp(-s));
-        out += ro2_w2[u] * ro2_scale * s * sg;
-        act_d[u] = ro2_w2[u] * (ro2_scale * sg + ro2_scale * s * sg * (1 - sg));
-      }
-      for (int k = 0; k < C; ++k) {
-        double g = 0;
-        for (int u = 0; u < nh; ++u) g += act_d[u] * ro2_w1[u * C + k];
-        H2_adj[static_cast<size_t>(i) * C + k] = g;
-      }
-      node_energies[i] += E + out;
-    }
+    });
   }
 
   // mace.cpp:203-271
-  void reverse_A0(int N, const int* ntype, const int* nneigh, const int* te, const double* xyz, const double* r) {
-    vecd phi_adj(nlm * C);
+  void reverse_A0(int N, const int* ntype, const int* te, const double* xyz, const double* r) {
     const int ns0 = (l_max + 1) * C;
-    long e = 0;
-    for (int i = 0; i < N; ++i) {
-      for (int l = 0; l <= l_max; ++l) {
-        const double* W = A0w[ntype[i]][l].data();
-        for (int lm = l * l; lm < (l + 1) * (l + 1); ++lm)
-          for (int kk = 0; kk < C; ++kk) {
-            double s = 0;
-            for (int k = 0; k < C; ++k) s += A0_adj[(static_cast<size_t>(i) * nlm + lm) * C + k] * W[kk * C + k];
-            phi_adj[lm * C + kk] = s;
-          }
-      }
-      for (int q = 0; q < nneigh[i]; ++q, ++e) {
-        const double* h0 = &H0w[te[e] * C];
-        const double* u = xyz + 3 * e;
-        double f[3] = {0, 0, 0};
+    par_nodes(N, [&](int i0, int i1) {
+      vecd phi_adj(nlm * C);
+      for (int i = i0; i < i1; ++i) {
         for (int l = 0; l <= l_max; ++l) {
-          const double* R = &R0[e * ns0 + l * C];
-          const double* Rd = &R0_deriv[e * ns0 + l * C];
-          for (int lm = l * l; lm < (l + 1) * (l + 1); ++lm) {
-            const double y = Y[e * nlm + lm];
-            const double gy[3] = {Y_grad[(3 * e + 0) * nlm + lm], Y_grad[(3 * e + 1) * nlm + lm],
-                                  Y_grad[(3 * e + 2) * nlm + lm]};
-            for (int k = 0; k < C; ++k) {
-              const double ph = phi_adj[lm * C + k] * h0[k];
-              for (int a = 0; a < 3; ++a) f[a] -= ph * (u[a] / r[e] * Rd[k] * y + R[k] * gy[a]);
+          const double* W = A0w[ntype[i]][l].data();
+          for (int lm = l * l; lm < (l + 1) * (l + 1); ++lm)
+            for (int kk = 0; kk < C; ++kk) {
+              double s = 0;
+              for (int k = 0; k < C; ++k) s += A0_adj[(static_cast<size_t>(i) * nlm + lm) * C + k] * W[kk * C + k];
+              phi_adj[lm * C + kk] = s;
+            }
+        }
+        for (long e = eoff[i]; e < eoff[i + 1]; ++e) {
+          const double* h0 = &H0w[te[e] * C];
+          const double* u = xyz + 3 * e;
+          double f[3] = {0, 0, 0};
+          for (int l = 0; l <= l_max; ++l) {
+            const double* R = &R0[e * ns0 + l * C];
+            const double* Rd = &R0_deriv[e * ns0 + l * C];
+            for (int lm = l * l; lm < (l + 1) * (l + 1); ++lm) {
+              const double y = Y[e * nlm + lm];
+              const double gy[3] = {Y_grad[(3 * e + 0) * nlm + lm], Y_grad[(3 * e + 1) * nlm + lm],
+                                    Y_grad[(3 * e + 2) * nlm + lm]};
+              for (int k = 0; k < C; ++k) {
+                const double ph = phi_adj[lm * C + k] * h0[k];
+                for (int a = 0; a < 3; ++a) f[a] -= ph * (u[a] / r[e] * Rd[k] * y + R[k] * gy[a]);
+              }
             }
           }
+          for (int a = 0; a < 3; ++a) node_forces[3 * e + a] += f[a];
         }
-        for (int a = 0; a < 3; ++a) node_forces[3 * e + a] += f[a];
       }
-    }
+    });
   }
 
   vecd* buffer(const std::string& n) {
@@ -787,6 +884,9 @@ void orc_free(void* h) { delete static_cast<Oracle*>(h); }
 // An independent evaluator sharing nothing with h (copies the loaded model), so
 // several threads can evaluate in parallel without re-reading the model file.
 void* orc_clone(void* h) { return new Oracle(*static_cast<Oracle*>(h)); }
+
+// Worker threads one evaluation uses (1: serial).
+void orc_set_threads(void* h, int n) { static_cast<Oracle*>(h)->nthreads = n < 1 ? 1 : n; }
 
 int orc_info(void* h, int* out) {
   auto* o = static_cast<Oracle*>(h);

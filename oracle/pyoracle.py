@@ -38,6 +38,8 @@ def library(which="port"):
         f("clone").restype = P
         f("clone").argtypes = [P]
     f("info").argtypes = [P, ip]
+    if pre == "orc_":
+        f("set_threads").argtypes = [P, I]
     f("compute").restype = I
     f("compute").argtypes = [P, I, ip, ip, ip, ip, L, dp, dp]
     f("get").restype = L
@@ -83,6 +85,14 @@ class Evaluator:
         if self.pre != "orc_":
             raise ValueError("clone() is available for the port only")
         return Evaluator(None, "port", _clone_of=self)
+
+    def set_threads(self, n):
+        """Split each stage of one evaluation over n threads (port only; same results bit
+        for bit as a serial evaluation)."""
+        if self.pre != "orc_":
+            raise ValueError("set_threads() is available for the port only")
+        getattr(self.lib, "orc_set_threads")(self.h, int(n))
+        return self
 
     def __del__(self):
         if getattr(self, "h", None):

@@ -337,6 +337,24 @@ struct Oracle {
   // depend on the thread count, bit for bit.
   int nthreads = 1;
   std::vector<long> eoff;  // [N+1] first edge of each node
+  // lean: the radials R0, R1 and their derivatives are not stored per edge (the
+  // reference's layout, ~20 KB per edge) but evaluated where each stage needs them, by
+  // the same spline code: the same numbers, in far less memory (large boxes)
+  bool lean = false;
+  // R, R' of edge e (centre type ti, neighbour type tj): the stored row, or (lean) the
+  // spline evaluated into the caller's buffers
+  void radial_row(const std::vector<SplineSet>& spl, const vecd& R, const vecd& Rd, int ti, int tj, long e, double r,
+                  double* bR, double* bRd, const double*& pR, const double*& pRd) const {
+    const size_t ns = spl[0].ns;
+    if (!lean) {
+      pR = &R[e * ns];
+      pRd = &Rd[e * ns];
+      return;
+    }
+    spl[pair_index(ti, tj)].eval(r, bR, bRd);
+    pR = bR;
+    pRd = bRd;
+  }
   template <typename F>
   void par_nodes(int N, F&& f) {  // f(i0, i1) over disjoint node ranges
     const int T = std::max(1, std::min(nthreads, N / 4));
@@ -374,12 +392,12 @@ struct Oracle {
     if (has_zbl) zbl_stage(N, ntype, ntypes_e, xyz, r);
     stage_Y(N, E, xyz);
     stage_R(N, ntype, ntypes_e, r, spl0, R0, R0_deriv);
-    stage_A0(N, ntype, ntypes_e);
+    stage_A0(N, ntype, ntypes_e, r);
     scale_fwd(N, ntype, ntypes_e, r, A0_scaled, A0s, A0);
     stage_M0(N, ntype);
     stage_H1(N);
     stage_R(N, ntype, ntypes_e, r, spl1, R1, R1_deriv);
-    stage_Phi1(N, nidx);
+    stage_Phi1(N, ntype, nidx, ntypes_e, r);
     stage_A1(N);
     scale_fwd(N, ntype, ntypes_e, r, A1_scaled, A1s, A1);
     stage_M1(N, ntype);
@@ -389,7 +407,7 @@ struct Oracle {
     reverse_M1(N);
     scale_rev(N, ntype, ntypes_e, xyz, r, A1_scaled, A1s, A1, A1_adj);
     reverse_A1(N);
-    reverse_Phi1(N, nidx, xyz, r);
+    reverse_Phi1(N, ntype, nidx, ntypes_e, xyz, r);
     reverse_H1(N);
     reverse_M0(N);
     scale_rev(N, ntype, ntypes_e, xyz, r, A0_scaled, A0s, A0, A0_adj);
@@ -422,6 +440,11 @@ struct Oracle {
                vecd& Rd) {
     const int ns = spl[0].ns;
     const long E = eoff[N];
+    if (lean) {
+      R.clear();
+      Rd.clear();
+      return;
+    }
     R.assign(E * ns, 0.0);
     Rd.assign(E * ns, 0.0);
     par_nodes(N, [&](int i0, int i1) {
@@ -432,16 +455,18 @@ struct Oracle {
   }
 
   // mace.cpp:150-201: Phi0 = sum_j R0 Y H0[type_j], then per-l channel mixing
-  void stage_A0(int N, const int* ntype, const int* te) {
+  void stage_A0(int N, const int* ntype, const int* te, const double* r) {
     A0.assign(static_cast<size_t>(N) * nlm * C, 0.0);
     par_nodes(N, [&](int i0, int i1) {
-      vecd phi0(nlm * C);
+      vecd phi0(nlm * C), bR(spl0[0].ns), bRd(spl0[0].ns);
       for (int i = i0; i < i1; ++i) {
         std::fill(phi0.begin(), phi0.end(), 0.0);
         for (long e = eoff[i]; e < eoff[i + 1]; ++e) {
           const double* h0 = &H0w[te[e] * C];
+          const double *R0e, *R0de;
+          radial_row(spl0, R0, R0_deriv, ntype[i], te[e], e, r[e], bR.data(), bRd.data(), R0e, R0de);
           for (int l = 0; l <= l_max; ++l) {
-            const double* rl = &R0[e * (l_max + 1) * C + l * C];
+            const double* rl = R0e + l * C;
             for (int lm = l * l; lm < (l + 1) * (l + 1); ++lm) {
               const double y = Y[e * nlm + lm];
               for (int k = 0; k < C; ++k) phi0[lm * C + k] += rl[k] * y * h0[k];
@@ -558,18 +583,20 @@ struct Oracle {
   void reverse_H1(int N) { mix(N, H1_adj, M0_adj, H1w, L_max, nLM, true); }
 
   // mace.cpp:453-502
-  void stage_Phi1(int N, const int* nidx) {
-    const int ns1 = spl1[0].ns;
+  void stage_Phi1(int N, const int* ntype, const int* nidx, const int* te, const double* r) {
     Phi1r.assign(static_cast<size_t>(N) * n_p * C, 0.0);
     Phi1.assign(static_cast<size_t>(N) * n_lme * C, 0.0);
     par_nodes(N, [&](int i0, int i1) {
+      vecd bR(spl1[0].ns), bRd(spl1[0].ns);
       for (int i = i0; i < i1; ++i) {
         double* out = &Phi1r[static_cast<size_t>(i) * n_p * C];
         for (long e = eoff[i]; e < eoff[i + 1]; ++e) {
           const double* hj = &H1[static_cast<size_t>(nidx[e]) * nLM * C];
+          const double *R1e, *R1de;
+          radial_row(spl1, R1, R1_deriv, ntype[i], te[e], e, r[e], bR.data(), bRd.data(), R1e, R1de);
           int p = 0;
           for (size_t ins = 0; ins < phi_l.size(); ++ins) {
-            const double* R = &R1[e * ns1 + ins * C];
+            const double* R = R1e + ins * C;
             const int l1 = phi_l1[ins], l2 = phi_l2[ins];
             for (int lm1 = l1 * l1; lm1 < (l1 + 1) * (l1 + 1); ++lm1) {
               const double y = Y[e * nlm + lm1];
@@ -589,8 +616,7 @@ struct Oracle {
   // mace.cpp:504-605: node_forces of every edge i->j, and H1_adj[j] += R1 Y dPhi1r[i].
   // The H1_adj sums are formed per node j over its incoming edges in ascending edge
   // order, the order a serial pass over the edges adds them in.
-  void reverse_Phi1(int N, const int* nidx, const double* xyz, const double* r) {
-    const int ns1 = spl1[0].ns;
+  void reverse_Phi1(int N, const int* ntype, const int* nidx, const int* te, const double* xyz, const double* r) {
     const long E = eoff[N];
     dPhi1r.assign(static_cast<size_t>(N) * n_p * C, 0.0);
     par_nodes(N, [&](int i0, int i1) {
@@ -601,16 +627,19 @@ struct Oracle {
                 phi_cg[t] * dPhi1[(static_cast<size_t>(i) * n_lme + phi_lme[t]) * C + k];
     });
     par_nodes(N, [&](int i0, int i1) {
+      vecd bR(spl1[0].ns), bRd(spl1[0].ns);
       for (int i = i0; i < i1; ++i) {
         const double* g = &dPhi1r[static_cast<size_t>(i) * n_p * C];
         for (long e = eoff[i]; e < eoff[i + 1]; ++e) {
           const double* hj = &H1[static_cast<size_t>(nidx[e]) * nLM * C];
           const double* u = xyz + 3 * e;
+          const double *R1e, *R1de;
+          radial_row(spl1, R1, R1_deriv, ntype[i], te[e], e, r[e], bR.data(), bRd.data(), R1e, R1de);
           double f[3] = {0, 0, 0};
           int p = 0;
           for (size_t ins = 0; ins < phi_l.size(); ++ins) {
-            const double* R = &R1[e * ns1 + ins * C];
-            const double* Rd = &R1_deriv[e * ns1 + ins * C];
+            const double* R = R1e + ins * C;
+            const double* Rd = R1de + ins * C;
             const int l1 = phi_l1[ins], l2 = phi_l2[ins];
             for (int lm1 = l1 * l1; lm1 < (l1 + 1) * (l1 + 1); ++lm1) {
               const double y = Y[e * nlm + lm1];
@@ -641,14 +670,17 @@ struct Oracle {
       for (long e = 0; e < E; ++e) in_e[fill[nidx[e]]++] = e;
     }
     par_nodes(N, [&](int j0, int j1) {
+      vecd bR(spl1[0].ns), bRd(spl1[0].ns);
       for (int j = j0; j < j1; ++j) {
         double* aj = &H1_adj[static_cast<size_t>(j) * nLM * C];
         for (long q = in_off[j]; q < in_off[j + 1]; ++q) {
           const long e = in_e[q];
           const double* g = &dPhi1r[static_cast<size_t>(src[e]) * n_p * C];
+          const double *R1e, *R1de;
+          radial_row(spl1, R1, R1_deriv, ntype[src[e]], te[e], e, r[e], bR.data(), bRd.data(), R1e, R1de);
           int p = 0;
           for (size_t ins = 0; ins < phi_l.size(); ++ins) {
-            const double* R = &R1[e * ns1 + ins * C];
+            const double* R = R1e + ins * C;
             const int l1 = phi_l1[ins], l2 = phi_l2[ins];
             for (int lm1 = l1 * l1; lm1 < (l1 + 1) * (l1 + 1); ++lm1) {
               const double y = Y[e * nlm + lm1];
@@ -798,9 +830,8 @@ struct Oracle {
 
   // mace.cpp:203-271
   void reverse_A0(int N, const int* ntype, const int* te, const double* xyz, const double* r) {
-    const int ns0 = (l_max + 1) * C;
     par_nodes(N, [&](int i0, int i1) {
-      vecd phi_adj(nlm * C);
+      vecd phi_adj(nlm * C), bR(spl0[0].ns), bRd(spl0[0].ns);
       for (int i = i0; i < i1; ++i) {
         for (int l = 0; l <= l_max; ++l) {
           const double* W = A0w[ntype[i]][l].data();
@@ -814,10 +845,12 @@ struct Oracle {
         for (long e = eoff[i]; e < eoff[i + 1]; ++e) {
           const double* h0 = &H0w[te[e] * C];
           const double* u = xyz + 3 * e;
+          const double *R0e, *R0de;
+          radial_row(spl0, R0, R0_deriv, ntype[i], te[e], e, r[e], bR.data(), bRd.data(), R0e, R0de);
           double f[3] = {0, 0, 0};
           for (int l = 0; l <= l_max; ++l) {
-            const double* R = &R0[e * ns0 + l * C];
-            const double* Rd = &R0_deriv[e * ns0 + l * C];
+            const double* R = R0e + l * C;
+            const double* Rd = R0de + l * C;
             for (int lm = l * l; lm < (l + 1) * (l + 1); ++lm) {
               const double y = Y[e * nlm + lm];
               const double gy[3] = {Y_grad[(3 * e + 0) * nlm + lm], Y_grad[(3 * e + 1) * nlm + lm],
@@ -887,6 +920,10 @@ void* orc_clone(void* h) { return new Oracle(*static_cast<Oracle*>(h)); }
 
 // Worker threads one evaluation uses (1: serial).
 void orc_set_threads(void* h, int n) { static_cast<Oracle*>(h)->nthreads = n < 1 ? 1 : n; }
+
+// 1: evaluate the radials where they are used instead of storing them per edge (large
+// boxes; the R0/R1 stage buffers are then empty).  Same results bit for bit.
+void orc_set_lean(void* h, int on) { static_cast<Oracle*>(h)->lean = on != 0; }
 
 int orc_info(void* h, int* out) {
   auto* o = static_cast<Oracle*>(h);

@@ -40,6 +40,7 @@ def library(which="port"):
     f("info").argtypes = [P, ip]
     if pre == "orc_":
         f("set_threads").argtypes = [P, I]
+        f("set_lean").argtypes = [P, I]
     f("compute").restype = I
     f("compute").argtypes = [P, I, ip, ip, ip, ip, L, dp, dp]
     f("get").restype = L
@@ -92,6 +93,14 @@ class Evaluator:
         if self.pre != "orc_":
             raise ValueError("set_threads() is available for the port only")
         getattr(self.lib, "orc_set_threads")(self.h, int(n))
+        return self
+
+    def set_lean(self, on=True):
+        """Evaluate the radials where they are used instead of storing them per edge (port
+        only; for boxes whose per-edge radial rows would not fit in memory).  Same results."""
+        if self.pre != "orc_":
+            raise ValueError("set_lean() is available for the port only")
+        getattr(self.lib, "orc_set_lean")(self.h, 1 if on else 0)
         return self
 
     def __del__(self):

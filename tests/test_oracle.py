@@ -60,15 +60,16 @@ def test_small_golden_matches_reference_outputs(small_model_path, small_golden):
     np.testing.assert_allclose(ev.node_forces, g["node_forces"], rtol=1e-8, atol=1e-10)
 
 
-@pytest.mark.parametrize("threads", [2, 5])
-def test_threaded_evaluation_is_bitwise_serial(small_model_path, small_golden, threads):
-    """One evaluation split over node ranges (the H1_adj scatter as an ordered gather)
-    gives the serial result bit for bit, stage buffers included."""
+@pytest.mark.parametrize("threads,lean", [(2, False), (5, False), (3, True)])
+def test_threaded_evaluation_is_bitwise_serial(small_model_path, small_golden, threads, lean):
+    """One evaluation split over node ranges (the H1_adj scatter as an ordered gather),
+    and the lean form that evaluates the radials where they are used, give the serial
+    result bit for bit, stage buffers included."""
     g = small_golden
     species = g["species"].astype(np.int32)
     nl = {k: g[k] for k in ("num_neigh", "neigh_indices", "xyz", "r")}
     serial = Evaluator(small_model_path, "port")
-    par = Evaluator(small_model_path, "port").set_threads(threads)
+    par = Evaluator(small_model_path, "port").set_threads(threads).set_lean(lean)
     for ev in (serial, par):
         ev.compute_node_energies_forces(*edge_args(species, nl))
     for name in ("node_energies", "node_forces", "A0", "M0", "H1", "Phi1", "A1", "M1", "H2", "H2_adj", "M1_adj",

@@ -8,8 +8,8 @@ distance 0.9 A, seeded random insertion) with a seeded random 2-layer MACE of
 p=5 envelope tabulated on 200 spline knots.  Synthetic data: no public dataset or
 checkpoint is involved.
 
-The model carries MACE's ZBL pair repulsion (the random synthetic potential has no
-short-range core of its own, and MD needs one).
+The model has no ZBL pair repulsion and no density normalisation, as the
+configuration states.
 
 A step is one velocity-Verlet MD step of the whole box (dt 0.5 fs, Maxwell-Boltzmann
 velocities at 300 K): edge geometry, the full E+F evaluation (forward and adjoint
@@ -20,8 +20,11 @@ the engine's stream).  No L2 flush between steps: the working set of a step (spl
 tables, node features and adjoints, edge arrays) is several times the 129 MB L2.
 Both forms run the same MD: `value` is the BF16-mixed form (channel-mixing GEMMs on
 the tcgen05 tensor cores with bf16 split operands), `forms` holds both forms'
-throughput and their energy / force / virial errors against the float64 oracle on a
-256-atom box of the same model (the CPU baseline's sample).
+throughput and their energy / force / virial errors against the float64 oracle on
+the timed structure itself (the full box; for the 32768- and 1,048,576-atom shapes a
+4096-atom box of the same model, density and species mix, and with --full-check the
+whole 32768-atom box).  The CPU baseline is the same float64 oracle evaluating that
+structure on all host threads (and one thread on a 256-atom box).
 `e2e` is the same metric through the host-pointer C ABI evaluator call a LAMMPS/ASE
 caller makes every step (host->device copy of the neighbour list and device->host
 copy of energies and forces inside the timed region).  Per-kernel times for the
@@ -29,6 +32,10 @@ roofline come from engine CUDA events over a separate pass of evaluation steps o
 the same structure, with L2 flushed between those steps.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                       [--workload fp32_4096|precision_32768|large_1m|molecules]
+                       [--detail PATH] [--full-check]
+--detail writes the long form of the result (per-stage FLOP and byte rates, MD energy
+record, schedules) to PATH; stdout carries one compact line.
 Multi-GPU (torchrun): every rank evaluates its own replica of the box (the
 engine does not shard one box over GPUs); value is the job's total.
 """
@@ -52,20 +59,21 @@ UNIT = "atom-steps/s"
 WORKLOADS = {
     # the headline: 4096 atoms, 128x0e+128x1o, H/C/N/O, r_cut 5
     "fp32_4096": dict(name="fp32_4096", config="fp32_4096", n_atoms=4096, density=0.10, min_dist=0.9, n_species=4,
-                      r_cut=5.0, model_seed=1, struct_seed=2, cpu_sample_atoms=256,
+                      r_cut=5.0, model_seed=1, struct_seed=2, cpu_sample_atoms=256, err_atoms=None,
                       text="fp32_4096: periodic box, 4096 atoms, 0.10 atoms/A^3, H/C/N/O, 128x0e+128x1o, l_max 3, "
-                           "correlation 3, r_cut 5 A, 200 spline knots, ZBL"),
+                           "correlation 3, r_cut 5 A, 200 spline knots"),
     # the precision-form shape: 32768 atoms, 128x0e+128x1o+128x2e, 10 species, r_cut 6
     # the large single system: 1,048,576 atoms, 128x0e+128x1o, 10 species, r_cut 5 (MD only)
     "large_1m": dict(name="large_1m", config="large_1m", n_atoms=1048576, density=0.10, min_dist=0.9, n_species=10,
-                     r_cut=5.0, model_seed=1, struct_seed=2, cpu_sample_atoms=128,
+                     r_cut=5.0, model_seed=1, struct_seed=2, cpu_sample_atoms=128, err_atoms=4096,
                      text="large_1m: periodic box, 1,048,576 atoms, 0.10 atoms/A^3, 10 species, 128x0e+128x1o, "
-                          "l_max 3, correlation 3, r_cut 5 A, 200 spline knots, ZBL"),
+                          "l_max 3, correlation 3, r_cut 5 A, 200 spline knots"),
     "precision_32768": dict(name="precision_32768", config="bf16_32768", n_atoms=32768, density=0.09, min_dist=0.9,
                             n_species=10, r_cut=6.0, model_seed=1, struct_seed=2, cpu_sample_atoms=128,
+                            err_atoms=4096,
                             text="precision_32768: periodic box, 32768 atoms, 0.09 atoms/A^3, 10 species, "
                                  "128x0e+128x1o+128x2e (L_max 2), l_max 3, correlation 3, r_cut 6 A, 200 spline "
-                                 "knots, ZBL"),
+                                 "knots"),
 }
 WORKLOAD = WORKLOADS["fp32_4096"]
 CACHE = os.path.join(tempfile.gettempdir(), "smx_bench")
@@ -81,10 +89,10 @@ def log(*a):
 def model_path():
     from symmetrix_gb300.synth.model import CONFIGS, make_model, write_model
     os.makedirs(CACHE, exist_ok=True)
-    path = os.path.join(CACHE, f"model_{WORKLOAD['name']}_zbl_s{WORKLOAD['model_seed']}.json")
+    path = os.path.join(CACHE, f"model_{WORKLOAD['name']}_s{WORKLOAD['model_seed']}.json")
     if not os.path.exists(path):
         t = time.time()
-        model = make_model(**CONFIGS[WORKLOAD["config"]], seed=WORKLOAD["model_seed"], zbl=True)
+        model = make_model(**CONFIGS[WORKLOAD["config"]], seed=WORKLOAD["model_seed"])
         json.dump(dims_of(model), open(path + ".dims.json", "w"))
         write_model(model, path + ".tmp")
         del model
@@ -209,60 +217,48 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
-# CPU baseline (the oracle: reference build where present, else the port)
+# the float64 oracle: the error reference and the CPU baseline
 # ---------------------------------------------------------------------------
-def cpu_evaluators(path, threads):
-    """The reference's own evaluator (oracle/_ref) where it was built here, else the port."""
-    from oracle import build as ob
+def host_threads():
+    return len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+
+
+def edge_tuple(species, nl):
+    return (len(species), species, nl["num_neigh"], nl["neigh_indices"], species[nl["neigh_indices"]], nl["xyz"],
+            nl["r"])
+
+
+def sig(x, n=4):
+    """x rounded to n significant digits (keeps the JSON line short)."""
+    return float(f"{x:.{n}g}") if x is not None else None
+
+
+def oracle_eval(path, a, threads, repeats=0, lean=None):
+    """The float64 oracle's result for one structure, evaluated on `threads` host threads
+    (each stage split over node ranges, bitwise equal to one thread), and with repeats > 0
+    the median time of `repeats` evaluations after one warm-up.  The radials are stored per
+    edge as the reference does unless that would take more than 16 GB (lean)."""
     from oracle.pyoracle import Evaluator
-    if os.path.exists(ob.REF_SO) and os.path.isdir(ob.REF_SRC):
-        evs = [None] * threads
-
-        def load(q):
-            evs[q] = Evaluator(path, "reference")
-
-        ths = [threading.Thread(target=load, args=(q,)) for q in range(threads)]
-        for th in ths:
-            th.start()
-        for th in ths:
-            th.join()
-        return "reference", evs
-    ev = Evaluator(path, "port")
-    return "port", [ev] + [ev.clone() for _ in range(threads - 1)]
-
-
-def cpu_rate(path, threads, repeats, n_atoms):
-    """atom-steps/s of `threads` independent evaluations of an n_atoms sub-box; also the
-    sub-box and the float64 result (the error reference of the GPU forms)."""
-    kind, evs = cpu_evaluators(path, threads)
-    pos, L, species, nl = structure(n_atoms, WORKLOAD["struct_seed"] + 100)
-    args = (n_atoms, species, nl["num_neigh"], nl["neigh_indices"], species[nl["neigh_indices"]], nl["xyz"], nl["r"])
-
-    def run(ev):
-        ev.compute_node_energies_forces(*args)
-
+    ev = Evaluator(path, "port").set_threads(threads)
+    if lean is None:
+        lean = len(a[6]) * ev.num_channels * 17 * 16 > 16e9
+    ev.set_lean(lean)
     times = []
-    for rep in range(repeats + 1):
+    for _ in range(repeats + 1):
         t = time.perf_counter()
-        ths = [threading.Thread(target=run, args=(ev,)) for ev in evs]
-        for th in ths:
-            th.start()
-        for th in ths:
-            th.join()
-        if rep > 0:
-            times.append(time.perf_counter() - t)
-    dt = statistics.median(times)
-    ref = {"node_energies": np.array(evs[0].node_energies), "node_forces": np.array(evs[0].node_forces)}
-    return kind, threads * n_atoms / dt, dt, len(nl["r"]), (args, nl, ref)
+        ev.compute_node_energies_forces(*a)
+        times.append(time.perf_counter() - t)
+    ref = {"node_energies": np.array(ev.node_energies), "node_forces": np.array(ev.node_forces)}
+    return ref, (statistics.median(times[1:]) if repeats > 0 else times[0])
 
 
-def form_errors(eng, sample):
-    """Errors of one GPU form against the float64 oracle on the CPU sample box."""
-    args, nl, ref = sample
-    eng.compute_node_energies_forces(*args)
-    n = args[0]
-    e, f = np.asarray(eng.node_energies), np.asarray(eng.node_forces).reshape(-1, 3)
-    er, fr = ref["node_energies"], ref["node_forces"].reshape(-1, 3)
+def errors(e, f, ref, nl):
+    """Energy, force and virial errors of GPU outputs (node energies, per-edge forces)
+    against the float64 oracle's for the same structure."""
+    n = len(e)
+    f = np.asarray(f).reshape(-1, 3)
+    fr = ref["node_forces"].reshape(-1, 3)
+    er = ref["node_energies"]
 
     def atomic(fe):
         F = np.zeros((n, 3))
@@ -275,11 +271,11 @@ def form_errors(eng, sample):
         return -(x[:, :, None] * fe[:, None, :]).sum(0)
 
     dF = np.abs(atomic(f) - atomic(fr))
-    return {"energy_per_atom_eV": abs(e.sum() - er.sum()) / n, "max_node_energy_eV": float(np.abs(e - er).max()),
-            "max_force_eV_per_A": float(dF.max()), "rms_force_eV_per_A": float(np.sqrt((dF ** 2).mean())),
-            "max_edge_force_eV_per_A": float(np.abs(f - fr).max()),
-            "max_virial_eV": float(np.abs(virial(f) - virial(fr)).max()),
-            "sample": f"{n}-atom box of the same model, density and species mix, vs the float64 oracle"}
+    return {"energy_per_atom_eV": sig(abs(np.sum(e) - er.sum()) / n, 3),
+            "max_node_energy_eV": sig(float(np.abs(np.asarray(e) - er).max()), 3),
+            "max_force_eV_per_A": sig(float(dF.max()), 3), "rms_force_eV_per_A": sig(float(np.sqrt((dF ** 2).mean())), 3),
+            "max_edge_force_eV_per_A": sig(float(np.abs(f - fr).max()), 3),
+            "max_virial_eV": sig(float(np.abs(virial(f) - virial(fr)).max()), 3)}
 
 
 def cpu_model():
@@ -299,39 +295,34 @@ def cpu_model():
 
 
 def reference_arm(args, rank, world):
+    """The CPU path: the float64 oracle (restatement of libsymmetrix/source/mace.cpp)
+    evaluating the GPU arm's structure on all host threads, one evaluation per step."""
     if rank != 0:
         return
     path = model_path()
-    threads = os.cpu_count() or 1
-    n = WORKLOAD["cpu_sample_atoms"]
-    kind, evs = cpu_evaluators(path, threads)
-    pos, L, species, nl = structure(n, WORKLOAD["struct_seed"] + 100)
-    a = (n, species, nl["num_neigh"], nl["neigh_indices"], species[nl["neigh_indices"]], nl["xyz"], nl["r"])
-
-    def step():
-        ths = [threading.Thread(target=ev.compute_node_energies_forces, args=a) for ev in evs]
-        for th in ths:
-            th.start()
-        for th in ths:
-            th.join()
-
+    threads = host_threads()
+    n = WORKLOAD["err_atoms"] or WORKLOAD["n_atoms"]
+    full = n == WORKLOAD["n_atoms"]
+    pos, L, species, nl = structure(n, WORKLOAD["struct_seed"] + (0 if full else 100))
+    from oracle.pyoracle import Evaluator
+    ev = Evaluator(path, "port").set_threads(threads)
+    a = edge_tuple(species, nl)
     for _ in range(args.warmup):
-        step()
+        ev.compute_node_energies_forces(*a)
     t = time.perf_counter()
     for _ in range(args.steps):
-        step()
+        ev.compute_node_energies_forces(*a)
     dt = (time.perf_counter() - t) / args.steps
-    value = threads * n / dt
-    sample = (f"{threads} threads, each one E+F evaluation per step of a {n}-atom box of the same model, density "
-              f"and species mix ({len(nl['r'])} edges); " + ("the reference's libsymmetrix/source/mace.cpp built "
-              "from its sources" if kind == "reference" else "float64 oracle restatement of libsymmetrix/source/"
-              "mace.cpp"))
+    value = n / dt
+    sample = (f"one E+F evaluation per step of the {n}-atom box " + ("the GPU arm times" if full else
+              "of the same model, density and species mix") + f" ({len(nl['r'])} edges), float64 oracle "
+              f"restatement of libsymmetrix/source/mace.cpp, each stage split over {threads} host threads")
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD["name"], "atoms_per_step": n * threads, "threads": threads},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample,
+        "config": {"workload": WORKLOAD["name"], "atoms_per_step": n, "threads": threads},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
                          "cpu": cpu_model()},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
@@ -382,11 +373,11 @@ def time_md(eng, pos, species, masses, L, vel, args, dist, estream):
                 "T_after_warmup_K": kelvin(stw["velocities"]),
                 "E_total_end": st1["potential_energy"] + ke(st1["velocities"]),
                 "T_end_K": kelvin(st1["velocities"]), "edges_skin_list": md.num_edges,
-                "note": "random-weight synthetic potential on a random-insertion box: forces of a few eV/A "
-                        "turn potential into kinetic energy from the first step, and once the structure "
-                        "collapses (beyond ~10 fs) close encounters break energy conservation at dt 0.5 fs, "
-                        "so E_total_end and T_end_K of a long run say nothing about the integrator; "
-                        "the per-step work (the skin-list edges) stays the same"}
+                "note": "random-weight synthetic potential (no short-range repulsion) on a random-insertion "
+                        "box: forces of a few eV/A turn potential into kinetic energy from the first step, pairs "
+                        "close to ~0.1 A within ~12 fs, and close encounters then break energy conservation at "
+                        "dt 0.5 fs, so E_total_end and T_end_K of a long run say nothing about the integrator; "
+                        "the per-step work (the skin-list edges) stays about the same"}
     del md
     return T, t_wall, clk, md_check
 
@@ -522,13 +513,40 @@ def gpu_arm(args, rank, world, local_rank):
             dist.destroy_process_group()
         return
 
-    # ---- CPU baseline (the oracle, one thread, bounded sample) and the error report ----
-    kind, cpu_val, cpu_dt, cpu_edges, sample = cpu_rate(path, 1, 2, WORKLOAD["cpu_sample_atoms"])
-    cpu = {"value": cpu_val, "unit": UNIT, "cores": 1, "kind": kind, "cpu": cpu_model(),
-           "sample": f"median of 2 E+F evaluations of a {WORKLOAD['cpu_sample_atoms']}-atom box of the same model, "
-                     f"density and species mix ({cpu_edges} edges), float64, 1 thread"}
-    for form in forms.values():
-        form["errors"] = form_errors(form["eng"], sample)
+    # ---- errors against the float64 oracle on the timed structure (or a 4096-atom box of
+    # the same model for the larger shapes), and the CPU baseline on that structure ----
+    threads = host_threads()
+    err_n = WORKLOAD["err_atoms"] or N
+    if err_n == N:
+        nl_err, a_err = nl, edge_tuple(species, nl)
+        err_box = f"the timed {N}-atom structure ({E} edges)"
+    else:
+        _, _, sp_e, nl_err = structure(err_n, WORKLOAD["struct_seed"] + 100)
+        a_err = edge_tuple(sp_e, nl_err)
+        err_box = f"a {err_n}-atom box of the same model, density and species mix ({len(nl_err['r'])} edges)"
+    ref, t_cpu = oracle_eval(path, a_err, threads, repeats=3)
+    errs = {"box": err_box}
+    for name, form in forms.items():
+        form["eng"].compute_node_energies_forces(*a_err)
+        errs[name] = errors(form["eng"].node_energies, form["eng"].node_forces, ref, nl_err)
+    del ref
+    if args.full_check and err_n != N:  # the whole timed box against the oracle (lean radials)
+        t = time.time()
+        ref_full, _ = oracle_eval(path, edge_tuple(species, nl), threads, lean=True)
+        errs_full = {"box": f"the timed {N}-atom structure ({E} edges)"}
+        for name, form in forms.items():
+            form["eng"].compute_node_energies_forces(*edge_tuple(species, nl))
+            errs_full[name] = errors(form["eng"].node_energies, form["eng"].node_forces, ref_full, nl)
+        del ref_full
+        log(f"full-box oracle check in {time.time() - t:.0f} s")
+    _, _, sp1, nl1 = structure(WORKLOAD["cpu_sample_atoms"], WORKLOAD["struct_seed"] + 100)
+    _, t_one = oracle_eval(path, edge_tuple(sp1, nl1), 1, repeats=2)
+    cpu = {"value": err_n / t_cpu, "unit": UNIT, "cores": threads, "kind": "port", "cpu": cpu_model(),
+           "sample": f"median of 3 E+F evaluations after 1 warm-up of {err_box}, float64 oracle restatement of "
+                     f"libsymmetrix/source/mace.cpp, each stage split over {threads} host threads",
+           "single_core": {"value": sig(WORKLOAD["cpu_sample_atoms"] / t_one),
+                           "sample": f"{WORKLOAD['cpu_sample_atoms']}-atom box, 1 thread, median of 2 after 1 "
+                                     "warm-up"}}
 
     # ---- roofline of the dominant kernel (headline form) ----
     costs = stage_costs(dims, N, E)
@@ -549,12 +567,12 @@ def gpu_arm(args, rank, world, local_rank):
     # DRAM bytes per launch of the dominant kernel from one ncu capture of this build
     # (dram__bytes_read.sum + dram__bytes_write.sum), where one exists for the workload
     traffic = NCU_TRAFFIC.get((WORKLOAD["name"], dom))
-    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": achieved / hbm, "peak_source": peak_src,
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": sig(achieved), "peak": hbm, "unit": "GB/s",
+                "frac": sig(achieved / hbm), "peak_source": peak_src,
                 "traffic": traffic[0] if traffic else None, "traffic_source": traffic[1] if traffic else None,
-                "algorithmic_bytes_per_launch": bytes_, "avg_launch_ms": avg[dom],
-                "fp32_simt": {"achieved_tflops": flops / t_dom / 1e12, "peak_tflops": fp32_peak,
-                              "frac": flops / t_dom / 1e12 / fp32_peak,
+                "algorithmic_bytes_per_launch": bytes_, "avg_launch_ms": sig(avg[dom]),
+                "fp32_simt": {"achieved_tflops": sig(flops / t_dom / 1e12), "peak_tflops": sig(fp32_peak),
+                              "frac": sig(flops / t_dom / 1e12 / fp32_peak),
                               "peak_source": "152 SMs x 128 FP32 lanes x 2 x median SM clock under load"}}
 
     def per_stage(a):
@@ -564,9 +582,10 @@ def gpu_arm(args, rank, world, local_rank):
     # kernels per MD step of the BF16 form: vv_first, edge geometry with the in-cut-off packing,
     # the scatter of the packed forces, atom_forces, vv_second and 11
     # evaluation kernels (layer0_fwd, layer1_fwd, node_tail, layer1_rev, contract0_rev, layer0_rev,
-    # four grouped tcgen05 GEMM launches: H1, A1 (all l), Phi1_adj (all l), M0_adj, and the bf16
-    # conversion of H1_adj), one more when the centre atoms are species-sorted; plus per rebuild:
-    # wrap, 4 cell-list kernels, 2 neighbour passes, scan, reverse map
+    # four grouped tcgen05 GEMM launches: H1, A1 (all l), Phi1_adj (all l), M0_adj, and the
+    # H1_adj rows' conversion to the M0_adj GEMM's operand), one more when the centre atoms
+    # are species-sorted; plus per rebuild: wrap, 4 cell-list kernels, 2 neighbour passes,
+    # scan, reverse map
     rebuilds = (args.warmup + args.steps + 9) // 10 - (args.warmup + 9) // 10
     per_step = 5 + 11 + (1 if eng.get_option("species_order") == 1 else 0)
     launches = per_step * args.steps + 9 * rebuilds
@@ -575,35 +594,36 @@ def gpu_arm(args, rank, world, local_rank):
         "metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": head["T"] / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
-        "config": {"workload": WORKLOAD["text"],
-                   "atoms": N, "edges_r_cut": E,
-                   "form": "BF16-mixed: channel-mixing GEMMs on tcgen05 with bf16 split operands (3 terms) and "
-                           "f32 accumulation; radials, Y_lm, contractions and adjoint in f32; f64 sums",
-                   "step": "velocity-Verlet MD step: E+F evaluation + integration; neighbour list rebuilt on the "
-                           "GPU every 10 steps (1 A skin); steps between rebuilds in one CUDA graph",
-                   "dt_fs": 0.5, "T0_K": 300,
-                   "l2": "no flush: per-step working set (>400 MB of tables, node features, adjoints) exceeds L2",
-                   "replicas_per_gpu": 1},
-        "forms": {
-            "bf16": {"value": head["value"], "ms_per_step": head["T"] / args.steps * 1e3, "errors": head["errors"],
-                     "ms_per_eval": head["eval_ms"], "schedule": head["schedule"]},
-            "fp32": {"value": fp["value"], "ms_per_step": fp["T"] / args.steps * 1e3, "errors": fp["errors"],
-                     "ms_per_eval": fp["eval_ms"], "md_check": fp["md_check"], "clocks": fp["clk"],
-                     "schedule": fp["schedule"]},
-            "bf16_over_fp32": head["value"] / fp["value"],
-        },
+        "config": {"workload": WORKLOAD["text"], "atoms": N, "edges_r_cut": E,
+                   "form": f"BF16-mixed: channel-mixing GEMMs on tcgen05, bf16 split operands "
+                           f"({eng.get_option('tc_terms')} terms), f32 accumulation; radials, Y_lm, contractions, "
+                           "adjoint f32; f64 sums",
+                   "step": "velocity-Verlet MD step (E+F + integration); neighbour list rebuilt on the GPU every 10 "
+                           "steps (1 A skin); CUDA graph between rebuilds",
+                   "l2": "no flush: the per-step working set (>400 MB) exceeds L2", "replicas_per_gpu": 1},
         "roofline": roofline,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": launches,
         "clocks": clk,
-        "eval_only": {"ms_per_eval": head["eval_ms"], "atom_evals_per_s": N / (head["eval_ms"] / 1e3),
-                      "l2": "flushed between evaluations"},
-        "stages_ms": per_stage(avg),
-        "stages_ms_fp32": per_stage(fp["stages"]),
-        "md_check": head["md_check"],
-        "wall_s_timed_region": head["t_wall"],
+        "stages_ms": {"bf16": {n_: sig(v, 3) for n_, v in avg.items()},
+                      "fp32": {n_: sig(v, 3) for n_, v in fp["stages"].items()}},
+        "forms": {name: {"value": sig(f_["value"]), "ms_per_step": sig(f_["T"] / args.steps * 1e3),
+                         "ms_per_eval": sig(f_["eval_ms"])} for name, f_ in forms.items()},
+        "bf16_over_fp32": sig(head["value"] / fp["value"]),
+        "errors_vs_fp64": errs,
     }
+    if args.full_check and err_n != N:
+        line["errors_vs_fp64_full_box"] = errs_full
+    if args.detail:
+        detail = dict(line)
+        detail.update({"stages": {"bf16": per_stage(avg), "fp32": per_stage(fp["stages"])},
+                       "md_check": {name: f_["md_check"] for name, f_ in forms.items()},
+                       "schedule": {name: f_["schedule"] for name, f_ in forms.items()},
+                       "clocks_fp32": fp["clk"], "wall_s_timed_region": head["t_wall"],
+                       "eval_only": {"ms_per_eval": head["eval_ms"], "l2": "flushed between evaluations"}})
+        with open(args.detail, "w") as fh:
+            json.dump(detail, fh, indent=1)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -614,6 +634,49 @@ def gpu_arm(args, rank, world, local_rank):
 # ---------------------------------------------------------------------------
 MOLECULES = dict(name="molecules_2048", n_mol=2048, sizes=(8, 120), density=0.08, min_dist=0.95, seed=4,
                  species=("H", "C", "N", "O", "F", "S", "Cl"), probs=(0.45, 0.30, 0.08, 0.10, 0.03, 0.02, 0.02))
+
+
+def molecule_reference(path, pos, sp, first, r_cut):
+    """float64 oracle energies and atomic forces of every molecule (host threads over molecules)."""
+    from oracle.pyoracle import Evaluator
+    from symmetrix_gb300.synth.structures import neighbor_list
+    n_mol = len(first) - 1
+    threads = host_threads()
+    base = Evaluator(path, "port")
+    evs = [base] + [base.clone() for _ in range(threads - 1)]
+    E_ref, F_ref = np.zeros(n_mol), [None] * n_mol
+
+    def work(t):
+        ev = evs[t]
+        for m in range(t, n_mol, threads):
+            p, s_ = pos[first[m]:first[m + 1]], sp[first[m]:first[m + 1]]
+            nl = neighbor_list(p, r_cut)
+            ev.compute_node_energies_forces(*edge_tuple(s_, nl))
+            E_ref[m] = ev.node_energies.sum()
+            f = ev.node_forces.reshape(-1, 3)
+            F = np.zeros((len(p), 3))
+            np.add.at(F, nl["neigh_indices"], f)
+            np.add.at(F, nl["i"], -f)
+            F_ref[m] = F
+
+    t0 = time.time()
+    ths = [threading.Thread(target=work, args=(t,)) for t in range(threads)]
+    for th in ths:
+        th.start()
+    for th in ths:
+        th.join()
+    log(f"oracle over {n_mol} molecules in {time.time() - t0:.0f} s ({threads} threads)")
+    return E_ref, F_ref
+
+
+def molecule_errors(e_mol, F, ref, first):
+    E_ref, F_ref = ref
+    n = np.diff(first)
+    dF = np.concatenate([np.abs(a - b) for a, b in zip(F, F_ref)])
+    return {"box": f"all {len(n)} molecules ({int(n.sum())} atoms)",
+            "energy_per_atom_eV": sig(abs(np.sum(e_mol) - E_ref.sum()) / n.sum(), 3),
+            "max_molecule_energy_per_atom_eV": sig(float((np.abs(np.asarray(e_mol) - E_ref) / n).max()), 3),
+            "max_force_eV_per_A": sig(float(dF.max()), 3), "rms_force_eV_per_A": sig(float(np.sqrt((dF ** 2).mean())), 3)}
 
 
 def molecules_arm(args):
@@ -627,9 +690,9 @@ def molecules_arm(args):
 
     build()
     os.makedirs(CACHE, exist_ok=True)
-    path = os.path.join(CACHE, "model_molecules_zbl_s1.json")
+    path = os.path.join(CACHE, "model_molecules_s1.json")
     if not os.path.exists(path):
-        write_model(make_model(**CONFIGS["molecules"], seed=1, zbl=True), path + ".tmp")
+        write_model(make_model(**CONFIGS["molecules"], seed=1), path + ".tmp")
         os.replace(path + ".tmp", path)
     W = MOLECULES
     sfile = os.path.join(CACHE, f"{W['name']}_s{W['seed']}.npz")
@@ -652,6 +715,7 @@ def molecules_arm(args):
     N = len(pos)
     dev = torch.device("cuda", 0)
     out = {}
+    ref = None
     for form in ("fp32", "bf16"):
         eng = MACE(path, precision=form)
         estream = torch.cuda.ExternalStream(eng.stream, device=dev)
@@ -669,13 +733,20 @@ def molecules_arm(args):
         T = e0.elapsed_time(e1) / 1e3
         out[form] = {"value": N * args.steps / T, "ms_per_step": T / args.steps * 1e3, "edges": md.num_edges,
                      "schedule": schedule_of(eng)}
-        del md, eng
+        del md
+        # every molecule's energy and forces in one batched evaluation, against the oracle
+        if ref is None:
+            ref = molecule_reference(path, pos, sp, first, CONFIGS["molecules"]["r_cut"])
+        e_mol, _, F = eng.compute_molecules([(pos[first[m]:first[m + 1]], sp[first[m]:first[m + 1]])
+                                             for m in range(len(first) - 1)])
+        out[form]["errors_vs_fp64"] = molecule_errors(e_mol, F, ref, first)
+        del eng
     print(json.dumps({
         "metric": METRIC, "value": out["bf16"]["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": out["bf16"]["ms_per_step"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
         "config": {"workload": f"{W['name']}: {W['n_mol']} non-periodic molecules of {W['sizes'][0]}-{W['sizes'][1]} "
-                               f"atoms ({N} atoms), 64x0e+64x1o, r_cut 5 A, H/C/N/O/F/S/Cl, ZBL; batch MD, dt 0.5 fs, "
+                               f"atoms ({N} atoms), 64x0e+64x1o, r_cut 5 A, H/C/N/O/F/S/Cl; batch MD, dt 0.5 fs, "
                                "neighbour list per molecule rebuilt every 10 steps, CUDA graph between rebuilds",
                    "atoms": N},
         "forms": out, "bf16_over_fp32": out["bf16"]["value"] / out["fp32"]["value"],
@@ -695,7 +766,8 @@ def large_arm(args):
     from symmetrix_gb300.synth.structures import maxwell_boltzmann, random_box, species_masses
 
     build()
-    path = engine_model_path(model_path())
+    json_path = model_path()
+    path = engine_model_path(json_path)
     W = WORKLOAD
     sfile = os.path.join(CACHE, f"{W['name']}_s{W['struct_seed']}.npz")
     if os.path.exists(sfile):
@@ -709,6 +781,10 @@ def large_arm(args):
     N = len(pos)
     dev = torch.device("cuda", 0)
     out = {}
+    # errors on a 4096-atom box of the same model, density and species mix
+    _, _, sp_e, nl_e = structure(W["err_atoms"], W["struct_seed"] + 100)
+    a_e = edge_tuple(sp_e, nl_e)
+    ref, _ = oracle_eval(json_path, a_e, host_threads())
     for form in ("fp32", "bf16"):
         eng = MACE(path, precision=form)
         estream = torch.cuda.ExternalStream(eng.stream, device=dev)
@@ -727,7 +803,12 @@ def large_arm(args):
         st = md.state()
         out[form] = {"value": N * args.steps / T, "ms_per_step": T / args.steps * 1e3, "edges_skin_list": md.num_edges,
                      "potential_energy_per_atom": st["potential_energy"] / N}
-        del md, eng
+        del md
+        eng.compute_node_energies_forces(*a_e)
+        out[form]["errors_vs_fp64"] = dict(box=f"a {W['err_atoms']}-atom box of the same model, density and species "
+                                               f"mix ({len(nl_e['r'])} edges)",
+                                           **errors(eng.node_energies, eng.node_forces, ref, nl_e))
+        del eng
         gc.collect()
     print(json.dumps({
         "metric": METRIC, "value": out["bf16"]["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
@@ -745,6 +826,9 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--detail", default=None, help="write the long form of the result to this JSON file")
+    ap.add_argument("--full-check", action="store_true",
+                    help="precision_32768 / large_1m: also check the whole timed box against the float64 oracle")
     ap.add_argument("--workload", default="fp32_4096",
                     choices=["fp32_4096", "precision_32768", "large_1m", "molecules"],
                     help="fp32_4096: the headline line; precision_32768: L_max 2, 10 species, 32768 atoms; "

@@ -129,6 +129,40 @@ struct AtomCursor {
   }
 };
 
+// H1_adj accumulation in 64-bit fixed point.  The layer-1 adjoint scatters every edge's
+// R1 Y g term into H1_adj of the neighbour node; float atomics would make the sum depend
+// on the order in which blocks arrive.  Integer addition is associative, so each term is
+// rounded once to a multiple of 2^-34 and added as a two's-complement int64: the sum is
+// the same bit pattern on every run, and converted to float once at the end.  Range:
+// |H1_adj| < 2^29 (5.4e8, far above any model's dE/dH1: O(1)); resolution 2^-34
+// (5.8e-11, far below the float32 rounding of a term).
+using fix64 = unsigned long long;
+constexpr double kFixInv = 1.0 / 17179869184.0;  // 2^-34
+// round(v 2^34) as an int64, round-to-nearest-even, for |v| < 2^29, in three exact FP32
+// steps and no conversion instruction (whose issue cost is several times these): v is
+// split as a 2^10 + b 2^-12 + c 2^-34 with a, b, c integers of at most 22 bits, each
+// found by adding 1.5 2^23 (whose ulp is 1) to the scaled remainder and reading the
+// integer from the low mantissa bits.  Each remainder is exact (v minus its rounding to
+// a multiple of a power of two at or above its ulp), and a 2^44 + b 2^22 is an even
+// integer, so a 2^44 + b 2^22 + c is the rounding of v 2^34 itself.
+__device__ __forceinline__ fix64 to_fixed(float v) {
+  constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
+  const float ta = fmaf(v, 1.0f / 1024.0f, kMagic);
+  const float va = fmaf(-(ta - kMagic), 1024.0f, v);  // v - a 2^10
+  const float tb = fmaf(va, 4096.0f, kMagic);
+  const float vb = fmaf(-(tb - kMagic), 1.0f / 4096.0f, va);  // va - b 2^-12
+  const float tc = fmaf(vb, 17179869184.0f, kMagic);
+  const int a = __float_as_int(ta) - 0x4B400000, b = __float_as_int(tb) - 0x4B400000,
+            c = __float_as_int(tc) - 0x4B400000;
+  // a 2^44 + b 2^22 + c
+  return (static_cast<fix64>(static_cast<long long>(a)) << 44) + (static_cast<fix64>(static_cast<long long>(b)) << 22) +
+         static_cast<fix64>(static_cast<long long>(c));
+}
+__device__ __forceinline__ void add_fixed(fix64* dst, float v) { atomicAdd(dst, to_fixed(v)); }
+__device__ __forceinline__ float from_fixed(fix64 q) {
+  return static_cast<float>(static_cast<double>(static_cast<long long>(q)) * kFixInv);
+}
+
 // Host side: the kernel's model copy and grid for n atoms under the current schedule.
 inline int atom_grid(const DevModel& m, int k, int n, DevModel& mk) {
   mk = m;

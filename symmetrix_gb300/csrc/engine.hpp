@@ -81,6 +81,7 @@ struct smx_engine {
   float *A0_adj = nullptr, *M0_adj = nullptr, *H1_adj = nullptr, *Phi1_adj = nullptr, *A1_adj = nullptr;
   float *M1_adj = nullptr, *H2_adj = nullptr;
   double* f1 = nullptr;  // layer-1 edge forces (float64 accumulation)
+  smx::fix64* H1_adj_fx = nullptr;  // H1_adj accumulator (fixed point: order-independent sums)
   // precision form: bf16 GEMM operands (M0 and H1_adj as [N*nLM][C]; Phi1 and A1_adj
   // regrouped per l as [N*(2l+1)][n_eta*C] and [N*(2l+1)][C])
   __nv_bfloat16 *M0_bf = nullptr, *Phi1_bf = nullptr, *A1adj_bf = nullptr, *H1adj_bf = nullptr;
@@ -297,6 +298,8 @@ struct smx_engine {
       dm.dens_s[layer] = dm.dens_c[layer] = nullptr;
     }
     f1 = nullptr;
+    if (H1_adj_fx) cudaFree(H1_adj_fx);
+    H1_adj_fx = nullptr;
     if (zbl_e) cudaFree(zbl_e);
     zbl_e = nullptr;
     first = ntype = nidx = ntype_e = atom_order = nneigh = nullptr;
@@ -320,6 +323,7 @@ struct smx_engine {
     A0_adj = dalloc<float>(nN * 16 * C);
     M0_adj = dalloc<float>(nN * dm.nLM * C);
     H1_adj = dalloc<float>(nN * dm.nLM * C);
+    H1_adj_fx = dalloc<smx::fix64>(nN * dm.nLM * C);
     Phi1_adj = dalloc<float>(nN * dm.n_lme * C);
     A1_adj = dalloc<float>(nN * 16 * C);
     M1_adj = dalloc<float>(nN * C);
@@ -646,7 +650,7 @@ struct smx_engine {
       smx::launch_gemm(b, s);
     }
     mark(4, s);
-    smx::launch_node_tail(dm, in.node_type, N, A1, H1, M1, H2, A1adj_out, H1_adj, M1_adj, H2_adj,
+    smx::launch_node_tail(dm, in.node_type, N, A1, H1, M1, H2, A1adj_out, H1_adj_fx, M1_adj, H2_adj,
                           dm.has_zbl ? zbl_e : nullptr, out_e, s);
     mark(5, s);
     {  // Phi1_adj = A1_adj @ A1W[l]^T  (mace.cpp:644-679)
@@ -670,10 +674,11 @@ struct smx_engine {
       smx::launch_gemm(b, s);
     }
     mark(6, s);
-    smx::launch_layer1_rev(dm, in, H1, Phi1_adj, H1_adj, f1, s);
+    smx::launch_layer1_rev(dm, in, H1, Phi1_adj, H1_adj_fx, f1, s);
     mark(7, s);
+    // the float H1_adj rows (and the BF16 form's split operand) from the fixed-point sums
+    smx::launch_fixed_rows(H1_adj_fx, H1_adj, tc_H1 ? H1adj_bf : nullptr, static_cast<long>(N) * dm.nLM, C, T, s);
     if (tc_H1) {  // M0_adj = H1_adj @ H1W[L]^T  (mace.cpp:425-451), tensor cores
-      smx::launch_rows_to_bf16(H1_adj, H1adj_bf, static_cast<long>(N) * dm.nLM, C, 1, C, 0, 0, T, s);
       smx::UmmaGemm g{H1adj_bf, static_cast<long>(N) * dm.nLM, T * C, W_M0adj, 2 * C, C,
                        smx::UmmaOut{M0_adj, static_cast<long>(N) * dm.nLM, dm.nLM, static_cast<long>(dm.nLM) * C, 0,
                                     C, 1}};

@@ -310,13 +310,25 @@ __device__ __forceinline__ void l1_rev_edge(const float2* g, const float2* R, co
   fz = az;
 }
 
+// Barrier of the two warps (one per half) that own the same channel pairs: id 1 + p for
+// pair p, 64 threads; the block's barrier 0 is __syncthreads.
+__device__ __forceinline__ void pair_barrier(int pair) {
+  asm volatile("bar.sync %0, 64;" ::"r"(1 + pair) : "memory");
+}
+
 // Adjoint, one staged chunk, half H.  The spline row of an edge is reduced to R and
 // R' first; the gathers of the next edge are then issued into the freed registers so
 // that their L2 latency overlaps this edge's arithmetic.
+//
+// Both halves produce terms for all NL2 H1_adj rows of the same channel pair.  Half H
+// adds rows [H NL2/2, (H + 1) NL2/2) of both halves to the fixed-point accumulator and
+// hands the other rows to its partner warp through xchg ([2][NL2][C/2] float2,
+// double-buffered by edge parity, so one pair barrier per edge suffices): half the
+// atomics of each half adding every row.
 template <int LMAX, int H>
 __device__ __forceinline__ void l1_rev_chunk(const DevModel& m, const float* __restrict__ H1,
-                                             float* __restrict__ H1_adj, const L1Stage<true>& st, const Lane2& L,
-                                             const float2* g, float (*sF)[8][3]) {
+                                             fix64* __restrict__ H1_adj, const L1Stage<true>& st, const Lane2& L,
+                                             const float2* g, float (*sF)[8][3], float2* xchg, int pair) {
   constexpr int NL2 = (LMAX + 1) * (LMAX + 1);
   constexpr int NQ = half_count(H);
   const int na = st.nact;
@@ -341,10 +353,23 @@ __device__ __forceinline__ void l1_rev_chunk(const DevModel& m, const float* __r
     l1_rev_edge<LMAX, H>(g, R, Rd, st.Y2[t], st.G[t], st.u[t], hv, hadj, fx, fy, fz);
     if (!L.live) fx = fy = fz = 0.0f;
     block_reduce3(fx, fy, fz, sF, t);
+    constexpr int NR = NL2 / 2;
+    float2* xb = xchg + (a & 1) * NL2 * L.C2;
     if (L.live) {
-      float2* dst = reinterpret_cast<float2*>(H1_adj + static_cast<size_t>(j) * NL2 * L.C + L.kc);
 #pragma unroll
-      for (int b = 0; b < NL2; ++b) atomicAdd(dst + b * L.C2, hadj[b]);
+      for (int b = 0; b < NL2; ++b)
+        if (b / NR != H) xb[b * L.C2 + L.cp] = hadj[b];
+    }
+    pair_barrier(pair);
+    if (L.live) {
+      fix64* dst = H1_adj + static_cast<size_t>(j) * NL2 * L.C + L.kc;
+#pragma unroll
+      for (int q = 0; q < NR; ++q) {
+        const int b = H * NR + q;
+        const float2 o = xb[b * L.C2 + L.cp];
+        add_fixed(dst + b * L.C, hadj[b].x + o.x);
+        add_fixed(dst + b * L.C + 1, hadj[b].y + o.y);
+      }
     }
   }
 }
@@ -447,17 +472,20 @@ __global__ void __launch_bounds__(256) k_layer1_fwd(DevModel m, EdgeIn in, const
 // ---------------------------------------------------------------------------
 template <int LMAX, int CT>
 __device__ __forceinline__ void layer1_rev_atom(const DevModel& m, const EdgeIn& in, const float* __restrict__ H1,
-                                                const float* __restrict__ dPhi1, float* __restrict__ H1_adj,
+                                                const float* __restrict__ dPhi1, fix64* __restrict__ H1_adj,
                                                 double* __restrict__ f1, int i) {
   static_assert(LMAX == 1, "instruction halves are tabulated for L_max = 1");
   constexpr int NP = ins_np(LMAX);
+  constexpr int NL2 = (LMAX + 1) * (LMAX + 1);
   constexpr int NG = half_np<LMAX, 0>() > half_np<LMAX, 1>() ? half_np<LMAX, 0>() : half_np<LMAX, 1>();
   extern __shared__ float dyn[];
   __shared__ L1Stage<true> st;
   __shared__ float sF[kEdgeChunk][8][3];
+  __shared__ float2 xchg[2 * NL2 * 128];  // the halves' H1_adj hand-over, up to 256 channels
   const int C = CT > 0 ? CT : m.C;
   int half;
   const Lane2 L = lane2(C, half);
+  const int pair = (threadIdx.x >> 5) % (blockDim.x >> 6);  // warp w of half 0 with warp w of half 1
   const int nwarp = blockDim.x >> 5;
   const int ti = in.node_type[i];
   const int e0 = in.first[i], e1 = in.end(i);
@@ -496,9 +524,9 @@ __device__ __forceinline__ void layer1_rev_atom(const DevModel& m, const EdgeIn&
     stage_l1<true>(m, in, ti, eb, ne, st);
     __syncthreads();
     if (half == 0)
-      l1_rev_chunk<LMAX, 0>(m, H1, H1_adj, st, L, g, sF);
+      l1_rev_chunk<LMAX, 0>(m, H1, H1_adj, st, L, g, sF, xchg, pair);
     else
-      l1_rev_chunk<LMAX, 1>(m, H1, H1_adj, st, L, g, sF);
+      l1_rev_chunk<LMAX, 1>(m, H1, H1_adj, st, L, g, sF, xchg, pair);
     __syncthreads();
     for (int t = threadIdx.x; t < ne; t += blockDim.x) {
       double s[3] = {0.0, 0.0, 0.0};
@@ -520,7 +548,7 @@ __device__ __forceinline__ void layer1_rev_atom(const DevModel& m, const EdgeIn&
 
 template <int LMAX, int CT, bool P>
 __global__ void __launch_bounds__(256) k_layer1_rev(DevModel m, EdgeIn in, const float* __restrict__ H1,
-                                                    const float* __restrict__ dPhi1, float* __restrict__ H1_adj,
+                                                    const float* __restrict__ dPhi1, fix64* __restrict__ H1_adj,
                                                     double* __restrict__ f1) {
   AtomCursor cur{P ? m.sched : nullptr, in.N, 0};
   for (int b = cur.first(); b < in.N; b = cur.next())
@@ -720,7 +748,7 @@ __host__ __device__ constexpr bool l2_uses_l2(int l2) {
 // Adjoint, group G, one staged chunk (as l1_rev_edge, scalar, this group's paths).
 template <int G>
 __device__ __forceinline__ void l2_rev_chunk(const DevModel& m, const float* __restrict__ H1,
-                                             float* __restrict__ H1_adj, const L1Stage<true>& st, int C, int k,
+                                             fix64* __restrict__ H1_adj, const L1Stage<true>& st, int C, int k,
                                              bool live, const float* g, float (*sF)[16][3]) {
   constexpr int NL2 = 9, NI = 17;
   const int na = st.nact;
@@ -773,12 +801,12 @@ __device__ __forceinline__ void l2_rev_chunk(const DevModel& m, const float* __r
     if (!live) fx = fy = fz = 0.0f;
     block_reduce3_w16(fx, fy, fz, sF, t);
     if (live) {
-      float* dst = H1_adj + static_cast<size_t>(j) * NL2 * C + k;
+      fix64* dst = H1_adj + static_cast<size_t>(j) * NL2 * C + k;
       static_for<3>([&](auto lc) {
         constexpr int l2 = decltype(lc)::value;
         if constexpr (l2_uses_l2<G>(l2)) {
 #pragma unroll
-          for (int b = 0; b < 2 * l2 + 1; ++b) atomicAdd(dst + (l2 * l2 + b) * C, hadj[l2 * l2 + b]);
+          for (int b = 0; b < 2 * l2 + 1; ++b) add_fixed(dst + (l2 * l2 + b) * C, hadj[l2 * l2 + b]);
         }
       });
     }
@@ -791,7 +819,7 @@ __device__ __forceinline__ void l2_rev_chunk(const DevModel& m, const float* __r
 // writes its partial per-edge forces to its own f1 slice (f1 + h * f1_stride); the
 // layer-0 adjoint adds the slices.
 __device__ __forceinline__ void layer1_rev_l2_atom(const DevModel& m, const EdgeIn& in, const float* __restrict__ H1,
-                                                   const float* __restrict__ dPhi1, float* __restrict__ H1_adj,
+                                                   const float* __restrict__ dPhi1, fix64* __restrict__ H1_adj,
                                                    double* __restrict__ f1, int i, int h) {
   constexpr int NP = 243;
   extern __shared__ float dyn[];
@@ -871,7 +899,7 @@ __device__ __forceinline__ void layer1_rev_l2_atom(const DevModel& m, const Edge
 template <bool P>
 __global__ void __launch_bounds__(512, 1) k_layer1_rev_l2(DevModel m, EdgeIn in, const float* __restrict__ H1,
                                                           const float* __restrict__ dPhi1,
-                                                          float* __restrict__ H1_adj, double* __restrict__ f1) {
+                                                          fix64* __restrict__ H1_adj, double* __restrict__ f1) {
   const int ns = m.l2_split, n = in.N * ns;
   AtomCursor cur{P ? m.sched : nullptr, n, 0};
   for (int b = cur.first(); b < n; b = cur.next())
@@ -957,7 +985,7 @@ void launch_layer1_fwd(const DevModel& m, const EdgeIn& in, const float* H1, flo
   });
 }
 
-void launch_layer1_rev(const DevModel& m, const EdgeIn& in, const float* H1, const float* dPhi1, float* H1_adj,
+void launch_layer1_rev(const DevModel& m, const EdgeIn& in, const float* H1, const float* dPhi1, fix64* H1_adj,
                        double* f1, cudaStream_t s) {
   if (in.N <= 0) return;
   DevModel mk;

@@ -94,13 +94,13 @@ void launch_gemm(const GemmBatch& b, cudaStream_t s) {
 //   M1[k] = P1_{ti,k}(A1[i,:,k]) and its gradient,
 //   H2 = W_H1[ti]^T H1[i,0,:] + W_M1^T M1,
 //   E_i = e0[ti] + w1 . H1[i,0,:] + w2 . s*silu(W1 H2)           (float64 output),
-//   dE/dH2 (MLP gradient), H1_adj[i,0,:] = w1 + W_H1[ti] dE/dH2 (other rows 0),
+//   dE/dH2 (MLP gradient), H1_adj[i,0,:] = w1 + W_H1[ti] dE/dH2 (other rows 0; fixed point),
 //   M1_adj = W_M1 dE/dH2, A1_adj[i,lm,k] = dM1/dA1[lm] * M1_adj[k].
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void node_tail_atom(const DevModel& m, const int* __restrict__ ntype, float* __restrict__ A1,
                                                const float* __restrict__ H1, float* __restrict__ M1o,
                                                float* __restrict__ H2o, float* __restrict__ A1_adj,
-                                               float* __restrict__ H1_adj, float* __restrict__ M1_adj_o,
+                                               fix64* __restrict__ H1_adj, float* __restrict__ M1_adj_o,
                                                float* __restrict__ H2_adj_o, const float* __restrict__ zbl_e,
                                                double* __restrict__ energies, int N, int i) {
   extern __shared__ float dyn[];
@@ -240,8 +240,9 @@ __device__ __forceinline__ void node_tail_atom(const DevModel& m, const int* __r
       }
     }
   }
-  H1_adj[static_cast<size_t>(i) * m.nLM * C + k] = ha;
-  for (int LM = 1; LM < m.nLM; ++LM) H1_adj[(static_cast<size_t>(i) * m.nLM + LM) * C + k] = 0.0f;
+  // H1_adj in fixed point: the layer-1 adjoint adds its edge terms to these rows
+  H1_adj[static_cast<size_t>(i) * m.nLM * C + k] = to_fixed(ha);
+  for (int LM = 1; LM < m.nLM; ++LM) H1_adj[(static_cast<size_t>(i) * m.nLM + LM) * C + k] = 0ull;
   M1o[static_cast<size_t>(i) * C + k] = f;
   H2o[static_cast<size_t>(i) * C + k] = h2;
   M1_adj_o[static_cast<size_t>(i) * C + k] = m1a;
@@ -252,7 +253,7 @@ template <bool P>
 __global__ void __launch_bounds__(256) k_node_tail(DevModel m, const int* __restrict__ ntype, float* __restrict__ A1,
                                                    const float* __restrict__ H1, float* __restrict__ M1o,
                                                    float* __restrict__ H2o, float* __restrict__ A1_adj,
-                                                   float* __restrict__ H1_adj, float* __restrict__ M1_adj_o,
+                                                   fix64* __restrict__ H1_adj, float* __restrict__ M1_adj_o,
                                                    float* __restrict__ H2_adj_o, const float* __restrict__ zbl_e,
                                                    double* __restrict__ energies, int N) {
   AtomCursor cur{P ? m.sched : nullptr, N, 0};
@@ -264,7 +265,7 @@ __global__ void __launch_bounds__(256) k_node_tail(DevModel m, const int* __rest
 size_t node_tail_smem(const DevModel& m) { return sizeof(float) * (34 * m.C + 4 * m.C + 33 * 8 + 33); }
 
 void launch_node_tail(const DevModel& m, const int* node_type, int N, float* A1, const float* H1, float* M1,
-                      float* H2, float* A1_adj, float* H1_adj, float* M1_adj, float* H2_adj, const float* zbl_e,
+                      float* H2, float* A1_adj, fix64* H1_adj, float* M1_adj, float* H2_adj, const float* zbl_e,
                       double* energies, cudaStream_t s) {
   if (N <= 0) return;
   DevModel mk;
@@ -279,6 +280,30 @@ void launch_node_tail(const DevModel& m, const int* node_type, int N, float* A1,
 
 void node_tail_residency(const DevModel& m, int* per_sm) {
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[kAkNodeTail], k_node_tail<true>, m.C, node_tail_smem(m));
+}
+
+// H1_adj from its fixed-point accumulator: float rows for the SIMT GEMM and the stage
+// reads, and in the BF16 form the M0_adj GEMM's split operand rows (pitch terms * C, as
+// launch_rows_to_bf16 writes them).
+__global__ void k_fixed_rows(const fix64* __restrict__ src, float* __restrict__ dst, __nv_bfloat16* __restrict__ bf,
+                             long rows, int C, int terms) {
+  const long n = rows * C;
+  for (long t = blockIdx.x * static_cast<long>(blockDim.x) + threadIdx.x; t < n;
+       t += static_cast<long>(gridDim.x) * blockDim.x) {
+    const float v = from_fixed(src[t]);
+    dst[t] = v;
+    if (bf) {
+      const long r = t / C;
+      write_split(bf + r * terms * C, C, terms, static_cast<int>(t - r * C), v);
+    }
+  }
+}
+
+void launch_fixed_rows(const fix64* src, float* dst, __nv_bfloat16* bf, long rows, int C, int terms, cudaStream_t s) {
+  if (rows <= 0) return;
+  const long n = rows * C;
+  const int blocks = static_cast<int>(std::min<long>((n + 255) / 256, 152L * 16));
+  k_fixed_rows<<<blocks, 256, 0, s>>>(src, dst, bf, rows, C, terms);
 }
 
 // Centre atoms sorted by species (a counting sort; the order inside a species is

@@ -23,7 +23,8 @@ void launch_layer0_rev(const DevModel& m, const EdgeIn& in, const float* A0, con
 cudaError_t init_layer1_kernels(const DevModel& m);
 int layer1_block(int C);
 void launch_layer1_fwd(const DevModel& m, const EdgeIn& in, const float* H1, float* Phi1, cudaStream_t s);
-void launch_layer1_rev(const DevModel& m, const EdgeIn& in, const float* H1, const float* dPhi1, float* H1_adj,
+// H1_adj: fixed-point accumulator (see to_fixed), seeded by launch_node_tail
+void launch_layer1_rev(const DevModel& m, const EdgeIn& in, const float* H1, const float* dPhi1, fix64* H1_adj,
                        double* f1, cudaStream_t s);
 
 // k_node.cu
@@ -48,8 +49,11 @@ struct GemmBatch {
 void launch_gemm(const GemmBatch& b, cudaStream_t s);
 
 void launch_node_tail(const DevModel& m, const int* node_type, int N, float* A1, const float* H1, float* M1,
-                      float* H2, float* A1_adj, float* H1_adj, float* M1_adj, float* H2_adj, const float* zbl_e,
+                      float* H2, float* A1_adj, fix64* H1_adj, float* M1_adj, float* H2_adj, const float* zbl_e,
                       double* energies, cudaStream_t s);
+// dst[rows][C] = the fixed-point rows src as float; bf (optional): their bf16 split terms,
+// row pitch terms * C
+void launch_fixed_rows(const fix64* src, float* dst, __nv_bfloat16* bf, long rows, int C, int terms, cudaStream_t s);
 void launch_scan_first(const int* num_neigh, int N, int* first, cudaStream_t s);
 // input check of the host API (bits of the flags word)
 constexpr unsigned kBadNodeType = 1, kBadNumNeigh = 2, kBadEdgeCount = 4, kBadNeighIndex = 8, kBadNeighType = 16,

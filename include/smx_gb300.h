@@ -20,8 +20,13 @@
  *                                   device-pointer call
  *   smx_num_elements, smx_num_channels, smx_r_cut, smx_l_max, smx_L_max, smx_num_LM,
  *   smx_atomic_numbers              public fields of class MACE (mace.hpp:18-25)
- *   smx_get_stage                   the read-only stage buffers the Python binding exposes
+ *   smx_get_stage, smx_set_stage    the stage buffers the Python binding exposes read/write
  *                                   (symmetrix/source/cpp/mace.cpp:14-34)
+ *   smx_run_stage                   the binding's per-stage calls compute_H1 / reverse_H1,
+ *                                   compute_Phi1 / reverse_Phi1 (with compute_R1 and
+ *                                   compute_Y, fused), compute_A1 / reverse_A1
+ *                                   (symmetrix/source/cpp/mace.cpp:152-179;
+ *                                   libsymmetrix/source/mace.cpp:397-679)
  *   smx_compute_atoms               what the callers do around the evaluator: neighbour list,
  *                                   evaluation, F_j += f_e / F_i -= f_e and the virial
  *                                   (Symmetrix.calculate, symmetrix_calc.py:72-102;
@@ -117,6 +122,42 @@ int smx_sync(smx_engine* eng, void* stream);
  * writes only after smx_set_option(eng, "keep_stages", 1); -3 on a CUDA error.
  * smx_last_error() says which. */
 long smx_get_stage(smx_engine* eng, const char* name, double* out, long cap);
+/* "node_energies" (N) and "node_forces" (3E, the last host-pointer call's or stage call's
+ * edges) are read the same way, as stored (float64). */
+
+/* Writes stage buffer `name` (M0, H1, Phi1, A1, M0_adj, H1_adj, Phi1_adj, A1_adj: float32,
+ * rounded from the float64 values; node_forces: float64) of the node count of the last
+ * evaluation or stage call, in the layout smx_get_stage reads; n must be that stage's
+ * length.  Returns n, or minus an SMX_ERR_* code.  The reference binding's buffers are
+ * read-write attributes (symmetrix/source/cpp/mace.cpp:14-34). */
+long smx_set_stage(smx_engine* eng, const char* name, const double* values, long n);
+
+/* Runs one stage on the engine's stage buffers (what the reference's per-stage calls
+ * do on its members, libsymmetrix/source/mace.cpp:397-679):
+ *   "compute_H1"   H1 = M0 . H1_weights[L]              (mace.cpp:397-423)
+ *   "reverse_H1"   M0_adj = H1_adj . H1_weights[L]^T      (mace.cpp:425-451)
+ *   "compute_A1"   A1 = Phi1 . A1_weights[l]             (mace.cpp:607-642)
+ *   "reverse_A1"   Phi1_adj = A1_adj . A1_weights[l]^T   (mace.cpp:644-679)
+ *     node stages: num_nodes must be the last evaluation's; the edge arguments are
+ *     ignored (NULL / 0);
+ *   "compute_Phi1" R1, Y and Phi1 from H1 on the given edges (mace.cpp:92-148, 453-502)
+ *   "reverse_Phi1" on the given edges: H1_adj += the Phi1_adj-contracted terms and
+ *                  node_forces += -dPhi1/dxyz . Phi1_adj (mace.cpp:504-605); the flags
+ *                  SMX_STAGE_ZERO_DXYZ / SMX_STAGE_ZERO_H1_ADJ start either from zero,
+ *                  as the reference's zero_dxyz / zero_H1_adj arguments do.
+ *     edge stages: the edge list is copied and checked as by the host-pointer call; a
+ *     node count other than the last call's starts the buffers from zero.
+ * The GEMMs run on the float32 SIMT kernel in both precision forms; the layer-1 stages
+ * leave out the density normalisation (compute_A1_scaled / reverse_A1_scaled, fused
+ * into the node tail with compute_M1, compute_H2, compute_readouts and their reverses,
+ * which, like the layer-0 stages compute_Y, compute_R0, compute_A0(_scaled) and
+ * compute_M0 and their reverses, run only inside a full evaluation).  Results are
+ * read with smx_get_stage. */
+#define SMX_STAGE_ZERO_DXYZ 1
+#define SMX_STAGE_ZERO_H1_ADJ 2
+int smx_run_stage(smx_engine* eng, const char* stage, int num_nodes, const int* node_types, const int* num_neigh,
+                  const int* neigh_indices, const int* neigh_types, long num_edges, const double* xyz,
+                  const double* r, int flags);
 
 /* Options: "keep_stages" (the BF16 form also writes the float32 M0, Phi1 and A1_adj
  * rows for smx_get_stage), "profile" (record CUDA

@@ -34,6 +34,8 @@ SIGNATURES = [
     ("smx_compute_node_energies_forces_device", _I, [_P, _I, _P, _P, _P, _P, _L, _P, _P, _P, _P, _P]),
     ("smx_sync", _I, [_P, _P]),
     ("smx_get_stage", _L, [_P, _S, _P, _L]),
+    ("smx_set_stage", _L, [_P, _S, _P, _L]),
+    ("smx_run_stage", _I, [_P, _S, _I, _P, _P, _P, _P, _L, _P, _P, _I]),
     ("smx_set_option", _I, [_P, _S, _L]),
     ("smx_get_option", _L, [_P, _S]),
     ("smx_engine_stream", _P, [_P]),

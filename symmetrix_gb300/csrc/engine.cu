@@ -193,50 +193,65 @@ long smx_get_option(const smx_engine* eng, const char* key) {
   return -1;
 }
 
+namespace {
+
+// Copy the host edge list of a call into the engine's workspace (reserved for it) and
+// check it on the device; SMX_OK, or the failure recorded by fail().
+int upload_edges(smx_engine* eng, int num_nodes, const int* node_types, const int* num_neigh,
+                 const int* neigh_indices, const int* neigh_types, long num_edges, const double* xyz,
+                 const double* r) {
+  if (num_nodes < 0 || num_edges < 0) return fail(SMX_ERR_INVALID, "negative size");
+  if (num_nodes > 0 && (!node_types || !num_neigh)) return fail(SMX_ERR_INVALID, "NULL node array");
+  if (num_edges > 0 && (!neigh_indices || !neigh_types || !xyz || !r)) return fail(SMX_ERR_INVALID, "NULL edge array");
+  const int S = eng->hm.S;
+  const double rc = eng->hm.r_cut;
+  // The inputs are checked on the device after the copies (the reference trusts its
+  // caller here); nothing is evaluated until the check has passed.
+  eng->reserve(num_nodes, num_edges);
+  cudaStream_t s = eng->stream;
+  if (num_nodes > 0) {
+    check(cudaMemcpyAsync(eng->ntype, node_types, sizeof(int) * num_nodes, cudaMemcpyHostToDevice, s), "H2D");
+    check(cudaMemcpyAsync(eng->nneigh, num_neigh, sizeof(int) * num_nodes, cudaMemcpyHostToDevice, s), "H2D");
+  }
+  if (num_edges > 0) {
+    check(cudaMemcpyAsync(eng->nidx, neigh_indices, sizeof(int) * num_edges, cudaMemcpyHostToDevice, s), "H2D");
+    check(cudaMemcpyAsync(eng->ntype_e, neigh_types, sizeof(int) * num_edges, cudaMemcpyHostToDevice, s), "H2D");
+    check(cudaMemcpyAsync(eng->xyz, xyz, sizeof(double) * 3 * num_edges, cudaMemcpyHostToDevice, s), "H2D");
+    check(cudaMemcpyAsync(eng->r, r, sizeof(double) * num_edges, cudaMemcpyHostToDevice, s), "H2D");
+  }
+  if (num_nodes > 0)
+    smx::launch_scan_first(eng->nneigh, num_nodes, eng->first, s);
+  else
+    check(cudaMemsetAsync(eng->first, 0, sizeof(int), s), "cudaMemsetAsync");
+  *reinterpret_cast<volatile unsigned*>(eng->check_host) = 0;
+  smx::launch_validate_inputs(num_nodes, num_edges, S, rc, eng->ntype, eng->nneigh, eng->first, eng->nidx,
+                              eng->ntype_e, eng->xyz, eng->r, eng->check_dev, s);
+  check(cudaStreamSynchronize(s), "input check");
+  const unsigned bad = *reinterpret_cast<volatile unsigned*>(eng->check_host);
+  if (bad & smx::kBadNodeType) return fail(SMX_ERR_INVALID, "node_types out of range");
+  if (bad & smx::kBadNumNeigh) return fail(SMX_ERR_INVALID, "negative num_neigh");
+  if (bad & smx::kBadEdgeCount) return fail(SMX_ERR_INVALID, "sum(num_neigh) != num_edges");
+  if (bad & smx::kBadNeighIndex) return fail(SMX_ERR_INVALID, "neigh_indices out of range (must be < num_nodes)");
+  if (bad & smx::kBadNeighType) return fail(SMX_ERR_INVALID, "neigh_types out of range");
+  if (bad & smx::kBadEdge) return fail(SMX_ERR_INVALID, "edge length outside (0, r_cut) or non-finite edge vector");
+  return SMX_OK;
+}
+
+}  // namespace
+
 int smx_compute_node_energies_forces(smx_engine* eng, int num_nodes, const int* node_types, const int* num_neigh,
                                      const int* neigh_indices, const int* neigh_types, long num_edges,
                                      const double* xyz, const double* r, double* node_energies,
                                      double* node_forces) {
   if (!eng) return fail(SMX_ERR_INVALID, "engine is NULL");
-  if (num_nodes < 0 || num_edges < 0) return fail(SMX_ERR_INVALID, "negative size");
-  if (num_nodes > 0 && (!node_types || !num_neigh || !node_energies))
-    return fail(SMX_ERR_INVALID, "NULL node array");
-  if (num_edges > 0 && (!neigh_indices || !neigh_types || !xyz || !r || !node_forces))
-    return fail(SMX_ERR_INVALID, "NULL edge array");
-  const int S = eng->hm.S;
-  const double rc = eng->hm.r_cut;
-  // The inputs are checked on the device after the copies (the reference trusts its
-  // caller here); nothing is evaluated until the check has passed.
+  if (num_nodes > 0 && !node_energies) return fail(SMX_ERR_INVALID, "NULL node array");
+  if (num_edges > 0 && !node_forces) return fail(SMX_ERR_INVALID, "NULL edge array");
   try {
     check(cudaSetDevice(eng->device), "cudaSetDevice");
-    eng->reserve(num_nodes, num_edges);
+    const int code = upload_edges(eng, num_nodes, node_types, num_neigh, neigh_indices, neigh_types, num_edges, xyz, r);
+    if (code != SMX_OK) return code;
     cudaStream_t s = eng->stream;
-    if (num_nodes > 0) {
-      check(cudaMemcpyAsync(eng->ntype, node_types, sizeof(int) * num_nodes, cudaMemcpyHostToDevice, s), "H2D");
-      check(cudaMemcpyAsync(eng->nneigh, num_neigh, sizeof(int) * num_nodes, cudaMemcpyHostToDevice, s), "H2D");
-    }
-    if (num_edges > 0) {
-      check(cudaMemcpyAsync(eng->nidx, neigh_indices, sizeof(int) * num_edges, cudaMemcpyHostToDevice, s), "H2D");
-      check(cudaMemcpyAsync(eng->ntype_e, neigh_types, sizeof(int) * num_edges, cudaMemcpyHostToDevice, s), "H2D");
-      check(cudaMemcpyAsync(eng->xyz, xyz, sizeof(double) * 3 * num_edges, cudaMemcpyHostToDevice, s), "H2D");
-      check(cudaMemcpyAsync(eng->r, r, sizeof(double) * num_edges, cudaMemcpyHostToDevice, s), "H2D");
-    }
-    if (num_nodes > 0)
-      smx::launch_scan_first(eng->nneigh, num_nodes, eng->first, s);
-    else
-      check(cudaMemsetAsync(eng->first, 0, sizeof(int), s), "cudaMemsetAsync");
-    *reinterpret_cast<volatile unsigned*>(eng->check_host) = 0;
-    smx::launch_validate_inputs(num_nodes, num_edges, S, rc, eng->ntype, eng->nneigh, eng->first, eng->nidx,
-                                eng->ntype_e, eng->xyz, eng->r, eng->check_dev, s);
-    check(cudaStreamSynchronize(s), "input check");
-    const unsigned bad = *reinterpret_cast<volatile unsigned*>(eng->check_host);
-    if (bad & smx::kBadNodeType) return fail(SMX_ERR_INVALID, "node_types out of range");
-    if (bad & smx::kBadNumNeigh) return fail(SMX_ERR_INVALID, "negative num_neigh");
-    if (bad & smx::kBadEdgeCount) return fail(SMX_ERR_INVALID, "sum(num_neigh) != num_edges");
-    if (bad & smx::kBadNeighIndex) return fail(SMX_ERR_INVALID, "neigh_indices out of range (must be < num_nodes)");
-    if (bad & smx::kBadNeighType) return fail(SMX_ERR_INVALID, "neigh_types out of range");
-    if (bad & smx::kBadEdge)
-      return fail(SMX_ERR_INVALID, "edge length outside (0, r_cut) or non-finite edge vector");
+    eng->lastE = num_edges;
     smx::EdgeIn in{eng->first, eng->ntype, eng->nidx, eng->ntype_e, eng->xyz, eng->r, num_nodes};
     eng->run(in, eng->energies, eng->forces, s);
     if (num_nodes > 0)
@@ -262,6 +277,7 @@ int smx_compute_node_energies_forces_device(smx_engine* eng, int num_nodes, cons
     eng->reserve(num_nodes, num_edges);
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : eng->stream;
     if (num_nodes > 0) smx::launch_scan_first(num_neigh, num_nodes, eng->first, s);
+    eng->lastE = 0;  // the edge arrays are the caller's: no node_forces stage read
     smx::EdgeIn in{eng->first, node_types, neigh_indices, neigh_types, xyz, r, num_nodes};
     eng->run(in, node_energies, node_forces, s);
   } catch (const std::exception& e) {
@@ -308,6 +324,25 @@ long smx_get_stage(smx_engine* eng, const char* name, double* out, long cap) {
   bool kept = true;
   long n = 0;
   const std::string s(name);
+  if (s == "node_energies" || s == "node_forces") {  // float64 outputs of the last host call or stage call
+    if (!eng->evaluated) {
+      fail(SMX_ERR_INVALID, "no evaluation has run since the engine's buffers were (re)allocated");
+      return -2;
+    }
+    const double* d = s == "node_energies" ? eng->energies : eng->forces;
+    n = s == "node_energies" ? N : 3 * eng->lastE;
+    if (out && cap > 0 && n > 0) {
+      try {
+        check(cudaSetDevice(eng->device), "cudaSetDevice");
+        check(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
+        check(cudaMemcpy(out, d, sizeof(double) * std::min(n, cap), cudaMemcpyDeviceToHost), "D2H");
+      } catch (const std::exception& e) {
+        fail(SMX_ERR_CUDA, e.what());
+        return -3;
+      }
+    }
+    return n;
+  }
   if (s == "A0") { src = eng->A0; n = N * 16 * C; }
   else if (s == "M0") { src = eng->M0; n = N * eng->dm.nLM * C; kept = eng->M0_kept; }
   else if (s == "H1") { src = eng->H1; n = N * eng->dm.nLM * C; }
@@ -348,6 +383,93 @@ long smx_get_stage(smx_engine* eng, const char* name, double* out, long cap) {
     for (long q = 0; q < n && q < cap; ++q) out[q] = tmp[q];
   }
   return n;
+}
+
+// Float32 stage buffers are written from float64 values (rounded); node_forces (float64,
+// the per-edge forces of the last call's edges) is copied as is.
+long smx_set_stage(smx_engine* eng, const char* name, const double* values, long n) {
+  if (!eng || !name || (n > 0 && !values)) return -fail(SMX_ERR_INVALID, "NULL argument");
+  if (!eng->evaluated) return -fail(SMX_ERR_INVALID, "no evaluation has set up the engine's buffers yet");
+  const long N = eng->lastN, C = eng->dm.C;
+  const std::string s(name);
+  float* dst = nullptr;
+  long want = 0;
+  if (s == "M0") { dst = eng->M0; want = N * eng->dm.nLM * C; eng->M0_kept = true; }
+  else if (s == "H1") { dst = eng->H1; want = N * eng->dm.nLM * C; }
+  else if (s == "Phi1") { dst = eng->Phi1; want = N * eng->dm.n_lme * C; eng->Phi1_kept = true; }
+  else if (s == "A1") { dst = eng->A1; want = N * 16 * C; }
+  else if (s == "M0_adj") { dst = eng->M0_adj; want = N * eng->dm.nLM * C; }
+  else if (s == "H1_adj") { dst = eng->H1_adj; want = N * eng->dm.nLM * C; }
+  else if (s == "Phi1_adj") { dst = eng->Phi1_adj; want = N * eng->dm.n_lme * C; }
+  else if (s == "A1_adj") { dst = eng->A1_adj; want = N * 16 * C; eng->A1adj_kept = true; }
+  else if (s != "node_forces") return -fail(SMX_ERR_INVALID, std::string("stage '") + name + "' cannot be written");
+  if (s == "node_forces") want = 3 * eng->lastE;
+  if (n != want)
+    return -fail(SMX_ERR_INVALID, "stage " + s + " holds " + std::to_string(want) + " values, got " + std::to_string(n));
+  try {
+    check(cudaSetDevice(eng->device), "cudaSetDevice");
+    check(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
+    if (n == 0) return 0;
+    if (s == "node_forces") {
+      check(cudaMemcpy(eng->forces, values, sizeof(double) * n, cudaMemcpyHostToDevice), "H2D");
+    } else {
+      std::vector<float> tmp(values, values + n);
+      check(cudaMemcpy(dst, tmp.data(), sizeof(float) * n, cudaMemcpyHostToDevice), "H2D");
+    }
+  } catch (const std::exception& e) {
+    return -fail(SMX_ERR_CUDA, e.what());
+  }
+  return n;
+}
+
+int smx_run_stage(smx_engine* eng, const char* stage, int num_nodes, const int* node_types, const int* num_neigh,
+                  const int* neigh_indices, const int* neigh_types, long num_edges, const double* xyz,
+                  const double* r, int flags) {
+  if (!eng || !stage) return fail(SMX_ERR_INVALID, "NULL argument");
+  const std::string st(stage);
+  const bool edge_stage = st == "compute_Phi1" || st == "reverse_Phi1";
+  const bool node_stage = st == "compute_H1" || st == "reverse_H1" || st == "compute_A1" || st == "reverse_A1";
+  if (!edge_stage && !node_stage) return fail(SMX_ERR_INVALID, "unknown stage '" + st + "'");
+  try {
+    check(cudaSetDevice(eng->device), "cudaSetDevice");
+    cudaStream_t s = eng->stream;
+    if (node_stage) {
+      if (!eng->evaluated) return fail(SMX_ERR_INVALID, "no evaluation has set up the engine's buffers yet");
+      if (num_nodes != eng->lastN)
+        return fail(SMX_ERR_INVALID, "num_nodes differs from the evaluation that set up the engine's buffers");
+      if (st == "reverse_A1" && !eng->A1adj_kept)
+        return fail(SMX_ERR_INVALID, "A1_adj was not written by the last evaluation (set it or keep_stages)");
+      if (st == "compute_H1" && !eng->M0_kept)
+        return fail(SMX_ERR_INVALID, "M0 was not written by the last evaluation (set it or keep_stages)");
+      if (st == "compute_A1" && !eng->Phi1_kept)
+        return fail(SMX_ERR_INVALID, "Phi1 was not written by the last evaluation (set it or keep_stages)");
+      eng->run_node_stage(st, s);
+    } else {
+      const int code = upload_edges(eng, num_nodes, node_types, num_neigh, neigh_indices, neigh_types, num_edges, xyz, r);
+      if (code != SMX_OK) return code;
+      // (the upload may have regrown the workspace, which drops its contents)
+      if (!eng->evaluated || num_nodes != eng->lastN) {  // buffers for a new node count: nothing to read yet
+        const long C = eng->dm.C;
+        check(cudaMemsetAsync(eng->H1, 0, sizeof(float) * num_nodes * eng->dm.nLM * C, s), "cudaMemsetAsync");
+        check(cudaMemsetAsync(eng->H1_adj, 0, sizeof(float) * num_nodes * eng->dm.nLM * C, s), "cudaMemsetAsync");
+        check(cudaMemsetAsync(eng->Phi1_adj, 0, sizeof(float) * num_nodes * eng->dm.n_lme * C, s), "cudaMemsetAsync");
+        eng->lastN = num_nodes;
+        eng->evaluated = true;
+        eng->M0_kept = eng->Phi1_kept = eng->A1adj_kept = false;
+      }
+      if (num_edges != eng->lastE) check(cudaMemsetAsync(eng->forces, 0, sizeof(double) * 3 * num_edges, s), "memset");
+      eng->lastE = num_edges;
+      smx::EdgeIn in{eng->first, eng->ntype, eng->nidx, eng->ntype_e, eng->xyz, eng->r, num_nodes};
+      eng->run_edge_stage(st == "reverse_Phi1", in, num_edges, (flags & SMX_STAGE_ZERO_DXYZ) != 0,
+                          (flags & SMX_STAGE_ZERO_H1_ADJ) != 0, s);
+    }
+    check(cudaGetLastError(), "kernel launch");
+    check(cudaStreamSynchronize(s), "stage");
+  } catch (const std::exception& e) {
+    return fail(SMX_ERR_CUDA, e.what());
+  }
+  if (eng->take_status() != SMX_OK) return fail(SMX_ERR_TIMEOUT, "a device-side wait timed out; results are invalid");
+  return SMX_OK;
 }
 
 }  // extern "C"

@@ -91,6 +91,7 @@ struct smx_engine {
   int* nneigh = nullptr;      // num_neigh of the host-pointer call
   double *xyz = nullptr, *r = nullptr, *energies = nullptr, *forces = nullptr;
   int lastN = 0;
+  long lastE = 0;                  // edges of the last host- or device-pointer call or stage call
   bool evaluated = false;          // the workspace holds the stages of an evaluation
   bool M0_kept = false, Phi1_kept = false, A1adj_kept = false;  // float32 rows written by it
 
@@ -564,6 +565,77 @@ struct smx_engine {
     if (v == 0) return SMX_OK;
     *reinterpret_cast<volatile unsigned*>(status_host) = 0;
     return SMX_ERR_TIMEOUT;
+  }
+
+  // ---- single stages (the reference binding's compute_* / reverse_*, symmetrix/source/
+  // cpp/mace.cpp:152-179) on the workspace of the last evaluation.  The channel-mixing
+  // GEMMs run on the float32 SIMT kernel in both precision forms; compute_Phi1 also
+  // evaluates R1 and Y (one fused kernel, as in the full pass); the layer-1 kernels run
+  // without the density-normalisation terms, which belong to compute_A1_scaled and
+  // reverse_A1_scaled (fused into the node tail).
+  smx::GemmBatch node_gemm(const float* X, float* Y, const float* const* W, int nb, bool per_l, bool trans) const {
+    // per_l false: the L blocks of [N][nLM][C] (H1 and its adjoint); true: the l blocks of
+    // Phi1 [N][n_lme][C] against A1 [N][16][C] (trans: A1_adj -> Phi1_adj)
+    const int C = dm.C, N = lastN;
+    smx::GemmBatch b{};
+    if (!per_l) {
+      for (int L = 0; L < nb; ++L)
+        b.s[b.n++] = seg_rows(X, Y, W[L], N, 2 * L + 1, C, C, static_cast<long>(dm.nLM) * C, L * L * C, C,
+                              static_cast<long>(dm.nLM) * C, L * L * C, C);
+      return b;
+    }
+    for (int l = 0; l < 4; ++l) {
+      if (dm.num_e[l] == 0) continue;
+      const int K = dm.num_e[l] * C;
+      if (!trans)
+        b.s[b.n++] = seg_rows(X, Y, W[l], N, 2 * l + 1, K, C, static_cast<long>(dm.n_lme) * C, dm.lme_off[l] * C, K,
+                              16L * C, l * l * C, C);
+      else
+        b.s[b.n++] = seg_rows(X, Y, W[l], N, 2 * l + 1, C, K, 16L * C, l * l * C, C,
+                              static_cast<long>(dm.n_lme) * C, dm.lme_off[l] * C, K);
+    }
+    return b;
+  }
+
+  // "compute_H1", "reverse_H1", "compute_A1", "reverse_A1": node stages of the last N
+  bool run_node_stage(const std::string& st, cudaStream_t s) {
+    const int C = dm.C;
+    const float* WH[3] = {dm.H1W, dm.H1W + static_cast<size_t>(C) * C, dm.H1W + 2 * static_cast<size_t>(C) * C};
+    const float* WHT[3] = {dm.H1W_T, dm.H1W_T + static_cast<size_t>(C) * C, dm.H1W_T + 2 * static_cast<size_t>(C) * C};
+    if (st == "compute_H1") {
+      smx::launch_gemm(node_gemm(M0, H1, WH, dm.L_max + 1, false, false), s);
+    } else if (st == "reverse_H1") {
+      smx::launch_gemm(node_gemm(H1_adj, M0_adj, WHT, dm.L_max + 1, false, false), s);
+    } else if (st == "compute_A1") {
+      smx::launch_gemm(node_gemm(Phi1, A1, dm.A1W, 4, true, false), s);
+    } else if (st == "reverse_A1") {
+      smx::launch_gemm(node_gemm(A1_adj, Phi1_adj, dm.A1W_T, 4, true, true), s);
+      A1adj_kept = true;
+    } else {
+      return false;
+    }
+    return true;
+  }
+
+  // "compute_Phi1" (with R1 and Y) and "reverse_Phi1" on the edges `in` (E edges): the
+  // forward writes Phi1; the adjoint adds dPhi1-contracted terms to H1_adj (from zero with
+  // zero_h1adj) and sets node_forces to its per-edge forces (added to the current ones
+  // unless zero_dxyz), as mace.cpp:504-605 with its two flags
+  void run_edge_stage(bool reverse, const smx::EdgeIn& in, long E, bool zero_dxyz, bool zero_h1adj,
+                      cudaStream_t s) {
+    smx::DevModel m = dm;
+    m.dens_spl[0] = m.dens_spl[1] = nullptr;
+    m.op_phi1 = nullptr;
+    const long nh = static_cast<long>(in.N) * dm.nLM * dm.C;
+    if (!reverse) {
+      smx::launch_layer1_fwd(m, in, H1, Phi1, s);
+      Phi1_kept = true;
+      return;
+    }
+    smx::launch_rows_to_fixed(H1_adj, H1_adj_fx, nh, zero_h1adj, s);
+    smx::launch_layer1_rev(m, in, H1, Phi1_adj, H1_adj_fx, f1, s);
+    smx::launch_fixed_rows(H1_adj_fx, H1_adj, nullptr, in.N * static_cast<long>(dm.nLM), dm.C, 1, s);
+    smx::launch_forces_from_f1(forces, f1, dm.f1_stride, dm.l2_split, 3 * E, zero_dxyz, s);
   }
 
   // The full forward + adjoint pass on device-resident inputs (tuning the atom schedule

@@ -306,6 +306,37 @@ void launch_fixed_rows(const fix64* src, float* dst, __nv_bfloat16* bf, long row
   k_fixed_rows<<<blocks, 256, 0, s>>>(src, dst, bf, rows, C, terms);
 }
 
+// Single-stage calls (the reference binding's reverse_Phi1): the fixed-point H1_adj
+// accumulator from float rows (zero: from nothing), and the per-edge forces of the layer-1
+// adjoint, node_forces = (zero ? 0 : node_forces) - sum over channel slices of f1.
+__global__ void k_rows_to_fixed(const float* __restrict__ src, fix64* __restrict__ dst, long n, int zero) {
+  for (long t = blockIdx.x * static_cast<long>(blockDim.x) + threadIdx.x; t < n;
+       t += static_cast<long>(gridDim.x) * blockDim.x)
+    dst[t] = zero ? 0ull : to_fixed(src[t]);
+}
+
+__global__ void k_forces_from_f1(double* __restrict__ forces, const double* __restrict__ f1, long stride, int nslices,
+                                 long n, int zero) {
+  for (long t = blockIdx.x * static_cast<long>(blockDim.x) + threadIdx.x; t < n;
+       t += static_cast<long>(gridDim.x) * blockDim.x) {
+    double f = f1[t];
+    for (int h = 1; h < nslices; ++h) f += f1[h * stride + t];
+    forces[t] = (zero ? 0.0 : forces[t]) - f;
+  }
+}
+
+void launch_rows_to_fixed(const float* src, fix64* dst, long n, bool zero, cudaStream_t s) {
+  if (n <= 0) return;
+  k_rows_to_fixed<<<static_cast<int>(std::min<long>((n + 255) / 256, 152L * 16)), 256, 0, s>>>(src, dst, n, zero);
+}
+
+void launch_forces_from_f1(double* forces, const double* f1, long stride, int nslices, long n, bool zero,
+                           cudaStream_t s) {
+  if (n <= 0) return;
+  k_forces_from_f1<<<static_cast<int>(std::min<long>((n + 255) / 256, 152L * 16)), 256, 0, s>>>(forces, f1, stride,
+                                                                                               nslices, n, zero);
+}
+
 // Centre atoms sorted by species (a counting sort; the order inside a species is
 // arbitrary: every atom's results are computed the same way whichever block takes it).
 // One block.

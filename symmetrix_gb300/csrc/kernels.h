@@ -54,6 +54,11 @@ void launch_node_tail(const DevModel& m, const int* node_type, int N, float* A1,
 // dst[rows][C] = the fixed-point rows src as float; bf (optional): their bf16 split terms,
 // row pitch terms * C
 void launch_fixed_rows(const fix64* src, float* dst, __nv_bfloat16* bf, long rows, int C, int terms, cudaStream_t s);
+// single-stage calls: dst = fixed-point copy of src (zero: dst = 0); forces = (zero ? 0 :
+// forces) - the sum of the nslices f1 slices (stride apart), n = 3 * edges
+void launch_rows_to_fixed(const float* src, fix64* dst, long n, bool zero, cudaStream_t s);
+void launch_forces_from_f1(double* forces, const double* f1, long stride, int nslices, long n, bool zero,
+                           cudaStream_t s);
 void launch_scan_first(const int* num_neigh, int N, int* first, cudaStream_t s);
 // input check of the host API (bits of the flags word)
 constexpr unsigned kBadNodeType = 1, kBadNumNeigh = 2, kBadEdgeCount = 4, kBadNeighIndex = 8, kBadNeighType = 16,

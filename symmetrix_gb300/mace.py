@@ -4,8 +4,15 @@ Mirrors `symmetrix.MACE` (symmetrix/source/cpp/mace.cpp:12-243): construct from 
 JSON model path, call `compute_node_energies_forces(num_nodes, node_types,
 num_neigh, neigh_indices, neigh_types, xyz, r)`, then read `node_energies` and
 `node_forces` (= -dE/dxyz per directed edge).  Stage buffers (`A0`, `M0`, `H1`,
-`Phi1`, `A1`, `M1`, `H2` and the `*_adj` adjoints) are exposed read-only for
-stage-level checks like the reference's test_mace.py.  Errors raise ValueError /
+`Phi1`, `A1`, `M1`, `H2` and the `*_adj` adjoints) are attributes as in the reference
+binding; those of the separately launched stages are also writable (`M0`, `H1`, `Phi1`,
+`A1`, `M0_adj`, `H1_adj`, `Phi1_adj`, `A1_adj`), and the binding's per-stage calls
+compute_H1 / reverse_H1, compute_Phi1 / reverse_Phi1 and compute_A1 / reverse_A1 run
+single GPU launches on them, so stage-level checks read like the reference's
+test_mace.py.  compute_R1 and compute_Y record their edge inputs for compute_Phi1,
+which evaluates R1 and Y in its own kernel; the stages fused into one kernel (the
+layer-0 stages; compute_A1_scaled, compute_M1, compute_H2, compute_readouts and their
+reverses) run only inside compute_node_energies_forces.  Errors raise ValueError /
 RuntimeError like the reference binding.
 """
 import ctypes
@@ -16,6 +23,7 @@ from . import _lib
 
 STAGES = ("A0", "M0", "H1", "Phi1", "A1", "M1", "H2", "A0_adj", "M0_adj", "H1_adj", "Phi1_adj", "A1_adj",
           "M1_adj", "H2_adj")
+WRITABLE = ("M0", "H1", "Phi1", "A1", "M0_adj", "H1_adj", "Phi1_adj", "A1_adj")
 
 
 def _ptr(a):
@@ -180,6 +188,72 @@ class MACE:
         if name in STAGES:
             return self.stage(name)
         raise AttributeError(name)
+
+    def __setattr__(self, name, value):
+        if name in WRITABLE:
+            self.set_stage(name, value)
+        else:
+            object.__setattr__(self, name, value)
+
+    def set_stage(self, name, values):
+        """Write a stage buffer of the current node count (float64 values, the layout stage() reads)."""
+        v = np.ascontiguousarray(values, dtype=np.float64).reshape(-1)
+        n = self._lib.smx_set_stage(self._h, name.encode(), _ptr(v), v.size)
+        if n < 0:
+            _lib.raise_for(-n, self._lib)
+
+    # ---- per-stage calls (symmetrix/source/cpp/mace.cpp:52-179) ----
+    def _run(self, stage, num_nodes, edges=None, flags=0):
+        if edges is None:
+            code = self._lib.smx_run_stage(self._h, stage.encode(), int(num_nodes), None, None, None, None, 0, None,
+                                           None, flags)
+        else:
+            node_types, num_neigh, neigh_indices, neigh_types, xyz, r = edges
+            a = [np.ascontiguousarray(node_types, np.int32)[:num_nodes],
+                 np.ascontiguousarray(num_neigh, np.int32)[:num_nodes], np.ascontiguousarray(neigh_indices, np.int32),
+                 np.ascontiguousarray(neigh_types, np.int32), np.ascontiguousarray(xyz, np.float64).reshape(-1),
+                 np.ascontiguousarray(r, np.float64)]
+            E = len(a[5])
+            if len(a[2]) != E or len(a[3]) != E or len(a[4]) != 3 * E:
+                raise ValueError("edge arrays have inconsistent lengths")
+            code = self._lib.smx_run_stage(self._h, stage.encode(), int(num_nodes), _ptr(a[0]), _ptr(a[1]),
+                                           _ptr(a[2]), _ptr(a[3]), E, _ptr(a[4]), _ptr(a[5]), flags)
+        _lib.raise_for(code, self._lib)
+
+    def compute_R1(self, num_nodes, node_types, num_neigh, neigh_types, r):
+        """Records the centre/neighbour species and edge lengths for compute_Phi1, whose
+        kernel evaluates the radials R1 itself (no R1 buffer)."""
+        object.__setattr__(self, "_r1_args", (np.array(node_types), np.array(neigh_types), np.array(r)))
+
+    def compute_Y(self, xyz):
+        """Records the edge vectors for compute_Phi1, whose kernel evaluates Y itself."""
+        object.__setattr__(self, "_y_args", np.array(xyz, dtype=np.float64))
+
+    def compute_Phi1(self, num_nodes, num_neigh, neigh_indices):
+        """Phi1 from H1 on the edges of compute_R1 / compute_Y (mace.cpp:453-502)."""
+        node_types, neigh_types, r = self._r1_args
+        self._run("compute_Phi1", num_nodes, (node_types, num_neigh, neigh_indices, neigh_types, self._y_args, r))
+
+    def reverse_Phi1(self, num_nodes, num_neigh, neigh_indices, xyz, r, zero_dxyz, zero_H1_adj):
+        """H1_adj and node_forces from Phi1_adj (mace.cpp:504-605), with the reference's two flags."""
+        node_types, neigh_types, _ = self._r1_args
+        if not zero_dxyz:  # add to the current node_forces, as the reference does
+            self.set_stage("node_forces", self.node_forces)
+        self._run("reverse_Phi1", num_nodes, (node_types, num_neigh, neigh_indices, neigh_types, xyz, r),
+                  (1 if zero_dxyz else 0) | (2 if zero_H1_adj else 0))
+        object.__setattr__(self, "node_forces", self.stage("node_forces"))
+
+    def compute_H1(self, num_nodes):
+        self._run("compute_H1", num_nodes)
+
+    def reverse_H1(self, num_nodes):
+        self._run("reverse_H1", num_nodes)
+
+    def compute_A1(self, num_nodes):
+        self._run("compute_A1", num_nodes)
+
+    def reverse_A1(self, num_nodes):
+        self._run("reverse_A1", num_nodes)
 
 
 class MACEKokkos(MACE):

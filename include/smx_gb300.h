@@ -176,7 +176,10 @@ int smx_run_stage(smx_engine* eng, const char* stage, int num_nodes, const int* 
  * "cg_padded" (1, the default: the layer-1 Clebsch-Gordan contractions read tables padded
  * to a fixed number of terms per row, with independent loads; 0: the compressed rows);
  * BF16 form: "tc_terms" (1, 2 or 3 bf16 split terms of the GEMM operands, default 3;
- * set before the first evaluation).
+ * set before the first evaluation); "test_gemm_timeout" (n in [0, 16]: a test of the
+ * timeout path, the next n tensor-core GEMM launches issue no load so that their bounded
+ * wait gives up after 2 ms with nothing in flight; the call that ran them, or smx_sync
+ * after a device-pointer call, returns SMX_ERR_TIMEOUT and the results are invalid).
  * No counterpart in the reference (its MACE object has no options). */
 int smx_set_option(smx_engine* eng, const char* key, long value);
 /* Read an option or a tuned schedule entry ("tc_nt_<G>", "tc_stages_<G>",

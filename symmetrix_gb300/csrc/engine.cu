@@ -153,6 +153,12 @@ int smx_set_option(smx_engine* eng, const char* key, long value) {
     eng->sched_set(value == 1 ? 1 : 0);
     return SMX_OK;
   }
+  if (std::strcmp(key, "test_gemm_timeout") == 0) {  // test of the error path (see engine.hpp)
+    if (value < 0 || value > 16) return fail(SMX_ERR_INVALID, "test_gemm_timeout must be in [0, 16]");
+    if (eng->precision != SMX_PRECISION_BF16) return fail(SMX_ERR_INVALID, "test_gemm_timeout applies to the bf16 form");
+    eng->test_gemm_timeout = static_cast<int>(value);
+    return SMX_OK;
+  }
   if (std::strcmp(key, "tc_terms") == 0) {  // precision form: bf16 split terms of the GEMMs
     if (value < 1 || value > 3) return fail(SMX_ERR_INVALID, "tc_terms must be 1, 2 or 3");
     if (eng->precision != SMX_PRECISION_BF16) return fail(SMX_ERR_INVALID, "tc_terms applies to the bf16 form");

@@ -399,6 +399,9 @@ struct smx_engine {
   bool tc_tuned[4] = {false, false, false, false};
   bool autotune = true;
   float tc_tuned_us[4] = {0, 0, 0, 0};
+  // test of the timeout path: this many of the next tensor-core GEMM launches issue no
+  // load, so their bounded wait gives up (option "test_gemm_timeout")
+  int test_gemm_timeout = 0;
 
   void tc_apply(const TcCfg& c, smx::UmmaGemm* g, int ng, bool tile_n) const {
     for (int q = 0; q < ng; ++q) {
@@ -454,7 +457,9 @@ struct smx_engine {
       if (cs == cudaStreamCaptureStatusNone) tc_tune(gid, g, ng, tile_n, s);
     }
     tc_apply(tc_cfg[gid], g, ng, tile_n);
-    smx::launch_umma_gemms(g, ng, status_dev, s);
+    const bool test = test_gemm_timeout > 0;
+    if (test) --test_gemm_timeout;
+    smx::launch_umma_gemms(g, ng, status_dev, s, test);
   }
 
   // padded Clebsch-Gordan tables (option "cg_padded" 0 switches the kernels to the

@@ -49,6 +49,10 @@ struct UmmaSegDev {
 };
 struct UmmaGroupDev {
   UmmaSegDev s[4];
+  // test of the error path: the producer issues no load and the MMA thread waits
+  // wait_ns for one, so its bounded wait runs out with nothing in flight
+  int skip_loads;
+  uint64_t wait_ns;
 };
 
 __global__ void __launch_bounds__(128, 1) k_umma_gemm(const __grid_constant__ UmmaGroupDev grp, unsigned* status) {
@@ -90,7 +94,7 @@ __global__ void __launch_bounds__(128, 1) k_umma_gemm(const __grid_constant__ Um
   // producer: k-block kb goes to stage kb % S once the MMAs of k-block kb - S released it
   int loads = 0;
   bool prod_ok = true;
-  if (threadIdx.x == 0) {
+  if (threadIdx.x == 0 && !grp.skip_loads) {
     for (int kb = 0; kb < KB; ++kb) {
       const int s = kb % S;
       if (kb >= S && !sm100::mbar_wait(&empty[s], ((kb / S) - 1) & 1)) {
@@ -110,7 +114,7 @@ __global__ void __launch_bounds__(128, 1) k_umma_gemm(const __grid_constant__ Um
     const uint32_t idesc = sm100::idesc_bf16_f32(kTileM, NT);
     for (int kb = 0; kb < KB; ++kb) {
       const int s = kb % S;
-      if (!sm100::mbar_wait(&full[s], (kb / S) & 1)) {
+      if (!sm100::mbar_wait(&full[s], (kb / S) & 1, grp.wait_ns)) {
         mma_ok = false;
         break;
       }
@@ -254,10 +258,12 @@ cudaError_t init_umma_kernels() {
                               static_cast<int>(kMaxDynSmem));
 }
 
-void launch_umma_gemms(const UmmaGemm* g, int n, unsigned* status, cudaStream_t s) {
+void launch_umma_gemms(const UmmaGemm* g, int n, unsigned* status, cudaStream_t s, bool test_timeout) {
   if (n < 1 || n > 4) throw std::invalid_argument("1 to 4 tensor-core GEMMs per launch");
   UmmaGroupDev grp;
   std::memset(&grp, 0, sizeof(grp));
+  grp.skip_loads = test_timeout ? 1 : 0;
+  grp.wait_ns = test_timeout ? 2000000ull : sm100::kWaitLimitNs;  // 2 ms when testing
   unsigned gx = 0, gy = 0;
   size_t smem = 0;
   int used = 0;

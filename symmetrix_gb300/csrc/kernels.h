@@ -96,7 +96,9 @@ struct UmmaGemm {
   int stages = 4;  // shared-memory ring depth, 1..4
 };
 // 1 to 4 GEMMs in one launch.
-void launch_umma_gemms(const UmmaGemm* g, int n, unsigned* status, cudaStream_t s);
+// test_timeout: a test of the error path (no TMA load is issued and the MMA thread's
+// wait gives up after 2 ms: the launch records a timeout in *status and writes nothing)
+void launch_umma_gemms(const UmmaGemm* g, int n, unsigned* status, cudaStream_t s, bool test_timeout = false);
 // Row r of dst (pitch terms*width): the bf16 split terms (hi), (hi | hi) or (hi | lo | hi) of
 // src[(r / rpn) * s_ns + s_off + (r % rpn) * s_rs + c], c < width (multiple of 4)
 void launch_rows_to_bf16(const float* src, __nv_bfloat16* dst, long rows, int width, int rpn, long s_ns, int s_off,

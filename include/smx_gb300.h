@@ -237,9 +237,11 @@ void smx_md_destroy(smx_md* md);
  * node_forces[3*num_edges] (as returned by smx_compute_node_energies_forces_device),
  * out[10] = {sum of node energies, W_xx, W_xy, ..., W_zz} with W_ab = sum_e xyz_e,a f_e,b.
  * Scratch is a fixed 1.25 MiB device array inside the library (one float64 partial per
- * 4096 nodes/edges), so at most 67,108,864 nodes and edges are accepted; larger inputs
- * return SMX_ERR_CAPACITY without launching.  The first call on each device looks up
- * that array's device address; make it before any stream capture.  Every call on a
+ * 4096 nodes/edges), so at most 67,108,864 nodes and at most 67,108,864 edges are
+ * accepted; larger inputs return SMX_ERR_CAPACITY without launching.  The first call on
+ * each device looks up that array's device address; make it before any stream capture.
+ * That address belongs to the device's primary context: a process that resets the
+ * device (cudaDeviceReset) must not call this entry point on it afterwards.  Every call on a
  * device shares that array (it keeps the last call's partial sums; nothing in it needs
  * to start at zero), so calls that overlap on the same GPU, e.g. on two streams, race:
  * serialise them.  Enqueued on `stream`

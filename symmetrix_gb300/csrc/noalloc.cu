@@ -29,7 +29,7 @@ int fail(int code, const std::string& msg);
 namespace {
 
 constexpr int kChunk = 4096;          // nodes and edges summed by one block into one partial
-constexpr int kMaxPartials = 16384;   // => at most 16384 * 4096 = 67,108,864 nodes and edges
+constexpr int kMaxPartials = 16384;   // => at most 16384 * 4096 = 67,108,864 nodes, and as many edges
 constexpr int kMaxDevices = 128;
 
 // 10 float64 per partial: energy, then the 9 virial components.  Every slot the final
@@ -42,6 +42,9 @@ double* g_partials_addr[kMaxDevices] = {};  // device address of g_partials, per
 
 // Device address of g_partials on the current device.  Resolved once per device, on
 // that device's first call (which should therefore happen before any stream capture).
+// The address belongs to the device's primary context: after cudaDeviceReset (or
+// anything else that destroys and recreates that context) it is stale, and a caller
+// that resets a device must not call this entry point on it again in the same process.
 cudaError_t scratch_address(double** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -69,7 +72,9 @@ __global__ void __launch_bounds__(256) k_partials_noalloc(int N, long E, const d
   const long b0 = static_cast<long>(blockIdx.x) * kChunk;
   for (long e = b0 + threadIdx.x; e < b0 + kChunk && e < E; e += blockDim.x)
     for (int a = 0; a < 3; ++a)
-      for (int c = 0; c < 3; ++c) acc[1 + 3 * a + c].add(xyz[3 * e + a] * f[3 * e + c]);
+      // __dmul_rn: the product is rounded on its own (no fused multiply-add with the
+      // compensated sum's addition), so add() sees exactly the value it compensates for
+      for (int c = 0; c < 3; ++c) acc[1 + 3 * a + c].add(__dmul_rn(xyz[3 * e + a], f[3 * e + c]));
   for (long i = b0 + threadIdx.x; i < b0 + kChunk && i < N; i += blockDim.x) acc[0].add(energies[i]);
   for (int q = 0; q < 10; ++q) sh[q][threadIdx.x] = acc[q].value();
   __syncthreads();
@@ -100,7 +105,8 @@ extern "C" int smx_energy_virial_device_noalloc(int num_nodes, long num_edges, c
   if (chunks > kMaxPartials)
     return smx::fail(SMX_ERR_CAPACITY,
                      "smx_energy_virial_device_noalloc: at most " + std::to_string(long(kMaxPartials) * kChunk) +
-                         " nodes and edges (fixed device scratch of " + std::to_string(kMaxPartials) +
+                         " nodes and at most " + std::to_string(long(kMaxPartials) * kChunk) +
+                         " edges (fixed device scratch of " + std::to_string(kMaxPartials) +
                          " partial sums); got " + std::to_string(num_nodes) + " nodes, " +
                          std::to_string(num_edges) + " edges");
   if (!out || (num_nodes > 0 && !node_energies) || (num_edges > 0 && (!xyz || !node_forces)))

@@ -26,6 +26,8 @@
 // (DevModel::l2_split) so that two blocks share an SM.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "device.cuh"
 #include "kernels.h"
 
@@ -745,14 +747,17 @@ __host__ __device__ constexpr bool l2_uses_l2(int l2) {
   return false;
 }
 
-// Adjoint, group G, one staged chunk (as l1_rev_edge, scalar, this group's paths).
+// Adjoint, group G, edges [a0, a1) of a staged chunk (as l1_rev_edge, scalar, this
+// group's paths).  The H1_adj terms of the four groups meet in hold ([kSub2][4 groups]
+// [NL2][CH] floats, zero for the rows a group does not touch), and after a block barrier
+// l2_rev_flush adds each row once per channel (as in the L_max = 1 adjoint).
+constexpr int kSub2 = 8;
 template <int G>
-__device__ __forceinline__ void l2_rev_chunk(const DevModel& m, const float* __restrict__ H1,
-                                             fix64* __restrict__ H1_adj, const L1Stage<true>& st, int C, int k,
-                                             bool live, const float* g, float (*sF)[16][3]) {
+__device__ __forceinline__ void l2_rev_chunk(const DevModel& m, const float* __restrict__ H1, const L1Stage<true>& st,
+                                             int C, int k, bool live, const float* g, float (*sF)[16][3],
+                                             float* hold, int CH, int kk, int a0, int a1) {
   constexpr int NL2 = 9, NI = 17;
-  const int na = st.nact;
-  for (int a = 0; a < na; ++a) {
+  for (int a = a0; a < a1; ++a) {
     const int t = st.act[a];
     const float x = st.x[t];
     const int j = st.j[t];
@@ -801,14 +806,27 @@ __device__ __forceinline__ void l2_rev_chunk(const DevModel& m, const float* __r
     if (!live) fx = fy = fz = 0.0f;
     block_reduce3_w16(fx, fy, fz, sF, t);
     if (live) {
-      fix64* dst = H1_adj + static_cast<size_t>(j) * NL2 * C + k;
-      static_for<3>([&](auto lc) {
-        constexpr int l2 = decltype(lc)::value;
-        if constexpr (l2_uses_l2<G>(l2)) {
+      float* hb = hold + ((a - a0) * kL2Groups + G) * NL2 * CH + kk;
 #pragma unroll
-          for (int b = 0; b < 2 * l2 + 1; ++b) add_fixed(dst + (l2 * l2 + b) * C, hadj[l2 * l2 + b]);
-        }
-      });
+      for (int b = 0; b < NL2; ++b) hb[b * CH] = hadj[b];
+    }
+  }
+}
+
+// After the barrier that follows l2_rev_chunk: the rows b = grp (mod 4) of edges [a0, a1),
+// the four groups' terms summed in group order, to the fixed-point accumulator.
+__device__ __forceinline__ void l2_rev_flush(fix64* __restrict__ H1_adj, const L1Stage<true>& st, int C, int k,
+                                             bool live, const float* hold, int CH, int kk, int grp, int a0, int a1) {
+  constexpr int NL2 = 9;
+  if (!live) return;
+  for (int a = a0; a < a1; ++a) {
+    const float* hb = hold + (a - a0) * kL2Groups * NL2 * CH + kk;
+    fix64* dst = H1_adj + static_cast<size_t>(st.j[st.act[a]]) * NL2 * C + k;
+    for (int b = grp; b < NL2; b += kL2Groups) {
+      float v = hb[b * CH];
+#pragma unroll
+      for (int q = 1; q < kL2Groups; ++q) v += hb[(q * NL2 + b) * CH];
+      add_fixed(dst + b * C, v);
     }
   }
 }
@@ -871,13 +889,20 @@ __device__ __forceinline__ void layer1_rev_l2_atom(const DevModel& m, const Edge
     __syncthreads();
     stage_l1<true>(m, in, ti, eb, ne, st);
     __syncthreads();
-    switch (grp) {
-      case 0: l2_rev_chunk<0>(m, H1, H1_adj, st, C, k, live, g, sF); break;
-      case 1: l2_rev_chunk<1>(m, H1, H1_adj, st, C, k, live, g, sF); break;
-      case 2: l2_rev_chunk<2>(m, H1, H1_adj, st, C, k, live, g, sF); break;
-      default: l2_rev_chunk<3>(m, H1, H1_adj, st, C, k, live, g, sF); break;
+    // the staged dPhi1 rows and sP are dead now: the H1_adj terms of kSub2 edges at a time
+    float* hold = dyn;
+    for (int a0 = 0; a0 < st.nact; a0 += kSub2) {
+      const int a1 = min(st.nact, a0 + kSub2);
+      switch (grp) {
+        case 0: l2_rev_chunk<0>(m, H1, st, C, k, live, g, sF, hold, CH, kk, a0, a1); break;
+        case 1: l2_rev_chunk<1>(m, H1, st, C, k, live, g, sF, hold, CH, kk, a0, a1); break;
+        case 2: l2_rev_chunk<2>(m, H1, st, C, k, live, g, sF, hold, CH, kk, a0, a1); break;
+        default: l2_rev_chunk<3>(m, H1, st, C, k, live, g, sF, hold, CH, kk, a0, a1); break;
+      }
+      __syncthreads();
+      l2_rev_flush(H1_adj, st, C, k, live, hold, CH, kk, grp, a0, a1);
+      __syncthreads();
     }
-    __syncthreads();
     for (int t = threadIdx.x; t < ne; t += blockDim.x) {
       double sum[3] = {0.0, 0.0, 0.0};
       const long e = static_cast<long>(eb) + t;
@@ -912,13 +937,22 @@ int layer1_block(int C) { return 2 * (((C >> 1) + 31) & ~31); }
 
 namespace {
 
+// dynamic shared memory of the L_max = 2 adjoint: the staged dPhi1 rows and the g table,
+// and later the H1_adj terms of kSub2 edges (see l2_rev_chunk)
+size_t rev_l2_smem(const DevModel& m) {
+  return sizeof(float) * std::max<size_t>(m.n_lme + ins_np(2), kSub2 * kL2Groups * 9) * l2_slice_width(m);
+}
+
+// dynamic shared memory of the L_max = 1 adjoint: the staged dPhi1 rows and the g table
+size_t rev_l1_smem(const DevModel& m) { return sizeof(float) * (m.n_lme + ins_np(1)) * m.C; }
+
 template <int CT, bool P>
 cudaError_t set_smem(const DevModel& m) {
   cudaError_t e = cudaFuncSetAttribute(k_layer1_fwd<1, CT, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(sizeof(float) * ins_np(1) * m.C));
   if (e != cudaSuccess) return e;
   return cudaFuncSetAttribute(k_layer1_rev<1, CT, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              static_cast<int>(sizeof(float) * (m.n_lme + ins_np(1)) * m.C));
+                              static_cast<int>(rev_l1_smem(m)));
 }
 
 template <bool P>
@@ -926,8 +960,10 @@ cudaError_t set_smem_l2(const DevModel& m) {
   cudaError_t e = cudaFuncSetAttribute(k_layer1_fwd_l2<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(sizeof(float) * ins_np(2) * m.C));
   if (e != cudaSuccess) return e;
+  // (sized for one slice of all C channels: the largest rev_l2_smem of any slice count)
   return cudaFuncSetAttribute(k_layer1_rev_l2<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              static_cast<int>(sizeof(float) * (m.n_lme + ins_np(2)) * m.C));
+                              static_cast<int>(sizeof(float) * std::max(m.n_lme + ins_np(2), kSub2 * kL2Groups * 9) *
+                                               m.C));
 }
 
 // Channel counts with a compile-time specialisation (addresses fold to immediates).
@@ -994,10 +1030,10 @@ void launch_layer1_rev(const DevModel& m, const EdgeIn& in, const float* H1, con
     constexpr bool P = decltype(pc)::value;
     if (m.L_max == 2) {
       k_layer1_rev_l2<P><<<grid, kL2Groups * l2_slice_width(m),
-                           sizeof(float) * (m.n_lme + ins_np(2)) * l2_slice_width(m), s>>>(mk, in, H1, dPhi1, H1_adj, f1);
+                           rev_l2_smem(m), s>>>(mk, in, H1, dPhi1, H1_adj, f1);
       return;
     }
-    const size_t smem = sizeof(float) * (m.n_lme + ins_np(1)) * m.C;
+    const size_t smem = rev_l1_smem(m);
     dispatch_c(m.C, [&](auto ct) {
       k_layer1_rev<1, decltype(ct)::value, P><<<grid, layer1_block(m.C), smem, s>>>(mk, in, H1, dPhi1, H1_adj, f1);
     });
@@ -1011,13 +1047,13 @@ void layer1_residency(const DevModel& m, int* per_sm) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f, k_layer1_fwd_l2<true>, kL2Groups * l2_slice_width(m),
                                                   sizeof(float) * ins_np(2) * l2_slice_width(m));
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_layer1_rev_l2<true>, kL2Groups * l2_slice_width(m),
-                                                  sizeof(float) * (m.n_lme + ins_np(2)) * l2_slice_width(m));
+                                                  rev_l2_smem(m));
   } else {
     dispatch_c(m.C, [&](auto ct) {
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f, k_layer1_fwd<1, decltype(ct)::value, true>, m.C,
                                                     sizeof(float) * ins_np(1) * m.C);
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_layer1_rev<1, decltype(ct)::value, true>,
-                                                    layer1_block(m.C), sizeof(float) * (m.n_lme + ins_np(1)) * m.C);
+                                                    layer1_block(m.C), rev_l1_smem(m));
     });
   }
   per_sm[kAkLayer1Fwd] = f;

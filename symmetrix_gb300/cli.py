@@ -2,6 +2,7 @@
 
     python -m symmetrix_gb300.cli gen-model --config fp32_4096 --seed 1 --zbl out.json
     python -m symmetrix_gb300.cli eval --model out.json --atoms 4096 --density 0.10 --evals 3 [--precision bfloat16]
+                                       [--option KEY=VALUE ...]
 
     python -m symmetrix_gb300.cli cache model.json model.smxb
 
@@ -10,7 +11,8 @@
 evaluations of it through the device-pointer C ABI (the call a GPU-resident caller
 makes), printing per-evaluation device times.  `cache` writes the binary model cache
 that MACE() (smx_create) loads without parsing the JSON.  `eval` is also the small, fixed target
-used for ncu captures of single kernels.
+used for ncu captures of single kernels; --option sets engine options (smx_set_option)
+before the first evaluation, e.g. autotune=0 for a fixed schedule without tuning launches.
 """
 import argparse
 import json
@@ -38,6 +40,9 @@ def evaluate(args):
 
     build()
     eng = MACE(args.model, device=args.device, precision=args.precision)
+    for kv in args.option:
+        k, v = kv.split("=", 1)
+        eng.set_option(k, int(v))
     pos, L, species = random_box(args.atoms, args.density, args.min_dist, eng.num_elements, seed=args.seed)
     nl = neighbor_list(pos, eng.r_cut, L)
     N, E = args.atoms, len(nl["r"])
@@ -94,6 +99,7 @@ def main(argv=None):
     e.add_argument("--evals", type=int, default=3)
     e.add_argument("--device", type=int, default=0)
     e.add_argument("--precision", default="float32", choices=["float32", "bfloat16"])
+    e.add_argument("--option", action="append", default=[], help="engine option KEY=VALUE (repeatable)")
     c = sub.add_parser("cache")
     c.add_argument("model")
     c.add_argument("out")

@@ -81,6 +81,8 @@ struct DevModel {
   // between the per-slice partial edge forces in f1 (0: one slice)
   int l2_split;
   long f1_stride;
+  // the engine's status word (mapped host memory): a bounded wait that gave up sets bit 0
+  unsigned* status;
 };
 
 // Per-atom kernels, indices into DevModel::pgrid.

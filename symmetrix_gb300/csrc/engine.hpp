@@ -251,6 +251,7 @@ struct smx_engine {
       model_mem.push_back(sc);
       check(cudaMemset(sc, 0, 2 * sizeof(int)), "cudaMemset");
       m.sched = sc;
+      m.status = status_dev;  // bounded waits inside the edge kernels report here
       int nsm = 0, per_sm[smx::kAkCount] = {};
       check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device), "cudaDeviceGetAttribute");
       smx::layer0_residency(m, per_sm);

@@ -1,7 +1,7 @@
 """Python handle on the LAMMPS pair-style adapter (smx_pair_* in include/smx_gb300.h).
 
 LAMMPS itself drives the adapter from C++ (the pair style's compute() passes its own
-neighbour list and atom arrays); this wrapper exposes the same
+neighbour list and atom arrays to smx_pair_compute); this wrapper exposes the same
 call with numpy arrays for testing and for Python MD drivers that keep LAMMPS-style
 ghost atoms.  Semantics follow pair_symmetrix/pair_symmetrix_mace.cpp:242-372.
 """

@@ -3,7 +3,8 @@
 * `build_oracle()` compiles the float64 restatement oracle/mace_oracle.cpp into
   oracle/_build/liborc.so.  It builds anywhere g++ is present.
 * `build_reference()` compiles the reference's own evaluator, unchanged, from the
-  sources where they lie in the reference tree (libsymmetrix/source/*.cpp) with the
+  sources where they lie in the reference tree (libsymmetrix/source/*.cpp under
+  $SMX_REFERENCE_ROOT, default the container's reference checkout) with the
   stand-in headers under oracle/shim, plus oracle/ref_capi.cpp, into
   oracle/_ref/libsmx_ref.so.  It is skipped when the reference tree is absent.
 
@@ -15,7 +16,9 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_SRC = "/root/reference/libsymmetrix/source"
+# the reference tree (read-only); SMX_REFERENCE_ROOT points elsewhere when it lives elsewhere
+REF_ROOT = os.environ.get("SMX_REFERENCE_ROOT", "/root/reference")
+REF_SRC = os.path.join(REF_ROOT, "libsymmetrix", "source")
 REF_FILES = ["mace.cpp", "cubic_spline.cpp", "cubic_spline_set.cpp", "multivariate_polynomial.cpp",
              "multilayer_perceptron.cpp", "zbl.cpp", "tools.cpp", "spherical_harmonic.cpp"]
 

@@ -378,6 +378,34 @@ void launch_cell_list(const double* pos, int N, double3 box, int3 nc, int* cell,
   k_cell_sort<<<ceil_div(ncell, 4), 128, 0, s>>>(ncell, cell_start, cell_tmp, cell_atoms);  // one warp per cell
 }
 
+// Spatial renumbering of the MD atoms: slot k takes atom perm[k] (the cell list's order),
+// gathered into tmp_d [pos 3N | vel 3N | F 3N | inv_m N] and tmp_i [species N | orig N];
+// the caller copies them back, so that device pointers (and captured graphs) stay valid.
+__global__ void k_permute_atoms(int N, const int* __restrict__ perm, const double* __restrict__ pos,
+                                const double* __restrict__ vel, const double* __restrict__ F,
+                                const double* __restrict__ inv_m, const int* __restrict__ species,
+                                const int* __restrict__ orig, double* __restrict__ tmp_d, int* __restrict__ tmp_i) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= N) return;
+  const int a = perm[k];
+  const long n3 = 3L * N;
+  for (int c = 0; c < 3; ++c) {
+    tmp_d[3L * k + c] = pos[3L * a + c];
+    tmp_d[n3 + 3L * k + c] = vel[3L * a + c];
+    tmp_d[2 * n3 + 3L * k + c] = F[3L * a + c];
+  }
+  tmp_d[3 * n3 + k] = inv_m[a];
+  tmp_i[k] = species[a];
+  tmp_i[N + k] = orig[a];
+}
+
+void launch_permute_atoms(int N, const int* perm, const double* pos, const double* vel, const double* F,
+                          const double* inv_m, const int* species, const int* orig, double* tmp_d, int* tmp_i,
+                          cudaStream_t s) {
+  if (N <= 0) return;
+  k_permute_atoms<<<ceil_div(N, 256), 256, 0, s>>>(N, perm, pos, vel, F, inv_m, species, orig, tmp_d, tmp_i);
+}
+
 void launch_neigh_pass(bool fill, bool brute, const double* pos, const int* species, int N, double3 box, int3 nc,
                        int3 periodic, int3 nimg, double rl, const int* cell, const int* cell_start,
                        const int* cell_atoms, const int* seg_of, const int* seg_first, int* num_neigh,

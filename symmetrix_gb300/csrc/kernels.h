@@ -108,6 +108,11 @@ void launch_rows_to_bf16(const float* src, __nv_bfloat16* dst, long rows, int wi
 void launch_wrap(int N, double3 box, int3 periodic, double* pos, cudaStream_t s);
 void launch_cell_list(const double* pos, int N, double3 box, int3 nc, int* cell, int* cell_count, int* cell_start,
                       int* cell_fill, int* cell_tmp, int* cell_atoms, cudaStream_t s);
+// slot k of the MD atom arrays takes atom perm[k]: gathered into tmp_d [pos 3N | vel 3N |
+// F 3N | inv_m N] and tmp_i [species N | orig N]
+void launch_permute_atoms(int N, const int* perm, const double* pos, const double* vel, const double* F,
+                          const double* inv_m, const int* species, const int* orig, double* tmp_d, int* tmp_i,
+                          cudaStream_t s);
 void launch_neigh_pass(bool fill, bool brute, const double* pos, const int* species, int N, double3 box, int3 nc,
                        int3 periodic, int3 nimg, double rl, const int* cell, const int* cell_start,
                        const int* cell_atoms, const int* seg_of, const int* seg_first, int* num_neigh,

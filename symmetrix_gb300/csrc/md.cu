@@ -188,6 +188,18 @@ struct smx_md {
          *reduced = nullptr;
   int* species = nullptr;
   int *seg_of = nullptr, *seg_first = nullptr;  // molecule batch: atom -> molecule, molecule atom offsets
+  // Spatial renumbering (periodic boxes): every kSortEvery steps, at a neighbour rebuild, the
+  // atoms are renumbered in cell-list order (cells in index order, atoms of a cell by index),
+  // as MD codes sort their atoms: the neighbours of the centres that the blocks in flight
+  // work on then sit in a few contiguous index ranges, so their node features (H1, the
+  // fixed-point H1_adj rows, A0 ...) stay in L2 on boxes whose features exceed it.  orig[k]
+  // is the caller's index of the atom in slot k; smx_md_state reports in the caller's order.
+  bool sort_atoms = false;
+  static constexpr int kSortEvery = 200;
+  long last_sort = -1;
+  int* orig = nullptr;
+  double* tmp_d = nullptr;  // [10 N]: the gather of a renumbering
+  int* tmp_i = nullptr;     // [2 N]
   NeighList nl;
   cudaGraphExec_t graph = nullptr;
   int graph_steps = 0;
@@ -195,7 +207,7 @@ struct smx_md {
 
   ~smx_md() {
     if (graph) cudaGraphExecDestroy(graph);
-    void* ps[] = {pos, vel, F, inv_m, energies, partial, reduced, species, seg_of, seg_first};
+    void* ps[] = {pos, vel, F, inv_m, energies, partial, reduced, species, seg_of, seg_first, orig, tmp_d, tmp_i};
     for (void* p : ps)
       if (p) cudaFree(p);
   }
@@ -229,7 +241,35 @@ struct smx_md {
     smx::launch_vv_second(N, dt, F, inv_m, vel, s);
   }
 
+  // renumber the atoms in the cell list's order (no-op for boxes too small for cells)
+  void renumber(cudaStream_t s) {
+    const double rl = eng->hm.r_cut + skin;
+    const double L[3] = {box.x, box.y, box.z};
+    int n[3];
+    for (int d = 0; d < 3; ++d) {
+      n[d] = static_cast<int>(std::floor(L[d] / rl));
+      if (n[d] < 3) return;
+    }
+    const int3 nc = make_int3(n[0], n[1], n[2]);
+    nl.reserve_nodes(N, nc.x * nc.y * nc.z);
+    smx::launch_wrap(N, box, periodic, pos, s);
+    smx::launch_cell_list(pos, N, box, nc, nl.cell, nl.cell_count, nl.cell_start, nl.cell_fill, nl.cell_tmp,
+                          nl.cell_atoms, s);
+    smx::launch_permute_atoms(N, nl.cell_atoms, pos, vel, F, inv_m, species, orig, tmp_d, tmp_i, s);
+    const size_t n3 = sizeof(double) * 3 * N;
+    check(cudaMemcpyAsync(pos, tmp_d, n3, cudaMemcpyDeviceToDevice, s), "D2D");
+    check(cudaMemcpyAsync(vel, tmp_d + 3L * N, n3, cudaMemcpyDeviceToDevice, s), "D2D");
+    check(cudaMemcpyAsync(F, tmp_d + 6L * N, n3, cudaMemcpyDeviceToDevice, s), "D2D");
+    check(cudaMemcpyAsync(inv_m, tmp_d + 9L * N, sizeof(double) * N, cudaMemcpyDeviceToDevice, s), "D2D");
+    check(cudaMemcpyAsync(species, tmp_i, sizeof(int) * N, cudaMemcpyDeviceToDevice, s), "D2D");
+    check(cudaMemcpyAsync(orig, tmp_i + N, sizeof(int) * N, cudaMemcpyDeviceToDevice, s), "D2D");
+  }
+
   void rebuild(cudaStream_t s) {
+    if (sort_atoms && (last_sort < 0 || step - last_sort >= kSortEvery)) {
+      renumber(s);
+      last_sort = step;
+    }
     nl.realloc_happened = false;
     nl.build(pos, species, N, box, periodic, eng->hm.r_cut + skin, s, seg_of, seg_first);
     eng->reserve(N, nl.capE);
@@ -382,6 +422,17 @@ smx_md* md_create_impl(smx_engine* eng, int n_atoms, const double* positions, co
     check(cudaMemcpyAsync(md->inv_m, inv.data(), sizeof(double) * n_atoms, cudaMemcpyHostToDevice, s), "H2D");
     check(cudaMemcpyAsync(md->species, species, sizeof(int) * n_atoms, cudaMemcpyHostToDevice, s), "H2D");
     if (mol_first) md->set_molecules(n_mol, mol_first, s);
+    if (box_lengths && !mol_first) {  // periodic box: spatial renumbering (see smx_md)
+      md->sort_atoms = true;
+      md->orig = dalloc<int>(n_atoms);
+      md->tmp_d = dalloc<double>(10L * n_atoms);
+      md->tmp_i = dalloc<int>(2L * n_atoms);
+      std::vector<int> id(n_atoms);
+      for (int a = 0; a < n_atoms; ++a) id[a] = a;
+      check(cudaMemcpyAsync(md->orig, id.data(), sizeof(int) * n_atoms, cudaMemcpyHostToDevice, s), "H2D");
+      check(cudaMemsetAsync(md->F, 0, sizeof(double) * 3 * n_atoms, s), "cudaMemsetAsync");
+      check(cudaStreamSynchronize(s), "upload");  // `id` goes out of scope
+    }
     md->rebuild(s);
     md->forces(s);
     check(cudaStreamSynchronize(s), "initial forces");
@@ -473,10 +524,25 @@ int smx_md_state(smx_md* md, double* positions, double* velocities, double* forc
                        md->reduced, s);
     double red[10];
     check(cudaMemcpyAsync(red, md->reduced, sizeof(red), cudaMemcpyDeviceToHost, s), "D2H");
-    if (positions) check(cudaMemcpyAsync(positions, md->pos, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, s), "D2H");
-    if (velocities) check(cudaMemcpyAsync(velocities, md->vel, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, s), "D2H");
-    if (forces) check(cudaMemcpyAsync(forces, md->F, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, s), "D2H");
-    check(cudaStreamSynchronize(s), "MD state");
+    if (!md->sort_atoms) {
+      if (positions) check(cudaMemcpyAsync(positions, md->pos, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, s), "D2H");
+      if (velocities) check(cudaMemcpyAsync(velocities, md->vel, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, s), "D2H");
+      if (forces) check(cudaMemcpyAsync(forces, md->F, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, s), "D2H");
+      check(cudaStreamSynchronize(s), "MD state");
+    } else {  // renumbered atoms: slot k back to the caller's index orig[k]
+      std::vector<int> orig(N);
+      std::vector<double> tmp(3 * static_cast<size_t>(N));
+      check(cudaMemcpyAsync(orig.data(), md->orig, sizeof(int) * N, cudaMemcpyDeviceToHost, s), "D2H");
+      check(cudaStreamSynchronize(s), "MD state");
+      for (int q = 0; q < 3; ++q) {
+        double* out = q == 0 ? positions : (q == 1 ? velocities : forces);
+        const double* src = q == 0 ? md->pos : (q == 1 ? md->vel : md->F);
+        if (!out) continue;
+        check(cudaMemcpy(tmp.data(), src, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost), "D2H");
+        for (int k = 0; k < N; ++k)
+          for (int c = 0; c < 3; ++c) out[3 * static_cast<size_t>(orig[k]) + c] = tmp[3 * static_cast<size_t>(k) + c];
+      }
+    }
     if (potential_energy) *potential_energy = red[0];
     if (virial)
       for (int q = 0; q < 9; ++q) virial[q] = red[1 + q];

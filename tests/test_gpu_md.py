@@ -118,3 +118,26 @@ def test_gpu_forces_are_energy_gradients(engine_lib, small_model_path, precision
             q[a, c] -= h
             fd = -(m.compute_atoms(p, species)[0] - m.compute_atoms(q, species)[0]) / (2 * h)
             assert abs(fd - F[a, c]) < 5e-3 * max(1.0, abs(F[a, c])), (a, c, fd, F[a, c])
+
+
+def test_md_renumbering_keeps_caller_order(engine_lib, small_model_path):
+    """Periodic MD renumbers the atoms spatially at the first rebuild and every 200 steps;
+    the state is reported in the caller's order: after 205 steps (two renumberings) the
+    reported forces are those of an evaluation at the reported positions with the
+    caller's species."""
+    from symmetrix_gb300.md import MD
+    pos, L, sp = random_box(400, 0.064, 0.9, 2, seed=15)
+    sp = (sp + 1).astype(np.int32)  # C and O
+    m = _engine(small_model_path)
+    masses = species_masses(m.atomic_numbers, sp)
+    v = maxwell_boltzmann(masses, 300.0, np.random.default_rng(16))
+    md = MD(m, pos, sp, masses, box=L, velocities=v, dt=0.1, skin=1.0, rebuild_every=10)
+    md.run(205)
+    st = md.state()
+    assert st["step"] == 205
+    _, _, F, _ = m.compute_atoms(st["positions"], sp, box=L)
+    np.testing.assert_allclose(st["forces"], F, atol=1e-5)
+    # momentum is conserved in the caller's order too (masses of the caller's species)
+    p = (masses[:, None] * st["velocities"]).sum(0)
+    p0 = (masses[:, None] * v).sum(0)
+    np.testing.assert_allclose(p, p0, atol=1e-6 * np.abs(masses[:, None] * v).sum())

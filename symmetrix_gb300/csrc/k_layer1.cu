@@ -330,7 +330,7 @@ __device__ __forceinline__ void pair_barrier(int pair) {
 template <int LMAX, int H>
 __device__ __forceinline__ void l1_rev_chunk(const DevModel& m, const float* __restrict__ H1,
                                              fix64* __restrict__ H1_adj, const L1Stage<true>& st, const Lane2& L,
-                                             const float2* g, float (*sF)[8][3], float2* xchg, int pair) {
+                                             const float2* g, float* sFT, float2* xchg, int pair) {
   constexpr int NL2 = (LMAX + 1) * (LMAX + 1);
   constexpr int NQ = half_count(H);
   const int na = st.nact;
@@ -354,7 +354,10 @@ __device__ __forceinline__ void l1_rev_chunk(const DevModel& m, const float* __r
     float fx, fy, fz;
     l1_rev_edge<LMAX, H>(g, R, Rd, st.Y2[t], st.G[t], st.u[t], hv, hadj, fx, fy, fz);
     if (!L.live) fx = fy = fz = 0.0f;
-    block_reduce3(fx, fy, fz, sF, t);
+    // this thread's share of the edge force, summed over the block after the chunk
+    sFT[(3 * t) * blockDim.x + threadIdx.x] = fx;
+    sFT[(3 * t + 1) * blockDim.x + threadIdx.x] = fy;
+    sFT[(3 * t + 2) * blockDim.x + threadIdx.x] = fz;
     constexpr int NR = NL2 / 2;
     float2* xb = xchg + (a & 1) * NL2 * L.C2;
     if (L.live) {
@@ -510,6 +513,10 @@ __device__ __forceinline__ void layer1_rev_atom(const DevModel& m, const EdgeIn&
   }
   __syncthreads();
   float2 g[NG];
+  // during the edge loop the staged dPhi1 rows (and sP) are dead: the dynamic shared memory
+  // holds every thread's share of the chunk's edge forces, [kEdgeChunk][3][blockDim] floats
+  // (the chunk loop's first barrier follows every read of sD and sP)
+  float* sFT = dyn;
   if (m.cg_rev_pad) {
     if (half == 0)
       l1_load_g_sd<LMAX, 0>(m, sD, L, g);
@@ -526,9 +533,26 @@ __device__ __forceinline__ void layer1_rev_atom(const DevModel& m, const EdgeIn&
     stage_l1<true>(m, in, ti, eb, ne, st);
     __syncthreads();
     if (half == 0)
-      l1_rev_chunk<LMAX, 0>(m, H1, H1_adj, st, L, g, sF, xchg, pair);
+      l1_rev_chunk<LMAX, 0>(m, H1, H1_adj, st, L, g, sFT, xchg, pair);
     else
-      l1_rev_chunk<LMAX, 1>(m, H1, H1_adj, st, L, g, sF, xchg, pair);
+      l1_rev_chunk<LMAX, 1>(m, H1, H1_adj, st, L, g, sFT, xchg, pair);
+    __syncthreads();
+    {  // each warp sums its 32 lanes' shares of every (edge, component): four partial sums of
+       // eight in a fixed order, the reads rotated by lane so the warp hits 32 banks
+      const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+      for (int q = lane; q < 3 * ne; q += 32) {
+        const float* row = sFT + q * blockDim.x + w * 32;
+        float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
+#pragma unroll
+        for (int i = 0; i < 32; i += 4) {
+          a0 += row[(i + lane) & 31];
+          a1 += row[(i + 1 + lane) & 31];
+          a2 += row[(i + 2 + lane) & 31];
+          a3 += row[(i + 3 + lane) & 31];
+        }
+        sF[q / 3][w][q % 3] = (a0 + a1) + (a2 + a3);
+      }
+    }
     __syncthreads();
     for (int t = threadIdx.x; t < ne; t += blockDim.x) {
       double s[3] = {0.0, 0.0, 0.0};
@@ -944,7 +968,9 @@ size_t rev_l2_smem(const DevModel& m) {
 }
 
 // dynamic shared memory of the L_max = 1 adjoint: the staged dPhi1 rows and the g table
-size_t rev_l1_smem(const DevModel& m) { return sizeof(float) * (m.n_lme + ins_np(1)) * m.C; }
+size_t rev_l1_smem(const DevModel& m) {
+  return sizeof(float) * std::max<size_t>((m.n_lme + ins_np(1)) * m.C, kEdgeChunk * 3 * layer1_block(m.C));
+}
 
 template <int CT, bool P>
 cudaError_t set_smem(const DevModel& m) {

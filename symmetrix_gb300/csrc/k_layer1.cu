@@ -774,12 +774,14 @@ __host__ __device__ constexpr bool l2_uses_l2(int l2) {
 // Adjoint, group G, edges [a0, a1) of a staged chunk (as l1_rev_edge, scalar, this
 // group's paths).  The H1_adj terms of the four groups meet in hold ([kSub2][4 groups]
 // [NL2][CH] floats, zero for the rows a group does not touch), and after a block barrier
-// l2_rev_flush adds each row once per channel (as in the L_max = 1 adjoint).
-constexpr int kSub2 = 8;
+// l2_rev_flush adds each row once per channel (as in the L_max = 1 adjoint); each thread's
+// share of the edge force goes to the [kSub2][3][blockDim] floats after hold, summed by
+// l2_rev_flush too.
+constexpr int kSub2 = 7;
 template <int G>
 __device__ __forceinline__ void l2_rev_chunk(const DevModel& m, const float* __restrict__ H1, const L1Stage<true>& st,
-                                             int C, int k, bool live, const float* g, float (*sF)[16][3],
-                                             float* hold, int CH, int kk, int a0, int a1) {
+                                             int C, int k, bool live, const float* g, float* hold, int CH, int kk,
+                                             int a0, int a1) {
   constexpr int NL2 = 9, NI = 17;
   for (int a = a0; a < a1; ++a) {
     const int t = st.act[a];
@@ -828,7 +830,10 @@ __device__ __forceinline__ void l2_rev_chunk(const DevModel& m, const float* __r
       }
     });
     if (!live) fx = fy = fz = 0.0f;
-    block_reduce3_w16(fx, fy, fz, sF, t);
+    float* fs = hold + kSub2 * kL2Groups * NL2 * CH + (3 * (a - a0)) * blockDim.x + threadIdx.x;
+    fs[0] = fx;
+    fs[blockDim.x] = fy;
+    fs[2 * blockDim.x] = fz;
     if (live) {
       float* hb = hold + ((a - a0) * kL2Groups + G) * NL2 * CH + kk;
 #pragma unroll
@@ -852,6 +857,26 @@ __device__ __forceinline__ void l2_rev_flush(fix64* __restrict__ H1_adj, const L
       for (int q = 1; q < kL2Groups; ++q) v += hb[(q * NL2 + b) * CH];
       add_fixed(dst + b * C, v);
     }
+  }
+}
+
+// After the same barrier: each warp sums its 32 lanes' shares of the force of edges
+// [a0, a1) (fs: [kSub2][3][blockDim] floats; four partial sums in a fixed order, the reads
+// rotated by lane so that the warp hits 32 banks) into sF[staged slot][warp].
+__device__ __forceinline__ void l2_rev_force_sums(const L1Stage<true>& st, const float* fs, float (*sF)[16][3], int a0,
+                                                  int a1) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int q = lane; q < 3 * (a1 - a0); q += 32) {
+    const float* row = fs + q * blockDim.x + w * 32;
+    float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 32; i += 4) {
+      s0 += row[(i + lane) & 31];
+      s1 += row[(i + 1 + lane) & 31];
+      s2 += row[(i + 2 + lane) & 31];
+      s3 += row[(i + 3 + lane) & 31];
+    }
+    sF[st.act[a0 + q / 3]][w][q % 3] = (s0 + s1) + (s2 + s3);
   }
 }
 
@@ -913,18 +938,20 @@ __device__ __forceinline__ void layer1_rev_l2_atom(const DevModel& m, const Edge
     __syncthreads();
     stage_l1<true>(m, in, ti, eb, ne, st);
     __syncthreads();
-    // the staged dPhi1 rows and sP are dead now: the H1_adj terms of kSub2 edges at a time
+    // the staged dPhi1 rows and sP are dead now: the H1_adj terms and the force shares of
+    // kSub2 edges at a time
     float* hold = dyn;
     for (int a0 = 0; a0 < st.nact; a0 += kSub2) {
       const int a1 = min(st.nact, a0 + kSub2);
       switch (grp) {
-        case 0: l2_rev_chunk<0>(m, H1, st, C, k, live, g, sF, hold, CH, kk, a0, a1); break;
-        case 1: l2_rev_chunk<1>(m, H1, st, C, k, live, g, sF, hold, CH, kk, a0, a1); break;
-        case 2: l2_rev_chunk<2>(m, H1, st, C, k, live, g, sF, hold, CH, kk, a0, a1); break;
-        default: l2_rev_chunk<3>(m, H1, st, C, k, live, g, sF, hold, CH, kk, a0, a1); break;
+        case 0: l2_rev_chunk<0>(m, H1, st, C, k, live, g, hold, CH, kk, a0, a1); break;
+        case 1: l2_rev_chunk<1>(m, H1, st, C, k, live, g, hold, CH, kk, a0, a1); break;
+        case 2: l2_rev_chunk<2>(m, H1, st, C, k, live, g, hold, CH, kk, a0, a1); break;
+        default: l2_rev_chunk<3>(m, H1, st, C, k, live, g, hold, CH, kk, a0, a1); break;
       }
       __syncthreads();
       l2_rev_flush(H1_adj, st, C, k, live, hold, CH, kk, grp, a0, a1);
+      l2_rev_force_sums(st, hold + kSub2 * kL2Groups * 9 * CH, sF, a0, a1);
       __syncthreads();
     }
     for (int t = threadIdx.x; t < ne; t += blockDim.x) {
@@ -963,8 +990,8 @@ namespace {
 
 // dynamic shared memory of the L_max = 2 adjoint: the staged dPhi1 rows and the g table,
 // and later the H1_adj terms of kSub2 edges (see l2_rev_chunk)
-size_t rev_l2_smem(const DevModel& m) {
-  return sizeof(float) * std::max<size_t>(m.n_lme + ins_np(2), kSub2 * kL2Groups * 9) * l2_slice_width(m);
+size_t rev_l2_smem(const DevModel& m) {  // (the block is kL2Groups * CH threads)
+  return sizeof(float) * std::max<size_t>(m.n_lme + ins_np(2), kSub2 * kL2Groups * (9 + 3)) * l2_slice_width(m);
 }
 
 // dynamic shared memory of the L_max = 1 adjoint: the staged dPhi1 rows and the g table
@@ -988,7 +1015,7 @@ cudaError_t set_smem_l2(const DevModel& m) {
   if (e != cudaSuccess) return e;
   // (sized for one slice of all C channels: the largest rev_l2_smem of any slice count)
   return cudaFuncSetAttribute(k_layer1_rev_l2<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              static_cast<int>(sizeof(float) * std::max(m.n_lme + ins_np(2), kSub2 * kL2Groups * 9) *
+                              static_cast<int>(sizeof(float) * std::max(m.n_lme + ins_np(2), kSub2 * kL2Groups * (9 + 3)) *
                                                m.C));
 }
 

@@ -384,7 +384,7 @@ def time_md(eng, pos, species, masses, L, vel, args, dist, estream):
 
 # (workload, stage) -> (DRAM bytes per launch, the ncu summary it comes from)
 NCU_TRAFFIC = {
-    ("fp32_4096", "layer1_rev"): (165.7e6 + 11.4e6, "profiles/layer1_rev_fp32_4096.md (ncu --set full, 1 launch)"),
+    ("fp32_4096", "layer1_rev"): (165.6e6 + 11.5e6, "profiles/layer1_rev_fp32_4096.md (ncu --set full, 1 launch)"),
 }
 
 ATOM_KERNELS = ("layer0_fwd", "contract0_rev", "layer0_rev", "layer1_fwd", "layer1_rev", "node_tail")

@@ -146,14 +146,30 @@ __global__ void __launch_bounds__(128, 1) k_umma_gemm(const __grid_constant__ Um
              (o.select ? 0 : n0);
       if (o.select) write = ((r % o.rpn) == 0) == (blockIdx.y == 0);
     }
+    // Each 32-column chunk goes through a 4 KB staging tile per warp (the ring's shared
+    // memory is free once every MMA has completed): a lane holds one row after tcgen05.ld,
+    // while a coalesced store wants eight lanes on 128 contiguous bytes of one row.  The
+    // float4 groups of row t sit at slot q ^ (t & 7), so both the row-wise writes and the
+    // transposed reads hit all 32 banks.
+    float* stg = reinterpret_cast<float*>(smem) + warp * 32 * 32;
+    const int sub = lane >> 3, c4 = lane & 7;
     for (int c0 = 0; c0 < NT; c0 += 32) {
       float v[32];
       sm100::tmem_ld32(tmem + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(c0), v);
-      if (write) {
-        float4* dst = reinterpret_cast<float4*>(o.Y + base + c0);
 #pragma unroll
-        for (int q = 0; q < 8; ++q) dst[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+      for (int q = 0; q < 8; ++q)
+        reinterpret_cast<float4*>(stg + lane * 32)[q ^ (lane & 7)] =
+            make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+      __syncwarp();
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int t = 4 * j + sub;  // the warp's row this lane stores now
+        const long b = __shfl_sync(0xffffffffu, base, t);
+        const int w = __shfl_sync(0xffffffffu, write ? 1 : 0, t);
+        const float4 val = reinterpret_cast<const float4*>(stg + t * 32)[c4 ^ (t & 7)];
+        if (w) reinterpret_cast<float4*>(o.Y + b + c0)[c4] = val;
       }
+      __syncwarp();  // the next chunk overwrites the staging tile
     }
   } else if (threadIdx.x == 0) {
     record_timeout(status);

@@ -182,7 +182,8 @@ int smx_run_stage(smx_engine* eng, const char* stage, int num_nodes, const int* 
  * after a device-pointer call, returns SMX_ERR_TIMEOUT and the results are invalid).
  * No counterpart in the reference (its MACE object has no options). */
 int smx_set_option(smx_engine* eng, const char* key, long value);
-/* Read an option or a tuned schedule entry ("tc_nt_<G>", "tc_stages_<G>",
+/* Read an option or a tuned schedule entry ("tc_nt_<G>": the N-tile width, 0 when each
+ * GEMM of the group is one N-tile of its whole width; "tc_stages_<G>",
  * "tc_tuned_ns_<G>" for G in H1, A1, Phi1_adj, M0_adj; "persistent": bit k set when
  * per-atom kernel k (layer0_fwd, contract0_rev, layer0_rev, layer1_fwd, layer1_rev,
  * node_tail) runs as a persistent grid; "species_order": 1 when the sorted order is in

@@ -192,7 +192,8 @@ long smx_get_option(const smx_engine* eng, const char* key) {
   if (k == "l2_split") return eng->dm.l2_split;       // channel slices of the L_max = 2 layer-1 kernels
   static const char* groups[4] = {"H1", "A1", "Phi1_adj", "M0_adj"};
   for (int q = 0; q < 4; ++q) {
-    if (k == std::string("tc_nt_") + groups[q]) return eng->tc_cfg[q].NT ? eng->tc_cfg[q].NT : eng->dm.C;
+    if (k == std::string("tc_nt_") + groups[q])
+      return eng->tc_cfg[q].NT > 0 ? eng->tc_cfg[q].NT : (eng->tc_cfg[q].NT < 0 ? 0 : eng->dm.C);
     if (k == std::string("tc_stages_") + groups[q]) return eng->tc_cfg[q].stages;
     if (k == std::string("tc_tuned_ns_") + groups[q]) return static_cast<long>(eng->tc_tuned_us[q] * 1000.0f);
   }

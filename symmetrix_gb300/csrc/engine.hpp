@@ -393,7 +393,7 @@ struct smx_engine {
   // TMA ring depth are picked by timing the candidates on the first evaluation's own
   // operands (CUDA events, one warm-up and three timed launches each), then kept.
   struct TcCfg {
-    int NT = 0;  // 0: C
+    int NT = 0;  // 0: C; -1: each GEMM's whole B width (one N-tile: X is read once)
     int stages = 4;
   };
   TcCfg tc_cfg[4];
@@ -406,7 +406,7 @@ struct smx_engine {
 
   void tc_apply(const TcCfg& c, smx::UmmaGemm* g, int ng, bool tile_n) const {
     for (int q = 0; q < ng; ++q) {
-      if (tile_n) g[q].NT = c.NT ? c.NT : dm.C;
+      if (tile_n) g[q].NT = c.NT > 0 ? c.NT : (c.NT < 0 ? g[q].nb_rows : dm.C);
       g[q].stages = c.stages;
     }
   }
@@ -420,6 +420,15 @@ struct smx_engine {
       for (int q = 0; q < ng && ok; ++q) ok = g[q].nb_rows % nt == 0 && smx::umma_supported(g[q].K, nt);
       if (!ok) continue;
       for (int st : {2, 3, 4}) cand.push_back(TcCfg{nt == C ? 0 : nt, st});
+    }
+    if (tile_n) {  // one N-tile per GEMM where some B is wider than C and all fit a tile
+      bool ok = true, wider = false;
+      for (int q = 0; q < ng && ok; ++q) {
+        ok = g[q].nb_rows <= 256 && smx::umma_supported(g[q].K, g[q].nb_rows);
+        wider = wider || g[q].nb_rows != C;
+      }
+      if (ok && wider)
+        for (int st : {2, 3, 4}) cand.push_back(TcCfg{-1, st});
     }
     cudaEvent_t a, b;
     check(cudaEventCreate(&a), "cudaEventCreate");

@@ -41,7 +41,9 @@ __device__ __forceinline__ void record_timeout(unsigned* status) {
 constexpr int kStages = 4;     // maximum shared-memory ring depth (k-blocks in flight)
 
 // Up to four independent GEMMs in one launch (blockIdx.z selects the segment; the
-// blocks beyond a segment's tile counts return at once).
+// blocks beyond a segment's tile counts return at once).  blockIdx.x runs over the
+// segment's tiles N-tile fastest, so the CTAs that read the same 128-row X tile run
+// back to back and all but the first find it in L2.
 struct UmmaSegDev {
   CUtensorMap ta, tb;
   UmmaOut o;
@@ -57,7 +59,9 @@ struct UmmaGroupDev {
 
 __global__ void __launch_bounds__(128, 1) k_umma_gemm(const __grid_constant__ UmmaGroupDev grp, unsigned* status) {
   const UmmaSegDev& seg = grp.s[blockIdx.z];
-  if (static_cast<int>(blockIdx.x) >= seg.tiles_m || static_cast<int>(blockIdx.y) >= seg.tiles_n) return;
+  const int tile_n = static_cast<int>(blockIdx.x % static_cast<unsigned>(seg.tiles_n));
+  const int tile_m = static_cast<int>(blockIdx.x / static_cast<unsigned>(seg.tiles_n));
+  if (tile_m >= seg.tiles_m) return;
   const CUtensorMap& ta = seg.ta;
   const CUtensorMap& tb = seg.tb;
   const UmmaOut& o = seg.o;
@@ -71,7 +75,7 @@ __global__ void __launch_bounds__(128, 1) k_umma_gemm(const __grid_constant__ Um
   const uint32_t a_bytes = kTileM * kBoxK * 2, b_bytes = static_cast<uint32_t>(NT) * kBoxK * 2;
   const uint32_t stage_bytes = a_bytes + b_bytes;  // stage = A box then B box (both 1024-B multiples)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.x * kTileM, n0 = blockIdx.y * NT;
+  const int m0 = tile_m * kTileM, n0 = tile_n * NT;
   const uint32_t ncols = NT <= 32 ? 32u : (NT <= 64 ? 64u : (NT <= 128 ? 128u : 256u));
 
   if (threadIdx.x == 0) {
@@ -144,7 +148,7 @@ __global__ void __launch_bounds__(128, 1) k_umma_gemm(const __grid_constant__ Um
     if (row_ok) {
       base = static_cast<long>(r / o.rpn) * o.y_ns + o.y_off + static_cast<long>(r % o.rpn) * o.y_rs +
              (o.select ? 0 : n0);
-      if (o.select) write = ((r % o.rpn) == 0) == (blockIdx.y == 0);
+      if (o.select) write = ((r % o.rpn) == 0) == (tile_n == 0);
     }
     // Each 32-column chunk goes through a 4 KB staging tile per warp (the ring's shared
     // memory is free once every MMA has completed): a lane holds one row after tcgen05.ld,
@@ -280,7 +284,7 @@ void launch_umma_gemms(const UmmaGemm* g, int n, unsigned* status, cudaStream_t 
   std::memset(&grp, 0, sizeof(grp));
   grp.skip_loads = test_timeout ? 1 : 0;
   grp.wait_ns = test_timeout ? 2000000ull : sm100::kWaitLimitNs;  // 2 ms when testing
-  unsigned gx = 0, gy = 0;
+  long gx = 0;
   size_t smem = 0;
   int used = 0;
   for (int q = 0; q < n; ++q) {
@@ -297,12 +301,12 @@ void launch_umma_gemms(const UmmaGemm* g, int n, unsigned* status, cudaStream_t 
     d.tiles_m = static_cast<int>((a.rows + kTileM - 1) / kTileM);
     d.tiles_n = a.nb_rows / a.NT;
     d.stages = a.stages >= 1 && a.stages <= kStages ? a.stages : kStages;
-    gx = std::max(gx, static_cast<unsigned>(d.tiles_m));
-    gy = std::max(gy, static_cast<unsigned>(d.tiles_n));
+    gx = std::max(gx, static_cast<long>(d.tiles_m) * d.tiles_n);
     smem = std::max(smem, umma_smem_bytes(a.K, a.NT, d.stages));
   }
   if (used == 0) return;
-  k_umma_gemm<<<dim3(gx, gy, used), 128, smem, s>>>(grp, status);
+  if (gx > 0x7fffffffL) throw std::invalid_argument("tensor-core GEMM too large for one launch");
+  k_umma_gemm<<<dim3(static_cast<unsigned>(gx), 1, used), 128, smem, s>>>(grp, status);
 }
 
 void launch_rows_to_bf16(const float* src, __nv_bfloat16* dst, long rows, int width, int rpn, long s_ns, int s_off,

@@ -175,7 +175,10 @@ int smx_run_stage(smx_engine* eng, const char* stage, int num_nodes, const int* 
  * 0: input order; 1: always sorted; results do not depend on it);
  * "cg_padded" (1, the default: the layer-1 Clebsch-Gordan contractions read tables padded
  * to a fixed number of terms per row, with independent loads; 0: the compressed rows);
- * BF16 form: "tc_terms" (1, 2 or 3 bf16 split terms of the GEMM operands, default 3;
+ * "pdl" (1, the default: the chained kernels of an evaluation and of an MD step are
+ * launched with programmatic dependent launch, each waiting for its predecessor at its
+ * first instruction; 0: plain launches; process-wide, read by later launches and graph
+ * captures); BF16 form: "tc_terms" (1, 2 or 3 bf16 split terms of the GEMM operands, default 3;
  * set before the first evaluation); "test_gemm_timeout" (n in [0, 16]: a test of the
  * timeout path, the next n tensor-core GEMM launches issue no load so that their bounded
  * wait gives up after 2 ms with nothing in flight; the call that ran them, or smx_sync

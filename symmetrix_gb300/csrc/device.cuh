@@ -165,6 +165,38 @@ __device__ __forceinline__ float from_fixed(fix64 q) {
   return static_cast<float>(static_cast<double>(static_cast<long long>(q)) * kFixInv);
 }
 
+// Programmatic dependent launch.  The chained kernels of an evaluation and of an MD step
+// are launched with the programmatic-serialization attribute (launch_pdl); each starts
+// with pdl_begin, whose griddepcontrol.wait holds its blocks until the previous grid has
+// completed and its writes are visible (a no-op after a normal launch), and reads or
+// writes nothing before it.  No kernel signals griddepcontrol.launch_dependents early, so
+// a dependent grid is launched as its predecessor's blocks exit: on the 4096-atom MD step
+// this saves ~4 us (1.911 -> 1.907 ms), while a signal at every block's start, which
+// lets the next grid's blocks sit waiting on the SMs through the last wave, cost 0.03 ms.
+__device__ __forceinline__ void pdl_begin() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+// process-wide switch (option "pdl"); off: plain launches
+inline bool& pdl_enabled() {
+  static bool on = true;
+  return on;
+}
+// launch errors surface through cudaGetLastError, as for <<<...>>>
+template <typename... KArgs, typename... Args>
+inline void launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl_enabled() ? 1 : 0;
+  (void)cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...);
+}
+
 // Host side: the kernel's model copy and grid for n atoms under the current schedule.
 inline int atom_grid(const DevModel& m, int k, int n, DevModel& mk) {
   mk = m;

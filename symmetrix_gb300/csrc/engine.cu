@@ -153,6 +153,11 @@ int smx_set_option(smx_engine* eng, const char* key, long value) {
     eng->sched_set(value == 1 ? 1 : 0);
     return SMX_OK;
   }
+  if (std::strcmp(key, "pdl") == 0) {  // programmatic dependent launch of the chained kernels, process-wide
+    if (value < 0 || value > 1) return fail(SMX_ERR_INVALID, "pdl must be 0 or 1");
+    smx::pdl_enabled() = value != 0;
+    return SMX_OK;
+  }
   if (std::strcmp(key, "test_gemm_timeout") == 0) {  // test of the error path (see engine.hpp)
     if (value < 0 || value > 16) return fail(SMX_ERR_INVALID, "test_gemm_timeout must be in [0, 16]");
     if (eng->precision != SMX_PRECISION_BF16) return fail(SMX_ERR_INVALID, "test_gemm_timeout applies to the bf16 form");
@@ -184,6 +189,7 @@ long smx_get_option(const smx_engine* eng, const char* key) {
   if (k == "profile") return eng->profile;
   if (k == "precision") return eng->precision;
   if (k == "tc_terms") return eng->tc_terms;
+  if (k == "pdl") return smx::pdl_enabled() ? 1 : 0;
   if (k == "autotune") return eng->autotune;
   if (k == "persistent") return eng->sched_mask();  // bit k: per-atom kernel k runs persistent
   if (k == "species_order") return eng->order_species() ? 1 : 0;  // in effect

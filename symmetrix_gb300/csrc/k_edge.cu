@@ -226,6 +226,7 @@ __device__ __forceinline__ void layer0_fwd_atom(const DevModel& m, const EdgeIn&
 template <bool P, int NLM>
 __global__ void __launch_bounds__(256) k_layer0_fwd(DevModel m, EdgeIn in, float* __restrict__ A0,
                                                     float* __restrict__ M0, float* __restrict__ zbl_e) {
+  pdl_begin();
   AtomCursor cur{P ? m.sched : nullptr, in.N, 0};
   for (int b = cur.first(); b < in.N; b = cur.next())
     layer0_fwd_atom<NLM>(m, in, A0, M0, zbl_e, in.atom_at(b));
@@ -312,6 +313,7 @@ template <bool P, int NLM>
 __global__ void __launch_bounds__(256) k_contract0_rev(DevModel m, const int* __restrict__ node_type,
                                                        const float* __restrict__ A0, const float* __restrict__ M0_adj,
                                                        float* __restrict__ A0_adj, int N) {
+  pdl_begin();
   AtomCursor cur{P ? m.sched : nullptr, N, 0};
   for (int i = cur.first(); i < N; i = cur.next()) contract0_rev_atom<NLM>(m, node_type, A0, M0_adj, A0_adj, i);
   cur.done();
@@ -416,6 +418,7 @@ __device__ __forceinline__ void layer0_rev_atom(const DevModel& m, const EdgeIn&
 template <bool P>
 __global__ void __launch_bounds__(128) k_layer0_rev(DevModel m, EdgeIn in, const float* __restrict__ A0_adj,
                                                     const double* __restrict__ f1, double* __restrict__ forces) {
+  pdl_begin();
   AtomCursor cur{P ? m.sched : nullptr, in.N, 0};
   for (int b = cur.first(); b < in.N; b = cur.next())
     layer0_rev_atom(m, in, A0_adj, f1, forces, in.atom_at(b));
@@ -450,9 +453,9 @@ void launch_layer0_fwd(const DevModel& m, const EdgeIn& in, float* A0, float* M0
   dispatch_nlm(m, [&](auto nc) {
     constexpr int NLM = decltype(nc)::value;
     if (mk.sched)
-      k_layer0_fwd<true, NLM><<<grid, 2 * layer0_block(m.C), smem, s>>>(mk, in, A0, M0, zbl_e);
+      launch_pdl(k_layer0_fwd<true, NLM>, grid, 2 * layer0_block(m.C), smem, s, mk, in, A0, M0, zbl_e);
     else
-      k_layer0_fwd<false, NLM><<<grid, 2 * layer0_block(m.C), smem, s>>>(mk, in, A0, M0, zbl_e);
+      launch_pdl(k_layer0_fwd<false, NLM>, grid, 2 * layer0_block(m.C), smem, s, mk, in, A0, M0, zbl_e);
   });
 }
 
@@ -465,15 +468,15 @@ void launch_layer0_rev(const DevModel& m, const EdgeIn& in, const float* A0, con
   dispatch_nlm(m, [&](auto nc) {
     constexpr int NLM = decltype(nc)::value;
     if (mk.sched)
-      k_contract0_rev<true, NLM><<<grid, m.C, smem, s>>>(mk, in.node_type, A0, M0_adj, A0_adj, in.N);
+      launch_pdl(k_contract0_rev<true, NLM>, grid, m.C, smem, s, mk, in.node_type, A0, M0_adj, A0_adj, in.N);
     else
-      k_contract0_rev<false, NLM><<<grid, m.C, smem, s>>>(mk, in.node_type, A0, M0_adj, A0_adj, in.N);
+      launch_pdl(k_contract0_rev<false, NLM>, grid, m.C, smem, s, mk, in.node_type, A0, M0_adj, A0_adj, in.N);
   });
   grid = atom_grid(m, kAkLayer0Rev, in.N, mk);
   if (mk.sched)
-    k_layer0_rev<true><<<grid, layer0_block(m.C), 0, s>>>(mk, in, A0_adj, f1, forces);
+    launch_pdl(k_layer0_rev<true>, grid, layer0_block(m.C), 0, s, mk, in, A0_adj, f1, forces);
   else
-    k_layer0_rev<false><<<grid, layer0_block(m.C), 0, s>>>(mk, in, A0_adj, f1, forces);
+    launch_pdl(k_layer0_rev<false>, grid, layer0_block(m.C), 0, s, mk, in, A0_adj, f1, forces);
 }
 
 // resident blocks per SM of the persistent layer-0 kernels at this model's launch shapes

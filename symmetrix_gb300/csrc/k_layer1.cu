@@ -465,6 +465,7 @@ __device__ __forceinline__ void layer1_fwd_atom(const DevModel& m, const EdgeIn&
 template <int LMAX, int CT, bool P>
 __global__ void __launch_bounds__(256) k_layer1_fwd(DevModel m, EdgeIn in, const float* __restrict__ H1,
                                                     float* __restrict__ Phi1) {
+  pdl_begin();
   AtomCursor cur{P ? m.sched : nullptr, in.N, 0};
   for (int b = cur.first(); b < in.N; b = cur.next())
     layer1_fwd_atom<LMAX, CT>(m, in, H1, Phi1, in.atom_at(b));
@@ -576,6 +577,7 @@ template <int LMAX, int CT, bool P>
 __global__ void __launch_bounds__(256) k_layer1_rev(DevModel m, EdgeIn in, const float* __restrict__ H1,
                                                     const float* __restrict__ dPhi1, fix64* __restrict__ H1_adj,
                                                     double* __restrict__ f1) {
+  pdl_begin();
   AtomCursor cur{P ? m.sched : nullptr, in.N, 0};
   for (int b = cur.first(); b < in.N; b = cur.next())
     layer1_rev_atom<LMAX, CT>(m, in, H1, dPhi1, H1_adj, f1, in.atom_at(b));
@@ -756,6 +758,7 @@ __device__ __forceinline__ void layer1_fwd_l2_atom(const DevModel& m, const Edge
 template <bool P>
 __global__ void __launch_bounds__(512, 1) k_layer1_fwd_l2(DevModel m, EdgeIn in, const float* __restrict__ H1,
                                                           float* __restrict__ Phi1) {
+  pdl_begin();
   const int ns = m.l2_split, n = in.N * ns;
   AtomCursor cur{P ? m.sched : nullptr, n, 0};
   for (int b = cur.first(); b < n; b = cur.next()) layer1_fwd_l2_atom(m, in, H1, Phi1, in.atom_at(b / ns), b % ns);
@@ -976,6 +979,7 @@ template <bool P>
 __global__ void __launch_bounds__(512, 1) k_layer1_rev_l2(DevModel m, EdgeIn in, const float* __restrict__ H1,
                                                           const float* __restrict__ dPhi1,
                                                           fix64* __restrict__ H1_adj, double* __restrict__ f1) {
+  pdl_begin();
   const int ns = m.l2_split, n = in.N * ns;
   AtomCursor cur{P ? m.sched : nullptr, n, 0};
   for (int b = cur.first(); b < n; b = cur.next())
@@ -1063,13 +1067,13 @@ void launch_layer1_fwd(const DevModel& m, const EdgeIn& in, const float* H1, flo
   dispatch_p(mk.sched != nullptr, [&](auto pc) {
     constexpr bool P = decltype(pc)::value;
     if (m.L_max == 2) {
-      k_layer1_fwd_l2<P><<<grid, kL2Groups * l2_slice_width(m), sizeof(float) * ins_np(2) * l2_slice_width(m), s>>>(
-          mk, in, H1, Phi1);
+      launch_pdl(k_layer1_fwd_l2<P>, grid, kL2Groups * l2_slice_width(m),
+                 sizeof(float) * ins_np(2) * l2_slice_width(m), s, mk, in, H1, Phi1);
       return;
     }
     const size_t smem = sizeof(float) * ins_np(1) * m.C;
     dispatch_c(m.C, [&](auto ct) {
-      k_layer1_fwd<1, decltype(ct)::value, P><<<grid, m.C, smem, s>>>(mk, in, H1, Phi1);
+      launch_pdl(k_layer1_fwd<1, decltype(ct)::value, P>, grid, m.C, smem, s, mk, in, H1, Phi1);
     });
   });
 }
@@ -1082,13 +1086,14 @@ void launch_layer1_rev(const DevModel& m, const EdgeIn& in, const float* H1, con
   dispatch_p(mk.sched != nullptr, [&](auto pc) {
     constexpr bool P = decltype(pc)::value;
     if (m.L_max == 2) {
-      k_layer1_rev_l2<P><<<grid, kL2Groups * l2_slice_width(m),
-                           rev_l2_smem(m), s>>>(mk, in, H1, dPhi1, H1_adj, f1);
+      launch_pdl(k_layer1_rev_l2<P>, grid, kL2Groups * l2_slice_width(m), rev_l2_smem(m), s, mk, in, H1, dPhi1,
+                 H1_adj, f1);
       return;
     }
     const size_t smem = rev_l1_smem(m);
     dispatch_c(m.C, [&](auto ct) {
-      k_layer1_rev<1, decltype(ct)::value, P><<<grid, layer1_block(m.C), smem, s>>>(mk, in, H1, dPhi1, H1_adj, f1);
+      launch_pdl(k_layer1_rev<1, decltype(ct)::value, P>, grid, layer1_block(m.C), smem, s, mk, in, H1, dPhi1, H1_adj,
+                 f1);
     });
   });
 }

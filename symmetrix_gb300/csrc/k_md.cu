@@ -212,6 +212,7 @@ __global__ void k_reverse_edges(int N, const int* __restrict__ first, const int*
 __global__ void k_edge_geometry(long cap, int N, const int* __restrict__ first, const double* __restrict__ pos,
                                 double3 box, const int* __restrict__ nidx, const int* __restrict__ edge_i,
                                 const char4* __restrict__ shift, double* __restrict__ xyz, double* __restrict__ r) {
+  pdl_begin();
   const long e = static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x;
   const long E = first[N] < cap ? first[N] : cap;
   if (e >= E) return;
@@ -237,6 +238,7 @@ __global__ void k_edge_geometry_packed(int N, const int* __restrict__ first, con
                                        double* __restrict__ r, double* __restrict__ f_skin, int* __restrict__ last,
                                        int* __restrict__ emap, int* __restrict__ nidx_p, int* __restrict__ ntype_p,
                                        double* __restrict__ xyz_p, double* __restrict__ r_p) {
+  pdl_begin();
   const int a = static_cast<int>((static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
   if (a >= N) return;
@@ -283,6 +285,7 @@ __global__ void k_edge_geometry_packed(int N, const int* __restrict__ first, con
 __global__ void k_scatter_packed_forces(int N, const int* __restrict__ first, const int* __restrict__ last,
                                         const int* __restrict__ emap, const double* __restrict__ f_p,
                                         double* __restrict__ f_skin) {
+  pdl_begin();
   const int a = static_cast<int>((static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
   if (a >= N) return;
@@ -295,6 +298,7 @@ __global__ void k_scatter_packed_forces(int N, const int* __restrict__ first, co
 // F_a = sum_{e in out(a)} (f[rev e] - f[e]); one thread per atom, no atomics
 __global__ void k_atom_forces(int N, const int* __restrict__ first, const int* __restrict__ rev,
                               const double* __restrict__ f, double* __restrict__ F) {
+  pdl_begin();
   // one warp per atom; fixed lane assignment and reduction tree: deterministic
   const int a = static_cast<int>((static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
@@ -347,6 +351,7 @@ constexpr double kAccel = 9.648533212331e-3;  // (eV/A)/amu in A/fs^2
 
 __global__ void k_vv_first(int N, double dt, const double* __restrict__ F, const double* __restrict__ inv_m,
                            double* __restrict__ v, double* __restrict__ x) {
+  pdl_begin();
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= N) return;
   const double h = 0.5 * dt * kAccel * inv_m[a];
@@ -358,6 +363,7 @@ __global__ void k_vv_first(int N, double dt, const double* __restrict__ F, const
 
 __global__ void k_vv_second(int N, double dt, const double* __restrict__ F, const double* __restrict__ inv_m,
                             double* __restrict__ v) {
+  pdl_begin();
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= N) return;
   const double h = 0.5 * dt * kAccel * inv_m[a];
@@ -441,7 +447,8 @@ void launch_reverse_edges(long cap, int N, const int* first, const int* nidx, co
 
 void launch_edge_geometry(long cap, int N, const int* first, const double* pos, double3 box, const int* nidx,
                           const int* edge_i, const char4* shift, double* xyz, double* r, cudaStream_t s) {
-  if (cap > 0) k_edge_geometry<<<ceil_div(cap, 256), 256, 0, s>>>(cap, N, first, pos, box, nidx, edge_i, shift, xyz, r);
+  if (cap > 0)
+    launch_pdl(k_edge_geometry, ceil_div(cap, 256), 256, 0, s, cap, N, first, pos, box, nidx, edge_i, shift, xyz, r);
 }
 
 void launch_edge_geometry_packed(int N, const int* first, const double* pos, double3 box, const int* nidx,
@@ -449,17 +456,17 @@ void launch_edge_geometry_packed(int N, const int* first, const double* pos, dou
                                  double* f_skin, int* last, int* emap, int* nidx_p, int* ntype_p, double* xyz_p,
                                  double* r_p, cudaStream_t s) {
   if (N > 0)
-    k_edge_geometry_packed<<<ceil_div(N, 4), 128, 0, s>>>(N, first, pos, box, nidx, ntype_e, shift, r_cut, xyz, r,
-                                                          f_skin, last, emap, nidx_p, ntype_p, xyz_p, r_p);
+    launch_pdl(k_edge_geometry_packed, ceil_div(N, 4), 128, 0, s, N, first, pos, box, nidx, ntype_e, shift, r_cut, xyz,
+               r, f_skin, last, emap, nidx_p, ntype_p, xyz_p, r_p);
 }
 
 void launch_scatter_packed_forces(int N, const int* first, const int* last, const int* emap, const double* f_p,
                                   double* f_skin, cudaStream_t s) {
-  if (N > 0) k_scatter_packed_forces<<<ceil_div(N, 4), 128, 0, s>>>(N, first, last, emap, f_p, f_skin);
+  if (N > 0) launch_pdl(k_scatter_packed_forces, ceil_div(N, 4), 128, 0, s, N, first, last, emap, f_p, f_skin);
 }
 
 void launch_atom_forces(int N, const int* first, const int* rev, const double* f, double* F, cudaStream_t s) {
-  if (N > 0) k_atom_forces<<<ceil_div(N, 4), 128, 0, s>>>(N, first, rev, f, F);  // one warp per atom
+  if (N > 0) launch_pdl(k_atom_forces, ceil_div(N, 4), 128, 0, s, N, first, rev, f, F);  // one warp per atom
 }
 
 void launch_reduce(int N, const int* first, const double* energies, const double* xyz, const double* f,
@@ -469,11 +476,11 @@ void launch_reduce(int N, const int* first, const double* energies, const double
 }
 
 void launch_vv_first(int N, double dt, const double* F, const double* inv_m, double* v, double* x, cudaStream_t s) {
-  if (N > 0) k_vv_first<<<ceil_div(N, 128), 128, 0, s>>>(N, dt, F, inv_m, v, x);
+  if (N > 0) launch_pdl(k_vv_first, ceil_div(N, 128), 128, 0, s, N, dt, F, inv_m, v, x);
 }
 
 void launch_vv_second(int N, double dt, const double* F, const double* inv_m, double* v, cudaStream_t s) {
-  if (N > 0) k_vv_second<<<ceil_div(N, 128), 128, 0, s>>>(N, dt, F, inv_m, v);
+  if (N > 0) launch_pdl(k_vv_second, ceil_div(N, 128), 128, 0, s, N, dt, F, inv_m, v);
 }
 
 }  // namespace smx

@@ -21,6 +21,7 @@ namespace smx {
 // tile each.  blockIdx.z selects the segment.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_gemm(GemmBatch gb) {
+  pdl_begin();
   const GemmSeg g = gb.s[blockIdx.z];
   const int row0 = blockIdx.x * 64, col0 = blockIdx.y * 64;
   if (row0 >= g.rows || col0 >= g.ncols) return;
@@ -86,7 +87,7 @@ void launch_gemm(const GemmBatch& b, cudaStream_t s) {
   }
   if (maxr == 0 || b.n == 0) return;
   dim3 grid(ceil_div(maxr, 64), ceil_div(maxc, 64), b.n);
-  k_gemm<<<grid, 256, 0, s>>>(b);
+  launch_pdl(k_gemm, grid, 256, 0, s, b);
 }
 
 // ---------------------------------------------------------------------------
@@ -256,6 +257,7 @@ __global__ void __launch_bounds__(256) k_node_tail(DevModel m, const int* __rest
                                                    fix64* __restrict__ H1_adj, float* __restrict__ M1_adj_o,
                                                    float* __restrict__ H2_adj_o, const float* __restrict__ zbl_e,
                                                    double* __restrict__ energies, int N) {
+  pdl_begin();
   AtomCursor cur{P ? m.sched : nullptr, N, 0};
   for (int i = cur.first(); i < N; i = cur.next())
     node_tail_atom(m, ntype, A1, H1, M1o, H2o, A1_adj, H1_adj, M1_adj_o, H2_adj_o, zbl_e, energies, N, i);
@@ -271,11 +273,11 @@ void launch_node_tail(const DevModel& m, const int* node_type, int N, float* A1,
   DevModel mk;
   const int grid = atom_grid(m, kAkNodeTail, N, mk);
   if (mk.sched)
-    k_node_tail<true><<<grid, m.C, node_tail_smem(m), s>>>(mk, node_type, A1, H1, M1, H2, A1_adj, H1_adj, M1_adj,
-                                                           H2_adj, zbl_e, energies, N);
+    launch_pdl(k_node_tail<true>, grid, m.C, node_tail_smem(m), s, mk, node_type, A1, H1, M1, H2, A1_adj, H1_adj,
+               M1_adj, H2_adj, zbl_e, energies, N);
   else
-    k_node_tail<false><<<grid, m.C, node_tail_smem(m), s>>>(mk, node_type, A1, H1, M1, H2, A1_adj, H1_adj, M1_adj,
-                                                            H2_adj, zbl_e, energies, N);
+    launch_pdl(k_node_tail<false>, grid, m.C, node_tail_smem(m), s, mk, node_type, A1, H1, M1, H2, A1_adj, H1_adj,
+               M1_adj, H2_adj, zbl_e, energies, N);
 }
 
 void node_tail_residency(const DevModel& m, int* per_sm) {
@@ -287,6 +289,7 @@ void node_tail_residency(const DevModel& m, int* per_sm) {
 // launch_rows_to_bf16 writes them).
 __global__ void k_fixed_rows(const fix64* __restrict__ src, float* __restrict__ dst, __nv_bfloat16* __restrict__ bf,
                              long rows, int C, int terms) {
+  pdl_begin();
   const long n = rows * C;
   for (long t = blockIdx.x * static_cast<long>(blockDim.x) + threadIdx.x; t < n;
        t += static_cast<long>(gridDim.x) * blockDim.x) {
@@ -303,7 +306,7 @@ void launch_fixed_rows(const fix64* src, float* dst, __nv_bfloat16* bf, long row
   if (rows <= 0) return;
   const long n = rows * C;
   const int blocks = static_cast<int>(std::min<long>((n + 255) / 256, 152L * 16));
-  k_fixed_rows<<<blocks, 256, 0, s>>>(src, dst, bf, rows, C, terms);
+  launch_pdl(k_fixed_rows, blocks, 256, 0, s, src, dst, bf, rows, C, terms);
 }
 
 // Single-stage calls (the reference binding's reverse_Phi1): the fixed-point H1_adj
@@ -342,6 +345,7 @@ void launch_forces_from_f1(double* forces, const double* f1, long stride, int ns
 // One block.
 __global__ void __launch_bounds__(1024) k_species_order(const int* __restrict__ ntype, int N, int S,
                                                         int* __restrict__ order) {
+  pdl_begin();
   extern __shared__ int cnt[];  // [S]: counts, then scatter cursors
   for (int t = threadIdx.x; t < S; t += blockDim.x) cnt[t] = 0;
   __syncthreads();
@@ -361,7 +365,7 @@ __global__ void __launch_bounds__(1024) k_species_order(const int* __restrict__ 
 
 void launch_species_order(const int* node_type, int N, int S, int* order, cudaStream_t s) {
   if (N <= 0) return;
-  k_species_order<<<1, 1024, sizeof(int) * S, s>>>(node_type, N, S, order);
+  launch_pdl(k_species_order, 1, 1024, sizeof(int) * S, s, node_type, N, S, order);
 }
 
 // The host API's input check, on the device: flags (a mapped host word) receive one bit

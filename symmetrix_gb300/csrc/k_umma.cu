@@ -58,6 +58,7 @@ struct UmmaGroupDev {
 };
 
 __global__ void __launch_bounds__(128, 1) k_umma_gemm(const __grid_constant__ UmmaGroupDev grp, unsigned* status) {
+  pdl_begin();
   const UmmaSegDev& seg = grp.s[blockIdx.z];
   const int tile_n = static_cast<int>(blockIdx.x % static_cast<unsigned>(seg.tiles_n));
   const int tile_m = static_cast<int>(blockIdx.x / static_cast<unsigned>(seg.tiles_n));
@@ -306,7 +307,7 @@ void launch_umma_gemms(const UmmaGemm* g, int n, unsigned* status, cudaStream_t 
   }
   if (used == 0) return;
   if (gx > 0x7fffffffL) throw std::invalid_argument("tensor-core GEMM too large for one launch");
-  k_umma_gemm<<<dim3(static_cast<unsigned>(gx), 1, used), 128, smem, s>>>(grp, status);
+  launch_pdl(k_umma_gemm, dim3(static_cast<unsigned>(gx), 1, used), 128, smem, s, grp, status);
 }
 
 void launch_rows_to_bf16(const float* src, __nv_bfloat16* dst, long rows, int width, int rpn, long s_ns, int s_off,

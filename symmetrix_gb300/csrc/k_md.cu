@@ -227,17 +227,20 @@ __global__ void k_edge_geometry(long cap, int N, const int* __restrict__ first, 
   r[e] = sqrt(dx * dx + dy * dy + dz * dz);
 }
 
-// Edge geometry of a skin list at the current positions, and its in-cut-off edges
-// packed to the front of each centre atom's segment: one warp per atom, ballot ranks
-// (list order kept, deterministic).  Atom a's packed edges are [first[a], last[a]) of
-// the packed arrays (emap: their skin-list index); the skin-list forces of edges at or
-// beyond r_cut are zeroed here, those inside are scattered back after the evaluation.
+// velocity Verlet units: positions A, velocities A/fs, forces eV/A, masses amu, dt fs
+constexpr double kAccel = 9.648533212331e-3;  // (eV/A)/amu in A/fs^2
+
+// The in-cut-off edges of a skin list at the current positions, packed to the front of
+// each centre atom's segment: one warp per atom, ballot ranks (list order kept,
+// deterministic).  Atom a's packed edges are [first[a], last[a]) of the packed arrays;
+// emap maps a packed edge to its skin-list index and pinv a skin-list edge to its packed
+// index (-1 at or beyond r_cut).  The skin list's own geometry and forces are not
+// written: only a state read-out needs them (launch_edge_geometry and the scatter below).
 __global__ void k_edge_geometry_packed(int N, const int* __restrict__ first, const double* __restrict__ pos,
                                        double3 box, const int* __restrict__ nidx, const int* __restrict__ ntype_e,
-                                       const char4* __restrict__ shift, double r_cut, double* __restrict__ xyz,
-                                       double* __restrict__ r, double* __restrict__ f_skin, int* __restrict__ last,
-                                       int* __restrict__ emap, int* __restrict__ nidx_p, int* __restrict__ ntype_p,
-                                       double* __restrict__ xyz_p, double* __restrict__ r_p) {
+                                       const char4* __restrict__ shift, double r_cut, int* __restrict__ pinv,
+                                       int* __restrict__ last, int* __restrict__ emap, int* __restrict__ nidx_p,
+                                       int* __restrict__ ntype_p, double* __restrict__ xyz_p, double* __restrict__ r_p) {
   pdl_begin();
   const int a = static_cast<int>((static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
@@ -257,28 +260,55 @@ __global__ void k_edge_geometry_packed(int N, const int* __restrict__ first, con
       dy = pos[3 * j + 1] + sh.y * box.y - py;
       dz = pos[3 * j + 2] + sh.z * box.z - pz;
       re = sqrt(dx * dx + dy * dy + dz * dz);
-      xyz[3 * static_cast<long>(e)] = dx;
-      xyz[3 * static_cast<long>(e) + 1] = dy;
-      xyz[3 * static_cast<long>(e) + 2] = dz;
-      r[e] = re;
       active = re < r_cut;
-      if (!active)
-        for (int c = 0; c < 3; ++c) f_skin[3 * static_cast<long>(e) + c] = 0.0;
     }
     const unsigned ball = __ballot_sync(0xffffffffu, active);
+    const int q = e0 + count + __popc(ball & ((1u << lane) - 1u));
+    if (e < e1) pinv[e] = active ? q : -1;
     if (active) {
-      const long q = e0 + count + __popc(ball & ((1u << lane) - 1u));
       emap[q] = e;
       nidx_p[q] = j;
       ntype_p[q] = ntype_e[e];
-      xyz_p[3 * q] = dx;
-      xyz_p[3 * q + 1] = dy;
-      xyz_p[3 * q + 2] = dz;
+      xyz_p[3 * static_cast<long>(q)] = dx;
+      xyz_p[3 * static_cast<long>(q) + 1] = dy;
+      xyz_p[3 * static_cast<long>(q) + 2] = dz;
       r_p[q] = re;
     }
     count += __popc(ball);
   }
   if (lane == 0) last[a] = e0 + count;
+}
+
+// F_a = sum over a's packed edges q of (f[q'] - f[q]), q' the packed reverse edge
+// (pinv[rev[emap[q]]]; the reverse of an edge inside the cut-off is inside it too, its
+// length being computed from the negated vector); one warp per atom, fixed lane
+// assignment and reduction tree (deterministic).  With dt > 0 also the second
+// velocity-Verlet half step of atom a, as k_vv_second.
+__global__ void k_atom_forces_packed(int N, const int* __restrict__ first, const int* __restrict__ last,
+                                     const int* __restrict__ emap, const int* __restrict__ rev,
+                                     const int* __restrict__ pinv, const double* __restrict__ f,
+                                     double* __restrict__ F, double dt, const double* __restrict__ inv_m,
+                                     double* __restrict__ v) {
+  pdl_begin();
+  const int a = static_cast<int>((static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (a >= N) return;
+  double s[3] = {0.0, 0.0, 0.0};
+  for (int q = first[a] + lane; q < last[a]; q += 32) {
+    const int er = rev[emap[q]];
+    const int qr = er >= 0 ? pinv[er] : -1;
+    for (int c = 0; c < 3; ++c)
+      s[c] += (qr >= 0 ? f[3 * static_cast<long>(qr) + c] : 0.0) - f[3 * static_cast<long>(q) + c];
+  }
+  for (int o = 16; o > 0; o >>= 1)
+    for (int c = 0; c < 3; ++c) s[c] += __shfl_xor_sync(0xffffffffu, s[c], o);
+  if (lane == 0) {
+    for (int c = 0; c < 3; ++c) F[3 * a + c] = s[c];
+    if (dt > 0.0) {
+      const double h = 0.5 * dt * kAccel * inv_m[a];
+      for (int c = 0; c < 3; ++c) v[3 * a + c] += h * s[c];
+    }
+  }
 }
 
 // skin-list forces of the packed edges: f_skin[emap[e]] = f_p[e]; one warp per atom
@@ -346,8 +376,7 @@ __global__ void k_reduce_final(int nblocks, const double* __restrict__ partial, 
   }
 }
 
-// velocity Verlet halves (positions A, velocities A/fs, forces eV/A, masses amu, dt fs)
-constexpr double kAccel = 9.648533212331e-3;  // (eV/A)/amu in A/fs^2
+// velocity Verlet halves
 
 __global__ void k_vv_first(int N, double dt, const double* __restrict__ F, const double* __restrict__ inv_m,
                            double* __restrict__ v, double* __restrict__ x) {
@@ -452,12 +481,19 @@ void launch_edge_geometry(long cap, int N, const int* first, const double* pos, 
 }
 
 void launch_edge_geometry_packed(int N, const int* first, const double* pos, double3 box, const int* nidx,
-                                 const int* ntype_e, const char4* shift, double r_cut, double* xyz, double* r,
-                                 double* f_skin, int* last, int* emap, int* nidx_p, int* ntype_p, double* xyz_p,
-                                 double* r_p, cudaStream_t s) {
+                                 const int* ntype_e, const char4* shift, double r_cut, int* pinv, int* last, int* emap,
+                                 int* nidx_p, int* ntype_p, double* xyz_p, double* r_p, cudaStream_t s) {
   if (N > 0)
-    launch_pdl(k_edge_geometry_packed, ceil_div(N, 4), 128, 0, s, N, first, pos, box, nidx, ntype_e, shift, r_cut, xyz,
-               r, f_skin, last, emap, nidx_p, ntype_p, xyz_p, r_p);
+    launch_pdl(k_edge_geometry_packed, ceil_div(N, 4), 128, 0, s, N, first, pos, box, nidx, ntype_e, shift, r_cut,
+               pinv, last, emap, nidx_p, ntype_p, xyz_p, r_p);
+}
+
+void launch_atom_forces_packed(int N, const int* first, const int* last, const int* emap, const int* rev,
+                               const int* pinv, const double* f_p, double* F, double dt, const double* inv_m, double* v,
+                               cudaStream_t s) {
+  if (N > 0)
+    launch_pdl(k_atom_forces_packed, ceil_div(N, 4), 128, 0, s, N, first, last, emap, rev, pinv, f_p, F, dt, inv_m,
+               v);  // one warp per atom
 }
 
 void launch_scatter_packed_forces(int N, const int* first, const int* last, const int* emap, const double* f_p,

@@ -122,11 +122,15 @@ void launch_reverse_edges(long cap, int N, const int* first, const int* nidx, co
                           int* rev, cudaStream_t s);
 void launch_edge_geometry(long cap, int N, const int* first, const double* pos, double3 box, const int* nidx,
                           const int* edge_i, const char4* shift, double* xyz, double* r, cudaStream_t s);
-// skin-list geometry plus the in-cut-off edges packed per centre atom (see k_md.cu)
+// the in-cut-off edges of a skin list packed per centre atom, with the maps both ways
+// (see k_md.cu)
 void launch_edge_geometry_packed(int N, const int* first, const double* pos, double3 box, const int* nidx,
-                                 const int* ntype_e, const char4* shift, double r_cut, double* xyz, double* r,
-                                 double* f_skin, int* last, int* emap, int* nidx_p, int* ntype_p, double* xyz_p,
-                                 double* r_p, cudaStream_t s);
+                                 const int* ntype_e, const char4* shift, double r_cut, int* pinv, int* last, int* emap,
+                                 int* nidx_p, int* ntype_p, double* xyz_p, double* r_p, cudaStream_t s);
+// atomic forces from the packed edges' forces; dt > 0: also the second velocity-Verlet half
+void launch_atom_forces_packed(int N, const int* first, const int* last, const int* emap, const int* rev,
+                               const int* pinv, const double* f_p, double* F, double dt, const double* inv_m, double* v,
+                               cudaStream_t s);
 void launch_scatter_packed_forces(int N, const int* first, const int* last, const int* emap, const double* f_p,
                                   double* f_skin, cudaStream_t s);
 void launch_atom_forces(int N, const int* first, const int* rev, const double* f, double* F, cudaStream_t s);

@@ -29,7 +29,7 @@ struct NeighList {
   char4* shift = nullptr;
   double *xyz = nullptr, *r = nullptr, *forces = nullptr;
   // the edges inside the cut-off, packed per centre atom each step (a skin list)
-  int *last = nullptr, *emap = nullptr, *nidx_p = nullptr, *ntype_p = nullptr;
+  int *last = nullptr, *emap = nullptr, *pinv = nullptr, *nidx_p = nullptr, *ntype_p = nullptr;
   double *xyz_p = nullptr, *r_p = nullptr, *forces_p = nullptr;
   long E = 0;
   bool realloc_happened = false;
@@ -37,12 +37,12 @@ struct NeighList {
   ~NeighList() { release(); }
   void release() {
     void* ps[] = {cell,  cell_count, cell_start, cell_fill, cell_atoms, num_neigh, first, nidx,  ntype_e,
-                  edge_i, rev,       shift,      xyz,       r,          forces,    last,  emap,  nidx_p,
-                  ntype_p, xyz_p,    r_p,        forces_p,  cell_tmp};
+                  edge_i, rev,       shift,      xyz,       r,          forces,    last,  emap,  pinv,
+                  nidx_p, ntype_p,   xyz_p,      r_p,       forces_p,   cell_tmp};
     for (void* p : ps)
       if (p) cudaFree(p);
     cell = cell_count = cell_start = cell_fill = cell_atoms = num_neigh = first = nidx = ntype_e = edge_i = rev = nullptr;
-    last = emap = nidx_p = ntype_p = cell_tmp = nullptr;
+    last = emap = pinv = nidx_p = ntype_p = cell_tmp = nullptr;
     shift = nullptr;
     xyz = r = forces = xyz_p = r_p = forces_p = nullptr;
     capN = ncell_cap = cell_atoms_cap = 0;
@@ -78,7 +78,8 @@ struct NeighList {
   void reserve_edges(long E_) {
     if (E_ <= capE) return;
     const long nE = static_cast<long>(E_ * 1.25) + 1024;
-    void* ps[] = {nidx, ntype_e, edge_i, rev, shift, xyz, r, forces, emap, nidx_p, ntype_p, xyz_p, r_p, forces_p};
+    void* ps[] = {nidx, ntype_e, edge_i, rev, shift, xyz, r, forces, emap, pinv, nidx_p, ntype_p, xyz_p, r_p,
+                  forces_p};
     for (void* p : ps)
       if (p) cudaFree(p);
     nidx = dalloc<int>(nE);
@@ -90,6 +91,7 @@ struct NeighList {
     r = dalloc<double>(nE);
     forces = dalloc<double>(3 * nE);
     emap = dalloc<int>(nE);
+    pinv = dalloc<int>(nE);
     nidx_p = dalloc<int>(nE);
     ntype_p = dalloc<int>(nE);
     xyz_p = dalloc<double>(3 * nE);
@@ -216,29 +218,41 @@ struct smx_md {
     return smx::EdgeIn{nl.first, species, nl.nidx, nl.ntype_e, nl.xyz, nl.r, N};
   }
 
-  // forces at the current positions (geometry + evaluator + scatter); graph-capturable.
-  // With a skin the evaluator sees only the edges inside the cut-off, packed per atom
-  // (the skin edges would cost it ~5% of its time), and their forces go back to the
-  // skin list, whose reverse-edge map gives the atomic forces.
-  void forces(cudaStream_t s) {
+  // forces at the current positions (geometry + evaluator + atomic forces), and with
+  // kick the second velocity-Verlet half step; graph-capturable.  With a skin the
+  // evaluator sees only the edges inside the cut-off, packed per atom (the skin edges
+  // would cost it ~5% of its time), and the atomic forces come from the packed edges'
+  // forces through the skin list's reverse-edge map (skin_view restores the skin list's
+  // geometry and forces for a state read-out).
+  void forces(cudaStream_t s, bool kick = false) {
     if (skin > 0.0) {
-      smx::launch_edge_geometry_packed(N, nl.first, pos, box, nl.nidx, nl.ntype_e, nl.shift, eng->hm.r_cut, nl.xyz,
-                                       nl.r, nl.forces, nl.last, nl.emap, nl.nidx_p, nl.ntype_p, nl.xyz_p, nl.r_p, s);
+      smx::launch_edge_geometry_packed(N, nl.first, pos, box, nl.nidx, nl.ntype_e, nl.shift, eng->hm.r_cut, nl.pinv,
+                                       nl.last, nl.emap, nl.nidx_p, nl.ntype_p, nl.xyz_p, nl.r_p, s);
       smx::EdgeIn in{nl.first, species, nl.nidx_p, nl.ntype_p, nl.xyz_p, nl.r_p, N};
       in.last = nl.last;
       eng->run(in, energies, nl.forces_p, s);
-      smx::launch_scatter_packed_forces(N, nl.first, nl.last, nl.emap, nl.forces_p, nl.forces, s);
-    } else {
-      smx::launch_edge_geometry(nl.capE, N, nl.first, pos, box, nl.nidx, nl.edge_i, nl.shift, nl.xyz, nl.r, s);
-      eng->run(edges(), energies, nl.forces, s);
+      smx::launch_atom_forces_packed(N, nl.first, nl.last, nl.emap, nl.rev, nl.pinv, nl.forces_p, F, kick ? dt : 0.0,
+                                     inv_m, vel, s);
+      return;
     }
+    smx::launch_edge_geometry(nl.capE, N, nl.first, pos, box, nl.nidx, nl.edge_i, nl.shift, nl.xyz, nl.r, s);
+    eng->run(edges(), energies, nl.forces, s);
     smx::launch_atom_forces(N, nl.first, nl.rev, nl.forces, F, s);
+    if (kick) smx::launch_vv_second(N, dt, F, inv_m, vel, s);
+  }
+
+  // the skin list's edge vectors and per-edge forces (zero beyond the cut-off) of the last
+  // force evaluation, for the energy and virial sums
+  void skin_view(cudaStream_t s) {
+    if (skin <= 0.0 || N == 0) return;
+    smx::launch_edge_geometry(nl.capE, N, nl.first, pos, box, nl.nidx, nl.edge_i, nl.shift, nl.xyz, nl.r, s);
+    check(cudaMemsetAsync(nl.forces, 0, sizeof(double) * 3 * nl.E, s), "cudaMemsetAsync");
+    smx::launch_scatter_packed_forces(N, nl.first, nl.last, nl.emap, nl.forces_p, nl.forces, s);
   }
 
   void one_step(cudaStream_t s) {
     smx::launch_vv_first(N, dt, F, inv_m, vel, pos, s);
-    forces(s);
-    smx::launch_vv_second(N, dt, F, inv_m, vel, s);
+    forces(s, true);
   }
 
   // renumber the atoms in the cell list's order (no-op for boxes too small for cells)
@@ -520,6 +534,7 @@ int smx_md_state(smx_md* md, double* positions, double* velocities, double* forc
   try {
     cudaStream_t s = md->eng->stream;
     const int N = md->N;
+    md->skin_view(s);
     smx::launch_reduce(N, md->nl.first, md->energies, md->nl.xyz, md->nl.forces, md->partial, smx_md::kReduceBlocks,
                        md->reduced, s);
     double red[10];

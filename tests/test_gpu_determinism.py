@@ -58,6 +58,14 @@ def test_forces_bitwise_reproducible(engine_lib, tmp_path, L_max, precision):
     m2.set_option("persistent", 0)
     m2.compute_node_energies_forces(*args)
     assert _same(m2.node_energies, e0) and _same(m2.node_forces, f0)
+    # plain launches instead of programmatic dependent launches (a process-wide option)
+    assert m2.get_option("pdl") == 1
+    m2.set_option("pdl", 0)
+    try:
+        m2.compute_node_energies_forces(*args)
+        assert _same(m2.node_energies, e0) and _same(m2.node_forces, f0)
+    finally:
+        m2.set_option("pdl", 1)
     # and the result is the right one
     ref = Evaluator(path, "port")
     ref.compute_node_energies_forces(*args)

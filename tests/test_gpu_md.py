@@ -135,8 +135,12 @@ def test_md_renumbering_keeps_caller_order(engine_lib, small_model_path):
     md.run(205)
     st = md.state()
     assert st["step"] == 205
-    _, _, F, _ = m.compute_atoms(st["positions"], sp, box=L)
+    E, _, F, W = m.compute_atoms(st["positions"], sp, box=L)
     np.testing.assert_allclose(st["forces"], F, atol=1e-5)
+    # the energy and virial sums over the skin list (its geometry and per-edge forces are
+    # filled for the read-out from the packed in-cut-off edges)
+    assert abs(st["potential_energy"] - E) < 1e-6 * len(sp)
+    np.testing.assert_allclose(st["virial"], W, atol=1e-4 * max(1.0, np.abs(W).max()))
     # momentum is conserved in the caller's order too (masses of the caller's species)
     p = (masses[:, None] * st["velocities"]).sum(0)
     p0 = (masses[:, None] * v).sum(0)

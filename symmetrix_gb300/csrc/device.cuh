@@ -63,8 +63,9 @@ struct DevModel {
   // s_i = 1 + sum_j s(r_ij) and c_i = (dE/dA_scaled . A_scaled) / s_i
   float* dens_s[2];
   float* dens_c[2];
-  // BF16 form: the producers also write the tensor-core GEMM X operands as `tc_terms`
-  // bf16 split terms per row (see write_split); nullptr in the FP32 form.
+  // BF16 form: the producers also write the tensor-core GEMM X operands as
+  // XT = split_xterms(tc_terms) bf16 split terms per row (see write_split); nullptr in
+  // the FP32 form.  Offsets and pitches below are in units of T = XT.
   //   op_m0    [N*nLM][T*C]                rows (node, LM)              (H1 GEMM)
   //   op_phi1  per l: [N(2l+1)][T*n_e*C]   at T*N*lme_off[l]*C          (A1 GEMM)
   //   op_a1adj per l: [N(2l+1)][T*C]       at T*N*l*l*C                 (Phi1_adj GEMM)
@@ -205,17 +206,18 @@ inline int atom_grid(const DevModel& m, int k, int n, DevModel& mk) {
   return n;
 }
 
-// Element `col` of a GEMM operand row of width K as bf16 split terms: (hi), (hi | hi)
-// or (hi | lo | hi) for 1, 2, 3 terms, hi = bf16(v), lo = bf16(v - hi); the B operand
-// rows carry (W_hi), (W_hi | W_lo), (W_hi | W_hi | W_lo).
+// The split-term products of a tensor-core GEMM with T terms: x_hi W_hi (T = 1),
+// + x_hi W_lo (T = 2), + x_lo W_hi (T = 3), hi = bf16(v), lo = bf16(v - hi).  An X
+// operand row stores split_xterms(T) blocks of width K, (hi) or (hi | lo); a B operand
+// row stores (W_hi) for T = 1, else (W_hi | W_lo); the GEMM reads each block once per
+// k-block and issues the T products from shared memory.
+__host__ __device__ __forceinline__ int split_xterms(int T) { return T == 3 ? 2 : 1; }
+__host__ __device__ __forceinline__ int split_wterms(int T) { return T == 1 ? 1 : 2; }
+// element `col` of an X operand row of width K (row pitch split_xterms(T) * K)
 __device__ __forceinline__ void write_split(__nv_bfloat16* row, int K, int T, int col, float v) {
   const __nv_bfloat16 hi = __float2bfloat16_rn(v);
   row[col] = hi;
-  if (T == 2) row[K + col] = hi;
-  if (T == 3) {
-    row[K + col] = __float2bfloat16_rn(v - __bfloat162float(hi));
-    row[2 * K + col] = hi;
-  }
+  if (T == 3) row[K + col] = __float2bfloat16_rn(v - __bfloat162float(hi));
 }
 
 // ZBL energy of one directed edge and its r-derivative, as zbl.cpp:22-94

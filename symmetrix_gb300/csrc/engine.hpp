@@ -60,7 +60,7 @@ struct smx_engine {
   unsigned* check_host = nullptr;
   unsigned* check_dev = nullptr;
   // precision form: bf16 B operands (K contiguous) of the tensor-core GEMMs
-  // (K contiguous, `tc_terms` bf16 split terms concatenated along K: see tc_operand)
+  // (K contiguous, split_wterms(tc_terms) bf16 split terms concatenated along K: see tc_operand)
   const __nv_bfloat16 *W_H1 = nullptr, *W_M0adj = nullptr, *W_A1[4] = {}, *W_Phi1adj[4] = {};
   bool tc_H1 = false, tc_A1[4] = {}, tc_Phi1adj[4] = {};
   // 1: bf16 operands; 2: weights split hi + lo (x_hi W_hi + x_hi W_lo); 3: both
@@ -96,11 +96,11 @@ struct smx_engine {
   bool M0_kept = false, Phi1_kept = false, A1adj_kept = false;  // float32 rows written by it
 
   // B operand of a tensor-core GEMM from a row-major float [nrows][K] matrix: row n
-  // holds (W_hi), (W_hi | W_lo) or (W_hi | W_hi | W_lo) for 1, 2, 3 terms,
-  // W_lo = bf16(W - W_hi).
+  // holds (W_hi) for 1 split product, (W_hi | W_lo) for 2 or 3, W_lo = bf16(W - W_hi)
+  // (see write_split).
   const __nv_bfloat16* tc_operand(const std::vector<float>& W, int nrows, int K) {
-    const int T = tc_terms;
-    std::vector<uint16_t> b(static_cast<size_t>(nrows) * K * T);
+    const int WT = smx::split_wterms(tc_terms);
+    std::vector<uint16_t> b(static_cast<size_t>(nrows) * K * WT);
     for (int n = 0; n < nrows; ++n)
       for (int k = 0; k < K; ++k) {
         const float w = W[static_cast<size_t>(n) * K + k];
@@ -109,8 +109,7 @@ struct smx_engine {
         float hf;
         std::memcpy(&hf, &hu, 4);
         const uint16_t lo = smx::bf16_bits(w - hf);
-        for (int t = 0; t < T; ++t)
-          b[(static_cast<size_t>(n) * T + t) * K + k] = (t == T - 1 && T > 1) ? lo : hi;
+        for (int t = 0; t < WT; ++t) b[(static_cast<size_t>(n) * WT + t) * K + k] = t == 0 ? hi : lo;
       }
     return reinterpret_cast<const __nv_bfloat16*>(upload(b));
   }
@@ -266,11 +265,12 @@ struct smx_engine {
     if (precision == SMX_PRECISION_BF16) {
       check(smx::init_umma_kernels(), "cudaFuncSetAttribute");
       const int C = pm.C;
-      tc_H1 = smx::umma_supported(C, C) && pm.L_max == 1;
+      // (three split products, the most the tc_terms option allows)
+      tc_H1 = smx::umma_supported(C, C, 3) && pm.L_max == 1;
       for (int l = 0; l < 4; ++l) {
         if (pm.num_e[l] == 0) continue;
-        tc_A1[l] = smx::umma_supported(pm.num_e[l] * C, C);
-        tc_Phi1adj[l] = smx::umma_supported(C, C);
+        tc_A1[l] = smx::umma_supported(pm.num_e[l] * C, C, 3);
+        tc_Phi1adj[l] = smx::umma_supported(C, C, 3);
       }
       hw_H1W = pm.H1W;
       hw_H1W_T = pm.H1W_T;
@@ -345,7 +345,7 @@ struct smx_engine {
     atom_order = dalloc<int>(nN);
     nneigh = dalloc<int>(nN);
     if (precision == SMX_PRECISION_BF16) {
-      const long T = tc_terms;
+      const long T = smx::split_xterms(tc_terms);  // stored X terms
       M0_bf = dalloc<__nv_bfloat16>(T * nN * dm.nLM * C);
       Phi1_bf = dalloc<__nv_bfloat16>(T * nN * dm.n_lme * C);
       A1adj_bf = dalloc<__nv_bfloat16>(T * nN * 16 * C);
@@ -417,18 +417,18 @@ struct smx_engine {
     for (int nt : {C, C / 2, 2 * C}) {
       if (!tile_n && nt != C) continue;
       bool ok = nt >= 64 && nt <= 256;
-      for (int q = 0; q < ng && ok; ++q) ok = g[q].nb_rows % nt == 0 && smx::umma_supported(g[q].K, nt);
+      for (int q = 0; q < ng && ok; ++q) ok = g[q].nb_rows % nt == 0 && smx::umma_supported(g[q].K, nt, g[q].terms);
       if (!ok) continue;
-      for (int st : {2, 3, 4}) cand.push_back(TcCfg{nt == C ? 0 : nt, st});
+      for (int st : {1, 2, 3, 4}) cand.push_back(TcCfg{nt == C ? 0 : nt, st});
     }
     if (tile_n) {  // one N-tile per GEMM where some B is wider than C and all fit a tile
       bool ok = true, wider = false;
       for (int q = 0; q < ng && ok; ++q) {
-        ok = g[q].nb_rows <= 256 && smx::umma_supported(g[q].K, g[q].nb_rows);
+        ok = g[q].nb_rows <= 256 && smx::umma_supported(g[q].K, g[q].nb_rows, g[q].terms);
         wider = wider || g[q].nb_rows != C;
       }
       if (ok && wider)
-        for (int st : {2, 3, 4}) cand.push_back(TcCfg{-1, st});
+        for (int st : {1, 2, 3, 4}) cand.push_back(TcCfg{-1, st});
     }
     cudaEvent_t a, b;
     check(cudaEventCreate(&a), "cudaEventCreate");
@@ -672,7 +672,7 @@ struct smx_engine {
       in.order = atom_order;
     }
     const int C = dm.C;
-    const int T = tc_terms;
+    const int T = tc_terms, XT = smx::split_xterms(T);
     lastN = N;
     if (N == 0) {
       evaluated = true;
@@ -702,9 +702,10 @@ struct smx_engine {
     mark(1, s);
     if (tc_H1) {  // H1 = M0 @ H1W[L]  (mace.cpp:397-423), tensor cores
       // (layer0_fwd wrote M0 as split bf16 rows into M0_bf)
-      smx::UmmaGemm g{M0_bf, static_cast<long>(N) * dm.nLM, T * C, W_H1, 2 * C, C,
+      smx::UmmaGemm g{M0_bf, static_cast<long>(N) * dm.nLM, C, W_H1, 2 * C, C,
                        smx::UmmaOut{H1, static_cast<long>(N) * dm.nLM, dm.nLM, static_cast<long>(dm.nLM) * C, 0, C,
                                     1}};
+      g.terms = T;
       run_tc(0, &g, 1, false, s);
     } else {  // H1 = M0 @ H1W[L]  (mace.cpp:397-423)
       smx::GemmBatch b{};
@@ -724,8 +725,9 @@ struct smx_engine {
         if (dm.num_e[l] > 0 && tc_A1[l]) {
           const long rows = static_cast<long>(N) * (2 * l + 1);
           const int K = dm.num_e[l] * C;
-          g[ng++] = smx::UmmaGemm{Phi1_bf + static_cast<size_t>(T) * N * dm.lme_off[l] * C, rows, T * K, W_A1[l], C,
-                                  C, smx::UmmaOut{A1, rows, 2 * l + 1, 16L * C, l * l * C, C, 0}};
+          g[ng] = smx::UmmaGemm{Phi1_bf + static_cast<size_t>(XT) * N * dm.lme_off[l] * C, rows, K, W_A1[l], C, C,
+                                smx::UmmaOut{A1, rows, 2 * l + 1, 16L * C, l * l * C, C, 0}};
+          g[ng++].terms = T;
         }
       run_tc(1, g, ng, true, s);
       smx::GemmBatch b{};
@@ -747,10 +749,11 @@ struct smx_engine {
       for (int l = 0; l < 4; ++l)
         if (dm.num_e[l] > 0 && tc_Phi1adj[l]) {
           const long rows = static_cast<long>(N) * (2 * l + 1);
-          g[ng++] = smx::UmmaGemm{A1adj_bf + static_cast<size_t>(T) * N * l * l * C, rows, T * C, W_Phi1adj[l],
-                                  dm.num_e[l] * C, C,
-                                  smx::UmmaOut{Phi1_adj, rows, 2 * l + 1, static_cast<long>(dm.n_lme) * C,
-                                               dm.lme_off[l] * C, dm.num_e[l] * C, 0}};
+          g[ng] = smx::UmmaGemm{A1adj_bf + static_cast<size_t>(XT) * N * l * l * C, rows, C, W_Phi1adj[l],
+                                dm.num_e[l] * C, C,
+                                smx::UmmaOut{Phi1_adj, rows, 2 * l + 1, static_cast<long>(dm.n_lme) * C,
+                                             dm.lme_off[l] * C, dm.num_e[l] * C, 0}};
+          g[ng++].terms = T;
         }
       run_tc(2, g, ng, true, s);
       smx::GemmBatch b{};
@@ -766,9 +769,10 @@ struct smx_engine {
     // the float H1_adj rows (and the BF16 form's split operand) from the fixed-point sums
     smx::launch_fixed_rows(H1_adj_fx, H1_adj, tc_H1 ? H1adj_bf : nullptr, static_cast<long>(N) * dm.nLM, C, T, s);
     if (tc_H1) {  // M0_adj = H1_adj @ H1W[L]^T  (mace.cpp:425-451), tensor cores
-      smx::UmmaGemm g{H1adj_bf, static_cast<long>(N) * dm.nLM, T * C, W_M0adj, 2 * C, C,
+      smx::UmmaGemm g{H1adj_bf, static_cast<long>(N) * dm.nLM, C, W_M0adj, 2 * C, C,
                        smx::UmmaOut{M0_adj, static_cast<long>(N) * dm.nLM, dm.nLM, static_cast<long>(dm.nLM) * C, 0,
                                     C, 1}};
+      g.terms = T;
       run_tc(3, &g, 1, false, s);
     } else {  // M0_adj = H1_adj @ H1W[L]^T  (mace.cpp:425-451)
       smx::GemmBatch b{};

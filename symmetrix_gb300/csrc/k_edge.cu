@@ -203,7 +203,8 @@ __device__ __forceinline__ void layer0_fwd_atom(const DevModel& m, const EdgeIn&
       for (int LM = 0; LM < NLM; ++LM) {
         if (M0) out[LM * C] = v[LM];  // nullptr: only the split rows are consumed
         if (m.op_m0)  // BF16 form: the H1 GEMM's split operand
-          write_split(m.op_m0 + (static_cast<size_t>(i) * m.nLM + LM) * m.tc_terms * C, C, m.tc_terms, k, v[LM]);
+          write_split(m.op_m0 + (static_cast<size_t>(i) * m.nLM + LM) * split_xterms(m.tc_terms) * C, C, m.tc_terms,
+                      k, v[LM]);
       }
       continue;
     }
@@ -218,7 +219,8 @@ __device__ __forceinline__ void layer0_fwd_atom(const DevModel& m, const EdgeIn&
       }
       if (M0) M0[(static_cast<size_t>(i) * m.nLM + LM) * C + k] = f;
       if (m.op_m0)
-        write_split(m.op_m0 + (static_cast<size_t>(i) * m.nLM + LM) * m.tc_terms * C, C, m.tc_terms, k, f);
+        write_split(m.op_m0 + (static_cast<size_t>(i) * m.nLM + LM) * split_xterms(m.tc_terms) * C, C, m.tc_terms, k,
+                    f);
     }
   }
 }

@@ -122,7 +122,7 @@ __device__ __forceinline__ void dispatch_kf(int kp, F&& f) {
 template <int KF>
 __device__ __forceinline__ void l1_fwd_epilogue(const DevModel& m, int N, int i, const float* sP, int stride, int kk,
                                                 int k, int row_group, int nrow_groups, float* __restrict__ Phi1) {
-  const int C = m.C, T = m.tc_terms;
+  const int C = m.C, T = m.tc_terms, XT = split_xterms(T);
   for (int l = 0; l < 4; ++l) {
     const int ne = m.num_e[l], Kl = ne * C;
     for (int mm = 0; mm < 2 * l + 1; ++mm)
@@ -139,8 +139,8 @@ __device__ __forceinline__ void l1_fwd_epilogue(const DevModel& m, int N, int i,
         }
         if (Phi1) Phi1[(static_cast<size_t>(i) * m.n_lme + lme) * C + k] = s;  // nullptr: split rows only
         if (m.op_phi1) {
-          __nv_bfloat16* row = m.op_phi1 + static_cast<size_t>(T) * N * m.lme_off[l] * C +
-                               (static_cast<size_t>(i) * (2 * l + 1) + mm) * T * Kl;
+          __nv_bfloat16* row = m.op_phi1 + static_cast<size_t>(XT) * N * m.lme_off[l] * C +
+                               (static_cast<size_t>(i) * (2 * l + 1) + mm) * XT * Kl;
           write_split(row, Kl, T, e * C + k, s);
         }
       }

@@ -231,12 +231,12 @@ __device__ __forceinline__ void node_tail_atom(const DevModel& m, const int* __r
 #pragma unroll
     for (int q = 0; q < 16; ++q) A1_adj[(static_cast<size_t>(i) * 16 + q) * C + k] = sG[q * C + k] * m1a / S1;
   if (m.op_a1adj) {  // BF16 form: the Phi1_adj GEMM's split operand, rows (node, m) per l
-    const int T = m.tc_terms;
+    const int T = m.tc_terms, XT = split_xterms(T);
     for (int l = 0; l < 4; ++l) {
       if (m.num_e[l] == 0) continue;
       for (int mm = 0; mm < 2 * l + 1; ++mm) {
-        __nv_bfloat16* row = m.op_a1adj + static_cast<size_t>(T) * N * l * l * C +
-                             (static_cast<size_t>(i) * (2 * l + 1) + mm) * T * C;
+        __nv_bfloat16* row = m.op_a1adj + static_cast<size_t>(XT) * N * l * l * C +
+                             (static_cast<size_t>(i) * (2 * l + 1) + mm) * XT * C;
         write_split(row, C, T, k, sG[(l * l + mm) * C + k] * m1a / S1);
       }
     }
@@ -287,8 +287,8 @@ void node_tail_residency(const DevModel& m, int* per_sm) {
 }
 
 // H1_adj from its fixed-point accumulator: float rows for the SIMT GEMM and the stage
-// reads, and in the BF16 form the M0_adj GEMM's split operand rows (pitch terms * C, as
-// launch_rows_to_bf16 writes them).
+// reads, and in the BF16 form the M0_adj GEMM's split operand rows (write_split with
+// `terms` products: row pitch split_xterms(terms) * C).
 __global__ void k_fixed_rows(const fix64* __restrict__ src, float* __restrict__ dst, __nv_bfloat16* __restrict__ bf,
                              long rows, int C, int terms) {
   pdl_begin();
@@ -299,7 +299,7 @@ __global__ void k_fixed_rows(const fix64* __restrict__ src, float* __restrict__ 
     dst[t] = v;
     if (bf) {
       const long r = t / C;
-      write_split(bf + r * terms * C, C, terms, static_cast<int>(t - r * C), v);
+      write_split(bf + r * split_xterms(terms) * C, C, terms, static_cast<int>(t - r * C), v);
     }
   }
 }

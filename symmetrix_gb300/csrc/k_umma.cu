@@ -4,11 +4,14 @@
 //
 // One CTA per 128-row x NT-column tile.  Thread 0 streams 64-wide k-blocks of the X
 // tile and the B tile with TMA (128-byte swizzled boxes) through a ring of up to four
-// shared-memory stages (full/empty mbarriers); thread 32 issues four tcgen05.mma
-// (M=128, N=NT, K=16) per k-block into an f32 accumulator in tensor memory and
-// releases each stage with tcgen05.commit; after the last commit the four warps read
-// their 32 accumulator lanes back with tcgen05.ld and store them through an affine row
-// map straight into the engine's feature layouts.
+// shared-memory stages (full/empty mbarriers); a stage holds the k-block of every stored
+// split term (X: hi, lo; B: W_hi, W_lo).  Thread 32 issues, per 16-wide step of the
+// k-block, one tcgen05.mma (M=128, N=NT, K=16) per split product (x_hi W_hi, x_hi W_lo,
+// x_lo W_hi) into an f32 accumulator in tensor memory, so each term is loaded once and
+// used by every product that needs it, and releases each stage with tcgen05.commit;
+// after the last commit the four warps read their 32 accumulator lanes back with
+// tcgen05.ld and store them through an affine row map straight into the engine's
+// feature layouts.
 //
 // These GEMMs restate compute_H1, compute_A1, reverse_A1 and reverse_H1
 // (libsymmetrix/source/mace.cpp:397-451, :607-679) with bf16 operands and f32
@@ -47,7 +50,7 @@ constexpr int kStages = 4;     // maximum shared-memory ring depth (k-blocks in 
 struct UmmaSegDev {
   CUtensorMap ta, tb;
   UmmaOut o;
-  int K, NT, tiles_m, tiles_n, stages;
+  int K, NT, tiles_m, tiles_n, stages, terms;
 };
 struct UmmaGroupDev {
   UmmaSegDev s[4];
@@ -66,7 +69,8 @@ __global__ void __launch_bounds__(128, 1) k_umma_gemm(const __grid_constant__ Um
   const CUtensorMap& ta = seg.ta;
   const CUtensorMap& tb = seg.tb;
   const UmmaOut& o = seg.o;
-  const int K = seg.K, NT = seg.NT;
+  const int K = seg.K, NT = seg.NT, terms = seg.terms;
+  const int XT = split_xterms(terms), WT = split_wterms(terms);
   extern __shared__ uint8_t smem_raw[];
   __shared__ uint64_t full[kStages], empty[kStages], bar_mma;  // kStages >= seg.stages
   __shared__ uint32_t tmem_base;
@@ -74,7 +78,8 @@ __global__ void __launch_bounds__(128, 1) k_umma_gemm(const __grid_constant__ Um
   const int KB = K / kBoxK;
   const int S = KB < seg.stages ? KB : seg.stages;
   const uint32_t a_bytes = kTileM * kBoxK * 2, b_bytes = static_cast<uint32_t>(NT) * kBoxK * 2;
-  const uint32_t stage_bytes = a_bytes + b_bytes;  // stage = A box then B box (both 1024-B multiples)
+  // stage = the XT X boxes, then the WT B boxes (all 1024-B multiples)
+  const uint32_t stage_bytes = XT * a_bytes + WT * b_bytes;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = tile_m * kTileM, n0 = tile_n * NT;
   const uint32_t ncols = NT <= 32 ? 32u : (NT <= 64 ? 64u : (NT <= 128 ? 128u : 256u));
@@ -108,8 +113,9 @@ __global__ void __launch_bounds__(128, 1) k_umma_gemm(const __grid_constant__ Um
       }
       uint8_t* st = smem + static_cast<size_t>(s) * stage_bytes;
       sm100::mbar_arrive_expect_tx(&full[s], stage_bytes);
-      sm100::tma_load_2d(st, &ta, kb * kBoxK, m0, &full[s]);
-      sm100::tma_load_2d(st + a_bytes, &tb, kb * kBoxK, n0, &full[s]);
+      for (int t = 0; t < XT; ++t) sm100::tma_load_2d(st + t * a_bytes, &ta, t * K + kb * kBoxK, m0, &full[s]);
+      for (int u = 0; u < WT; ++u)
+        sm100::tma_load_2d(st + XT * a_bytes + u * b_bytes, &tb, u * K + kb * kBoxK, n0, &full[s]);
       ++loads;
     }
   }
@@ -124,11 +130,19 @@ __global__ void __launch_bounds__(128, 1) k_umma_gemm(const __grid_constant__ Um
         break;
       }
       sm100::tc_fence_after();
-      const uint32_t a0 = sm100::smem_u32(smem + static_cast<size_t>(s) * stage_bytes), b0 = a0 + a_bytes;
+      const uint32_t x0 = sm100::smem_u32(smem + static_cast<size_t>(s) * stage_bytes), w0 = x0 + XT * a_bytes;
 #pragma unroll
-      for (int k = 0; k < kBoxK / 16; ++k)  // 16 elements (32 B) per MMA inside the 128-B swizzled row
-        sm100::umma_bf16(tmem, sm100::sdesc_sw128(a0 + k * 32), sm100::sdesc_sw128(b0 + k * 32), idesc,
+      for (int k = 0; k < kBoxK / 16; ++k) {  // 16 elements (32 B) per MMA inside the 128-B swizzled row
+        // x_hi W_hi, then x_hi W_lo (terms >= 2), then x_lo W_hi (terms 3)
+        sm100::umma_bf16(tmem, sm100::sdesc_sw128(x0 + k * 32), sm100::sdesc_sw128(w0 + k * 32), idesc,
                          (kb | k) != 0 ? 1u : 0u);
+        if (terms >= 2)
+          sm100::umma_bf16(tmem, sm100::sdesc_sw128(x0 + k * 32), sm100::sdesc_sw128(w0 + b_bytes + k * 32), idesc,
+                           1u);
+        if (terms == 3)
+          sm100::umma_bf16(tmem, sm100::sdesc_sw128(x0 + a_bytes + k * 32), sm100::sdesc_sw128(w0 + k * 32), idesc,
+                           1u);
+      }
       sm100::umma_commit(&empty[s]);
       issued = true;
     }
@@ -187,44 +201,6 @@ __global__ void __launch_bounds__(128, 1) k_umma_gemm(const __grid_constant__ Um
   if (warp == 0) sm100::tmem_dealloc(tmem, ncols);
 }
 
-// Split of x into bf16 terms: hi = bf16(x), lo = bf16(x - hi).  Row r of dst holds
-// `terms` blocks of `width`: (hi), (hi | hi) or (hi | lo | hi), matching B operands
-// (W_hi), (W_hi | W_lo) or (W_hi | W_hi | W_lo), so that one GEMM over terms*width
-// sums x_hi W_hi (+ x_hi W_lo) or x_hi W_hi + x_lo W_hi + x_hi W_lo.
-// Source element c of row r: src[(r / rpn) * s_ns + s_off + (r % rpn) * s_rs + c].
-__global__ void k_rows_to_bf16(const float* __restrict__ src, __nv_bfloat16* __restrict__ dst, long rows, int width,
-                               int rpn, long s_ns, int s_off, int s_rs, int terms) {
-  const int w4 = width >> 2;
-  const long n = rows * w4;
-  const long pitch = static_cast<long>(terms) * width;
-  for (long t = blockIdx.x * static_cast<long>(blockDim.x) + threadIdx.x; t < n;
-       t += static_cast<long>(gridDim.x) * blockDim.x) {
-    const long r = t / w4;
-    const int c = static_cast<int>(t - r * w4) * 4;
-    const float4 v = *reinterpret_cast<const float4*>(src + (r / rpn) * s_ns + s_off + (r % rpn) * s_rs + c);
-    const __nv_bfloat162 h0 = __floats2bfloat162_rn(v.x, v.y), h1 = __floats2bfloat162_rn(v.z, v.w);
-    __nv_bfloat162* d = reinterpret_cast<__nv_bfloat162*>(dst + r * pitch + c);
-    d[0] = h0;
-    d[1] = h1;
-    if (terms == 2) {
-      __nv_bfloat162* dh = reinterpret_cast<__nv_bfloat162*>(dst + r * pitch + width + c);
-      dh[0] = h0;
-      dh[1] = h1;
-    }
-    if (terms == 3) {
-      const float2 f0 = __bfloat1622float2(h0), f1 = __bfloat1622float2(h1);
-      __nv_bfloat162* dl = reinterpret_cast<__nv_bfloat162*>(dst + r * pitch + width + c);
-      dl[0] = __floats2bfloat162_rn(v.x - f0.x, v.y - f0.y);
-      dl[1] = __floats2bfloat162_rn(v.z - f1.x, v.w - f1.y);
-    }
-    if (terms > 2) {
-      __nv_bfloat162* dh = reinterpret_cast<__nv_bfloat162*>(dst + r * pitch + 2 * width + c);
-      dh[0] = h0;
-      dh[1] = h1;
-    }
-  }
-}
-
 using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                    const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                    CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -262,16 +238,18 @@ CUtensorMap make_map(const void* base, long rows, int K, int box_rows) {
 
 }  // namespace
 
-size_t umma_smem_bytes(int K, int NT, int stages) {
+size_t umma_smem_bytes(int K, int NT, int stages, int terms) {
   stages = std::min(K / kBoxK, std::min(stages, kStages));
-  return static_cast<size_t>(stages) * (kTileM + NT) * kBoxK * 2 + 1024;
+  return static_cast<size_t>(stages) * (split_xterms(terms) * kTileM + split_wterms(terms) * NT) * kBoxK * 2 + 1024;
 }
 
 // dynamic shared memory available next to the kernel's few static words
 constexpr size_t kMaxDynSmem = 226 * 1024;
 
-bool umma_supported(int K, int NT) {
-  return K % kBoxK == 0 && NT % 32 == 0 && NT >= 32 && NT <= 256 && umma_smem_bytes(K, NT, kStages) <= kMaxDynSmem;
+// (the launch lowers a schedule's ring depth until its stages fit)
+bool umma_supported(int K, int NT, int terms) {
+  return K % kBoxK == 0 && K > 0 && NT % 32 == 0 && NT >= 32 && NT <= 256 && terms >= 1 && terms <= 3 &&
+         umma_smem_bytes(K, NT, 1, terms) <= kMaxDynSmem;
 }
 
 cudaError_t init_umma_kernels() {
@@ -290,32 +268,26 @@ void launch_umma_gemms(const UmmaGemm* g, int n, unsigned* status, cudaStream_t 
   int used = 0;
   for (int q = 0; q < n; ++q) {
     const UmmaGemm& a = g[q];
-    if (!umma_supported(a.K, a.NT) || a.nb_rows % a.NT != 0)
+    if (!umma_supported(a.K, a.NT, a.terms) || a.nb_rows % a.NT != 0)
       throw std::invalid_argument("unsupported tensor-core GEMM shape");
     if (a.rows <= 0) continue;
     UmmaSegDev& d = grp.s[used++];
-    d.ta = make_map(a.X, a.rows, a.K, kTileM);
-    d.tb = make_map(a.B, a.nb_rows, a.K, a.NT);
+    d.ta = make_map(a.X, a.rows, split_xterms(a.terms) * a.K, kTileM);
+    d.tb = make_map(a.B, a.nb_rows, split_wterms(a.terms) * a.K, a.NT);
     d.o = a.o;
     d.K = a.K;
     d.NT = a.NT;
+    d.terms = a.terms;
     d.tiles_m = static_cast<int>((a.rows + kTileM - 1) / kTileM);
     d.tiles_n = a.nb_rows / a.NT;
     d.stages = a.stages >= 1 && a.stages <= kStages ? a.stages : kStages;
+    while (d.stages > 1 && umma_smem_bytes(a.K, a.NT, d.stages, a.terms) > kMaxDynSmem) --d.stages;
     gx = std::max(gx, static_cast<long>(d.tiles_m) * d.tiles_n);
-    smem = std::max(smem, umma_smem_bytes(a.K, a.NT, d.stages));
+    smem = std::max(smem, umma_smem_bytes(a.K, a.NT, d.stages, a.terms));
   }
   if (used == 0) return;
   if (gx > 0x7fffffffL) throw std::invalid_argument("tensor-core GEMM too large for one launch");
   launch_pdl(k_umma_gemm, dim3(static_cast<unsigned>(gx), 1, used), 128, smem, s, grp, status);
-}
-
-void launch_rows_to_bf16(const float* src, __nv_bfloat16* dst, long rows, int width, int rpn, long s_ns, int s_off,
-                         int s_rs, int terms, cudaStream_t s) {
-  if (rows <= 0) return;
-  const long n = rows * (width / 4);
-  const int blocks = static_cast<int>(std::min<long>((n + 255) / 256, 152L * 16));
-  k_rows_to_bf16<<<blocks, 256, 0, s>>>(src, dst, rows, width, rpn, s_ns, s_off, s_rs, terms);
 }
 
 }  // namespace smx

@@ -51,8 +51,8 @@ void launch_gemm(const GemmBatch& b, cudaStream_t s);
 void launch_node_tail(const DevModel& m, const int* node_type, int N, float* A1, const float* H1, float* M1,
                       float* H2, float* A1_adj, fix64* H1_adj, float* M1_adj, float* H2_adj, const float* zbl_e,
                       double* energies, cudaStream_t s);
-// dst[rows][C] = the fixed-point rows src as float; bf (optional): their bf16 split terms,
-// row pitch terms * C
+// dst[rows][C] = the fixed-point rows src as float; bf (optional): their bf16 split terms
+// for a GEMM with `terms` products (write_split), row pitch split_xterms(terms) * C
 void launch_fixed_rows(const fix64* src, float* dst, __nv_bfloat16* bf, long rows, int C, int terms, cudaStream_t s);
 // single-stage calls: dst = fixed-point copy of src (zero: dst = 0); forces = (zero ? 0 :
 // forces) - the sum of the nslices f1 slices (stride apart), n = 3 * edges
@@ -83,9 +83,11 @@ struct UmmaOut {
   int select;
 };
 cudaError_t init_umma_kernels();
-size_t umma_smem_bytes(int K, int NT, int stages);
-bool umma_supported(int K, int NT);
-// One GEMM: X [rows][K] bf16, B [nb_rows][K] bf16 (N-tiles of NT rows), output map o.
+size_t umma_smem_bytes(int K, int NT, int stages, int terms);
+bool umma_supported(int K, int NT, int terms);
+// One GEMM, Y = sum of the `terms` split products (write_split): X [rows][XT * K] bf16
+// (XT = split_xterms(terms) blocks of K), B [nb_rows][WT * K] bf16 (WT = split_wterms(terms);
+// N-tiles of NT rows), output map o.
 struct UmmaGemm {
   const __nv_bfloat16* X;
   long rows;
@@ -94,15 +96,12 @@ struct UmmaGemm {
   int nb_rows, NT;
   UmmaOut o;
   int stages = 4;  // shared-memory ring depth, 1..4
+  int terms = 1;   // split products: 1, 2 or 3
 };
 // 1 to 4 GEMMs in one launch.
 // test_timeout: a test of the error path (no TMA load is issued and the MMA thread's
 // wait gives up after 2 ms: the launch records a timeout in *status and writes nothing)
 void launch_umma_gemms(const UmmaGemm* g, int n, unsigned* status, cudaStream_t s, bool test_timeout = false);
-// Row r of dst (pitch terms*width): the bf16 split terms (hi), (hi | hi) or (hi | lo | hi) of
-// src[(r / rpn) * s_ns + s_off + (r % rpn) * s_rs + c], c < width (multiple of 4)
-void launch_rows_to_bf16(const float* src, __nv_bfloat16* dst, long rows, int width, int rpn, long s_ns, int s_off,
-                         int s_rs, int terms, cudaStream_t s);
 
 // k_md.cu
 void launch_wrap(int N, double3 box, int3 periodic, double* pos, cudaStream_t s);

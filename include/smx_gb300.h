@@ -180,8 +180,9 @@ int smx_run_stage(smx_engine* eng, const char* stage, int num_nodes, const int* 
  * first instruction; 0: plain launches; process-wide, read by later launches and graph
  * captures); BF16 form: "tc_terms" (1, 2 or 3 bf16 split products of the GEMMs: x_hi W_hi,
  * + x_hi W_lo, + x_lo W_hi; default 3; set before the first evaluation);
- * "test_gemm_timeout" (n in [0, 16]: a test of the timeout path, the next n tensor-core GEMM launches issue no load so that their bounded
- * wait gives up after 2 ms with nothing in flight; the call that ran them, or smx_sync
+ * "test_gemm_timeout" (n in [0, 16]: a test of the timeout path, the next n tensor-core
+ * GEMM launches issue no load so that their bounded wait gives up after 2 ms with
+ * nothing in flight; the call that ran them, or smx_sync
  * after a device-pointer call, returns SMX_ERR_TIMEOUT and the results are invalid).
  * No counterpart in the reference (its MACE object has no options). */
 int smx_set_option(smx_engine* eng, const char* key, long value);

@@ -140,7 +140,6 @@ struct AtomCursor {
 // |H1_adj| < 2^29 (5.4e8, far above any model's dE/dH1: O(1)); resolution 2^-34
 // (5.8e-11, far below the float32 rounding of a term).
 using fix64 = unsigned long long;
-constexpr double kFixInv = 1.0 / 17179869184.0;  // 2^-34
 // round(v 2^34) as an int64, round-to-nearest-even, for |v| < 2^29, in three exact FP32
 // steps and no conversion instruction (whose issue cost is several times these): v is
 // split as a 2^10 + b 2^-12 + c 2^-34 with a, b, c integers of at most 22 bits, each
@@ -162,8 +161,18 @@ __device__ __forceinline__ fix64 to_fixed(float v) {
          static_cast<fix64>(static_cast<long long>(c));
 }
 __device__ __forceinline__ void add_fixed(fix64* dst, float v) { atomicAdd(dst, to_fixed(v)); }
+// q 2^-34 as a float without float64 arithmetic (whose conversions run on this part's
+// slow float64 pipe): q = a 2^44 + b 2^22 + c with a signed, b and c in [0, 2^22), all
+// exact as floats; t = a 2^10 + b 2^-12 is exact when |q 2^-34| < 2^10 (then |a 2^22 + b|
+// < 2^22 + 1), so the last fmaf rounds once: the float nearest q 2^-34, as the float64
+// route gives; above 2^10, within one ulp of it.
 __device__ __forceinline__ float from_fixed(fix64 q) {
-  return static_cast<float>(static_cast<double>(static_cast<long long>(q)) * kFixInv);
+  const long long s = static_cast<long long>(q);
+  const float a = static_cast<float>(static_cast<int>(s >> 44));
+  const float b = static_cast<float>(static_cast<int>((s >> 22) & 0x3FFFFF));
+  const float c = static_cast<float>(static_cast<int>(s & 0x3FFFFF));
+  const float t = fmaf(a, 1024.0f, b * (1.0f / 4096.0f));
+  return fmaf(c, 1.0f / 17179869184.0f, t);
 }
 
 // Programmatic dependent launch.  The chained kernels of an evaluation and of an MD step

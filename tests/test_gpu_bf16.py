@@ -133,7 +133,7 @@ def test_bf16_form_force_error_vs_fp64_oracle(engine_lib, wide, terms):
 def test_autotuned_schedule_is_valid_and_exact(engine_lib, wide):
     """The autotuner only changes the N-tile width and the TMA ring depth: the K order of
     every accumulation is unchanged, so the GEMM outputs are bitwise those of the default
-    schedule (M0_adj to the float32 rounding of its atomically summed operand)."""
+    schedule (M0_adj too: its operand H1_adj is summed in fixed point)."""
     from symmetrix_gb300 import MACE
     path, species, nl = wide
     tuned = MACE(path, precision="bf16", keep_stages=True)
@@ -145,14 +145,13 @@ def test_autotuned_schedule_is_valid_and_exact(engine_lib, wide):
     print("tuned schedule:", sched)
     C = tuned.num_channels
     for g, v in sched.items():
-        assert v["stages"] in (2, 3, 4), g
-        assert v["NT"] in (C // 2, C, 2 * C), g
+        assert v["stages"] in (1, 2, 3, 4), g
+        assert v["NT"] in (0, C // 2, C, 2 * C), g  # 0: one N-tile of each GEMM's width
         assert v["us"] > 0, g
-    for s in ("H1", "A1", "Phi1_adj"):
+    for s in ("H1", "A1", "Phi1_adj", "M0_adj"):
         assert np.array_equal(tuned.stage(s), plain.stage(s)), s
     assert np.array_equal(tuned.node_energies, plain.node_energies)
-    # M0_adj's operand H1_adj is summed with float atomics in the layer-1 adjoint
-    assert _rel(tuned.stage("M0_adj"), plain.stage("M0_adj")) < 1e-5
+    assert np.array_equal(tuned.node_forces, plain.node_forces)
 
 
 def test_stage_rows_skipped_without_keep_stages(engine_lib, wide):

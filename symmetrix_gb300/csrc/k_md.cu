@@ -247,6 +247,7 @@ __global__ void k_edge_geometry_packed(int N, const int* __restrict__ first, con
   if (a >= N) return;
   const int e0 = first[a], e1 = first[a + 1];
   const double px = pos[3 * a], py = pos[3 * a + 1], pz = pos[3 * a + 2];
+  const float r_cut_f = static_cast<float>(r_cut);
   int count = 0;
   for (int base = e0; base < e1; base += 32) {
     const int e = base + lane;
@@ -259,8 +260,12 @@ __global__ void k_edge_geometry_packed(int N, const int* __restrict__ first, con
       dx = pos[3 * j] + sh.x * box.x - px;
       dy = pos[3 * j + 1] + sh.y * box.y - py;
       dz = pos[3 * j + 2] + sh.z * box.z - pz;
-      re = sqrt(dx * dx + dy * dy + dz * dz);
-      active = re < r_cut;
+      // the length in float32 (the evaluator reads r as a float; float64 arithmetic runs
+      // on this part's slow float64 pipe)
+      const float fx = static_cast<float>(dx), fy = static_cast<float>(dy), fz = static_cast<float>(dz);
+      const float rf = sqrtf(fmaf(fx, fx, fmaf(fy, fy, fz * fz)));
+      re = rf;
+      active = rf < r_cut_f;
     }
     const unsigned ball = __ballot_sync(0xffffffffu, active);
     const int q = e0 + count + __popc(ball & ((1u << lane) - 1u));
@@ -280,8 +285,9 @@ __global__ void k_edge_geometry_packed(int N, const int* __restrict__ first, con
 }
 
 // F_a = sum over a's packed edges q of (f[q'] - f[q]), q' the packed reverse edge
-// (pinv[rev[emap[q]]]; the reverse of an edge inside the cut-off is inside it too, its
-// length being computed from the negated vector); one warp per atom, fixed lane
+// pinv[rev[emap[q]]] (the reverse vector is the negated one up to the rounding of a
+// periodic image shift, so only an edge within rounding of r_cut, where the forces
+// vanish, can lack a packed reverse: it then adds nothing); one warp per atom, fixed lane
 // assignment and reduction tree (deterministic).  With dt > 0 also the second
 // velocity-Verlet half step of atom a, as k_vv_second.
 __global__ void k_atom_forces_packed(int N, const int* __restrict__ first, const int* __restrict__ last,

@@ -62,11 +62,20 @@ __global__ void k_cell_sort(int ncell, const int* __restrict__ cell_start, const
   }
 }
 
+// float32 copy of the positions for the neighbour search: the skin (1 A at the usual
+// settings) absorbs its rounding, and the float64 pipe is slow on this part
+__global__ void k_pos_to_float(int N, const double* __restrict__ pos, float4* __restrict__ posf) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= N) return;
+  posf[a] = make_float4(static_cast<float>(pos[3 * a]), static_cast<float>(pos[3 * a + 1]),
+                        static_cast<float>(pos[3 * a + 2]), 0.0f);
+}
+
 // Pass 0 counts, pass 1 fills.  Periodic images enter through the integer shift
 // (sx, sy, sz) in box lengths; the list holds pairs with r < rl, excluding i itself.
 template <bool FILL>
-__global__ void k_neigh_cells(const double* __restrict__ pos, const int* __restrict__ species, int N, double3 box,
-                              int3 nc, int3 periodic, double rl2, const int* __restrict__ cell,
+__global__ void k_neigh_cells(const float4* __restrict__ pos, const int* __restrict__ species, int N, float3 box,
+                              int3 nc, int3 periodic, float rl2, const int* __restrict__ cell,
                               const int* __restrict__ cell_start, const int* __restrict__ cell_atoms,
                               int* __restrict__ num_neigh, const int* __restrict__ first, int* __restrict__ nidx,
                               int* __restrict__ ntype_e, int* __restrict__ edge_i, char4* __restrict__ shift,
@@ -77,7 +86,7 @@ __global__ void k_neigh_cells(const double* __restrict__ pos, const int* __restr
   const int lane = threadIdx.x & 31;
   if (i >= N) return;
   const unsigned below = (1u << lane) - 1u;
-  const double xi = pos[3 * i], yi = pos[3 * i + 1], zi = pos[3 * i + 2];
+  const float4 pi = pos[i];
   const int ci = cell[i];
   const int cz = ci % nc.z, cy = (ci / nc.z) % nc.y, cx = ci / (nc.z * nc.y);
   long slot = FILL ? first[i] : 0;
@@ -94,7 +103,7 @@ __global__ void k_neigh_cells(const double* __restrict__ pos, const int* __restr
         if (qz < 0) { if (!periodic.z) continue; qz += nc.z; sz = -1; }
         if (qz >= nc.z) { if (!periodic.z) continue; qz -= nc.z; sz = 1; }
         const int q = (qx * nc.y + qy) * nc.z + qz;
-        const double ox = sx * box.x, oy = sy * box.y, oz = sz * box.z;
+        const float ox = sx * box.x, oy = sy * box.y, oz = sz * box.z;
         const int w1 = cell_start[q + 1];
         for (int w0 = cell_start[q]; w0 < w1; w0 += 32) {
           const int w = w0 + lane;
@@ -103,8 +112,9 @@ __global__ void k_neigh_cells(const double* __restrict__ pos, const int* __restr
           if (w < w1) {
             j = cell_atoms[w];
             if (!(j == i && sx == 0 && sy == 0 && sz == 0)) {
-              const double ddx = pos[3 * j] + ox - xi, ddy = pos[3 * j + 1] + oy - yi, ddz = pos[3 * j + 2] + oz - zi;
-              hit = ddx * ddx + ddy * ddy + ddz * ddz < rl2;
+              const float4 pj = pos[j];
+              const float ddx = pj.x + ox - pi.x, ddy = pj.y + oy - pi.y, ddz = pj.z + oz - pi.z;
+              hit = fmaf(ddx, ddx, fmaf(ddy, ddy, ddz * ddz)) < rl2;
             }
           }
           const unsigned ball = __ballot_sync(0xffffffffu, hit);
@@ -127,8 +137,8 @@ __global__ void k_neigh_cells(const double* __restrict__ pos, const int* __restr
 
 // Small or non-periodic systems: all pairs over the periodic images in range.
 template <bool FILL>
-__global__ void k_neigh_brute(const double* __restrict__ pos, const int* __restrict__ species, int N, double3 box,
-                              int3 nimg, double rl2, const int* __restrict__ seg_of, const int* __restrict__ seg_first,
+__global__ void k_neigh_brute(const float4* __restrict__ pos, const int* __restrict__ species, int N, float3 box,
+                              int3 nimg, float rl2, const int* __restrict__ seg_of, const int* __restrict__ seg_first,
                               int* __restrict__ num_neigh, const int* __restrict__ first, int* __restrict__ nidx,
                               int* __restrict__ ntype_e, int* __restrict__ edge_i, char4* __restrict__ shift,
                               long cap) {
@@ -137,7 +147,7 @@ __global__ void k_neigh_brute(const double* __restrict__ pos, const int* __restr
   const int lane = threadIdx.x & 31;
   if (i >= N) return;
   const unsigned below = (1u << lane) - 1u;
-  const double xi = pos[3 * i], yi = pos[3 * i + 1], zi = pos[3 * i + 2];
+  const float4 pi = pos[i];
   long slot = FILL ? first[i] : 0;
   // with segments (a batch of molecules), only atoms of i's own segment are candidates
   const int j0 = seg_of ? seg_first[seg_of[i]] : 0, j1 = seg_of ? seg_first[seg_of[i] + 1] : N;
@@ -149,9 +159,9 @@ __global__ void k_neigh_brute(const double* __restrict__ pos, const int* __restr
         for (int sz = -nimg.z; sz <= nimg.z; ++sz) {
           bool hit = false;
           if (live && !(j == i && sx == 0 && sy == 0 && sz == 0)) {
-            const double ddx = pos[3 * j] + sx * box.x - xi, ddy = pos[3 * j + 1] + sy * box.y - yi,
-                         ddz = pos[3 * j + 2] + sz * box.z - zi;
-            hit = ddx * ddx + ddy * ddy + ddz * ddz < rl2;
+            const float4 pj = pos[j];
+            const float ddx = pj.x + sx * box.x - pi.x, ddy = pj.y + sy * box.y - pi.y, ddz = pj.z + sz * box.z - pi.z;
+            hit = fmaf(ddx, ddx, fmaf(ddy, ddy, ddz * ddz)) < rl2;
           }
           const unsigned ball = __ballot_sync(0xffffffffu, hit);
           if (FILL && hit) {
@@ -447,12 +457,15 @@ void launch_permute_atoms(int N, const int* perm, const double* pos, const doubl
   k_permute_atoms<<<ceil_div(N, 256), 256, 0, s>>>(N, perm, pos, vel, F, inv_m, species, orig, tmp_d, tmp_i);
 }
 
-void launch_neigh_pass(bool fill, bool brute, const double* pos, const int* species, int N, double3 box, int3 nc,
-                       int3 periodic, int3 nimg, double rl, const int* cell, const int* cell_start,
-                       const int* cell_atoms, const int* seg_of, const int* seg_first, int* num_neigh,
-                       const int* first, int* nidx, int* ntype_e, int* edge_i, char4* shift, long cap,
+void launch_neigh_pass(bool fill, bool brute, const double* pos_d, float4* pos, const int* species, int N,
+                       double3 box_d, int3 nc, int3 periodic, int3 nimg, double rl, const int* cell,
+                       const int* cell_start, const int* cell_atoms, const int* seg_of, const int* seg_first,
+                       int* num_neigh, const int* first, int* nidx, int* ntype_e, int* edge_i, char4* shift, long cap,
                        cudaStream_t s) {
-  const double rl2 = rl * rl;
+  if (N <= 0) return;
+  if (!fill) k_pos_to_float<<<ceil_div(N, 256), 256, 0, s>>>(N, pos_d, pos);  // the fill pass reuses it
+  const float rl2 = static_cast<float>(rl * rl);
+  const float3 box = make_float3(static_cast<float>(box_d.x), static_cast<float>(box_d.y), static_cast<float>(box_d.z));
   const int g = ceil_div(N, 4);  // 128-thread blocks, one warp per atom
   if (brute || seg_of) {
     if (fill)

@@ -112,10 +112,12 @@ void launch_cell_list(const double* pos, int N, double3 box, int3 nc, int* cell,
 void launch_permute_atoms(int N, const int* perm, const double* pos, const double* vel, const double* F,
                           const double* inv_m, const int* species, const int* orig, double* tmp_d, int* tmp_i,
                           cudaStream_t s);
-void launch_neigh_pass(bool fill, bool brute, const double* pos, const int* species, int N, double3 box, int3 nc,
-                       int3 periodic, int3 nimg, double rl, const int* cell, const int* cell_start,
-                       const int* cell_atoms, const int* seg_of, const int* seg_first, int* num_neigh,
-                       const int* first, int* nidx, int* ntype_e, int* edge_i, char4* shift, long cap,
+// the two passes of the neighbour build (count, then fill); the count pass writes pos, the
+// float32 copy of pos_d that both search
+void launch_neigh_pass(bool fill, bool brute, const double* pos_d, float4* pos, const int* species, int N,
+                       double3 box_d, int3 nc, int3 periodic, int3 nimg, double rl, const int* cell,
+                       const int* cell_start, const int* cell_atoms, const int* seg_of, const int* seg_first,
+                       int* num_neigh, const int* first, int* nidx, int* ntype_e, int* edge_i, char4* shift, long cap,
                        cudaStream_t s);
 void launch_reverse_edges(long cap, int N, const int* first, const int* nidx, const int* edge_i, const char4* shift,
                           int* rev, cudaStream_t s);

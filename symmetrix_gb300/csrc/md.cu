@@ -25,6 +25,7 @@ struct NeighList {
   long capE = 0;
   int *cell = nullptr, *cell_count = nullptr, *cell_start = nullptr, *cell_fill = nullptr, *cell_atoms = nullptr;
   int* cell_tmp = nullptr;  // the binned atoms before each cell is sorted
+  float4* posf = nullptr;   // float32 positions of the neighbour search
   int *num_neigh = nullptr, *first = nullptr, *nidx = nullptr, *ntype_e = nullptr, *edge_i = nullptr, *rev = nullptr;
   char4* shift = nullptr;
   double *xyz = nullptr, *r = nullptr, *forces = nullptr;
@@ -38,12 +39,13 @@ struct NeighList {
   void release() {
     void* ps[] = {cell,  cell_count, cell_start, cell_fill, cell_atoms, num_neigh, first, nidx,  ntype_e,
                   edge_i, rev,       shift,      xyz,       r,          forces,    last,  emap,  pinv,
-                  nidx_p, ntype_p,   xyz_p,      r_p,       forces_p,   cell_tmp};
+                  nidx_p, ntype_p,   xyz_p,      r_p,       forces_p,   cell_tmp,  posf};
     for (void* p : ps)
       if (p) cudaFree(p);
     cell = cell_count = cell_start = cell_fill = cell_atoms = num_neigh = first = nidx = ntype_e = edge_i = rev = nullptr;
     last = emap = pinv = nidx_p = ntype_p = cell_tmp = nullptr;
     shift = nullptr;
+    posf = nullptr;
     xyz = r = forces = xyz_p = r_p = forces_p = nullptr;
     capN = ncell_cap = cell_atoms_cap = 0;
     capE = 0;
@@ -52,10 +54,12 @@ struct NeighList {
     if (N > capN) {
       for (int** p : {&cell, &num_neigh, &first, &last})
         if (*p) cudaFree(*p);
+      if (posf) cudaFree(posf);
       cell = dalloc<int>(N);
       num_neigh = dalloc<int>(N);
       first = dalloc<int>(N + 1);
       last = dalloc<int>(N);
+      posf = dalloc<float4>(N);
       capN = N;
       realloc_happened = true;
     }
@@ -129,16 +133,16 @@ struct NeighList {
     smx::launch_wrap(N, box, periodic, pos, s);
     if (!brute)
       smx::launch_cell_list(pos, N, box, nc, cell, cell_count, cell_start, cell_fill, cell_tmp, cell_atoms, s);
-    smx::launch_neigh_pass(false, brute, pos, species, N, box, nc, periodic, nimg, rl, cell, cell_start, cell_atoms,
-                           seg_of, seg_first, num_neigh, first, nidx, ntype_e, edge_i, shift, capE, s);
+    smx::launch_neigh_pass(false, brute, pos, posf, species, N, box, nc, periodic, nimg, rl, cell, cell_start,
+                           cell_atoms, seg_of, seg_first, num_neigh, first, nidx, ntype_e, edge_i, shift, capE, s);
     smx::launch_scan_first(num_neigh, N, first, s);
     int total = 0;
     check(cudaMemcpyAsync(&total, first + N, sizeof(int), cudaMemcpyDeviceToHost, s), "D2H");
     check(cudaStreamSynchronize(s), "neighbour count");
     E = total;
     reserve_edges(E);
-    smx::launch_neigh_pass(true, brute, pos, species, N, box, nc, periodic, nimg, rl, cell, cell_start, cell_atoms,
-                           seg_of, seg_first, num_neigh, first, nidx, ntype_e, edge_i, shift, capE, s);
+    smx::launch_neigh_pass(true, brute, pos, posf, species, N, box, nc, periodic, nimg, rl, cell, cell_start,
+                           cell_atoms, seg_of, seg_first, num_neigh, first, nidx, ntype_e, edge_i, shift, capE, s);
     smx::launch_reverse_edges(capE, N, first, nidx, edge_i, shift, rev, s);
   }
 };

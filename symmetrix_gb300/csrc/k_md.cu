@@ -12,6 +12,8 @@
 // the reverse-edge map, in float64.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "compsum.h"
 #include "device.cuh"
 #include "kernels.h"
@@ -79,9 +81,10 @@ __global__ void k_neigh_cells(const float4* __restrict__ pos, const int* __restr
                               const int* __restrict__ cell_start, const int* __restrict__ cell_atoms,
                               int* __restrict__ num_neigh, const int* __restrict__ first, int* __restrict__ nidx,
                               int* __restrict__ ntype_e, int* __restrict__ edge_i, char4* __restrict__ shift,
-                              long cap) {
+                              long cap, int* __restrict__ cellseg) {
   // one warp per atom: the lanes test 32 candidates of a cell at a time and a ballot
-  // keeps the hits in candidate order, so the list order is the sequential one
+  // keeps the hits in candidate order, so the list order is the sequential one; the fill
+  // pass records where each of the 27 neighbour cells' hits start (cellseg, optional)
   const int i = static_cast<int>((static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
   if (i >= N) return;
@@ -99,6 +102,8 @@ __global__ void k_neigh_cells(const float4* __restrict__ pos, const int* __restr
       if (qy < 0) { if (!periodic.y) continue; qy += nc.y; sy = -1; }
       if (qy >= nc.y) { if (!periodic.y) continue; qy -= nc.y; sy = 1; }
       for (int dz = -1; dz <= 1; ++dz) {
+        if (FILL && cellseg && lane == 0)
+          cellseg[28L * i + ((dx + 1) * 3 + (dy + 1)) * 3 + (dz + 1)] = static_cast<int>(slot);
         int qz = cz + dz, sz = 0;
         if (qz < 0) { if (!periodic.z) continue; qz += nc.z; sz = -1; }
         if (qz >= nc.z) { if (!periodic.z) continue; qz -= nc.z; sz = 1; }
@@ -133,6 +138,7 @@ __global__ void k_neigh_cells(const float4* __restrict__ pos, const int* __restr
     }
   }
   if (!FILL && lane == 0) num_neigh[i] = static_cast<int>(slot);
+  if (FILL && cellseg && lane == 0) cellseg[28L * i + 27] = static_cast<int>(slot);
 }
 
 // Small or non-periodic systems: all pairs over the periodic images in range.
@@ -216,6 +222,46 @@ __global__ void k_reverse_edges(int N, const int* __restrict__ first, const int*
     }
     if (lane == 0) rev[e] = found;
   }
+}
+
+// rev[e] for a cell-list build: the reverse of e = (i -> j, shift) lies in j's segment for
+// the neighbour cell at the negated cell offset (cellseg), a few entries, scanned in order
+// (the first match, as k_reverse_edges finds).  One thread per edge.
+__global__ void k_reverse_edges_cells(long cap, int N, const int* __restrict__ first, const int* __restrict__ nidx,
+                                      const int* __restrict__ edge_i, const char4* __restrict__ shift,
+                                      const int* __restrict__ cell, int3 nc, const int* __restrict__ cellseg,
+                                      int* __restrict__ rev) {
+  const long E = first[N];
+  for (long e = blockIdx.x * static_cast<long>(blockDim.x) + threadIdx.x; e < E && e < cap;
+       e += static_cast<long>(gridDim.x) * blockDim.x) {
+    const int i = edge_i[e], j = nidx[e];
+    const char4 sh = shift[e];
+    const int ci = cell[i], cj = cell[j];
+    // offset of j's cell from i's in i's search: cell(j) + shift * nc - cell(i), each in [-1, 1]
+    const int ox = (cj / (nc.z * nc.y)) + sh.x * nc.x - ci / (nc.z * nc.y);
+    const int oy = (cj / nc.z) % nc.y + sh.y * nc.y - (ci / nc.z) % nc.y;
+    const int oz = cj % nc.z + sh.z * nc.z - ci % nc.z;
+    int found = -1;
+    if (ox >= -1 && ox <= 1 && oy >= -1 && oy <= 1 && oz >= -1 && oz <= 1) {
+      const int k = ((1 - ox) * 3 + (1 - oy)) * 3 + (1 - oz);  // in j's search the offset is negated
+      const int w1 = cellseg[28L * j + k + 1];
+      for (int w = cellseg[28L * j + k]; w < w1; ++w) {
+        const char4 t = shift[w];
+        if (nidx[w] == i && t.x == -sh.x && t.y == -sh.y && t.z == -sh.z) {
+          found = w;
+          break;
+        }
+      }
+    }
+    rev[e] = found;
+  }
+}
+
+// *dst = *src into mapped host memory (a host polling dst sees it without a copy engine
+// transfer or a stream synchronisation)
+__global__ void k_publish_int(const int* __restrict__ src, int* dst) {
+  *reinterpret_cast<volatile int*>(dst) = *src;
+  __threadfence_system();
 }
 
 // xyz_e = x_j + shift_e * box - x_i, r_e = |xyz_e|
@@ -461,7 +507,7 @@ void launch_neigh_pass(bool fill, bool brute, const double* pos_d, float4* pos, 
                        double3 box_d, int3 nc, int3 periodic, int3 nimg, double rl, const int* cell,
                        const int* cell_start, const int* cell_atoms, const int* seg_of, const int* seg_first,
                        int* num_neigh, const int* first, int* nidx, int* ntype_e, int* edge_i, char4* shift, long cap,
-                       cudaStream_t s) {
+                       cudaStream_t s, int* cellseg) {
   if (N <= 0) return;
   if (!fill) k_pos_to_float<<<ceil_div(N, 256), 256, 0, s>>>(N, pos_d, pos);  // the fill pass reuses it
   const float rl2 = static_cast<float>(rl * rl);
@@ -477,10 +523,10 @@ void launch_neigh_pass(bool fill, bool brute, const double* pos_d, float4* pos, 
   } else {
     if (fill)
       k_neigh_cells<true><<<g, 128, 0, s>>>(pos, species, N, box, nc, periodic, rl2, cell, cell_start, cell_atoms,
-                                            num_neigh, first, nidx, ntype_e, edge_i, shift, cap);
+                                            num_neigh, first, nidx, ntype_e, edge_i, shift, cap, cellseg);
     else
       k_neigh_cells<false><<<g, 128, 0, s>>>(pos, species, N, box, nc, periodic, rl2, cell, cell_start, cell_atoms,
-                                             num_neigh, first, nidx, ntype_e, edge_i, shift, cap);
+                                             num_neigh, first, nidx, ntype_e, edge_i, shift, cap, nullptr);
   }
 }
 
@@ -491,6 +537,16 @@ void launch_wrap(int N, double3 box, int3 periodic, double* pos, cudaStream_t s)
 void launch_reverse_edges(long cap, int N, const int* first, const int* nidx, const int* edge_i, const char4* shift,
                           int* rev, cudaStream_t s) {
   if (cap > 0 && N > 0) k_reverse_edges<<<N, 128, 0, s>>>(N, first, nidx, shift, rev);  // block per atom
+}
+
+void launch_publish_int(const int* src, int* dst, cudaStream_t s) { k_publish_int<<<1, 1, 0, s>>>(src, dst); }
+
+void launch_reverse_edges_cells(long cap, int N, const int* first, const int* nidx, const int* edge_i,
+                                const char4* shift, const int* cell, int3 nc, const int* cellseg, int* rev,
+                                cudaStream_t s) {
+  if (cap > 0 && N > 0)
+    k_reverse_edges_cells<<<static_cast<int>(std::min<long>(ceil_div(cap, 256), 152L * 16)), 256, 0, s>>>(
+        cap, N, first, nidx, edge_i, shift, cell, nc, cellseg, rev);
 }
 
 void launch_edge_geometry(long cap, int N, const int* first, const double* pos, double3 box, const int* nidx,

@@ -118,7 +118,14 @@ void launch_neigh_pass(bool fill, bool brute, const double* pos_d, float4* pos, 
                        double3 box_d, int3 nc, int3 periodic, int3 nimg, double rl, const int* cell,
                        const int* cell_start, const int* cell_atoms, const int* seg_of, const int* seg_first,
                        int* num_neigh, const int* first, int* nidx, int* ntype_e, int* edge_i, char4* shift, long cap,
-                       cudaStream_t s);
+                       cudaStream_t s, int* cellseg = nullptr);
+// *dst = *src, dst a device pointer of mapped host memory
+void launch_publish_int(const int* src, int* dst, cudaStream_t s);
+// rev[e] from the cell-list fill pass's per-atom segments (cellseg [N][28]: where each of
+// the 27 neighbour cells' hits start in an atom's list, then its end)
+void launch_reverse_edges_cells(long cap, int N, const int* first, const int* nidx, const int* edge_i,
+                                const char4* shift, const int* cell, int3 nc, const int* cellseg, int* rev,
+                                cudaStream_t s);
 void launch_reverse_edges(long cap, int N, const int* first, const int* nidx, const int* edge_i, const char4* shift,
                           int* rev, cudaStream_t s);
 void launch_edge_geometry(long cap, int N, const int* first, const double* pos, double3 box, const int* nidx,

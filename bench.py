@@ -580,15 +580,15 @@ def gpu_arm(args, rank, world, local_rank):
                      "gbs": costs[n_][1] / (a[n_] / 1e3) / 1e9} for n_ in a}
 
     # kernels per MD step of the BF16 form: vv_first, edge geometry with the in-cut-off packing,
-    # the scatter of the packed forces, atom_forces, vv_second and 11
-    # evaluation kernels (layer0_fwd, layer1_fwd, node_tail, layer1_rev, contract0_rev, layer0_rev,
-    # four grouped tcgen05 GEMM launches: H1, A1 (all l), Phi1_adj (all l), M0_adj, and the
-    # H1_adj rows' conversion to the M0_adj GEMM's operand), one more when the centre atoms
-    # are species-sorted; plus per rebuild: wrap, 4 cell-list kernels, 2 neighbour passes,
-    # scan, reverse map
+    # the atomic forces with the second half-kick, and 11 evaluation kernels (layer0_fwd,
+    # layer1_fwd, node_tail, layer1_rev, contract0_rev, layer0_rev, four grouped tcgen05 GEMM
+    # launches: H1, A1 (all l), Phi1_adj (all l), M0_adj, and the H1_adj rows' conversion to
+    # the M0_adj GEMM's operand), one more when the centre atoms are species-sorted; plus per
+    # rebuild: wrap, 4 cell-list kernels, the float copy of the positions, 2 neighbour passes,
+    # scan, the edge count's publication, reverse map
     rebuilds = (args.warmup + args.steps + 9) // 10 - (args.warmup + 9) // 10
-    per_step = 5 + 11 + (1 if eng.get_option("species_order") == 1 else 0)
-    launches = per_step * args.steps + 9 * rebuilds
+    per_step = 3 + 11 + (1 if eng.get_option("species_order") == 1 else 0)
+    launches = per_step * args.steps + 11 * rebuilds
     fp = forms["fp32"]
     line = {
         "metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,

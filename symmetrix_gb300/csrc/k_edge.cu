@@ -171,7 +171,8 @@ __device__ __forceinline__ void layer0_fwd_atom(const DevModel& m, const EdgeIn&
 #pragma unroll
     for (int q = 0; q < 16; ++q) {
       const float2 o = *reinterpret_cast<const float2*>(sA + q * C + kc);
-      const float2 v = make_float2((acc[q].x + o.x) / S, (acc[q].y + o.y) / S);
+      float2 v = make_float2(acc[q].x + o.x, acc[q].y + o.y);
+      if (S != 1.0f) v = make_float2(v.x / S, v.y / S);  // (no division sequence without the scaling)
       *reinterpret_cast<float2*>(sA + q * C + kc) = v;
       *reinterpret_cast<float2*>(A0 + (static_cast<size_t>(i) * 16 + q) * C + kc) = v;
     }

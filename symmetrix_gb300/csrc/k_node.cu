@@ -227,9 +227,11 @@ __device__ __forceinline__ void node_tail_atom(const DevModel& m, const int* __r
     dot = block_sum(dot);
     if (k == 0) m.dens_c[1][i] = dot / S1;
   }
+  // A1_adj = dM1/dA1 * M1_adj (/ S1 when density-normalised; no division sequence otherwise)
+  auto a1adj = [&](int q) { return dens ? sG[q * C + k] * m1a / S1 : sG[q * C + k] * m1a; };
   if (A1_adj)  // nullptr: only the split rows below are consumed
 #pragma unroll
-    for (int q = 0; q < 16; ++q) A1_adj[(static_cast<size_t>(i) * 16 + q) * C + k] = sG[q * C + k] * m1a / S1;
+    for (int q = 0; q < 16; ++q) A1_adj[(static_cast<size_t>(i) * 16 + q) * C + k] = a1adj(q);
   if (m.op_a1adj) {  // BF16 form: the Phi1_adj GEMM's split operand, rows (node, m) per l
     const int T = m.tc_terms, XT = split_xterms(T);
     for (int l = 0; l < 4; ++l) {
@@ -237,7 +239,7 @@ __device__ __forceinline__ void node_tail_atom(const DevModel& m, const int* __r
       for (int mm = 0; mm < 2 * l + 1; ++mm) {
         __nv_bfloat16* row = m.op_a1adj + static_cast<size_t>(XT) * N * l * l * C +
                              (static_cast<size_t>(i) * (2 * l + 1) + mm) * XT * C;
-        write_split(row, C, T, k, sG[(l * l + mm) * C + k] * m1a / S1);
+        write_split(row, C, T, k, a1adj(l * l + mm));
       }
     }
   }

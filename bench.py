@@ -585,10 +585,10 @@ def gpu_arm(args, rank, world, local_rank):
     # launches: H1, A1 (all l), Phi1_adj (all l), M0_adj, and the H1_adj rows' conversion to
     # the M0_adj GEMM's operand), one more when the centre atoms are species-sorted; plus per
     # rebuild: wrap, 4 cell-list kernels, the float copy of the positions, 2 neighbour passes,
-    # scan, the edge count's publication, reverse map
+    # scan, reverse map
     rebuilds = (args.warmup + args.steps + 9) // 10 - (args.warmup + 9) // 10
     per_step = 3 + 11 + (1 if eng.get_option("species_order") == 1 else 0)
-    launches = per_step * args.steps + 11 * rebuilds
+    launches = per_step * args.steps + 10 * rebuilds
     fp = forms["fp32"]
     line = {
         "metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,

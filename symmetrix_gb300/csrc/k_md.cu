@@ -257,13 +257,6 @@ __global__ void k_reverse_edges_cells(long cap, int N, const int* __restrict__ f
   }
 }
 
-// *dst = *src into mapped host memory (a host polling dst sees it without a copy engine
-// transfer or a stream synchronisation)
-__global__ void k_publish_int(const int* __restrict__ src, int* dst) {
-  *reinterpret_cast<volatile int*>(dst) = *src;
-  __threadfence_system();
-}
-
 // xyz_e = x_j + shift_e * box - x_i, r_e = |xyz_e|
 __global__ void k_edge_geometry(long cap, int N, const int* __restrict__ first, const double* __restrict__ pos,
                                 double3 box, const int* __restrict__ nidx, const int* __restrict__ edge_i,
@@ -538,8 +531,6 @@ void launch_reverse_edges(long cap, int N, const int* first, const int* nidx, co
                           int* rev, cudaStream_t s) {
   if (cap > 0 && N > 0) k_reverse_edges<<<N, 128, 0, s>>>(N, first, nidx, shift, rev);  // block per atom
 }
-
-void launch_publish_int(const int* src, int* dst, cudaStream_t s) { k_publish_int<<<1, 1, 0, s>>>(src, dst); }
 
 void launch_reverse_edges_cells(long cap, int N, const int* first, const int* nidx, const int* edge_i,
                                 const char4* shift, const int* cell, int3 nc, const int* cellseg, int* rev,

@@ -119,8 +119,6 @@ void launch_neigh_pass(bool fill, bool brute, const double* pos_d, float4* pos, 
                        const int* cell_start, const int* cell_atoms, const int* seg_of, const int* seg_first,
                        int* num_neigh, const int* first, int* nidx, int* ntype_e, int* edge_i, char4* shift, long cap,
                        cudaStream_t s, int* cellseg = nullptr);
-// *dst = *src, dst a device pointer of mapped host memory
-void launch_publish_int(const int* src, int* dst, cudaStream_t s);
 // rev[e] from the cell-list fill pass's per-atom segments (cellseg [N][28]: where each of
 // the 27 neighbour cells' hits start in an atom's list, then its end)
 void launch_reverse_edges_cells(long cap, int N, const int* first, const int* nidx, const int* edge_i,

@@ -8,7 +8,6 @@
 // pair_symmetrix/test/test_pair_symmetrix_mace.py:253).
 #include <cuda_runtime.h>
 
-#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -28,8 +27,6 @@ struct NeighList {
   int* cell_tmp = nullptr;  // the binned atoms before each cell is sorted
   float4* posf = nullptr;   // float32 positions of the neighbour search
   int* cellseg = nullptr;   // [N][28]: start of each of the 27 neighbour cells' segment in an atom's list, end
-  int* count_h = nullptr;   // mapped pinned host word (count_d on the device): the edge count of a build
-  int* count_d = nullptr;
   int *num_neigh = nullptr, *first = nullptr, *nidx = nullptr, *ntype_e = nullptr, *edge_i = nullptr, *rev = nullptr;
   char4* shift = nullptr;
   double *xyz = nullptr, *r = nullptr, *forces = nullptr;
@@ -51,8 +48,6 @@ struct NeighList {
     shift = nullptr;
     posf = nullptr;
     cellseg = nullptr;
-    if (count_h) cudaFreeHost(count_h);
-    count_h = count_d = nullptr;
     xyz = r = forces = xyz_p = r_p = forces_p = nullptr;
     capN = ncell_cap = cell_atoms_cap = 0;
     capE = 0;
@@ -145,22 +140,10 @@ struct NeighList {
     smx::launch_neigh_pass(false, brute, pos, posf, species, N, box, nc, periodic, nimg, rl, cell, cell_start,
                            cell_atoms, seg_of, seg_first, num_neigh, first, nidx, ntype_e, edge_i, shift, capE, s);
     smx::launch_scan_first(num_neigh, N, first, s);
-    // The edge count sizes the fill pass.  A one-thread kernel stores it in mapped host
-    // memory, which the host polls (a device-to-host copy and a stream synchronisation
-    // took ~50 us per build); the poll gives up after a second and the synchronisation
-    // that follows reports any device error.
-    if (!count_h) {
-      check(cudaHostAlloc(reinterpret_cast<void**>(&count_h), sizeof(int), cudaHostAllocMapped), "cudaHostAlloc");
-      check(cudaHostGetDevicePointer(reinterpret_cast<void**>(&count_d), count_h, 0), "cudaHostGetDevicePointer");
-    }
-    volatile int* cnt = count_h;
-    *cnt = -1;
-    smx::launch_publish_int(first + N, count_d, s);
-    const auto t0 = std::chrono::steady_clock::now();
-    while (*cnt < 0 && std::chrono::steady_clock::now() - t0 < std::chrono::seconds(1)) {
-    }
+    int total = 0;
+    check(cudaMemcpyAsync(&total, first + N, sizeof(int), cudaMemcpyDeviceToHost, s), "D2H");
     check(cudaStreamSynchronize(s), "neighbour count");
-    E = *cnt;
+    E = total;
     reserve_edges(E);
     int* seg = brute ? nullptr : cellseg;
     smx::launch_neigh_pass(true, brute, pos, posf, species, N, box, nc, periodic, nimg, rl, cell, cell_start,

@@ -458,6 +458,16 @@ struct smx_engine {
     tc_tuned_us[gid] = best * 1000.0f / 3.0f;
   }
 
+  // The M0_adj GEMM (L_max 1) as two segments, one per L block: X rows grouped by L
+  // (lgroup_row), B = the block's C x C weights, output rows (node, LM) of Y [N][4][C].
+  void lblock_gemms(const __nv_bfloat16* X, const __nv_bfloat16* W, float* Y, int N, smx::UmmaGemm* g) const {
+    const int C = dm.C, T = tc_terms;
+    const long XT = smx::split_xterms(T), WT = smx::split_wterms(T), ns = static_cast<long>(dm.nLM) * C;
+    g[0] = smx::UmmaGemm{X, N, C, W, C, C, smx::UmmaOut{Y, N, 1, ns, 0, 0, 0}};
+    g[1] = smx::UmmaGemm{X + XT * N * C, 3L * N, C, W + WT * C * C, C, C, smx::UmmaOut{Y, 3L * N, 3, ns, C, C, 0}};
+    g[0].terms = g[1].terms = T;
+  }
+
   // launch one GEMM group with its tuned schedule (tuning it first if due)
   void run_tc(int gid, smx::UmmaGemm* g, int ng, bool tile_n, cudaStream_t s) {
     if (ng == 0) return;
@@ -649,7 +659,7 @@ struct smx_engine {
     }
     smx::launch_rows_to_fixed(H1_adj, H1_adj_fx, nh, zero_h1adj, s);
     smx::launch_layer1_rev(m, in, H1, Phi1_adj, H1_adj_fx, f1, s);
-    smx::launch_fixed_rows(H1_adj_fx, H1_adj, nullptr, in.N * static_cast<long>(dm.nLM), dm.C, 1, s);
+    smx::launch_fixed_rows(H1_adj_fx, H1_adj, nullptr, in.N * static_cast<long>(dm.nLM), dm.C, 1, dm.nLM, s);
     smx::launch_forces_from_f1(forces, f1, dm.f1_stride, dm.l2_split, 3 * E, zero_dxyz, s);
   }
 
@@ -767,13 +777,12 @@ struct smx_engine {
     smx::launch_layer1_rev(dm, in, H1, Phi1_adj, H1_adj_fx, f1, s);
     mark(7, s);
     // the float H1_adj rows (and the BF16 form's split operand) from the fixed-point sums
-    smx::launch_fixed_rows(H1_adj_fx, H1_adj, tc_H1 ? H1adj_bf : nullptr, static_cast<long>(N) * dm.nLM, C, T, s);
+    smx::launch_fixed_rows(H1_adj_fx, H1_adj, tc_H1 ? H1adj_bf : nullptr, static_cast<long>(N) * dm.nLM, C, T, dm.nLM,
+                           s);
     if (tc_H1) {  // M0_adj = H1_adj @ H1W[L]^T  (mace.cpp:425-451), tensor cores
-      smx::UmmaGemm g{H1adj_bf, static_cast<long>(N) * dm.nLM, C, W_M0adj, 2 * C, C,
-                       smx::UmmaOut{M0_adj, static_cast<long>(N) * dm.nLM, dm.nLM, static_cast<long>(dm.nLM) * C, 0,
-                                    C, 1}};
-      g.terms = T;
-      run_tc(3, &g, 1, false, s);
+      smx::UmmaGemm g[2];
+      lblock_gemms(H1adj_bf, W_M0adj, M0_adj, N, g);
+      run_tc(3, g, 2, false, s);
     } else {  // M0_adj = H1_adj @ H1W[L]^T  (mace.cpp:425-451)
       smx::GemmBatch b{};
       for (int L = 0; L <= dm.L_max; ++L)

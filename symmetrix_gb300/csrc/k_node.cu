@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <stdexcept>
 
 #include "device.cuh"
 #include "kernels.h"
@@ -290,7 +291,7 @@ void node_tail_residency(const DevModel& m, int* per_sm) {
 
 // H1_adj from its fixed-point accumulator: float rows for the SIMT GEMM and the stage
 // reads, and in the BF16 form the M0_adj GEMM's split operand rows (write_split with
-// `terms` products: row pitch split_xterms(terms) * C).
+// `terms` products: row pitch split_xterms(terms) * C; rows grouped by L, lgroup_row).
 __global__ void k_fixed_rows(const fix64* __restrict__ src, float* __restrict__ dst, __nv_bfloat16* __restrict__ bf,
                              long rows, int C, int terms) {
   pdl_begin();
@@ -299,14 +300,17 @@ __global__ void k_fixed_rows(const fix64* __restrict__ src, float* __restrict__ 
        t += static_cast<long>(gridDim.x) * blockDim.x) {
     const float v = from_fixed(src[t]);
     dst[t] = v;
-    if (bf) {
+    if (bf) {  // (L_max 1: nLM = 4)
       const long r = t / C;
-      write_split(bf + r * split_xterms(terms) * C, C, terms, static_cast<int>(t - r * C), v);
+      write_split(bf + lgroup_row(rows >> 2, r >> 2, static_cast<int>(r & 3)) * split_xterms(terms) * C, C, terms,
+                  static_cast<int>(t - r * C), v);
     }
   }
 }
 
-void launch_fixed_rows(const fix64* src, float* dst, __nv_bfloat16* bf, long rows, int C, int terms, cudaStream_t s) {
+void launch_fixed_rows(const fix64* src, float* dst, __nv_bfloat16* bf, long rows, int C, int terms, int nLM,
+                       cudaStream_t s) {
+  if (bf && nLM != 4) throw std::invalid_argument("the split H1_adj rows exist for L_max 1 only");
   if (rows <= 0) return;
   const long n = rows * C;
   const int blocks = static_cast<int>(std::min<long>((n + 255) / 256, 152L * 16));

@@ -51,9 +51,11 @@ void launch_gemm(const GemmBatch& b, cudaStream_t s);
 void launch_node_tail(const DevModel& m, const int* node_type, int N, float* A1, const float* H1, float* M1,
                       float* H2, float* A1_adj, fix64* H1_adj, float* M1_adj, float* H2_adj, const float* zbl_e,
                       double* energies, cudaStream_t s);
-// dst[rows][C] = the fixed-point rows src as float; bf (optional): their bf16 split terms
-// for a GEMM with `terms` products (write_split), row pitch split_xterms(terms) * C
-void launch_fixed_rows(const fix64* src, float* dst, __nv_bfloat16* bf, long rows, int C, int terms, cudaStream_t s);
+// dst[rows][C] = the fixed-point rows src ([N][nLM][C]) as float; bf (optional, L_max 1):
+// their bf16 split terms for a GEMM with `terms` products (write_split), row pitch
+// split_xterms(terms) * C, rows grouped by L (lgroup_row)
+void launch_fixed_rows(const fix64* src, float* dst, __nv_bfloat16* bf, long rows, int C, int terms, int nLM,
+                       cudaStream_t s);
 // single-stage calls: dst = fixed-point copy of src (zero: dst = 0); forces = (zero ? 0 :
 // forces) - the sum of the nslices f1 slices (stride apart), n = 3 * edges
 void launch_rows_to_fixed(const float* src, fix64* dst, long n, bool zero, cudaStream_t s);

@@ -234,14 +234,12 @@ __device__ __forceinline__ void node_tail_atom(const DevModel& m, const int* __r
 #pragma unroll
     for (int q = 0; q < 16; ++q) A1_adj[(static_cast<size_t>(i) * 16 + q) * C + k] = a1adj(q);
   if (m.op_a1adj) {  // BF16 form: the Phi1_adj GEMM's split operand, rows (node, m) per l
-    const int T = m.tc_terms, XT = split_xterms(T);
+    const int T = m.tc_terms;
+    const size_t pitch = static_cast<size_t>(split_xterms(T)) * C;
     for (int l = 0; l < 4; ++l) {
       if (m.num_e[l] == 0) continue;
-      for (int mm = 0; mm < 2 * l + 1; ++mm) {
-        __nv_bfloat16* row = m.op_a1adj + static_cast<size_t>(XT) * N * l * l * C +
-                             (static_cast<size_t>(i) * (2 * l + 1) + mm) * XT * C;
-        write_split(row, C, T, k, a1adj(l * l + mm));
-      }
+      __nv_bfloat16* row = m.op_a1adj + pitch * (static_cast<size_t>(N) * l * l + static_cast<size_t>(i) * (2 * l + 1));
+      for (int mm = 0; mm < 2 * l + 1; ++mm, row += pitch) write_split(row, C, T, k, a1adj(l * l + mm));
     }
   }
   // H1_adj in fixed point: the layer-1 adjoint adds its edge terms to these rows
@@ -254,7 +252,9 @@ __device__ __forceinline__ void node_tail_atom(const DevModel& m, const int* __r
 }
 
 // at most 64 registers: eight 128-thread blocks per SM instead of six at 80 (0.129 -> 0.124 ms
-// on the 4096-atom workload; 12 bytes of spills)
+// on the 4096-atom workload; 12 bytes of spills).  At this cap the register allocation of
+// the whole kernel is sensitive to the split-row block: its row pointer is bumped row by
+// row (computing each row's address afresh took 16/24 bytes of spills and 0.010 ms).
 template <bool P>
 __global__ void __launch_bounds__(256, 4) k_node_tail(DevModel m, const int* __restrict__ ntype, float* __restrict__ A1,
                                                    const float* __restrict__ H1, float* __restrict__ M1o,

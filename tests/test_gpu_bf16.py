@@ -97,6 +97,27 @@ def test_tensor_core_gemms_are_exact_bf16_products(engine_lib, wide, terms):
         print(f"terms={terms} A1 l={l} rel", _rel(got, ref))
         assert _rel(got, ref) < 2e-5
         off += (2 * l + 1) * n_e[l]
+    # the adjoint GEMMs: Phi1_adj[i, (l, m, e), :] = A1_adj[i, l^2 + m, :] . A1W[l][e]^T, and
+    # M0_adj[i, lm, :] = H1_adj[i, lm, :] . H1W[L(lm)]^T (one segment per L block)
+    A1_adj = m.stage("A1_adj").reshape(N, 16, C)
+    Phi1_adj = m.stage("Phi1_adj").reshape(N, -1, C)
+    off = 0
+    for l in range(4):
+        if n_e[l] == 0:
+            continue
+        Wl = np.asarray(d["A1_weights"][l], dtype=np.float64).reshape(n_e[l] * C, C).astype(np.float32)
+        ref = split_product(A1_adj[:, l * l:(l + 1) ** 2], Wl.T, terms)
+        got = Phi1_adj[:, off:off + (2 * l + 1) * n_e[l]].reshape(N, 2 * l + 1, n_e[l] * C)
+        print(f"terms={terms} Phi1_adj l={l} rel", _rel(got, ref))
+        assert _rel(got, ref) < 2e-5
+        off += (2 * l + 1) * n_e[l]
+    H1_adj = m.stage("H1_adj").reshape(N, 4, C)
+    M0_adj = m.stage("M0_adj").reshape(N, 4, C)
+    ref = np.empty_like(M0_adj)
+    ref[:, 0] = split_product(H1_adj[:, 0], W[0].T.astype(np.float32), terms)
+    ref[:, 1:] = split_product(H1_adj[:, 1:], W[1].T.astype(np.float32), terms)
+    print(f"terms={terms} M0_adj rel", _rel(M0_adj, ref))
+    assert _rel(M0_adj, ref) < 2e-5
 
 
 def test_adjoint_gemms_close_to_plain_form(engine_lib, wide):

@@ -378,36 +378,43 @@ struct Oracle {
   }
 
   // ----- forward + reverse (mace.cpp:17-64) -----
+  // N1 < N: layer 0 over all N nodes, layer 1, the readouts and ZBL over the first N1
+  // only, as the pair style's no-MPI-message-passing mode calls the stages
+  // (pair_symmetrix/pair_symmetrix_mace.cpp:672-698): the trailing N - N1 nodes are a
+  // halo whose H1 rows the first N1 nodes' layer-1 edges read; node_energies has N1
+  // entries and node_forces one triple per edge of all N nodes.
   void compute(int N, const int* ntype, const int* nneigh, const int* nidx, const int* ntypes_e, long E,
-               const double* xyz, const double* r) {
+               const double* xyz, const double* r, int N1 = -1) {
+    if (N1 < 0) N1 = N;
+    if (N1 > N) throw std::invalid_argument("more layer-1 nodes than nodes");
     long check = 0;
     for (int i = 0; i < N; ++i) check += nneigh[i];
     if (check != E) throw std::invalid_argument("sum(num_neigh) != number of edges");
-    for (long e = 0; e < E; ++e)
-      if (nidx[e] < 0 || nidx[e] >= N) throw std::invalid_argument("neighbor index out of range");
     eoff.assign(N + 1, 0);
     for (int i = 0; i < N; ++i) eoff[i + 1] = eoff[i] + nneigh[i];
-    node_energies.assign(N, 0.0);
+    for (long e = 0; e < eoff[N1]; ++e)  // the halo's own edges index nothing
+      if (nidx[e] < 0 || nidx[e] >= N) throw std::invalid_argument("neighbor index out of range");
+    node_energies.assign(N1, 0.0);
     node_forces.assign(3 * E, 0.0);
-    if (has_zbl) zbl_stage(N, ntype, ntypes_e, xyz, r);
+    if (has_zbl) zbl_stage(N1, ntype, ntypes_e, xyz, r);
     stage_Y(N, E, xyz);
     stage_R(N, ntype, ntypes_e, r, spl0, R0, R0_deriv);
     stage_A0(N, ntype, ntypes_e, r);
     scale_fwd(N, ntype, ntypes_e, r, A0_scaled, A0s, A0);
     stage_M0(N, ntype);
     stage_H1(N);
-    stage_R(N, ntype, ntypes_e, r, spl1, R1, R1_deriv);
-    stage_Phi1(N, ntype, nidx, ntypes_e, r);
-    stage_A1(N);
-    scale_fwd(N, ntype, ntypes_e, r, A1_scaled, A1s, A1);
-    stage_M1(N, ntype);
-    stage_H2(N, ntype);
-    stage_readouts(N, ntype);
-    reverse_H2(N, ntype);
-    reverse_M1(N);
-    scale_rev(N, ntype, ntypes_e, xyz, r, A1_scaled, A1s, A1, A1_adj);
-    reverse_A1(N);
-    reverse_Phi1(N, ntype, nidx, ntypes_e, xyz, r);
+    stage_R(N1, ntype, ntypes_e, r, spl1, R1, R1_deriv);
+    stage_Phi1(N1, ntype, nidx, ntypes_e, r);
+    stage_A1(N1);
+    scale_fwd(N1, ntype, ntypes_e, r, A1_scaled, A1s, A1);
+    stage_M1(N1, ntype);
+    stage_H2(N1, ntype);
+    stage_readouts(N1, ntype);
+    reverse_H2(N1, ntype);
+    reverse_M1(N1);
+    scale_rev(N1, ntype, ntypes_e, xyz, r, A1_scaled, A1s, A1, A1_adj);
+    reverse_A1(N1);
+    reverse_Phi1(N1, ntype, nidx, ntypes_e, xyz, r);
     reverse_H1(N);
     reverse_M0(N);
     scale_rev(N, ntype, ntypes_e, xyz, r, A0_scaled, A0s, A0, A0_adj);
@@ -656,20 +663,22 @@ struct Oracle {
         }
       }
     });
-    // incoming edges of every node, ascending, and each edge's source node
-    std::vector<long> in_off(N + 1, 0), in_e(E);
+    // incoming edges of every node with an H1 row (the halo's too), ascending, and each
+    // edge's source node
+    const int NH = static_cast<int>(H1.size() / (static_cast<size_t>(nLM) * C));
+    std::vector<long> in_off(NH + 1, 0), in_e(E);
     std::vector<int> src(E);
     for (int i = 0; i < N; ++i)
       for (long e = eoff[i]; e < eoff[i + 1]; ++e) {
         src[e] = i;
         ++in_off[nidx[e] + 1];
       }
-    for (int j = 0; j < N; ++j) in_off[j + 1] += in_off[j];
+    for (int j = 0; j < NH; ++j) in_off[j + 1] += in_off[j];
     {
       std::vector<long> fill(in_off.begin(), in_off.end() - 1);
       for (long e = 0; e < E; ++e) in_e[fill[nidx[e]]++] = e;
     }
-    par_nodes(N, [&](int j0, int j1) {
+    par_nodes(NH, [&](int j0, int j1) {
       vecd bR(spl1[0].ns), bRd(spl1[0].ns);
       for (int j = j0; j < j1; ++j) {
         double* aj = &H1_adj[static_cast<size_t>(j) * nLM * C];
@@ -798,7 +807,7 @@ struct Oracle {
 
   // mace.cpp:876-903 and multilayer_perceptron.cpp:76-150 (shape {C, 16, 1})
   void stage_readouts(int N, const int* ntype) {
-    H1_adj.assign(static_cast<size_t>(N) * nLM * C, 0.0);
+    H1_adj.assign(H1.size(), 0.0);  // every H1 row, a halo's too (mace.cpp:881-885)
     H2_adj.assign(static_cast<size_t>(N) * C, 0.0);
     const int nh = static_cast<int>(ro2_w2.size());
     par_nodes(N, [&](int i0, int i1) {
@@ -941,6 +950,22 @@ int orc_compute(void* h, int num_nodes, const int* node_types, const int* num_ne
   try {
     static_cast<Oracle*>(h)->compute(num_nodes, node_types, num_neigh, neigh_indices, neigh_types, num_edges,
                                      xyz, r);
+    return 0;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return 1;
+  }
+}
+
+// Layer 0 over num_nodes nodes, layer 1, readouts and ZBL over the first num_local_nodes
+// (the pair style's no-MPI-message-passing mode, pair_symmetrix_mace.cpp:672-698).
+int orc_compute_halo(void* h, int num_local_nodes, int num_nodes, const int* node_types, const int* num_neigh,
+                     const int* neigh_indices, const int* neigh_types, long num_edges, const double* xyz,
+                     const double* r) {
+  try {
+    if (num_local_nodes < 0) throw std::invalid_argument("negative num_local_nodes");
+    static_cast<Oracle*>(h)->compute(num_nodes, node_types, num_neigh, neigh_indices, neigh_types, num_edges,
+                                     xyz, r, num_local_nodes);
     return 0;
   } catch (const std::exception& e) {
     g_err = e.what();

@@ -43,6 +43,8 @@ def library(which="port"):
         f("set_lean").argtypes = [P, I]
     f("compute").restype = I
     f("compute").argtypes = [P, I, ip, ip, ip, ip, L, dp, dp]
+    f("compute_halo").restype = I
+    f("compute_halo").argtypes = [P, I, I, ip, ip, ip, ip, L, dp, dp]
     f("get").restype = L
     f("get").argtypes = [P, ctypes.c_char_p, dp, L]
     f("last_error").restype = ctypes.c_char_p
@@ -115,6 +117,18 @@ class Evaluator:
         rc = getattr(self.lib, self.pre + "compute")(self.h, int(num_nodes), _ip(keep[0]), _ip(keep[1]),
                                                      _ip(keep[2]), _ip(keep[3]), len(keep[5]), _dp(keep[4]),
                                                      _dp(keep[5]))
+        if rc != 0:
+            raise RuntimeError(getattr(self.lib, self.pre + "last_error")().decode())
+
+    def compute_halo(self, num_local_nodes, num_nodes, node_types, num_neigh, neigh_indices, neigh_types, xyz, r):
+        """Layer 0 over num_nodes nodes; layer 1, readouts and ZBL over the first
+        num_local_nodes (the stage calls of pair_symmetrix_mace.cpp:672-698)."""
+        keep = [np.ascontiguousarray(node_types, np.int32), np.ascontiguousarray(num_neigh, np.int32),
+                np.ascontiguousarray(neigh_indices, np.int32), np.ascontiguousarray(neigh_types, np.int32),
+                np.ascontiguousarray(xyz, np.float64).reshape(-1), np.ascontiguousarray(r, np.float64)]
+        rc = getattr(self.lib, self.pre + "compute_halo")(self.h, int(num_local_nodes), int(num_nodes), _ip(keep[0]),
+                                                          _ip(keep[1]), _ip(keep[2]), _ip(keep[3]), len(keep[5]),
+                                                          _dp(keep[4]), _dp(keep[5]))
         if rc != 0:
             raise RuntimeError(getattr(self.lib, self.pre + "last_error")().decode())
 

@@ -89,6 +89,51 @@ int ref_compute(void* h, int num_nodes, const int* node_types, const int* num_ne
   }
 }
 
+// The reference's stages in the order and with the node counts of the pair style's
+// no-MPI-message-passing mode (pair_symmetrix/pair_symmetrix_mace.cpp:657-698): layer 0
+// over num_nodes nodes, layer 1, readouts and ZBL over the first num_local_nodes.
+int ref_compute_halo(void* h, int num_local_nodes, int num_nodes, const int* node_types, const int* num_neigh,
+                     const int* neigh_indices, const int* neigh_types, long num_edges, const double* xyz,
+                     const double* r) {
+  try {
+    auto* m = static_cast<MACE*>(h);
+    const int nl = num_local_nodes, na = num_nodes;
+    const std::span<const int> nt(node_types, na), nn(num_neigh, na), ni(neigh_indices, num_edges),
+        te(neigh_types, num_edges);
+    const std::span<const double> x(xyz, 3 * num_edges), rr(r, num_edges);
+    m->node_energies.assign(nl, 0.0);
+    m->node_forces.assign(3 * num_edges, 0.0);
+    if (m->has_zbl)
+      m->zbl.compute_ZBL(nl, nt, nn, te, m->atomic_numbers, rr, x, m->node_energies, m->node_forces);
+    m->compute_Y(x);
+    m->compute_R0(na, nt, nn, te, rr);
+    m->compute_A0(na, nt, nn, te);
+    m->compute_A0_scaled(na, nt, nn, te, rr);
+    m->compute_M0(na, nt);
+    m->compute_H1(na);
+    m->compute_R1(nl, nt, nn, te, rr);
+    m->compute_Phi1(nl, nn, ni);
+    m->compute_A1(nl);
+    m->compute_A1_scaled(nl, nt, nn, te, rr);
+    m->compute_M1(nl, nt);
+    m->compute_H2(nl, nt);
+    m->compute_readouts(nl, nt);
+    m->reverse_H2(nl, nt, false);
+    m->reverse_M1(nl, nt);
+    m->reverse_A1_scaled(nl, nt, nn, te, x, rr, false);
+    m->reverse_A1(nl);
+    m->reverse_Phi1(nl, nn, ni, x, rr, false, false);
+    m->reverse_H1(na);
+    m->reverse_M0(na, nt);
+    m->reverse_A0_scaled(na, nt, nn, te, x, rr);
+    m->reverse_A0(na, nt, nn, te, x, rr);
+    return 0;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return 1;
+  }
+}
+
 // Copies a stage buffer; returns its length (copies at most cap values).
 long ref_get(void* h, const char* name, double* out, long cap) {
   auto* v = buffer(static_cast<MACE*>(h), name);

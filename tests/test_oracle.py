@@ -281,3 +281,66 @@ def test_port_matches_reference_with_zbl(tmp_path):
         ev.compute_node_energies_forces(*edge_args(species, nl))
     np.testing.assert_allclose(port.node_energies, ref.node_energies, rtol=1e-12, atol=1e-12)
     np.testing.assert_allclose(port.node_forces, ref.node_forces, rtol=1e-10, atol=1e-12)
+
+
+def _halo_golden(tmp_path):
+    from make_golden import halo_case, halo_model, model_fingerprint
+    g = dict(np.load(os.path.join(GOLD, "halo_golden.npz")))
+    path = halo_model(str(tmp_path / "halo.json"))
+    np.testing.assert_allclose(model_fingerprint(path), g["model_fingerprint"], rtol=1e-10)
+    c = halo_case()
+    assert np.array_equal(c["node_atom"], g["node_atom"])
+    assert np.array_equal(c["num_neigh"], g["num_neigh"])
+    assert np.array_equal(c["neigh_indices"], g["neigh_indices"])
+    return g, c, path
+
+
+def _halo_eval(path, which, c, n_local):
+    ev = Evaluator(path, which)
+    ev.compute_halo(n_local, len(c["node_atom"]), c["node_types"], c["num_neigh"], c["neigh_indices"],
+                    c["neigh_types"], c["xyz"], c["r"])
+    return ev
+
+
+def test_halo_golden_matches_reference_outputs(tmp_path):
+    """The pair style's no-MPI-message-passing stage calls (pair_symmetrix_mace.cpp:672-698:
+    layer 0 over local + halo nodes, layer 1, readouts and ZBL over the local ones) in
+    the port, against the reference's outputs on the same halo graph."""
+    g, c, path = _halo_golden(tmp_path)
+    ev = _halo_eval(path, "port", c, int(g["n_local"]))
+    assert len(ev.node_energies) == int(g["n_local"])
+    np.testing.assert_allclose(ev.node_energies, g["node_energies"], rtol=1e-9, atol=1e-10)
+    np.testing.assert_allclose(ev.node_forces, g["node_forces"], rtol=1e-8, atol=1e-10)
+    for s in ("A0", "M0", "H1", "Phi1", "A1", "M1", "H2", "H1_adj", "M0_adj", "A0_adj", "Phi1_adj"):
+        assert ev.get(s).sum() == pytest.approx(g["sum_" + s], rel=1e-9, abs=1e-10), s
+
+
+@needs_ref
+def test_port_matches_reference_halo_stagewise(tmp_path):
+    g, c, path = _halo_golden(tmp_path)
+    port, ref = (_halo_eval(path, w, c, int(g["n_local"])) for w in ("port", "reference"))
+    for name in ("A0", "M0", "H1", "Phi1", "A1", "M1", "H2", "node_energies", "H2_adj", "M1_adj", "A1_adj",
+                 "Phi1_adj", "H1_adj", "M0_adj", "A0_adj", "node_forces"):
+        a, b = port.get(name), ref.get(name)
+        assert a.shape == b.shape, name
+        np.testing.assert_allclose(a, b, rtol=1e-9, atol=1e-12 * max(1.0, np.abs(b).max()), err_msg=name)
+
+
+def test_halo_evaluation_equals_periodic_evaluation(tmp_path):
+    """On one rank the halo nodes are periodic images, so the halo form gives the periodic
+    box's node energies, and after each ghost's force is added to its local atom (LAMMPS's
+    reverse communication) its atomic forces and virial."""
+    from helpers import fold_halo_forces, virial
+    g, c, path = _halo_golden(tmp_path)
+    n = int(g["n_local"])
+    halo = _halo_eval(path, "port", c, n)
+    nl = neighbor_list(c["pos"], 5.0, c["L"])
+    per = Evaluator(path, "port")
+    per.compute_node_energies_forces(*edge_args(c["species"].astype(np.int32), nl))
+    np.testing.assert_allclose(halo.node_energies, per.node_energies, rtol=1e-12, atol=1e-12)
+    F_halo = fold_halo_forces(len(c["x"]), c["local_of"], c["node_atom"], c["num_neigh"], c["neigh_atom"],
+                              halo.node_forces)
+    F_per = atomic_forces(n, nl["i"], nl["neigh_indices"], per.node_forces)
+    np.testing.assert_allclose(F_halo, F_per, rtol=1e-10, atol=1e-11)
+    np.testing.assert_allclose(virial(c["xyz"], halo.node_forces), virial(nl["xyz"], per.node_forces), rtol=1e-10,
+                               atol=1e-10)

@@ -11,6 +11,10 @@
  *                                   the results the reference leaves in the members
  *                                   node_energies / node_forces are written to caller
  *                                   buffers instead
+ *   smx_compute_halo                the stage calls of the pair style's
+ *                                   no-MPI-message-passing mode, layer 0 over local and
+ *                                   halo nodes and layer 1 over the local ones
+ *                                   (pair_symmetrix/pair_symmetrix_mace.cpp:672-698)
  *   smx_compute_node_energies_forces_device
  *                                   the same call on device-resident arrays, as the Kokkos
  *                                   pair style passes them (pair_symmetrix/
@@ -32,6 +36,9 @@
  *                                   (Symmetrix.calculate, symmetrix_calc.py:72-102;
  *                                   PairSymmetrixMACE::compute_no_domain_decomposition,
  *                                   pair_symmetrix/pair_symmetrix_mace.cpp:242-372)
+ *   smx_pair_*                      pair_style symmetrix/mace's compute() in its three modes
+ *                                   on one rank (pair_symmetrix/pair_symmetrix_mace.cpp:
+ *                                   64-77, :242-748)
  *   smx_md_*                        a GPU-resident velocity-Verlet loop with a skin neighbour
  *                                   list, the role LAMMPS `fix nve` plays around the pair
  *                                   style (pair_symmetrix/test/test_pair_symmetrix_mace.py:253)
@@ -96,6 +103,20 @@ int smx_compute_node_energies_forces(smx_engine* eng, int num_nodes, const int* 
                                      const int* neigh_indices, const int* neigh_types, long num_edges,
                                      const double* xyz, const double* r, double* node_energies,
                                      double* node_forces);
+
+/* The evaluation the pair style's no-MPI-message-passing mode runs stage by stage
+ * (pair_symmetrix/pair_symmetrix_mace.cpp:672-698): layer 0 (A0, M0, H1 and their
+ * adjoints, density factor included) over all num_nodes nodes; ZBL, layer 1, the
+ * readouts and their adjoints over the first num_local_nodes only.  The trailing nodes
+ * are a halo: their H1 rows are read by the local nodes' layer-1 edges and the
+ * H1_adj those edges scatter to them flows back through layer 0 into the halo's own
+ * edges.  Arrays and checks as smx_compute_node_energies_forces over num_nodes nodes
+ * (a halo node's neigh_indices must be in range but are never read); node_energies
+ * receives num_local_nodes values, node_forces one triple per edge of every node.
+ * num_local_nodes == num_nodes is smx_compute_node_energies_forces. */
+int smx_compute_halo(smx_engine* eng, int num_local_nodes, int num_nodes, const int* node_types,
+                     const int* num_neigh, const int* neigh_indices, const int* neigh_types, long num_edges,
+                     const double* xyz, const double* r, double* node_energies, double* node_forces);
 
 /* Same, with every pointer in device memory of the engine's device; runs on
  * `stream` (a cudaStream_t, or NULL for the engine's own stream) and returns
@@ -290,6 +311,33 @@ int smx_pair_compute(smx_pair* pair, int inum, int nall, const int* ilist, const
                      const int* const* firstneigh, int neighmask, int neigh_changed, const double* x,
                      const int* type, const int* local_of, const int* mace_types, int ntypes, int eflag_global,
                      int eflag_atom, int vflag_global, double* f, double* eng_vdwl, double* eatom, double* virial);
+
+/* The pair style's three modes (PairSymmetrixMACE::settings, pair_symmetrix/
+ * pair_symmetrix_mace.cpp:95-113, and compute, :64-77), as they run on one rank.
+ *   SMX_PAIR_NO_DOMAIN_DECOMPOSITION  smx_pair_compute above (:242-372).
+ *   SMX_PAIR_MPI_MESSAGE_PASSING      :376-547.  On one rank LAMMPS's forward exchange of
+ *       H1 to the ghosts (:462-470) gives each ghost its owner's H1 and the reverse
+ *       exchange of H1_adj (:487-489) adds each ghost's to its owner's, which is the
+ *       ghost -> owner map local_of itself, so the evaluation is the first mode's; the
+ *       force of a ghost neighbour stays on its ghost row (F_j += f_e) for LAMMPS's own
+ *       reverse communication of forces.
+ *   SMX_PAIR_NO_MPI_MESSAGE_PASSING   :551-748.  The nodes are the local atoms, then the
+ *       ghosts within r_cut of a local atom in ascending index order (found on the GPU
+ *       each call); layer 0 runs over all of them, ZBL, layer 1 and the readouts over the
+ *       local ones (smx_compute_halo), and each edge's force lands on its two atoms,
+ *       ghosts included.  Needs LAMMPS's ghost neighbour list (the reference requests
+ *       REQ_FULL | REQ_GHOST and a communication cutoff of 2 r_cut + skin, :175-190):
+ *       ilist holds inum local then gnum ghost entries, numneigh and firstneigh cover
+ *       them all; local_of may be NULL.  A ghost node without a list is an error.
+ * gnum is ignored by the first two modes; every other argument is smx_pair_compute's. */
+#define SMX_PAIR_NO_DOMAIN_DECOMPOSITION 0
+#define SMX_PAIR_MPI_MESSAGE_PASSING 1
+#define SMX_PAIR_NO_MPI_MESSAGE_PASSING 2
+int smx_pair_compute_mode(smx_pair* pair, int mode, int inum, int gnum, int nall, const int* ilist,
+                          const int* numneigh, const int* const* firstneigh, int neighmask, int neigh_changed,
+                          const double* x, const int* type, const int* local_of, const int* mace_types, int ntypes,
+                          int eflag_global, int eflag_atom, int vflag_global, double* f, double* eng_vdwl,
+                          double* eatom, double* virial);
 
 #ifdef __cplusplus
 }

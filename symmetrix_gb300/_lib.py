@@ -31,6 +31,7 @@ SIGNATURES = [
     ("smx_num_LM", _I, [_P]),
     ("smx_atomic_numbers", _I, [_P, _P, _I]),
     ("smx_compute_node_energies_forces", _I, [_P, _I, _P, _P, _P, _P, _L, _P, _P, _P, _P]),
+    ("smx_compute_halo", _I, [_P, _I, _I, _P, _P, _P, _P, _L, _P, _P, _P, _P]),
     ("smx_compute_node_energies_forces_device", _I, [_P, _I, _P, _P, _P, _P, _L, _P, _P, _P, _P, _P]),
     ("smx_sync", _I, [_P, _P]),
     ("smx_get_stage", _L, [_P, _S, _P, _L]),
@@ -53,6 +54,8 @@ SIGNATURES = [
     ("smx_pair_create", _P, [_P]),
     ("smx_pair_destroy", None, [_P]),
     ("smx_pair_compute", _I, [_P, _I, _I, _P, _P, _P, _I, _I, _P, _P, _P, _P, _I, _I, _I, _I, _P, _P, _P, _P]),
+    ("smx_pair_compute_mode", _I, [_P, _I, _I, _I, _I, _P, _P, _P, _I, _I, _P, _P, _P, _P, _I, _I, _I, _I, _P, _P,
+                                   _P, _P]),
 ]
 
 STAGE_NAMES = ("layer0_fwd", "gemm_H1", "layer1_fwd", "gemm_A1", "node_tail", "gemm_Phi1_adj", "layer1_rev",

@@ -286,6 +286,9 @@ struct EdgeIn {
   // End of each centre atom's edges (nullptr: first[i + 1]): a list whose segments are
   // only partly filled, e.g. the in-cut-off edges packed at the front of a skin list's.
   const int* last = nullptr;
+  // Centres i >= n_local are a halo evaluated by layer 0 only (the pair style's
+  // no-MPI-message-passing form): their edges carry neither ZBL nor layer-1 forces.
+  int n_local = 0x7fffffff;
   __device__ __forceinline__ int atom_at(int b) const { return order ? order[b] : b; }
   __device__ __forceinline__ int end(int i) const { return last ? last[i] : first[i + 1]; }
 };

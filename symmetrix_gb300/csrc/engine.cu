@@ -279,6 +279,38 @@ int smx_compute_node_energies_forces(smx_engine* eng, int num_nodes, const int* 
   return SMX_OK;
 }
 
+int smx_compute_halo(smx_engine* eng, int num_local_nodes, int num_nodes, const int* node_types,
+                     const int* num_neigh, const int* neigh_indices, const int* neigh_types, long num_edges,
+                     const double* xyz, const double* r, double* node_energies, double* node_forces) {
+  if (!eng) return fail(SMX_ERR_INVALID, "engine is NULL");
+  if (num_local_nodes < 0 || num_local_nodes > num_nodes)
+    return fail(SMX_ERR_INVALID, "need 0 <= num_local_nodes <= num_nodes");
+  if (num_local_nodes > 0 && !node_energies) return fail(SMX_ERR_INVALID, "NULL node array");
+  if (num_edges > 0 && !node_forces) return fail(SMX_ERR_INVALID, "NULL edge array");
+  try {
+    check(cudaSetDevice(eng->device), "cudaSetDevice");
+    const int code = upload_edges(eng, num_nodes, node_types, num_neigh, neigh_indices, neigh_types, num_edges, xyz, r);
+    if (code != SMX_OK) return code;
+    if (num_local_nodes == 0) {  // no layer-1 node: no energy, and no force reaches any edge
+      if (num_edges > 0) std::memset(node_forces, 0, sizeof(double) * 3 * num_edges);
+      return SMX_OK;
+    }
+    cudaStream_t s = eng->stream;
+    eng->lastE = num_edges;
+    smx::EdgeIn in{eng->first, eng->ntype, eng->nidx, eng->ntype_e, eng->xyz, eng->r, num_nodes};
+    eng->run(in, eng->energies, eng->forces, s, num_local_nodes);
+    check(cudaMemcpyAsync(node_energies, eng->energies, sizeof(double) * num_local_nodes, cudaMemcpyDeviceToHost, s),
+          "D2H");
+    if (num_edges > 0)
+      check(cudaMemcpyAsync(node_forces, eng->forces, sizeof(double) * 3 * num_edges, cudaMemcpyDeviceToHost, s), "D2H");
+    check(cudaStreamSynchronize(s), "evaluation");
+  } catch (const std::exception& e) {
+    return fail(SMX_ERR_CUDA, e.what());
+  }
+  if (eng->take_status() != SMX_OK) return fail(SMX_ERR_TIMEOUT, "a device-side wait timed out; results are invalid");
+  return SMX_OK;
+}
+
 int smx_compute_node_energies_forces_device(smx_engine* eng, int num_nodes, const int* node_types,
                                             const int* num_neigh, const int* neigh_indices, const int* neigh_types,
                                             long num_edges, const double* xyz, const double* r,
@@ -332,7 +364,8 @@ long smx_get_stage(smx_engine* eng, const char* name, double* out, long cap) {
     fail(SMX_ERR_INVALID, "NULL argument");
     return -1;
   }
-  const long N = eng->lastN, C = eng->dm.C;
+  // layer-0 stages hold a row block per node, layer-1 stages per layer-1 node
+  const long N = eng->lastN, N1 = eng->lastN1, C = eng->dm.C;
   const float* src = nullptr;
   bool kept = true;
   long n = 0;
@@ -343,7 +376,7 @@ long smx_get_stage(smx_engine* eng, const char* name, double* out, long cap) {
       return -2;
     }
     const double* d = s == "node_energies" ? eng->energies : eng->forces;
-    n = s == "node_energies" ? N : 3 * eng->lastE;
+    n = s == "node_energies" ? N1 : 3 * eng->lastE;
     if (out && cap > 0 && n > 0) {
       try {
         check(cudaSetDevice(eng->device), "cudaSetDevice");
@@ -359,17 +392,17 @@ long smx_get_stage(smx_engine* eng, const char* name, double* out, long cap) {
   if (s == "A0") { src = eng->A0; n = N * 16 * C; }
   else if (s == "M0") { src = eng->M0; n = N * eng->dm.nLM * C; kept = eng->M0_kept; }
   else if (s == "H1") { src = eng->H1; n = N * eng->dm.nLM * C; }
-  else if (s == "Phi1") { src = eng->Phi1; n = N * eng->dm.n_lme * C; kept = eng->Phi1_kept; }
-  else if (s == "A1") { src = eng->A1; n = N * 16 * C; }
-  else if (s == "M1") { src = eng->M1; n = N * C; }
-  else if (s == "H2") { src = eng->H2; n = N * C; }
+  else if (s == "Phi1") { src = eng->Phi1; n = N1 * eng->dm.n_lme * C; kept = eng->Phi1_kept; }
+  else if (s == "A1") { src = eng->A1; n = N1 * 16 * C; }
+  else if (s == "M1") { src = eng->M1; n = N1 * C; }
+  else if (s == "H2") { src = eng->H2; n = N1 * C; }
   else if (s == "A0_adj") { src = eng->A0_adj; n = N * 16 * C; }
   else if (s == "M0_adj") { src = eng->M0_adj; n = N * eng->dm.nLM * C; }
   else if (s == "H1_adj") { src = eng->H1_adj; n = N * eng->dm.nLM * C; }
-  else if (s == "Phi1_adj") { src = eng->Phi1_adj; n = N * eng->dm.n_lme * C; }
-  else if (s == "A1_adj") { src = eng->A1_adj; n = N * 16 * C; kept = eng->A1adj_kept; }
-  else if (s == "M1_adj") { src = eng->M1_adj; n = N * C; }
-  else if (s == "H2_adj") { src = eng->H2_adj; n = N * C; }
+  else if (s == "Phi1_adj") { src = eng->Phi1_adj; n = N1 * eng->dm.n_lme * C; }
+  else if (s == "A1_adj") { src = eng->A1_adj; n = N1 * 16 * C; kept = eng->A1adj_kept; }
+  else if (s == "M1_adj") { src = eng->M1_adj; n = N1 * C; }
+  else if (s == "H2_adj") { src = eng->H2_adj; n = N1 * C; }
   else {
     fail(SMX_ERR_INVALID, std::string("unknown stage '") + name + "'");
     return -1;
@@ -403,18 +436,18 @@ long smx_get_stage(smx_engine* eng, const char* name, double* out, long cap) {
 long smx_set_stage(smx_engine* eng, const char* name, const double* values, long n) {
   if (!eng || !name || (n > 0 && !values)) return -fail(SMX_ERR_INVALID, "NULL argument");
   if (!eng->evaluated) return -fail(SMX_ERR_INVALID, "no evaluation has set up the engine's buffers yet");
-  const long N = eng->lastN, C = eng->dm.C;
+  const long N = eng->lastN, N1 = eng->lastN1, C = eng->dm.C;
   const std::string s(name);
   float* dst = nullptr;
   long want = 0;
   if (s == "M0") { dst = eng->M0; want = N * eng->dm.nLM * C; eng->M0_kept = true; }
   else if (s == "H1") { dst = eng->H1; want = N * eng->dm.nLM * C; }
-  else if (s == "Phi1") { dst = eng->Phi1; want = N * eng->dm.n_lme * C; eng->Phi1_kept = true; }
-  else if (s == "A1") { dst = eng->A1; want = N * 16 * C; }
+  else if (s == "Phi1") { dst = eng->Phi1; want = N1 * eng->dm.n_lme * C; eng->Phi1_kept = true; }
+  else if (s == "A1") { dst = eng->A1; want = N1 * 16 * C; }
   else if (s == "M0_adj") { dst = eng->M0_adj; want = N * eng->dm.nLM * C; }
   else if (s == "H1_adj") { dst = eng->H1_adj; want = N * eng->dm.nLM * C; }
-  else if (s == "Phi1_adj") { dst = eng->Phi1_adj; want = N * eng->dm.n_lme * C; }
-  else if (s == "A1_adj") { dst = eng->A1_adj; want = N * 16 * C; eng->A1adj_kept = true; }
+  else if (s == "Phi1_adj") { dst = eng->Phi1_adj; want = N1 * eng->dm.n_lme * C; }
+  else if (s == "A1_adj") { dst = eng->A1_adj; want = N1 * 16 * C; eng->A1adj_kept = true; }
   else if (s != "node_forces") return -fail(SMX_ERR_INVALID, std::string("stage '") + name + "' cannot be written");
   if (s == "node_forces") want = 3 * eng->lastE;
   if (n != want)
@@ -448,7 +481,8 @@ int smx_run_stage(smx_engine* eng, const char* stage, int num_nodes, const int* 
     cudaStream_t s = eng->stream;
     if (node_stage) {
       if (!eng->evaluated) return fail(SMX_ERR_INVALID, "no evaluation has set up the engine's buffers yet");
-      if (num_nodes != eng->lastN)
+      const bool layer1 = st == "compute_A1" || st == "reverse_A1";
+      if (num_nodes != (layer1 ? eng->lastN1 : eng->lastN))
         return fail(SMX_ERR_INVALID, "num_nodes differs from the evaluation that set up the engine's buffers");
       if (st == "reverse_A1" && !eng->A1adj_kept)
         return fail(SMX_ERR_INVALID, "A1_adj was not written by the last evaluation (set it or keep_stages)");
@@ -466,7 +500,7 @@ int smx_run_stage(smx_engine* eng, const char* stage, int num_nodes, const int* 
         check(cudaMemsetAsync(eng->H1, 0, sizeof(float) * num_nodes * eng->dm.nLM * C, s), "cudaMemsetAsync");
         check(cudaMemsetAsync(eng->H1_adj, 0, sizeof(float) * num_nodes * eng->dm.nLM * C, s), "cudaMemsetAsync");
         check(cudaMemsetAsync(eng->Phi1_adj, 0, sizeof(float) * num_nodes * eng->dm.n_lme * C, s), "cudaMemsetAsync");
-        eng->lastN = num_nodes;
+        eng->lastN = eng->lastN1 = num_nodes;
         eng->evaluated = true;
         eng->M0_kept = eng->Phi1_kept = eng->A1adj_kept = false;
       }

@@ -90,7 +90,9 @@ struct smx_engine {
   int* atom_order = nullptr;  // centre atoms sorted by species (when species_order is on)
   int* nneigh = nullptr;      // num_neigh of the host-pointer call
   double *xyz = nullptr, *r = nullptr, *energies = nullptr, *forces = nullptr;
-  int lastN = 0;
+  // nodes of the last evaluation: all of them (layer 0) and the layer-1 ones (fewer when
+  // the trailing nodes were a halo)
+  int lastN = 0, lastN1 = 0;
   long lastE = 0;                  // edges of the last host- or device-pointer call or stage call
   bool evaluated = false;          // the workspace holds the stages of an evaluation
   bool M0_kept = false, Phi1_kept = false, A1adj_kept = false;  // float32 rows written by it
@@ -535,7 +537,7 @@ struct smx_engine {
     }
   }
 
-  void tune_sched(const smx::EdgeIn& in, double* out_e, double* out_f, cudaStream_t s) {
+  void tune_sched(const smx::EdgeIn& in, double* out_e, double* out_f, cudaStream_t s, int n1) {
     static constexpr int kStageOf[smx::kAkCount] = {0, 8, 8, 2, 6, 4};  // stage index of each kernel
     const bool prof = profile;
     profile = true;
@@ -545,7 +547,7 @@ struct smx_engine {
     for (int rep = 0; rep < 2; ++rep)
       for (int mode = 0; mode < 2; ++mode) {
         sched_set(mode);
-        run_pass(in, out_e, out_f, s);
+        run_pass(in, out_e, out_f, s, n1);
         check(cudaEventSynchronize(ev[kStages]), "autotune");
         for (int q = 0; q < kStages; ++q) {
           float ms = 0.0f;
@@ -562,7 +564,7 @@ struct smx_engine {
       for (int rep = 0; rep < 2; ++rep)
         for (int ns = 1; ns <= l2_split_max; ++ns) {
           set_l2_split(ns);
-          run_pass(in, out_e, out_f, s);
+          run_pass(in, out_e, out_f, s, n1);
           check(cudaEventSynchronize(ev[kStages]), "autotune");
           float a = 0.0f, b = 0.0f;
           check(cudaEventElapsedTime(&a, ev[2], ev[3]), "cudaEventElapsedTime");
@@ -601,7 +603,7 @@ struct smx_engine {
   smx::GemmBatch node_gemm(const float* X, float* Y, const float* const* W, int nb, bool per_l, bool trans) const {
     // per_l false: the L blocks of [N][nLM][C] (H1 and its adjoint); true: the l blocks of
     // Phi1 [N][n_lme][C] against A1 [N][16][C] (trans: A1_adj -> Phi1_adj)
-    const int C = dm.C, N = lastN;
+    const int C = dm.C, N = per_l ? lastN1 : lastN;
     smx::GemmBatch b{};
     if (!per_l) {
       for (int L = 0; L < nb; ++L)
@@ -664,26 +666,36 @@ struct smx_engine {
   }
 
   // The full forward + adjoint pass on device-resident inputs (tuning the atom schedule
-  // first when due).
-  void run(const smx::EdgeIn& in, double* out_e, double* out_f, cudaStream_t s) {
+  // first when due).  n1 (0 < n1 <= in.N; -1: in.N): layer 1, the readouts and ZBL run
+  // over the first n1 nodes only and the rest form a halo that layer 0 evaluates for the
+  // H1 rows the first n1 nodes' edges read (the pair style's no-MPI-message-passing
+  // form, pair_symmetrix/pair_symmetrix_mace.cpp:672-698); out_e then receives n1 values.
+  void run(const smx::EdgeIn& in, double* out_e, double* out_f, cudaStream_t s, int n1 = -1) {
     if (autotune && sched_force < 0 && !sched_tuned && in.N > 0) {
       cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
       check(cudaStreamIsCapturing(s, &cs), "cudaStreamIsCapturing");
-      if (cs == cudaStreamCaptureStatusNone) tune_sched(in, out_e, out_f, s);
+      if (cs == cudaStreamCaptureStatusNone) tune_sched(in, out_e, out_f, s, n1);
     }
-    run_pass(in, out_e, out_f, s);
+    run_pass(in, out_e, out_f, s, n1);
   }
 
-  void run_pass(const smx::EdgeIn& in_, double* out_e, double* out_f, cudaStream_t s) {
-    smx::EdgeIn in = in_;
+  void run_pass(const smx::EdgeIn& in_, double* out_e, double* out_f, cudaStream_t s, int n1 = -1) {
+    smx::EdgeIn in = in_;  // layer 0: all N nodes
     const int N = in.N;
-    if (N > 0 && order_species()) {
+    const int N1 = n1 < 0 ? N : n1;
+    if (N1 > N || (N > 0 && N1 == 0)) throw std::invalid_argument("layer-1 node count outside (0, num_nodes]");
+    const bool halo = N1 < N;
+    if (N > 0 && !halo && order_species()) {
       smx::launch_species_order(in.node_type, N, dm.S, atom_order, s);
       in.order = atom_order;
     }
+    smx::EdgeIn in1 = in;  // layer 1: the first N1 nodes (a prefix of the edge list)
+    in1.N = N1;
+    if (halo) in.n_local = N1;
     const int C = dm.C;
     const int T = tc_terms, XT = smx::split_xterms(T);
     lastN = N;
+    lastN1 = N1;
     if (N == 0) {
       evaluated = true;
       return;
@@ -692,6 +704,11 @@ struct smx_engine {
       for (auto& e : ev) check(cudaEventCreate(&e), "cudaEventCreate");
     prof_stream = s;
     mark(0, s);
+    // the halo's H1_adj rows receive only the local nodes' layer-1 scatter (the node tail
+    // seeds the first N1 rows)
+    if (halo)
+      smx::launch_rows_to_fixed(nullptr, H1_adj_fx + static_cast<size_t>(N1) * dm.nLM * C,
+                                static_cast<long>(N - N1) * dm.nLM * C, true, s);
     // The BF16 form's GEMMs read the producers' split bf16 rows; the float32 copies of
     // M0, Phi1 and A1_adj are then written only for inspection or a SIMT fallback.
     bool all_A1 = true, all_Phi1adj = true;
@@ -725,7 +742,7 @@ struct smx_engine {
       smx::launch_gemm(b, s);
     }
     mark(2, s);
-    smx::launch_layer1_fwd(dm, in, H1, Phi1_out, s);
+    smx::launch_layer1_fwd(dm, in1, H1, Phi1_out, s);
     mark(3, s);
     {  // A1 = Phi1 @ A1W[l]  (mace.cpp:607-642)
       // tensor cores on the per-l regrouped split bf16 rows layer1_fwd wrote, one launch
@@ -733,9 +750,9 @@ struct smx_engine {
       int ng = 0;
       for (int l = 0; l < 4; ++l)
         if (dm.num_e[l] > 0 && tc_A1[l]) {
-          const long rows = static_cast<long>(N) * (2 * l + 1);
+          const long rows = static_cast<long>(N1) * (2 * l + 1);
           const int K = dm.num_e[l] * C;
-          g[ng] = smx::UmmaGemm{Phi1_bf + static_cast<size_t>(XT) * N * dm.lme_off[l] * C, rows, K, W_A1[l], C, C,
+          g[ng] = smx::UmmaGemm{Phi1_bf + static_cast<size_t>(XT) * N1 * dm.lme_off[l] * C, rows, K, W_A1[l], C, C,
                                 smx::UmmaOut{A1, rows, 2 * l + 1, 16L * C, l * l * C, C, 0}};
           g[ng++].terms = T;
         }
@@ -743,13 +760,13 @@ struct smx_engine {
       smx::GemmBatch b{};
       for (int l = 0; l < 4; ++l)
         if (dm.num_e[l] > 0 && !tc_A1[l])
-          b.s[b.n++] = seg_rows(Phi1, A1, dm.A1W[l], N, 2 * l + 1, dm.num_e[l] * C, C,
+          b.s[b.n++] = seg_rows(Phi1, A1, dm.A1W[l], N1, 2 * l + 1, dm.num_e[l] * C, C,
                                 static_cast<long>(dm.n_lme) * C, dm.lme_off[l] * C, dm.num_e[l] * C,
                                 16L * C, l * l * C, C);
       smx::launch_gemm(b, s);
     }
     mark(4, s);
-    smx::launch_node_tail(dm, in.node_type, N, A1, H1, M1, H2, A1adj_out, H1_adj_fx, M1_adj, H2_adj,
+    smx::launch_node_tail(dm, in.node_type, N1, A1, H1, M1, H2, A1adj_out, H1_adj_fx, M1_adj, H2_adj,
                           dm.has_zbl ? zbl_e : nullptr, out_e, s);
     mark(5, s);
     {  // Phi1_adj = A1_adj @ A1W[l]^T  (mace.cpp:644-679)
@@ -758,8 +775,8 @@ struct smx_engine {
       int ng = 0;
       for (int l = 0; l < 4; ++l)
         if (dm.num_e[l] > 0 && tc_Phi1adj[l]) {
-          const long rows = static_cast<long>(N) * (2 * l + 1);
-          g[ng] = smx::UmmaGemm{A1adj_bf + static_cast<size_t>(XT) * N * l * l * C, rows, C, W_Phi1adj[l],
+          const long rows = static_cast<long>(N1) * (2 * l + 1);
+          g[ng] = smx::UmmaGemm{A1adj_bf + static_cast<size_t>(XT) * N1 * l * l * C, rows, C, W_Phi1adj[l],
                                 dm.num_e[l] * C, C,
                                 smx::UmmaOut{Phi1_adj, rows, 2 * l + 1, static_cast<long>(dm.n_lme) * C,
                                              dm.lme_off[l] * C, dm.num_e[l] * C, 0}};
@@ -769,12 +786,12 @@ struct smx_engine {
       smx::GemmBatch b{};
       for (int l = 0; l < 4; ++l)
         if (dm.num_e[l] > 0 && !tc_Phi1adj[l])
-          b.s[b.n++] = seg_rows(A1_adj, Phi1_adj, dm.A1W_T[l], N, 2 * l + 1, C, dm.num_e[l] * C, 16L * C, l * l * C,
+          b.s[b.n++] = seg_rows(A1_adj, Phi1_adj, dm.A1W_T[l], N1, 2 * l + 1, C, dm.num_e[l] * C, 16L * C, l * l * C,
                                 C, static_cast<long>(dm.n_lme) * C, dm.lme_off[l] * C, dm.num_e[l] * C);
       smx::launch_gemm(b, s);
     }
     mark(6, s);
-    smx::launch_layer1_rev(dm, in, H1, Phi1_adj, H1_adj_fx, f1, s);
+    smx::launch_layer1_rev(dm, in1, H1, Phi1_adj, H1_adj_fx, f1, s);
     mark(7, s);
     // the float H1_adj rows (and the BF16 form's split operand) from the fixed-point sums
     smx::launch_fixed_rows(H1_adj_fx, H1_adj, tc_H1 ? H1adj_bf : nullptr, static_cast<long>(N) * dm.nLM, C, T, dm.nLM,

@@ -340,6 +340,7 @@ __device__ __forceinline__ void layer0_rev_atom(const DevModel& m, const EdgeIn&
   const int nwarp = blockDim.x >> 5;
   const int ti = in.node_type[i];
   const int e0 = in.first[i], e1 = in.end(i);
+  const bool local = i < in.n_local;  // a halo centre: layer 0 only
   float2 dA[16];
 #pragma unroll
   for (int q = 0; q < 16; ++q)
@@ -396,7 +397,7 @@ __device__ __forceinline__ void layer0_rev_atom(const DevModel& m, const EdgeIn&
       if (st.row[t] >= 0)
         for (int w = 0; w < nwarp; ++w)
           for (int a = 0; a < 3; ++a) s[a] += static_cast<double>(sF[t][w][a]);
-      if (m.has_zbl) {  // node_forces -= xyz / r * dV_ZBL/dr (zbl.cpp:118-121)
+      if (m.has_zbl && local) {  // node_forces -= xyz / r * dV_ZBL/dr (zbl.cpp:118-121)
         float V, dV;
         const double r = in.r[e];
         zbl_edge(m, m.zbl_pair[ti * m.S + in.ntype_e[e]], static_cast<float>(r), V, dV);
@@ -410,8 +411,11 @@ __device__ __forceinline__ void layer0_rev_atom(const DevModel& m, const EdgeIn&
         for (int a = 0; a < 3; ++a) s[a] -= g * in.xyz[3 * e + a];
       }
       for (int a = 0; a < 3; ++a) {
-        double f = f1[3 * e + a];
-        for (int h = 1; h < m.l2_split; ++h) f += f1[h * m.f1_stride + 3 * e + a];  // channel slices (L_max = 2)
+        double f = 0.0;
+        if (local) {
+          f = f1[3 * e + a];
+          for (int h = 1; h < m.l2_split; ++h) f += f1[h * m.f1_stride + 3 * e + a];  // channel slices (L_max = 2)
+        }
         forces[3 * e + a] = -(s[a] + f);
       }
     }

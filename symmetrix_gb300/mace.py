@@ -91,6 +91,29 @@ class MACE:
         self.node_energies = energies
         self.node_forces = forces
 
+    def compute_halo(self, num_local_nodes, num_nodes, node_types, num_neigh, neigh_indices, neigh_types, xyz, r):
+        """The stage calls of the pair style's no-MPI-message-passing mode
+        (pair_symmetrix_mace.cpp:672-698): layer 0 over all num_nodes nodes; ZBL, layer 1
+        and the readouts over the first num_local_nodes.  node_energies gets
+        num_local_nodes values, node_forces one triple per edge of every node."""
+        node_types = np.ascontiguousarray(node_types, dtype=np.int32)[:num_nodes]
+        num_neigh = np.ascontiguousarray(num_neigh, dtype=np.int32)[:num_nodes]
+        neigh_indices = np.ascontiguousarray(neigh_indices, dtype=np.int32)
+        neigh_types = np.ascontiguousarray(neigh_types, dtype=np.int32)
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1)
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        E = len(r)
+        if len(neigh_indices) != E or len(neigh_types) != E or len(xyz) != 3 * E:
+            raise ValueError("edge arrays have inconsistent lengths")
+        energies = np.zeros(max(int(num_local_nodes), 0))
+        forces = np.zeros(3 * E)
+        code = self._lib.smx_compute_halo(
+            self._h, int(num_local_nodes), int(num_nodes), _ptr(node_types), _ptr(num_neigh), _ptr(neigh_indices),
+            _ptr(neigh_types), E, _ptr(xyz), _ptr(r), _ptr(energies), _ptr(forces))
+        _lib.raise_for(code, self._lib)
+        self.node_energies = energies
+        self.node_forces = forces
+
     def compute_device(self, num_nodes, node_types, num_neigh, neigh_indices, neigh_types, num_edges, xyz, r,
                        node_energies, node_forces, stream=None):
         """Device-pointer variant: every argument is an integer device address."""

@@ -372,6 +372,10 @@ __device__ __forceinline__ void layer0_rev_atom(const DevModel& m, const EdgeIn&
         float2 dRl = make_float2(0.0f, 0.0f);
 #pragma unroll
         for (int q = l * l; q < (l + 1) * (l + 1); ++q) {
+          if (q == 0) {  // Y_00 = 1 with a zero gradient (sph_harm16): the R_0' term alone
+            dRl = dA[0];
+            continue;
+          }
           const float4 g = st.G[t][q];  // (dY/dx, dY/dy, dY/dz, Y)
           dRl = fma2(dA[q], make_float2(g.w, g.w), dRl);
           const float2 w = mul2(dA[q], R[l]);

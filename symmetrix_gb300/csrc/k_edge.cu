@@ -140,9 +140,10 @@ __device__ __forceinline__ void layer0_fwd_atom(const DevModel& m, const EdgeIn&
 #pragma unroll
       for (int l = 0; l < 4; ++l) R[l] = spline2_val(c[2 * l], c[2 * l + 1], x2);
       if (a + 2 < na) fetch(a + 2);
+      acc[0] = __fadd2_rn(R[0], acc[0]);  // Y_00 = 1 (sph_harm16)
 #pragma unroll
-      for (int q = 0; q < 16; ++q) {
-        const int l = q < 1 ? 0 : (q < 4 ? 1 : (q < 9 ? 2 : 3));
+      for (int q = 1; q < 16; ++q) {
+        const int l = q < 4 ? 1 : (q < 9 ? 2 : 3);
         acc[q] = fma2(R[l], st.Y2[t][q], acc[q]);
       }
     }

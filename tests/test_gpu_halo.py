@@ -11,6 +11,7 @@ import pytest
 
 from helpers import edge_args
 from oracle.pyoracle import Evaluator
+from symmetrix_gb300.synth.model import make_model, write_model
 from symmetrix_gb300.synth.structures import neighbor_list, random_box
 
 pytestmark = pytest.mark.gpu
@@ -79,6 +80,30 @@ def test_any_trailing_halo_matches_oracle(engine_lib, small_model_path, precisio
     e_h, f_h = m.node_energies.copy(), m.node_forces.copy()
     m.compute_node_energies_forces(64, *args)
     assert np.array_equal(m.node_energies, e_h) and np.array_equal(m.node_forces, f_h)
+
+
+@pytest.mark.parametrize("precision", ["float32", "bfloat16"])
+def test_lmax2_halo_and_schedules_match_oracle(engine_lib, tmp_path, precision):
+    """L_max = 2 (17 instructions, four instruction groups; 64 channels, so the layer-1
+    kernels may run two channel slices per node, both tried while tuning) with density
+    scaling and ZBL, in both atom schedules (one block per atom, persistent grids)."""
+    from symmetrix_gb300 import MACE
+    path = write_model(make_model(num_channels=64, species=("H", "C", "O"), r_cut=5.0, L_max=2, num_knots=60,
+                                  seed=3, density_scaled=True, zbl=True), str(tmp_path / "l2.json"))
+    pos, L, species = random_box(64, 0.064, 0.9, 3, seed=4)
+    nl = neighbor_list(pos, 5.0, L)
+    args = edge_args(species, nl)[1:]
+    ref = Evaluator(path, "port")
+    ref.compute_halo(40, 64, *args)
+    m = MACE(path, precision=precision)
+    e_tol, f_tol = TOL[precision]
+    for persistent in (-1, 0, 1):
+        m.set_option("persistent", persistent)
+        m.compute_halo(40, 64, *args)
+        de, df = _max(m.node_energies, ref.node_energies), _max(m.node_forces, ref.node_forces)
+        print(f"{precision} persistent={persistent} l2_split={m.get_option('l2_split')}: dE_i={de:.2e} "
+              f"df_edge={df:.2e}")
+        assert de < e_tol and df < f_tol
 
 
 def test_halo_rejects_bad_counts(engine_lib, small_model_path):

@@ -32,7 +32,7 @@ roofline come from engine CUDA events over a separate pass of evaluation steps o
 the same structure, with L2 flushed between those steps.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                       [--workload fp32_4096|precision_32768|large_1m|molecules]
+                       [--workload fp32_4096|precision_32768|large_1m|molecules|pair_modes]
                        [--detail PATH] [--full-check]
 --detail writes the long form of the result (per-stage FLOP and byte rates, MD energy
 record, schedules) to PATH; stdout carries one compact line.
@@ -753,6 +753,86 @@ def molecules_arm(args):
     }), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# LAMMPS pair-style adapter (--workload pair_modes): not the headline line
+# ---------------------------------------------------------------------------
+def pair_modes_arm(args):
+    """One compute() of pair_style symmetrix/mace per step, in each of its three modes,
+    on the headline box laid out as one LAMMPS rank (4096 local atoms, ghost images
+    2 r_cut + 1 A deep, full lists within r_cut + 1 A of every atom): host positions in,
+    host forces, energy and virial out, timed on the host clock around the synchronous
+    call (smx_pair_compute_mode).  Each mode's forces, folded onto the local atoms as
+    LAMMPS's reverse communication does, are compared with the first mode's."""
+    from symmetrix_gb300 import MACE
+    from symmetrix_gb300.build import build
+    from symmetrix_gb300.lammps import MODES, PairAdapter
+    from symmetrix_gb300.synth.structures import lammps_rank, random_box
+
+    build()
+    path = engine_model_path(model_path())
+    W = WORKLOAD
+    pos, L, species = random_box(W["n_atoms"], W["density"], W["min_dist"], W["n_species"], seed=W["struct_seed"])
+    n = len(pos)
+    rc = W["r_cut"]
+    t = time.time()
+    x, local_of, lists = lammps_rank(pos, L, rc + 1.0, 2 * rc + 1.0)
+    nall = len(x)
+    log(f"LAMMPS layout: {n} local + {nall - n} ghost atoms, {sum(len(a) for a in lists)} list entries "
+        f"({time.time() - t:.1f} s)")
+    types = (species[local_of] + 1).astype(np.int32)
+    mace_types = np.arange(W["n_species"], dtype=np.int32)
+
+    def fold(f):
+        out = np.zeros((n, 3))
+        np.add.at(out, local_of, f)
+        return out
+
+    out = {}
+    for form in ("fp32", "bf16"):
+        eng = MACE(path, precision=form)
+        base = None
+        for mode in MODES:
+            pair = PairAdapter(eng, mace_types, mode)
+            halo = mode == "no_mpi_message_passing"
+            call = (lambda changed: pair.compute(x, types, None, np.arange(nall), lists, neigh_changed=changed,
+                                                 gnum=nall - n)) if halo else \
+                   (lambda changed: pair.compute(x, types, local_of, np.arange(n), lists[:n], neigh_changed=changed))
+            res = call(True)
+            for _ in range(args.warmup - 1):
+                res = call(False)
+            times = []
+            for _ in range(args.steps):
+                t0 = time.perf_counter()
+                res = call(False)
+                times.append(time.perf_counter() - t0)
+            T = float(np.median(times))
+            e, f, _, vir = res
+            r = {"value": n / T, "ms_per_call": T * 1e3, "ms_mean": float(np.mean(times)) * 1e3}
+            if base is None:
+                base = (e, fold(f), vir)
+            else:
+                r["vs_first_mode"] = {"energy_eV": sig(abs(e - base[0]), 3),
+                                      "max_folded_force_eV_per_A": sig(float(np.abs(fold(f) - base[1]).max()), 3),
+                                      "max_virial_eV": sig(float(np.abs(vir - base[2]).max()), 3)}
+            out.setdefault(mode, {})[form] = r
+            log(f"{form} {mode}: {r}")
+            del pair
+        del eng
+    first = next(iter(MODES))
+    print(json.dumps({
+        "metric": "atom-steps/s (one pair_style symmetrix/mace compute() per step, host arrays in and out)",
+        "value": out[first]["bf16"]["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": out[first]["bf16"]["ms_per_call"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+        "config": {"workload": f"pair_modes_4096: the headline box and model as one LAMMPS rank, {n} local and "
+                               f"{nall - n} ghost atoms ({2 * rc + 1.0:g} A shell), full lists within "
+                               f"{rc + 1.0:g} A of every atom; median host time of one compute() per mode",
+                   "atoms": n, "ghosts": nall - n},
+        "h2d_bytes_per_call": 8 * 3 * nall, "d2h_bytes_per_call": 8 * 3 * nall,
+        "modes": out,
+    }), flush=True)
+
+
 def large_arm(args):
     """MD of the 1,048,576-atom box in both forms (one engine alive at a time: the node
     features of one form take ~90 GB)."""
@@ -830,9 +910,10 @@ def main():
     ap.add_argument("--full-check", action="store_true",
                     help="precision_32768 / large_1m: also check the whole timed box against the float64 oracle")
     ap.add_argument("--workload", default="fp32_4096",
-                    choices=["fp32_4096", "precision_32768", "large_1m", "molecules"],
+                    choices=["fp32_4096", "precision_32768", "large_1m", "molecules", "pair_modes"],
                     help="fp32_4096: the headline line; precision_32768: L_max 2, 10 species, 32768 atoms; "
-                         "molecules: the batching form (2048 molecules)")
+                         "molecules: the batching form (2048 molecules); pair_modes: the headline box through "
+                         "the LAMMPS pair-style adapter in its three modes")
     args = ap.parse_args()
     global WORKLOAD
     if args.workload in WORKLOADS:
@@ -850,6 +931,9 @@ def main():
     elif args.workload == "large_1m":
         if rank == 0:
             large_arm(args)
+    elif args.workload == "pair_modes":
+        if rank == 0:
+            pair_modes_arm(args)
     else:
         gpu_arm(args, rank, world, local_rank)
 

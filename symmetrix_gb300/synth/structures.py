@@ -141,6 +141,38 @@ def neighbor_list(pos, cutoff, box=None):
                 r=np.ascontiguousarray(r), i=I.astype(np.int32), shift=S)
 
 
+def lammps_rank(pos, box, cutoff, shell, ghost_lists=True):
+    """A periodic cubic box as one LAMMPS rank holds it (one process, no domain
+    decomposition): the local atoms pos[n] wrapped into the box, then their periodic
+    images within `shell` of it as ghosts; local_of[a] is the local atom that atom a is
+    an image of (atom->map(atom->tag[a])), and lists[a] the full neighbour list of atom a
+    (all atoms within `cutoff`, LAMMPS's pair cutoff plus skin, ascending index) for
+    the local atoms or, with ghost_lists (LAMMPS's ghost neighbour request), for every
+    atom.  Returns x[nall, 3], local_of[nall] int32, lists (int32 arrays)."""
+    pos = np.asarray(pos, dtype=np.float64)
+    pos = pos - box * np.floor(pos / box)
+    n = len(pos)
+    k = int(np.ceil(shell / box))
+    xs, owner = [pos], [np.arange(n)]
+    for s in np.array(np.meshgrid(*[np.arange(-k, k + 1)] * 3, indexing="ij")).reshape(3, -1).T:
+        if not s.any():
+            continue
+        p = pos + s * box
+        keep = np.all((p > -shell) & (p < box + shell), axis=1)
+        xs.append(p[keep])
+        owner.append(np.nonzero(keep)[0])
+    x = np.concatenate(xs)
+    local_of = np.concatenate(owner).astype(np.int32)
+    from scipy.spatial import cKDTree
+    centres = x if ghost_lists else x[:n]
+    found = cKDTree(x).query_ball_point(centres, cutoff, return_sorted=True)
+    lists = []
+    for a, js in enumerate(found):
+        js = np.asarray(js, dtype=np.int32)
+        lists.append(js[js != a])
+    return x, local_of, lists
+
+
 def maxwell_boltzmann(masses, T, rng):
     """Velocities in A/fs at temperature T (K) with zero net momentum (masses in amu)."""
     m = np.asarray(masses, dtype=np.float64)[:, None]

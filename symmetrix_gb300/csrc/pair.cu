@@ -39,73 +39,111 @@ using smx::fail;
 
 namespace {
 
-// in-cut-off candidates of each node: num_neigh[ii] for the atom nodes[ii]
-__global__ void k_pair_count(int n_nodes, const int* __restrict__ nodes, const int* __restrict__ aoff,
-                             const int* __restrict__ cand_j, const double* __restrict__ x, double rc2,
-                             int* __restrict__ num_neigh) {
-  const int ii = blockIdx.x * blockDim.x + threadIdx.x;
-  if (ii >= n_nodes) return;
-  const int i = nodes[ii];
+// The per-node kernels below run one warp per node (blocks of kWarpsPerBlock whole warps,
+// a warp exits as one) and walk the node's candidates 32 at a time in list order, so a
+// ballot keeps the edges in that order.  Candidate j of centre i is an edge when
+// 0 < r^2 < r_cut^2, r^2 formed by explicit FMAs so that every kernel takes the same
+// decision for the same pair.
+constexpr int kWarpsPerBlock = 8;
+
+__device__ __forceinline__ double pair_r2(const double* __restrict__ x, double xi, double yi, double zi, int j,
+                                          double& dx, double& dy, double& dz) {
+  dx = x[3 * j] - xi;
+  dy = x[3 * j + 1] - yi;
+  dz = x[3 * j + 2] - zi;
+  return fma(dz, dz, fma(dy, dy, dx * dx));
+}
+
+__device__ __forceinline__ int node_warp() {
+  return static_cast<int>((blockIdx.x * static_cast<long>(blockDim.x) + threadIdx.x) >> 5);
+}
+
+// in-cut-off candidates of each node: num_neigh[w] for the atom nodes[w]
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+    k_pair_count(int n_nodes, const int* __restrict__ nodes, const int* __restrict__ aoff,
+                 const int* __restrict__ cand_j, const double* __restrict__ x, double rc2,
+                 int* __restrict__ num_neigh) {
+  const int w = node_warp(), lane = threadIdx.x & 31;
+  if (w >= n_nodes) return;
+  const int i = nodes[w];
   const double xi = x[3 * i], yi = x[3 * i + 1], zi = x[3 * i + 2];
+  const int c1 = aoff[i + 1];
   int n = 0;
-  for (int c = aoff[i]; c < aoff[i + 1]; ++c) {
-    const int j = cand_j[c];
-    const double dx = x[3 * j] - xi, dy = x[3 * j + 1] - yi, dz = x[3 * j + 2] - zi;
-    const double r2 = dx * dx + dy * dy + dz * dz;
-    n += (r2 < rc2 && r2 > 0.0) ? 1 : 0;
+  for (int c0 = aoff[i]; c0 < c1; c0 += 32) {
+    const int c = c0 + lane;
+    bool in = false;
+    if (c < c1) {
+      double dx, dy, dz;
+      const double r2 = pair_r2(x, xi, yi, zi, cand_j[c], dx, dy, dz);
+      in = r2 < rc2 && r2 > 0.0;
+    }
+    n += __popc(__ballot_sync(0xffffffffu, in));
   }
-  num_neigh[ii] = n;
+  if (lane == 0) num_neigh[w] = n;
 }
 
 // The edges: neighbour node node_map[owner ? owner[j] : j] (a node whose H1 row is read;
 // -1 is an error for the first n_local nodes and 0 for a halo node's edge, whose index
 // is never read, as the reference's map lookup gives), force target owner[j] when
 // scatter_owner, else j.
-__global__ void k_pair_fill(int n_nodes, int n_local, const int* __restrict__ nodes, const int* __restrict__ aoff,
-                            const int* __restrict__ cand_j, const double* __restrict__ x, double rc2,
-                            const int* __restrict__ first, const int* __restrict__ mtype,
-                            const int* __restrict__ owner, const int* __restrict__ node_map, int scatter_owner,
-                            int* __restrict__ node_type, int* __restrict__ nidx, int* __restrict__ ntype_e,
-                            double* __restrict__ xyz, double* __restrict__ r, int* __restrict__ nbr_atom,
-                            unsigned* __restrict__ bad) {
-  const int ii = blockIdx.x * blockDim.x + threadIdx.x;
-  if (ii >= n_nodes) return;
-  const int i = nodes[ii];
-  node_type[ii] = mtype[i];
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+    k_pair_fill(int n_nodes, int n_local, const int* __restrict__ nodes, const int* __restrict__ aoff,
+                const int* __restrict__ cand_j, const double* __restrict__ x, double rc2,
+                const int* __restrict__ first, const int* __restrict__ mtype, const int* __restrict__ owner,
+                const int* __restrict__ node_map, int scatter_owner, int* __restrict__ node_type,
+                int* __restrict__ nidx, int* __restrict__ ntype_e, double* __restrict__ xyz, double* __restrict__ r,
+                int* __restrict__ nbr_atom, unsigned* __restrict__ bad) {
+  const int w = node_warp(), lane = threadIdx.x & 31;
+  if (w >= n_nodes) return;
+  const int i = nodes[w];
+  if (lane == 0) node_type[w] = mtype[i];
   const double xi = x[3 * i], yi = x[3 * i + 1], zi = x[3 * i + 2];
-  int e = first[ii];
-  for (int c = aoff[i]; c < aoff[i + 1]; ++c) {
-    const int j = cand_j[c];
-    const double dx = x[3 * j] - xi, dy = x[3 * j + 1] - yi, dz = x[3 * j + 2] - zi;
-    const double r2 = dx * dx + dy * dy + dz * dz;
-    if (!(r2 < rc2 && r2 > 0.0)) continue;
-    const int jo = owner ? owner[j] : j;
-    const int node = node_map[jo];
-    if (node < 0 && ii < n_local) atomicOr(bad, 1u);
-    nidx[e] = node < 0 ? 0 : node;
-    ntype_e[e] = mtype[j];
-    xyz[3 * e] = dx;
-    xyz[3 * e + 1] = dy;
-    xyz[3 * e + 2] = dz;
-    r[e] = sqrt(r2);
-    nbr_atom[e] = scatter_owner ? jo : j;
-    ++e;
+  const int c1 = aoff[i + 1];
+  const int e_end = first[w + 1];
+  int e = first[w];
+  for (int c0 = aoff[i]; c0 < c1; c0 += 32) {
+    const int c = c0 + lane;
+    bool in = false;
+    int j = 0;
+    double dx = 0.0, dy = 0.0, dz = 0.0, r2 = 0.0;
+    if (c < c1) {
+      j = cand_j[c];
+      r2 = pair_r2(x, xi, yi, zi, j, dx, dy, dz);
+      in = r2 < rc2 && r2 > 0.0;
+    }
+    const unsigned ball = __ballot_sync(0xffffffffu, in);
+    const int slot = e + __popc(ball & ((1u << lane) - 1u));
+    if (in && slot < e_end) {  // (the count pass took the same decisions: slot < e_end)
+      const int jo = owner ? owner[j] : j;
+      const int node = node_map[jo];
+      if (node < 0 && w < n_local) atomicOr(bad, 1u);
+      nidx[slot] = node < 0 ? 0 : node;
+      ntype_e[slot] = mtype[j];
+      xyz[3 * slot] = dx;
+      xyz[3 * slot + 1] = dy;
+      xyz[3 * slot + 2] = dz;
+      r[slot] = sqrt(r2);
+      nbr_atom[slot] = scatter_owner ? jo : j;
+    }
+    e += __popc(ball);
   }
 }
 
 // no-MPI-message-passing mode: flag[j] = 1 for every non-local atom within r_cut of a
 // local one (pair_symmetrix_mace.cpp:557-580)
-__global__ void k_halo_mark(int inum, const int* __restrict__ nodes, const int* __restrict__ aoff,
-                            const int* __restrict__ cand_j, const double* __restrict__ x, double rc2,
-                            const int* __restrict__ node_of_local, int* __restrict__ flag) {
-  const int ii = blockIdx.x * blockDim.x + threadIdx.x;
-  if (ii >= inum) return;
-  const int i = nodes[ii];
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+    k_halo_mark(int inum, const int* __restrict__ nodes, const int* __restrict__ aoff,
+                const int* __restrict__ cand_j, const double* __restrict__ x, double rc2,
+                const int* __restrict__ node_of_local, int* __restrict__ flag) {
+  const int w = node_warp(), lane = threadIdx.x & 31;
+  if (w >= inum) return;
+  const int i = nodes[w];
   const double xi = x[3 * i], yi = x[3 * i + 1], zi = x[3 * i + 2];
-  for (int c = aoff[i]; c < aoff[i + 1]; ++c) {
+  const int c1 = aoff[i + 1];
+  for (int c = aoff[i] + lane; c < c1; c += 32) {
     const int j = cand_j[c];
-    const double dx = x[3 * j] - xi, dy = x[3 * j + 1] - yi, dz = x[3 * j + 2] - zi;
-    const double r2 = dx * dx + dy * dy + dz * dz;
+    double dx, dy, dz;
+    const double r2 = pair_r2(x, xi, yi, zi, j, dx, dy, dz);
     if (r2 < rc2 && r2 > 0.0 && node_of_local[j] < 0) flag[j] = 1;
   }
 }
@@ -127,13 +165,14 @@ __global__ void k_halo_nodes(int nall, int inum, const int* __restrict__ flag, c
   }
 }
 
-__global__ void k_pair_scatter(int n_nodes, const int* __restrict__ first, const int* __restrict__ nodes,
-                               const int* __restrict__ nbr_atom, const double* __restrict__ fe,
-                               double* __restrict__ f) {
-  const int ii = blockIdx.x * blockDim.x + threadIdx.x;
-  if (ii >= n_nodes) return;
+// F_i -= sum_e f_e over the node's edges (a warp sum), F_target(e) += f_e
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+    k_pair_scatter(int n_nodes, const int* __restrict__ first, const int* __restrict__ nodes,
+                   const int* __restrict__ nbr_atom, const double* __restrict__ fe, double* __restrict__ f) {
+  const int w = node_warp(), lane = threadIdx.x & 31;
+  if (w >= n_nodes) return;
   double sx = 0.0, sy = 0.0, sz = 0.0;
-  for (int e = first[ii]; e < first[ii + 1]; ++e) {
+  for (int e = first[w] + lane; e < first[w + 1]; e += 32) {
     const double fx = fe[3 * e], fy = fe[3 * e + 1], fz = fe[3 * e + 2];
     sx += fx;
     sy += fy;
@@ -143,10 +182,18 @@ __global__ void k_pair_scatter(int n_nodes, const int* __restrict__ first, const
     atomicAdd(f + 3 * j + 1, fy);
     atomicAdd(f + 3 * j + 2, fz);
   }
-  const int i = nodes[ii];
-  atomicAdd(f + 3 * i, -sx);
-  atomicAdd(f + 3 * i + 1, -sy);
-  atomicAdd(f + 3 * i + 2, -sz);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    sx += __shfl_xor_sync(0xffffffffu, sx, o);
+    sy += __shfl_xor_sync(0xffffffffu, sy, o);
+    sz += __shfl_xor_sync(0xffffffffu, sz, o);
+  }
+  if (lane == 0) {
+    const int i = nodes[w];
+    atomicAdd(f + 3 * i, -sx);
+    atomicAdd(f + 3 * i + 1, -sy);
+    atomicAdd(f + 3 * i + 2, -sz);
+  }
 }
 
 constexpr int kReduceBlocks = 64;
@@ -163,9 +210,11 @@ struct smx_pair {
   int *flag = nullptr, *gfirst = nullptr, *node_of_atom = nullptr;  // halo search (no-MPI-message-passing)
   double *x = nullptr, *f = nullptr, *partial = nullptr, *out = nullptr;
   unsigned* bad = nullptr;
+  // pinned host staging: positions in, forces / node energies / sums / flags out
+  double *hx = nullptr, *hf = nullptr, *he = nullptr, *hout = nullptr;
+  unsigned* hbad = nullptr;
   int* count_host = nullptr;  // pinned: the halo node count read back each call
   long cap_nall = 0, cap_cand = 0;
-  std::vector<double> h_out = std::vector<double>(10);
 
   void free_all() {
     void* ps[] = {nodes, aoff, cand_j, mtype, local_of, node_of_local, has_list, num_neigh, nbr_atom, flag,
@@ -176,7 +225,19 @@ struct smx_pair {
     flag = gfirst = node_of_atom = nullptr;
     x = f = partial = out = nullptr;
     bad = nullptr;
+    void* hs[] = {hx, hf, he, hout, hbad};
+    for (void* h : hs)
+      if (h) cudaFreeHost(h);
+    hx = hf = he = hout = nullptr;
+    hbad = nullptr;
     cap_nall = cap_cand = 0;
+  }
+
+  template <typename T>
+  static T* host_alloc(long n) {
+    void* h = nullptr;
+    smx::check(cudaMallocHost(&h, sizeof(T) * static_cast<size_t>(n)), "cudaMallocHost");
+    return static_cast<T*>(h);
   }
 
   // nodes never outnumber the atoms: buffers per node are sized by nall
@@ -202,6 +263,11 @@ struct smx_pair {
     partial = dalloc<double>(10 * kReduceBlocks);
     out = dalloc<double>(10);
     bad = dalloc<unsigned>(1);
+    hx = host_alloc<double>(3 * cap_nall);
+    hf = host_alloc<double>(3 * cap_nall);
+    he = host_alloc<double>(cap_nall);
+    hout = host_alloc<double>(10);
+    hbad = host_alloc<unsigned>(1);
   }
 };
 
@@ -299,15 +365,16 @@ int smx_pair_compute_mode(smx_pair* p, int mode, int inum, int gnum, int nall, c
     }
     if (inum == 0) return SMX_OK;
     const double rc = eng->hm.r_cut;
-    check(cudaMemcpyAsync(p->x, x, sizeof(double) * 3 * nall, cudaMemcpyHostToDevice, s), "H2D");
+    std::memcpy(p->hx, x, sizeof(double) * 3 * nall);
+    check(cudaMemcpyAsync(p->x, p->hx, sizeof(double) * 3 * nall, cudaMemcpyHostToDevice, s), "H2D");
     check(cudaMemsetAsync(p->f, 0, sizeof(double) * 3 * nall, s), "memset");
     check(cudaMemsetAsync(p->bad, 0, sizeof(unsigned), s), "memset");
     int n_nodes = inum;
     const int* node_map = p->node_of_local;
     if (halo) {  // the ghosts within r_cut of a local atom become halo nodes
       check(cudaMemsetAsync(p->flag, 0, sizeof(int) * nall, s), "memset");
-      k_halo_mark<<<smx::ceil_div(inum, 128), 128, 0, s>>>(inum, p->nodes, p->aoff, p->cand_j, p->x, rc * rc,
-                                                           p->node_of_local, p->flag);
+      k_halo_mark<<<smx::ceil_div(inum, kWarpsPerBlock), 32 * kWarpsPerBlock, 0, s>>>(
+          inum, p->nodes, p->aoff, p->cand_j, p->x, rc * rc, p->node_of_local, p->flag);
       smx::launch_scan_first(p->flag, nall, p->gfirst, s);
       check(cudaMemcpyAsync(p->count_host, p->gfirst + nall, sizeof(int), cudaMemcpyDeviceToHost, s), "D2H");
       check(cudaStreamSynchronize(s), "halo count");
@@ -317,28 +384,29 @@ int smx_pair_compute_mode(smx_pair* p, int mode, int inum, int gnum, int nall, c
       node_map = p->node_of_atom;
     }
     eng->reserve(n_nodes, p->ncand);  // edges are a subset of the listed candidates
-    const int nb = smx::ceil_div(n_nodes, 128);
-    k_pair_count<<<nb, 128, 0, s>>>(n_nodes, p->nodes, p->aoff, p->cand_j, p->x, rc * rc, p->num_neigh);
+    const int nb = smx::ceil_div(n_nodes, kWarpsPerBlock), bt = 32 * kWarpsPerBlock;
+    k_pair_count<<<nb, bt, 0, s>>>(n_nodes, p->nodes, p->aoff, p->cand_j, p->x, rc * rc, p->num_neigh);
     smx::launch_scan_first(p->num_neigh, n_nodes, eng->first, s);
     if (n_nodes > inum)  // the halo nodes' energy slots stay zero for the reduction below
       check(cudaMemsetAsync(eng->energies + inum, 0, sizeof(double) * (n_nodes - inum), s), "memset");
-    k_pair_fill<<<nb, 128, 0, s>>>(n_nodes, inum, p->nodes, p->aoff, p->cand_j, p->x, rc * rc, eng->first,
+    k_pair_fill<<<nb, bt, 0, s>>>(n_nodes, inum, p->nodes, p->aoff, p->cand_j, p->x, rc * rc, eng->first,
                                    p->mtype, halo ? nullptr : p->local_of, node_map,
                                    mode == SMX_PAIR_NO_DOMAIN_DECOMPOSITION ? 1 : 0, eng->ntype, eng->nidx,
                                    eng->ntype_e, eng->xyz, eng->r, p->nbr_atom, p->bad);
     smx::EdgeIn in{eng->first, eng->ntype, eng->nidx, eng->ntype_e, eng->xyz, eng->r, n_nodes};
     eng->run(in, eng->energies, eng->forces, s, inum);
-    k_pair_scatter<<<nb, 128, 0, s>>>(n_nodes, eng->first, p->nodes, p->nbr_atom, eng->forces, p->f);
+    k_pair_scatter<<<nb, bt, 0, s>>>(n_nodes, eng->first, p->nodes, p->nbr_atom, eng->forces, p->f);
     smx::launch_reduce(n_nodes, eng->first, eng->energies, eng->xyz, eng->forces, p->partial, kReduceBlocks, p->out,
                        s);
-    std::vector<double> hf(static_cast<size_t>(3) * nall);
-    unsigned hbad = 0;
-    check(cudaMemcpyAsync(hf.data(), p->f, sizeof(double) * 3 * nall, cudaMemcpyDeviceToHost, s), "D2H");
-    check(cudaMemcpyAsync(p->h_out.data(), p->out, sizeof(double) * 10, cudaMemcpyDeviceToHost, s), "D2H");
-    check(cudaMemcpyAsync(&hbad, p->bad, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "D2H");
-    if (eflag_atom && eatom)
-      check(cudaMemcpyAsync(eatom, eng->energies, sizeof(double) * inum, cudaMemcpyDeviceToHost, s), "D2H");
+    check(cudaMemcpyAsync(p->hf, p->f, sizeof(double) * 3 * nall, cudaMemcpyDeviceToHost, s), "D2H");
+    check(cudaMemcpyAsync(p->hout, p->out, sizeof(double) * 10, cudaMemcpyDeviceToHost, s), "D2H");
+    check(cudaMemcpyAsync(p->hbad, p->bad, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "D2H");
+    const bool want_eatom = eflag_atom && eatom;
+    if (want_eatom)
+      check(cudaMemcpyAsync(p->he, eng->energies, sizeof(double) * inum, cudaMemcpyDeviceToHost, s), "D2H");
     check(cudaStreamSynchronize(s), "pair compute");
+    const unsigned hbad = *p->hbad;
+    const double* hf = p->hf;
     if (eng->take_status() != SMX_OK) return fail(SMX_ERR_TIMEOUT, "a device-side wait timed out; results are invalid");
     if (hbad & 2u)
       return fail(SMX_ERR_INVALID,
@@ -346,7 +414,8 @@ int smx_pair_compute_mode(smx_pair* p, int mode, int inum, int gnum, int nall, c
                   "ghost neighbour list)");
     if (hbad & 1u) return fail(SMX_ERR_INVALID, "a neighbour's local owner is not in ilist");
     for (long q = 0; q < 3L * nall; ++q) f[q] += hf[q];
-    const double* o = p->h_out.data();
+    if (want_eatom) std::memcpy(eatom, p->he, sizeof(double) * inum);
+    const double* o = p->hout;
     if (eflag_global && eng_vdwl) *eng_vdwl += o[0];
     if (vflag_global && virial) {
       const double* W = o + 1;  // W_ab = sum_e xyz_a f_b, row-major

@@ -685,6 +685,8 @@ struct smx_engine {
     const int N1 = n1 < 0 ? N : n1;
     if (N1 > N || (N > 0 && N1 == 0)) throw std::invalid_argument("layer-1 node count outside (0, num_nodes]");
     const bool halo = N1 < N;
+    // (the species order permutes all nodes; with a halo the layer-1 kernels must see the
+    // first N1 nodes, so a halo pass keeps the input order)
     if (N > 0 && !halo && order_species()) {
       smx::launch_species_order(in.node_type, N, dm.S, atom_order, s);
       in.order = atom_order;

@@ -87,7 +87,7 @@ struct smx_engine {
   __nv_bfloat16 *M0_bf = nullptr, *Phi1_bf = nullptr, *A1adj_bf = nullptr, *H1adj_bf = nullptr;
   float* zbl_e = nullptr;  // per-node ZBL energy
   int *first = nullptr, *ntype = nullptr, *nidx = nullptr, *ntype_e = nullptr;
-  int* atom_order = nullptr;  // centre atoms sorted by species (when species_order is on)
+  int* atom_order = nullptr;  // centre atoms sorted by species (when species_order is on), [2][capN]
   int* nneigh = nullptr;      // num_neigh of the host-pointer call
   double *xyz = nullptr, *r = nullptr, *energies = nullptr, *forces = nullptr;
   // nodes of the last evaluation: all of them (layer 0) and the layer-1 ones (fewer when
@@ -344,7 +344,7 @@ struct smx_engine {
     r = dalloc<double>(nE);
     energies = dalloc<double>(nN);
     forces = dalloc<double>(3 * nE);
-    atom_order = dalloc<int>(nN);
+    atom_order = dalloc<int>(2 * nN);  // all nodes, then the layer-1 nodes of a halo pass
     nneigh = dalloc<int>(nN);
     if (precision == SMX_PRECISION_BF16) {
       const long T = smx::split_xterms(tc_terms);  // stored X terms
@@ -685,14 +685,16 @@ struct smx_engine {
     const int N1 = n1 < 0 ? N : n1;
     if (N1 > N || (N > 0 && N1 == 0)) throw std::invalid_argument("layer-1 node count outside (0, num_nodes]");
     const bool halo = N1 < N;
-    // (the species order permutes all nodes; with a halo the layer-1 kernels must see the
-    // first N1 nodes, so a halo pass keeps the input order)
-    if (N > 0 && !halo && order_species()) {
+    if (N > 0 && order_species()) {
       smx::launch_species_order(in.node_type, N, dm.S, atom_order, s);
       in.order = atom_order;
     }
     smx::EdgeIn in1 = in;  // layer 1: the first N1 nodes (a prefix of the edge list)
     in1.N = N1;
+    if (halo && in.order) {  // the layer-1 kernels visit the first N1 nodes, in their own order
+      smx::launch_species_order(in.node_type, N1, dm.S, atom_order + capN, s);
+      in1.order = atom_order + capN;
+    }
     if (halo) in.n_local = N1;
     const int C = dm.C;
     const int T = tc_terms, XT = smx::split_xterms(T);

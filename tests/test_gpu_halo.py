@@ -106,6 +106,25 @@ def test_lmax2_halo_and_schedules_match_oracle(engine_lib, tmp_path, precision):
         assert de < e_tol and df < f_tol
 
 
+def test_halo_with_species_order(engine_lib, small_model_path):
+    """Centre atoms sorted by species (as for spline tables larger than L2): layer 0 visits
+    all nodes in one species order, layer 1 the local nodes in an order of their own."""
+    from symmetrix_gb300 import MACE
+    pos, L, species = random_box(64, 0.064, 0.9, 3, seed=4)
+    nl = neighbor_list(pos, 5.0, L)
+    args = edge_args(species, nl)[1:]
+    m = MACE(small_model_path)
+    m.set_option("species_order", 1)
+    assert m.get_option("species_order") == 1
+    ref = Evaluator(small_model_path, "port")
+    for n1 in (7, 40, 64):
+        ref.compute_halo(n1, 64, *args)
+        m.compute_halo(n1, 64, *args)
+        de, df = _max(m.node_energies, ref.node_energies), _max(m.node_forces, ref.node_forces)
+        print(f"species order n1={n1}: dE_i={de:.2e} df_edge={df:.2e}")
+        assert de < TOL["float32"][0] and df < TOL["float32"][1]
+
+
 def test_halo_rejects_bad_counts(engine_lib, small_model_path):
     from symmetrix_gb300 import MACE
     pos, L, species = random_box(16, 0.064, 0.9, 3, seed=4)

@@ -45,6 +45,9 @@ def library(which="port"):
     f("compute").argtypes = [P, I, ip, ip, ip, ip, L, dp, dp]
     f("compute_halo").restype = I
     f("compute_halo").argtypes = [P, I, I, ip, ip, ip, ip, L, dp, dp]
+    if pre == "ref_":
+        f("compute_message_passing").restype = I
+        f("compute_message_passing").argtypes = [P, I, I, ip, ip, ip, ip, L, dp, dp, ip]
     f("get").restype = L
     f("get").argtypes = [P, ctypes.c_char_p, dp, L]
     f("last_error").restype = ctypes.c_char_p
@@ -129,6 +132,23 @@ class Evaluator:
         rc = getattr(self.lib, self.pre + "compute_halo")(self.h, int(num_local_nodes), int(num_nodes), _ip(keep[0]),
                                                           _ip(keep[1]), _ip(keep[2]), _ip(keep[3]), len(keep[5]),
                                                           _dp(keep[4]), _dp(keep[5]))
+        if rc != 0:
+            raise RuntimeError(getattr(self.lib, self.pre + "last_error")().decode())
+
+    def compute_message_passing(self, num_nodes, num_atoms, node_types, num_neigh, neigh_atoms, neigh_types, xyz, r,
+                                owner):
+        """(reference only) The stage calls of the pair style's MPI-message-passing mode on
+        one rank (pair_symmetrix_mace.cpp:438-497), the two communications done through
+        owner[atom]."""
+        if self.pre != "ref_":
+            raise ValueError("compute_message_passing() drives the reference build only")
+        keep = [np.ascontiguousarray(node_types, np.int32), np.ascontiguousarray(num_neigh, np.int32),
+                np.ascontiguousarray(neigh_atoms, np.int32), np.ascontiguousarray(neigh_types, np.int32),
+                np.ascontiguousarray(xyz, np.float64).reshape(-1), np.ascontiguousarray(r, np.float64),
+                np.ascontiguousarray(owner, np.int32)]
+        rc = getattr(self.lib, "ref_compute_message_passing")(
+            self.h, int(num_nodes), int(num_atoms), _ip(keep[0]), _ip(keep[1]), _ip(keep[2]), _ip(keep[3]),
+            len(keep[5]), _dp(keep[4]), _dp(keep[5]), _ip(keep[6]))
         if rc != 0:
             raise RuntimeError(getattr(self.lib, self.pre + "last_error")().decode())
 

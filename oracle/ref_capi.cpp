@@ -4,6 +4,7 @@
 // restatement (oracle/mace_oracle.cpp) and generates the golden fixtures under
 // tests/golden.  The function names and arguments match the oracle's C ABI with
 // the prefix ref_ instead of orc_, so tests can drive either one.
+#include <algorithm>
 #include <cstring>
 #include <exception>
 #include <span>
@@ -127,6 +128,63 @@ int ref_compute_halo(void* h, int num_local_nodes, int num_nodes, const int* nod
     m->reverse_M0(na, nt);
     m->reverse_A0_scaled(na, nt, nn, te, x, rr);
     m->reverse_A0(na, nt, nn, te, x, rr);
+    return 0;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return 1;
+  }
+}
+
+// The reference's stages in the order of the pair style's MPI-message-passing mode on one
+// rank (pair_symmetrix/pair_symmetrix_mace.cpp:438-497): num_nodes local nodes whose edges
+// index atoms (neigh_atoms < num_atoms, local atoms first); H1 rows of the ghost atoms are
+// filled from their owners (owner[a], the single-rank forward communication, :462-470) and
+// the ghosts' H1_adj rows are added to their owners' (the reverse communication, :487-489).
+int ref_compute_message_passing(void* h, int num_nodes, int num_atoms, const int* node_types, const int* num_neigh,
+                                const int* neigh_atoms, const int* neigh_types, long num_edges, const double* xyz,
+                                const double* r, const int* owner) {
+  try {
+    auto* m = static_cast<MACE*>(h);
+    const int n = num_nodes;
+    const std::span<const int> nt(node_types, n), nn(num_neigh, n), nj(neigh_atoms, num_edges),
+        te(neigh_types, num_edges);
+    const std::span<const double> x(xyz, 3 * num_edges), rr(r, num_edges);
+    const long row = static_cast<long>(m->num_LM) * m->num_channels;
+    m->node_energies.assign(n, 0.0);
+    m->node_forces.assign(3 * num_edges, 0.0);
+    if (m->has_zbl)
+      m->zbl.compute_ZBL(n, nt, nn, te, m->atomic_numbers, rr, x, m->node_energies, m->node_forces);
+    m->compute_Y(x);
+    m->compute_R0(n, nt, nn, te, rr);
+    m->compute_A0(n, nt, nn, te);
+    m->compute_A0_scaled(n, nt, nn, te, rr);
+    m->compute_M0(n, nt);
+    m->compute_H1(n);
+    std::vector<double> H1(static_cast<size_t>(num_atoms) * row, 0.0);
+    std::copy(m->H1.begin(), m->H1.begin() + n * row, H1.begin());
+    for (int a = n; a < num_atoms; ++a)
+      std::copy(H1.begin() + owner[a] * row, H1.begin() + (owner[a] + 1) * row, H1.begin() + a * row);
+    m->H1 = H1;
+    m->compute_R1(n, nt, nn, te, rr);
+    m->compute_Phi1(n, nn, nj);
+    m->compute_A1(n);
+    m->compute_A1_scaled(n, nt, nn, te, rr);
+    m->compute_M1(n, nt);
+    m->compute_H2(n, nt);
+    m->compute_readouts(n, nt);
+    m->reverse_H2(n, nt, false);
+    m->reverse_M1(n, nt);
+    m->reverse_A1_scaled(n, nt, nn, te, x, rr, false);
+    m->reverse_A1(n);
+    m->reverse_Phi1(n, nn, nj, x, rr, false, false);
+    std::vector<double> H1_adj = m->H1_adj;
+    for (int a = n; a < num_atoms; ++a)
+      for (long k = 0; k < row; ++k) H1_adj[owner[a] * row + k] += H1_adj[a * row + k];
+    m->H1_adj = H1_adj;
+    m->reverse_H1(n);
+    m->reverse_M0(n, nt);
+    m->reverse_A0_scaled(n, nt, nn, te, x, rr);
+    m->reverse_A0(n, nt, nn, te, x, rr);
     return 0;
   } catch (const std::exception& e) {
     g_err = e.what();

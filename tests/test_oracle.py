@@ -344,3 +344,35 @@ def test_halo_evaluation_equals_periodic_evaluation(tmp_path):
     np.testing.assert_allclose(F_halo, F_per, rtol=1e-10, atol=1e-11)
     np.testing.assert_allclose(virial(c["xyz"], halo.node_forces), virial(nl["xyz"], per.node_forces), rtol=1e-10,
                                atol=1e-10)
+
+
+@needs_ref
+def test_reference_message_passing_on_one_rank_is_the_owner_map(tmp_path):
+    """The identity the pair adapter's mpi_message_passing mode rests on, shown with the
+    reference's own stages: its stage sequence on one rank, with the ghosts' H1 rows filled
+    from their owners and their H1_adj rows added back (pair_symmetrix_mace.cpp:438-497),
+    gives the energies and per-edge forces of the plain evaluation whose neighbour indices
+    are the owners themselves."""
+    from make_golden import halo_model
+    from symmetrix_gb300.synth.structures import lammps_rank
+    path = halo_model(str(tmp_path / "halo.json"))
+    pos, L, species = random_box(24, 0.064, 0.9, 3, seed=7)
+    n, rc = len(pos), 5.0
+    x, owner, lists = lammps_rank(pos, L, rc + 0.5, rc + 0.5, ghost_lists=False)
+    sp = species[owner].astype(np.int32)
+    ei, ej = [], []
+    for i in range(n):
+        d = np.linalg.norm(x[lists[i]] - x[i], axis=1)
+        js = lists[i][d < rc]
+        ei.append(np.full(len(js), i))
+        ej.append(js)
+    ei, ej = np.concatenate(ei), np.concatenate(ej)
+    assert (ej >= n).any()  # some neighbours are ghosts
+    xyz = x[ej] - x[ei]
+    r = np.linalg.norm(xyz, axis=1)
+    nn = np.bincount(ei, minlength=n)
+    mp, plain = Evaluator(path, "reference"), Evaluator(path, "reference")
+    mp.compute_message_passing(n, len(x), sp[:n], nn, ej, sp[ej], xyz, r, owner)
+    plain.compute_node_energies_forces(n, sp[:n], nn, owner[ej], sp[ej], xyz, r)
+    np.testing.assert_allclose(mp.node_energies, plain.node_energies, rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(mp.node_forces, plain.node_forces, rtol=1e-10, atol=1e-12)

@@ -376,3 +376,25 @@ def test_reference_message_passing_on_one_rank_is_the_owner_map(tmp_path):
     plain.compute_node_energies_forces(n, sp[:n], nn, owner[ej], sp[ej], xyz, r)
     np.testing.assert_allclose(mp.node_energies, plain.node_energies, rtol=1e-12, atol=1e-12)
     np.testing.assert_allclose(mp.node_forces, plain.node_forces, rtol=1e-10, atol=1e-12)
+
+
+@pytest.mark.parametrize("threads,lean", [(3, False), (4, True)])
+def test_threaded_halo_evaluation_is_bitwise_serial(tmp_path, threads, lean):
+    """The halo evaluation split over node ranges (the H1_adj gather runs over every H1
+    row, the halo's included) gives the serial result bit for bit; with no halo it is the
+    plain evaluation bit for bit."""
+    g, c, path = _halo_golden(tmp_path)
+    n = int(g["n_local"])
+    serial = _halo_eval(path, "port", c, n)
+    par = Evaluator(path, "port").set_threads(threads).set_lean(lean)
+    par.compute_halo(n, len(c["node_atom"]), c["node_types"], c["num_neigh"], c["neigh_indices"],
+                     c["neigh_types"], c["xyz"], c["r"])
+    for name in ("node_energies", "node_forces", "H1", "A1", "H1_adj", "M0_adj", "A0_adj", "Phi1_adj"):
+        assert np.array_equal(serial.get(name).view(np.uint64), par.get(name).view(np.uint64)), name
+    N0 = len(c["node_atom"])
+    args = (c["node_types"], c["num_neigh"], c["neigh_indices"], c["neigh_types"], c["xyz"], c["r"])
+    full, plain = Evaluator(path, "port"), Evaluator(path, "port")
+    full.compute_halo(N0, N0, *args)
+    plain.compute_node_energies_forces(N0, *args)
+    for name in ("node_energies", "node_forces", "H1_adj", "A0_adj"):
+        assert np.array_equal(full.get(name).view(np.uint64), plain.get(name).view(np.uint64)), name

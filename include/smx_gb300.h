@@ -23,7 +23,7 @@
  *                                   it reports a timed-out device wait after the
  *                                   device-pointer call
  *   smx_num_elements, smx_num_channels, smx_r_cut, smx_l_max, smx_L_max, smx_num_LM,
- *   smx_atomic_numbers              public fields of class MACE (mace.hpp:18-25)
+ *   smx_atomic_numbers, smx_has_zbl public fields of class MACE (mace.hpp:18-25, :38)
  *   smx_get_stage, smx_set_stage    the stage buffers the Python binding exposes read/write
  *                                   (symmetrix/source/cpp/mace.cpp:14-34)
  *   smx_run_stage                   the binding's per-stage calls compute_H1 / reverse_H1,
@@ -94,6 +94,8 @@ double smx_r_cut(const smx_engine* eng);
 int smx_l_max(const smx_engine* eng);
 int smx_L_max(const smx_engine* eng);
 int smx_num_LM(const smx_engine* eng);
+/* 1 when the model adds the ZBL pair repulsion (MACE::has_zbl, mace.hpp:38), else 0. */
+int smx_has_zbl(const smx_engine* eng);
 /* Copies up to cap atomic numbers (none when out is NULL); returns the number of species. */
 int smx_atomic_numbers(const smx_engine* eng, int* out, int cap);
 

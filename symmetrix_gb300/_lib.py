@@ -29,6 +29,7 @@ SIGNATURES = [
     ("smx_l_max", _I, [_P]),
     ("smx_L_max", _I, [_P]),
     ("smx_num_LM", _I, [_P]),
+    ("smx_has_zbl", _I, [_P]),
     ("smx_atomic_numbers", _I, [_P, _P, _I]),
     ("smx_compute_node_energies_forces", _I, [_P, _I, _P, _P, _P, _P, _L, _P, _P, _P, _P]),
     ("smx_compute_halo", _I, [_P, _I, _I, _P, _P, _P, _P, _L, _P, _P, _P, _P]),

@@ -112,6 +112,7 @@ double smx_r_cut(const smx_engine* eng) { return eng ? eng->hm.r_cut : -1.0; }
 int smx_l_max(const smx_engine* eng) { return eng ? eng->hm.l_max : -1; }
 int smx_L_max(const smx_engine* eng) { return eng ? eng->hm.L_max : -1; }
 int smx_num_LM(const smx_engine* eng) { return eng ? eng->hm.nLM : -1; }
+int smx_has_zbl(const smx_engine* eng) { return eng ? (eng->hm.has_zbl ? 1 : 0) : -1; }
 int smx_atomic_numbers(const smx_engine* eng, int* out, int cap) {
   if (!eng) return -1;
   for (int q = 0; out && q < eng->hm.S && q < cap; ++q) out[q] = eng->hm.Z[q];

@@ -72,6 +72,11 @@ class MACE:
             self._lib.smx_destroy(h)
             self._h = None
 
+    @property
+    def has_zbl(self):
+        """Whether the model adds the ZBL pair repulsion (MACE::has_zbl)."""
+        return self._lib.smx_has_zbl(self._h) == 1
+
     def compute_node_energies_forces(self, num_nodes, node_types, num_neigh, neigh_indices, neigh_types, xyz, r):
         node_types = np.ascontiguousarray(node_types, dtype=np.int32)[:num_nodes]
         num_neigh = np.ascontiguousarray(num_neigh, dtype=np.int32)[:num_nodes]

@@ -34,6 +34,7 @@ def test_small_workload_matches_reference_golden(engine_lib, small_model_path, s
     species = g["species"].astype(np.int32)
     nl = {k: g[k] for k in ("num_neigh", "neigh_indices", "xyz", "r")}
     m = _engine(small_model_path)
+    assert not m.has_zbl
     m.compute_node_energies_forces(*edge_args(species, nl))
     assert _report("E_i", m.node_energies, g["node_energies"]) < E_TOL
     assert _report("f_edge", m.node_forces, g["node_forces"]) < F_TOL
@@ -148,6 +149,7 @@ def test_zbl_model_matches_oracle(engine_lib, tmp_path):
     nl = neighbor_list(pos, 5.0, L)
     assert (nl["r"] < 1.3).sum() > 0  # C/O pairs inside the ZBL range (r_max = 1.32-1.52 A)
     m = _engine(path)
+    assert m.has_zbl
     m.compute_node_energies_forces(*edge_args(species, nl))
     ref = Evaluator(path, "port")
     ref.compute_node_energies_forces(*edge_args(species, nl))
